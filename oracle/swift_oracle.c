@@ -1,0 +1,959 @@
+/*
+ * swift_oracle.c — CPU restatement of the reference aligner's hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY: the checker for the CUDA path and the timed CPU
+ * baseline ("port") of the benchmark.  The product never links or calls it.
+ *
+ * Pipeline restated (paths relative to the reference project root):
+ *   reference FASTA parse ............ refMapCreate      src/refMap.cu:59-117
+ *   k-mer code + hash ................ getHash           src/preprocess.cu:30-48,70-91
+ *   SSAHA index ...................... lookupTable5Create src/lookupTable5.cu:101-252
+ *   query stream ..................... qryGetNext2       src/query.cu:174-213
+ *   reverse complement ............... qryGetReverseComplement src/query.cu:265-282
+ *   hit emission ..................... lookupTable5MapQry src/lookupTable5.cu:557-603
+ *   best clusters .................... mapHits6GetBestHits src/mapHits6.cu:40-318
+ *   Phase-1 driver ................... searchQueries3    src/search.cu:275-382
+ *   Phase-2 driver ................... alignQueries3     src/align.cu:574-808
+ *   window fetch ..................... refMapGetOffsets  src/refMap.cu:148-155
+ *                                      getRefSeq2        src/input.cu:348-403
+ *   query fetch ...................... getSeq2           src/input.cu:216-258
+ *   batch sizing ..................... getNumQueriesPerIteration src/align.cu:2767-2793
+ *   Smith-Waterman (GPU semantics) ... smithWaterman     src/smithWaterman.cu:360-395,510-645,911-1026
+ *   best per read .................... chooseBestAlignment src/align.cu:844-905
+ *   record writer .................... printOutput       src/output.cu:154-201
+ *
+ * Tie rules that are random in the reference are pinned: mapHits6 keeps the
+ * first biggest clusters in sort order (src/mapHits6.cu:152-155) and
+ * chooseBestAlignment keeps the first maximum (src/align.cu:891).
+ */
+#include "swift_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define SO_LINE_MAX 100000  /* MAX_LINE_LENGTH, src/common.h:41       */
+#define SO_NAME_MAX 50      /* MAX_QRY_NAME_LENGTH, src/common.h:37    */
+#define SO_QSEQ_MAX 200     /* MAX_QRY_SEQ_LENGTH, src/common.h:40     */
+#define SO_WIN 300          /* REF_LENGTH, src/common.h:57             */
+#define SO_SHIFT_BASES 100  /* refSeqLength / 3, src/align.cu:668      */
+#define SO_MEM_MARGIN 100000000LL /* GLOBAL_MEM_MARGIN, src/common.h:43 */
+
+static void so_err(char *err, size_t n, const char *fmt, ...) {
+  if (!err || !n) return;
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(err, n, fmt, ap);
+  va_end(ap);
+}
+
+void so_free(void *p) { free(p); }
+
+/* ------------------------------------------------------------------ */
+/* codes and hash                                                      */
+
+static inline int so_code(unsigned char c) {
+  switch (c) {
+    case 'C': case 'c': return 1;
+    case 'G': case 'g': return 2;
+    case 'T': case 't': return 3;
+    default: return 0; /* A, a, N, n and every other byte */
+  }
+}
+
+int so_hash(const char *s, int k) {
+  int h = 0, p = 1;
+  for (int i = 0; i < k; ++i) {
+    h += p * so_code((unsigned char)s[i]);
+    p *= 4;
+  }
+  return h;
+}
+
+void so_revcomp(const char *seq, int len, char *out) {
+  for (int i = 0; i < len; ++i) {
+    char c = seq[len - 1 - i];
+    out[i] = c == 'A' ? 'T' : c == 'C' ? 'G' : c == 'G' ? 'C' : 'A';
+  }
+  out[len] = '\0';
+}
+
+/* fgets(line, MAX_LINE_LENGTH, f) starting at byte pos: chunk length. */
+static size_t so_chunk(const char *b, size_t n, size_t pos) {
+  if (pos >= n) return 0;
+  size_t lim = n - pos;
+  if (lim > SO_LINE_MAX - 1) lim = SO_LINE_MAX - 1;
+  const char *nl = (const char *)memchr(b + pos, '\n', lim);
+  return nl ? (size_t)(nl - (b + pos)) + 1 : lim;
+}
+
+static int so_check_bytes(const char *b, size_t n, const char *what, char *err,
+                          size_t errlen) {
+  for (size_t i = 0; i < n; ++i) {
+    unsigned char c = (unsigned char)b[i];
+    if (c == 0 || c >= 128) {
+      so_err(err, errlen, "%s: byte %u at offset %zu is not 7-bit text", what,
+             c, i);
+      return -1;
+    }
+    if (c == '>' && i > 0 && b[i - 1] != '\n') {
+      so_err(err, errlen, "%s: '>' inside a line at offset %zu", what, i);
+      return -1;
+    }
+  }
+  return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* reference FASTA                                                     */
+
+typedef struct {
+  size_t name_off, seq_off;
+  unsigned bpl;           /* _numBasesPerLine (refMap)                */
+  char name[SO_NAME_MAX];
+  size_t cat_start, cat_len;
+} so_rec;
+
+typedef struct {
+  const char *file;
+  size_t file_len;
+  so_rec *recs;
+  int n;
+  char *cat;               /* concatenated sequence lines of each record */
+  size_t cat_len;
+} so_ref;
+
+static void so_ref_free(so_ref *r) {
+  free(r->recs);
+  free(r->cat);
+  memset(r, 0, sizeof(*r));
+}
+
+static int so_ref_parse(const char *b, size_t n, so_ref *r, char *err,
+                        size_t errlen) {
+  memset(r, 0, sizeof(*r));
+  if (so_check_bytes(b, n, "reference", err, errlen)) return -1;
+  r->file = b;
+  r->file_len = n;
+  r->cat = (char *)malloc(n + 1);
+  int cap = 16;
+  r->recs = (so_rec *)calloc(cap, sizeof(so_rec));
+  if (!r->cat || !r->recs) return -2;
+  /* refMapCreate state (src/refMap.cu:61-116) */
+  long prev_ll = 0, old_ll = 0;
+  unsigned pos_count = 0;
+  int num_lines = 0;
+  size_t pos = 0, c;
+  while ((c = so_chunk(b, n, pos)) > 0) {
+    long ll = (long)c - (b[pos + c - 1] == '\n');
+    if (prev_ll > 0) old_ll = prev_ll;
+    prev_ll = ll;
+    if (ll == 0) { pos += c; continue; }
+    if (b[pos] == '>') {
+      if (r->n >= 1) {
+        so_rec *p = &r->recs[r->n - 1];
+        p->bpl = num_lines > 1
+                     ? (unsigned)(pos_count - (unsigned)old_ll) / (unsigned)(num_lines - 1)
+                     : 0;
+      }
+      if (r->n == 127) {
+        so_err(err, errlen, "reference: more than 127 sequences (the "
+               "reference keeps the sequence index in a char)");
+        return -1;
+      }
+      if (r->n == cap) {
+        cap *= 2;
+        r->recs = (so_rec *)realloc(r->recs, cap * sizeof(so_rec));
+      }
+      so_rec *q = &r->recs[r->n++];
+      memset(q, 0, sizeof(*q));
+      q->name_off = pos + c - (size_t)ll - 1;
+      q->seq_off = pos + c;
+      if (ll - 1 >= SO_NAME_MAX) {
+        so_err(err, errlen, "reference: name longer than %d characters",
+               SO_NAME_MAX - 1);
+        return -1;
+      }
+      memcpy(q->name, b + pos + 1, (size_t)(ll - 1));
+      q->name[ll - 1] = '\0';
+      q->cat_start = r->cat_len;
+      pos_count = 0;
+      num_lines = 0;
+    } else {
+      if (r->n == 0) {
+        so_err(err, errlen, "reference: sequence before the first header");
+        return -1;
+      }
+      ++num_lines;
+      pos_count += (unsigned)ll;
+      memcpy(r->cat + r->cat_len, b + pos, (size_t)ll);
+      r->cat_len += (size_t)ll;
+      r->recs[r->n - 1].cat_len += (size_t)ll;
+    }
+    pos += c;
+  }
+  if (prev_ll > 0) old_ll = prev_ll;
+  if (r->n >= 1) {
+    so_rec *p = &r->recs[r->n - 1];
+    p->bpl = num_lines > 1
+                 ? (unsigned)(pos_count - (unsigned)old_ll) / (unsigned)(num_lines - 1)
+                 : 0;
+  }
+  if (r->n == 0) {
+    so_err(err, errlen, "reference: no sequence header");
+    return -1;
+  }
+  return 0;
+}
+
+/* getRefSeq2 from file offset (src/input.cu:348-403) into out[SO_WIN+1]
+ * (NUL padded).  Returns the window length. */
+static int so_fetch_window(const char *b, size_t n, size_t off, char *out) {
+  char tmp[SO_WIN + 1];
+  int cnt = 0, got = 0;
+  size_t pos = off, c;
+  memset(out, 0, SO_WIN + 1);
+  while ((c = so_chunk(b, n, pos)) > 0) {
+    const char *line = b + pos;
+    pos += c;
+    if (line[0] == '>') break;
+    int ll = (int)c - (line[c - 1] == '\n');
+    cnt += ll;
+    if (cnt > SO_WIN) ll -= cnt - SO_WIN;
+    if (ll > 0) {
+      memcpy(tmp + got, line, (size_t)ll);
+      got += ll;
+    }
+    if (cnt >= SO_WIN) break;
+  }
+  tmp[got] = '\0';
+  /* N trimming, including the reference's indexing of the trailing loop
+   * through the shifted pointer (src/input.cu:394-402): with one leading N
+   * the trailing loop reads the terminator and trims nothing; with more it
+   * reads bytes past the string, which this restatement treats as not N. */
+  int lead = 0;
+  while (lead < got && (tmp[lead] == 'n' || tmp[lead] == 'N')) ++lead;
+  int len = got;
+  if (lead == 0) {
+    while (len > 0 && (tmp[len - 1] == 'n' || tmp[len - 1] == 'N')) --len;
+  }
+  int w = len - lead;
+  if (w < 0) w = 0;
+  memcpy(out, tmp + lead, (size_t)w);
+  return w;
+}
+
+/* ------------------------------------------------------------------ */
+/* SSAHA index                                                         */
+
+struct so_index {
+  int k, thres, nb, total;
+  int *lookup;      /* _lookupTable                 */
+  int *repeats;     /* _numRepeatsPerTuple          */
+  int *actual;      /* _numActualRepeatsPerTuple    */
+  int8_t *ref_idx;  /* total + 1                    */
+  int32_t *ref_pos; /* total + 1                    */
+  int nrefs;
+};
+
+static int so_index_from_ref(const so_ref *r, int k, int thres, so_index **out,
+                             char *err, size_t errlen) {
+  if (k < 1 || k > 15) {
+    so_err(err, errlen, "seed length %d outside 1..15", k);
+    return -1;
+  }
+  so_index *ix = (so_index *)calloc(1, sizeof(so_index));
+  ix->k = k;
+  ix->thres = thres;
+  ix->nb = 1 << (2 * k);
+  ix->nrefs = r->n;
+  ix->lookup = (int *)calloc((size_t)ix->nb, sizeof(int));
+  ix->repeats = (int *)calloc((size_t)ix->nb, sizeof(int));
+  ix->actual = (int *)calloc((size_t)ix->nb, sizeof(int));
+  int *nrep = (int *)calloc((size_t)ix->nb, sizeof(int));
+  size_t ntup = 0;
+  for (int i = 0; i < r->n; ++i) ntup += r->recs[i].cat_len / (size_t)k;
+  int32_t *th = (int32_t *)malloc((ntup + 1) * sizeof(int32_t));
+  int32_t *tr = (int32_t *)malloc((ntup + 1) * sizeof(int32_t));
+  int32_t *tp = (int32_t *)malloc((ntup + 1) * sizeof(int32_t));
+  size_t nt = 0;
+  long total = 0;
+  /* pass 1 (src/lookupTable5.cu:127-187) */
+  for (int ri = 0; ri < r->n; ++ri) {
+    const char *s = r->cat + r->recs[ri].cat_start;
+    size_t len = r->recs[ri].cat_len;
+    for (size_t p = 0; p + (size_t)k <= len; p += (size_t)k) {
+      int h = so_hash(s + p, k);
+      ++ix->repeats[h];
+      if (ix->repeats[h] <= thres) {
+        ++ix->actual[h];
+        ++nrep[h];
+        ++total;
+        th[nt] = h;
+        tr[nt] = ri;
+        tp[nt] = (int32_t)p;
+        ++nt;
+      } else if (ix->repeats[h] == ix->actual[h] + 1) {
+        ix->actual[h] = 0;
+        nrep[h] = 0;
+        total -= thres;
+      }
+    }
+  }
+  ix->total = (int)total;
+  ix->ref_idx = (int8_t *)calloc((size_t)total + 1, 1);
+  ix->ref_pos = (int32_t *)calloc((size_t)total + 1, sizeof(int32_t));
+  ix->ref_idx[0] = -1;
+  ix->ref_pos[0] = -1;
+  /* bucket starts (src/lookupTable5.cu:201-211) */
+  int start = 1;
+  for (int h = 0; h < ix->nb; ++h)
+    if (ix->repeats[h] > 0 && ix->repeats[h] <= thres) {
+      ix->lookup[h] = start;
+      start += ix->repeats[h];
+    }
+  /* pass 2 (src/lookupTable5.cu:219-231) */
+  for (size_t t = 0; t < nt; ++t) {
+    int h = th[t];
+    if (ix->repeats[h] <= thres) {
+      int idx = ix->lookup[h] + nrep[h] - 1;
+      ix->ref_idx[idx] = (int8_t)tr[t];
+      ix->ref_pos[idx] = tp[t];
+      --nrep[h];
+    }
+  }
+  free(th);
+  free(tr);
+  free(tp);
+  free(nrep);
+  *out = ix;
+  return 0;
+}
+
+int so_index_build(const char *fasta, size_t len, int k, int thres,
+                   so_index **out, char *err, size_t errlen) {
+  so_ref r;
+  int rc = so_ref_parse(fasta, len, &r, err, errlen);
+  if (rc == 0) rc = so_index_from_ref(&r, k, thres, out, err, errlen);
+  so_ref_free(&r);
+  return rc;
+}
+
+void so_index_free(so_index *ix) {
+  if (!ix) return;
+  free(ix->lookup);
+  free(ix->repeats);
+  free(ix->actual);
+  free(ix->ref_idx);
+  free(ix->ref_pos);
+  free(ix);
+}
+int so_index_num_buckets(const so_index *ix) { return ix->nb; }
+int so_index_total(const so_index *ix) { return ix->total; }
+int so_index_start(const so_index *ix, int h) { return ix->lookup[h]; }
+int so_index_repeats(const so_index *ix, int h) { return ix->repeats[h]; }
+int so_index_actual(const so_index *ix, int h) { return ix->actual[h]; }
+int so_index_num_refs(const so_index *ix) { return ix->nrefs; }
+void so_index_postings(const so_index *ix, int8_t *ri, int32_t *rp) {
+  memcpy(ri, ix->ref_idx, (size_t)ix->total + 1);
+  memcpy(rp, ix->ref_pos, ((size_t)ix->total + 1) * sizeof(int32_t));
+}
+
+/* ------------------------------------------------------------------ */
+/* hits and best clusters                                              */
+
+typedef struct { int8_t ri; int32_t sh, rp; } so_hit;
+
+static int so_hit_cmp(const void *a, const void *b) {
+  const so_hit *x = (const so_hit *)a, *y = (const so_hit *)b;
+  if (x->ri != y->ri) return x->ri < y->ri ? -1 : 1;
+  if (x->sh != y->sh) return x->sh < y->sh ? -1 : 1;
+  if (x->rp != y->rp) return x->rp < y->rp ? -1 : 1;
+  return 0;
+}
+
+static int so_best_of_sorted(int max_hits, const so_hit *h, int n,
+                             int8_t *o_ri, int32_t *o_sh, int32_t *o_rp) {
+  if (n == 0) return 0;
+  /* createClusters / findBiggestClusterSize (src/mapHits6.cu:202-272) */
+  int biggest = 0;
+  for (int i = 0; i < n;) {
+    int j = i + 1;
+    while (j < n && h[j].ri == h[i].ri && h[j].sh == h[i].sh) ++j;
+    if (j - i > biggest) biggest = j - i;
+    i = j;
+  }
+  /* findBiggestClusters (src/mapHits6.cu:132-167), first clusters kept */
+  int got = 0;
+  for (int i = 0; i < n && got < max_hits;) {
+    int j = i + 1;
+    while (j < n && h[j].ri == h[i].ri && h[j].sh == h[i].sh) ++j;
+    if (j - i == biggest) {
+      o_ri[got] = h[i].ri;
+      o_sh[got] = h[i].sh;
+      o_rp[got] = h[i].rp;
+      ++got;
+    }
+    i = j;
+  }
+  return got;
+}
+
+int so_best_hits(int max_hits, const int8_t *ri, const int32_t *sh,
+                 const int32_t *rp, int n, int8_t *o_ri, int32_t *o_sh,
+                 int32_t *o_rp) {
+  if (n <= 0) return 0;
+  so_hit *h = (so_hit *)malloc((size_t)n * sizeof(so_hit));
+  for (int i = 0; i < n; ++i) {
+    h[i].ri = ri[i];
+    h[i].sh = sh[i];
+    h[i].rp = rp[i];
+  }
+  qsort(h, (size_t)n, sizeof(so_hit), so_hit_cmp);
+  int got = so_best_of_sorted(max_hits, h, n, o_ri, o_sh, o_rp);
+  free(h);
+  return got;
+}
+
+int so_map_query(const so_index *ix, const char *seq, int len, int max_hits,
+                 int8_t *o_ri, int32_t *o_sh, int32_t *o_rp) {
+  int nq = len - ix->k + 1;
+  if (nq <= 0) return 0;
+  size_t n = 0;
+  for (int i = 0; i < nq; ++i) {
+    int h = so_hash(seq + i, ix->k);
+    n += (size_t)ix->actual[h];
+  }
+  if (n == 0) return 0;
+  so_hit *hits = (so_hit *)malloc(n * sizeof(so_hit));
+  size_t m = 0;
+  for (int i = 0; i < nq; ++i) {
+    int h = so_hash(seq + i, ix->k);
+    if (ix->actual[h] == 0) continue;
+    int s = ix->lookup[h], e = s + ix->actual[h] - 1;
+    for (int j = s; j <= e; ++j) {
+      hits[m].ri = ix->ref_idx[j];
+      hits[m].sh = ix->ref_pos[j] - i;
+      hits[m].rp = ix->ref_pos[j];
+      ++m;
+    }
+  }
+  qsort(hits, m, sizeof(so_hit), so_hit_cmp);
+  int got = so_best_of_sorted(max_hits, hits, (int)m, o_ri, o_sh, o_rp);
+  free(hits);
+  return got;
+}
+
+/* ------------------------------------------------------------------ */
+/* Smith-Waterman with the GPU kernel's semantics                      */
+
+static inline unsigned char so_up(unsigned char c) {
+  return (unsigned)(c - 'a') < 26u ? (unsigned char)(c - 'a' + 'A') : c;
+}
+
+void so_sw(const char *q, int Q, const char *r, int R, int m, int x, int o,
+           int e, so_aln *out, char *qcons, char *rcons, uint8_t *dirs) {
+  const int W = R + 1;
+  uint8_t *dir = dirs ? dirs : (uint8_t *)malloc((size_t)(Q + 1) * W);
+  memset(dir, 0, (size_t)(Q + 1) * W);
+  int *hp = (int *)calloc((size_t)W, sizeof(int));
+  int *hc = (int *)calloc((size_t)W, sizeof(int));
+  int best = 0, best_cell = 0;
+  for (int i = 1; i <= Q; ++i) {
+    unsigned char qc = so_up((unsigned char)q[i - 1]);
+    int row_best = 0, row_cell = 0;
+    hc[0] = 0;
+    for (int j = 1; j <= R; ++j) {
+      unsigned char rc = so_up((unsigned char)r[j - 1]);
+      int s = (qc == rc || qc == 'N' || rc == 'N') ? m : x;
+      int d = hp[j - 1] + s;
+      int t = hp[j] + (dir[(i - 1) * W + j] == SO_UP ? e : o);
+      int l = hc[j - 1] + (dir[i * W + j - 1] == SO_LEFT ? e : o);
+      int v = 0;
+      uint8_t dd = SO_NONE;
+      if (v < d) { v = d; dd = SO_DIAG; }
+      if (v < t) { v = t; dd = SO_UP; }
+      if (v < l) { v = l; dd = SO_LEFT; }
+      hc[j] = v;
+      dir[i * W + j] = dd;
+      if (row_best < v) { row_best = v; row_cell = i * W + j; }
+    }
+    if (best < row_best) { best = row_best; best_cell = row_cell; }
+    int *t = hp; hp = hc; hc = t;
+  }
+  free(hp);
+  free(hc);
+  /* backtrack (src/smithWaterman.cu:911-1026) */
+  int cur = best_cell, cr = cur / W, cc = cur % W, nxt;
+  uint8_t d0 = dir[cur];
+  if (d0 == SO_UP) nxt = cur - W;
+  else if (d0 == SO_LEFT) nxt = cur - 1;
+  else if (d0 == SO_DIAG) nxt = cur - W - 1;
+  else nxt = cur; /* the reference leaves nextCell unset here (score 0) */
+  int nr = nxt / W, nc = nxt % W;
+  int tick = -1, nref = -1, start = 0;
+  while ((cr != nr || cc != nc) && nc != 0 && nr != 0) {
+    ++tick;
+    if (nc == cc) rcons[tick] = '-';
+    else { rcons[tick] = r[cc - 1]; ++nref; }
+    qcons[tick] = (nr == cr) ? '-' : q[cr - 1];
+    start = cc;
+    cur = nxt; cr = nr; cc = nc;
+    uint8_t dd = dir[cur];
+    if (dd == SO_UP) nxt = cur - W;
+    else if (dd == SO_LEFT) nxt = cur - 1;
+    else if (dd == SO_DIAG) nxt = cur - W - 1;
+    else break;
+    nr = nxt / W; nc = nxt % W;
+  }
+  if ((cr != nr || cc != nc) && (nc == 0 || nr == 0)) {
+    ++tick;
+    if (nc == cc) rcons[tick] = '-';
+    else { rcons[tick] = r[cc - 1]; ++nref; }
+    qcons[tick] = (nr == cr) ? '-' : q[cr - 1];
+    start = cc;
+  }
+  out->score = (float)best;
+  out->cell_max = best_cell;
+  out->start = start;
+  out->end = start + nref;
+  out->len = tick + 1;
+  if (!dirs) free(dir);
+}
+
+/* ------------------------------------------------------------------ */
+/* reads (qryGetNext2 stream) and Phase 1                              */
+
+typedef struct {
+  size_t name_off, seq_off;
+  const char *seq;
+  int len;
+  char name[SO_NAME_MAX];
+} so_read;
+
+typedef struct {
+  so_read *r;
+  int n;
+  long n_gt;      /* getSeqCount: '>' bytes in the file (src/input.cu:505-524) */
+  int first_len;  /* getSeqSize (src/input.cu:475-496)                         */
+} so_reads;
+
+static int so_reads_parse(const char *b, size_t n, so_reads *rd, char *err,
+                          size_t errlen) {
+  memset(rd, 0, sizeof(*rd));
+  if (so_check_bytes(b, n, "reads", err, errlen)) return -1;
+  int cap = 1024;
+  rd->r = (so_read *)malloc((size_t)cap * sizeof(so_read));
+  size_t pos = 0, c;
+  int have_header = 0, nheaders = 0;
+  so_read cur;
+  memset(&cur, 0, sizeof(cur));
+  for (size_t i = 0; i < n; ++i) rd->n_gt += b[i] == '>';
+  while ((c = so_chunk(b, n, pos)) > 0) {
+    const char *line = b + pos;
+    int ll = (int)c - (line[c - 1] == '\n');
+    if (ll == 0) {
+      so_err(err, errlen, "reads: empty line at offset %zu (the reference "
+             "reader loops forever on it)", pos);
+      return -1;
+    }
+    if (line[0] == '>') {
+      if (have_header) {
+        so_err(err, errlen, "reads: header without a sequence line at "
+               "offset %zu", cur.name_off);
+        return -1;
+      }
+      if (ll - 1 > SO_NAME_MAX - 2) {
+        so_err(err, errlen, "reads: name longer than %d characters",
+               SO_NAME_MAX - 2);
+        return -1;
+      }
+      memcpy(cur.name, line + 1, (size_t)(ll - 1));
+      cur.name[ll - 1] = '\0';
+      cur.name_off = pos + c - (size_t)ll - 1;
+      cur.seq_off = pos + c;
+      have_header = 1;
+      ++nheaders;
+    } else {
+      if (!have_header) {
+        so_err(err, errlen, "reads: sequence line without a header at "
+               "offset %zu (multi-line reads are not supported)", pos);
+        return -1;
+      }
+      if (ll >= SO_QSEQ_MAX) {
+        so_err(err, errlen, "reads: read longer than %d bases", SO_QSEQ_MAX - 1);
+        return -1;
+      }
+      cur.seq = line;
+      cur.len = ll;
+      if (rd->n == 0) rd->first_len = (int)c - 1; /* strlen(line) - 1 */
+      if (rd->n == cap) {
+        cap *= 2;
+        rd->r = (so_read *)realloc(rd->r, (size_t)cap * sizeof(so_read));
+      }
+      rd->r[rd->n++] = cur;
+      have_header = 0;
+    }
+    pos += c;
+  }
+  if (have_header) {
+    so_err(err, errlen, "reads: trailing header without a sequence line");
+    return -1;
+  }
+  return 0;
+}
+
+/* Phase-1 slot schedule of searchQueries3 (src/search.cu:325-357): batches
+ * of 16 calls to qryGetNext2 while i < numQrs; a call past the end of the
+ * file leaves its slot holding the read it last held.  Fills order[] with
+ * read indices (-1: slot never filled) and returns the count. */
+#define SO_P1_THREADS 16 /* NUM_THREADS, src/common.h:97 */
+static long so_p1_schedule(const so_reads *rd, int **order) {
+  long nb = (rd->n_gt + SO_P1_THREADS - 1) / SO_P1_THREADS;
+  if (rd->n_gt <= 0) nb = 0;
+  long tot = nb * SO_P1_THREADS;
+  int *o = (int *)malloc((size_t)(tot > 0 ? tot : 1) * sizeof(int));
+  int slot[SO_P1_THREADS];
+  for (int j = 0; j < SO_P1_THREADS; ++j) slot[j] = -1;
+  long next = 0;
+  for (long bi = 0; bi < nb; ++bi)
+    for (int j = 0; j < SO_P1_THREADS; ++j) {
+      if (next < rd->n) slot[j] = (int)next++;
+      o[bi * SO_P1_THREADS + j] = slot[j];
+    }
+  *order = o;
+  return tot;
+}
+
+typedef struct {
+  const so_index *ix;
+  const so_reads *rd;
+  int max_hits;
+  int8_t *ri;   /* per read: 2*max_hits entries */
+  int32_t *sh, *rp;
+  int *cnt;     /* per read: [fwd, rev] */
+  long next;
+  pthread_mutex_t mu;
+} so_p1_job;
+
+static void *so_p1_worker(void *arg) {
+  so_p1_job *jb = (so_p1_job *)arg;
+  char rev[SO_QSEQ_MAX + 1];
+  for (;;) {
+    pthread_mutex_lock(&jb->mu);
+    long i = jb->next;
+    jb->next += 64;
+    pthread_mutex_unlock(&jb->mu);
+    if (i >= jb->rd->n) break;
+    long e = i + 64 < jb->rd->n ? i + 64 : jb->rd->n;
+    for (; i < e; ++i) {
+      const so_read *r = &jb->rd->r[i];
+      int mh = jb->max_hits;
+      size_t b0 = (size_t)i * 2 * (size_t)mh;
+      jb->cnt[2 * i] = so_map_query(jb->ix, r->seq, r->len, mh, jb->ri + b0,
+                                    jb->sh + b0, jb->rp + b0);
+      so_revcomp(r->seq, r->len, rev);
+      jb->cnt[2 * i + 1] =
+          so_map_query(jb->ix, rev, r->len, mh, jb->ri + b0 + mh,
+                       jb->sh + b0 + mh, jb->rp + b0 + mh);
+    }
+  }
+  return NULL;
+}
+
+static int so_run_phase1(const so_index *ix, const so_reads *rd, int max_hits,
+                         int threads, so_match **out, int *n_out) {
+  so_p1_job jb;
+  memset(&jb, 0, sizeof(jb));
+  jb.ix = ix;
+  jb.rd = rd;
+  jb.max_hits = max_hits;
+  size_t per = (size_t)2 * (size_t)max_hits;
+  size_t nr = (size_t)(rd->n > 0 ? rd->n : 1);
+  jb.ri = (int8_t *)malloc(nr * per);
+  jb.sh = (int32_t *)malloc(nr * per * sizeof(int32_t));
+  jb.rp = (int32_t *)malloc(nr * per * sizeof(int32_t));
+  jb.cnt = (int *)calloc(nr * 2, sizeof(int));
+  pthread_mutex_init(&jb.mu, NULL);
+  if (threads < 1) threads = 1;
+  pthread_t *th = (pthread_t *)malloc((size_t)threads * sizeof(pthread_t));
+  for (int t = 0; t < threads; ++t) pthread_create(&th[t], NULL, so_p1_worker, &jb);
+  for (int t = 0; t < threads; ++t) pthread_join(th[t], NULL);
+  free(th);
+  pthread_mutex_destroy(&jb.mu);
+  int *order;
+  long tot = so_p1_schedule(rd, &order);
+  long nm = 0;
+  for (long s = 0; s < tot; ++s)
+    if (order[s] >= 0) nm += jb.cnt[2 * order[s]] + jb.cnt[2 * order[s] + 1];
+  so_match *m = (so_match *)malloc((size_t)(nm > 0 ? nm : 1) * sizeof(so_match));
+  long k = 0;
+  for (long s = 0; s < tot; ++s) {
+    int ridx = order[s];
+    if (ridx < 0) continue;
+    for (int strand = 0; strand < 2; ++strand) {
+      size_t b0 = (size_t)ridx * per + (size_t)strand * (size_t)max_hits;
+      for (int h = 0; h < jb.cnt[2 * ridx + strand]; ++h) {
+        m[k].slot_read = ridx;
+        m[k].strand = strand;
+        m[k].ref_idx = jb.ri[b0 + h];
+        m[k].shift = jb.sh[b0 + h];
+        m[k].ref_pos = jb.rp[b0 + h];
+        ++k;
+      }
+    }
+  }
+  free(order);
+  free(jb.ri);
+  free(jb.sh);
+  free(jb.rp);
+  free(jb.cnt);
+  *out = m;
+  *n_out = (int)nm;
+  return 0;
+}
+
+int so_phase1(const char *ref, size_t ref_len, const char *reads,
+              size_t reads_len, const so_params *p, so_match **out, int *n_out,
+              char *err, size_t errlen) {
+  so_ref r;
+  so_reads rd;
+  so_index *ix = NULL;
+  int rc = so_ref_parse(ref, ref_len, &r, err, errlen);
+  if (rc == 0) rc = so_index_from_ref(&r, p->seed_len, p->ignore_thres, &ix, err, errlen);
+  if (rc == 0) rc = so_reads_parse(reads, reads_len, &rd, err, errlen);
+  if (rc == 0) {
+    rc = so_run_phase1(ix, &rd, p->max_hits, p->threads, out, n_out);
+    free(rd.r);
+  }
+  so_index_free(ix);
+  so_ref_free(&r);
+  return rc;
+}
+
+/* ------------------------------------------------------------------ */
+/* Phase 2                                                             */
+
+/* getNumQueriesPerIteration (src/align.cu:2767-2793) with the per-pair
+ * memory of getMemPerRefQryPair (src/align.cu:2739-2756). */
+static long so_p2_batch(long long device_mem, int Q, long nm) {
+  long per_iter;
+  if (device_mem > 0) {
+    int mem_pair = (SO_WIN + 1) + (Q + 1) + 4 + 4 + 4 + 2 + 2 * (SO_WIN + Q + 2);
+    long gm = (long)(device_mem - SO_MEM_MARGIN);
+    per_iter = (int)floor((float)gm / mem_pair);
+    if (per_iter > 2147483647L) per_iter = 2147483647L;
+  } else {
+    per_iter = nm;
+  }
+  if (per_iter > nm) per_iter = nm;
+  if (per_iter >= 2 && per_iter % 2 == 1) --per_iter;
+  return per_iter;
+}
+
+/* qryNameCmp (src/align.cu:1501-1519) */
+static int so_name_cmp(const char *s, const char *t, int size) {
+  int i;
+  for (i = 0; i < size; ++i) {
+    if (s[i] == '\0' && t[i] == '\0') return 0;
+    else if (s[i] == '\0' || t[i] == '\0') break;
+    else if (s[i] != t[i]) return -1;
+  }
+  if ((s[i] == '*' && s[i + 1] == '\0') || (t[i] == '*' && t[i + 1] == '\0'))
+    return 0;
+  return -1;
+}
+
+typedef struct {
+  char qname[SO_NAME_MAX + 1];
+  const char *rname;
+  int ref_dist;
+  char q[SO_QSEQ_MAX + 2];
+  char w[SO_WIN + 1];
+  so_aln a;
+  char *qc, *rc;
+} so_pair;
+
+typedef struct {
+  so_pair *pp;
+  long n;
+  int Q;
+  const so_params *p;
+  long next;
+  pthread_mutex_t mu;
+} so_p2_job;
+
+static void *so_p2_worker(void *arg) {
+  so_p2_job *jb = (so_p2_job *)arg;
+  for (;;) {
+    pthread_mutex_lock(&jb->mu);
+    long i = jb->next;
+    jb->next += 16;
+    pthread_mutex_unlock(&jb->mu);
+    if (i >= jb->n) break;
+    long e = i + 16 < jb->n ? i + 16 : jb->n;
+    for (; i < e; ++i) {
+      so_pair *x = &jb->pp[i];
+      so_sw(x->q, jb->Q, x->w, SO_WIN, jb->p->match, jb->p->mismatch,
+            jb->p->gap_open, jb->p->gap_ext, &x->a, x->qc, x->rc, NULL);
+    }
+  }
+  return NULL;
+}
+
+typedef struct { char *b; size_t n, cap; } so_sb;
+static void so_sb_put(so_sb *s, const char *p, size_t n) {
+  if (s->n + n + 1 > s->cap) {
+    while (s->n + n + 1 > s->cap) s->cap = s->cap ? s->cap * 2 : 1 << 16;
+    s->b = (char *)realloc(s->b, s->cap);
+  }
+  memcpy(s->b + s->n, p, n);
+  s->n += n;
+}
+
+static void so_print_record(so_sb *sb, const so_pair *x) {
+  char hdr[512];
+  int len = x->a.len;
+  so_sb_put(sb, "\n****************************************\n", 42);
+  int hn = snprintf(hdr, sizeof(hdr),
+                    "Qry: %s | Ref: %s | Score: %.1f | AlignStart: %d | "
+                    "AlignEnd: %d | AlignLength: %d\n",
+                    x->qname, x->rname, x->a.score, x->a.start + x->ref_dist,
+                    x->a.end + x->ref_dist, len);
+  so_sb_put(sb, hdr, (size_t)hn);
+  so_sb_put(sb, "R: ", 3);
+  for (int z = len - 1; z >= 0; --z) so_sb_put(sb, &x->rc[z], 1);
+  so_sb_put(sb, "\n   ", 4);
+  for (int z = len - 1; z >= 0; --z) {
+    char rc = x->rc[z], qc = x->qc[z];
+    int ur = (unsigned)(rc - 'a') < 26u ? rc - 32 : rc;
+    int uq = (unsigned)(qc - 'a') < 26u ? qc - 32 : qc;
+    char ch = (ur == uq || rc == 'N' || qc == 'N') ? '|'
+              : (rc == '-' || qc == '-')          ? '-'
+                                                  : '.';
+    so_sb_put(sb, &ch, 1);
+  }
+  so_sb_put(sb, "\nQ: ", 4);
+  for (int z = len - 1; z >= 0; --z) so_sb_put(sb, &x->qc[z], 1);
+  so_sb_put(sb, "\n", 1);
+}
+
+int so_align(const char *ref, size_t ref_len, const char *reads,
+             size_t reads_len, const so_params *p, char **out, size_t *out_len,
+             char *err, size_t errlen) {
+  so_ref r;
+  so_reads rd;
+  so_index *ix = NULL;
+  so_match *m = NULL;
+  int nm = 0;
+  memset(&rd, 0, sizeof(rd));
+  int rc = so_ref_parse(ref, ref_len, &r, err, errlen);
+  if (rc == 0) rc = so_index_from_ref(&r, p->seed_len, p->ignore_thres, &ix, err, errlen);
+  if (rc == 0) rc = so_reads_parse(reads, reads_len, &rd, err, errlen);
+  if (rc == 0) rc = so_run_phase1(ix, &rd, p->max_hits, p->threads, &m, &nm);
+  so_index_free(ix);
+  if (rc != 0) {
+    free(rd.r);
+    so_ref_free(&r);
+    return rc;
+  }
+  int Q = p->qry_len > 0 ? p->qry_len : rd.first_len;
+  if (Q < 1 || Q > SO_QSEQ_MAX) {
+    so_err(err, errlen, "query length %d outside 1..%d", Q, SO_QSEQ_MAX);
+    free(rd.r); free(m); so_ref_free(&r);
+    return -1;
+  }
+  long per_iter = so_p2_batch(p->device_mem, Q, nm);
+  int n_iter = per_iter > 0 ? (int)ceil((float)nm / per_iter) : 0;
+  so_sb sb = {0};
+  /* query buffers that persist like the reference's: the per-slot host
+   * buffer querySeq and the stack buffer tmpQrySeq (src/align.cu:660-728) */
+  char *slotq = (char *)calloc((size_t)(per_iter > 0 ? per_iter : 1), (size_t)Q + 1);
+  char *tmpq = (char *)calloc((size_t)Q + 2, 1);
+  long done = 0;
+  for (int it = 0; it < n_iter; ++it) {
+    long cnt = per_iter;
+    if (it == n_iter - 1) {
+      long maxs = (long)n_iter * per_iter;
+      cnt = nm < maxs ? nm - (long)(n_iter - 1) * per_iter : per_iter;
+    }
+    so_pair *pp = (so_pair *)calloc((size_t)cnt, sizeof(so_pair));
+    char *cons = (char *)malloc((size_t)cnt * 2 * (size_t)(SO_WIN + Q + 2));
+    for (long j = 0; j < cnt; ++j) {
+      const so_match *mm = &m[done + j];
+      const so_read *rr = &rd.r[mm->slot_read];
+      so_pair *x = &pp[j];
+      x->qc = cons + (size_t)j * 2 * (size_t)(SO_WIN + Q + 2);
+      x->rc = x->qc + (SO_WIN + Q + 2);
+      int dist = mm->ref_pos - SO_SHIFT_BASES;
+      if (dist < 0) dist = 0;
+      x->ref_dist = dist;
+      const so_rec *rec = &r.recs[mm->ref_idx];
+      unsigned off = (unsigned)rec->seq_off + (unsigned)dist +
+                     (rec->bpl > 0 ? (unsigned)dist / rec->bpl : 0u);
+      so_fetch_window(r.file, r.file_len, off, x->w);
+      x->rname = rec->name;
+      /* getSeq2 from the read's sequence offset (src/input.cu:216-258) */
+      int avail = rr->len < Q ? rr->len : Q;
+      char *dst = (mm->strand == 1) ? tmpq : slotq + (size_t)j * (Q + 1);
+      memcpy(dst, rr->seq, (size_t)avail);
+      dst[avail] = '\0';
+      strcpy(x->qname, rr->name);
+      if (mm->strand == 1) {
+        char *sq = slotq + (size_t)j * (Q + 1);
+        so_revcomp(tmpq, Q, sq);
+        strcat(x->qname, "*");
+      }
+      memcpy(x->q, slotq + (size_t)j * (Q + 1), (size_t)Q);
+    }
+    so_p2_job jb;
+    memset(&jb, 0, sizeof(jb));
+    jb.pp = pp;
+    jb.n = cnt;
+    jb.Q = Q;
+    jb.p = p;
+    pthread_mutex_init(&jb.mu, NULL);
+    int threads = p->threads < 1 ? 1 : p->threads;
+    pthread_t *th = (pthread_t *)malloc((size_t)threads * sizeof(pthread_t));
+    for (int t = 0; t < threads; ++t) pthread_create(&th[t], NULL, so_p2_worker, &jb);
+    for (int t = 0; t < threads; ++t) pthread_join(th[t], NULL);
+    free(th);
+    pthread_mutex_destroy(&jb.mu);
+    /* chooseBestAlignment over this batch (src/align.cu:844-905) */
+    long start = 0;
+    while (start < cnt) {
+      long end = start;
+      while (end + 1 < cnt &&
+             so_name_cmp(pp[end + 1].qname, pp[end].qname, SO_NAME_MAX) == 0)
+        ++end;
+      float mx = 0.0f;
+      for (long i = start; i <= end; ++i)
+        if (mx < pp[i].a.score) mx = pp[i].a.score;
+      long keep = -1;
+      for (long i = start; i <= end; ++i)
+        if (pp[i].a.score == mx) { keep = i; break; }
+      for (long i = start; i <= end; ++i)
+        if (i != keep) pp[i].a.score = -1.0f;
+      start = end + 1;
+    }
+    for (long j = 0; j < cnt; ++j)
+      if (!(pp[j].a.score < 0.0f)) so_print_record(&sb, &pp[j]);
+    free(pp);
+    free(cons);
+    done += cnt;
+  }
+  free(slotq);
+  free(tmpq);
+  free(m);
+  free(rd.r);
+  so_ref_free(&r);
+  so_sb_put(&sb, "", 0);
+  if (!sb.b) { sb.b = (char *)malloc(1); }
+  sb.b[sb.n] = '\0';
+  *out = sb.b;
+  *out_len = sb.n;
+  return 0;
+}
