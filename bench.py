@@ -1,0 +1,277 @@
+"""Benchmark: reads/s of the SWIFT hot path on GB300.
+
+One step = one pass of the whole pipeline over one batch of reads already
+resident on the device: SSAHA seeding of both strands, window construction,
+Smith-Waterman with traceback for every candidate, best alignment per read and
+the default text records (left on the device).  The one-time index build is
+excluded and reported separately.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload scale|small] [--reads N]
+
+Workload "scale" (default): 50 Mbp reference in 24 sequences (log-normal
+lengths, 10 % diverged repeat copies), 1,000,000 reads x 100 bp (1 % subs,
+0.1 % indels, 5 % random reads); seeded synthetic data.  With N GPUs each rank
+aligns its own 1M reads (weak scaling; no collective on the data path).
+
+--impl reference times the reference algorithm's CPU implementation (the
+oracle port, multithreaded over all host cores) on a bounded sample per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "reads/s (SSAHA seeding + Smith-Waterman + best per read + records), bit-exact"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="scale", choices=["scale", "small"])
+    ap.add_argument("--reads", type=int, default=None)
+    ap.add_argument("--cpu-sample", type=int, default=20000)
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during a region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.file = None
+
+    def __enter__(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.file, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.file:
+            return None
+        self.file.flush()
+        rows = []
+        with open(self.file.name) as f:
+            for line in f:
+                p = [x.strip() for x in line.split(",")]
+                if len(p) >= 9:
+                    rows.append(p)
+        os.unlink(self.file.name)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def make_workload(args, rank):
+    from swift_gb300 import synth
+    if args.workload == "small":
+        names, seqs = synth.make_reference(1_000_000, 1, seed=0)
+        n = args.reads or 10_000
+        rn, rs, _ = synth.make_reads(seqs, n, 100, 0.01, 0.001, 0.0, seed=1 + rank)
+        desc = "small: 1 Mbp / 1 seq, %d x 100 bp reads" % n
+    else:
+        names, seqs = synth.make_reference(50_000_000, 24, sigma=0.8, repeat_frac=0.10,
+                                           n_units=500, unit_len=300, divergence=0.03, seed=0)
+        n = args.reads or 1_000_000
+        rn, rs, _ = synth.make_reads(seqs, n, 100, 0.01, 0.001, 0.05, seed=1 + rank)
+        desc = ("scale: 50 Mbp / 24 seqs (log-normal sigma 0.8, 10%% repeats of 500 x 300 bp "
+                "units at 3%% divergence), %d x 100 bp reads (1%% subs, 0.1%% indels, 5%% random)"
+                % n)
+    return synth.fasta_bytes(names, seqs), synth.reads_fasta(rn, rs), n, desc
+
+
+def sample_reads(reads: bytes, n: int) -> bytes:
+    lines = reads.split(b"\n", 2 * n)
+    return b"\n".join(lines[: 2 * n]) + b"\n"
+
+
+def cpu_reference(ref: bytes, reads: bytes, n_sample: int, steps: int, warmup: int):
+    """The reference algorithm on the host cores (oracle port), reads/s."""
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    sess = O.Session(ref, O.default_params(threads=threads))
+    sample = sample_reads(reads, n_sample)
+    for _ in range(warmup):
+        sess.align(sample)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        sess.align(sample)
+    dt = time.perf_counter() - t0
+    return n_sample * steps / dt, threads, dt
+
+
+def main():
+    args = parse_args()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        ref, reads, n, desc = make_workload(args, 0)
+        steps, warm = max(args.steps, 1), max(args.warmup, 0)
+        n_sample = min(args.cpu_sample, n)
+        rps, threads, dt = cpu_reference(ref, reads, n_sample, steps, min(warm, 1))
+        line = {
+            "impl": "reference", "metric": METRIC, "value": rps, "unit": "reads/s",
+            "n_gpus": args.gpus, "steps": steps, "warmup": warm,
+            "ms_per_step": dt * 1e3 / steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+            "config": {"workload": desc, "sample_reads_per_step": n_sample},
+            "cpu_baseline": {"value": rps, "unit": "reads/s", "cores": threads, "kind": "port",
+                             "sample": f"{n_sample} reads of the workload per step"},
+            "e2e": {"value": rps, "unit": "reads/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+        }
+        print(json.dumps(line))
+        return 0
+
+    import torch
+    import swift_gb300 as sg
+    from swift_gb300 import build as b
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    device = local
+    torch.cuda.set_device(device)
+    b.build()
+    ref, reads, n, desc = make_workload(args, rank)
+    # a dedicated (non-default) stream shared by the library and the events
+    stream = torch.cuda.Stream(device)
+    torch.cuda.set_stream(stream)
+    ctx = sg.Context(device, stream.cuda_stream)
+    t0 = time.perf_counter()
+    idx = ctx.index(ref)
+    torch.cuda.synchronize()
+    index_s = time.perf_counter() - t0
+    rd = ctx.reads(reads)
+    peak_cells = ctx.peak_dpx_cells_per_s()
+    stats = []
+    for _ in range(max(args.warmup, 3)):
+        out_n, st = ctx.align_resident(idx, rd)
+    # timed region: K steps bracketed by barrier + synchronize
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(device) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            out_n, st = ctx.align_resident(idx, rd)
+            stats.append(st)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    value = n * world * args.steps / (ms * 1e-3)
+    sw_ms = statistics.median(s["sw_ms"] for s in stats)
+    seed_ms = statistics.median(s["seed_ms"] for s in stats)
+    cells = stats[-1]["cells"]
+    gcups = cells / (sw_ms * 1e-3) / 1e9
+    # end to end through the C ABI: host reads (pinned) in, host text out
+    e2e = None
+    if not args.no_e2e:
+        pinned = torch.empty(len(reads), dtype=torch.uint8, pin_memory=True)
+        pinned.numpy()[:] = memoryview(reads)
+        for _ in range(2):
+            ctx.align(idx, pinned.data_ptr(), nbytes=len(reads))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out_bytes = 0
+        for _ in range(args.steps):
+            data = ctx.align(idx, pinned.data_ptr(), nbytes=len(reads))
+            out_bytes = len(data)
+        torch.cuda.synchronize()
+        e2e_s = time.perf_counter() - t0
+        e2e = {"value": n * world * args.steps / e2e_s, "unit": "reads/s",
+               "h2d_bytes_per_step": len(reads), "d2h_bytes_per_step": out_bytes}
+    if rank != 0:
+        return 0
+    cpu = None
+    try:
+        rps, threads, dt = cpu_reference(ref, reads, min(args.cpu_sample, n), 1, 0)
+        cpu = {"value": rps, "unit": "reads/s", "cores": threads, "kind": "port",
+               "sample": f"{min(args.cpu_sample, n)} reads of the workload, index prebuilt"}
+    except Exception as ex:  # the baseline must not break the GPU line
+        cpu = {"value": None, "unit": "reads/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"failed: {ex}"}
+    achieved = gcups
+    peak = peak_cells / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": "reads/s", "n_gpus": world,
+        "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "int32", "data": "synthetic",
+        "config": {"workload": desc, "l2": "inputs larger than L2 (reads %.0f MB, index %.0f MB)"
+                   % (len(reads) / 1e6, (2 * 4 ** 12 * 4 + 8 * idx.info()["total"]) / 1e6),
+                   "records_per_step": stats[-1]["records"], "index_build_s": index_s},
+        "sw_gcups": gcups,
+        "phase_ms": {k: statistics.median(s[k] for s in stats)
+                     for k in ("seed_ms", "pairs_ms", "sw_ms", "select_ms", "format_ms",
+                               "total_ms")},
+        "roofline": {"bound": "dpx", "kernel": "sw", "achieved": achieved, "peak": peak,
+                     "unit": "Gcells/s", "frac": achieved / peak if peak else None,
+                     "traffic": None,
+                     "peak_source": "measured on this GPU: 2 cells per __vimax3_s16x2_relu "
+                                    "lane instruction"},
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": int(sum(s["launches"] for s in stats)),
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,157 @@
+/*
+ * swift_gb300.h — C ABI of the GB300 (sm_103a) implementation of the SWIFT
+ * two-phase short-read aligner hot path: SSAHA seeding (Phase 1) and
+ * Smith-Waterman with traceback (Phase 2), then best-per-read selection and
+ * the default text record.
+ *
+ * All functions return 0 on success and a negative SWIFT_E_* code on
+ * failure; they never exit the process.  swift_last_error() gives a message
+ * for the last failure on a context.  A context is used by one host thread
+ * at a time.
+ *
+ * Reference interfaces replaced (paths relative to the reference project):
+ *   swift_index_build  <- lookupTable5Create           src/lookupTable5.h:28
+ *                         + refMapCreate               src/refMap.h (src/refMap.cu:59)
+ *   swift_seed         <- searchQueries3               src/search.h:33
+ *                         (lookupTable5MapQry          src/lookupTable5.h:42,
+ *                          mapHits6GetBestHits         src/mapHits6.h:34)
+ *   swift_sw_batch     <- alignSequences               src/align.cu:2904-2921
+ *                         (kernel smithWaterman        src/smithWaterman.h)
+ *   swift_align        <- searchQueries3 + alignQueries3 (src/align.h:33)
+ *                         with chooseBestAlignment and printOutput
+ *   swift_align_files  <- the swift CLI, src/main.cu:42-223
+ */
+#ifndef SWIFT_GB300_H_
+#define SWIFT_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SWIFT_OK 0
+#define SWIFT_E_ARG (-1)     /* invalid argument                          */
+#define SWIFT_E_INPUT (-2)   /* malformed or unsupported FASTA input      */
+#define SWIFT_E_CUDA (-3)    /* CUDA runtime error                        */
+#define SWIFT_E_NOMEM (-4)   /* device or host allocation failed          */
+#define SWIFT_E_LIMIT (-5)   /* size beyond a documented maximum          */
+#define SWIFT_E_DEVICE (-6)  /* a kernel reported an internal error       */
+
+typedef struct swift_ctx swift_ctx;
+typedef struct swift_index swift_index;
+
+/* Parameters of one alignment run; defaults from swift_params_default() are
+ * the reference's (src/common.h:29-75, src/main.cu:52-62). */
+typedef struct {
+  int32_t seed_len;      /* -l  (12)                                       */
+  int32_t ignore_thres;  /* -t  (1000)                                     */
+  int32_t max_hits;      /* hits per read strand (3)                       */
+  int32_t match;         /* -m  (2)                                        */
+  int32_t mismatch;      /* -M  (-1)                                       */
+  int32_t gap_open;      /* -O  (-10)                                      */
+  int32_t gap_ext;       /* -E  (-1)                                       */
+  int32_t qry_len;       /* -s; <= 0: length of the first read             */
+  int64_t device_mem;    /* bytes used to size Phase-2 batches the way the
+                            reference does from its device; 0: this GPU's  */
+} swift_params;
+
+/* One Phase-1 record (one line of the reference's match file,
+ * src/search.cu:2230-2240). */
+typedef struct {
+  int32_t read;      /* read index in file order                          */
+  int32_t strand;    /* 0 forward, 1 reverse complement                   */
+  int32_t ref_idx;   /* reference sequence index                          */
+  int32_t shift;     /* reference position - query offset                 */
+  int32_t ref_pos;   /* first reference position of the cluster           */
+} swift_match;
+
+/* Timings of the last swift_align call, in milliseconds of device time
+ * (CUDA events on the context stream). */
+typedef struct {
+  double seed_ms, pairs_ms, sw_ms, select_ms, format_ms, total_ms;
+  int64_t reads, records, printed, cells, out_bytes;
+  int64_t seed_overflow_strands, sw_generic_pairs;
+  int64_t launches;   /* kernels this library launched for the call       */
+} swift_stats;
+
+void swift_params_default(swift_params *p);
+
+/* device: CUDA ordinal; stream: a cudaStream_t to run on, or NULL to make
+ * one owned by the context. */
+int swift_ctx_create(int device, void *stream, swift_ctx **out);
+int swift_ctx_destroy(swift_ctx *ctx);
+const char *swift_last_error(const swift_ctx *ctx);
+/* Device facts the pipeline depends on: total device memory (it sizes the
+ * Phase-2 batches, as in the reference) and the SM count. */
+int swift_ctx_info(const swift_ctx *ctx, int64_t *total_mem, int32_t *sm_count);
+
+/* Builds the device-resident reference (file bytes, 2-bit codes) and SSAHA
+ * index from a reference FASTA held in host memory. */
+int swift_index_build(swift_ctx *ctx, const char *ref_fasta, size_t len,
+                      int32_t seed_len, int32_t ignore_thres,
+                      swift_index **out);
+int swift_index_destroy(swift_index *idx);
+/* Index contents in the reference layout (src/lookupTable5.cu:199-231):
+ * lookup[h] is the 1-based start of bucket h or 0; ref_idx/ref_pos have
+ * total+1 entries with slot 0 = -1.  Any pointer may be NULL. */
+int swift_index_info(swift_ctx *ctx, const swift_index *idx, int32_t *n_refs,
+                     int64_t *total_tuples, int64_t *n_buckets);
+int swift_index_export(swift_ctx *ctx, const swift_index *idx, int32_t *lookup,
+                       int32_t *repeats, int8_t *ref_idx, int32_t *ref_pos);
+
+/* Phase 1: SSAHA seeding of every read (and its reverse complement) of a
+ * reads FASTA in host memory.  Writes up to cap records in match-file order
+ * and the total count to *n (records beyond cap are counted, not written). */
+int swift_seed(swift_ctx *ctx, const swift_index *idx, const char *reads_fasta,
+               size_t len, int32_t max_hits, swift_match *out, int64_t cap,
+               int64_t *n);
+
+/* Phase 2 on explicit pairs, the alignSequences contract: n pairs, query i
+ * at qry + i*(Q+1) (Q bytes used), window i at ref + i*(R+1) (R bytes
+ * used), outputs per pair: score, start, end, length and the reversed
+ * consensus strings at qcons/rcons + i*(Q+R+2).  Pointers may be host or
+ * device memory.  Q <= 256, R <= 1024. */
+int swift_sw_batch(swift_ctx *ctx, const char *qry, const char *ref, int32_t Q,
+                   int32_t R, int64_t n_pairs, int32_t match, int32_t mismatch,
+                   int32_t gap_open, int32_t gap_ext, float *score,
+                   int32_t *start, int32_t *end, int32_t *len, char *qcons,
+                   char *rcons);
+
+/* The whole pipeline on a reads FASTA in host memory: seeding, windows,
+ * Smith-Waterman, best alignment per read, default records.  *out receives
+ * a buffer owned by the library (free with swift_free). */
+int swift_align(swift_ctx *ctx, const swift_index *idx, const char *reads_fasta,
+                size_t len, const swift_params *p, char **out, size_t *out_len,
+                swift_stats *stats);
+
+/* Resident form for serving and benchmarking: reads parsed and kept on the
+ * device; the output text stays on the device until fetched. */
+typedef struct swift_reads swift_reads;
+int swift_reads_upload(swift_ctx *ctx, const char *reads_fasta, size_t len,
+                       swift_reads **out);
+int swift_reads_destroy(swift_reads *r);
+int swift_align_resident(swift_ctx *ctx, const swift_index *idx,
+                         const swift_reads *reads, const swift_params *p,
+                         size_t *out_len, swift_stats *stats);
+/* Copies the text of the last swift_align_resident call into dst (at most
+ * cap bytes). */
+int swift_fetch_output(swift_ctx *ctx, char *dst, size_t cap);
+
+/* File-to-file pipeline, the CLI: reads the two FASTA files and writes the
+ * default output records to out_path. */
+int swift_align_files(swift_ctx *ctx, const char *qry_path, const char *ref_path,
+                      const char *out_path, const swift_params *p);
+
+/* Measured peak cell-update rate of the packed-int16 max-plus instruction
+ * on this GPU (2 cells per __vimax3_s16x2_relu lane instruction): the
+ * denominator of the Smith-Waterman roofline. */
+int swift_peak_dpx(swift_ctx *ctx, double *cells_per_s);
+
+void swift_free(void *p);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

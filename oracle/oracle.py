@@ -94,6 +94,12 @@ def lib():
                                 C.POINTER(Params), C.POINTER(C.c_void_p),
                                 C.POINTER(C.c_int), C.c_char_p, C.c_size_t]
         L.so_free.argtypes = [C.c_void_p]
+        L.so_session_create.argtypes = [C.c_char_p, C.c_size_t, C.POINTER(Params),
+                                        C.POINTER(C.c_void_p), C.c_char_p, C.c_size_t]
+        L.so_session_align.argtypes = [C.c_void_p, C.c_char_p, C.c_size_t,
+                                       C.POINTER(C.c_void_p), C.POINTER(C.c_size_t),
+                                       C.c_char_p, C.c_size_t]
+        L.so_session_free.argtypes = [C.c_void_p]
         _lib = L
     return _lib
 
@@ -227,3 +233,32 @@ def phase1(ref: bytes, reads: bytes, params: Params | None = None):
            for i in range(n.value)]
     lib().so_free(out)
     return res
+
+
+class Session:
+    """Reference parsed and indexed once; align() runs Phase 1 + Phase 2."""
+
+    def __init__(self, ref: bytes, params: Params | None = None):
+        self.p = params or default_params()
+        h = C.c_void_p()
+        err = C.create_string_buffer(512)
+        rc = lib().so_session_create(ref, len(ref), C.byref(self.p), C.byref(h), err, 512)
+        if rc != 0:
+            raise OracleError(err.value.decode())
+        self._h = h
+
+    def align(self, reads: bytes) -> bytes:
+        out = C.c_void_p()
+        n = C.c_size_t()
+        err = C.create_string_buffer(512)
+        rc = lib().so_session_align(self._h, reads, len(reads), C.byref(out), C.byref(n), err, 512)
+        if rc != 0:
+            raise OracleError(err.value.decode())
+        data = C.string_at(out, n.value)
+        lib().so_free(out)
+        return data
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().so_session_free(self._h)
+            self._h = None

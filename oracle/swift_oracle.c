@@ -841,29 +841,61 @@ static void so_print_record(so_sb *sb, const so_pair *x) {
   so_sb_put(sb, "\n", 1);
 }
 
+struct so_session {
+  so_ref r;
+  so_index *ix;
+  so_params p;
+};
+
+int so_session_create(const char *ref, size_t ref_len, const so_params *p,
+                      so_session **out, char *err, size_t errlen) {
+  so_session *s = (so_session *)calloc(1, sizeof(so_session));
+  s->p = *p;
+  int rc = so_ref_parse(ref, ref_len, &s->r, err, errlen);
+  if (rc == 0) rc = so_index_from_ref(&s->r, p->seed_len, p->ignore_thres, &s->ix, err, errlen);
+  if (rc != 0) {
+    so_session_free(s);
+    return rc;
+  }
+  *out = s;
+  return 0;
+}
+
+void so_session_free(so_session *s) {
+  if (!s) return;
+  so_index_free(s->ix);
+  so_ref_free(&s->r);
+  free(s);
+}
+
 int so_align(const char *ref, size_t ref_len, const char *reads,
              size_t reads_len, const so_params *p, char **out, size_t *out_len,
              char *err, size_t errlen) {
-  so_ref r;
+  so_session *s = NULL;
+  int rc = so_session_create(ref, ref_len, p, &s, err, errlen);
+  if (rc == 0) rc = so_session_align(s, reads, reads_len, out, out_len, err, errlen);
+  so_session_free(s);
+  return rc;
+}
+
+int so_session_align(so_session *ss, const char *reads, size_t reads_len,
+                     char **out, size_t *out_len, char *err, size_t errlen) {
+  const so_params *p = &ss->p;
+  so_ref r = ss->r;
   so_reads rd;
-  so_index *ix = NULL;
   so_match *m = NULL;
   int nm = 0;
   memset(&rd, 0, sizeof(rd));
-  int rc = so_ref_parse(ref, ref_len, &r, err, errlen);
-  if (rc == 0) rc = so_index_from_ref(&r, p->seed_len, p->ignore_thres, &ix, err, errlen);
-  if (rc == 0) rc = so_reads_parse(reads, reads_len, &rd, err, errlen);
-  if (rc == 0) rc = so_run_phase1(ix, &rd, p->max_hits, p->threads, &m, &nm);
-  so_index_free(ix);
+  int rc = so_reads_parse(reads, reads_len, &rd, err, errlen);
+  if (rc == 0) rc = so_run_phase1(ss->ix, &rd, p->max_hits, p->threads, &m, &nm);
   if (rc != 0) {
     free(rd.r);
-    so_ref_free(&r);
     return rc;
   }
   int Q = p->qry_len > 0 ? p->qry_len : rd.first_len;
   if (Q < 1 || Q > SO_QSEQ_MAX) {
     so_err(err, errlen, "query length %d outside 1..%d", Q, SO_QSEQ_MAX);
-    free(rd.r); free(m); so_ref_free(&r);
+    free(rd.r); free(m);
     return -1;
   }
   long per_iter = so_p2_batch(p->device_mem, Q, nm);
@@ -949,7 +981,6 @@ int so_align(const char *ref, size_t ref_len, const char *reads,
   free(tmpq);
   free(m);
   free(rd.r);
-  so_ref_free(&r);
   so_sb_put(&sb, "", 0);
   if (!sb.b) { sb.b = (char *)malloc(1); }
   sb.b[sb.n] = '\0';

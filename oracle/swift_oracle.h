@@ -96,6 +96,15 @@ int so_align(const char *ref, size_t ref_len, const char *reads,
              size_t reads_len, const so_params *p, char **out,
              size_t *out_len, char *err, size_t errlen);
 
+/* The same pipeline with the reference parsed and indexed once (the index
+ * build is then outside the timed alignment). */
+typedef struct so_session so_session;
+int so_session_create(const char *ref, size_t ref_len, const so_params *p,
+                      so_session **out, char *err, size_t errlen);
+int so_session_align(so_session *s, const char *reads, size_t reads_len,
+                     char **out, size_t *out_len, char *err, size_t errlen);
+void so_session_free(so_session *s);
+
 /* Phase 1 only: the match-file records in file order (including the
  * trailing-batch repeats of searchQueries3).  *out is malloc'ed. */
 int so_phase1(const char *ref, size_t ref_len, const char *reads,

@@ -1,0 +1,280 @@
+"""Python binding of libswift_gb300.so, the GB300 SWIFT aligner hot path.
+
+The library is the product: CUDA kernels for sm_103a behind the C ABI in
+include/swift_gb300.h.  This module only loads it with ctypes.  There is no
+CPU fallback: if the library cannot be loaded or no CUDA device is present,
+every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libswift_gb300.so")
+CLI_PATH = os.path.join(HERE, "swift")
+
+SWIFT_OK = 0
+ERRORS = {-1: "argument", -2: "input", -3: "cuda", -4: "memory", -5: "limit", -6: "device"}
+
+# Exported C symbols (kept in step with include/swift_gb300.h).
+EXPORTS = [
+    "swift_params_default", "swift_ctx_create", "swift_ctx_destroy", "swift_last_error",
+    "swift_ctx_info",
+    "swift_index_build", "swift_index_destroy", "swift_index_info", "swift_index_export",
+    "swift_seed", "swift_sw_batch", "swift_align", "swift_reads_upload",
+    "swift_reads_destroy", "swift_align_resident", "swift_fetch_output",
+    "swift_align_files", "swift_free", "swift_peak_dpx",
+]
+
+
+class SwiftError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"swift error {code} ({ERRORS.get(code, '?')}): {msg}")
+        self.code = code
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("seed_len", C.c_int32), ("ignore_thres", C.c_int32), ("max_hits", C.c_int32),
+        ("match", C.c_int32), ("mismatch", C.c_int32), ("gap_open", C.c_int32),
+        ("gap_ext", C.c_int32), ("qry_len", C.c_int32), ("device_mem", C.c_int64),
+    ]
+
+
+class Match(C.Structure):
+    _fields_ = [("read", C.c_int32), ("strand", C.c_int32), ("ref_idx", C.c_int32),
+                ("shift", C.c_int32), ("ref_pos", C.c_int32)]
+
+
+class Stats(C.Structure):
+    _fields_ = [
+        ("seed_ms", C.c_double), ("pairs_ms", C.c_double), ("sw_ms", C.c_double),
+        ("select_ms", C.c_double), ("format_ms", C.c_double), ("total_ms", C.c_double),
+        ("reads", C.c_int64), ("records", C.c_int64), ("printed", C.c_int64),
+        ("cells", C.c_int64), ("out_bytes", C.c_int64),
+        ("seed_overflow_strands", C.c_int64), ("sw_generic_pairs", C.c_int64),
+        ("launches", C.c_int64),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+
+
+def lib():
+    """Loads the in-tree library; raises if it is missing (no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise SwiftError(-3, f"{LIB_PATH} is missing: run __graft_entry__.build()")
+        L = C.CDLL(LIB_PATH)
+        vp, i32, i64, sz = C.c_void_p, C.c_int32, C.c_int64, C.c_size_t
+        L.swift_params_default.argtypes = [C.POINTER(Params)]
+        L.swift_params_default.restype = None
+        L.swift_ctx_create.argtypes = [C.c_int, vp, C.POINTER(vp)]
+        L.swift_ctx_destroy.argtypes = [vp]
+        L.swift_last_error.argtypes = [vp]
+        L.swift_last_error.restype = C.c_char_p
+        L.swift_ctx_info.argtypes = [vp, C.POINTER(i64), C.POINTER(i32)]
+        L.swift_index_build.argtypes = [vp, C.c_char_p, sz, i32, i32, C.POINTER(vp)]
+        L.swift_index_destroy.argtypes = [vp]
+        L.swift_index_info.argtypes = [vp, vp, C.POINTER(i32), C.POINTER(i64), C.POINTER(i64)]
+        L.swift_index_export.argtypes = [vp, vp, vp, vp, vp, vp]
+        L.swift_seed.argtypes = [vp, vp, C.c_char_p, sz, i32, vp, i64, C.POINTER(i64)]
+        L.swift_sw_batch.argtypes = [vp, vp, vp, i32, i32, i64, i32, i32, i32, i32,
+                                     vp, vp, vp, vp, vp, vp]
+        L.swift_align.argtypes = [vp, vp, vp, sz, C.POINTER(Params), C.POINTER(vp),
+                                  C.POINTER(sz), C.POINTER(Stats)]
+        L.swift_reads_upload.argtypes = [vp, C.c_char_p, sz, C.POINTER(vp)]
+        L.swift_reads_destroy.argtypes = [vp]
+        L.swift_align_resident.argtypes = [vp, vp, vp, C.POINTER(Params), C.POINTER(sz),
+                                           C.POINTER(Stats)]
+        L.swift_fetch_output.argtypes = [vp, vp, sz]
+        L.swift_align_files.argtypes = [vp, C.c_char_p, C.c_char_p, C.c_char_p,
+                                        C.POINTER(Params)]
+        L.swift_peak_dpx.argtypes = [vp, C.POINTER(C.c_double)]
+        L.swift_free.argtypes = [vp]
+        L.swift_free.restype = None
+        _lib = L
+    return _lib
+
+
+def default_params(**kw) -> Params:
+    p = Params()
+    lib().swift_params_default(C.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+class Context:
+    """A device context: one CUDA stream, one host thread at a time."""
+
+    def __init__(self, device: int = 0, stream: int | None = None):
+        h = C.c_void_p()
+        rc = lib().swift_ctx_create(device, C.c_void_p(stream) if stream else None, C.byref(h))
+        if rc != SWIFT_OK:
+            raise SwiftError(rc, "context creation failed (is a CUDA device present?)")
+        self._h = h
+
+    def _check(self, rc):
+        if rc != SWIFT_OK:
+            raise SwiftError(rc, lib().swift_last_error(self._h).decode(errors="replace"))
+
+    def info(self):
+        mem, sms = C.c_int64(), C.c_int32()
+        self._check(lib().swift_ctx_info(self._h, C.byref(mem), C.byref(sms)))
+        return dict(total_mem=mem.value, sm_count=sms.value)
+
+    def peak_dpx_cells_per_s(self) -> float:
+        v = C.c_double()
+        self._check(lib().swift_peak_dpx(self._h, C.byref(v)))
+        return v.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().swift_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    # -- index ---------------------------------------------------------------
+    def index(self, ref_fasta: bytes, seed_len: int = 12, ignore_thres: int = 1000) -> "Index":
+        return Index(self, ref_fasta, seed_len, ignore_thres)
+
+    def reads(self, reads_fasta: bytes) -> "Reads":
+        return Reads(self, reads_fasta)
+
+    # -- Phase 1 ---------------------------------------------------------------
+    def seed(self, index: "Index", reads_fasta: bytes, max_hits: int = 3):
+        n = C.c_int64()
+        self._check(lib().swift_seed(self._h, index._h, reads_fasta, len(reads_fasta), max_hits,
+                                     None, 0, C.byref(n)))
+        arr = (Match * max(n.value, 1))()
+        self._check(lib().swift_seed(self._h, index._h, reads_fasta, len(reads_fasta), max_hits,
+                                     arr, n.value, C.byref(n)))
+        return [(m.read, m.strand, m.ref_idx, m.shift, m.ref_pos) for m in arr[: n.value]]
+
+    # -- Phase 2 on explicit pairs (alignSequences) ------------------------------
+    def sw_batch(self, queries, windows, Q: int, R: int, match=2, mismatch=-1, gap_open=-10,
+                 gap_ext=-1):
+        import numpy as np
+        n = len(queries)
+        q = np.zeros((n, Q + 1), dtype=np.uint8)
+        w = np.zeros((n, R + 1), dtype=np.uint8)
+        for i, (a, b) in enumerate(zip(queries, windows)):
+            q[i, : min(len(a), Q)] = np.frombuffer(a[:Q], dtype=np.uint8)
+            w[i, : min(len(b), R)] = np.frombuffer(b[:R], dtype=np.uint8)
+        score = np.zeros(n, np.float32)
+        start = np.zeros(n, np.int32)
+        end = np.zeros(n, np.int32)
+        ln = np.zeros(n, np.int32)
+        qc = np.zeros((n, Q + R + 2), np.uint8)
+        rc = np.zeros((n, Q + R + 2), np.uint8)
+        self._check(lib().swift_sw_batch(
+            self._h, q.ctypes.data, w.ctypes.data, Q, R, n, match, mismatch, gap_open, gap_ext,
+            score.ctypes.data, start.ctypes.data, end.ctypes.data, ln.ctypes.data,
+            qc.ctypes.data, rc.ctypes.data))
+        out = []
+        for i in range(n):
+            L = int(ln[i])
+            out.append(dict(score=float(score[i]), start=int(start[i]), end=int(end[i]), len=L,
+                            qcons=bytes(qc[i, :max(L, 0)]), rcons=bytes(rc[i, :max(L, 0)])))
+        return out
+
+    # -- whole pipeline ----------------------------------------------------------
+    def align(self, index: "Index", reads_fasta, params: Params | None = None,
+              stats: bool = False, nbytes: int | None = None):
+        """reads_fasta: bytes, or an integer host address (e.g. of pinned
+        memory) with nbytes."""
+        p = params or default_params(seed_len=index.seed_len, ignore_thres=index.ignore_thres)
+        out = C.c_void_p()
+        n = C.c_size_t()
+        st = Stats()
+        if isinstance(reads_fasta, int):
+            ptr, ln = C.c_void_p(reads_fasta), nbytes
+        else:
+            ptr, ln = C.cast(C.c_char_p(reads_fasta), C.c_void_p), len(reads_fasta)
+        self._check(lib().swift_align(self._h, index._h, ptr, ln,
+                                      C.byref(p), C.byref(out), C.byref(n), C.byref(st)))
+        data = C.string_at(out, n.value) if n.value else b""
+        lib().swift_free(out)
+        return (data, st.as_dict()) if stats else data
+
+    def align_resident(self, index: "Index", reads: "Reads", params: Params | None = None):
+        p = params or default_params(seed_len=index.seed_len, ignore_thres=index.ignore_thres)
+        n = C.c_size_t()
+        st = Stats()
+        self._check(lib().swift_align_resident(self._h, index._h, reads._h, C.byref(p),
+                                               C.byref(n), C.byref(st)))
+        return n.value, st.as_dict()
+
+    def fetch_output(self, n: int) -> bytes:
+        buf = C.create_string_buffer(max(n, 1))
+        self._check(lib().swift_fetch_output(self._h, buf, n))
+        return buf.raw[:n]
+
+    def align_files(self, qry_path: str, ref_path: str, out_path: str,
+                    params: Params | None = None):
+        p = params or default_params()
+        self._check(lib().swift_align_files(self._h, qry_path.encode(), ref_path.encode(),
+                                            out_path.encode(), C.byref(p)))
+
+
+class Index:
+    """Device-resident reference (FASTA bytes, 2-bit codes) and SSAHA index."""
+
+    def __init__(self, ctx: Context, ref_fasta: bytes, seed_len=12, ignore_thres=1000):
+        h = C.c_void_p()
+        ctx._check(lib().swift_index_build(ctx._h, ref_fasta, len(ref_fasta), seed_len,
+                                           ignore_thres, C.byref(h)))
+        self._h = h
+        self.ctx = ctx
+        self.seed_len = seed_len
+        self.ignore_thres = ignore_thres
+
+    def info(self):
+        nr, tot, nb = C.c_int32(), C.c_int64(), C.c_int64()
+        self.ctx._check(lib().swift_index_info(self.ctx._h, self._h, C.byref(nr), C.byref(tot),
+                                               C.byref(nb)))
+        return dict(n_refs=nr.value, total=tot.value, n_buckets=nb.value)
+
+    def export(self):
+        import numpy as np
+        inf = self.info()
+        look = np.zeros(inf["n_buckets"], np.int32)
+        rep = np.zeros(inf["n_buckets"], np.int32)
+        ri = np.zeros(inf["total"] + 1, np.int8)
+        rp = np.zeros(inf["total"] + 1, np.int32)
+        self.ctx._check(lib().swift_index_export(self.ctx._h, self._h, look.ctypes.data,
+                                                 rep.ctypes.data, ri.ctypes.data, rp.ctypes.data))
+        return look, rep, ri, rp
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().swift_index_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
+class Reads:
+    """Reads parsed and resident on the device."""
+
+    def __init__(self, ctx: Context, reads_fasta: bytes):
+        h = C.c_void_p()
+        ctx._check(lib().swift_reads_upload(ctx._h, reads_fasta, len(reads_fasta), C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().swift_reads_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()

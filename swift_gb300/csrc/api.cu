@@ -1,0 +1,912 @@
+// C ABI and pipeline orchestration.  Everything on the data path runs on the
+// context's stream; the host only parses FASTA structure, sizes buffers and
+// reads back the few counts that size the next stage.
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "internal.h"
+
+
+using namespace swift;
+
+struct swift_ctx {
+  int device = 0;
+  cudaStream_t st = nullptr;
+  bool own_stream = false;
+  std::string err;
+  int64_t total_mem = 0;
+  cudaEvent_t ev[8] = {};
+  char* d_text = nullptr;
+  size_t text_len = 0, text_cap = 0;
+};
+
+struct swift_index {
+  int device = 0;
+  int k = 12, thres = 1000;
+  char* d_file = nullptr;
+  uint64_t file_len = 0;
+  DevRecord* d_recs = nullptr;
+  std::vector<RefRecord> recs;
+  uint8_t* d_cat = nullptr;
+  uint32_t* d_packed = nullptr;
+  uint64_t cat_len = 0;
+  uint32_t* d_count = nullptr;
+  uint32_t* d_offsets = nullptr;
+  uint2* d_post = nullptr;
+  int64_t total = 0;
+  int64_t nb = 0;
+};
+
+struct swift_reads {
+  int device = 0;
+  char* d_bytes = nullptr;
+  uint64_t len = 0;
+  DevRead* d_rd = nullptr;
+  HostReads h;
+  std::vector<int32_t> repeats;
+};
+
+namespace {
+
+int fail(swift_ctx* ctx, int code, const std::string& msg) {
+  if (ctx) ctx->err = msg;
+  return code;
+}
+
+#define CK(call)                                                                        \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess)                                                              \
+      return fail(ctx, SWIFT_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+#define CKLAUNCH()                                                                     \
+  do {                                                                                 \
+    cudaError_t e_ = cudaGetLastError();                                               \
+    if (e_ != cudaSuccess)                                                             \
+      return fail(ctx, SWIFT_E_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e_)); \
+  } while (0)
+
+// Stream-ordered temporaries released at the end of a call.
+struct Scratch {
+  cudaStream_t st;
+  std::vector<void*> ptrs;
+  explicit Scratch(cudaStream_t s) : st(s) {}
+  ~Scratch() {
+    for (void* p : ptrs) cudaFreeAsync(p, st);
+  }
+  template <typename T>
+  cudaError_t get(T** out, size_t count) {
+    void* p = nullptr;
+    cudaError_t e = cudaMallocAsync(&p, std::max<size_t>(count * sizeof(T), 16), st);
+    if (e != cudaSuccess) return e;
+    ptrs.push_back(p);
+    *out = (T*)p;
+    return cudaSuccess;
+  }
+};
+
+void keep_pool(int device) {
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+    uint64_t thr = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+}
+
+// Records of all read strands -> match arrays in match-file order.
+__global__ void fill_matches_kernel(const int32_t* __restrict__ nbest, const int3* __restrict__ best,
+                                    int max_hits, int64_t n_reads, const uint64_t* __restrict__ roff,
+                                    const int32_t* __restrict__ rep, const uint64_t* __restrict__ rep_off,
+                                    int64_t n_rep, int32_t* m_read, int32_t* m_strand, int32_t* m_ri,
+                                    int32_t* m_sh, int32_t* m_rp) {
+  int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= n_reads + n_rep) return;
+  int64_t read;
+  uint64_t o;
+  if (v < n_reads) {
+    read = v;
+    o = roff[v];
+  } else {
+    read = rep[v - n_reads];
+    o = rep_off[v - n_reads];
+  }
+  for (int s = 0; s < 2; ++s) {
+    const int64_t sid = 2 * read + s;
+    const int c = nbest[sid];
+    for (int h = 0; h < c; ++h) {
+      const int3 b = best[sid * max_hits + h];
+      m_read[o] = (int32_t)read;
+      m_strand[o] = s;
+      m_ri[o] = b.x;
+      m_sh[o] = b.y;
+      m_rp[o] = b.z;
+      ++o;
+    }
+  }
+}
+
+__global__ void read_counts_kernel(const int32_t* __restrict__ nbest, int64_t n_reads,
+                                   uint64_t* __restrict__ cnt) {
+  int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < n_reads) cnt[r] = (uint64_t)(nbest[2 * r] + nbest[2 * r + 1]);
+}
+
+__global__ void aln_to_ref_layout_kernel(const DevAln* __restrict__ aln, int64_t n, float* score,
+                                         int32_t* start, int32_t* end, int32_t* len) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  DevAln a = aln[i];
+  score[i] = (float)a.score;
+  start[i] = a.start;
+  end[i] = a.end;
+  len[i] = a.len;
+}
+
+struct SeedOut {
+  int32_t *m_read = nullptr, *m_strand = nullptr, *m_ri = nullptr, *m_sh = nullptr,
+          *m_rp = nullptr;
+  int64_t n = 0;
+  int64_t overflow = 0;
+  int64_t launches = 0;
+};
+
+// Phase 1 for resident reads: fills the match arrays (allocated in sc).
+int run_seed(swift_ctx* ctx, const swift_index* idx, const swift_reads* rd, int max_hits,
+             Scratch& sc, SeedOut* out) {
+  const int64_t n = (int64_t)rd->h.len.size();
+  const int64_t ns = 2 * n;
+  cudaStream_t st = ctx->st;
+  int3* best;
+  int32_t *nbest, *ovl, *novl;
+  CK(sc.get(&best, (size_t)std::max<int64_t>(ns, 1) * max_hits));
+  CK(sc.get(&nbest, (size_t)std::max<int64_t>(ns, 1)));
+  CK(sc.get(&ovl, (size_t)std::max<int64_t>(ns, 1)));
+  CK(sc.get(&novl, 1));
+  CK(cudaMemsetAsync(novl, 0, sizeof(int32_t), st));
+  SeedArgs a;
+  memset(&a, 0, sizeof(a));
+  a.reads = rd->d_bytes;
+  a.rd = rd->d_rd;
+  a.n_reads = n;
+  a.offsets = idx->d_offsets;
+  a.postings = idx->d_post;
+  a.k = idx->k;
+  a.max_hits = max_hits;
+  a.best = best;
+  a.nbest = nbest;
+  a.overflow_list = ovl;
+  a.n_overflow = novl;
+  launch_seed(st, a);
+  CKLAUNCH();
+  out->launches += n > 0 ? 1 : 0;
+  int32_t h_novl = 0;
+  CK(cudaMemcpyAsync(&h_novl, novl, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  out->overflow = h_novl;
+  if (h_novl > 0) {
+    std::vector<int32_t> list(h_novl), nb(ns);
+    CK(cudaMemcpyAsync(list.data(), ovl, h_novl * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(nb.data(), nbest, ns * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    std::vector<uint64_t> toff(h_novl);
+    std::vector<uint32_t> tsz(h_novl);
+    uint64_t tot = 0;
+    for (int i = 0; i < h_novl; ++i) {
+      uint32_t hits = (uint32_t)(-nb[list[i]]);
+      uint32_t S = 64;
+      while (S < 2 * hits) S <<= 1;
+      toff[i] = tot;
+      tsz[i] = S;
+      tot += 2 * (uint64_t)S;  // S keys (8 B) + 2 S counters (4 B)
+    }
+    uint64_t* scratch;
+    uint64_t* d_toff;
+    uint32_t* d_tsz;
+    CK(sc.get(&scratch, tot));
+    CK(sc.get(&d_toff, h_novl));
+    CK(sc.get(&d_tsz, h_novl));
+    CK(cudaMemsetAsync(scratch, 0, tot * sizeof(uint64_t), st));
+    CK(cudaMemcpyAsync(d_toff, toff.data(), h_novl * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(d_tsz, tsz.data(), h_novl * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    a.scratch = scratch;
+    launch_seed_overflow(st, a, h_novl, d_toff, d_tsz);
+    CKLAUNCH();
+    out->launches += 1;
+  }
+  // per-read record counts -> offsets
+  uint64_t *cnt, *roff, *tot_d;
+  void* tmp;
+  CK(sc.get(&cnt, (size_t)std::max<int64_t>(n, 1)));
+  CK(sc.get(&roff, (size_t)std::max<int64_t>(n, 1)));
+  CK(sc.get(&tot_d, 1));
+  CK(sc.get((uint8_t**)&tmp, scan_temp_bytes(n)));
+  if (n > 0) read_counts_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(nbest, n, cnt);
+  CKLAUNCH();
+  out->launches += (n > 0 ? 1 : 0) + exclusive_scan_u64(st, cnt, roff, n, tmp, tot_d);
+  CKLAUNCH();
+  uint64_t total_in = 0;
+  CK(cudaMemcpyAsync(&total_in, tot_d, sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+  const std::vector<int32_t>& rep = rd->repeats;
+  std::vector<uint64_t> rep_cnt(rep.size()), rep_off(rep.size());
+  std::vector<int32_t> rep_nb(2 * rep.size());
+  for (size_t i = 0; i < rep.size(); ++i)
+    CK(cudaMemcpyAsync(&rep_nb[2 * i], nbest + 2 * (int64_t)rep[i], 2 * sizeof(int32_t),
+                       cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  uint64_t total = total_in;
+  for (size_t i = 0; i < rep.size(); ++i) {
+    rep_off[i] = total;
+    total += (uint64_t)(rep_nb[2 * i] + rep_nb[2 * i + 1]);
+  }
+  int32_t* d_rep;
+  uint64_t* d_rep_off;
+  CK(sc.get(&d_rep, std::max<size_t>(rep.size(), 1)));
+  CK(sc.get(&d_rep_off, std::max<size_t>(rep.size(), 1)));
+  if (!rep.empty()) {
+    CK(cudaMemcpyAsync(d_rep, rep.data(), rep.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(d_rep_off, rep_off.data(), rep.size() * sizeof(uint64_t),
+                       cudaMemcpyHostToDevice, st));
+  }
+  const size_t tn = std::max<uint64_t>(total, 1);
+  CK(sc.get(&out->m_read, tn));
+  CK(sc.get(&out->m_strand, tn));
+  CK(sc.get(&out->m_ri, tn));
+  CK(sc.get(&out->m_sh, tn));
+  CK(sc.get(&out->m_rp, tn));
+  const int64_t nv = n + (int64_t)rep.size();
+  if (nv > 0)
+    fill_matches_kernel<<<(unsigned)((nv + 255) / 256), 256, 0, st>>>(
+        nbest, best, max_hits, n, roff, d_rep, d_rep_off, (int64_t)rep.size(), out->m_read,
+        out->m_strand, out->m_ri, out->m_sh, out->m_rp);
+  CKLAUNCH();
+  out->launches += nv > 0 ? 1 : 0;
+  out->n = (int64_t)total;
+  return SWIFT_OK;
+}
+
+int upload_reads(swift_ctx* ctx, const char* b, size_t len, swift_reads** out) {
+  swift_reads* r = new swift_reads();
+  r->device = ctx->device;
+  int rc = parse_reads(b, len, &r->h, &ctx->err);
+  if (rc != SWIFT_OK) {
+    delete r;
+    return rc;
+  }
+  r->repeats = phase1_stale_repeats((int64_t)r->h.len.size(), r->h.n_gt);
+  const size_t n = r->h.len.size();
+  std::vector<DevRead> dr(n);
+  for (size_t i = 0; i < n; ++i) {
+    dr[i].name_off = r->h.name_off[i];
+    dr[i].seq_off = r->h.seq_off[i];
+    dr[i].len = r->h.len[i];
+    dr[i].name_len = r->h.name_len[i];
+  }
+  r->len = len;
+  cudaError_t e = cudaMalloc(&r->d_bytes, len + 64);
+  if (e == cudaSuccess) e = cudaMalloc(&r->d_rd, std::max<size_t>(n, 1) * sizeof(DevRead));
+  if (e == cudaSuccess) e = cudaMemcpyAsync(r->d_bytes, b, len, cudaMemcpyHostToDevice, ctx->st);
+  if (e == cudaSuccess && n)
+    e = cudaMemcpyAsync(r->d_rd, dr.data(), n * sizeof(DevRead), cudaMemcpyHostToDevice, ctx->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->st);
+  if (e != cudaSuccess) {
+    swift_reads_destroy(r);
+    return fail(ctx, SWIFT_E_CUDA, std::string("reads upload: ") + cudaGetErrorString(e));
+  }
+  *out = r;
+  return SWIFT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void swift_params_default(swift_params* p) {
+  p->seed_len = 12;
+  p->ignore_thres = 1000;
+  p->max_hits = 3;
+  p->match = 2;
+  p->mismatch = -1;
+  p->gap_open = -10;
+  p->gap_ext = -1;
+  p->qry_len = 0;
+  p->device_mem = 0;
+}
+
+int swift_ctx_create(int device, void* stream, swift_ctx** out) {
+  if (!out) return SWIFT_E_ARG;
+  swift_ctx* ctx = new swift_ctx();
+  ctx->device = device;
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) {
+    if (stream) {
+      ctx->st = (cudaStream_t)stream;
+    } else {
+      e = cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking);
+      ctx->own_stream = true;
+    }
+  }
+  if (e == cudaSuccess) {
+    size_t fr = 0, tot = 0;
+    e = cudaMemGetInfo(&fr, &tot);
+    ctx->total_mem = (int64_t)tot;
+  }
+  for (int i = 0; i < 8 && e == cudaSuccess; ++i) e = cudaEventCreate(&ctx->ev[i]);
+  if (e != cudaSuccess) {
+    delete ctx;
+    return SWIFT_E_CUDA;
+  }
+  keep_pool(device);
+  *out = ctx;
+  return SWIFT_OK;
+}
+
+int swift_ctx_destroy(swift_ctx* ctx) {
+  if (!ctx) return SWIFT_OK;
+  cudaSetDevice(ctx->device);
+  if (ctx->st) cudaStreamSynchronize(ctx->st);
+  if (ctx->d_text) cudaFree(ctx->d_text);
+  for (int i = 0; i < 8; ++i)
+    if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
+  if (ctx->own_stream) cudaStreamDestroy(ctx->st);
+  delete ctx;
+  return SWIFT_OK;
+}
+
+const char* swift_last_error(const swift_ctx* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+int swift_ctx_info(const swift_ctx* ctx, int64_t* total_mem, int32_t* sm_count) {
+  if (!ctx) return SWIFT_E_ARG;
+  if (total_mem) *total_mem = ctx->total_mem;
+  if (sm_count) {
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, ctx->device) != cudaSuccess)
+      return SWIFT_E_CUDA;
+    *sm_count = v;
+  }
+  return SWIFT_OK;
+}
+
+void swift_free(void* p) { free(p); }
+
+int swift_peak_dpx(swift_ctx* ctx, double* cells_per_s) {
+  if (!ctx || !cells_per_s) return fail(ctx, SWIFT_E_ARG, "null argument");
+  CK(cudaSetDevice(ctx->device));
+  double ips = 0;
+  int rc = measure_dpx_peak(ctx->st, ctx->device, &ips);
+  if (rc != SWIFT_OK) return fail(ctx, rc, "calibration kernel failed");
+  *cells_per_s = 2.0 * ips;
+  return SWIFT_OK;
+}
+
+int swift_index_build(swift_ctx* ctx, const char* ref, size_t len, int32_t k, int32_t thres,
+                      swift_index** out) {
+  if (!ctx || !ref || !out) return fail(ctx, SWIFT_E_ARG, "null argument");
+  if (k < 1 || k > 15) return fail(ctx, SWIFT_E_ARG, "seed length outside 1..15");
+  if (thres < 0) return fail(ctx, SWIFT_E_ARG, "negative ignore threshold");
+  CK(cudaSetDevice(ctx->device));
+  HostRef hr;
+  int rc = parse_reference(ref, len, &hr, &ctx->err);
+  if (rc != SWIFT_OK) return rc;
+  cudaStream_t st = ctx->st;
+  swift_index* ix = new swift_index();
+  ix->device = ctx->device;
+  ix->k = k;
+  ix->thres = thres;
+  ix->file_len = len;
+  ix->recs = hr.recs;
+  ix->cat_len = hr.cat_len;
+  ix->nb = (int64_t)1 << (2 * k);
+  const int nr = (int)hr.recs.size();
+  std::vector<DevRecord> dr(nr);
+  std::vector<uint64_t> tbase(nr + 1, 0);
+  for (int i = 0; i < nr; ++i) {
+    memset(&dr[i], 0, sizeof(DevRecord));
+    dr[i].seq_off = hr.recs[i].seq_off;
+    dr[i].cat_start = hr.recs[i].cat_start;
+    dr[i].cat_len = hr.recs[i].cat_len;
+    dr[i].bpl = hr.recs[i].bpl;
+    dr[i].name_len = hr.recs[i].name_len;
+    memcpy(dr[i].name, hr.recs[i].name, kNameMax);
+    tbase[i + 1] = tbase[i] + hr.recs[i].cat_len / (uint64_t)k;
+  }
+  const uint64_t n_tuples = tbase[nr];
+  const int64_t n_lines = (int64_t)hr.line_len.size();
+  const int64_t n_words = (int64_t)((hr.cat_len + 15) / 16);
+  auto bail = [&](int code, const std::string& m) {
+    swift_index_destroy(ix);
+    return fail(ctx, code, m);
+  };
+#define CKI(call)                                                                       \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess) return bail(SWIFT_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+  CKI(cudaMalloc(&ix->d_file, len + 64));
+  CKI(cudaMalloc(&ix->d_recs, std::max(nr, 1) * sizeof(DevRecord)));
+  CKI(cudaMalloc(&ix->d_cat, (size_t)n_words * 16 + 64));
+  CKI(cudaMalloc(&ix->d_packed, ((size_t)n_words + 2) * sizeof(uint32_t)));
+  CKI(cudaMalloc(&ix->d_count, (size_t)ix->nb * sizeof(uint32_t)));
+  CKI(cudaMalloc(&ix->d_offsets, ((size_t)ix->nb + 1) * sizeof(uint32_t)));
+  {
+    Scratch sc(st);
+    uint64_t *d_src, *d_dst, *d_tbase;
+    uint32_t *d_len, *d_eff, *d_cursor;
+    void* tmp;
+    CKI(sc.get(&d_src, n_lines));
+    CKI(sc.get(&d_dst, n_lines));
+    CKI(sc.get(&d_len, n_lines));
+    CKI(sc.get(&d_tbase, nr + 1));
+    CKI(sc.get(&d_eff, (size_t)ix->nb));
+    CKI(sc.get(&d_cursor, (size_t)ix->nb));
+    CKI(sc.get((uint8_t**)&tmp, scan_temp_bytes(ix->nb)));
+    CKI(cudaMemcpyAsync(ix->d_file, ref, len, cudaMemcpyHostToDevice, st));
+    CKI(cudaMemcpyAsync(ix->d_recs, dr.data(), nr * sizeof(DevRecord), cudaMemcpyHostToDevice, st));
+    if (n_lines) {
+      CKI(cudaMemcpyAsync(d_src, hr.line_src.data(), n_lines * 8, cudaMemcpyHostToDevice, st));
+      CKI(cudaMemcpyAsync(d_dst, hr.line_dst.data(), n_lines * 8, cudaMemcpyHostToDevice, st));
+      CKI(cudaMemcpyAsync(d_len, hr.line_len.data(), n_lines * 4, cudaMemcpyHostToDevice, st));
+    }
+    CKI(cudaMemcpyAsync(d_tbase, tbase.data(), (nr + 1) * 8, cudaMemcpyHostToDevice, st));
+    CKI(cudaMemsetAsync(ix->d_cat, 0, (size_t)n_words * 16 + 64, st));
+    CKI(cudaMemsetAsync(ix->d_packed, 0, ((size_t)n_words + 2) * sizeof(uint32_t), st));
+    CKI(cudaMemsetAsync(ix->d_count, 0, (size_t)ix->nb * sizeof(uint32_t), st));
+    CKI(cudaMemsetAsync(d_cursor, 0, (size_t)ix->nb * sizeof(uint32_t), st));
+    launch_compact_lines(st, ix->d_file, d_src, d_dst, d_len, n_lines, ix->d_cat);
+    launch_pack2bit(st, ix->d_cat, n_words, ix->d_packed);
+    launch_count_tuples(st, ix->d_packed, ix->d_recs, d_tbase, nr, n_tuples, k, ix->d_count);
+    launch_threshold(st, ix->d_count, ix->nb, (uint32_t)thres, d_eff);
+    exclusive_scan_u32(st, d_eff, ix->d_offsets, ix->nb, tmp, ix->d_offsets + ix->nb);
+    uint32_t total = 0;
+    CKI(cudaMemcpyAsync(&total, ix->d_offsets + ix->nb, 4, cudaMemcpyDeviceToHost, st));
+    CKI(cudaStreamSynchronize(st));
+    ix->total = total;
+    CKI(cudaMalloc(&ix->d_post, std::max<size_t>(total, 1) * sizeof(uint2)));
+    launch_scatter_tuples(st, ix->d_packed, ix->d_recs, d_tbase, nr, n_tuples, k, (uint32_t)thres,
+                          ix->d_count, ix->d_offsets, d_cursor, ix->d_post);
+    launch_order_buckets(st, ix->d_offsets, ix->nb, ix->d_post);
+    CKI(cudaGetLastError());
+  }
+  CKI(cudaStreamSynchronize(st));
+#undef CKI
+  *out = ix;
+  return SWIFT_OK;
+}
+
+int swift_index_destroy(swift_index* ix) {
+  if (!ix) return SWIFT_OK;
+  cudaSetDevice(ix->device);
+  cudaFree(ix->d_file);
+  cudaFree(ix->d_recs);
+  cudaFree(ix->d_cat);
+  cudaFree(ix->d_packed);
+  cudaFree(ix->d_count);
+  cudaFree(ix->d_offsets);
+  cudaFree(ix->d_post);
+  delete ix;
+  return SWIFT_OK;
+}
+
+int swift_index_info(swift_ctx* ctx, const swift_index* ix, int32_t* n_refs, int64_t* total,
+                     int64_t* nb) {
+  if (!ix) return fail(ctx, SWIFT_E_ARG, "null index");
+  if (n_refs) *n_refs = (int32_t)ix->recs.size();
+  if (total) *total = ix->total;
+  if (nb) *nb = ix->nb;
+  return SWIFT_OK;
+}
+
+int swift_index_export(swift_ctx* ctx, const swift_index* ix, int32_t* lookup, int32_t* repeats,
+                       int8_t* ref_idx, int32_t* ref_pos) {
+  if (!ctx || !ix) return fail(ctx, SWIFT_E_ARG, "null argument");
+  CK(cudaSetDevice(ctx->device));
+  std::vector<uint32_t> cnt(ix->nb), off(ix->nb + 1);
+  std::vector<uint2> post(std::max<int64_t>(ix->total, 1));
+  CK(cudaMemcpy(cnt.data(), ix->d_count, ix->nb * 4, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(off.data(), ix->d_offsets, (ix->nb + 1) * 4, cudaMemcpyDeviceToHost));
+  if (ix->total) CK(cudaMemcpy(post.data(), ix->d_post, ix->total * 8, cudaMemcpyDeviceToHost));
+  for (int64_t h = 0; h < ix->nb; ++h) {
+    const bool kept = cnt[h] > 0 && cnt[h] <= (uint32_t)ix->thres;
+    if (lookup) lookup[h] = kept ? (int32_t)off[h] + 1 : 0;
+    if (repeats) repeats[h] = (int32_t)cnt[h];
+  }
+  if (ref_idx) {
+    ref_idx[0] = -1;
+    for (int64_t i = 0; i < ix->total; ++i) ref_idx[i + 1] = (int8_t)post[i].y;
+  }
+  if (ref_pos) {
+    ref_pos[0] = -1;
+    for (int64_t i = 0; i < ix->total; ++i) ref_pos[i + 1] = (int32_t)post[i].x;
+  }
+  return SWIFT_OK;
+}
+
+int swift_reads_upload(swift_ctx* ctx, const char* b, size_t len, swift_reads** out) {
+  if (!ctx || !b || !out) return fail(ctx, SWIFT_E_ARG, "null argument");
+  CK(cudaSetDevice(ctx->device));
+  return upload_reads(ctx, b, len, out);
+}
+
+int swift_reads_destroy(swift_reads* r) {
+  if (!r) return SWIFT_OK;
+  cudaSetDevice(r->device);
+  cudaFree(r->d_bytes);
+  cudaFree(r->d_rd);
+  delete r;
+  return SWIFT_OK;
+}
+
+int swift_seed(swift_ctx* ctx, const swift_index* idx, const char* reads, size_t len,
+               int32_t max_hits, swift_match* out, int64_t cap, int64_t* n) {
+  if (!ctx || !idx || !reads || !n) return fail(ctx, SWIFT_E_ARG, "null argument");
+  if (max_hits < 1 || max_hits > 64) return fail(ctx, SWIFT_E_ARG, "max_hits outside 1..64");
+  CK(cudaSetDevice(ctx->device));
+  swift_reads* rd = nullptr;
+  int rc = upload_reads(ctx, reads, len, &rd);
+  if (rc != SWIFT_OK) return rc;
+  {
+    Scratch sc(ctx->st);
+    SeedOut so;
+    rc = run_seed(ctx, idx, rd, max_hits, sc, &so);
+    if (rc == SWIFT_OK) {
+      *n = so.n;
+      int64_t w = std::min<int64_t>(so.n, cap);
+      if (w > 0 && out) {
+        std::vector<int32_t> a(w), b(w), c(w), d(w), f(w);
+        cudaStream_t st = ctx->st;
+        cudaError_t e = cudaMemcpyAsync(a.data(), so.m_read, w * 4, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(b.data(), so.m_strand, w * 4, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(c.data(), so.m_ri, w * 4, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(d.data(), so.m_rp, w * 4, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(f.data(), so.m_sh, w * 4, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) {
+          rc = fail(ctx, SWIFT_E_CUDA, cudaGetErrorString(e));
+        } else {
+          for (int64_t i = 0; i < w; ++i) {
+            out[i].read = a[i];
+            out[i].strand = b[i];
+            out[i].ref_idx = c[i];
+            out[i].ref_pos = d[i];
+            out[i].shift = f[i];
+          }
+        }
+      }
+    }
+  }
+  swift_reads_destroy(rd);
+  return rc;
+}
+
+int swift_sw_batch(swift_ctx* ctx, const char* qry, const char* ref, int32_t Q, int32_t R,
+                   int64_t n, int32_t m, int32_t x, int32_t o, int32_t e, float* score,
+                   int32_t* start, int32_t* end, int32_t* len, char* qcons, char* rcons) {
+  if (!ctx || !qry || !ref || !score || !start || !end || !len || !qcons || !rcons)
+    return fail(ctx, SWIFT_E_ARG, "null argument");
+  if (n < 0) return fail(ctx, SWIFT_E_ARG, "negative pair count");
+  if (Q < 1 || Q > kMaxQ || R < 1 || R > kMaxR)
+    return fail(ctx, SWIFT_E_LIMIT, "Q must be 1..256 and R 1..1024");
+  if (n == 0) return SWIFT_OK;
+  CK(cudaSetDevice(ctx->device));
+  cudaStream_t st = ctx->st;
+  Scratch sc(st);
+  auto is_dev = [](const void* p) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+  };
+  const int64_t cs = (int64_t)Q + R + 2;
+  const char* dq = qry;
+  const char* dw = ref;
+  if (!is_dev(qry)) {
+    char* t;
+    CK(sc.get(&t, (size_t)n * (Q + 1)));
+    CK(cudaMemcpyAsync(t, qry, (size_t)n * (Q + 1), cudaMemcpyHostToDevice, st));
+    dq = t;
+  }
+  if (!is_dev(ref)) {
+    char* t;
+    CK(sc.get(&t, (size_t)n * (R + 1)));
+    CK(cudaMemcpyAsync(t, ref, (size_t)n * (R + 1), cudaMemcpyHostToDevice, st));
+    dw = t;
+  }
+  DevAln* aln;
+  CK(sc.get(&aln, (size_t)n));
+  const bool out_dev = is_dev(score);
+  char *dqc = qcons, *drc = rcons;
+  if (!is_dev(qcons)) CK(sc.get(&dqc, (size_t)n * cs));
+  if (!is_dev(rcons)) CK(sc.get(&drc, (size_t)n * cs));
+  SwArgs a;
+  memset(&a, 0, sizeof(a));
+  a.q = dq;
+  a.w = dw;
+  a.q_stride = Q + 1;
+  a.w_stride = R + 1;
+  a.Q = Q;
+  a.R = R;
+  a.match = m;
+  a.mismatch = x;
+  a.gap_open = o;
+  a.gap_ext = e;
+  a.n = n;
+  a.aln = aln;
+  a.qcons = dqc;
+  a.rcons = drc;
+  a.cons_stride = cs;
+  int rc = launch_sw(st, a, &ctx->err);
+  if (rc != SWIFT_OK) return rc;
+  CKLAUNCH();
+  float* dscore = score;
+  int32_t *dstart = start, *dend = end, *dlen = len;
+  if (!out_dev) {
+    CK(sc.get(&dscore, n));
+    CK(sc.get(&dstart, n));
+    CK(sc.get(&dend, n));
+    CK(sc.get(&dlen, n));
+  }
+  aln_to_ref_layout_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(aln, n, dscore, dstart, dend,
+                                                                       dlen);
+  CKLAUNCH();
+  if (!out_dev) {
+    CK(cudaMemcpyAsync(score, dscore, n * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(start, dstart, n * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(end, dend, n * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(len, dlen, n * 4, cudaMemcpyDeviceToHost, st));
+  }
+  if (dqc != qcons) CK(cudaMemcpyAsync(qcons, dqc, (size_t)n * cs, cudaMemcpyDeviceToHost, st));
+  if (drc != rcons) CK(cudaMemcpyAsync(rcons, drc, (size_t)n * cs, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  return SWIFT_OK;
+}
+
+int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_reads* rd,
+                         const swift_params* p, size_t* out_len, swift_stats* stats) {
+  if (!ctx || !idx || !rd || !p) return fail(ctx, SWIFT_E_ARG, "null argument");
+  CK(cudaSetDevice(ctx->device));
+  if (p->seed_len != idx->k || p->ignore_thres != idx->thres)
+    return fail(ctx, SWIFT_E_ARG, "parameters differ from the index's seed length / threshold");
+  if (p->max_hits < 1 || p->max_hits > 64) return fail(ctx, SWIFT_E_ARG, "max_hits outside 1..64");
+  const int Q = p->qry_len > 0 ? p->qry_len : rd->h.first_len;
+  if (Q < 1 || Q > kMaxQ) return fail(ctx, SWIFT_E_LIMIT, "query length outside 1..256");
+  if (!rd->h.len.empty() && rd->h.min_len < Q)
+    return fail(ctx, SWIFT_E_INPUT,
+                "a read is shorter than the query length; the reference aligns such reads "
+                "against stale buffer contents");
+  cudaStream_t st = ctx->st;
+  Scratch sc(st);
+  swift_stats s;
+  memset(&s, 0, sizeof(s));
+  CK(cudaEventRecord(ctx->ev[0], st));
+  SeedOut so;
+  int rc = run_seed(ctx, idx, rd, p->max_hits, sc, &so);
+  if (rc != SWIFT_OK) return rc;
+  CK(cudaEventRecord(ctx->ev[1], st));
+  const int64_t nm = so.n;
+  const int64_t dev_mem = p->device_mem > 0 ? p->device_mem : ctx->total_mem;
+  const int64_t per_iter = phase2_batch(dev_mem, Q, nm);
+  const int n_iter = phase2_iterations(nm, per_iter);
+  int64_t nproc = 0;
+  if (n_iter > 0) {
+    const int64_t maxs = (int64_t)n_iter * per_iter;
+    const int64_t last = nm < maxs ? nm - (int64_t)(n_iter - 1) * per_iter : per_iter;
+    nproc = (int64_t)(n_iter - 1) * per_iter + last;
+  }
+  const int Qs = (Q + 16) & ~15;
+  const int64_t cs = (int64_t)Q + kWin + 2;
+  const size_t nn = (size_t)std::max<int64_t>(nproc, 1);
+  DevPair* pairs;
+  char *qbuf, *wbuf, *qcons, *rcons;
+  DevAln* aln;
+  int32_t* keep;
+  uint64_t *bytes, *offs, *tot_d;
+  void* tmp;
+  CK(sc.get(&pairs, nn));
+  CK(sc.get(&qbuf, nn * Qs));
+  CK(sc.get(&wbuf, nn * kWinPad));
+  CK(sc.get(&aln, nn));
+  CK(sc.get(&qcons, nn * cs));
+  CK(sc.get(&rcons, nn * cs));
+  CK(sc.get(&keep, nn));
+  CK(sc.get(&bytes, nn));
+  CK(sc.get(&offs, nn));
+  CK(sc.get(&tot_d, 1));
+  CK(sc.get((uint8_t**)&tmp, scan_temp_bytes(nproc)));
+  PairArgs pa;
+  memset(&pa, 0, sizeof(pa));
+  pa.ref_file = idx->d_file;
+  pa.ref_file_len = idx->file_len;
+  pa.recs = idx->d_recs;
+  pa.reads = rd->d_bytes;
+  pa.rd = rd->d_rd;
+  pa.m_read = so.m_read;
+  pa.m_strand = so.m_strand;
+  pa.m_ri = so.m_ri;
+  pa.m_rp = so.m_rp;
+  pa.n = nproc;
+  pa.Q = Q;
+  pa.pairs = pairs;
+  pa.qbuf = qbuf;
+  pa.wbuf = wbuf;
+  pa.Qs = Qs;
+  launch_build_pairs(st, pa);
+  CKLAUNCH();
+  CK(cudaEventRecord(ctx->ev[2], st));
+  SwArgs sa;
+  memset(&sa, 0, sizeof(sa));
+  sa.q = qbuf;
+  sa.w = wbuf;
+  sa.q_stride = Qs;
+  sa.w_stride = kWinPad;
+  sa.Q = Q;
+  sa.R = kWin;
+  sa.match = p->match;
+  sa.mismatch = p->mismatch;
+  sa.gap_open = p->gap_open;
+  sa.gap_ext = p->gap_ext;
+  sa.n = nproc;
+  sa.aln = aln;
+  sa.qcons = qcons;
+  sa.rcons = rcons;
+  sa.cons_stride = cs;
+  rc = launch_sw(st, sa, &ctx->err);
+  if (rc != SWIFT_OK) return rc;
+  CKLAUNCH();
+  CK(cudaEventRecord(ctx->ev[3], st));
+  FormatArgs fa;
+  memset(&fa, 0, sizeof(fa));
+  fa.reads = rd->d_bytes;
+  fa.rd = rd->d_rd;
+  fa.recs = idx->d_recs;
+  fa.pairs = pairs;
+  fa.aln = aln;
+  fa.qcons = qcons;
+  fa.rcons = rcons;
+  fa.cons_stride = cs;
+  fa.n = nproc;
+  fa.batch = per_iter > 0 ? per_iter : 1;
+  fa.keep = keep;
+  fa.bytes = bytes;
+  fa.offs = offs;
+  launch_select(st, fa);
+  CKLAUNCH();
+  CK(cudaEventRecord(ctx->ev[4], st));
+  launch_format_sizes(st, fa);
+  CKLAUNCH();
+  int scan_k = exclusive_scan_u64(st, bytes, offs, nproc, tmp, tot_d);
+  CKLAUNCH();
+  uint64_t total = 0;
+  CK(cudaMemcpyAsync(&total, tot_d, 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (total + 1 > ctx->text_cap) {
+    if (ctx->d_text) cudaFree(ctx->d_text);
+    ctx->d_text = nullptr;
+    size_t cap = (size_t)(total * 1.25) + 4096;
+    CK(cudaMalloc(&ctx->d_text, cap));
+    ctx->text_cap = cap;
+  }
+  fa.text = ctx->d_text;
+  launch_format_write(st, fa);
+  CKLAUNCH();
+  CK(cudaEventRecord(ctx->ev[5], st));
+  CK(cudaEventSynchronize(ctx->ev[5]));
+  ctx->text_len = total;
+  if (out_len) *out_len = total;
+  if (stats) {
+    float t;
+    cudaEventElapsedTime(&t, ctx->ev[0], ctx->ev[1]);
+    s.seed_ms = t;
+    cudaEventElapsedTime(&t, ctx->ev[1], ctx->ev[2]);
+    s.pairs_ms = t;
+    cudaEventElapsedTime(&t, ctx->ev[2], ctx->ev[3]);
+    s.sw_ms = t;
+    cudaEventElapsedTime(&t, ctx->ev[3], ctx->ev[4]);
+    s.select_ms = t;
+    cudaEventElapsedTime(&t, ctx->ev[4], ctx->ev[5]);
+    s.format_ms = t;
+    cudaEventElapsedTime(&t, ctx->ev[0], ctx->ev[5]);
+    s.total_ms = t;
+    s.reads = (int64_t)rd->h.len.size();
+    s.records = nm;
+    s.cells = nproc * (int64_t)Q * kWin;
+    s.out_bytes = (int64_t)total;
+    s.seed_overflow_strands = so.overflow;
+    s.printed = 0;
+    // build_pairs, sw, select, format sizes, scan, format write
+    s.launches = so.launches + (nproc > 0 ? 5 : 0) + scan_k;
+    *stats = s;
+  }
+  return SWIFT_OK;
+}
+
+int swift_fetch_output(swift_ctx* ctx, char* dst, size_t cap) {
+  if (!ctx || !dst) return fail(ctx, SWIFT_E_ARG, "null argument");
+  size_t n = std::min(cap, ctx->text_len);
+  if (n) CK(cudaMemcpy(dst, ctx->d_text, n, cudaMemcpyDeviceToHost));
+  return SWIFT_OK;
+}
+
+int swift_align(swift_ctx* ctx, const swift_index* idx, const char* reads, size_t len,
+                const swift_params* p, char** out, size_t* out_len, swift_stats* stats) {
+  if (!ctx || !idx || !reads || !p || !out || !out_len) return fail(ctx, SWIFT_E_ARG, "null argument");
+  CK(cudaSetDevice(ctx->device));
+  swift_reads* rd = nullptr;
+  int rc = upload_reads(ctx, reads, len, &rd);
+  if (rc != SWIFT_OK) return rc;
+  size_t n = 0;
+  rc = swift_align_resident(ctx, idx, rd, p, &n, stats);
+  if (rc == SWIFT_OK) {
+    char* h = (char*)malloc(n + 1);
+    if (!h) {
+      rc = fail(ctx, SWIFT_E_NOMEM, "host output buffer");
+    } else {
+      cudaError_t e = n ? cudaMemcpy(h, ctx->d_text, n, cudaMemcpyDeviceToHost) : cudaSuccess;
+      if (e != cudaSuccess) {
+        free(h);
+        rc = fail(ctx, SWIFT_E_CUDA, cudaGetErrorString(e));
+      } else {
+        h[n] = '\0';
+        *out = h;
+        *out_len = n;
+      }
+    }
+  }
+  swift_reads_destroy(rd);
+  return rc;
+}
+
+static int read_file(const char* path, std::vector<char>* buf, std::string* err) {
+  FILE* f = fopen(path, "rb");
+  if (!f) {
+    *err = std::string("cannot open ") + path;
+    return SWIFT_E_ARG;
+  }
+  fseek(f, 0, SEEK_END);
+  long n = ftell(f);
+  fseek(f, 0, SEEK_SET);
+  buf->resize((size_t)std::max(n, 0L));
+  size_t got = n > 0 ? fread(buf->data(), 1, (size_t)n, f) : 0;
+  fclose(f);
+  if ((long)got != n) {
+    *err = std::string("short read of ") + path;
+    return SWIFT_E_ARG;
+  }
+  return SWIFT_OK;
+}
+
+int swift_align_files(swift_ctx* ctx, const char* qry_path, const char* ref_path,
+                      const char* out_path, const swift_params* p) {
+  if (!ctx || !qry_path || !ref_path || !out_path || !p) return fail(ctx, SWIFT_E_ARG, "null argument");
+  std::vector<char> ref, qry;
+  int rc = read_file(ref_path, &ref, &ctx->err);
+  if (rc == SWIFT_OK) rc = read_file(qry_path, &qry, &ctx->err);
+  if (rc != SWIFT_OK) return rc;
+  swift_index* idx = nullptr;
+  rc = swift_index_build(ctx, ref.data(), ref.size(), p->seed_len, p->ignore_thres, &idx);
+  if (rc != SWIFT_OK) return rc;
+  char* out = nullptr;
+  size_t n = 0;
+  rc = swift_align(ctx, idx, qry.data(), qry.size(), p, &out, &n, nullptr);
+  swift_index_destroy(idx);
+  if (rc != SWIFT_OK) return rc;
+  FILE* f = fopen(out_path, "wb");
+  if (!f) {
+    free(out);
+    return fail(ctx, SWIFT_E_ARG, std::string("cannot write ") + out_path);
+  }
+  size_t w = fwrite(out, 1, n, f);
+  fclose(f);
+  free(out);
+  if (w != n) return fail(ctx, SWIFT_E_ARG, std::string("short write to ") + out_path);
+  return SWIFT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,235 @@
+// Host-side structural parse of the two FASTA inputs, with the reference's
+// reading rules:
+//   reference: refMapCreate (src/refMap.cu:59-117) for name/sequence offsets
+//              and bases-per-line; lookupTable5Create (src/lookupTable5.cu:
+//              127-187) for the concatenated sequence its tuples come from;
+//   reads:     qryGetNext2 (src/query.cu:174-213), getSeqCount and
+//              getSeqSize (src/input.cu:475-524).
+// The parse only records offsets; sequence bytes stay where they are and are
+// copied to the device as one block.
+#include <string.h>
+
+#include <cmath>
+
+#include "internal.h"
+
+namespace swift {
+
+namespace {
+
+// Length of the chunk fgets(buf, MAX_LINE_LENGTH, f) returns at pos.
+inline size_t chunk_at(const char* b, size_t n, size_t pos) {
+  if (pos >= n) return 0;
+  size_t lim = n - pos;
+  if (lim > (size_t)kLineMax - 1) lim = (size_t)kLineMax - 1;
+  const void* nl = memchr(b + pos, '\n', lim);
+  return nl ? (size_t)((const char*)nl - (b + pos)) + 1 : lim;
+}
+
+// Rejects NUL bytes, bytes >= 128 and '>' anywhere but at a line start:
+// the reference reads lines with strlen and indexes a 128-entry table with
+// each byte, and treats any chunk starting with '>' as a header.
+bool bytes_ok(const char* s, size_t len, bool header, std::string* err,
+              const char* what, size_t off) {
+  const unsigned char* u = (const unsigned char*)s;
+  size_t i = 0;
+  uint64_t acc_hi = 0;
+  for (; i + 8 <= len; i += 8) {
+    uint64_t w;
+    memcpy(&w, u + i, 8);
+    uint64_t zero = (w - 0x0101010101010101ull) & ~w & 0x8080808080808080ull;
+    acc_hi |= (w & 0x8080808080808080ull) | zero;
+  }
+  for (; i < len; ++i) acc_hi |= (u[i] & 0x80) | (u[i] == 0 ? 0x80 : 0);
+  if (acc_hi) {
+    *err = std::string(what) + ": byte outside 7-bit text in the line at offset " +
+           std::to_string(off);
+    return false;
+  }
+  const void* gt = len > 1 ? memchr(s + 1, '>', len - 1) : nullptr;
+  if (gt || (!header && len && s[0] == '>')) {
+    *err = std::string(what) + ": '>' inside a line at offset " + std::to_string(off);
+    return false;
+  }
+  return true;
+}
+
+}  // namespace
+
+int parse_reference(const char* b, size_t n, HostRef* out, std::string* err) {
+  HostRef& r = *out;
+  r = HostRef();
+  long prev_ll = 0, old_ll = 0;
+  uint32_t pos_count = 0;
+  int num_lines = 0;
+  size_t pos = 0, c;
+  auto finish = [&](RefRecord& p) {
+    p.bpl = num_lines > 1 ? (uint32_t)(pos_count - (uint32_t)old_ll) / (uint32_t)(num_lines - 1)
+                          : 0u;
+  };
+  while ((c = chunk_at(b, n, pos)) > 0) {
+    long ll = (long)c - (b[pos + c - 1] == '\n');
+    if (prev_ll > 0) old_ll = prev_ll;
+    prev_ll = ll;
+    if (ll == 0) {
+      pos += c;
+      continue;
+    }
+    if (b[pos] == '>') {
+      if (!bytes_ok(b + pos, (size_t)ll, true, err, "reference", pos)) return SWIFT_E_INPUT;
+      if (!r.recs.empty()) finish(r.recs.back());
+      if ((int)r.recs.size() == kMaxRefs) {
+        *err = "reference: more than 127 sequences (the reference keeps the "
+               "sequence index in a char)";
+        return SWIFT_E_LIMIT;
+      }
+      if (ll - 1 >= kNameMax) {
+        *err = "reference: sequence name longer than 49 characters";
+        return SWIFT_E_LIMIT;
+      }
+      RefRecord q;
+      memset(&q, 0, sizeof(q));
+      q.name_off = pos + c - (size_t)ll - 1;
+      q.seq_off = pos + c;
+      q.name_len = (uint32_t)(ll - 1);
+      memcpy(q.name, b + pos + 1, (size_t)(ll - 1));
+      q.cat_start = r.cat_len;
+      r.recs.push_back(q);
+      pos_count = 0;
+      num_lines = 0;
+    } else {
+      if (r.recs.empty()) {
+        *err = "reference: sequence before the first header";
+        return SWIFT_E_INPUT;
+      }
+      if (!bytes_ok(b + pos, (size_t)ll, false, err, "reference", pos)) return SWIFT_E_INPUT;
+      ++num_lines;
+      pos_count += (uint32_t)ll;
+      r.line_src.push_back(pos);
+      r.line_dst.push_back(r.cat_len);
+      r.line_len.push_back((uint32_t)ll);
+      r.cat_len += (uint64_t)ll;
+      r.recs.back().cat_len += (uint64_t)ll;
+    }
+    pos += c;
+  }
+  if (prev_ll > 0) old_ll = prev_ll;
+  if (!r.recs.empty()) finish(r.recs.back());
+  if (r.recs.empty()) {
+    *err = "reference: no sequence header";
+    return SWIFT_E_INPUT;
+  }
+  return SWIFT_OK;
+}
+
+int parse_reads(const char* b, size_t n, HostReads* out, std::string* err) {
+  HostReads& rd = *out;
+  rd = HostReads();
+  size_t est = n / 64 + 16;
+  rd.name_off.reserve(est);
+  rd.seq_off.reserve(est);
+  rd.len.reserve(est);
+  rd.name_len.reserve(est);
+  size_t pos = 0, c;
+  bool have_header = false;
+  uint64_t cur_name_off = 0;
+  int32_t cur_name_len = 0;
+  int32_t mn = 1 << 30, mx = 0;
+  while ((c = chunk_at(b, n, pos)) > 0) {
+    const char* line = b + pos;
+    long ll = (long)c - (line[c - 1] == '\n');
+    if (ll == 0) {
+      *err = "reads: empty line at offset " + std::to_string(pos) +
+             " (the reference reader loops forever on it)";
+      return SWIFT_E_INPUT;
+    }
+    if (line[0] == '>') {
+      if (!bytes_ok(line, (size_t)ll, true, err, "reads", pos)) return SWIFT_E_INPUT;
+      if (have_header) {
+        *err = "reads: header without a sequence line at offset " + std::to_string(cur_name_off);
+        return SWIFT_E_INPUT;
+      }
+      if (ll - 1 > kNameMax - 2) {
+        *err = "reads: read name longer than 48 characters";
+        return SWIFT_E_LIMIT;
+      }
+      cur_name_off = pos + c - (size_t)ll - 1;
+      cur_name_len = (int32_t)(ll - 1);
+      have_header = true;
+      ++rd.n_gt;
+    } else {
+      if (!have_header) {
+        *err = "reads: sequence line without a header at offset " + std::to_string(pos) +
+               " (multi-line reads are not supported)";
+        return SWIFT_E_INPUT;
+      }
+      if (!bytes_ok(line, (size_t)ll, false, err, "reads", pos)) return SWIFT_E_INPUT;
+      if (ll > kReadMax) {
+        *err = "reads: read longer than 199 bases (the reference's query buffer)";
+        return SWIFT_E_LIMIT;
+      }
+      if (rd.len.empty()) rd.first_len = (int32_t)c - 1;  // strlen(line) - 1
+      rd.name_off.push_back(cur_name_off);
+      rd.seq_off.push_back(pos);
+      rd.len.push_back((int32_t)ll);
+      rd.name_len.push_back(cur_name_len);
+      if (ll < mn) mn = (int32_t)ll;
+      if (ll > mx) mx = (int32_t)ll;
+      have_header = false;
+    }
+    pos += c;
+  }
+  if (have_header) {
+    *err = "reads: trailing header without a sequence line";
+    return SWIFT_E_INPUT;
+  }
+  rd.min_len = rd.len.empty() ? 0 : mn;
+  rd.max_len = mx;
+  return SWIFT_OK;
+}
+
+std::vector<int32_t> phase1_stale_repeats(int64_t n_reads, int64_t n_gt) {
+  // searchQueries3 (src/search.cu:325-357) calls qryGetNext2 in batches of
+  // 16 while i < numQrs; a slot whose call finds the end of the file keeps
+  // (and re-maps) the read it last held.  With well-formed input the first
+  // n_reads calls return reads in order; the remaining calls of the last
+  // batch repeat the slot's previous read.
+  std::vector<int32_t> rep;
+  if (n_gt <= 0) return rep;
+  int64_t nb = (n_gt + kP1Slots - 1) / kP1Slots;
+  int64_t calls = nb * kP1Slots;
+  int32_t slot[kP1Slots];
+  for (int j = 0; j < kP1Slots; ++j) slot[j] = -1;
+  int64_t next = 0;
+  for (int64_t call = 0; call < calls; ++call) {
+    int j = (int)(call % kP1Slots);
+    if (next < n_reads) {
+      slot[j] = (int32_t)next++;
+    } else if (slot[j] >= 0) {
+      rep.push_back(slot[j]);
+    }
+  }
+  return rep;
+}
+
+int64_t phase2_batch(int64_t device_mem, int Q, int64_t nm) {
+  int64_t per_iter;
+  if (device_mem > 0) {
+    int mem_pair = (kWin + 1) + (Q + 1) + 4 + 4 + 4 + 2 + 2 * (kWin + Q + 2);
+    long gm = (long)(device_mem - 100000000LL);  // GLOBAL_MEM_MARGIN
+    per_iter = (int)std::floor((float)gm / mem_pair);
+    if (per_iter > 2147483647LL) per_iter = 2147483647LL;
+  } else {
+    per_iter = nm;
+  }
+  if (per_iter > nm) per_iter = nm;
+  if (per_iter >= 2 && per_iter % 2 == 1) --per_iter;
+  return per_iter;
+}
+
+int phase2_iterations(int64_t nm, int64_t per_iter) {
+  if (per_iter <= 0) return 0;
+  return (int)std::ceil((float)nm / (float)per_iter);
+}
+
+}  // namespace swift

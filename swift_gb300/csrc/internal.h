@@ -1,0 +1,210 @@
+// Internal declarations shared by the host and device translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/swift_gb300.h"
+
+namespace swift {
+
+// Limits of the reference's data layout (src/common.h:37-57).
+constexpr int kNameMax = 50;      // MAX_QRY_NAME_LENGTH / MAX_REF_NAME_LENGTH
+constexpr int kReadMax = 199;     // MAX_QRY_SEQ_LENGTH - 1
+constexpr int kWin = 300;         // REF_LENGTH
+constexpr int kWinPad = 304;      // window stride in device buffers
+constexpr int kShiftBases = 100;  // REF_LENGTH / 3 (src/align.cu:668)
+constexpr int kMaxRefs = 127;     // refIdx is a char in the reference
+constexpr int kLineMax = 100000;  // MAX_LINE_LENGTH (fgets chunking)
+constexpr int kP1Slots = 16;      // NUM_THREADS of searchQueries3
+constexpr int kMaxQ = 256;        // query rows supported by the SW kernels
+constexpr int kMaxR = 1024;       // window columns supported by the SW kernels
+
+// ---------------------------------------------------------------------------
+// host-side FASTA structure (host_parse.cpp)
+
+struct RefRecord {
+  uint64_t name_off;   // file offset of the header line ('>')
+  uint64_t seq_off;    // file offset just past the header line
+  uint32_t bpl;        // bases per line as refMapCreate computes it
+  uint32_t name_len;
+  uint64_t cat_start;  // start in the concatenated sequence
+  uint64_t cat_len;    // bases in the record
+  char name[kNameMax];
+};
+
+struct HostRef {
+  std::vector<RefRecord> recs;
+  // sequence lines: file offset, destination in the concatenation, length
+  std::vector<uint64_t> line_src, line_dst;
+  std::vector<uint32_t> line_len;
+  uint64_t cat_len = 0;
+};
+
+struct HostReads {
+  std::vector<uint64_t> name_off;  // offset of '>'
+  std::vector<uint64_t> seq_off;   // offset of the sequence line
+  std::vector<int32_t> len;        // read length
+  std::vector<int32_t> name_len;   // characters after '>'
+  int64_t n_gt = 0;                // '>' bytes in the file (getSeqCount)
+  int32_t first_len = 0;           // getSeqSize of the file
+  int32_t min_len = 0, max_len = 0;
+};
+
+int parse_reference(const char* b, size_t n, HostRef* out, std::string* err);
+int parse_reads(const char* b, size_t n, HostReads* out, std::string* err);
+
+// Phase-1 slot schedule of searchQueries3: read index per slot call, -1 for
+// a slot never filled.  Returns the list of reads whose records follow the
+// in-order ones (slots that re-ran a stale read after end of file).
+std::vector<int32_t> phase1_stale_repeats(int64_t n_reads, int64_t n_gt);
+
+// Phase-2 batch size of getNumQueriesPerIteration (src/align.cu:2767-2793).
+int64_t phase2_batch(int64_t device_mem, int Q, int64_t n_matches);
+int phase2_iterations(int64_t n_matches, int64_t per_iter);
+
+// ---------------------------------------------------------------------------
+// device-side layouts
+
+struct DevRecord {        // per reference sequence
+  uint64_t seq_off;
+  uint64_t cat_start;
+  uint64_t cat_len;
+  uint32_t bpl;
+  uint32_t name_len;
+  char name[kNameMax];
+  char pad[6];
+};
+
+struct DevRead {          // per read
+  uint64_t name_off;      // offset of '>' in the reads buffer
+  uint64_t seq_off;
+  int32_t len;
+  int32_t name_len;
+};
+
+// One Phase-2 pair (one match record).
+struct DevPair {
+  int32_t read;
+  int32_t strand;
+  int32_t ref_idx;
+  int32_t ref_dist;       // max(0, refPos - 100)
+  int32_t win_len;        // window bases after N trimming
+  int32_t flags;          // bit 0: needs the generic SW kernel
+};
+
+// Result of one Smith-Waterman pair.
+struct DevAln {
+  int32_t score;
+  int32_t start, end, len;
+};
+
+// ---------------------------------------------------------------------------
+// kernels' host launchers (one per .cu file)
+
+// index.cu
+void launch_compact_lines(cudaStream_t st, const char* file, const uint64_t* src,
+                          const uint64_t* dst, const uint32_t* len, int64_t n_lines,
+                          uint8_t* cat);
+void launch_pack2bit(cudaStream_t st, const uint8_t* cat, int64_t n_words, uint32_t* packed);
+void launch_count_tuples(cudaStream_t st, const uint32_t* packed, const DevRecord* recs,
+                         const uint64_t* tbase, int n_recs, uint64_t n_tuples, int k,
+                         uint32_t* count);
+void launch_threshold(cudaStream_t st, const uint32_t* count, int64_t nb, uint32_t thres,
+                      uint32_t* eff);
+void launch_scatter_tuples(cudaStream_t st, const uint32_t* packed, const DevRecord* recs,
+                           const uint64_t* tbase, int n_recs, uint64_t n_tuples, int k,
+                           uint32_t thres, const uint32_t* count, const uint32_t* offsets,
+                           uint32_t* cursor, uint2* post);
+void launch_order_buckets(cudaStream_t st, const uint32_t* offsets, int64_t nb, uint2* post);
+
+// scan.cu
+size_t scan_temp_bytes(int64_t n);
+// Each returns the number of kernels it launched.
+int exclusive_scan_u32(cudaStream_t st, const uint32_t* in, uint32_t* out, int64_t n,
+                       void* temp, uint32_t* total_dev);
+int exclusive_scan_u64(cudaStream_t st, const uint64_t* in, uint64_t* out, int64_t n,
+                       void* temp, uint64_t* total_dev);
+
+// seed.cu
+struct SeedArgs {
+  const char* reads;          // reads file bytes
+  const DevRead* rd;
+  int64_t n_reads;
+  const uint32_t* offsets;    // bucket starts, 4^k + 1 entries
+  const uint2* postings;      // (ref_pos, ref_idx)
+  int k;
+  int max_hits;
+  int3* best;                 // per strand: max_hits x (ri, shift, rp)
+  int32_t* nbest;             // per strand
+  int32_t* overflow_list;     // strands too big for the on-chip path
+  int32_t* n_overflow;
+  uint64_t* scratch;          // overflow path: per-strand hash tables
+};
+void launch_seed(cudaStream_t st, const SeedArgs& a);
+void launch_seed_overflow(cudaStream_t st, const SeedArgs& a, int n_overflow,
+                          const uint64_t* tab_off, const uint32_t* tab_size);
+int seed_smem_cap();
+
+// pairs.cu
+struct PairArgs {
+  const char* ref_file;
+  uint64_t ref_file_len;
+  const DevRecord* recs;
+  const char* reads;
+  const DevRead* rd;
+  const int32_t* m_read;      // per record: read, strand, ref idx, ref pos
+  const int32_t* m_strand;
+  const int32_t* m_ri;
+  const int32_t* m_rp;
+  int64_t n;
+  int Q;
+  DevPair* pairs;
+  char* qbuf;                 // n x Qs
+  char* wbuf;                 // n x kWinPad
+  int Qs;                     // query stride
+};
+void launch_build_pairs(cudaStream_t st, const PairArgs& a);
+
+// sw.cu
+struct SwArgs {
+  const char* q;              // query i at q + i*q_stride
+  const char* w;              // window i at w + i*w_stride
+  int64_t q_stride, w_stride;
+  int Q, R;
+  int match, mismatch, gap_open, gap_ext;
+  int64_t n;
+  DevAln* aln;
+  char* qcons;                // reversed consensus strings, stride cons_stride
+  char* rcons;
+  int64_t cons_stride;
+  int32_t* err;
+};
+int launch_sw(cudaStream_t st, const SwArgs& a, std::string* err);
+int measure_dpx_peak(cudaStream_t st, int device, double* lane_instr_per_s);
+
+// out.cu
+struct FormatArgs {
+  const char* reads;
+  const DevRead* rd;
+  const DevRecord* recs;
+  const DevPair* pairs;
+  const DevAln* aln;
+  const char* qcons;
+  const char* rcons;
+  int64_t cons_stride;
+  int64_t n;
+  int64_t batch;              // Phase-2 batch size (best-per-read groups stop at batch ends)
+  int32_t* keep;              // per record: 1 if printed
+  uint64_t* bytes;            // per record: text bytes
+  uint64_t* offs;             // per record: text offset
+  char* text;
+};
+void launch_select(cudaStream_t st, const FormatArgs& a);
+void launch_format_sizes(cudaStream_t st, const FormatArgs& a);
+void launch_format_write(cudaStream_t st, const FormatArgs& a);
+
+}  // namespace swift

@@ -1,0 +1,204 @@
+// Best alignment per read and the default text record, on the device.
+//
+// Selection restates chooseBestAlignment (src/align.cu:844-905) with the
+// tie pinned to the first maximum: within one Phase-2 batch, consecutive
+// records whose query names compare equal under qryNameCmp
+// (src/align.cu:1501-1519: equal, or equal but for one trailing '*') form a
+// group; the group keeps its first record with the maximum score (maximum
+// starting from 0.0 with strict comparison) and drops the others.
+//
+// Formatting restates printOutput (src/output.cu:154-201):
+//   "\n****************************************\n"
+//   "Qry: %s | Ref: %s | Score: %.1f | AlignStart: %d | AlignEnd: %d | "
+//   "AlignLength: %d\n"
+//   "R: " reversed ref consensus "\n"
+//   "   " match line ('|' equal ignoring case or an 'N', '-' gap, '.') "\n"
+//   "Q: " reversed query consensus "\n"
+// Scores are integers, so "%.1f" prints them with ".0".  A size pass and an
+// exclusive scan give every record its output offset; a warp per record then
+// writes its text.
+#include "internal.h"
+
+namespace swift {
+namespace {
+
+
+// Query name of record j: the read's header text, plus '*' for strand 1.
+__device__ __forceinline__ int qname_len(const FormatArgs& a, const DevPair& p) {
+  return a.rd[p.read].name_len + (p.strand ? 1 : 0);
+}
+__device__ __forceinline__ char qname_at(const FormatArgs& a, const DevPair& p, int i) {
+  const DevRead& r = a.rd[p.read];
+  if (i < r.name_len) return a.reads[r.name_off + 1 + i];
+  if (p.strand && i == r.name_len) return '*';
+  return '\0';
+}
+
+__device__ bool names_equal(const FormatArgs& a, const DevPair& s, const DevPair& t) {
+  // qryNameCmp over the 50-byte name slots
+  int i;
+  for (i = 0; i < kNameMax; ++i) {
+    char cs = qname_at(a, s, i), ct = qname_at(a, t, i);
+    if (cs == '\0' && ct == '\0') return true;
+    if (cs == '\0' || ct == '\0') break;
+    if (cs != ct) return false;
+  }
+  if (i >= kNameMax) return false;
+  char s0 = qname_at(a, s, i), s1 = qname_at(a, s, i + 1);
+  char t0 = qname_at(a, t, i), t1 = qname_at(a, t, i + 1);
+  return (s0 == '*' && s1 == '\0') || (t0 == '*' && t1 == '\0');
+}
+
+__global__ void select_kernel(FormatArgs a) {
+  int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= a.n) return;
+  const int64_t bstart = (j / a.batch) * a.batch;
+  const int64_t bend = min(bstart + a.batch, a.n);
+  if (j != bstart && names_equal(a, a.pairs[j], a.pairs[j - 1])) return;  // not a group start
+  int64_t e = j;
+  while (e + 1 < bend && names_equal(a, a.pairs[e + 1], a.pairs[e])) ++e;
+  int mx = 0;
+  for (int64_t i = j; i <= e; ++i) mx = max(mx, a.aln[i].score);
+  int64_t keep = -1;
+  for (int64_t i = j; i <= e; ++i)
+    if (a.aln[i].score == mx) {
+      keep = i;
+      break;
+    }
+  for (int64_t i = j; i <= e; ++i) a.keep[i] = i == keep ? 1 : 0;
+}
+
+__device__ __forceinline__ int ndigits(int v) {
+  unsigned u = v < 0 ? (unsigned)(-(int64_t)v) : (unsigned)v;
+  int n = 1;
+  while (u >= 10) {
+    u /= 10;
+    ++n;
+  }
+  return n + (v < 0 ? 1 : 0);
+}
+
+__device__ __forceinline__ char* put_int(char* o, int v) {
+  char buf[12];
+  int n = 0;
+  unsigned u = v < 0 ? (unsigned)(-(int64_t)v) : (unsigned)v;
+  do {
+    buf[n++] = (char)('0' + u % 10);
+    u /= 10;
+  } while (u);
+  if (v < 0) *o++ = '-';
+  while (n) *o++ = buf[--n];
+  return o;
+}
+
+__device__ __forceinline__ char* put_str(char* o, const char* s) {
+  while (*s) *o++ = *s++;
+  return o;
+}
+
+constexpr int kLitQry = 5;            // "Qry: "
+constexpr int kLitRef = 8;            // " | Ref: "
+constexpr int kLitScore = 10;         // " | Score: "
+constexpr int kLitStart = 15;         // " | AlignStart: "
+constexpr int kLitEnd = 13;           // " | AlignEnd: "
+constexpr int kLitLen = 16;           // " | AlignLength: "
+
+__device__ uint64_t record_bytes(const FormatArgs& a, int64_t j) {
+  const DevPair p = a.pairs[j];
+  const DevAln al = a.aln[j];
+  const int dist = p.ref_dist;
+  uint64_t n = 42;
+  n += kLitQry + qname_len(a, p) + kLitRef + a.recs[p.ref_idx].name_len;
+  n += kLitScore + ndigits(al.score) + 2;
+  n += kLitStart + ndigits(al.start + dist) + kLitEnd + ndigits(al.end + dist);
+  n += kLitLen + ndigits(al.len) + 1;
+  const uint64_t L = al.len > 0 ? (uint64_t)al.len : 0;
+  n += 3 * (3 + L + 1);
+  return n;
+}
+
+__global__ void format_sizes_kernel(FormatArgs a) {
+  int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= a.n) return;
+  a.bytes[j] = a.keep[j] ? record_bytes(a, j) : 0;
+}
+
+constexpr int kFmtWarps = 8;
+
+__global__ void __launch_bounds__(kFmtWarps * 32) format_write_kernel(FormatArgs a) {
+  __shared__ char hdr_all[kFmtWarps][320];  // header line: at most 257 bytes
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t j = (int64_t)blockIdx.x * kFmtWarps + wib;
+  if (j >= a.n || !a.keep[j]) return;
+  const DevPair p = a.pairs[j];
+  const DevAln al = a.aln[j];
+  char* hdr = hdr_all[wib];
+  int hn = 0;
+  if (lane == 0) {
+    char* o = put_str(hdr, "\n****************************************\n");  // 42 bytes
+    o = put_str(o, "Qry: ");
+    const int ql = qname_len(a, p);
+    for (int i = 0; i < ql; ++i) *o++ = qname_at(a, p, i);
+    o = put_str(o, " | Ref: ");
+    const DevRecord& rec = a.recs[p.ref_idx];
+    for (uint32_t i = 0; i < rec.name_len; ++i) *o++ = rec.name[i];
+    o = put_str(o, " | Score: ");
+    o = put_int(o, al.score);
+    o = put_str(o, ".0 | AlignStart: ");
+    o = put_int(o, al.start + p.ref_dist);
+    o = put_str(o, " | AlignEnd: ");
+    o = put_int(o, al.end + p.ref_dist);
+    o = put_str(o, " | AlignLength: ");
+    o = put_int(o, al.len);
+    o = put_str(o, "\nR: ");
+    hn = (int)(o - hdr);
+  }
+  hn = __shfl_sync(0xffffffffu, hn, 0);
+  __syncwarp();
+  char* out = a.text + a.offs[j];
+  for (int i = lane; i < hn; i += 32) out[i] = hdr[i];
+  out += hn;
+  const int L = al.len > 0 ? al.len : 0;
+  const char* rc = a.rcons + j * a.cons_stride;
+  const char* qc = a.qcons + j * a.cons_stride;
+  // "R: " already written; reversed strings
+  for (int z = lane; z < L; z += 32) {
+    const char r = rc[L - 1 - z], q = qc[L - 1 - z];
+    out[z] = r;
+    const int ur = (unsigned)(r - 'a') < 26u ? r - 32 : r;
+    const int uq = (unsigned)(q - 'a') < 26u ? q - 32 : q;
+    const char m = (ur == uq || r == 'N' || q == 'N') ? '|' : (r == '-' || q == '-') ? '-' : '.';
+    out[L + 4 + z] = m;
+    out[2 * L + 8 + z] = q;
+  }
+  if (lane == 0) {
+    out[L] = '\n';
+    out[L + 1] = ' ';
+    out[L + 2] = ' ';
+    out[L + 3] = ' ';
+    out[2 * L + 4] = '\n';
+    out[2 * L + 5] = 'Q';
+    out[2 * L + 6] = ':';
+    out[2 * L + 7] = ' ';
+    out[3 * L + 8] = '\n';
+  }
+}
+
+}  // namespace
+
+void launch_select(cudaStream_t st, const FormatArgs& a) {
+  if (a.n <= 0) return;
+  select_kernel<<<(unsigned)((a.n + 255) / 256), 256, 0, st>>>(a);
+}
+
+void launch_format_sizes(cudaStream_t st, const FormatArgs& a) {
+  if (a.n <= 0) return;
+  format_sizes_kernel<<<(unsigned)((a.n + 255) / 256), 256, 0, st>>>(a);
+}
+
+void launch_format_write(cudaStream_t st, const FormatArgs& a) {
+  if (a.n <= 0) return;
+  format_write_kernel<<<(unsigned)((a.n + kFmtWarps - 1) / kFmtWarps), kFmtWarps * 32, 0, st>>>(a);
+}
+
+}  // namespace swift

@@ -1,0 +1,127 @@
+// Phase-2 pair construction on the device, one warp per match record.
+// Restates the per-record part of alignQueries3 (src/align.cu:693-728):
+//   refDistance = max(0, refPos - 100)
+//   file offset = seqOffset[refIdx] + refDistance + refDistance / basesPerLine
+//                 (refMapGetOffsets, src/refMap.cu:148-155, 32-bit unsigned)
+//   window      = getRefSeq2 (src/input.cu:348-403): up to 300 characters
+//                 from that offset, newlines skipped, stopping at a header
+//                 line or end of file, then leading / trailing N trimmed
+//                 with the reference's pointer arithmetic, NUL padded
+//   query       = the first Q characters of the read (getSeq2,
+//                 src/input.cu:216-258); for strand 1 the reverse complement
+//                 of those Q characters (qryGetReverseComplement).
+// The window bytes are compacted with ballots: each step the warp reads 32
+// file bytes, drops newlines and appends the rest.
+#include "internal.h"
+
+namespace swift {
+namespace {
+
+constexpr int kPairWarps = 8;
+
+__device__ __forceinline__ char comp_char(char c) {
+  return c == 'A' ? 'T' : c == 'C' ? 'G' : c == 'G' ? 'C' : 'A';
+}
+
+__global__ void __launch_bounds__(kPairWarps * 32) build_pairs_kernel(PairArgs a) {
+  __shared__ char tmp_all[kPairWarps][kWinPad + 32];
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t j = (int64_t)blockIdx.x * kPairWarps + wib;
+  if (j >= a.n) return;
+  char* tmp = tmp_all[wib];
+  const int32_t read = a.m_read[j], strand = a.m_strand[j], ri = a.m_ri[j], rp = a.m_rp[j];
+  const int32_t dist = rp - kShiftBases > 0 ? rp - kShiftBases : 0;
+  const DevRecord& rec = a.recs[ri];
+  const uint32_t off = (uint32_t)rec.seq_off + (uint32_t)dist +
+                       (rec.bpl > 0 ? (uint32_t)dist / rec.bpl : 0u);
+  // fetch up to 300 window characters
+  int got = 0;
+  uint64_t pos = off;
+  while (got < kWin) {
+    uint64_t p = pos + (uint64_t)lane;
+    char c = p < a.ref_file_len ? a.ref_file[p] : '\0';
+    bool eof = p >= a.ref_file_len;
+    bool stop = eof || c == '>';
+    uint32_t stop_bal = __ballot_sync(0xffffffffu, stop);
+    int first_stop = stop_bal ? __ffs(stop_bal) - 1 : 32;
+    bool keep = lane < first_stop && c != '\n';
+    uint32_t keep_bal = __ballot_sync(0xffffffffu, keep);
+    int rank = __popc(keep_bal & ((1u << lane) - 1));
+    if (keep && got + rank < kWin) tmp[got + rank] = c;
+    got += __popc(keep_bal);
+    if (got > kWin) got = kWin;
+    if (first_stop < 32) break;
+    pos += 32;
+  }
+  __syncwarp();
+  // N trimming (see the restatement notes at the top of this file)
+  int lead = 0;
+  {
+    bool isn = false;
+    for (int base = 0; base < got; base += 32) {
+      int i = base + lane;
+      isn = i < got && (tmp[i] == 'N' || tmp[i] == 'n');
+      uint32_t notn = __ballot_sync(0xffffffffu, !isn && i < got);
+      if (notn) {
+        lead = base + __ffs(notn) - 1;
+        break;
+      }
+      lead = base + 32 < got ? base + 32 : got;
+    }
+  }
+  int len = got;
+  if (lead == 0 && got > 0) {
+    for (int base = ((got - 1) / 32) * 32; base >= 0; base -= 32) {
+      int i = base + lane;
+      bool notn = i < got && !(tmp[i] == 'N' || tmp[i] == 'n');
+      uint32_t b = __ballot_sync(0xffffffffu, notn);
+      if (b) {
+        len = base + 31 - __clz(b) + 1;
+        break;
+      }
+      len = base;
+    }
+  }
+  int wl = len - lead;
+  if (wl < 0) wl = 0;
+  char* wout = a.wbuf + j * kWinPad;
+  for (int i = lane; i < kWinPad; i += 32) wout[i] = i < wl ? tmp[lead + i] : '\0';
+  // query
+  const DevRead rd = a.rd[read];
+  const char* s = a.reads + rd.seq_off;
+  const int Q = a.Q;
+  const int avail = rd.len < Q ? rd.len : Q;
+  char* qout = a.qbuf + j * (int64_t)a.Qs;
+  for (int i = lane; i < a.Qs; i += 32) {
+    char c = '\0';
+    if (i < Q) {
+      if (strand == 0) {
+        c = i < avail ? s[i] : '\0';
+      } else {
+        int src = Q - 1 - i;
+        c = comp_char(src < avail ? s[src] : '\0');
+      }
+    }
+    qout[i] = c;
+  }
+  if (lane == 0) {
+    DevPair pr;
+    pr.read = read;
+    pr.strand = strand;
+    pr.ref_idx = ri;
+    pr.ref_dist = dist;
+    pr.win_len = wl;
+    pr.flags = 0;
+    a.pairs[j] = pr;
+  }
+}
+
+}  // namespace
+
+void launch_build_pairs(cudaStream_t st, const PairArgs& a) {
+  if (a.n <= 0) return;
+  unsigned grid = (unsigned)((a.n + kPairWarps - 1) / kPairWarps);
+  build_pairs_kernel<<<grid, kPairWarps * 32, 0, st>>>(a);
+}
+
+}  // namespace swift

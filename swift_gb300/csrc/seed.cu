@@ -1,0 +1,304 @@
+// Phase 1 on the device: SSAHA hit emission and best-cluster selection for
+// every read strand.  Restates lookupTable5MapQry (src/lookupTable5.cu:
+// 557-603) and mapHits6GetBestHits (src/mapHits6.cu:40-318):
+//   hits  = { (refIdx, refPos - i, refPos) : query offset i, posting of the
+//             hash of query[i, i+k) }
+//   sort by (refIdx, shift, refPos), clusters = runs of equal
+//   (refIdx, shift), keep the first max_hits clusters of the biggest size and
+//   report each cluster's first hit.
+// The sort order is total (equal refIdx, refPos and shift imply equal i), so
+// any exact sort reproduces the reference; ties between clusters of the same
+// size keep the first ones in sort order.
+//
+// On-chip path: one warp per strand.  The warp hashes the strand's k-mers,
+// counts postings with a warp scan, writes 64-bit keys
+//   key = refIdx << 40 | (shift + 256) << 8 | i
+// into shared memory, sorts them (bitonic), and finds run lengths with
+// ballots.  Strands with more hits than fit on chip go to a per-strand hash
+// table in global scratch (one CTA each).
+#include "internal.h"
+
+namespace swift {
+namespace {
+
+constexpr int kSeedWarps = 8;          // warps per block, on-chip path
+constexpr int kShiftBias = 256;        // shift >= -(199 - 1) always
+
+__device__ __forceinline__ uint8_t fwd_code(uint8_t c) {
+  uint32_t u = c & 0xDFu;
+  return u == 'C' ? 1 : u == 'G' ? 2 : u == 'T' ? 3 : 0;
+}
+// code of qryGetReverseComplement's output character for input c:
+// A->T(3), C->G(2), G->C(1), anything else -> A(0) (case-sensitive)
+__device__ __forceinline__ uint8_t rev_code(uint8_t c) {
+  return c == 'A' ? 3 : c == 'C' ? 2 : c == 'G' ? 1 : 0;
+}
+
+__device__ __forceinline__ uint64_t make_key(uint32_t ri, int32_t shift, int32_t i) {
+  return ((uint64_t)ri << 40) | ((uint64_t)(uint32_t)(shift + kShiftBias) << 8) | (uint32_t)i;
+}
+
+// Loads the strand's 2-bit codes into smem codes[0..L).
+__device__ __forceinline__ void load_codes(const char* __restrict__ s, int L, int strand,
+                                           uint8_t* codes, int lane) {
+  for (int i = lane; i < L; i += 32) {
+    codes[i] = strand == 0 ? fwd_code((uint8_t)s[i]) : rev_code((uint8_t)s[L - 1 - i]);
+  }
+}
+
+__device__ __forceinline__ uint32_t hash_at(const uint8_t* codes, int i, int k) {
+  uint32_t h = 0;
+  for (int t = k - 1; t >= 0; --t) h = (h << 2) | codes[i + t];
+  return h;
+}
+
+template <int CAP>
+__global__ void __launch_bounds__(kSeedWarps * 32) seed_warp_kernel(SeedArgs a) {
+  __shared__ uint64_t keys_all[kSeedWarps][CAP];
+  __shared__ uint16_t runlen_all[kSeedWarps][CAP];
+  __shared__ uint8_t codes_all[kSeedWarps][kReadMax + 1];
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t sid = (int64_t)blockIdx.x * kSeedWarps + wib;
+  if (sid >= 2 * a.n_reads) return;
+  const int64_t read = sid >> 1;
+  const int strand = (int)(sid & 1);
+  uint64_t* keys = keys_all[wib];
+  uint16_t* runlen = runlen_all[wib];
+  uint8_t* codes = codes_all[wib];
+  const DevRead rd = a.rd[read];
+  const int L = rd.len, k = a.k;
+  const int nq = L - k + 1;
+  if (nq <= 0) {
+    if (lane == 0) a.nbest[sid] = 0;
+    return;
+  }
+  load_codes(a.reads + rd.seq_off, L, strand, codes, lane);
+  __syncwarp();
+  // offsets i = lane + 32 m, m < 7 (199 bases at most)
+  constexpr int kM = (kReadMax + 31) / 32;
+  uint32_t beg[kM], cnt[kM];
+  uint32_t my = 0;
+#pragma unroll
+  for (int m = 0; m < kM; ++m) {
+    int i = lane + 32 * m;
+    beg[m] = cnt[m] = 0;
+    if (i < nq) {
+      uint32_t h = hash_at(codes, i, k);
+      uint32_t b = __ldg(&a.offsets[h]), e = __ldg(&a.offsets[h + 1]);
+      beg[m] = b;
+      cnt[m] = e - b;
+      my += e - b;
+    }
+  }
+  uint32_t incl = my;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    uint32_t o = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= d) incl += o;
+  }
+  const uint32_t n = __shfl_sync(0xffffffffu, incl, 31);
+  if (n == 0) {
+    if (lane == 0) a.nbest[sid] = 0;
+    return;
+  }
+  if (n > (uint32_t)CAP) {
+    if (lane == 0) {
+      int slot = atomicAdd(a.n_overflow, 1);
+      a.overflow_list[slot] = (int32_t)sid;
+      a.nbest[sid] = -(int32_t)n;  // hit count, for sizing the overflow table
+    }
+    return;
+  }
+  uint32_t pos = incl - my;
+#pragma unroll
+  for (int m = 0; m < kM; ++m) {
+    int i = lane + 32 * m;
+    for (uint32_t j = 0; j < cnt[m]; ++j) {
+      uint2 p = __ldg(&a.postings[beg[m] + j]);
+      keys[pos++] = make_key(p.y, (int32_t)p.x - i, i);
+    }
+  }
+  uint32_t P = 32;
+  while (P < n) P <<= 1;
+  for (uint32_t i = n + lane; i < P; i += 32) keys[i] = ~0ull;
+  __syncwarp();
+  // bitonic sort of keys[0, P)
+  for (uint32_t size = 2; size <= P; size <<= 1) {
+    for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+      for (uint32_t t = lane; t < P / 2; t += 32) {
+        uint32_t i = 2 * stride * (t / stride) + (t % stride);
+        uint32_t j = i + stride;
+        bool asc = (i & size) == 0;
+        uint64_t x = keys[i], y = keys[j];
+        if ((x > y) == asc) {
+          keys[i] = y;
+          keys[j] = x;
+        }
+      }
+      __syncwarp();
+    }
+  }
+  // run lengths at run starts, scanning chunks back to front
+  const uint32_t nch = (n + 31) >> 5;
+  uint32_t next = n, biggest = 0;
+  for (int c = (int)nch - 1; c >= 0; --c) {
+    uint32_t idx = (uint32_t)c * 32 + lane;
+    bool start = false;
+    if (idx < n) start = idx == 0 || (keys[idx] >> 8) != (keys[idx - 1] >> 8);
+    uint32_t bal = __ballot_sync(0xffffffffu, start);
+    uint32_t above = lane < 31 ? (bal >> (lane + 1)) << (lane + 1) : 0u;
+    uint32_t nx = above ? (uint32_t)c * 32 + __ffs(above) - 1 : next;
+    if (start) {
+      uint32_t len = nx - idx;
+      runlen[idx] = (uint16_t)len;
+      biggest = max(biggest, len);
+    }
+    if (bal) next = (uint32_t)c * 32 + __ffs(bal) - 1;
+  }
+  __syncwarp();
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) biggest = max(biggest, __shfl_xor_sync(0xffffffffu, biggest, d));
+  // first max_hits runs of the biggest size
+  int got = 0;
+  int3* out = a.best + sid * a.max_hits;
+  for (uint32_t c = 0; c < nch && got < a.max_hits; ++c) {
+    uint32_t idx = c * 32 + lane;
+    bool hit = false;
+    if (idx < n) {
+      bool start = idx == 0 || (keys[idx] >> 8) != (keys[idx - 1] >> 8);
+      hit = start && runlen[idx] == biggest;
+    }
+    uint32_t bal = __ballot_sync(0xffffffffu, hit);
+    while (bal && got < a.max_hits) {
+      int b = __ffs(bal) - 1;
+      bal &= bal - 1;
+      if (lane == b) {
+        uint64_t key = keys[idx];
+        int32_t ri = (int32_t)(key >> 40);
+        int32_t shift = (int32_t)((key >> 8) & 0xffffffffu) - kShiftBias;
+        int32_t i = (int32_t)(key & 0xff);
+        out[got] = make_int3(ri, shift, shift + i);
+      }
+      ++got;
+    }
+  }
+  if (lane == 0) a.nbest[sid] = got;
+}
+
+// ---------------------------------------------------------------------------
+// Overflow path: one CTA per strand, open-addressing table over cluster keys
+// (refIdx, shift) with counts and the smallest query offset (kept as
+// 255 - offset under atomicMax so that the table starts all zero).
+
+constexpr int kOvThreads = 512;
+
+__device__ __forceinline__ uint32_t mix(uint64_t x) {
+  x ^= x >> 33;
+  x *= 0xff51afd7ed558ccdull;
+  x ^= x >> 33;
+  return (uint32_t)x;
+}
+
+__global__ void __launch_bounds__(kOvThreads) seed_overflow_kernel(SeedArgs a,
+                                                                   const uint64_t* tab_off,
+                                                                   const uint32_t* tab_size) {
+  __shared__ uint8_t codes[kReadMax + 1];
+  __shared__ uint64_t red[kOvThreads / 32];
+  const int64_t sid = a.overflow_list[blockIdx.x];
+  const int64_t read = sid >> 1;
+  const int strand = (int)(sid & 1);
+  const DevRead rd = a.rd[read];
+  const int L = rd.len, k = a.k, nq = L - k + 1;
+  const uint32_t S = tab_size[blockIdx.x];
+  uint64_t* tk = a.scratch + tab_off[blockIdx.x];
+  uint32_t* tc = reinterpret_cast<uint32_t*>(tk + S);
+  uint32_t* ti = tc + S;
+  const char* s = a.reads + rd.seq_off;
+  for (int i = threadIdx.x; i < L; i += blockDim.x)
+    codes[i] = strand == 0 ? fwd_code((uint8_t)s[i]) : rev_code((uint8_t)s[L - 1 - i]);
+  __syncthreads();
+  // insert every hit; each warp walks one query offset's bucket at a time
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int i = wid; i < nq; i += nw) {
+    uint32_t h = 0;
+    for (int t = k - 1; t >= 0; --t) h = (h << 2) | codes[i + t];
+    uint32_t b = a.offsets[h], e = a.offsets[h + 1];
+    for (uint32_t j = b + lane; j < e; j += 32) {
+      uint2 p = a.postings[j];
+      uint64_t ck = make_key(p.y, (int32_t)p.x - i, 0) >> 8;  // nonzero
+      uint32_t slot = mix(ck) & (S - 1);
+      for (uint32_t probe = 0; probe < S; ++probe) {
+        unsigned long long old = atomicCAS((unsigned long long*)&tk[slot], 0ull,
+                                           (unsigned long long)ck);
+        if (old == 0ull || old == ck) {
+          atomicAdd(&tc[slot], 1u);
+          atomicMax(&ti[slot], 255u - (uint32_t)i);  // zero-initialised table
+          break;
+        }
+        slot = (slot + 1) & (S - 1);
+      }
+    }
+  }
+  __syncthreads();
+  // biggest cluster size
+  uint32_t big = 0;
+  for (uint32_t x = threadIdx.x; x < S; x += blockDim.x) big = max(big, tc[x]);
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) big = max(big, __shfl_xor_sync(0xffffffffu, big, d));
+  if (lane == 0) red[wid] = big;
+  __syncthreads();
+  big = 0;
+  for (int w = 0; w < nw; ++w) big = max(big, (uint32_t)red[w]);
+  __syncthreads();
+  // the first max_hits cluster keys of that size, smallest first
+  uint64_t last = 0;
+  int got = 0;
+  int3* out = a.best + sid * a.max_hits;
+  for (int g = 0; g < a.max_hits; ++g) {
+    uint64_t mn = ~0ull;
+    for (uint32_t x = threadIdx.x; x < S; x += blockDim.x)
+      if (tc[x] == big && tk[x] > last && tk[x] < mn) mn = tk[x];
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+      uint64_t o = __shfl_xor_sync(0xffffffffu, mn, d);
+      mn = o < mn ? o : mn;
+    }
+    if (lane == 0) red[wid] = mn;
+    __syncthreads();
+    mn = ~0ull;
+    for (int w = 0; w < nw; ++w) mn = red[w] < mn ? red[w] : mn;
+    __syncthreads();
+    if (mn == ~0ull) break;
+    if (threadIdx.x == 0) {
+      uint32_t slot = mix(mn) & (S - 1);
+      while (tk[slot] != mn) slot = (slot + 1) & (S - 1);
+      int32_t ri = (int32_t)(mn >> 32);
+      int32_t shift = (int32_t)(mn & 0xffffffffu) - kShiftBias;
+      out[got] = make_int3(ri, shift, shift + (int32_t)(255u - ti[slot]));
+    }
+    ++got;
+    last = mn;
+  }
+  if (threadIdx.x == 0) a.nbest[sid] = got;
+}
+
+}  // namespace
+
+constexpr int kSeedCap = 512;  // 8 warps x 512 x 10 B = 40 KB of static shared memory
+
+void launch_seed(cudaStream_t st, const SeedArgs& a) {
+  int64_t strands = 2 * a.n_reads;
+  if (strands == 0) return;
+  unsigned grid = (unsigned)((strands + kSeedWarps - 1) / kSeedWarps);
+  seed_warp_kernel<kSeedCap><<<grid, kSeedWarps * 32, 0, st>>>(a);
+}
+
+int seed_smem_cap() { return kSeedCap; }
+
+void launch_seed_overflow(cudaStream_t st, const SeedArgs& a, int n_overflow,
+                          const uint64_t* tab_off, const uint32_t* tab_size) {
+  if (n_overflow <= 0) return;
+  seed_overflow_kernel<<<n_overflow, kOvThreads, 0, st>>>(a, tab_off, tab_size);
+}
+
+}  // namespace swift

@@ -1,0 +1,333 @@
+"""CUDA path against the CPU oracle: bit-exact on every output.
+
+Each test builds inputs with a fixed seed, runs the device path through the
+C ABI and compares with the oracle restatement of the reference.
+"""
+import os
+import random
+import subprocess
+import tempfile
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def sg():
+    from swift_gb300 import build as b
+    b.build()
+    import swift_gb300
+    return swift_gb300
+
+
+@pytest.fixture(scope="module")
+def ctx(sg):
+    return sg.Context(0)
+
+
+def oparams(ctx, O, **kw):
+    return O.default_params(device_mem=ctx.info()["total_mem"], **kw)
+
+
+def first_diff(a: bytes, b: bytes) -> int:
+    n = min(len(a), len(b))
+    for i in range(n):
+        if a[i] != b[i]:
+            return i
+    return n
+
+
+# ---------------------------------------------------------------------------
+# index
+
+GOLDEN_FASTA = [
+    (b">ref1\nACGTACGTGTACGTAACATC\n", 8, 15),
+    (b">ref1\nACGTACGTAATAACGTACGTATTTACGTACACCCGTACGT\n>ref2\n"
+     b"GCCGTACGACGTACGTAAACGTAACGTACGTATTTACG\n"
+     b">ref3\nCGTACGTAAAATAACGTCGTACGTAAACGTACGTACGTAA", 8, 15),
+    (b">ref1\nACGTACGTAATAACGTACGTATTT\nACGTACACCCGTACGT\n>ref2\n"
+     b"GCCGTACGACGTACGTAAACGTAA\nCGTACGTATTTACG\n"
+     b">ref3\nCGTACGTAAA\nATAACGTCGT\nACGTAAACGT\nACGTACGTAA", 8, 4),
+    (b">ref1\nACGTACGTAATAACGTACGTATTT\nACGTACACCCGTACGT\n>ref2\n"
+     b"GCCGTACGACGTACGTAAACGTAA\nCGTACGTATTTACG\n"
+     b">ref3\nCGTACGTAAA\nATAACGTCGT\nACGTAAACGT\nACGTACGTAA", 4, 7),
+]
+
+
+def messy_reference(seed=3, n_seqs=5, total=120_000):
+    """Multi-record FASTA with lowercase runs, N runs, IUPAC letters, blank
+    lines and uneven line widths."""
+    rng = random.Random(seed)
+    out = []
+    for r in range(n_seqs):
+        n = total // n_seqs + rng.randint(-5000, 5000)
+        s = bytearray(rng.choice(b"ACGT") for _ in range(n))
+        for _ in range(20):
+            a = rng.randrange(n)
+            for i in range(a, min(n, a + rng.randint(1, 40))):
+                s[i] = s[i] + 32 if rng.random() < 0.7 else ord("N")
+        for _ in range(5):
+            s[rng.randrange(n)] = rng.choice(b"RYKMSW")
+        out.append(b">seq%d some description\n" % r)
+        width = rng.choice([50, 60, 61, 70])
+        for i in range(0, n, width):
+            out.append(bytes(s[i:i + width]) + b"\n")
+            if rng.random() < 0.002:
+                out.append(b"\n")
+    return b"".join(out)
+
+
+@pytest.mark.parametrize("case", range(len(GOLDEN_FASTA)))
+def test_index_golden(ctx, oracle, case):
+    fa, k, t = GOLDEN_FASTA[case]
+    ix = ctx.index(fa, k, t)
+    look, rep, ri, rp = ix.export()
+    ox = oracle.Index(fa, k, t)
+    ori, orp = ox.postings()
+    assert list(ri) == list(ori) and list(rp) == list(orp)
+    for h in range(ox.num_buckets):
+        assert look[h] == ox.start(h) and rep[h] == ox.repeats(h)
+
+
+def test_index_messy_reference(ctx, oracle):
+    fa = messy_reference()
+    for k, t in [(12, 1000), (8, 3)]:
+        ix = ctx.index(fa, k, t)
+        look, rep, ri, rp = ix.export()
+        ox = oracle.Index(fa, k, t)
+        ori, orp = ox.postings()
+        assert np.array_equal(ri, ori) and np.array_equal(rp, orp)
+        nb = ox.num_buckets
+        assert all(look[h] == ox.start(h) for h in range(0, nb, max(1, nb // 50000)))
+
+
+# ---------------------------------------------------------------------------
+# Smith-Waterman (alignSequences contract)
+
+def test_sw_golden(ctx):
+    # test/testSmithWaterman.cu:29-124 and :304-386
+    r = ctx.sw_batch([b"ACGTACGTAA"], [b"CCCCAAAACGTCCGTTACGT"], 10, 20)[0]
+    assert (r["score"], r["start"], r["end"], r["len"]) == (14.0, 8, 17, 10)
+    assert r["qcons"] == b"AATGCATGCA" and r["rcons"] == b"ATTGCCTGCA"
+    r = ctx.sw_batch([b"CTTGTCACCATCCA"], [b"CTTGTCACCATCA"], 14, 13)[0]
+    assert r["score"] == 24.0
+    r = ctx.sw_batch([b"ACGTACGTAA"], [b"CCCCAAAACGTCCGTTACGT"], 10, 25)[0]
+    assert r["score"] == 14.0
+
+
+def mutate(rng, s: bytes, p_sub=0.05, p_indel=0.02) -> bytes:
+    out = bytearray()
+    for c in s:
+        x = rng.random()
+        if x < p_indel / 2:
+            continue
+        if x < p_indel:
+            out += bytes(rng.choice(b"ACGT") for _ in range(rng.randint(1, 4)))
+        out.append(rng.choice(b"ACGT") if rng.random() < p_sub else c)
+    return bytes(out)
+
+
+def random_pairs(seed, n, Q, R, alphabet=b"ACGT"):
+    rng = random.Random(seed)
+    qs, ws = [], []
+    for i in range(n):
+        kind = i % 5
+        w = bytes(rng.choice(alphabet) for _ in range(R))
+        if kind == 0:
+            q = bytes(rng.choice(alphabet) for _ in range(Q))
+        else:
+            a = rng.randrange(0, max(1, R - Q))
+            q = mutate(rng, w[a:a + Q + 10])[:Q]
+            q = q.ljust(Q, b"A")
+        if kind == 2:  # window cut short: NUL padding
+            w = w[: rng.randint(Q // 2, R)]
+        if kind == 3:  # case and N
+            w = bytes((c + 32 if rng.random() < 0.3 else c) for c in w)
+            q = bytes((ord("N") if rng.random() < 0.02 else c) for c in q)
+        qs.append(q)
+        ws.append(w)
+    return qs, ws
+
+
+@pytest.mark.parametrize("Q,R", [(100, 300), (37, 300), (128, 200), (200, 300), (256, 64)])
+def test_sw_random_vs_oracle(ctx, oracle, Q, R):
+    qs, ws = random_pairs(11 + Q + R, 300, Q, R)
+    got = ctx.sw_batch(qs, ws, Q, R)
+    for i, (q, w) in enumerate(zip(qs, ws)):
+        want = oracle.sw(q, w, Q, R)
+        for key in ("score", "start", "end", "len", "qcons", "rcons"):
+            assert got[i][key] == want[key], (i, key, got[i][key], want[key])
+
+
+def test_sw_scoring_parameters(ctx, oracle):
+    qs, ws = random_pairs(5, 100, 60, 150)
+    for m, x, o, e in [(1, -3, -5, -2), (5, -4, -20, -1), (2, -1, -1, -1)]:
+        got = ctx.sw_batch(qs, ws, 60, 150, m, x, o, e)
+        for i, (q, w) in enumerate(zip(qs, ws)):
+            want = oracle.sw(q, w, 60, 150, m, x, o, e)
+            assert (got[i]["score"], got[i]["start"], got[i]["end"], got[i]["len"],
+                    got[i]["qcons"], got[i]["rcons"]) == (
+                want["score"], want["start"], want["end"], want["len"], want["qcons"],
+                want["rcons"])
+
+
+def test_sw_zero_pairs_and_limits(ctx, sg):
+    assert ctx.sw_batch([], [], 10, 10) == []
+    with pytest.raises(sg.SwiftError):
+        ctx.sw_batch([b"A" * 10], [b"A" * 10], 300, 10)
+
+
+# ---------------------------------------------------------------------------
+# Phase 1
+
+def small_case(n_reads=2000, seed=21, ref_bp=200_000, n_seqs=3):
+    from swift_gb300 import synth
+    names, seqs = synth.make_reference(ref_bp, n_seqs, sigma=0.5, seed=seed)
+    ref = synth.fasta_bytes(names, seqs)
+    rn, rs, _ = synth.make_reads(seqs, n_reads, 100, 0.01, 0.001, 0.05, seed=seed + 1)
+    return ref, synth.reads_fasta(rn, rs)
+
+
+def test_seed_vs_oracle(ctx, oracle):
+    ref, reads = small_case()
+    ix = ctx.index(ref)
+    got = ctx.seed(ix, reads)
+    want = oracle.phase1(ref, reads, oparams(ctx, oracle))
+    assert got == want
+
+
+def test_seed_overflow_path(ctx, oracle):
+    # 100 exact copies of a 120-bp unit: reads over it hit ~800 postings per
+    # strand, more than the on-chip path holds
+    rng = random.Random(9)
+    unit = bytes(rng.choice(b"ACGT") for _ in range(120))
+    body = b"".join(unit for _ in range(100))
+    tail = bytes(rng.choice(b"ACGT") for _ in range(3000))
+    seq = tail + body + tail
+    ref = b">rep\n" + b"\n".join(seq[i:i + 60] for i in range(0, len(seq), 60)) + b"\n"
+    reads = []
+    for i in range(40):
+        a = rng.randrange(0, len(seq) - 100)
+        reads.append(b">q%d\n%s\n" % (i, seq[a:a + 100]))
+    reads = b"".join(reads)
+    ix = ctx.index(ref)
+    got = ctx.seed(ix, reads)
+    want = oracle.phase1(ref, reads, oparams(ctx, oracle))
+    assert got == want
+    _, st = ctx.align(ix, reads, stats=True)
+    assert st["seed_overflow_strands"] > 0
+
+
+# ---------------------------------------------------------------------------
+# whole pipeline
+
+def test_align_small_workload(ctx, oracle):
+    from swift_gb300 import synth
+    ref, reads, _ = synth.workload("small")
+    ix = ctx.index(ref)
+    got = ctx.align(ix, reads)
+    want = oracle.align(ref, reads, oparams(ctx, oracle))
+    assert len(got) == len(want) and got == want, first_diff(got, want)
+
+
+@pytest.mark.parametrize("n_reads", [1, 15, 16, 17, 33, 250])
+def test_align_read_counts(ctx, oracle, n_reads):
+    # trailing 16-read batches of searchQueries3 repeat stale reads
+    ref, reads = small_case(n_reads=n_reads, seed=40 + n_reads)
+    ix = ctx.index(ref)
+    got = ctx.align(ix, reads)
+    want = oracle.align(ref, reads, oparams(ctx, oracle))
+    assert got == want, first_diff(got, want)
+
+
+def test_align_messy_inputs(ctx, oracle):
+    fa = messy_reference(seed=8)
+    # reads drawn from the messy reference (lowercase, N), some reverse
+    # complemented, some shorter than the seed length
+    seqs = []
+    cur = None
+    for line in fa.split(b"\n"):
+        if line.startswith(b">"):
+            cur = bytearray()
+            seqs.append(cur)
+        elif cur is not None:
+            cur += line
+    rng = random.Random(12)
+    parts = []
+    for i in range(600):
+        s = seqs[rng.randrange(len(seqs))]
+        a = rng.randrange(0, len(s) - 100)
+        r = bytes(s[a:a + 100])
+        if i % 3 == 1:
+            r = oracle.revcomp(r)
+        if i % 7 == 3:
+            r = bytes(rng.choice(b"ACGTN") for _ in range(100))
+        parts.append(b">read_%d/x\n%s\n" % (i, r))
+    reads = b"".join(parts)
+    ix = ctx.index(fa)
+    got = ctx.align(ix, reads)
+    want = oracle.align(fa, reads, oparams(ctx, oracle))
+    assert got == want, first_diff(got, want)
+
+
+def test_align_scoring_and_seed_parameters(ctx, oracle, sg):
+    ref, reads = small_case(n_reads=300, seed=77)
+    for kw in [dict(seed_len=10, ignore_thres=50), dict(match=3, mismatch=-2, gap_open=-6,
+                                                        gap_ext=-2), dict(max_hits=1)]:
+        k = kw.get("seed_len", 12)
+        t = kw.get("ignore_thres", 1000)
+        ix = ctx.index(ref, k, t)
+        p = sg.default_params(**kw)
+        got = ctx.align(ix, reads, p)
+        want = oracle.align(ref, reads, oparams(ctx, oracle, **kw))
+        assert got == want, (kw, first_diff(got, want))
+
+
+def test_align_longer_reads_than_query_length(ctx, oracle, sg):
+    ref, reads = small_case(n_reads=200, seed=91)
+    ix = ctx.index(ref)
+    p = sg.default_params(qry_len=80)
+    got = ctx.align(ix, reads, p)
+    want = oracle.align(ref, reads, oparams(ctx, oracle, qry_len=80))
+    assert got == want
+
+
+def test_align_resident_matches_host_call(ctx, oracle):
+    ref, reads = small_case(n_reads=500, seed=93)
+    ix = ctx.index(ref)
+    host = ctx.align(ix, reads)
+    rd = ctx.reads(reads)
+    n, st = ctx.align_resident(ix, rd)
+    assert ctx.fetch_output(n) == host
+    n2, _ = ctx.align_resident(ix, rd)
+    assert n2 == n and ctx.fetch_output(n2) == host
+
+
+def test_input_errors(ctx, sg):
+    ref, _ = small_case(n_reads=1, seed=5)
+    ix = ctx.index(ref)
+    for bad, code in [(b">a\nACGT\n\n>b\nACGT\n", -2),       # empty line
+                      (b">a\nACGT\nACGT\n", -2),             # multi-line read
+                      (b">a\n", -2),                          # header without sequence
+                      (b">a\nAC>GT\n", -2),                  # '>' inside a line
+                      (b">a\n" + b"A" * 250 + b"\n", -5)]:    # read over 199 bases
+        with pytest.raises(sg.SwiftError) as e:
+            ctx.align(ix, bad)
+        assert e.value.code == code
+    with pytest.raises(sg.SwiftError):
+        ctx.index(b"ACGT\n>x\nACGT\n")
+
+
+def test_cli_matches_oracle(ctx, oracle, sg):
+    ref, reads = small_case(n_reads=300, seed=55)
+    with tempfile.TemporaryDirectory() as d:
+        rp, qp, op = (os.path.join(d, f) for f in ("ref.fa", "reads.fa", "out.txt"))
+        open(rp, "wb").write(ref)
+        open(qp, "wb").write(reads)
+        r = subprocess.run([sg.CLI_PATH, "-q", qp, "-r", rp, "-o", op], capture_output=True)
+        assert r.returncode == 0, r.stderr
+        got = open(op, "rb").read()
+    want = oracle.align(ref, reads, oparams(ctx, oracle))
+    assert got == want
