@@ -1,0 +1,320 @@
+/*
+ * harness.cpp — runs the reference's own code for validation of the oracle.
+ * TEST INFRASTRUCTURE ONLY; built from the reference sources where they lie
+ * (see Makefile), output only under oracle/_ref/.
+ *
+ * The reference functions called here are compiled unmodified from the
+ * reference's src/ directory.  Only glue the reference keeps in static
+ * functions or behind device APIs is restated here, each with its citation:
+ *   - the 16-slot loop of searchQueries3 (src/search.cu:275-382) and the
+ *     record line of printHeuristicMatches4 (src/search.cu:2230-2240),
+ *     run sequentially with mapHits6's random picks pinned to the first ones;
+ *   - the per-batch loop of alignQueries3 (src/align.cu:574-808) and the
+ *     batch sizing of getNumQueriesPerIteration (src/align.cu:2767-2793);
+ *   - chooseBestAlignment (src/align.cu:844-905) with the first maximum kept.
+ * The GPU kernel smithWaterman (src/smithWaterman.cu:360-395) runs on the
+ * CPU: one fiber per CUDA thread, __syncthreads() yields to the next fiber.
+ */
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <ucontext.h>
+
+#include <vector>
+
+#include "common.h"
+#include "input.h"
+#include "lookupTable5.h"
+#include "mapHits6.h"
+#include "output.h"
+#include "preprocess.h"
+#include "query.h"
+#include "refMap.h"
+
+/* declarations with C++ linkage, as the reference compiles them */
+void smithWaterman(char *refSeq, int refSeqLength, char *querySeq, int querySeqLength,
+                   float match, float mismatch, float gapOpenPenalty, float gapExtPenalty,
+                   float *maxScore, int *startPos, int *endPos, int *alignLength,
+                   char *refConsensus, char *queryConsensus, int numQueries, int numReferences);
+void smithWaterman_cpu(float *HMatrix, int *rowBacktracker, int *colBacktracker, char *refSeq,
+                       int refLen, char *qrySeq, int qryLen, float match, float mismatch,
+                       float gapOpenPenalty, float gapExtPenalty, float *alignScore,
+                       int *startPos, int *endPos, int *alignLen, char *refConsensus,
+                       char *qryConsensus);
+
+/* ---- shim runtime (declared in shim.h) ------------------------------- */
+struct ref_dim3 threadIdx, blockIdx, blockDim, gridDim;
+int arr_shr[1];
+
+cudaError_t cudaGetLastError(void) { return 0; }
+const char *cudaGetErrorString(cudaError_t) { return "no error"; }
+cudaError_t cudaMalloc(void **, size_t) { abort(); }
+cudaError_t cudaFree(void *) { abort(); }
+cudaError_t cudaMemcpy(void *, const void *, size_t, enum cudaMemcpyKind) { abort(); }
+cudaError_t cudaMemset(void *, int, size_t) { abort(); }
+
+static unsigned g_rand = 0;
+/* stands in for rand() in array.cu (arrGetRandomNums): 0, 1, 2, ... so the
+ * random biggest-cluster picks of mapHits6 become the first ones */
+extern "C" int ref_rand(void) { return (int)(g_rand++); }
+
+static ucontext_t g_main;
+static std::vector<ucontext_t> g_fib;
+static std::vector<int> g_done;
+static std::vector<char> g_stacks;
+static int g_cur = 0;
+
+void __syncthreads(void) { swapcontext(&g_fib[g_cur], &g_main); }
+
+struct KernelArgs {
+  char *ref;
+  int R;
+  char *qry;
+  int Q;
+  float m, x, o, e;
+  float *score;
+  int *start, *end, *len;
+  char *rcons, *qcons;
+};
+static KernelArgs g_args;
+
+static void fiber_entry(int tid) {
+  KernelArgs &a = g_args;
+  smithWaterman(a.ref, a.R, a.qry, a.Q, a.m, a.x, a.o, a.e, a.score, a.start, a.end, a.len,
+                a.rcons, a.qcons, 1, 1);
+  g_done[tid] = 1;
+}
+
+/* One CUDA block of T threads for block index b. */
+static void run_block(int T, int b) {
+  const size_t stack = 64 * 1024;
+  g_fib.assign(T, ucontext_t());
+  g_done.assign(T, 0);
+  g_stacks.resize((size_t)T * stack);
+  blockIdx.x = (unsigned)b;
+  blockDim.x = (unsigned)T;
+  for (int t = 0; t < T; ++t) {
+    getcontext(&g_fib[t]);
+    g_fib[t].uc_stack.ss_sp = g_stacks.data() + (size_t)t * stack;
+    g_fib[t].uc_stack.ss_size = stack;
+    g_fib[t].uc_link = &g_main;
+    makecontext(&g_fib[t], (void (*)())fiber_entry, 1, t);
+  }
+  for (;;) {
+    int alive = 0;
+    for (int t = 0; t < T; ++t) {
+      if (g_done[t]) continue;
+      g_cur = t;
+      threadIdx.x = (unsigned)t;
+      swapcontext(&g_main, &g_fib[t]);
+      if (!g_done[t]) alive = 1;
+    }
+    if (!alive) break;
+  }
+}
+
+extern "C" {
+
+/* The GPU kernel on one pair.  q has Q bytes, r has R bytes. */
+int ref_sw_kernel(const char *q, int Q, const char *r, int R, float m, float x, float o, float e,
+                  float *score, int *start, int *end, int *len, char *qcons, char *rcons) {
+  std::vector<char> qb(Q + 1, 0), rb(R + 1, 0);
+  memcpy(qb.data(), q, Q);
+  memcpy(rb.data(), r, R);
+  g_args = KernelArgs{rb.data(), R, qb.data(), Q, m, x, o, e, score, start, end, len, rcons, qcons};
+  *score = 0;
+  int T = Q + 1 > R ? Q + 1 : R;
+  run_block(T, 0);
+  return 0;
+}
+
+/* The reference's CPU Smith-Waterman (the timed baseline of the survey). */
+int ref_sw_cpu(const char *q, int Q, const char *r, int R, float m, float x, float o, float e,
+               float *score, int *start, int *end, int *len, char *qcons, char *rcons) {
+  std::vector<float> H((size_t)(Q + 1) * (R + 1), 0.0f);
+  std::vector<int> rb((size_t)(Q + 1) * (R + 1), 0), cb((size_t)(Q + 1) * (R + 1), 0);
+  std::vector<char> qq(q, q + Q), rr(r, r + R);
+  qq.push_back(0);
+  rr.push_back(0);
+  smithWaterman_cpu(H.data(), rb.data(), cb.data(), rr.data(), R, qq.data(), Q, m, x, o, e, score,
+                    start, end, len, rcons, qcons);
+  return 0;
+}
+
+/* lookupTable5Create on a FASTA file; exports the table in its layout. */
+int ref_index(const char *path, int k, int thres, int *n_buckets, int *total, int **lookup,
+              int **repeats, char **ref_idx, int **ref_pos) {
+  preprocessCreate();
+  int nd = 0;
+  lookupTable5Create_wrap(path, k, 3, lookup, ref_idx, ref_pos, &nd, repeats, thres);
+  *n_buckets = nd;
+  int t = 0;
+  for (int h = 0; h < nd; ++h)
+    if ((*repeats)[h] > 0 && (*repeats)[h] <= thres) t += (*repeats)[h];
+  *total = t;
+  return 0;
+}
+
+/* lookupTable5MapQry on the index built by the last ref_index call. */
+int ref_map_query(const char *seq, const char *rev, int len, int is_rev, char *ri, int *sh,
+                  int *rp) {
+  Query q;
+  std::vector<char> s(seq, seq + len), rv(rev, rev + len);
+  s.push_back(0);
+  rv.push_back(0);
+  char name[2] = "q";
+  q.name = name;
+  q.length = len;
+  q.seq = s.data();
+  q.revCompSeq = rv.data();
+  q.nameOffset = 0;
+  q.seqOffset = 0;
+  g_rand = 0;
+  return lookupTable5MapQry(&q, (uint)len, (uint)is_rev, ri, sh, rp);
+}
+
+/* mapHits6GetBestHits with the random picks pinned to the first ones. */
+int ref_best_hits(int max_hits, char *ri, int *sh, int *rp, int n, char *o_ri, int *o_sh,
+                  int *o_rp) {
+  g_rand = 0;
+  return mapHits6GetBestHits(max_hits, ri, sh, rp, n, o_ri, o_sh, o_rp);
+}
+
+static int qry_name_cmp(const char *s, const char *t, int size) {
+  int i;
+  for (i = 0; i < size; ++i) {
+    if (s[i] == '\0' && t[i] == '\0') return 0;
+    else if (s[i] == '\0' || t[i] == '\0') break;
+    else if (s[i] != t[i]) return -1;
+  }
+  if ((s[i] == '*' && s[i + 1] == '\0') || (t[i] == '*' && t[i + 1] == '\0')) return 0;
+  return -1;
+}
+
+static void choose_best(char *names, int name_len, float *score, int size) {
+  int start = 0, end = size - 1;
+  while (start < size) {
+    int i;
+    for (i = start + 1; i < size; ++i)
+      if (qry_name_cmp(names + i * name_len, names + (i - 1) * name_len, name_len) != 0) {
+        end = i - 1;
+        break;
+      }
+    if (end < start) end = size - 1;
+    float mx = 0.0f;
+    for (i = start; i <= end; ++i)
+      if (mx < score[i]) mx = score[i];
+    int keep = -1;
+    for (i = start; i <= end; ++i)
+      if (score[i] == mx) {
+        keep = i;
+        break;
+      }
+    for (i = start; i <= end; ++i)
+      if (i != keep) score[i] = -1.0f;
+    start = end + 1;
+  }
+}
+
+/* The SSAHA -> GPU Smith-Waterman -> best alignment pipeline with the
+ * reference's functions, file to file.  device_mem sizes the Phase-2
+ * batches as the reference does from its GPU.  Returns the number of
+ * match records. */
+long ref_pipeline(const char *ref_file, const char *qry_file, const char *out_file,
+                  const char *match_file, long long device_mem, int seed_len, int thres,
+                  float m, float x, float o, float e) {
+  preprocessCreate();
+  int num_qrs = getSeqCount((char *)qry_file);
+  int qry_len = getSeqSize((char *)qry_file);
+  refMapCreate(ref_file);
+  int total = 0;
+  lookupTable5Create(ref_file, seed_len, MAX_NUM_HITS_SINGLE_END, thres, &total);
+  FILE *mf = fopen(match_file, "w");
+  FILE *qf = fopen(qry_file, "r");
+  const int nt = NUM_THREADS;
+  Query *slot[NUM_THREADS];
+  for (int j = 0; j < nt; ++j) slot[j] = qryCreate2();
+  char ri[MAX_NUM_HITS_SINGLE_END];
+  int sh[MAX_NUM_HITS_SINGLE_END], rp[MAX_NUM_HITS_SINGLE_END];
+  long num_matches = 0;
+  for (int i = 0; i < num_qrs; i += nt) {
+    for (int j = 0; j < nt; ++j) qryGetNext2(qf, slot[j]);
+    for (int j = 0; j < nt; ++j) {
+      for (int strand = 0; strand < 2; ++strand) {
+        g_rand = 0;
+        int n = lookupTable5MapQry(slot[j], slot[j]->length, strand, ri, sh, rp);
+        for (int h = 0; h < n; ++h)
+          fprintf(mf, "%s\t%d\t%d\t%d\t%d\t%lu\t%lu\n", slot[j]->name, strand, ri[h], sh[h], rp[h],
+                  slot[j]->nameOffset, slot[j]->seqOffset);
+        num_matches += n;
+      }
+    }
+  }
+  fclose(mf);
+  fclose(qf);
+  /* Phase 2 */
+  const int R = REF_LENGTH, Q = qry_len, comb = R + Q + 2;
+  long per_iter;
+  {
+    int mem_pair = (R + 1) + (Q + 1) + 4 + 4 + 4 + 2 + 2 * (R + Q + 2);
+    long gm = (long)(device_mem - GLOBAL_MEM_MARGIN);
+    per_iter = (int)floor((float)gm / mem_pair);
+    if (per_iter > num_matches) per_iter = num_matches;
+    if (per_iter >= 2 && per_iter % 2 == 1) --per_iter;
+  }
+  int n_iter = per_iter > 0 ? (int)ceil((float)num_matches / per_iter) : 0;
+  std::vector<float> score(per_iter > 0 ? per_iter : 1);
+  std::vector<int> dist(score.size()), st(score.size()), en(score.size()), ln(score.size());
+  std::vector<char> rcons(score.size() * comb), qcons(score.size() * comb);
+  std::vector<char> qname(score.size() * MAX_SEQ_NAME_LENGTH), rname(score.size() * MAX_SEQ_NAME_LENGTH);
+  std::vector<char> qseq(score.size() * (Q + 1), 0), rseq(score.size() * (R + 1), 0);
+  std::vector<char> tmpq(Q + 1, 0);
+  mf = fopen(match_file, "r");
+  FILE *of = fopen(out_file, "w");
+  FILE *qfp = fopen(qry_file, "r");
+  FILE *rfp = fopen(ref_file, "r");
+  for (int it = 0; it < n_iter; ++it) {
+    memset(rseq.data(), 0, rseq.size());
+    long cnt = per_iter;
+    if (it == n_iter - 1) {
+      long maxs = (long)n_iter * per_iter;
+      cnt = num_matches < maxs ? num_matches - (long)(n_iter - 1) * per_iter : per_iter;
+    }
+    for (long j = 0; j < cnt; ++j) {
+      uint qno, qso, rno, rso, rfo, rev;
+      int ridx;
+      getOffsets(mf, &qno, &qso, &rno, &rso, &rfo, &dist[j], &rev, &ridx);
+      dist[j] = dist[j] - R / 3 > 0 ? dist[j] - R / 3 : 0;
+      refMapGetOffsets(ridx, dist[j], &rno, &rfo);
+      getRefSeq2(rfp, rfo, rseq.data() + j * (R + 1), R);
+      getSeqName(rfp, rno, rname.data() + j * MAX_SEQ_NAME_LENGTH);
+      if (rev == 1) {
+        getSeq2(qfp, qso, tmpq.data(), Q);
+        qryGetReverseComplement(tmpq.data(), Q, qseq.data() + j * (Q + 1));
+        getSeqName(qfp, qno, qname.data() + j * MAX_SEQ_NAME_LENGTH);
+        strcat(qname.data() + j * MAX_SEQ_NAME_LENGTH, "*");
+      } else {
+        getSeq2(qfp, qso, qseq.data() + j * (Q + 1), Q);
+        getSeqName(qfp, qno, qname.data() + j * MAX_SEQ_NAME_LENGTH);
+      }
+    }
+    for (long j = 0; j < cnt; ++j) score[j] = 0;
+    g_args = KernelArgs{rseq.data(), R, qseq.data(), Q, m, x, o, e, score.data(), st.data(),
+                        en.data(), ln.data(), rcons.data(), qcons.data()};
+    const int T = Q + 1 > R ? Q + 1 : R;
+    for (long j = 0; j < cnt; ++j) run_block(T, (int)j);
+    choose_best(qname.data(), MAX_SEQ_NAME_LENGTH, score.data(), (int)cnt);
+    printOutput((int)cnt, qname.data(), rname.data(), score.data(), dist.data(), st.data(),
+                en.data(), ln.data(), comb, qcons.data(), rcons.data(), of);
+  }
+  fclose(mf);
+  fclose(of);
+  fclose(qfp);
+  fclose(rfp);
+  for (int j = 0; j < nt; ++j) qryDelete(slot[j]);
+  refMapFree();
+  return num_matches;
+}
+
+}  // extern "C"

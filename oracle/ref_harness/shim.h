@@ -1,0 +1,76 @@
+/*
+ * shim.h — lets the reference's .cu sources compile as host C++ for the
+ * validation harness.  TEST INFRASTRUCTURE ONLY.
+ *
+ * CUDA qualifiers become nothing (or 'static' for __shared__ inside the
+ * Smith-Waterman kernel, so that one CPU "block" of fibers shares them);
+ * threadIdx/blockIdx/blockDim are globals set by the fiber scheduler;
+ * __syncthreads() yields to the next fiber.  CUDA runtime calls that the
+ * harness never reaches are declared so the files compile; they abort.
+ */
+#ifndef REF_SHIM_H_
+#define REF_SHIM_H_
+#include <ctype.h>
+#include <limits.h>
+#include <math.h>
+#include <pthread.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+#include "common.h"
+#undef TMP_DIR
+#define TMP_DIR REF_TMP_DIR
+
+#define __global__
+#define __device__
+#define __host__
+#define __constant__
+#ifdef REF_SHARED_STATIC
+#define __shared__ static
+/* the kernel file defines its own toupper; keep libc's declaration apart */
+#define toupper ref_sw_toupper
+#else
+#define __shared__
+#endif
+
+#ifdef REF_PIN_RAND
+/* array.cu: rand() -> a counter 0, 1, 2, ... reset before each call of
+ * interest, which pins mapHits6's random picks to the first clusters */
+extern "C" int ref_rand(void);
+#define rand ref_rand
+#endif
+
+/* device-side min/max that CUDA provides */
+static inline int max(int a, int b) { return a > b ? a : b; }
+static inline int min(int a, int b) { return a < b ? a : b; }
+static inline short max(short a, short b) { return a > b ? a : b; }
+static inline short min(short a, short b) { return a < b ? a : b; }
+
+struct ref_dim3 {
+  unsigned int x, y, z;
+};
+extern struct ref_dim3 threadIdx, blockIdx, blockDim, gridDim;
+void __syncthreads(void);
+
+typedef int cudaError_t;
+enum cudaMemcpyKind {
+  cudaMemcpyHostToHost,
+  cudaMemcpyHostToDevice,
+  cudaMemcpyDeviceToHost,
+  cudaMemcpyDeviceToDevice
+};
+#define cudaSuccess 0
+cudaError_t cudaGetLastError(void);
+const char *cudaGetErrorString(cudaError_t);
+cudaError_t cudaMalloc(void **, size_t);
+cudaError_t cudaFree(void *);
+cudaError_t cudaMemcpy(void *, const void *, size_t, enum cudaMemcpyKind);
+cudaError_t cudaMemset(void *, int, size_t);
+template <class T>
+cudaError_t cudaMemcpyToSymbol(const T &, const void *, size_t, size_t = 0,
+                               enum cudaMemcpyKind = cudaMemcpyHostToDevice) {
+  abort();
+}
+#endif

@@ -67,7 +67,7 @@ def messy_reference(seed=3, n_seqs=5, total=120_000):
         for _ in range(20):
             a = rng.randrange(n)
             for i in range(a, min(n, a + rng.randint(1, 40))):
-                s[i] = s[i] + 32 if rng.random() < 0.7 else ord("N")
+                s[i] = (s[i] | 0x20) if rng.random() < 0.7 else ord("N")
         for _ in range(5):
             s[rng.randrange(n)] = rng.choice(b"RYKMSW")
         out.append(b">seq%d some description\n" % r)
@@ -144,7 +144,7 @@ def random_pairs(seed, n, Q, R, alphabet=b"ACGT"):
         if kind == 2:  # window cut short: NUL padding
             w = w[: rng.randint(Q // 2, R)]
         if kind == 3:  # case and N
-            w = bytes((c + 32 if rng.random() < 0.3 else c) for c in w)
+            w = bytes(((c | 0x20) if rng.random() < 0.3 else c) for c in w)
             q = bytes((ord("N") if rng.random() < 0.02 else c) for c in q)
         qs.append(q)
         ws.append(w)

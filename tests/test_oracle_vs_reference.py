@@ -1,0 +1,118 @@
+"""The oracle against the reference's own code on seeded random inputs.
+
+Runs only where oracle/_ref was built from the reference sources (the build
+container); elsewhere the committed fixtures of test_golden_fixtures.py
+carry the same check.
+"""
+import random
+
+import pytest
+
+from oracle import ref as R
+
+pytestmark = pytest.mark.skipif(not R.available(), reason="reference harness not built")
+
+
+def rand_seq(rng, n, alphabet=b"ACGT"):
+    return bytes(rng.choice(alphabet) for _ in range(n))
+
+
+def mutate(rng, s, p_sub=0.04, p_indel=0.02):
+    out = bytearray()
+    for c in s:
+        x = rng.random()
+        if x < p_indel / 2:
+            continue
+        if x < p_indel:
+            out += rand_seq(rng, rng.randint(1, 3))
+        out.append(rng.choice(b"ACGT") if rng.random() < p_sub else c)
+    return bytes(out)
+
+
+def test_sw_kernel_random(oracle):
+    rng = random.Random(5)
+    for i in range(60):
+        Q, Rl = rng.choice([(100, 300), (12, 40), (50, 120), (30, 300)])
+        w = rand_seq(rng, Rl, b"ACGTacgtN" if i % 4 == 3 else b"ACGT")
+        if i % 3:
+            a = rng.randrange(0, max(1, Rl - Q))
+            q = mutate(rng, w[a:a + Q + 5].upper())[:Q].ljust(Q, b"C")
+        else:
+            q = rand_seq(rng, Q)
+        if i % 5 == 2:
+            w = w[: rng.randint(Q // 2, Rl)]
+        want = R.sw_kernel(q, w, Q, Rl)
+        got = oracle.sw(q, w, Q, Rl)
+        assert {k: got[k] for k in want} == want, (i, q, w)
+
+
+def test_sw_kernel_scoring(oracle):
+    rng = random.Random(6)
+    for m, x, o, e in [(1, -3, -5, -2), (5, -4, -20, -1), (2, -1, -1, -1)]:
+        for _ in range(5):
+            w = rand_seq(rng, 150)
+            q = mutate(rng, w[20:90])[:60].ljust(60, b"G")
+            want = R.sw_kernel(q, w, 60, 150, m, x, o, e)
+            got = oracle.sw(q, w, 60, 150, m, x, o, e)
+            assert {k: got[k] for k in want} == want
+
+
+def test_cpu_sw_agrees_on_score_and_end(oracle):
+    # the reference's CPU routine has the same DP and maximum cell; its
+    # traceback may continue through zero cells, so only score and end are
+    # compared (src/smithWaterman.cu:194-210, 263-335)
+    rng = random.Random(7)
+    for _ in range(40):
+        w = rand_seq(rng, 300)
+        q = mutate(rng, w[50:160])[:100].ljust(100, b"T")
+        a = R.sw_cpu(q, w)
+        b = oracle.sw(q, w)
+        assert a["score"] == b["score"] and a["end"] == b["end"]
+
+
+def test_index_and_map_query(oracle):
+    rng = random.Random(8)
+    parts = []
+    seqs = []
+    for r in range(3):
+        s = rand_seq(rng, rng.randint(3000, 6000))
+        unit = rand_seq(rng, 48)
+        s = s[:1000] + unit * 30 + s[1000:]
+        seqs.append(s)
+        w = rng.choice([60, 61, 50])
+        parts.append(b">c%d\n" % r + b"\n".join(s[i:i + w] for i in range(0, len(s), w)) + b"\n")
+    fa = b"".join(parts)
+    for k, t in [(12, 1000), (8, 10)]:
+        look, rep, ri, rp = R.index(fa, k, t)
+        ox = oracle.Index(fa, k, t)
+        ori, orp = ox.postings()
+        assert list(ori) == ri and list(orp) == rp
+        assert all(ox.start(h) == look[h] and ox.repeats(h) == rep[h]
+                   for h in range(0, len(look), 7))
+        for _ in range(40):
+            s = seqs[rng.randrange(3)]
+            a = rng.randrange(0, len(s) - 100)
+            q = mutate(rng, s[a:a + 100], 0.02, 0.005)[:100]
+            rc = oracle.revcomp(q)
+            assert R.map_query(q, rc, 0) == ox.map_query(q, 3)
+            assert R.map_query(q, rc, 1) == ox.map_query(rc, 3)
+
+
+def test_pipeline_random(oracle):
+    rng = random.Random(9)
+    seqs = [rand_seq(rng, n) for n in (7000, 5000)]
+    ref = b"".join(b">s%d\n" % i + b"\n".join(s[j:j + 60] for j in range(0, len(s), 60)) + b"\n"
+                   for i, s in enumerate(seqs))
+    reads = []
+    for i in range(37):
+        s = seqs[rng.randrange(2)]
+        a = rng.randrange(0, len(s) - 110)
+        r = mutate(rng, s[a:a + 110], 0.02, 0.005)[:100].ljust(100, b"A")
+        if i % 2:
+            r = oracle.revcomp(r)
+        reads.append(b">q%d\n%s\n" % (i, r))
+    reads = b"".join(reads)
+    dm = 288_000_000_000
+    want = R.pipeline(ref, reads, dm)
+    got = oracle.align(ref, reads, oracle.default_params(device_mem=dm))
+    assert got == want
