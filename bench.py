@@ -251,14 +251,18 @@ def main():
         "metric": METRIC, "value": value, "unit": "reads/s", "n_gpus": world,
         "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "int32", "data": "synthetic",
+        "dtype": "int16x2" if stats[-1]["sw_generic_pairs"] < stats[-1]["records"] else "int32",
+        "data": "synthetic",
         "config": {"workload": desc, "l2": "inputs larger than L2 (reads %.0f MB, index %.0f MB)"
                    % (len(reads) / 1e6, (2 * 4 ** 12 * 4 + 8 * idx.info()["total"]) / 1e6),
-                   "records_per_step": stats[-1]["records"], "index_build_s": index_s},
+                   "records_per_step": stats[-1]["records"],
+                   "printed_per_step": stats[-1]["printed"],
+                   "generic_pairs_per_step": stats[-1]["sw_generic_pairs"],
+                   "index_build_s": index_s},
         "sw_gcups": gcups,
         "phase_ms": {k: statistics.median(s[k] for s in stats)
-                     for k in ("seed_ms", "pairs_ms", "sw_ms", "select_ms", "format_ms",
-                               "total_ms")},
+                     for k in ("seed_ms", "pairs_ms", "sw_ms", "select_ms", "traceback_ms",
+                               "format_ms", "total_ms")},
         "roofline": {"bound": "dpx", "kernel": "sw", "achieved": achieved, "peak": peak,
                      "unit": "Gcells/s", "frac": achieved / peak if peak else None,
                      "traffic": None,

@@ -70,7 +70,7 @@ typedef struct {
 /* Timings of the last swift_align call, in milliseconds of device time
  * (CUDA events on the context stream). */
 typedef struct {
-  double seed_ms, pairs_ms, sw_ms, select_ms, format_ms, total_ms;
+  double seed_ms, pairs_ms, sw_ms, select_ms, traceback_ms, format_ms, total_ms;
   int64_t reads, records, printed, cells, out_bytes;
   int64_t seed_overflow_strands, sw_generic_pairs;
   int64_t launches;   /* kernels this library launched for the call       */
@@ -86,6 +86,10 @@ const char *swift_last_error(const swift_ctx *ctx);
 /* Device facts the pipeline depends on: total device memory (it sizes the
  * Phase-2 batches, as in the reference) and the SM count. */
 int swift_ctx_info(const swift_ctx *ctx, int64_t *total_mem, int32_t *sm_count);
+/* Phase-2 kernel choice: 0 (default) packed score pass for the pairs it
+ * takes, then traceback of the printed pairs; 1 the generic kernel for
+ * every pair.  Both give identical output. */
+int swift_ctx_set_sw_path(swift_ctx *ctx, int32_t path);
 
 /* Builds the device-resident reference (file bytes, 2-bit codes) and SSAHA
  * index from a reference FASTA held in host memory. */

@@ -20,7 +20,7 @@ ERRORS = {-1: "argument", -2: "input", -3: "cuda", -4: "memory", -5: "limit", -6
 # Exported C symbols (kept in step with include/swift_gb300.h).
 EXPORTS = [
     "swift_params_default", "swift_ctx_create", "swift_ctx_destroy", "swift_last_error",
-    "swift_ctx_info",
+    "swift_ctx_info", "swift_ctx_set_sw_path",
     "swift_index_build", "swift_index_destroy", "swift_index_info", "swift_index_export",
     "swift_seed", "swift_sw_batch", "swift_align", "swift_reads_upload",
     "swift_reads_destroy", "swift_align_resident", "swift_fetch_output",
@@ -50,7 +50,8 @@ class Match(C.Structure):
 class Stats(C.Structure):
     _fields_ = [
         ("seed_ms", C.c_double), ("pairs_ms", C.c_double), ("sw_ms", C.c_double),
-        ("select_ms", C.c_double), ("format_ms", C.c_double), ("total_ms", C.c_double),
+        ("select_ms", C.c_double), ("traceback_ms", C.c_double), ("format_ms", C.c_double),
+        ("total_ms", C.c_double),
         ("reads", C.c_int64), ("records", C.c_int64), ("printed", C.c_int64),
         ("cells", C.c_int64), ("out_bytes", C.c_int64),
         ("seed_overflow_strands", C.c_int64), ("sw_generic_pairs", C.c_int64),
@@ -79,6 +80,7 @@ def lib():
         L.swift_last_error.argtypes = [vp]
         L.swift_last_error.restype = C.c_char_p
         L.swift_ctx_info.argtypes = [vp, C.POINTER(i64), C.POINTER(i32)]
+        L.swift_ctx_set_sw_path.argtypes = [vp, i32]
         L.swift_index_build.argtypes = [vp, C.c_char_p, sz, i32, i32, C.POINTER(vp)]
         L.swift_index_destroy.argtypes = [vp]
         L.swift_index_info.argtypes = [vp, vp, C.POINTER(i32), C.POINTER(i64), C.POINTER(i64)]
@@ -128,6 +130,10 @@ class Context:
         mem, sms = C.c_int64(), C.c_int32()
         self._check(lib().swift_ctx_info(self._h, C.byref(mem), C.byref(sms)))
         return dict(total_mem=mem.value, sm_count=sms.value)
+
+    def set_sw_path(self, path: int):
+        """0: packed score pass + traceback of printed pairs; 1: generic only."""
+        self._check(lib().swift_ctx_set_sw_path(self._h, path))
 
     def peak_dpx_cells_per_s(self) -> float:
         v = C.c_double()

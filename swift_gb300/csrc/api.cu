@@ -24,6 +24,7 @@ struct swift_ctx {
   cudaEvent_t ev[8] = {};
   char* d_text = nullptr;
   size_t text_len = 0, text_cap = 0;
+  bool force_generic = false;
 };
 
 struct swift_index {
@@ -130,6 +131,27 @@ __global__ void fill_matches_kernel(const int32_t* __restrict__ nbest, const int
       ++o;
     }
   }
+}
+
+// Splits pairs into the packed score pass and the generic kernel.
+__global__ void partition_pairs_kernel(const DevPair* __restrict__ pairs, int64_t n, int all_generic,
+                                       int32_t* fast, int32_t* n_fast, int32_t* gen,
+                                       int32_t* n_gen) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const bool g = all_generic || (pairs[i].flags & 1);
+  int32_t* list = g ? gen : fast;
+  int32_t* cnt = g ? n_gen : n_fast;
+  list[atomicAdd(cnt, 1)] = (int32_t)i;
+}
+
+// Printed pairs that went through the score pass need the traceback pass.
+__global__ void traceback_list_kernel(const DevPair* __restrict__ pairs,
+                                      const int32_t* __restrict__ keep, int64_t n, int all_generic,
+                                      int32_t* list, int32_t* cnt) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || all_generic) return;
+  if (keep[i] && !(pairs[i].flags & 1)) list[atomicAdd(cnt, 1)] = (int32_t)i;
 }
 
 __global__ void read_counts_kernel(const int32_t* __restrict__ nbest, int64_t n_reads,
@@ -360,6 +382,12 @@ int swift_ctx_destroy(swift_ctx* ctx) {
 }
 
 const char* swift_last_error(const swift_ctx* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+int swift_ctx_set_sw_path(swift_ctx* ctx, int32_t path) {
+  if (!ctx || path < 0 || path > 1) return SWIFT_E_ARG;
+  ctx->force_generic = path == 1;
+  return SWIFT_OK;
+}
 
 int swift_ctx_info(const swift_ctx* ctx, int64_t* total_mem, int32_t* sm_count) {
   if (!ctx) return SWIFT_E_ARG;
@@ -740,6 +768,25 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
   launch_build_pairs(st, pa);
   CKLAUNCH();
   CK(cudaEventRecord(ctx->ev[2], st));
+  // split: packed score pass (then traceback of the printed pairs) or the
+  // generic kernel (full result at once)
+  int bias = 0;
+  const bool fast_ok =
+      !ctx->force_generic && fast_params_ok(Q, kWin, p->match, p->mismatch, p->gap_open, p->gap_ext, &bias);
+  int32_t *fast_list, *gen_list, *tb_list, *cnt3, *cell;
+  CK(sc.get(&fast_list, nn));
+  CK(sc.get(&gen_list, nn));
+  CK(sc.get(&tb_list, nn));
+  CK(sc.get(&cnt3, 3));
+  CK(sc.get(&cell, nn));
+  CK(cudaMemsetAsync(cnt3, 0, 3 * sizeof(int32_t), st));
+  int launches = 0;
+  if (nproc > 0) {
+    partition_pairs_kernel<<<(unsigned)((nproc + 255) / 256), 256, 0, st>>>(
+        pairs, nproc, fast_ok ? 0 : 1, fast_list, cnt3, gen_list, cnt3 + 1);
+    CKLAUNCH();
+    ++launches;
+  }
   SwArgs sa;
   memset(&sa, 0, sizeof(sa));
   sa.q = qbuf;
@@ -757,9 +804,35 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
   sa.qcons = qcons;
   sa.rcons = rcons;
   sa.cons_stride = cs;
-  rc = launch_sw(st, sa, &ctx->err);
-  if (rc != SWIFT_OK) return rc;
-  CKLAUNCH();
+  if (fast_ok && nproc > 0) {
+    FastArgs fa2;
+    memset(&fa2, 0, sizeof(fa2));
+    fa2.q = qbuf;
+    fa2.w = wbuf;
+    fa2.q_stride = Qs;
+    fa2.w_stride = kWinPad;
+    fa2.Q = Q;
+    fa2.R = kWin;
+    fa2.match = p->match;
+    fa2.mismatch = p->mismatch;
+    fa2.gap_open = p->gap_open;
+    fa2.gap_ext = p->gap_ext;
+    fa2.bias = bias;
+    fa2.list = fast_list;
+    fa2.count = cnt3;
+    fa2.aln = aln;
+    fa2.cell = cell;
+    launches += launch_sw_score(st, fa2, nproc);
+    CKLAUNCH();
+  }
+  if (nproc > 0) {
+    sa.list = gen_list;
+    sa.count = cnt3 + 1;
+    rc = launch_sw(st, sa, &ctx->err);
+    if (rc != SWIFT_OK) return rc;
+    CKLAUNCH();
+    ++launches;
+  }
   CK(cudaEventRecord(ctx->ev[3], st));
   FormatArgs fa;
   memset(&fa, 0, sizeof(fa));
@@ -778,13 +851,28 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
   fa.offs = offs;
   launch_select(st, fa);
   CKLAUNCH();
+  launches += nproc > 0 ? 1 : 0;
+  CK(cudaEventRecord(ctx->ev[6], st));
+  if (fast_ok && nproc > 0) {
+    traceback_list_kernel<<<(unsigned)((nproc + 255) / 256), 256, 0, st>>>(pairs, keep, nproc, 0,
+                                                                           tb_list, cnt3 + 2);
+    CKLAUNCH();
+    sa.list = tb_list;
+    sa.count = cnt3 + 2;
+    rc = launch_sw(st, sa, &ctx->err);
+    if (rc != SWIFT_OK) return rc;
+    CKLAUNCH();
+    launches += 2;
+  }
   CK(cudaEventRecord(ctx->ev[4], st));
   launch_format_sizes(st, fa);
   CKLAUNCH();
   int scan_k = exclusive_scan_u64(st, bytes, offs, nproc, tmp, tot_d);
   CKLAUNCH();
   uint64_t total = 0;
+  int32_t h_cnt3[3] = {0, 0, 0};
   CK(cudaMemcpyAsync(&total, tot_d, 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(h_cnt3, cnt3, sizeof(h_cnt3), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   if (total + 1 > ctx->text_cap) {
     if (ctx->d_text) cudaFree(ctx->d_text);
@@ -808,8 +896,10 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
     s.pairs_ms = t;
     cudaEventElapsedTime(&t, ctx->ev[2], ctx->ev[3]);
     s.sw_ms = t;
-    cudaEventElapsedTime(&t, ctx->ev[3], ctx->ev[4]);
+    cudaEventElapsedTime(&t, ctx->ev[3], ctx->ev[6]);
     s.select_ms = t;
+    cudaEventElapsedTime(&t, ctx->ev[6], ctx->ev[4]);
+    s.traceback_ms = t;
     cudaEventElapsedTime(&t, ctx->ev[4], ctx->ev[5]);
     s.format_ms = t;
     cudaEventElapsedTime(&t, ctx->ev[0], ctx->ev[5]);
@@ -819,9 +909,11 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
     s.cells = nproc * (int64_t)Q * kWin;
     s.out_bytes = (int64_t)total;
     s.seed_overflow_strands = so.overflow;
-    s.printed = 0;
-    // build_pairs, sw, select, format sizes, scan, format write
-    s.launches = so.launches + (nproc > 0 ? 5 : 0) + scan_k;
+    s.printed = h_cnt3[2];
+    s.sw_generic_pairs = h_cnt3[1];
+    // build_pairs + the Smith-Waterman passes and select (launches) +
+    // format sizes, scan, format write
+    s.launches = so.launches + (nproc > 0 ? 1 + 2 : 0) + launches + scan_k;
     *stats = s;
   }
   return SWIFT_OK;

@@ -181,9 +181,27 @@ struct SwArgs {
   char* qcons;                // reversed consensus strings, stride cons_stride
   char* rcons;
   int64_t cons_stride;
-  int32_t* err;
+  const int32_t* list;        // optional: pair ids to process ...
+  const int32_t* count;       // ... and their number (device); grid sized by n
 };
 int launch_sw(cudaStream_t st, const SwArgs& a, std::string* err);
+
+// sw_fast.cu: score-only pass in packed 16-bit lanes
+struct FastArgs {
+  const char* q;
+  const char* w;
+  int64_t q_stride, w_stride;
+  int Q, R;
+  int match, mismatch, gap_open, gap_ext;
+  int bias;
+  const int32_t* list;        // pair ids
+  const int32_t* count;       // number of ids (device)
+  DevAln* aln;                // .score written
+  int32_t* cell;              // first maximum cell, row * (R + 1) + column
+};
+int fast_rows_per_lane(int Q);
+bool fast_params_ok(int Q, int R, int m, int x, int o, int e, int* bias);
+int launch_sw_score(cudaStream_t st, const FastArgs& a, int64_t max_pairs);
 int measure_dpx_peak(cudaStream_t st, int device, double* lane_instr_per_s);
 
 // out.cu

@@ -19,6 +19,11 @@ namespace {
 
 constexpr int kPairWarps = 8;
 
+__device__ __forceinline__ bool is_acgt(char c) {
+  const uint32_t u = (uint8_t)c & 0xDFu;
+  return u == 'A' || u == 'C' || u == 'G' || u == 'T';
+}
+
 __device__ __forceinline__ char comp_char(char c) {
   return c == 'A' ? 'T' : c == 'C' ? 'G' : c == 'G' ? 'C' : 'A';
 }
@@ -85,7 +90,12 @@ __global__ void __launch_bounds__(kPairWarps * 32) build_pairs_kernel(PairArgs a
   int wl = len - lead;
   if (wl < 0) wl = 0;
   char* wout = a.wbuf + j * kWinPad;
-  for (int i = lane; i < kWinPad; i += 32) wout[i] = i < wl ? tmp[lead + i] : '\0';
+  bool odd = false;  // a byte the packed score pass does not take
+  for (int i = lane; i < kWinPad; i += 32) {
+    const char c = i < wl ? tmp[lead + i] : '\0';
+    wout[i] = c;
+    if (i < wl && !is_acgt(c)) odd = true;
+  }
   // query
   const DevRead rd = a.rd[read];
   const char* s = a.reads + rd.seq_off;
@@ -103,7 +113,9 @@ __global__ void __launch_bounds__(kPairWarps * 32) build_pairs_kernel(PairArgs a
       }
     }
     qout[i] = c;
+    if (i < Q && !is_acgt(c)) odd = true;
   }
+  odd = __any_sync(0xffffffffu, odd) || wl != kWin;
   if (lane == 0) {
     DevPair pr;
     pr.read = read;
@@ -111,7 +123,7 @@ __global__ void __launch_bounds__(kPairWarps * 32) build_pairs_kernel(PairArgs a
     pr.ref_idx = ri;
     pr.ref_dist = dist;
     pr.win_len = wl;
-    pr.flags = 0;
+    pr.flags = odd ? 1 : 0;
     a.pairs[j] = pr;
   }
 }

@@ -45,8 +45,13 @@ __global__ void __launch_bounds__(kSwWarps * 32) sw_generic_kernel(SwArgs a, int
   using DW = typename DirWord<RPL>::T;
   extern __shared__ __align__(16) uint8_t smem[];
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t pair = (int64_t)blockIdx.x * kSwWarps + wib;
-  if (pair >= a.n) return;
+  int64_t pair = (int64_t)blockIdx.x * kSwWarps + wib;
+  if (a.list) {
+    if (pair >= *a.count) return;
+    pair = a.list[pair];
+  } else if (pair >= a.n) {
+    return;
+  }
   const int Q = a.Q, R = a.R;
   uint8_t* base = smem + (size_t)wib * per_warp_bytes;
   uint8_t* wsh = base;                                  // R bytes (rounded to 16)

@@ -331,3 +331,34 @@ def test_cli_matches_oracle(ctx, oracle, sg):
         got = open(op, "rb").read()
     want = oracle.align(ref, reads, oparams(ctx, oracle))
     assert got == want
+
+
+def test_packed_and_generic_paths_agree(ctx, oracle):
+    # the packed score pass + traceback of printed pairs must print exactly
+    # what the generic kernel prints for every pair
+    ref, reads = small_case(n_reads=3000, seed=101)
+    ix = ctx.index(ref)
+    fast, st = ctx.align(ix, reads, stats=True)
+    assert st["sw_generic_pairs"] < st["records"]  # the packed pass ran
+    ctx.set_sw_path(1)
+    try:
+        slow, st2 = ctx.align(ix, reads, stats=True)
+    finally:
+        ctx.set_sw_path(0)
+    assert st2["sw_generic_pairs"] == st2["records"]
+    assert fast == slow
+    assert fast == oracle.align(ref, reads, oparams(ctx, oracle))
+
+
+@pytest.mark.parametrize("Q", [20, 50, 64, 100, 128, 150, 199])
+def test_packed_path_query_lengths(ctx, oracle, sg, Q):
+    # every rows-per-lane variant of the packed score pass
+    from swift_gb300 import synth
+    names, seqs = synth.make_reference(100_000, 2, sigma=0.3, seed=300 + Q)
+    ref = synth.fasta_bytes(names, seqs)
+    rn, rs, _ = synth.make_reads(seqs, 400, Q, 0.02, 0.002, 0.05, seed=301 + Q)
+    reads = synth.reads_fasta(rn, rs)
+    ix = ctx.index(ref)
+    got = ctx.align(ix, reads)
+    want = oracle.align(ref, reads, oparams(ctx, oracle))
+    assert got == want, first_diff(got, want)
