@@ -773,12 +773,11 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
   int bias = 0;
   const bool fast_ok =
       !ctx->force_generic && fast_params_ok(Q, kWin, p->match, p->mismatch, p->gap_open, p->gap_ext, &bias);
-  int32_t *fast_list, *gen_list, *tb_list, *cnt3, *cell;
+  int32_t *fast_list, *gen_list, *tb_list, *cnt3;
   CK(sc.get(&fast_list, nn));
   CK(sc.get(&gen_list, nn));
   CK(sc.get(&tb_list, nn));
   CK(sc.get(&cnt3, 3));
-  CK(sc.get(&cell, nn));
   CK(cudaMemsetAsync(cnt3, 0, 3 * sizeof(int32_t), st));
   int launches = 0;
   if (nproc > 0) {
@@ -804,24 +803,26 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
   sa.qcons = qcons;
   sa.rcons = rcons;
   sa.cons_stride = cs;
+  FastArgs fa2;
+  memset(&fa2, 0, sizeof(fa2));
+  fa2.q = qbuf;
+  fa2.w = wbuf;
+  fa2.q_stride = Qs;
+  fa2.w_stride = kWinPad;
+  fa2.Q = Q;
+  fa2.R = kWin;
+  fa2.match = p->match;
+  fa2.mismatch = p->mismatch;
+  fa2.gap_open = p->gap_open;
+  fa2.gap_ext = p->gap_ext;
+  fa2.bias = bias;
+  fa2.aln = aln;
+  fa2.qcons = qcons;
+  fa2.rcons = rcons;
+  fa2.cons_stride = cs;
   if (fast_ok && nproc > 0) {
-    FastArgs fa2;
-    memset(&fa2, 0, sizeof(fa2));
-    fa2.q = qbuf;
-    fa2.w = wbuf;
-    fa2.q_stride = Qs;
-    fa2.w_stride = kWinPad;
-    fa2.Q = Q;
-    fa2.R = kWin;
-    fa2.match = p->match;
-    fa2.mismatch = p->mismatch;
-    fa2.gap_open = p->gap_open;
-    fa2.gap_ext = p->gap_ext;
-    fa2.bias = bias;
     fa2.list = fast_list;
     fa2.count = cnt3;
-    fa2.aln = aln;
-    fa2.cell = cell;
     launches += launch_sw_score(st, fa2, nproc);
     CKLAUNCH();
   }
@@ -853,16 +854,30 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
   CKLAUNCH();
   launches += nproc > 0 ? 1 : 0;
   CK(cudaEventRecord(ctx->ev[6], st));
+  int32_t h_cnt3[3] = {0, 0, 0};
   if (fast_ok && nproc > 0) {
     traceback_list_kernel<<<(unsigned)((nproc + 255) / 256), 256, 0, st>>>(pairs, keep, nproc, 0,
                                                                            tb_list, cnt3 + 2);
     CKLAUNCH();
-    sa.list = tb_list;
-    sa.count = cnt3 + 2;
-    rc = launch_sw(st, sa, &ctx->err);
-    if (rc != SWIFT_OK) return rc;
-    CKLAUNCH();
-    launches += 2;
+    ++launches;
+    CK(cudaMemcpyAsync(h_cnt3, cnt3, sizeof(h_cnt3), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    // trace pass in chunks that bound the direction scratch
+    const int64_t chunk = 262144;
+    const int64_t ntb = h_cnt3[2];
+    if (ntb > 0) {
+      const int64_t words = trace_scratch_words(Q, kWin, std::min(ntb, chunk));
+      uint32_t* dirs;
+      CK(sc.get(&dirs, (size_t)words));
+      fa2.list = tb_list;
+      fa2.count = cnt3 + 2;
+      fa2.dirs = dirs;
+      for (int64_t off = 0; off < ntb; off += chunk) {
+        fa2.list_offset = off;
+        launches += launch_sw_trace(st, fa2, std::min(chunk, ntb - off));
+        CKLAUNCH();
+      }
+    }
   }
   CK(cudaEventRecord(ctx->ev[4], st));
   launch_format_sizes(st, fa);
@@ -870,7 +885,6 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
   int scan_k = exclusive_scan_u64(st, bytes, offs, nproc, tmp, tot_d);
   CKLAUNCH();
   uint64_t total = 0;
-  int32_t h_cnt3[3] = {0, 0, 0};
   CK(cudaMemcpyAsync(&total, tot_d, 8, cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(h_cnt3, cnt3, sizeof(h_cnt3), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));

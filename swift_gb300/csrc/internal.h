@@ -186,7 +186,7 @@ struct SwArgs {
 };
 int launch_sw(cudaStream_t st, const SwArgs& a, std::string* err);
 
-// sw_fast.cu: score-only pass in packed 16-bit lanes
+// sw_fast.cu: packed 16-bit passes (score of every pair; trace of printed pairs)
 struct FastArgs {
   const char* q;
   const char* w;
@@ -196,12 +196,17 @@ struct FastArgs {
   int bias;
   const int32_t* list;        // pair ids
   const int32_t* count;       // number of ids (device)
-  DevAln* aln;                // .score written
-  int32_t* cell;              // first maximum cell, row * (R + 1) + column
+  int64_t list_offset;        // first id of this launch
+  DevAln* aln;                // score pass: .score; trace pass: all fields
+  uint32_t* dirs;             // trace pass: direction scratch
+  char* qcons;                // trace pass: reversed consensus strings
+  char* rcons;
+  int64_t cons_stride;
 };
-int fast_rows_per_lane(int Q);
 bool fast_params_ok(int Q, int R, int m, int x, int o, int e, int* bias);
+int64_t trace_scratch_words(int Q, int R, int64_t pairs);
 int launch_sw_score(cudaStream_t st, const FastArgs& a, int64_t max_pairs);
+int launch_sw_trace(cudaStream_t st, const FastArgs& a, int64_t max_pairs);
 int measure_dpx_peak(cudaStream_t st, int device, double* lane_instr_per_s);
 
 // out.cu

@@ -1,49 +1,53 @@
-// Phase 2, score pass: the maximum score and its first row-major cell for
-// every pair, in packed 16-bit lanes with the DPX add-max instructions.
+// Phase 2 in packed 16-bit lanes with the DPX add-max instructions.
+//
 // Same recurrence and tie rules as sw.cu (the reference kernel's,
-// src/smithWaterman.cu:510-645); traceback strings for the pairs that are
-// printed come from a second pass (sw.cu) after best-per-read selection.
+// src/smithWaterman.cu:510-645 and 911-1026).  Two kernels share the DP:
+//   score pass   (TRACE = false): the maximum score of every pair, for
+//                best-per-read selection;
+//   trace pass   (TRACE = true):  for the printed pairs, the first
+//                row-major maximum, 4-bit directions streamed to global
+//                scratch, and the reference's traceback walk.
 //
 // Encoding.  Each cell is kept as Hx = 16*H + code + B, where code is the
 // one-hot direction the reference would store (NONE 8, DIAG 4, UP 2,
-// LEFT 1) and B is a bias that keeps every candidate non-negative.  The
-// candidates enter a plain max as
+// LEFT 1) and B a bias that keeps every candidate non-negative.  The
+// candidates enter one max as
 //     DIAG: 16*(H[i-1][j-1] + s) + 4 + B
 //     UP:   16*(H[i-1][j] + pen) + 2 + B
 //     LEFT: 16*(H[i][j-1] + pen) + 1 + B
 //     NONE: 8 + B   (H = 0)
 // so the max yields H and, on equal H, the reference's precedence
-// NONE > DIAG > UP > LEFT of its strict '>' updates.  The gap penalty of a
-// neighbour is its gap_ext when the neighbour's own code is UP (for the
-// cell below) or LEFT (for the cell to the right), else gap_open; the bits
-// 2 and 1 of Hx give that directly:
-//     xU = (Hx & ~15) + (Hx & 2) * 8 (e - o)     -> UP candidate + const
-//     xL = (Hx & ~15) + (Hx & 1) * 16 (e - o)    -> LEFT candidate + const
+// NONE > DIAG > UP > LEFT of its strict '>' updates.  A neighbour's gap
+// penalty is gap_ext when its own code is UP (for the cell below) or LEFT
+// (for the cell to the right), else gap_open; bits 1 and 0 of Hx give that:
+//     xU = (Hx & ~15) + (Hx & 2) * 8 (e - o)     UP candidate  = xU + 16 o + 2
+//     xL = (Hx & ~15) + (Hx & 1) * 16 (e - o)    LEFT candidate = xL + 16 o + 1
 // Two pairs share one 32-bit register (low / high 16 bits).
 //
-// Layout.  A warp holds four pairs: each 16-lane half runs two pairs packed
-// in 16-bit halves.  Lane t of a half owns query rows t*RPL+1 .. t*RPL+RPL
-// and sweeps the window one column behind lane t-1 (anti-diagonal wavefront
-// of row strips); the bottom row's UP candidate and H pass down with two
-// shuffles per column.  The substitution score comes from a per-row profile
-// register pair selected by one byte-permute per cell.  The first maximum
-// of every row is tracked with a packed compare (16-bit integer patterns
-// compared as non-negative half floats, whose order they share) and two
-// selects.
+// Layout.  A warp holds 32/G groups of G lanes; each group runs two pairs
+// packed in the 16-bit halves.  Lane t of a group owns query rows
+// t*RPL+1 .. t*RPL+RPL and sweeps the window one column behind lane t-1 (an
+// anti-diagonal wavefront of row strips); the bottom row's UP candidate and
+// H pass down with two shuffles per column.  The substitution score comes
+// from a per-row profile register pair selected by one byte permute per
+// cell.  Rows past the query get an all-mismatch profile: with negative
+// mismatch and gap penalties their cells stay strictly below the maximum of
+// the rows above, so the score pass can keep a single running maximum per
+// lane.  The trace pass keeps the first maximum of every row (packed compare:
+// 16-bit integer patterns compared as non-negative half floats, whose order
+// they share, then two selects).
 //
-// Preconditions (checked by the caller; other pairs take sw.cu): query and
-// window bytes in {A,C,G,T,a,c,g,t}, window length = R (no NUL padding),
-// mismatch, gap_open, gap_ext < 0, gap_ext >= gap_open, |16*score+4| < 128,
-// 16 * match * Q + B < 31744.
-#include <cuda_fp16.h>
-
+// Preconditions (checked by fast_params_ok and per pair by the pair kernel;
+// other pairs take sw.cu): query and window bytes in {A,C,G,T,a,c,g,t},
+// window length = R, mismatch, gap_open, gap_ext < 0, gap_ext >= gap_open,
+// |16*score+4| < 128, 16 * match * Q + B stays below 0x7C00.
 #include "internal.h"
 
 namespace swift {
 namespace {
 
-constexpr int kFastWarps = 8;
-constexpr int kFastMaxR = 512;  // window columns the score pass takes
+constexpr int kPkWarps = 8;
+constexpr int kFastMaxR = 512;  // window columns the packed passes take
 
 __device__ __forceinline__ uint32_t base_class(uint32_t c) {
   uint32_t u = c & 0xDFu;
@@ -57,8 +61,7 @@ __device__ __forceinline__ uint32_t gt_mask(uint32_t a, uint32_t b) {
   return d;
 }
 
-// byte permute with sign replication (PTX prmt, default mode): selector
-// nibble bit 3 replicates the sign of the chosen byte
+// byte permute with sign replication (PTX prmt, default mode)
 __device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t s) {
   uint32_t d;
   asm("prmt.b32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(s));
@@ -66,29 +69,32 @@ __device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t s) {
 }
 
 __device__ __forceinline__ uint32_t sel(uint32_t m, uint32_t a, uint32_t b) {
-  // m ? a : b, bitwise
   return (a & m) | (b & ~m);
 }
 
-template <int RPL>
-__global__ void __launch_bounds__(kFastWarps * 32) sw_score_kernel(FastArgs a) {
-  __shared__ uint32_t wsel_all[kFastWarps * 2][kFastMaxR + 1];
+template <int G, int RPL, bool TRACE>
+__global__ void __launch_bounds__(kPkWarps * 32) sw_packed_kernel(FastArgs a) {
+  constexpr int kGroups = 32 / G;      // groups per warp
+  constexpr int kPairs = 2 * kGroups;  // pairs per warp
+  constexpr int kNW = (RPL + 3) / 4;   // direction words per lane per column
+  extern __shared__ uint32_t wsel_all[];  // [warps * groups][R + 1]
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int half = lane >> 4, sl = lane & 15;
-  const int64_t nlist = *a.count;
-  const int64_t base = ((int64_t)blockIdx.x * kFastWarps + wib) * 4 + 2 * half;
-  if (((int64_t)blockIdx.x * kFastWarps + wib) * 4 >= nlist) return;  // whole warp
+  const int g = lane / G, sl = lane % G;
+  const int64_t nlist = *a.count - a.list_offset;
+  const int64_t warp = (int64_t)blockIdx.x * kPkWarps + wib;
+  if (warp * kPairs >= nlist) return;  // whole warp
+  const int64_t base = warp * kPairs + 2 * g;
   const int Q = a.Q, R = a.R;
-  // the two pairs of this half-warp (a missing second pair repeats the first)
+  const int32_t* list = a.list + a.list_offset;
   const bool has0 = base < nlist, has1 = base + 1 < nlist;
-  const int32_t p0 = has0 ? a.list[base] : a.list[nlist - 1];
-  const int32_t p1 = has1 ? a.list[base + 1] : p0;
+  const int32_t p0 = has0 ? list[base] : list[nlist - 1];
+  const int32_t p1 = has1 ? list[base + 1] : p0;
   const char* q0 = a.q + (int64_t)p0 * a.q_stride;
   const char* q1 = a.q + (int64_t)p1 * a.q_stride;
   const char* w0 = a.w + (int64_t)p0 * a.w_stride;
   const char* w1 = a.w + (int64_t)p1 * a.w_stride;
-  uint32_t* wsel = wsel_all[wib * 2 + half];
-  for (int c = sl; c < R; c += 16) {
+  uint32_t* wsel = wsel_all + (wib * kGroups + g) * (R + 1);
+  for (int c = sl; c < R; c += G) {
     uint32_t s0 = base_class((uint8_t)w0[c]), s1 = base_class((uint8_t)w1[c]);
     wsel[c + 1] = s0 | ((s0 | 8u) << 4) | ((4u + s1) << 8) | (((4u + s1) | 8u) << 12);
   }
@@ -96,64 +102,100 @@ __global__ void __launch_bounds__(kFastWarps * 32) sw_score_kernel(FastArgs a) {
   const uint32_t B = (uint32_t)a.bias;
   const uint32_t BB = B | (B << 16);
   const uint32_t B8 = BB + 0x00080008u;
-  const uint32_t CU = (uint32_t)(uint16_t)(int16_t)(16 * a.gap_open + 2) * 0x00010001u;
-  const uint32_t CL = (uint32_t)(uint16_t)(int16_t)(16 * a.gap_open + 1) * 0x00010001u;
+  // per-half subtraction as one 32-bit add: every half it meets is at least
+  // B > |constant|, so no borrow crosses between the halves
+  const uint32_t CU = (uint32_t)((int32_t)(16 * a.gap_open + 2) * 65537);
+  const uint32_t CL = (uint32_t)((int32_t)(16 * a.gap_open + 1) * 65537);
   const uint32_t KU = (uint32_t)(8 * (a.gap_ext - a.gap_open));
   const uint32_t KL = (uint32_t)(16 * (a.gap_ext - a.gap_open));
   const uint32_t sm = (uint32_t)(uint8_t)(int8_t)(16 * a.match + 4);
   const uint32_t sx = (uint32_t)(uint8_t)(int8_t)(16 * a.mismatch + 4);
-  // per-row state
-  uint32_t prof0[RPL], prof1[RPL], h16p[RPL], xl[RPL], bestv[RPL], bestc[RPL];
+  const uint32_t all_x = sx * 0x01010101u;
+  uint32_t prof0[RPL], prof1[RPL], h16p[RPL], xl[RPL];
+  uint32_t bestv[TRACE ? RPL : 1], bestc[TRACE ? RPL : 1];
 #pragma unroll
   for (int k = 0; k < RPL; ++k) {
     const int i = sl * RPL + k;
-    uint32_t c0 = i < Q ? base_class((uint8_t)q0[i]) : 0u;
-    uint32_t c1 = i < Q ? base_class((uint8_t)q1[i]) : 0u;
-    uint32_t t0 = 0, t1 = 0;
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      t0 |= ((uint32_t)c == c0 ? sm : sx) << (8 * c);
-      t1 |= ((uint32_t)c == c1 ? sm : sx) << (8 * c);
+    if (i < Q) {
+      const uint32_t c0 = base_class((uint8_t)q0[i]), c1 = base_class((uint8_t)q1[i]);
+      prof0[k] = all_x ^ ((sm ^ sx) << (8 * c0));
+      prof1[k] = all_x ^ ((sm ^ sx) << (8 * c1));
+    } else {
+      prof0[k] = prof1[k] = all_x;  // past the query: mismatch everywhere
     }
-    prof0[k] = t0;
-    prof1[k] = t1;
-    h16p[k] = BB;          // H[i][0] = 0
-    xl[k] = BB;            // LEFT candidate base of column 0 (NONE)
-    bestv[k] = BB;
-    bestc[k] = 0;
+    h16p[k] = BB;  // H[i][0] = 0
+    xl[k] = BB;    // column 0 is NONE
+    if (TRACE) {
+      bestv[k] = BB;
+      bestc[k] = 0;
+    }
   }
+  if (!TRACE) bestv[0] = BB;
+  uint32_t* dirs = nullptr;
+  if (TRACE) dirs = a.dirs + (warp * kGroups + g) * (int64_t)(R + 1) * kNW * G;
   uint32_t send_u = BB, send_h = BB, diag = BB;
-  const int steps = R + 15;
+  const int steps = R + G - 1;
   for (int s = 0; s < steps; ++s) {
-    uint32_t up = __shfl_up_sync(0xffffffffu, send_u, 1, 16);
-    const uint32_t rh = __shfl_up_sync(0xffffffffu, send_h, 1, 16);
+    uint32_t up = __shfl_up_sync(0xffffffffu, send_u, 1, G);
+    const uint32_t rh = __shfl_up_sync(0xffffffffu, send_h, 1, G);
     if (sl == 0) up = BB;  // row 0: H = 0, NONE
     const int j = s - sl + 1;
     if (j >= 1 && j <= R) {
       const uint32_t ws = wsel[j];
       const uint32_t jj = (uint32_t)j * 0x00010001u;
       uint32_t dg = diag;
+      uint32_t hpair = 0;  // score pass: even row waiting for its odd partner
+      uint32_t acc[kNW];
+#pragma unroll
+      for (int w = 0; w < kNW; ++w) acc[w] = 0;
 #pragma unroll
       for (int k = 0; k < RPL; ++k) {
         const uint32_t sc = prmt(prof0[k], prof1[k], ws);
-        const uint32_t t1 = __viaddmax_s16x2(xl[k], CL, B8);
-        const uint32_t t2 = __viaddmax_s16x2(up, CU, t1);
-        const uint32_t hx = __viaddmax_s16x2(dg, sc, t2);
+        // LEFT and UP candidates (plain adds, issued on the FMA pipe), the
+        // NONE floor, then DIAG with the signed substitution score
+        const uint32_t m3 = __vimax3_s16x2(xl[k] + CL, up + CU, B8);
+        const uint32_t hx = __viaddmax_s16x2(dg, sc, m3);
         dg = h16p[k];
         const uint32_t h16 = hx & 0xFFF0FFF0u;
         h16p[k] = h16;
         up = (hx & 0x00020002u) * KU + h16;
         xl[k] = (hx & 0x00010001u) * KL + h16;
-        const uint32_t m = gt_mask(h16, bestv[k]);
-        bestv[k] = sel(m, h16, bestv[k]);
-        bestc[k] = sel(m, jj, bestc[k]);
+        if (TRACE) {
+          const uint32_t m = gt_mask(h16, bestv[k]);
+          bestv[k] = sel(m, h16, bestv[k]);
+          bestc[k] = sel(m, jj, bestc[k]);
+          acc[k >> 2] |= (hx & 0x000F000Fu) << (4 * (k & 3));
+        } else if (k & 1) {
+          bestv[0] = __vimax3_s16x2_relu(bestv[0], hpair, h16);
+        } else if (k == RPL - 1) {
+          bestv[0] = __vimax_s16x2_relu(bestv[0], h16);
+        } else {
+          hpair = h16;
+        }
+      }
+      if (TRACE) {
+#pragma unroll
+        for (int w = 0; w < kNW; ++w) dirs[((int64_t)j * kNW + w) * G + sl] = acc[w];
       }
       send_u = up;
       send_h = h16p[RPL - 1];
     }
     diag = sl == 0 ? BB : rh;
   }
+  if (!TRACE) {
+    // maximum of the group, per packed pair
+    uint32_t v = bestv[0];
+#pragma unroll
+    for (int d = G / 2; d > 0; d >>= 1) v = __vimax_s16x2_relu(v, __shfl_xor_sync(0xffffffffu, v, d, G));
+    if (sl == 0) {
+      const uint32_t v0 = v & 0xFFFFu, v1 = v >> 16;
+      if (has0) a.aln[p0].score = v0 > B ? (int)((v0 - B) >> 4) : 0;
+      if (has1) a.aln[p1].score = v1 > B ? (int)((v1 - B) >> 4) : 0;
+    }
+    return;
+  }
   // first maximum in row-major order, per packed pair
+  int32_t cellm[2] = {0, 0}, scorem[2] = {0, 0};
 #pragma unroll
   for (int hp = 0; hp < 2; ++hp) {
     const int sh = 16 * hp;
@@ -169,64 +211,143 @@ __global__ void __launch_bounds__(kFastWarps * 32) sw_score_kernel(FastArgs a) {
       }
     }
 #pragma unroll
-    for (int d = 8; d > 0; d >>= 1) {
-      uint32_t ov = __shfl_xor_sync(0xffffffffu, bv, d, 16);
-      uint32_t oc = __shfl_xor_sync(0xffffffffu, bc, d, 16);
-      uint32_t orr = __shfl_xor_sync(0xffffffffu, br, d, 16);
+    for (int d = G / 2; d > 0; d >>= 1) {
+      uint32_t ov = __shfl_xor_sync(0xffffffffu, bv, d, G);
+      uint32_t oc = __shfl_xor_sync(0xffffffffu, bc, d, G);
+      uint32_t orr = __shfl_xor_sync(0xffffffffu, br, d, G);
       if (ov > bv || (ov == bv && orr < br)) {
         bv = ov;
         bc = oc;
         br = orr;
       }
     }
-    const bool has = hp == 0 ? has0 : has1;
-    if (sl == 0 && has) {
-      const int32_t p = hp == 0 ? p0 : p1;
-      const int score = bv > B ? (int)((bv - B) >> 4) : 0;
-      a.aln[p].score = score;
-      a.cell[p] = score > 0 ? (int32_t)(br * (uint32_t)(R + 1) + bc) : 0;
-    }
+    scorem[hp] = bv > B ? (int)((bv - B) >> 4) : 0;
+    cellm[hp] = scorem[hp] > 0 ? (int32_t)(br * (uint32_t)(R + 1) + bc) : 0;
   }
+  __syncwarp();
+  __threadfence_block();
+  // traceback walk (src/smithWaterman.cu:911-1026): lane 0 of the group
+  // walks the low pair, lane 1 the high pair
+  if (sl > 1) return;
+  const int hp = sl;
+  if (!(hp == 0 ? has0 : has1)) return;
+  const int32_t p = hp == 0 ? p0 : p1;
+  const char* qg = hp == 0 ? q0 : q1;
+  const char* wg = hp == 0 ? w0 : w1;
+  const int W = R + 1;
+  const int shift_half = 16 * hp;
+  auto dir_at = [&](int cell) -> uint32_t {
+    // 8 NONE, 4 DIAG, 2 UP, 1 LEFT
+    const int i = cell / W, jj = cell % W;
+    if (i == 0 || jj == 0) return 8u;
+    const int ln = (i - 1) / RPL, k = (i - 1) % RPL;
+    const uint32_t word = dirs[((int64_t)jj * kNW + (k >> 2)) * G + ln];
+    return (word >> (shift_half + 4 * (k & 3))) & 0xFu;
+  };
+  char* qc = a.qcons + (int64_t)p * a.cons_stride;
+  char* rc = a.rcons + (int64_t)p * a.cons_stride;
+  int cur = cellm[hp], cr = cur / W, cc = cur % W, nxt;
+  uint32_t d0 = dir_at(cur);
+  nxt = d0 == 2u ? cur - W : d0 == 1u ? cur - 1 : d0 == 4u ? cur - W - 1 : cur;
+  int nr = nxt / W, nc = nxt % W;
+  int tick = -1, nref = -1, start = 0;
+  while ((cr != nr || cc != nc) && nc != 0 && nr != 0) {
+    ++tick;
+    if (nc == cc) rc[tick] = '-';
+    else { rc[tick] = wg[cc - 1]; ++nref; }
+    qc[tick] = nr == cr ? '-' : qg[cr - 1];
+    start = cc;
+    cur = nxt; cr = nr; cc = nc;
+    const uint32_t dd = dir_at(cur);
+    if (dd == 8u) break;
+    nxt = dd == 2u ? cur - W : dd == 1u ? cur - 1 : cur - W - 1;
+    nr = nxt / W; nc = nxt % W;
+  }
+  if ((cr != nr || cc != nc) && (nc == 0 || nr == 0)) {
+    ++tick;
+    if (nc == cc) rc[tick] = '-';
+    else { rc[tick] = wg[cc - 1]; ++nref; }
+    qc[tick] = nr == cr ? '-' : qg[cr - 1];
+    start = cc;
+  }
+  DevAln out;
+  out.score = scorem[hp];
+  out.start = start;
+  out.end = start + nref;
+  out.len = tick + 1;
+  a.aln[p] = out;
+}
+
+struct Shape {
+  int G, RPL;
+};
+
+// lanes per group and rows per lane for a query length (Q <= 256)
+Shape shape_for(int Q) {
+  if (Q <= 32) return {8, 4};
+  if (Q <= 64) return {8, 8};
+  if (Q <= 104) return {8, 13};
+  if (Q <= 128) return {8, 16};
+  if (Q <= 208) return {16, 13};
+  if (Q <= 256) return {16, 16};
+  return {0, 0};
+}
+
+template <bool TRACE>
+int launch_shape(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {
+  const Shape s = shape_for(a.Q);
+  if (s.G == 0 || max_pairs <= 0) return 0;
+  const int pairs_per_warp = 2 * (32 / s.G);
+  const int64_t warps = (max_pairs + pairs_per_warp - 1) / pairs_per_warp;
+  const unsigned grid = (unsigned)((warps + kPkWarps - 1) / kPkWarps);
+  const int tb = kPkWarps * 32;
+  const size_t smem = (size_t)kPkWarps * (32 / s.G) * (a.R + 1) * sizeof(uint32_t);
+#define SWIFT_PK(G_, R_)                                                  \
+  if (s.G == G_ && s.RPL == R_) {                                          \
+    if (smem > 48 * 1024)                                                  \
+      cudaFuncSetAttribute(sw_packed_kernel<G_, R_, TRACE>,                \
+                           cudaFuncAttributeMaxDynamicSharedMemorySize,    \
+                           (int)smem);                                     \
+    sw_packed_kernel<G_, R_, TRACE><<<grid, tb, smem, st>>>(a);            \
+    return 1;                                                              \
+  }
+  SWIFT_PK(8, 4)
+  SWIFT_PK(8, 8)
+  SWIFT_PK(8, 13)
+  SWIFT_PK(8, 16)
+  SWIFT_PK(16, 13)
+  SWIFT_PK(16, 16)
+#undef SWIFT_PK
+  return 0;
 }
 
 }  // namespace
 
-int fast_rows_per_lane(int Q) {
-  if (Q <= 32) return 2;
-  if (Q <= 64) return 4;
-  if (Q <= 112) return 7;
-  if (Q <= 128) return 8;
-  if (Q <= 192) return 12;
-  if (Q <= 256) return 16;
-  return 0;
-}
-
 bool fast_params_ok(int Q, int R, int m, int x, int o, int e, int* bias) {
-  if (R < 1 || R > kFastMaxR || fast_rows_per_lane(Q) == 0) return false;
+  if (R < 1 || R > kFastMaxR || shape_for(Q).G == 0) return false;
   if (!(x < 0 && o < 0 && e < 0 && e >= o && m > 0)) return false;
   if (16 * m + 4 > 127 || 16 * x + 4 < -128) return false;
   int b = -(16 * o + 1);
   b = (b + 15) & ~15;
   if (16 * (e - o) >= 2048) return false;
-  if (16 * m * Q + b + 16 * (e - o) + 16 >= 31744) return false;
+  if (16 * m * Q + b + 16 * (e - o) + 16 >= 0x7C00) return false;
   *bias = b;
   return true;
 }
 
+int64_t trace_scratch_words(int Q, int R, int64_t pairs) {
+  const Shape s = shape_for(Q);
+  if (s.G == 0) return 0;
+  const int64_t groups = (pairs + 1) / 2 + 32;  // round up to whole warps
+  return groups * (int64_t)(R + 1) * ((s.RPL + 3) / 4) * s.G;
+}
+
 int launch_sw_score(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {
-  if (max_pairs <= 0) return 0;
-  const int64_t warps = (max_pairs + 3) / 4;
-  const unsigned grid = (unsigned)((warps + kFastWarps - 1) / kFastWarps);
-  switch (fast_rows_per_lane(a.Q)) {
-    case 2: sw_score_kernel<2><<<grid, kFastWarps * 32, 0, st>>>(a); break;
-    case 4: sw_score_kernel<4><<<grid, kFastWarps * 32, 0, st>>>(a); break;
-    case 7: sw_score_kernel<7><<<grid, kFastWarps * 32, 0, st>>>(a); break;
-    case 8: sw_score_kernel<8><<<grid, kFastWarps * 32, 0, st>>>(a); break;
-    case 12: sw_score_kernel<12><<<grid, kFastWarps * 32, 0, st>>>(a); break;
-    case 16: sw_score_kernel<16><<<grid, kFastWarps * 32, 0, st>>>(a); break;
-    default: return 0;
-  }
-  return 1;
+  return launch_shape<false>(st, a, max_pairs);
+}
+
+int launch_sw_trace(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {
+  return launch_shape<true>(st, a, max_pairs);
 }
 
 }  // namespace swift

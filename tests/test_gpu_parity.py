@@ -142,7 +142,7 @@ def random_pairs(seed, n, Q, R, alphabet=b"ACGT"):
             q = mutate(rng, w[a:a + Q + 10])[:Q]
             q = q.ljust(Q, b"A")
         if kind == 2:  # window cut short: NUL padding
-            w = w[: rng.randint(Q // 2, R)]
+            w = w[: rng.randint(min(R, Q // 2), R)]
         if kind == 3:  # case and N
             w = bytes(((c | 0x20) if rng.random() < 0.3 else c) for c in w)
             q = bytes((ord("N") if rng.random() < 0.02 else c) for c in q)
