@@ -228,13 +228,18 @@ def main():
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         out_bytes = 0
+        host = []
         for _ in range(args.steps):
-            data = ctx.align(idx, pinned.data_ptr(), nbytes=len(reads))
+            data, est = ctx.align(idx, pinned.data_ptr(), nbytes=len(reads), stats=True)
             out_bytes = len(data)
+            host.append(est)
         torch.cuda.synchronize()
         e2e_s = time.perf_counter() - t0
         e2e = {"value": n * world * args.steps / e2e_s, "unit": "reads/s",
-               "h2d_bytes_per_step": len(reads), "d2h_bytes_per_step": out_bytes}
+               "h2d_bytes_per_step": len(reads), "d2h_bytes_per_step": out_bytes,
+               "ms_per_step": e2e_s * 1e3 / args.steps,
+               "host_ms": {k: statistics.median(h[k] for h in host)
+                           for k in ("host_parse_ms", "h2d_ms", "d2h_ms", "total_ms")}}
     if rank != 0:
         return 0
     cpu = None

@@ -74,6 +74,7 @@ typedef struct {
   int64_t reads, records, printed, cells, out_bytes;
   int64_t seed_overflow_strands, sw_generic_pairs;
   int64_t launches;   /* kernels this library launched for the call       */
+  double host_parse_ms, h2d_ms, d2h_ms;  /* swift_align only: host side    */
 } swift_stats;
 
 void swift_params_default(swift_params *p);

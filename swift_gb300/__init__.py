@@ -55,7 +55,8 @@ class Stats(C.Structure):
         ("reads", C.c_int64), ("records", C.c_int64), ("printed", C.c_int64),
         ("cells", C.c_int64), ("out_bytes", C.c_int64),
         ("seed_overflow_strands", C.c_int64), ("sw_generic_pairs", C.c_int64),
-        ("launches", C.c_int64),
+        ("launches", C.c_int64), ("host_parse_ms", C.c_double), ("h2d_ms", C.c_double),
+        ("d2h_ms", C.c_double),
     ]
 
     def as_dict(self):

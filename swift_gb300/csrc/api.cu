@@ -6,6 +6,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <string>
 #include <vector>
@@ -293,9 +294,15 @@ int run_seed(swift_ctx* ctx, const swift_index* idx, const swift_reads* rd, int 
   return SWIFT_OK;
 }
 
-int upload_reads(swift_ctx* ctx, const char* b, size_t len, swift_reads** out) {
+double ms_since(std::chrono::steady_clock::time_point t0) {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+int upload_reads(swift_ctx* ctx, const char* b, size_t len, swift_reads** out,
+                 double* parse_ms = nullptr, double* h2d_ms = nullptr) {
   swift_reads* r = new swift_reads();
   r->device = ctx->device;
+  auto t0 = std::chrono::steady_clock::now();
   int rc = parse_reads(b, len, &r->h, &ctx->err);
   if (rc != SWIFT_OK) {
     delete r;
@@ -310,6 +317,8 @@ int upload_reads(swift_ctx* ctx, const char* b, size_t len, swift_reads** out) {
     dr[i].len = r->h.len[i];
     dr[i].name_len = r->h.name_len[i];
   }
+  if (parse_ms) *parse_ms = ms_since(t0);
+  t0 = std::chrono::steady_clock::now();
   r->len = len;
   cudaError_t e = cudaMalloc(&r->d_bytes, len + 64);
   if (e == cudaSuccess) e = cudaMalloc(&r->d_rd, std::max<size_t>(n, 1) * sizeof(DevRead));
@@ -321,6 +330,7 @@ int upload_reads(swift_ctx* ctx, const char* b, size_t len, swift_reads** out) {
     swift_reads_destroy(r);
     return fail(ctx, SWIFT_E_CUDA, std::string("reads upload: ") + cudaGetErrorString(e));
   }
+  if (h2d_ms) *h2d_ms = ms_since(t0);
   *out = r;
   return SWIFT_OK;
 }
@@ -868,7 +878,10 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
     if (ntb > 0) {
       const int64_t words = trace_scratch_words(Q, kWin, std::min(ntb, chunk));
       uint32_t* dirs;
+      int2* best2;
       CK(sc.get(&dirs, (size_t)words));
+      CK(sc.get(&best2, nn));
+      fa2.best = best2;
       fa2.list = tb_list;
       fa2.count = cnt3 + 2;
       fa2.dirs = dirs;
@@ -945,10 +958,12 @@ int swift_align(swift_ctx* ctx, const swift_index* idx, const char* reads, size_
   if (!ctx || !idx || !reads || !p || !out || !out_len) return fail(ctx, SWIFT_E_ARG, "null argument");
   CK(cudaSetDevice(ctx->device));
   swift_reads* rd = nullptr;
-  int rc = upload_reads(ctx, reads, len, &rd);
+  double parse_ms = 0, h2d_ms = 0;
+  int rc = upload_reads(ctx, reads, len, &rd, &parse_ms, &h2d_ms);
   if (rc != SWIFT_OK) return rc;
   size_t n = 0;
   rc = swift_align_resident(ctx, idx, rd, p, &n, stats);
+  auto t0 = std::chrono::steady_clock::now();
   if (rc == SWIFT_OK) {
     char* h = (char*)malloc(n + 1);
     if (!h) {
@@ -964,6 +979,11 @@ int swift_align(swift_ctx* ctx, const swift_index* idx, const char* reads, size_
         *out_len = n;
       }
     }
+  }
+  if (stats) {
+    stats->host_parse_ms = parse_ms;
+    stats->h2d_ms = h2d_ms;
+    stats->d2h_ms = ms_since(t0);
   }
   swift_reads_destroy(rd);
   return rc;

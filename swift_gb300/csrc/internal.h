@@ -198,7 +198,9 @@ struct FastArgs {
   const int32_t* count;       // number of ids (device)
   int64_t list_offset;        // first id of this launch
   DevAln* aln;                // score pass: .score; trace pass: all fields
+  int2* best;                 // trace pass: (score, first maximum cell) per pair
   uint32_t* dirs;             // trace pass: direction scratch
+  int64_t chunk;              // trace pass: pairs of this launch
   char* qcons;                // trace pass: reversed consensus strings
   char* rcons;
   int64_t cons_stride;

@@ -5,8 +5,9 @@
 //   score pass   (TRACE = false): the maximum score of every pair, for
 //                best-per-read selection;
 //   trace pass   (TRACE = true):  for the printed pairs, the first
-//                row-major maximum, 4-bit directions streamed to global
-//                scratch, and the reference's traceback walk.
+//                row-major maximum and 4-bit directions streamed to global
+//                scratch; sw_walk_kernel then walks the reference's
+//                traceback, one thread per pair.
 //
 // Encoding.  Each cell is kept as Hx = 16*H + code + B, where code is the
 // one-hot direction the reference would store (NONE 8, DIAG 4, UP 2,
@@ -224,16 +225,31 @@ __global__ void __launch_bounds__(kPkWarps * 32) sw_packed_kernel(FastArgs a) {
     scorem[hp] = bv > B ? (int)((bv - B) >> 4) : 0;
     cellm[hp] = scorem[hp] > 0 ? (int32_t)(br * (uint32_t)(R + 1) + bc) : 0;
   }
-  __syncwarp();
-  __threadfence_block();
-  // traceback walk (src/smithWaterman.cu:911-1026): lane 0 of the group
-  // walks the low pair, lane 1 the high pair
-  if (sl > 1) return;
-  const int hp = sl;
-  if (!(hp == 0 ? has0 : has1)) return;
-  const int32_t p = hp == 0 ? p0 : p1;
-  const char* qg = hp == 0 ? q0 : q1;
-  const char* wg = hp == 0 ? w0 : w1;
+  if (sl < 2 && (sl == 0 ? has0 : has1)) {
+    const int32_t p = sl == 0 ? p0 : p1;
+    a.best[p] = make_int2(scorem[sl], cellm[sl]);
+  }
+}
+
+// Traceback walk (src/smithWaterman.cu:911-1026), one thread per printed
+// pair: dependent loads of the 4-bit directions the trace pass streamed out;
+// many walks in flight hide each other's latency.
+template <int G, int RPL>
+__global__ void __launch_bounds__(256) sw_walk_kernel(FastArgs a) {
+  constexpr int kGroups = 32 / G;
+  constexpr int kPairs = 2 * kGroups;
+  constexpr int kNW = (RPL + 3) / 4;
+  const int64_t nlist = *a.count - a.list_offset;
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= nlist || idx >= a.chunk) return;
+  const int32_t p = a.list[a.list_offset + idx];
+  const int64_t warp = idx / kPairs;
+  const int g = (int)((idx % kPairs) >> 1);
+  const int hp = (int)(idx & 1);
+  const int R = a.R;
+  const uint32_t* dirs = a.dirs + (warp * kGroups + g) * (int64_t)(R + 1) * kNW * G;
+  const char* qg = a.q + (int64_t)p * a.q_stride;
+  const char* wg = a.w + (int64_t)p * a.w_stride;
   const int W = R + 1;
   const int shift_half = 16 * hp;
   auto dir_at = [&](int cell) -> uint32_t {
@@ -241,12 +257,13 @@ __global__ void __launch_bounds__(kPkWarps * 32) sw_packed_kernel(FastArgs a) {
     const int i = cell / W, jj = cell % W;
     if (i == 0 || jj == 0) return 8u;
     const int ln = (i - 1) / RPL, k = (i - 1) % RPL;
-    const uint32_t word = dirs[((int64_t)jj * kNW + (k >> 2)) * G + ln];
+    const uint32_t word = __ldcg(&dirs[((int64_t)jj * kNW + (k >> 2)) * G + ln]);
     return (word >> (shift_half + 4 * (k & 3))) & 0xFu;
   };
   char* qc = a.qcons + (int64_t)p * a.cons_stride;
   char* rc = a.rcons + (int64_t)p * a.cons_stride;
-  int cur = cellm[hp], cr = cur / W, cc = cur % W, nxt;
+  const int2 b = a.best[p];
+  int cur = b.y, cr = cur / W, cc = cur % W, nxt;
   uint32_t d0 = dir_at(cur);
   nxt = d0 == 2u ? cur - W : d0 == 1u ? cur - 1 : d0 == 4u ? cur - W - 1 : cur;
   int nr = nxt / W, nc = nxt % W;
@@ -271,7 +288,7 @@ __global__ void __launch_bounds__(kPkWarps * 32) sw_packed_kernel(FastArgs a) {
     start = cc;
   }
   DevAln out;
-  out.score = scorem[hp];
+  out.score = b.x;
   out.start = start;
   out.end = start + nref;
   out.len = tick + 1;
@@ -321,6 +338,25 @@ int launch_shape(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {
   return 0;
 }
 
+int launch_walk(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {
+  const Shape s = shape_for(a.Q);
+  if (s.G == 0 || max_pairs <= 0) return 0;
+  const unsigned grid = (unsigned)((max_pairs + 255) / 256);
+#define SWIFT_WK(G_, R_)                                      \
+  if (s.G == G_ && s.RPL == R_) {                              \
+    sw_walk_kernel<G_, R_><<<grid, 256, 0, st>>>(a);           \
+    return 1;                                                  \
+  }
+  SWIFT_WK(8, 4)
+  SWIFT_WK(8, 8)
+  SWIFT_WK(8, 13)
+  SWIFT_WK(8, 16)
+  SWIFT_WK(16, 13)
+  SWIFT_WK(16, 16)
+#undef SWIFT_WK
+  return 0;
+}
+
 }  // namespace
 
 bool fast_params_ok(int Q, int R, int m, int x, int o, int e, int* bias) {
@@ -347,7 +383,10 @@ int launch_sw_score(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {
 }
 
 int launch_sw_trace(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {
-  return launch_shape<true>(st, a, max_pairs);
+  FastArgs b = a;
+  b.chunk = max_pairs;
+  int k = launch_shape<true>(st, b, max_pairs);
+  return k + launch_walk(st, b, max_pairs);
 }
 
 }  // namespace swift
