@@ -138,21 +138,37 @@ __global__ void fill_matches_kernel(const int32_t* __restrict__ nbest, const int
 __global__ void partition_pairs_kernel(const DevPair* __restrict__ pairs, int64_t n, int all_generic,
                                        int32_t* fast, int32_t* n_fast, int32_t* gen,
                                        int32_t* n_gen) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const bool g = all_generic || (pairs[i].flags & 1);
-  int32_t* list = g ? gen : fast;
-  int32_t* cnt = g ? n_gen : n_fast;
-  list[atomicAdd(cnt, 1)] = (int32_t)i;
+  // warp-aggregated appends: one atomic per warp and list
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const bool valid = i < n;
+  const bool g = valid && (all_generic || (pairs[i].flags & 1));
+  const bool f = valid && !g;
+  const uint32_t bg = __ballot_sync(0xffffffffu, g), bf = __ballot_sync(0xffffffffu, f);
+  int32_t base_g = 0, base_f = 0;
+  if (lane == 0) {
+    if (bg) base_g = atomicAdd(n_gen, __popc(bg));
+    if (bf) base_f = atomicAdd(n_fast, __popc(bf));
+  }
+  base_g = __shfl_sync(0xffffffffu, base_g, 0);
+  base_f = __shfl_sync(0xffffffffu, base_f, 0);
+  const uint32_t below = (1u << lane) - 1;
+  if (g) gen[base_g + __popc(bg & below)] = (int32_t)i;
+  if (f) fast[base_f + __popc(bf & below)] = (int32_t)i;
 }
 
 // Printed pairs that went through the score pass need the traceback pass.
 __global__ void traceback_list_kernel(const DevPair* __restrict__ pairs,
                                       const int32_t* __restrict__ keep, int64_t n, int all_generic,
                                       int32_t* list, int32_t* cnt) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n || all_generic) return;
-  if (keep[i] && !(pairs[i].flags & 1)) list[atomicAdd(cnt, 1)] = (int32_t)i;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const bool t = i < n && !all_generic && keep[i] && !(pairs[i].flags & 1);
+  const uint32_t b = __ballot_sync(0xffffffffu, t);
+  int32_t base = 0;
+  if (lane == 0 && b) base = atomicAdd(cnt, __popc(b));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (t) list[base + __popc(b & ((1u << lane) - 1))] = (int32_t)i;
 }
 
 __global__ void read_counts_kernel(const int32_t* __restrict__ nbest, int64_t n_reads,
@@ -739,7 +755,9 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
     nproc = (int64_t)(n_iter - 1) * per_iter + last;
   }
   const int Qs = (Q + 16) & ~15;
-  const int64_t cs = (int64_t)Q + kWin + 2;
+  // consensus stride: Q + R + 2 bytes, rounded to 16 so the walk kernel can
+  // store 32-bit words
+  const int64_t cs = ((int64_t)Q + kWin + 2 + 15) & ~(int64_t)15;
   const size_t nn = (size_t)std::max<int64_t>(nproc, 1);
   DevPair* pairs;
   char *qbuf, *wbuf, *qcons, *rcons;
@@ -887,7 +905,9 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
       fa2.dirs = dirs;
       for (int64_t off = 0; off < ntb; off += chunk) {
         fa2.list_offset = off;
-        launches += launch_sw_trace(st, fa2, std::min(chunk, ntb - off));
+        const int k = launch_sw_trace(st, fa2, std::min(chunk, ntb - off));
+        if (k == 0) return fail(ctx, SWIFT_E_DEVICE, "trace pass could not launch");
+        launches += k;
         CKLAUNCH();
       }
     }

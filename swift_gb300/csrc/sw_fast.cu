@@ -133,7 +133,7 @@ __global__ void __launch_bounds__(kPkWarps * 32) sw_packed_kernel(FastArgs a) {
   }
   if (!TRACE) bestv[0] = BB;
   uint32_t* dirs = nullptr;
-  if (TRACE) dirs = a.dirs + (warp * kGroups + g) * (int64_t)(R + 1) * kNW * G;
+  if (TRACE) dirs = a.dirs + (warp * kGroups + g) * (int64_t)(R + G - 1) * kNW * G;
   uint32_t send_u = BB, send_h = BB, diag = BB;
   const int steps = R + G - 1;
   for (int s = 0; s < steps; ++s) {
@@ -175,8 +175,10 @@ __global__ void __launch_bounds__(kPkWarps * 32) sw_packed_kernel(FastArgs a) {
         }
       }
       if (TRACE) {
+        // indexed by wavefront step so the G lanes of a group store one
+        // contiguous run (lane t holds column s - t + 1)
 #pragma unroll
-        for (int w = 0; w < kNW; ++w) dirs[((int64_t)j * kNW + w) * G + sl] = acc[w];
+        for (int w = 0; w < kNW; ++w) __stcg(&dirs[((int64_t)s * kNW + w) * G + sl], acc[w]);
       }
       send_u = up;
       send_h = h16p[RPL - 1];
@@ -247,7 +249,7 @@ __global__ void __launch_bounds__(256) sw_walk_kernel(FastArgs a) {
   const int g = (int)((idx % kPairs) >> 1);
   const int hp = (int)(idx & 1);
   const int R = a.R;
-  const uint32_t* dirs = a.dirs + (warp * kGroups + g) * (int64_t)(R + 1) * kNW * G;
+  const uint32_t* dirs = a.dirs + (warp * kGroups + g) * (int64_t)(R + G - 1) * kNW * G;
   const char* qg = a.q + (int64_t)p * a.q_stride;
   const char* wg = a.w + (int64_t)p * a.w_stride;
   const int W = R + 1;
@@ -257,11 +259,24 @@ __global__ void __launch_bounds__(256) sw_walk_kernel(FastArgs a) {
     const int i = cell / W, jj = cell % W;
     if (i == 0 || jj == 0) return 8u;
     const int ln = (i - 1) / RPL, k = (i - 1) % RPL;
-    const uint32_t word = __ldcg(&dirs[((int64_t)jj * kNW + (k >> 2)) * G + ln]);
+    const int step = jj + ln - 1;
+    const uint32_t word = __ldcg(&dirs[((int64_t)step * kNW + (k >> 2)) * G + ln]);
     return (word >> (shift_half + 4 * (k & 3))) & 0xFu;
   };
-  char* qc = a.qcons + (int64_t)p * a.cons_stride;
-  char* rc = a.rcons + (int64_t)p * a.cons_stride;
+  // consensus bytes are gathered four at a time and stored as words
+  uint32_t* qcw = reinterpret_cast<uint32_t*>(a.qcons + (int64_t)p * a.cons_stride);
+  uint32_t* rcw = reinterpret_cast<uint32_t*>(a.rcons + (int64_t)p * a.cons_stride);
+  uint32_t qacc = 0, racc = 0;
+  auto emit = [&](int tick, char r, char q) {
+    const int sh = 8 * (tick & 3);
+    racc |= (uint32_t)(uint8_t)r << sh;
+    qacc |= (uint32_t)(uint8_t)q << sh;
+    if ((tick & 3) == 3) {
+      rcw[tick >> 2] = racc;
+      qcw[tick >> 2] = qacc;
+      racc = qacc = 0;
+    }
+  };
   const int2 b = a.best[p];
   int cur = b.y, cr = cur / W, cc = cur % W, nxt;
   uint32_t d0 = dir_at(cur);
@@ -270,9 +285,9 @@ __global__ void __launch_bounds__(256) sw_walk_kernel(FastArgs a) {
   int tick = -1, nref = -1, start = 0;
   while ((cr != nr || cc != nc) && nc != 0 && nr != 0) {
     ++tick;
-    if (nc == cc) rc[tick] = '-';
-    else { rc[tick] = wg[cc - 1]; ++nref; }
-    qc[tick] = nr == cr ? '-' : qg[cr - 1];
+    char rch = '-';
+    if (nc != cc) { rch = wg[cc - 1]; ++nref; }
+    emit(tick, rch, nr == cr ? '-' : qg[cr - 1]);
     start = cc;
     cur = nxt; cr = nr; cc = nc;
     const uint32_t dd = dir_at(cur);
@@ -282,10 +297,14 @@ __global__ void __launch_bounds__(256) sw_walk_kernel(FastArgs a) {
   }
   if ((cr != nr || cc != nc) && (nc == 0 || nr == 0)) {
     ++tick;
-    if (nc == cc) rc[tick] = '-';
-    else { rc[tick] = wg[cc - 1]; ++nref; }
-    qc[tick] = nr == cr ? '-' : qg[cr - 1];
+    char rch = '-';
+    if (nc != cc) { rch = wg[cc - 1]; ++nref; }
+    emit(tick, rch, nr == cr ? '-' : qg[cr - 1]);
     start = cc;
+  }
+  if (tick >= 0 && (tick & 3) != 3) {
+    rcw[tick >> 2] = racc;
+    qcw[tick >> 2] = qacc;
   }
   DevAln out;
   out.score = b.x;
@@ -375,7 +394,7 @@ int64_t trace_scratch_words(int Q, int R, int64_t pairs) {
   const Shape s = shape_for(Q);
   if (s.G == 0) return 0;
   const int64_t groups = (pairs + 1) / 2 + 32;  // round up to whole warps
-  return groups * (int64_t)(R + 1) * ((s.RPL + 3) / 4) * s.G;
+  return groups * (int64_t)(R + s.G - 1) * ((s.RPL + 3) / 4) * s.G;
 }
 
 int launch_sw_score(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {
@@ -383,6 +402,7 @@ int launch_sw_score(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {
 }
 
 int launch_sw_trace(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {
+  if (a.cons_stride % 4 != 0) return 0;  // the walk stores 32-bit words
   FastArgs b = a;
   b.chunk = max_pairs;
   int k = launch_shape<true>(st, b, max_pairs);
