@@ -223,15 +223,17 @@ def main():
     if not args.no_e2e:
         pinned = torch.empty(len(reads), dtype=torch.uint8, pin_memory=True)
         pinned.numpy()[:] = memoryview(reads)
+        cap = int(out_n * 1.1) + (1 << 20)
+        out_pinned = torch.empty(cap, dtype=torch.uint8, pin_memory=True)
         for _ in range(2):
-            ctx.align(idx, pinned.data_ptr(), nbytes=len(reads))
+            ctx.align_into(idx, pinned.data_ptr(), len(reads), out_pinned.data_ptr(), cap)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         out_bytes = 0
         host = []
         for _ in range(args.steps):
-            data, est = ctx.align(idx, pinned.data_ptr(), nbytes=len(reads), stats=True)
-            out_bytes = len(data)
+            out_bytes, est = ctx.align_into(idx, pinned.data_ptr(), len(reads),
+                                            out_pinned.data_ptr(), cap)
             host.append(est)
         torch.cuda.synchronize()
         e2e_s = time.perf_counter() - t0

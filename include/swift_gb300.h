@@ -131,6 +131,13 @@ int swift_align(swift_ctx *ctx, const swift_index *idx, const char *reads_fasta,
                 size_t len, const swift_params *p, char **out, size_t *out_len,
                 swift_stats *stats);
 
+/* swift_align writing the text into a caller buffer (for example pinned
+ * host memory, for the fastest copy).  If cap is too small nothing is
+ * copied, *out_len receives the size needed and SWIFT_E_LIMIT is returned. */
+int swift_align_into(swift_ctx *ctx, const swift_index *idx, const char *reads_fasta,
+                     size_t len, const swift_params *p, char *out, size_t cap,
+                     size_t *out_len, swift_stats *stats);
+
 /* Resident form for serving and benchmarking: reads parsed and kept on the
  * device; the output text stays on the device until fetched. */
 typedef struct swift_reads swift_reads;

@@ -24,7 +24,7 @@ EXPORTS = [
     "swift_index_build", "swift_index_destroy", "swift_index_info", "swift_index_export",
     "swift_seed", "swift_sw_batch", "swift_align", "swift_reads_upload",
     "swift_reads_destroy", "swift_align_resident", "swift_fetch_output",
-    "swift_align_files", "swift_free", "swift_peak_dpx",
+    "swift_align_files", "swift_free", "swift_peak_dpx", "swift_align_into",
 ]
 
 
@@ -91,6 +91,8 @@ def lib():
                                      vp, vp, vp, vp, vp, vp]
         L.swift_align.argtypes = [vp, vp, vp, sz, C.POINTER(Params), C.POINTER(vp),
                                   C.POINTER(sz), C.POINTER(Stats)]
+        L.swift_align_into.argtypes = [vp, vp, vp, sz, C.POINTER(Params), vp, sz, C.POINTER(sz),
+                                       C.POINTER(Stats)]
         L.swift_reads_upload.argtypes = [vp, C.c_char_p, sz, C.POINTER(vp)]
         L.swift_reads_destroy.argtypes = [vp]
         L.swift_align_resident.argtypes = [vp, vp, vp, C.POINTER(Params), C.POINTER(sz),
@@ -211,6 +213,18 @@ class Context:
         data = C.string_at(out, n.value) if n.value else b""
         lib().swift_free(out)
         return (data, st.as_dict()) if stats else data
+
+    def align_into(self, index: "Index", reads_ptr: int, nbytes: int, out_ptr: int, cap: int,
+                   params: Params | None = None):
+        """Pipeline with host input and output buffers given by address (for
+        example pinned memory); returns (bytes written, stats)."""
+        p = params or default_params(seed_len=index.seed_len, ignore_thres=index.ignore_thres)
+        n = C.c_size_t()
+        st = Stats()
+        self._check(lib().swift_align_into(self._h, index._h, C.c_void_p(reads_ptr), nbytes,
+                                           C.byref(p), C.c_void_p(out_ptr), cap, C.byref(n),
+                                           C.byref(st)))
+        return n.value, st.as_dict()
 
     def align_resident(self, index: "Index", reads: "Reads", params: Params | None = None):
         p = params or default_params(seed_len=index.seed_len, ignore_thres=index.ignore_thres)

@@ -50,7 +50,10 @@ struct swift_reads {
   char* d_bytes = nullptr;
   uint64_t len = 0;
   DevRead* d_rd = nullptr;
-  HostReads h;
+  int64_t n = 0;          // reads
+  int64_t n_gt = 0;       // '>' bytes (getSeqCount)
+  int32_t first_len = 0;  // getSeqSize
+  int32_t min_len = 0, max_len = 0;
   std::vector<int32_t> repeats;
 };
 
@@ -199,7 +202,7 @@ struct SeedOut {
 // Phase 1 for resident reads: fills the match arrays (allocated in sc).
 int run_seed(swift_ctx* ctx, const swift_index* idx, const swift_reads* rd, int max_hits,
              Scratch& sc, SeedOut* out) {
-  const int64_t n = (int64_t)rd->h.len.size();
+  const int64_t n = rd->n;
   const int64_t ns = 2 * n;
   cudaStream_t st = ctx->st;
   int3* best;
@@ -316,37 +319,74 @@ double ms_since(std::chrono::steady_clock::time_point t0) {
 
 int upload_reads(swift_ctx* ctx, const char* b, size_t len, swift_reads** out,
                  double* parse_ms = nullptr, double* h2d_ms = nullptr) {
+  // bytes to the device, then the record structure found there (parse.cu)
+  cudaStream_t st = ctx->st;
   swift_reads* r = new swift_reads();
   r->device = ctx->device;
-  auto t0 = std::chrono::steady_clock::now();
-  int rc = parse_reads(b, len, &r->h, &ctx->err);
-  if (rc != SWIFT_OK) {
-    delete r;
-    return rc;
-  }
-  r->repeats = phase1_stale_repeats((int64_t)r->h.len.size(), r->h.n_gt);
-  const size_t n = r->h.len.size();
-  std::vector<DevRead> dr(n);
-  for (size_t i = 0; i < n; ++i) {
-    dr[i].name_off = r->h.name_off[i];
-    dr[i].seq_off = r->h.seq_off[i];
-    dr[i].len = r->h.len[i];
-    dr[i].name_len = r->h.name_len[i];
-  }
-  if (parse_ms) *parse_ms = ms_since(t0);
-  t0 = std::chrono::steady_clock::now();
   r->len = len;
-  cudaError_t e = cudaMalloc(&r->d_bytes, len + 64);
-  if (e == cudaSuccess) e = cudaMalloc(&r->d_rd, std::max<size_t>(n, 1) * sizeof(DevRead));
-  if (e == cudaSuccess) e = cudaMemcpyAsync(r->d_bytes, b, len, cudaMemcpyHostToDevice, ctx->st);
-  if (e == cudaSuccess && n)
-    e = cudaMemcpyAsync(r->d_rd, dr.data(), n * sizeof(DevRead), cudaMemcpyHostToDevice, ctx->st);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->st);
-  if (e != cudaSuccess) {
+  auto t0 = std::chrono::steady_clock::now();
+  auto bail = [&](int code, const std::string& m) {
     swift_reads_destroy(r);
-    return fail(ctx, SWIFT_E_CUDA, std::string("reads upload: ") + cudaGetErrorString(e));
-  }
+    return fail(ctx, code, m);
+  };
+#define CKR(call)                                                                         \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess) return bail(SWIFT_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+  CKR(cudaMalloc(&r->d_bytes, len + 64));
+  CKR(cudaMemcpyAsync(r->d_bytes, b, len, cudaMemcpyHostToDevice, st));
+  CKR(cudaStreamSynchronize(st));
   if (h2d_ms) *h2d_ms = ms_since(t0);
+  t0 = std::chrono::steady_clock::now();
+  {
+    Scratch sc(st);
+    const uint64_t tiles = parse_tiles(len);
+    uint32_t *cnt, *off, *n_nl_d;
+    unsigned long long* err;
+    ParseSummary* sum;
+    void* tmp;
+    CKR(sc.get(&cnt, std::max<uint64_t>(tiles, 1)));
+    CKR(sc.get(&off, std::max<uint64_t>(tiles, 1)));
+    CKR(sc.get(&n_nl_d, 1));
+    CKR(sc.get(&err, 1));
+    CKR(sc.get(&sum, 1));
+    CKR(sc.get((uint8_t**)&tmp, scan_temp_bytes((int64_t)tiles)));
+    const ParseSummary init = {INT32_MAX, 0, 0, 0};
+    CKR(cudaMemcpyAsync(sum, &init, sizeof(init), cudaMemcpyHostToDevice, st));
+    CKR(cudaMemsetAsync(err, 0xFF, sizeof(unsigned long long), st));
+    launch_parse_tiles(st, r->d_bytes, len, cnt, err);
+    exclusive_scan_u32(st, cnt, off, (int64_t)tiles, tmp, n_nl_d);
+    CKR(cudaGetLastError());
+    uint32_t n_nl = 0;
+    CKR(cudaMemcpyAsync(&n_nl, n_nl_d, 4, cudaMemcpyDeviceToHost, st));
+    CKR(cudaStreamSynchronize(st));
+    const uint64_t n_lines = n_nl + ((len > 0 && b[len - 1] != '\n') ? 1 : 0);
+    uint64_t* nl;
+    CKR(sc.get(&nl, std::max<uint64_t>(n_nl, 1)));
+    CKR(cudaMalloc(&r->d_rd, std::max<uint64_t>(n_lines / 2, 1) * sizeof(DevRead)));
+    launch_parse_newlines(st, r->d_bytes, len, off, nl);
+    launch_parse_lines(st, r->d_bytes, len, nl, n_nl, n_lines, r->d_rd, sum, err);
+    CKR(cudaGetLastError());
+    unsigned long long h_err = 0;
+    ParseSummary h_sum;
+    CKR(cudaMemcpyAsync(&h_err, err, sizeof(h_err), cudaMemcpyDeviceToHost, st));
+    CKR(cudaMemcpyAsync(&h_sum, sum, sizeof(h_sum), cudaMemcpyDeviceToHost, st));
+    CKR(cudaStreamSynchronize(st));
+    if (h_err != ~0ull) {
+      std::string m;
+      const int code = parse_error((uint32_t)(h_err & 0xFF), h_err >> 8, &m);
+      return bail(code, m);
+    }
+    r->n = (int64_t)(n_lines / 2);
+    r->n_gt = (int64_t)((n_lines + 1) / 2);  // '>' occurs only at header starts
+    r->first_len = h_sum.first_len;
+    r->min_len = r->n ? h_sum.min_len : 0;
+    r->max_len = h_sum.max_len;
+  }
+#undef CKR
+  r->repeats = phase1_stale_repeats(r->n, r->n_gt);
+  if (parse_ms) *parse_ms = ms_since(t0);
   *out = r;
   return SWIFT_OK;
 }
@@ -729,9 +769,9 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
   if (p->seed_len != idx->k || p->ignore_thres != idx->thres)
     return fail(ctx, SWIFT_E_ARG, "parameters differ from the index's seed length / threshold");
   if (p->max_hits < 1 || p->max_hits > 64) return fail(ctx, SWIFT_E_ARG, "max_hits outside 1..64");
-  const int Q = p->qry_len > 0 ? p->qry_len : rd->h.first_len;
+  const int Q = p->qry_len > 0 ? p->qry_len : rd->first_len;
   if (Q < 1 || Q > kMaxQ) return fail(ctx, SWIFT_E_LIMIT, "query length outside 1..256");
-  if (!rd->h.len.empty() && rd->h.min_len < Q)
+  if (rd->n > 0 && rd->min_len < Q)
     return fail(ctx, SWIFT_E_INPUT,
                 "a read is shorter than the query length; the reference aligns such reads "
                 "against stale buffer contents");
@@ -951,7 +991,7 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
     s.format_ms = t;
     cudaEventElapsedTime(&t, ctx->ev[0], ctx->ev[5]);
     s.total_ms = t;
-    s.reads = (int64_t)rd->h.len.size();
+    s.reads = rd->n;
     s.records = nm;
     s.cells = nproc * (int64_t)Q * kWin;
     s.out_bytes = (int64_t)total;
@@ -998,6 +1038,37 @@ int swift_align(swift_ctx* ctx, const swift_index* idx, const char* reads, size_
         *out = h;
         *out_len = n;
       }
+    }
+  }
+  if (stats) {
+    stats->host_parse_ms = parse_ms;
+    stats->h2d_ms = h2d_ms;
+    stats->d2h_ms = ms_since(t0);
+  }
+  swift_reads_destroy(rd);
+  return rc;
+}
+
+int swift_align_into(swift_ctx* ctx, const swift_index* idx, const char* reads, size_t len,
+                     const swift_params* p, char* out, size_t cap, size_t* out_len,
+                     swift_stats* stats) {
+  if (!ctx || !idx || !reads || !p || !out_len) return fail(ctx, SWIFT_E_ARG, "null argument");
+  CK(cudaSetDevice(ctx->device));
+  swift_reads* rd = nullptr;
+  double parse_ms = 0, h2d_ms = 0;
+  int rc = upload_reads(ctx, reads, len, &rd, &parse_ms, &h2d_ms);
+  if (rc != SWIFT_OK) return rc;
+  size_t n = 0;
+  rc = swift_align_resident(ctx, idx, rd, p, &n, stats);
+  auto t0 = std::chrono::steady_clock::now();
+  if (rc == SWIFT_OK) {
+    *out_len = n;
+    if (n > cap) {
+      rc = fail(ctx, SWIFT_E_LIMIT, "output buffer too small");
+    } else if (n) {
+      cudaError_t e = cudaMemcpyAsync(out, ctx->d_text, n, cudaMemcpyDeviceToHost, ctx->st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->st);
+      if (e != cudaSuccess) rc = fail(ctx, SWIFT_E_CUDA, cudaGetErrorString(e));
     }
   }
   if (stats) {

@@ -1,12 +1,10 @@
-// Host-side structural parse of the two FASTA inputs, with the reference's
-// reading rules:
-//   reference: refMapCreate (src/refMap.cu:59-117) for name/sequence offsets
-//              and bases-per-line; lookupTable5Create (src/lookupTable5.cu:
-//              127-187) for the concatenated sequence its tuples come from;
-//   reads:     qryGetNext2 (src/query.cu:174-213), getSeqCount and
-//              getSeqSize (src/input.cu:475-524).
-// The parse only records offsets; sequence bytes stay where they are and are
-// copied to the device as one block.
+// Host-side structural parse of the reference FASTA (once per index), with
+// the reference's reading rules: refMapCreate (src/refMap.cu:59-117) for
+// name/sequence offsets and bases-per-line; lookupTable5Create
+// (src/lookupTable5.cu:127-187) for the concatenated sequence its tuples come
+// from.  The parse only records offsets; sequence bytes stay where they are
+// and are copied to the device as one block.  (Reads are parsed on the
+// device, parse.cu.)  Also the two batch schedules of the reference drivers.
 #include <string.h>
 
 #include <cmath>
@@ -119,72 +117,6 @@ int parse_reference(const char* b, size_t n, HostRef* out, std::string* err) {
     *err = "reference: no sequence header";
     return SWIFT_E_INPUT;
   }
-  return SWIFT_OK;
-}
-
-int parse_reads(const char* b, size_t n, HostReads* out, std::string* err) {
-  HostReads& rd = *out;
-  rd = HostReads();
-  size_t est = n / 64 + 16;
-  rd.name_off.reserve(est);
-  rd.seq_off.reserve(est);
-  rd.len.reserve(est);
-  rd.name_len.reserve(est);
-  size_t pos = 0, c;
-  bool have_header = false;
-  uint64_t cur_name_off = 0;
-  int32_t cur_name_len = 0;
-  int32_t mn = 1 << 30, mx = 0;
-  while ((c = chunk_at(b, n, pos)) > 0) {
-    const char* line = b + pos;
-    long ll = (long)c - (line[c - 1] == '\n');
-    if (ll == 0) {
-      *err = "reads: empty line at offset " + std::to_string(pos) +
-             " (the reference reader loops forever on it)";
-      return SWIFT_E_INPUT;
-    }
-    if (line[0] == '>') {
-      if (!bytes_ok(line, (size_t)ll, true, err, "reads", pos)) return SWIFT_E_INPUT;
-      if (have_header) {
-        *err = "reads: header without a sequence line at offset " + std::to_string(cur_name_off);
-        return SWIFT_E_INPUT;
-      }
-      if (ll - 1 > kNameMax - 2) {
-        *err = "reads: read name longer than 48 characters";
-        return SWIFT_E_LIMIT;
-      }
-      cur_name_off = pos + c - (size_t)ll - 1;
-      cur_name_len = (int32_t)(ll - 1);
-      have_header = true;
-      ++rd.n_gt;
-    } else {
-      if (!have_header) {
-        *err = "reads: sequence line without a header at offset " + std::to_string(pos) +
-               " (multi-line reads are not supported)";
-        return SWIFT_E_INPUT;
-      }
-      if (!bytes_ok(line, (size_t)ll, false, err, "reads", pos)) return SWIFT_E_INPUT;
-      if (ll > kReadMax) {
-        *err = "reads: read longer than 199 bases (the reference's query buffer)";
-        return SWIFT_E_LIMIT;
-      }
-      if (rd.len.empty()) rd.first_len = (int32_t)c - 1;  // strlen(line) - 1
-      rd.name_off.push_back(cur_name_off);
-      rd.seq_off.push_back(pos);
-      rd.len.push_back((int32_t)ll);
-      rd.name_len.push_back(cur_name_len);
-      if (ll < mn) mn = (int32_t)ll;
-      if (ll > mx) mx = (int32_t)ll;
-      have_header = false;
-    }
-    pos += c;
-  }
-  if (have_header) {
-    *err = "reads: trailing header without a sequence line";
-    return SWIFT_E_INPUT;
-  }
-  rd.min_len = rd.len.empty() ? 0 : mn;
-  rd.max_len = mx;
   return SWIFT_OK;
 }
 

@@ -44,18 +44,7 @@ struct HostRef {
   uint64_t cat_len = 0;
 };
 
-struct HostReads {
-  std::vector<uint64_t> name_off;  // offset of '>'
-  std::vector<uint64_t> seq_off;   // offset of the sequence line
-  std::vector<int32_t> len;        // read length
-  std::vector<int32_t> name_len;   // characters after '>'
-  int64_t n_gt = 0;                // '>' bytes in the file (getSeqCount)
-  int32_t first_len = 0;           // getSeqSize of the file
-  int32_t min_len = 0, max_len = 0;
-};
-
 int parse_reference(const char* b, size_t n, HostRef* out, std::string* err);
-int parse_reads(const char* b, size_t n, HostReads* out, std::string* err);
 
 // Phase-1 slot schedule of searchQueries3: read index per slot call, -1 for
 // a slot never filled.  Returns the list of reads whose records follow the
@@ -148,6 +137,31 @@ void launch_seed(cudaStream_t st, const SeedArgs& a);
 void launch_seed_overflow(cudaStream_t st, const SeedArgs& a, int n_overflow,
                           const uint64_t* tab_off, const uint32_t* tab_size);
 int seed_smem_cap();
+
+// parse.cu: reads FASTA structure found on the device
+enum : uint32_t {
+  kParseBadByte = 1,
+  kParseGtInLine,
+  kParseEmptyLine,
+  kParseSeqNoHeader,
+  kParseMultiLine,
+  kParseHeaderNoSeq,
+  kParseTrailingHeader,
+  kParseNameLong,
+  kParseReadLong,
+};
+struct ParseSummary {
+  int32_t min_len, max_len, first_len, pad;
+};
+unsigned parse_tiles(uint64_t n);
+void launch_parse_tiles(cudaStream_t st, const char* b, uint64_t n, uint32_t* cnt,
+                        unsigned long long* err);
+void launch_parse_newlines(cudaStream_t st, const char* b, uint64_t n, const uint32_t* off,
+                           uint64_t* nl);
+void launch_parse_lines(cudaStream_t st, const char* b, uint64_t n, const uint64_t* nl,
+                        uint64_t n_nl, uint64_t n_lines, DevRead* rd, ParseSummary* sum,
+                        unsigned long long* err);
+int parse_error(uint32_t code, uint64_t off, std::string* msg);
 
 // pairs.cu
 struct PairArgs {

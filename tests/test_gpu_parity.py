@@ -312,12 +312,48 @@ def test_input_errors(ctx, sg):
                       (b">a\nACGT\nACGT\n", -2),             # multi-line read
                       (b">a\n", -2),                          # header without sequence
                       (b">a\nAC>GT\n", -2),                  # '>' inside a line
-                      (b">a\n" + b"A" * 250 + b"\n", -5)]:    # read over 199 bases
+                      (b">a\n" + b"A" * 250 + b"\n", -5),    # read over 199 bases
+                      (b">" + b"n" * 60 + b"\nACGT\n", -5),  # name over 48 characters
+                      (b"ACGT\n>a\nACGT\n", -2),           # sequence before a header
+                      (b">a\n>b\nACGT\n", -2),              # header without sequence
+                      (b">a\nAC\x00GT\n", -2),              # NUL byte
+                      (b">a\nAC\xc3GT\n", -2),              # byte >= 128
+                      (b">a\nACGT\n>b\n", -2),             # trailing header
+                      (b"", -5)]:                             # no reads: query length 0
         with pytest.raises(sg.SwiftError) as e:
             ctx.align(ix, bad)
         assert e.value.code == code
     with pytest.raises(sg.SwiftError):
         ctx.index(b"ACGT\n>x\nACGT\n")
+
+
+def test_reads_without_final_newline(ctx, oracle):
+    # the first read's length is strlen(line) - 1 (getSeqSize); when that line
+    # ends the file without a newline the query is one base shorter
+    ref, reads = small_case(n_reads=200, seed=77)
+    ix = ctx.index(ref)
+    trimmed = reads.rstrip(b"\n")
+    got = ctx.align(ix, trimmed)
+    assert got == oracle.align(ref, trimmed, oparams(ctx, oracle))
+    one = b">only\n" + reads.split(b"\n")[1]
+    got = ctx.align(ix, one)
+    assert got == oracle.align(ref, one, oparams(ctx, oracle))
+
+
+def test_align_into_caller_buffer(ctx, oracle, sg):
+    import ctypes
+    ref, reads = small_case(n_reads=500, seed=78)
+    ix = ctx.index(ref)
+    want = ctx.align(ix, reads)
+    src = ctypes.create_string_buffer(reads, len(reads))
+    buf = ctypes.create_string_buffer(len(want) + 16)
+    n, st = ctx.align_into(ix, ctypes.addressof(src), len(reads), ctypes.addressof(buf), len(buf))
+    assert n == len(want) and buf.raw[:n] == want
+    assert st["printed"] > 0
+    small = ctypes.create_string_buffer(8)
+    with pytest.raises(sg.SwiftError) as e:
+        ctx.align_into(ix, ctypes.addressof(src), len(reads), ctypes.addressof(small), 8)
+    assert e.value.code == -5
 
 
 def test_cli_matches_oracle(ctx, oracle, sg):
