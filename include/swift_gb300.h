@@ -124,6 +124,31 @@ int swift_sw_batch(swift_ctx *ctx, const char *qry, const char *ref, int32_t Q,
                    int32_t *start, int32_t *end, int32_t *len, char *qcons,
                    char *rcons);
 
+/* swift_sw_batch for device buffers that allocates no memory: no
+ * cudaMalloc, no pool allocation, no library routine that allocates.  For
+ * callers that cannot allocate at call time, such as a serving loop that has
+ * reserved the rest of device memory for its own pools up front and must not
+ * have a request fail or stall in the allocator.  No counterpart in the
+ * reference (its alignSequences works on buffers alignQueries3 allocates for
+ * every batch).
+ *   - every pointer must be device memory (SWIFT_E_ARG otherwise);
+ *   - n_pairs <= SWIFT_SW_NOALLOC_MAX_PAIRS (SWIFT_E_LIMIT otherwise): the
+ *     per-pair intermediate results live in a fixed array in the library's
+ *     module memory (16 bytes per pair, 1 MiB);
+ *   - the call only enqueues work on the context's stream and returns;
+ *     outputs are ready when that stream is synchronised;
+ *   - the first call on a device looks up the array's address (a runtime
+ *     call, no allocation): make it once before any stream capture;
+ *   - all callers on a device share the array, so calls that can run at the
+ *     same time (other streams or contexts on that device) race; calls on one
+ *     stream are ordered and safe. */
+#define SWIFT_SW_NOALLOC_MAX_PAIRS 65536
+int swift_sw_batch_noalloc(swift_ctx *ctx, const char *qry, const char *ref, int32_t Q,
+                           int32_t R, int64_t n_pairs, int32_t match, int32_t mismatch,
+                           int32_t gap_open, int32_t gap_ext, float *score,
+                           int32_t *start, int32_t *end, int32_t *len, char *qcons,
+                           char *rcons);
+
 /* The whole pipeline on a reads FASTA in host memory: seeding, windows,
  * Smith-Waterman, best alignment per read, default records.  *out receives
  * a buffer owned by the library (free with swift_free). */

@@ -25,6 +25,7 @@ EXPORTS = [
     "swift_seed", "swift_sw_batch", "swift_align", "swift_reads_upload",
     "swift_reads_destroy", "swift_align_resident", "swift_fetch_output",
     "swift_align_files", "swift_free", "swift_peak_dpx", "swift_align_into",
+    "swift_sw_batch_noalloc",
 ]
 
 
@@ -91,6 +92,7 @@ def lib():
                                      vp, vp, vp, vp, vp, vp]
         L.swift_align.argtypes = [vp, vp, vp, sz, C.POINTER(Params), C.POINTER(vp),
                                   C.POINTER(sz), C.POINTER(Stats)]
+        L.swift_sw_batch_noalloc.argtypes = L.swift_sw_batch.argtypes
         L.swift_align_into.argtypes = [vp, vp, vp, sz, C.POINTER(Params), vp, sz, C.POINTER(sz),
                                        C.POINTER(Stats)]
         L.swift_reads_upload.argtypes = [vp, C.c_char_p, sz, C.POINTER(vp)]

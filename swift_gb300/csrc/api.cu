@@ -762,6 +762,63 @@ int swift_sw_batch(swift_ctx* ctx, const char* qry, const char* ref, int32_t Q, 
   return SWIFT_OK;
 }
 
+int swift_sw_batch_noalloc(swift_ctx* ctx, const char* qry, const char* ref, int32_t Q,
+                           int32_t R, int64_t n, int32_t m, int32_t x, int32_t o, int32_t e,
+                           float* score, int32_t* start, int32_t* end, int32_t* len,
+                           char* qcons, char* rcons) {
+  // Same kernels as swift_sw_batch; the per-pair records go to the static
+  // array of sw.cu instead of pool memory, and the host never waits.
+  if (!ctx || !qry || !ref || !score || !start || !end || !len || !qcons || !rcons)
+    return fail(ctx, SWIFT_E_ARG, "null argument");
+  if (n < 0) return fail(ctx, SWIFT_E_ARG, "negative pair count");
+  if (n > kStaticSwPairs)
+    return fail(ctx, SWIFT_E_LIMIT,
+                "n_pairs above SWIFT_SW_NOALLOC_MAX_PAIRS (65536), the size of the static "
+                "scratch; split the batch or use swift_sw_batch");
+  if (Q < 1 || Q > kMaxQ || R < 1 || R > kMaxR)
+    return fail(ctx, SWIFT_E_LIMIT, "Q must be 1..256 and R 1..1024");
+  CK(cudaSetDevice(ctx->device));
+  const void* ptrs[] = {qry, ref, score, start, end, len, qcons, rcons};
+  for (const void* q : ptrs) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, q) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(ctx, SWIFT_E_ARG, "swift_sw_batch_noalloc takes device pointers only");
+    }
+    if (at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged)
+      return fail(ctx, SWIFT_E_ARG, "swift_sw_batch_noalloc takes device pointers only");
+  }
+  DevAln* aln = nullptr;
+  int rc = static_sw_scratch(ctx->device, &aln, &ctx->err);
+  if (rc != SWIFT_OK) return rc;
+  if (n == 0) return SWIFT_OK;
+  cudaStream_t st = ctx->st;
+  SwArgs a;
+  memset(&a, 0, sizeof(a));
+  a.q = qry;
+  a.w = ref;
+  a.q_stride = Q + 1;
+  a.w_stride = R + 1;
+  a.Q = Q;
+  a.R = R;
+  a.match = m;
+  a.mismatch = x;
+  a.gap_open = o;
+  a.gap_ext = e;
+  a.n = n;
+  a.aln = aln;
+  a.qcons = qcons;
+  a.rcons = rcons;
+  a.cons_stride = (int64_t)Q + R + 2;
+  rc = launch_sw(st, a, &ctx->err);
+  if (rc != SWIFT_OK) return rc;
+  CKLAUNCH();
+  aln_to_ref_layout_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(aln, n, score, start, end,
+                                                                       len);
+  CKLAUNCH();
+  return SWIFT_OK;
+}
+
 int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_reads* rd,
                          const swift_params* p, size_t* out_len, swift_stats* stats) {
   if (!ctx || !idx || !rd || !p) return fail(ctx, SWIFT_E_ARG, "null argument");

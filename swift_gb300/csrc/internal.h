@@ -198,6 +198,9 @@ struct SwArgs {
   const int32_t* list;        // optional: pair ids to process ...
   const int32_t* count;       // ... and their number (device); grid sized by n
 };
+// Static scratch of swift_sw_batch_noalloc (sw.cu): room for this many pairs.
+constexpr int64_t kStaticSwPairs = SWIFT_SW_NOALLOC_MAX_PAIRS;
+int static_sw_scratch(int device, DevAln** out, std::string* err);
 int launch_sw(cudaStream_t st, const SwArgs& a, std::string* err);
 
 // sw_fast.cu: packed 16-bit passes (score of every pair; trace of printed pairs)

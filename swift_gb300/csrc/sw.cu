@@ -21,6 +21,8 @@
 // downward gap candidate pass to the next lane with one shuffle per step.
 // 2-bit directions of the lane's rows are packed per column into shared
 // memory; lane 0 walks them for the traceback.
+#include <mutex>
+
 #include "internal.h"
 
 namespace swift {
@@ -206,6 +208,36 @@ int launch_generic(cudaStream_t st, const SwArgs& a, std::string* err) {
 }
 
 }  // namespace
+
+// Per-pair results for swift_sw_batch_noalloc, held in module memory that is
+// reserved when the module loads, so that call needs no allocation.  Each
+// record is written by the kernel before anything reads it: nothing here has
+// to start at zero.  Every caller on a device shares this one array.
+__device__ __align__(256) DevAln g_static_aln[kStaticSwPairs];
+
+int static_sw_scratch(int device, DevAln** out, std::string* err) {
+  // The symbol's address is looked up once per device, with that device
+  // current (the caller has made it so), and kept.
+  constexpr int kDevices = 64;
+  static std::mutex mu;
+  static DevAln* addr[kDevices] = {};
+  if (device < 0 || device >= kDevices) {
+    *err = "device ordinal outside 0..63";
+    return SWIFT_E_ARG;
+  }
+  std::lock_guard<std::mutex> lock(mu);
+  if (!addr[device]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_static_aln);
+    if (e != cudaSuccess) {
+      *err = std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e);
+      return SWIFT_E_CUDA;
+    }
+    addr[device] = static_cast<DevAln*>(p);
+  }
+  *out = addr[device];
+  return SWIFT_OK;
+}
 
 int launch_sw(cudaStream_t st, const SwArgs& a, std::string* err) {
   if (a.n <= 0) return SWIFT_OK;
