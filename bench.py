@@ -265,6 +265,9 @@ def main():
                    "records_per_step": stats[-1]["records"],
                    "printed_per_step": stats[-1]["printed"],
                    "generic_pairs_per_step": stats[-1]["sw_generic_pairs"],
+                   "traced_pairs_per_step": stats[-1]["traced_pairs"],
+                   "retraced_pairs_per_step": stats[-1]["retraced_pairs"],
+                   "bound_pruned_pairs_per_step": stats[-1]["bound_pruned"],
                    "index_build_s": index_s},
         "sw_gcups": gcups,
         "phase_ms": {k: statistics.median(s[k] for s in stats)

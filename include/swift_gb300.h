@@ -75,6 +75,11 @@ typedef struct {
   int64_t seed_overflow_strands, sw_generic_pairs;
   int64_t launches;   /* kernels this library launched for the call       */
   double host_parse_ms, h2d_ms, d2h_ms;  /* swift_align only: host side    */
+  int64_t traced_pairs;  /* pairs that went through the traceback pass       */
+  int64_t bound_pruned;  /* pairs whose score bound ruled them out, so they
+                            needed no exact score                            */
+  int64_t retraced_pairs;/* printed pairs traced after selection (bounded
+                            selection: the read's candidate was not best)    */
 } swift_stats;
 
 void swift_params_default(swift_params *p);
@@ -87,9 +92,14 @@ const char *swift_last_error(const swift_ctx *ctx);
 /* Device facts the pipeline depends on: total device memory (it sizes the
  * Phase-2 batches, as in the reference) and the SM count. */
 int swift_ctx_info(const swift_ctx *ctx, int64_t *total_mem, int32_t *sm_count);
-/* Phase-2 kernel choice: 0 (default) packed score pass for the pairs it
- * takes, then traceback of the printed pairs; 1 the generic kernel for
- * every pair.  Both give identical output. */
+/* Phase-2 kernel choice; all give identical output.
+ *   0 (default) bounded selection: an upper bound of every packed-path
+ *     pair's score, the exact score and traceback of each read's most
+ *     promising pair, exact scores only for the pairs the bound cannot rule
+ *     out, then traceback of any printed pair not traced yet;
+ *   1 the generic kernel for every pair;
+ *   2 the exact score of every packed-path pair, then traceback of the
+ *     printed ones. */
 int swift_ctx_set_sw_path(swift_ctx *ctx, int32_t path);
 
 /* Builds the device-resident reference (file bytes, 2-bit codes) and SSAHA

@@ -57,7 +57,8 @@ class Stats(C.Structure):
         ("cells", C.c_int64), ("out_bytes", C.c_int64),
         ("seed_overflow_strands", C.c_int64), ("sw_generic_pairs", C.c_int64),
         ("launches", C.c_int64), ("host_parse_ms", C.c_double), ("h2d_ms", C.c_double),
-        ("d2h_ms", C.c_double),
+        ("d2h_ms", C.c_double), ("traced_pairs", C.c_int64), ("bound_pruned", C.c_int64),
+        ("retraced_pairs", C.c_int64),
     ]
 
     def as_dict(self):
@@ -137,7 +138,8 @@ class Context:
         return dict(total_mem=mem.value, sm_count=sms.value)
 
     def set_sw_path(self, path: int):
-        """0: packed score pass + traceback of printed pairs; 1: generic only."""
+        """0: bounded selection (default); 1: generic kernel only; 2: exact score
+        of every packed-path pair.  All give identical output."""
         self._check(lib().swift_ctx_set_sw_path(self._h, path))
 
     def peak_dpx_cells_per_s(self) -> float:

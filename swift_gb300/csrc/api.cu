@@ -25,7 +25,7 @@ struct swift_ctx {
   cudaEvent_t ev[8] = {};
   char* d_text = nullptr;
   size_t text_len = 0, text_cap = 0;
-  bool force_generic = false;
+  int sw_path = 0;  // 0 bounded selection, 1 generic kernel only, 2 exact score of every pair
 };
 
 struct swift_index {
@@ -160,16 +160,23 @@ __global__ void partition_pairs_kernel(const DevPair* __restrict__ pairs, int64_
   if (f) fast[base_f + __popc(bf & below)] = (int32_t)i;
 }
 
-// Printed pairs that went through the score pass need the traceback pass.
+// Printed pairs of the packed path that have not been traced yet (with
+// bounded selection the candidates already were); also counts all printed
+// records.
 __global__ void traceback_list_kernel(const DevPair* __restrict__ pairs,
-                                      const int32_t* __restrict__ keep, int64_t n, int all_generic,
-                                      int32_t* list, int32_t* cnt) {
+                                      const int32_t* __restrict__ keep,
+                                      const int32_t* __restrict__ cand, int64_t n, int all_generic,
+                                      int32_t* list, int32_t* cnt, int32_t* printed) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
-  const bool t = i < n && !all_generic && keep[i] && !(pairs[i].flags & 1);
-  const uint32_t b = __ballot_sync(0xffffffffu, t);
+  const bool k = i < n && keep[i];
+  const bool t = k && !all_generic && !(pairs[i].flags & 1) && !(cand && cand[i] == (int32_t)i);
+  const uint32_t b = __ballot_sync(0xffffffffu, t), bk = __ballot_sync(0xffffffffu, k);
   int32_t base = 0;
-  if (lane == 0 && b) base = atomicAdd(cnt, __popc(b));
+  if (lane == 0) {
+    if (b) base = atomicAdd(cnt, __popc(b));
+    if (bk) atomicAdd(printed, __popc(bk));
+  }
   base = __shfl_sync(0xffffffffu, base, 0);
   if (t) list[base + __popc(b & ((1u << lane) - 1))] = (int32_t)i;
 }
@@ -450,8 +457,8 @@ int swift_ctx_destroy(swift_ctx* ctx) {
 const char* swift_last_error(const swift_ctx* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
 
 int swift_ctx_set_sw_path(swift_ctx* ctx, int32_t path) {
-  if (!ctx || path < 0 || path > 1) return SWIFT_E_ARG;
-  ctx->force_generic = path == 1;
+  if (!ctx || path < 0 || path > 2) return SWIFT_E_ARG;
+  ctx->sw_path = path;
   return SWIFT_OK;
 }
 
@@ -897,17 +904,20 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
   // generic kernel (full result at once)
   int bias = 0;
   const bool fast_ok =
-      !ctx->force_generic && fast_params_ok(Q, kWin, p->match, p->mismatch, p->gap_open, p->gap_ext, &bias);
-  int32_t *fast_list, *gen_list, *tb_list, *cnt3;
+      ctx->sw_path != 1 && fast_params_ok(Q, kWin, p->match, p->mismatch, p->gap_open, p->gap_ext, &bias);
+  const bool bounded = fast_ok && ctx->sw_path == 0;
+  // counters: 0 packed-path pairs, 1 generic pairs, 2 trace list,
+  // 3 exact-score list, 4 second trace list, 5 printed records
+  int32_t *fast_list, *gen_list, *tb_list, *cnt;
   CK(sc.get(&fast_list, nn));
   CK(sc.get(&gen_list, nn));
   CK(sc.get(&tb_list, nn));
-  CK(sc.get(&cnt3, 3));
-  CK(cudaMemsetAsync(cnt3, 0, 3 * sizeof(int32_t), st));
+  CK(sc.get(&cnt, 8));
+  CK(cudaMemsetAsync(cnt, 0, 8 * sizeof(int32_t), st));
   int launches = 0;
   if (nproc > 0) {
     partition_pairs_kernel<<<(unsigned)((nproc + 255) / 256), 256, 0, st>>>(
-        pairs, nproc, fast_ok ? 0 : 1, fast_list, cnt3, gen_list, cnt3 + 1);
+        pairs, nproc, fast_ok ? 0 : 1, fast_list, cnt, gen_list, cnt + 1);
     CKLAUNCH();
     ++launches;
   }
@@ -945,15 +955,21 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
   fa2.qcons = qcons;
   fa2.rcons = rcons;
   fa2.cons_stride = cs;
+  int32_t *ub = nullptr, *cand = nullptr;
+  if (bounded) {
+    CK(sc.get(&ub, nn));
+    CK(sc.get(&cand, nn));
+  }
+  fa2.ub = ub;
   if (fast_ok && nproc > 0) {
     fa2.list = fast_list;
-    fa2.count = cnt3;
-    launches += launch_sw_score(st, fa2, nproc);
+    fa2.count = cnt;
+    launches += bounded ? launch_sw_bound(st, fa2, nproc) : launch_sw_score(st, fa2, nproc);
     CKLAUNCH();
   }
   if (nproc > 0) {
     sa.list = gen_list;
-    sa.count = cnt3 + 1;
+    sa.count = cnt + 1;
     rc = launch_sw(st, sa, &ctx->err);
     if (rc != SWIFT_OK) return rc;
     CKLAUNCH();
@@ -975,39 +991,71 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
   fa.keep = keep;
   fa.bytes = bytes;
   fa.offs = offs;
+  fa.ub = ub;
+  fa.cand = cand;
+  int2* best2 = nullptr;
+  if (fast_ok && nproc > 0) CK(sc.get(&best2, nn));
+  fa2.best = best2;
+  // trace pass + walk over list[0, n), in chunks that bound the direction
+  // scratch
+  auto trace_list = [&](int32_t* list, int32_t* count, int64_t n) -> int {
+    const int64_t chunk = 262144;
+    if (n <= 0) return SWIFT_OK;
+    const int64_t words = trace_scratch_words(Q, kWin, std::min(n, chunk));
+    uint32_t* dirs;
+    CK(sc.get(&dirs, (size_t)words));
+    fa2.list = list;
+    fa2.count = count;
+    fa2.dirs = dirs;
+    for (int64_t off = 0; off < n; off += chunk) {
+      fa2.list_offset = off;
+      const int k = launch_sw_trace(st, fa2, std::min(chunk, n - off));
+      if (k == 0) return fail(ctx, SWIFT_E_DEVICE, "trace pass could not launch");
+      launches += k;
+      CKLAUNCH();
+    }
+    fa2.list_offset = 0;
+    return SWIFT_OK;
+  };
+  int32_t h_cnt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  int64_t pruned = 0;
+  if (bounded && nproc > 0) {
+    // candidates: traced first, then pairs their scores cannot rule out get
+    // exact scores
+    launch_candidates(st, fa, tb_list, cnt + 2);
+    CKLAUNCH();
+    ++launches;
+    CK(cudaMemcpyAsync(h_cnt, cnt, sizeof(h_cnt), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    CK(cudaEventRecord(ctx->ev[6], st));
+    rc = trace_list(tb_list, cnt + 2, h_cnt[2]);
+    if (rc != SWIFT_OK) return rc;
+    int32_t* ex_list = fast_list;  // free once the bound pass has run
+    launch_prune(st, fa, aln, ex_list, cnt + 3);
+    CKLAUNCH();
+    ++launches;
+    fa2.list = ex_list;
+    fa2.count = cnt + 3;
+    fa2.list_offset = 0;
+    launches += launch_sw_score(st, fa2, std::max<int64_t>(h_cnt[0] - h_cnt[2], 0));
+    CKLAUNCH();
+  }
   launch_select(st, fa);
   CKLAUNCH();
   launches += nproc > 0 ? 1 : 0;
-  CK(cudaEventRecord(ctx->ev[6], st));
-  int32_t h_cnt3[3] = {0, 0, 0};
-  if (fast_ok && nproc > 0) {
-    traceback_list_kernel<<<(unsigned)((nproc + 255) / 256), 256, 0, st>>>(pairs, keep, nproc, 0,
-                                                                           tb_list, cnt3 + 2);
+  if (!bounded) CK(cudaEventRecord(ctx->ev[6], st));
+  if (nproc > 0) {
+    // printed packed-path pairs not traced yet
+    int32_t* list2 = bounded ? gen_list : tb_list;  // generic list no longer needed
+    traceback_list_kernel<<<(unsigned)((nproc + 255) / 256), 256, 0, st>>>(
+        pairs, keep, cand, nproc, fast_ok ? 0 : 1, list2, cnt + 4, cnt + 5);
     CKLAUNCH();
     ++launches;
-    CK(cudaMemcpyAsync(h_cnt3, cnt3, sizeof(h_cnt3), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(h_cnt, cnt, sizeof(h_cnt), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    // trace pass in chunks that bound the direction scratch
-    const int64_t chunk = 262144;
-    const int64_t ntb = h_cnt3[2];
-    if (ntb > 0) {
-      const int64_t words = trace_scratch_words(Q, kWin, std::min(ntb, chunk));
-      uint32_t* dirs;
-      int2* best2;
-      CK(sc.get(&dirs, (size_t)words));
-      CK(sc.get(&best2, nn));
-      fa2.best = best2;
-      fa2.list = tb_list;
-      fa2.count = cnt3 + 2;
-      fa2.dirs = dirs;
-      for (int64_t off = 0; off < ntb; off += chunk) {
-        fa2.list_offset = off;
-        const int k = launch_sw_trace(st, fa2, std::min(chunk, ntb - off));
-        if (k == 0) return fail(ctx, SWIFT_E_DEVICE, "trace pass could not launch");
-        launches += k;
-        CKLAUNCH();
-      }
-    }
+    rc = trace_list(list2, cnt + 4, h_cnt[4]);
+    if (rc != SWIFT_OK) return rc;
+    if (bounded) pruned = std::max<int64_t>(h_cnt[0] - h_cnt[2] - h_cnt[3], 0);
   }
   CK(cudaEventRecord(ctx->ev[4], st));
   launch_format_sizes(st, fa);
@@ -1016,7 +1064,7 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
   CKLAUNCH();
   uint64_t total = 0;
   CK(cudaMemcpyAsync(&total, tot_d, 8, cudaMemcpyDeviceToHost, st));
-  CK(cudaMemcpyAsync(h_cnt3, cnt3, sizeof(h_cnt3), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(h_cnt, cnt, sizeof(h_cnt), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   if (total + 1 > ctx->text_cap) {
     if (ctx->d_text) cudaFree(ctx->d_text);
@@ -1053,8 +1101,11 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
     s.cells = nproc * (int64_t)Q * kWin;
     s.out_bytes = (int64_t)total;
     s.seed_overflow_strands = so.overflow;
-    s.printed = h_cnt3[2];
-    s.sw_generic_pairs = h_cnt3[1];
+    s.printed = h_cnt[5];
+    s.sw_generic_pairs = h_cnt[1];
+    s.traced_pairs = h_cnt[2] + h_cnt[4];
+    s.bound_pruned = pruned;
+    s.retraced_pairs = bounded ? h_cnt[4] : 0;
     // build_pairs + the Smith-Waterman passes and select (launches) +
     // format sizes, scan, format write
     s.launches = so.launches + (nproc > 0 ? 1 + 2 : 0) + launches + scan_k;

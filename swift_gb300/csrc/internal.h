@@ -215,6 +215,7 @@ struct FastArgs {
   const int32_t* count;       // number of ids (device)
   int64_t list_offset;        // first id of this launch
   DevAln* aln;                // score pass: .score; trace pass: all fields
+  int32_t* ub;                // bound pass: upper bound of the score per pair
   int2* best;                 // trace pass: (score, first maximum cell) per pair
   uint32_t* dirs;             // trace pass: direction scratch
   int64_t chunk;              // trace pass: pairs of this launch
@@ -226,6 +227,7 @@ bool fast_params_ok(int Q, int R, int m, int x, int o, int e, int* bias);
 int64_t trace_scratch_words(int Q, int R, int64_t pairs);
 int launch_sw_score(cudaStream_t st, const FastArgs& a, int64_t max_pairs);
 int launch_sw_trace(cudaStream_t st, const FastArgs& a, int64_t max_pairs);
+int launch_sw_bound(cudaStream_t st, const FastArgs& a, int64_t max_pairs);
 int measure_dpx_peak(cudaStream_t st, int device, double* lane_instr_per_s);
 
 // out.cu
@@ -244,8 +246,12 @@ struct FormatArgs {
   uint64_t* bytes;            // per record: text bytes
   uint64_t* offs;             // per record: text offset
   char* text;
+  const int32_t* ub;          // bounded selection: upper bound per packed-path pair
+  int32_t* cand;              // bounded selection: the group's candidate per pair
 };
 void launch_select(cudaStream_t st, const FormatArgs& a);
+void launch_candidates(cudaStream_t st, const FormatArgs& a, int32_t* list, int32_t* cnt);
+void launch_prune(cudaStream_t st, const FormatArgs& a, DevAln* aln, int32_t* list, int32_t* cnt);
 void launch_format_sizes(cudaStream_t st, const FormatArgs& a);
 void launch_format_write(cudaStream_t st, const FormatArgs& a);
 

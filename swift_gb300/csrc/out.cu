@@ -68,6 +68,70 @@ __global__ void select_kernel(FormatArgs a) {
   for (int64_t i = j; i <= e; ++i) a.keep[i] = i == keep ? 1 : 0;
 }
 
+// Appends the flagged ids of a warp to list with one atomic.
+__device__ __forceinline__ void warp_append(bool flag, int32_t id, int32_t* list, int32_t* cnt) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t b = __ballot_sync(0xffffffffu, flag);
+  int32_t base = 0;
+  if (lane == 0 && b) base = atomicAdd(cnt, __popc(b));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (flag) list[base + __popc(b & ((1u << lane) - 1))] = id;
+}
+
+// Bounded selection, step 1: per best-per-read group (the groups of
+// select_kernel) the candidate is the first pair with the largest key, the
+// exact score for pairs of the generic kernel and the upper bound for the
+// others.  Every pair learns its group's candidate; packed-path candidates
+// are listed for the trace pass.
+__global__ void candidate_kernel(FormatArgs a, int32_t* list, int32_t* cnt) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  bool app = false;
+  int32_t cand = 0;
+  if (j < a.n) {
+    const int64_t bstart = (j / a.batch) * a.batch;
+    const int64_t bend = min(bstart + a.batch, a.n);
+    if (j == bstart || !names_equal(a, a.pairs[j], a.pairs[j - 1])) {
+      int64_t e = j;
+      while (e + 1 < bend && names_equal(a, a.pairs[e + 1], a.pairs[e])) ++e;
+      int64_t best = j;
+      int bk = -1;
+      for (int64_t i = j; i <= e; ++i) {
+        const int k = (a.pairs[i].flags & 1) ? a.aln[i].score : a.ub[i];
+        if (k > bk) {
+          bk = k;
+          best = i;
+        }
+      }
+      for (int64_t i = j; i <= e; ++i) a.cand[i] = (int32_t)best;
+      cand = (int32_t)best;
+      app = !(a.pairs[best].flags & 1);
+    }
+  }
+  warp_append(app, cand, list, cnt);
+}
+
+// Bounded selection, step 2 (after the candidates' exact scores): a
+// packed-path pair other than the candidate can still be its group's first
+// maximum only if its bound exceeds the candidate's score, or equals it and
+// the pair comes first.  Those are listed for the exact score pass; the rest
+// get score -1, below any score, so select_kernel never keeps them.
+__global__ void prune_kernel(FormatArgs a, DevAln* aln, int32_t* list, int32_t* cnt) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  bool app = false;
+  if (i < a.n && !(a.pairs[i].flags & 1)) {
+    const int32_t c = a.cand[i];
+    if (c != (int32_t)i) {
+      const int S = aln[c].score, u = a.ub[i];
+      if (u > S || (u == S && i < c)) {
+        app = true;
+      } else {
+        aln[i].score = -1;
+      }
+    }
+  }
+  warp_append(app, (int32_t)i, list, cnt);
+}
+
 __device__ __forceinline__ int ndigits(int v) {
   unsigned u = v < 0 ? (unsigned)(-(int64_t)v) : (unsigned)v;
   int n = 1;
@@ -189,6 +253,16 @@ __global__ void __launch_bounds__(kFmtWarps * 32) format_write_kernel(FormatArgs
 void launch_select(cudaStream_t st, const FormatArgs& a) {
   if (a.n <= 0) return;
   select_kernel<<<(unsigned)((a.n + 255) / 256), 256, 0, st>>>(a);
+}
+
+void launch_candidates(cudaStream_t st, const FormatArgs& a, int32_t* list, int32_t* cnt) {
+  if (a.n <= 0) return;
+  candidate_kernel<<<(unsigned)((a.n + 255) / 256), 256, 0, st>>>(a, list, cnt);
+}
+
+void launch_prune(cudaStream_t st, const FormatArgs& a, DevAln* aln, int32_t* list, int32_t* cnt) {
+  if (a.n <= 0) return;
+  prune_kernel<<<(unsigned)((a.n + 255) / 256), 256, 0, st>>>(a, aln, list, cnt);
 }
 
 void launch_format_sizes(cudaStream_t st, const FormatArgs& a) {

@@ -1,8 +1,12 @@
 // Phase 2 in packed 16-bit lanes with the DPX add-max instructions.
 //
 // Same recurrence and tie rules as sw.cu (the reference kernel's,
-// src/smithWaterman.cu:510-645 and 911-1026).  Two kernels share the DP:
-//   score pass   (TRACE = false): the maximum score of every pair, for
+// src/smithWaterman.cu:510-645 and 911-1026).  Three kernels share the
+// layout:
+//   bound pass   (sw_bound_kernel): an upper bound of every pair's score
+//                from a relaxed recurrence, so most pairs that cannot be
+//                their read's best need no exact pass;
+//   score pass   (TRACE = false): the exact maximum score of a pair, for
 //                best-per-read selection;
 //   trace pass   (TRACE = true):  for the printed pairs, the first
 //                row-major maximum and 4-bit directions streamed to global
@@ -233,6 +237,104 @@ __global__ void __launch_bounds__(kPkWarps * 32) sw_packed_kernel(FastArgs a) {
   }
 }
 
+// Upper bound of every pair's score: the same recurrence with every gap
+// charged gap_ext (>= gap_open), so by induction each cell is at least the
+// reference's cell and the maximum is an upper bound of the score.  Without
+// directions a cell is one plain 16-bit H; with Z = -gap_ext
+//     H + Z = max(H[i-1][j-1] + (s - gap_ext), H[i-1][j], H[i][j-1], Z)
+//     H     = (H + Z) + gap_ext
+// i.e. a byte permute, a three-way max, an add-max and one plain add per two
+// cells, against six ALU operations of the exact pass.  Rows past the query
+// (all mismatch) stay strictly below the maximum of the rows above, as in the
+// exact pass.  Writes a.ub[p] = the bound.
+template <int G, int RPL>
+__global__ void __launch_bounds__(kPkWarps * 32) sw_bound_kernel(FastArgs a) {
+  constexpr int kGroups = 32 / G;
+  constexpr int kPairs = 2 * kGroups;
+  extern __shared__ uint32_t wsel_all[];
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int g = lane / G, sl = lane % G;
+  const int64_t nlist = *a.count - a.list_offset;
+  const int64_t warp = (int64_t)blockIdx.x * kPkWarps + wib;
+  if (warp * kPairs >= nlist) return;  // whole warp
+  const int64_t base = warp * kPairs + 2 * g;
+  const int Q = a.Q, R = a.R;
+  const int32_t* list = a.list + a.list_offset;
+  const bool has0 = base < nlist, has1 = base + 1 < nlist;
+  const int32_t p0 = has0 ? list[base] : list[nlist - 1];
+  const int32_t p1 = has1 ? list[base + 1] : p0;
+  const char* q0 = a.q + (int64_t)p0 * a.q_stride;
+  const char* q1 = a.q + (int64_t)p1 * a.q_stride;
+  const char* w0 = a.w + (int64_t)p0 * a.w_stride;
+  const char* w1 = a.w + (int64_t)p1 * a.w_stride;
+  uint32_t* wsel = wsel_all + (wib * kGroups + g) * (R + 1);
+  for (int c = sl; c < R; c += G) {
+    uint32_t s0 = base_class((uint8_t)w0[c]), s1 = base_class((uint8_t)w1[c]);
+    wsel[c + 1] = s0 | ((s0 | 8u) << 4) | ((4u + s1) << 8) | (((4u + s1) | 8u) << 12);
+  }
+  __syncwarp();
+  const uint32_t Z = (uint32_t)(-a.gap_ext);
+  const uint32_t ZZ = Z * 0x00010001u;
+  // per-half add of gap_ext as one 32-bit add: every half it meets is at
+  // least Z = -gap_ext, so no borrow crosses between the halves
+  const uint32_t EE = (uint32_t)((int32_t)a.gap_ext * 65537);
+  const uint32_t sm = (uint32_t)(uint8_t)(int8_t)(a.match - a.gap_ext);
+  const uint32_t sx = (uint32_t)(uint8_t)(int8_t)(a.mismatch - a.gap_ext);
+  const uint32_t all_x = sx * 0x01010101u;
+  uint32_t prof0[RPL], prof1[RPL], h[RPL];
+#pragma unroll
+  for (int k = 0; k < RPL; ++k) {
+    const int i = sl * RPL + k;
+    if (i < Q) {
+      const uint32_t c0 = base_class((uint8_t)q0[i]), c1 = base_class((uint8_t)q1[i]);
+      prof0[k] = all_x ^ ((sm ^ sx) << (8 * c0));
+      prof1[k] = all_x ^ ((sm ^ sx) << (8 * c1));
+    } else {
+      prof0[k] = prof1[k] = all_x;
+    }
+    h[k] = 0;  // H[i][0] = 0
+  }
+  uint32_t best = ZZ, send = 0, prev_up = 0;
+  const int steps = R + G - 1;
+  for (int s = 0; s < steps; ++s) {
+    uint32_t up = __shfl_up_sync(0xffffffffu, send, 1, G);
+    if (sl == 0) up = 0;  // row 0
+    // the diagonal of the lane's first row is the lane above's last row one
+    // column back: what arrived as `up` one step earlier
+    uint32_t dg = prev_up;
+    prev_up = up;
+    const int j = s - sl + 1;
+    if (j >= 1 && j <= R) {
+      const uint32_t ws = wsel[j];
+      uint32_t hpair = 0;
+#pragma unroll
+      for (int k = 0; k < RPL; ++k) {
+        const uint32_t sc = prmt(prof0[k], prof1[k], ws);
+        const uint32_t t = __vimax3_s16x2(up, h[k], ZZ);
+        const uint32_t hz = __viaddmax_s16x2(dg, sc, t);
+        dg = h[k];
+        up = hz + EE;
+        h[k] = up;
+        if (k & 1) {
+          best = __vimax3_s16x2(best, hpair, hz);
+        } else if (k == RPL - 1) {
+          best = __vimax_s16x2_relu(best, hz);
+        } else {
+          hpair = hz;
+        }
+      }
+      send = up;
+    }
+  }
+  uint32_t v = best;
+#pragma unroll
+  for (int d = G / 2; d > 0; d >>= 1) v = __vimax_s16x2_relu(v, __shfl_xor_sync(0xffffffffu, v, d, G));
+  if (sl == 0) {
+    if (has0) a.ub[p0] = (int32_t)(v & 0xFFFFu) - (int32_t)Z;
+    if (has1) a.ub[p1] = (int32_t)(v >> 16) - (int32_t)Z;
+  }
+}
+
 // Traceback walk (src/smithWaterman.cu:911-1026), one thread per printed
 // pair: dependent loads of the 4-bit directions the trace pass streamed out;
 // many walks in flight hide each other's latency.
@@ -357,6 +459,32 @@ int launch_shape(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {
   return 0;
 }
 
+int launch_bound(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {
+  const Shape s = shape_for(a.Q);
+  if (s.G == 0 || max_pairs <= 0) return 0;
+  const int pairs_per_warp = 2 * (32 / s.G);
+  const int64_t warps = (max_pairs + pairs_per_warp - 1) / pairs_per_warp;
+  const unsigned grid = (unsigned)((warps + kPkWarps - 1) / kPkWarps);
+  const size_t smem = (size_t)kPkWarps * (32 / s.G) * (a.R + 1) * sizeof(uint32_t);
+#define SWIFT_BD(G_, R_)                                                  \
+  if (s.G == G_ && s.RPL == R_) {                                          \
+    if (smem > 48 * 1024)                                                  \
+      cudaFuncSetAttribute(sw_bound_kernel<G_, R_>,                        \
+                           cudaFuncAttributeMaxDynamicSharedMemorySize,    \
+                           (int)smem);                                     \
+    sw_bound_kernel<G_, R_><<<grid, kPkWarps * 32, smem, st>>>(a);         \
+    return 1;                                                              \
+  }
+  SWIFT_BD(8, 4)
+  SWIFT_BD(8, 8)
+  SWIFT_BD(8, 13)
+  SWIFT_BD(8, 16)
+  SWIFT_BD(16, 13)
+  SWIFT_BD(16, 16)
+#undef SWIFT_BD
+  return 0;
+}
+
 int launch_walk(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {
   const Shape s = shape_for(a.Q);
   if (s.G == 0 || max_pairs <= 0) return 0;
@@ -399,6 +527,10 @@ int64_t trace_scratch_words(int Q, int R, int64_t pairs) {
 
 int launch_sw_score(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {
   return launch_shape<false>(st, a, max_pairs);
+}
+
+int launch_sw_bound(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {
+  return launch_bound(st, a, max_pairs);
 }
 
 int launch_sw_trace(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {

@@ -370,20 +370,48 @@ def test_cli_matches_oracle(ctx, oracle, sg):
 
 
 def test_packed_and_generic_paths_agree(ctx, oracle):
-    # the packed score pass + traceback of printed pairs must print exactly
-    # what the generic kernel prints for every pair
+    # bounded selection (default), the exact score of every pair, and the
+    # generic kernel for every pair must print exactly the same records
     ref, reads = small_case(n_reads=3000, seed=101)
     ix = ctx.index(ref)
     fast, st = ctx.align(ix, reads, stats=True)
-    assert st["sw_generic_pairs"] < st["records"]  # the packed pass ran
-    ctx.set_sw_path(1)
+    assert st["sw_generic_pairs"] < st["records"]  # the packed passes ran
+    assert st["bound_pruned"] > 0
+    outs = {}
+    for path in (1, 2):
+        ctx.set_sw_path(path)
+        try:
+            outs[path], sts = ctx.align(ix, reads, stats=True)
+        finally:
+            ctx.set_sw_path(0)
+        if path == 1:
+            assert sts["sw_generic_pairs"] == sts["records"]
+        assert sts["printed"] == st["printed"]
+    assert fast == outs[1] == outs[2]
+    assert fast == oracle.align(ref, reads, oparams(ctx, oracle))
+
+
+def test_bounded_selection_with_repeats(ctx, oracle):
+    # a repeat-rich reference gives reads several near-equal candidates, so
+    # the bound keeps pairs for exact scoring and some reads' most promising
+    # pair is not their best (second traceback round)
+    from swift_gb300 import synth
+    names, seqs = synth.make_reference(400_000, 4, sigma=0.5, repeat_frac=0.3, n_units=40,
+                                       unit_len=300, divergence=0.02, seed=211)
+    ref = synth.fasta_bytes(names, seqs)
+    rn, rs, _ = synth.make_reads(seqs, 6000, 100, 0.02, 0.004, 0.05, seed=212)
+    reads = synth.reads_fasta(rn, rs)
+    ix = ctx.index(ref)
+    got, st = ctx.align(ix, reads, stats=True)
+    assert st["retraced_pairs"] > 0
+    assert st["bound_pruned"] < st["records"] - st["sw_generic_pairs"]
+    ctx.set_sw_path(2)
     try:
-        slow, st2 = ctx.align(ix, reads, stats=True)
+        exact = ctx.align(ix, reads)
     finally:
         ctx.set_sw_path(0)
-    assert st2["sw_generic_pairs"] == st2["records"]
-    assert fast == slow
-    assert fast == oracle.align(ref, reads, oparams(ctx, oracle))
+    assert got == exact
+    assert got == oracle.align(ref, reads, oparams(ctx, oracle)), first_diff(got, oracle.align(ref, reads, oparams(ctx, oracle)))
 
 
 @pytest.mark.parametrize("Q", [20, 50, 64, 100, 128, 150, 199])
