@@ -181,6 +181,58 @@ __global__ void traceback_list_kernel(const DevPair* __restrict__ pairs,
   if (t) list[base + __popc(b & ((1u << lane) - 1))] = (int32_t)i;
 }
 
+// Early-stop order of a pair list.  The exact passes stop a warp once the
+// bound pass's suffix maxima rule out every remaining column for all of its
+// pairs, so pairs expected to stop at the same block should share warps.
+// Key: the first block m >= 1 whose suffix maximum is below the pair's
+// score bound (m_max + 1 if none).  A counting sort by key.
+__device__ __forceinline__ int stop_key(const int32_t* ub, const uint16_t* suf, int32_t p,
+                                        int m_max) {
+  const int u = ub[p];
+  for (int m = 1; m <= m_max; ++m)
+    if ((int)suf[(int64_t)p * kSufBlocks + m] < u) return m;
+  return m_max + 1;
+}
+
+__global__ void stop_key_count_kernel(const int32_t* __restrict__ list, const int32_t* __restrict__ n,
+                                      const int32_t* __restrict__ ub, const uint16_t* __restrict__ suf,
+                                      int m_max, int32_t* __restrict__ keys, int32_t* hist) {
+  __shared__ int32_t h[kSufBlocks + 1];
+  if (threadIdx.x <= kSufBlocks) h[threadIdx.x] = 0;
+  __syncthreads();
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < *n) {
+    const int k = stop_key(ub, suf, list[i], m_max);
+    keys[i] = k;
+    atomicAdd(&h[k], 1);
+  }
+  __syncthreads();
+  if (threadIdx.x <= kSufBlocks && h[threadIdx.x]) atomicAdd(&hist[threadIdx.x], h[threadIdx.x]);
+}
+
+__global__ void stop_key_scatter_kernel(const int32_t* __restrict__ list, const int32_t* __restrict__ n,
+                                        const int32_t* __restrict__ keys,
+                                        const int32_t* __restrict__ hist, int32_t* fill,
+                                        int32_t* __restrict__ out) {
+  __shared__ int32_t base[kSufBlocks + 1], cnt[kSufBlocks + 1];
+  if (threadIdx.x <= kSufBlocks) cnt[threadIdx.x] = 0;
+  __syncthreads();
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int k = 0, r = 0;
+  if (i < *n) {
+    k = keys[i];
+    r = atomicAdd(&cnt[k], 1);
+  }
+  __syncthreads();
+  if (threadIdx.x <= kSufBlocks) {
+    int b = 0;
+    for (int t = 0; t < (int)threadIdx.x; ++t) b += hist[t];
+    base[threadIdx.x] = cnt[threadIdx.x] ? b + atomicAdd(&fill[threadIdx.x], cnt[threadIdx.x]) : 0;
+  }
+  __syncthreads();
+  if (i < *n) out[base[k] + r] = list[i];
+}
+
 __global__ void read_counts_kernel(const int32_t* __restrict__ nbest, int64_t n_reads,
                                    uint64_t* __restrict__ cnt) {
   int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -908,12 +960,13 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
   const bool bounded = fast_ok && ctx->sw_path == 0;
   // counters: 0 packed-path pairs, 1 generic pairs, 2 trace list,
   // 3 exact-score list, 4 second trace list, 5 printed records
+  // counters 8.. : histogram and fill of the early-stop sort (two uses)
   int32_t *fast_list, *gen_list, *tb_list, *cnt;
   CK(sc.get(&fast_list, nn));
   CK(sc.get(&gen_list, nn));
   CK(sc.get(&tb_list, nn));
-  CK(sc.get(&cnt, 8));
-  CK(cudaMemsetAsync(cnt, 0, 8 * sizeof(int32_t), st));
+  CK(sc.get(&cnt, 8 + 4 * (kSufBlocks + 1)));
+  CK(cudaMemsetAsync(cnt, 0, (8 + 4 * (kSufBlocks + 1)) * sizeof(int32_t), st));
   int launches = 0;
   if (nproc > 0) {
     partition_pairs_kernel<<<(unsigned)((nproc + 255) / 256), 256, 0, st>>>(
@@ -956,11 +1009,14 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
   fa2.rcons = rcons;
   fa2.cons_stride = cs;
   int32_t *ub = nullptr, *cand = nullptr;
+  uint16_t* suf = nullptr;
   if (bounded) {
     CK(sc.get(&ub, nn));
     CK(sc.get(&cand, nn));
+    CK(sc.get(&suf, nn * kSufBlocks));
   }
   fa2.ub = ub;
+  fa2.suf = suf;
   if (fast_ok && nproc > 0) {
     fa2.list = fast_list;
     fa2.count = cnt;
@@ -1019,6 +1075,27 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
   };
   int32_t h_cnt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   int64_t pruned = 0;
+  // list[0, *count) -> out in early-stop order (grid sized by max_n)
+  int32_t *keys = nullptr, *sorted = nullptr;
+  if (bounded) {
+    CK(sc.get(&keys, nn));
+    CK(sc.get(&sorted, nn));
+  }
+  const int m_max = (kWin - 1) / kSufSteps;
+  int sort_uses = 0;
+  auto sort_by_stop = [&](const int32_t* list, const int32_t* count, int64_t max_n,
+                          int32_t* out) -> int {
+    if (max_n <= 0) return SWIFT_OK;
+    int32_t* hist = cnt + 8 + 2 * (kSufBlocks + 1) * sort_uses;
+    int32_t* fill = hist + (kSufBlocks + 1);
+    ++sort_uses;
+    const unsigned grid = (unsigned)((max_n + 255) / 256);
+    stop_key_count_kernel<<<grid, 256, 0, st>>>(list, count, ub, suf, m_max, keys, hist);
+    stop_key_scatter_kernel<<<grid, 256, 0, st>>>(list, count, keys, hist, fill, out);
+    CKLAUNCH();
+    launches += 2;
+    return SWIFT_OK;
+  };
   if (bounded && nproc > 0) {
     // candidates: traced first, then pairs their scores cannot rule out get
     // exact scores
@@ -1028,16 +1105,21 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
     CK(cudaMemcpyAsync(h_cnt, cnt, sizeof(h_cnt), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     CK(cudaEventRecord(ctx->ev[6], st));
-    rc = trace_list(tb_list, cnt + 2, h_cnt[2]);
+    rc = sort_by_stop(tb_list, cnt + 2, h_cnt[2], sorted);
+    if (rc != SWIFT_OK) return rc;
+    rc = trace_list(sorted, cnt + 2, h_cnt[2]);
     if (rc != SWIFT_OK) return rc;
     int32_t* ex_list = fast_list;  // free once the bound pass has run
     launch_prune(st, fa, aln, ex_list, cnt + 3);
     CKLAUNCH();
     ++launches;
-    fa2.list = ex_list;
+    const int64_t ex_max = std::max<int64_t>(h_cnt[0] - h_cnt[2], 0);
+    rc = sort_by_stop(ex_list, cnt + 3, ex_max, sorted);
+    if (rc != SWIFT_OK) return rc;
+    fa2.list = sorted;
     fa2.count = cnt + 3;
     fa2.list_offset = 0;
-    launches += launch_sw_score(st, fa2, std::max<int64_t>(h_cnt[0] - h_cnt[2], 0));
+    launches += launch_sw_score(st, fa2, ex_max);
     CKLAUNCH();
   }
   launch_select(st, fa);

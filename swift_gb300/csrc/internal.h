@@ -204,6 +204,9 @@ int static_sw_scratch(int device, DevAln** out, std::string* err);
 int launch_sw(cudaStream_t st, const SwArgs& a, std::string* err);
 
 // sw_fast.cu: packed 16-bit passes (score of every pair; trace of printed pairs)
+// Bound-pass suffix maxima: blocks of wavefront steps, blocks per pair.
+constexpr int kSufSteps = 32;
+constexpr int kSufBlocks = 16;
 struct FastArgs {
   const char* q;
   const char* w;
@@ -216,6 +219,9 @@ struct FastArgs {
   int64_t list_offset;        // first id of this launch
   DevAln* aln;                // score pass: .score; trace pass: all fields
   int32_t* ub;                // bound pass: upper bound of the score per pair
+  uint16_t* suf;              // bound pass: per pair, kSufBlocks suffix maxima of
+                              // kSufSteps-step blocks (read by the exact passes
+                              // to stop early); may be null
   int2* best;                 // trace pass: (score, first maximum cell) per pair
   uint32_t* dirs;             // trace pass: direction scratch
   int64_t chunk;              // trace pass: pairs of this launch

@@ -77,11 +77,25 @@ __device__ __forceinline__ uint32_t sel(uint32_t m, uint32_t a, uint32_t b) {
   return (a & m) | (b & ~m);
 }
 
+// Direction scratch of the trace pass, per group (two pairs): for each lane
+// ln and word w, the words of all wavefront steps are contiguous,
+//     region[(ln * kDirWords + w) * steps8 + step],  steps8 = steps rounded up to 8,
+// so a traceback, which moves one step back on most cells, reads
+// consecutive words.  A word holds 8 rows x 2 pairs x 2 bits: bits
+// 2 * (k & 7) (first pair) and 16 + 2 * (k & 7) (second pair) of row k are
+// 2 for DIAG, 1 for UP and 0 for LEFT or NONE (NONE is the cell with H = 0,
+// which the traceback knows from the scores).
+template <int RPL>
+struct DirLayout {
+  static constexpr int kWords = (RPL + 7) / 8;  // words per lane and step
+};
+__host__ __device__ constexpr int steps8(int R, int G) { return (R + G - 1 + 7) & ~7; }
+
 template <int G, int RPL, bool TRACE>
 __global__ void __launch_bounds__(kPkWarps * 32) sw_packed_kernel(FastArgs a) {
   constexpr int kGroups = 32 / G;      // groups per warp
   constexpr int kPairs = 2 * kGroups;  // pairs per warp
-  constexpr int kNW = (RPL + 3) / 4;   // direction words per lane per column
+  constexpr int kNW = DirLayout<RPL>::kWords;
   extern __shared__ uint32_t wsel_all[];  // [warps * groups][R + 1]
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int g = lane / G, sl = lane % G;
@@ -136,23 +150,23 @@ __global__ void __launch_bounds__(kPkWarps * 32) sw_packed_kernel(FastArgs a) {
     }
   }
   if (!TRACE) bestv[0] = BB;
+  const int S8 = steps8(R, G);
   uint32_t* dirs = nullptr;
-  if (TRACE) dirs = a.dirs + (warp * kGroups + g) * (int64_t)(R + G - 1) * kNW * G;
+  if (TRACE) dirs = a.dirs + ((warp * kGroups + g) * G + sl) * (int64_t)kNW * S8;
   uint32_t send_u = BB, send_h = BB, diag = BB;
-  const int steps = R + G - 1;
-  for (int s = 0; s < steps; ++s) {
+  // one wavefront step; acc receives the step's direction words
+  auto step = [&](const int s, uint32_t* acc) {
     uint32_t up = __shfl_up_sync(0xffffffffu, send_u, 1, G);
     const uint32_t rh = __shfl_up_sync(0xffffffffu, send_h, 1, G);
     if (sl == 0) up = BB;  // row 0: H = 0, NONE
     const int j = s - sl + 1;
+#pragma unroll
+    for (int w = 0; w < kNW; ++w) acc[w] = 0;
     if (j >= 1 && j <= R) {
       const uint32_t ws = wsel[j];
       const uint32_t jj = (uint32_t)j * 0x00010001u;
       uint32_t dg = diag;
       uint32_t hpair = 0;  // score pass: even row waiting for its odd partner
-      uint32_t acc[kNW];
-#pragma unroll
-      for (int w = 0; w < kNW; ++w) acc[w] = 0;
 #pragma unroll
       for (int k = 0; k < RPL; ++k) {
         const uint32_t sc = prmt(prof0[k], prof1[k], ws);
@@ -169,7 +183,12 @@ __global__ void __launch_bounds__(kPkWarps * 32) sw_packed_kernel(FastArgs a) {
           const uint32_t m = gt_mask(h16, bestv[k]);
           bestv[k] = sel(m, h16, bestv[k]);
           bestc[k] = sel(m, jj, bestc[k]);
-          acc[k >> 2] |= (hx & 0x000F000Fu) << (4 * (k & 3));
+          // bits 1 (UP) and 2 (DIAG) of each half's code to 2 * (k & 7)
+          if ((k & 7) == 0) {
+            acc[k >> 3] |= (hx >> 1) & 0x00030003u;
+          } else {
+            acc[k >> 3] |= (hx << (2 * (k & 7) - 1)) & (0x00030003u << (2 * (k & 7)));
+          }
         } else if (k & 1) {
           bestv[0] = __vimax3_s16x2_relu(bestv[0], hpair, h16);
         } else if (k == RPL - 1) {
@@ -178,16 +197,49 @@ __global__ void __launch_bounds__(kPkWarps * 32) sw_packed_kernel(FastArgs a) {
           hpair = h16;
         }
       }
-      if (TRACE) {
-        // indexed by wavefront step so the G lanes of a group store one
-        // contiguous run (lane t holds column s - t + 1)
-#pragma unroll
-        for (int w = 0; w < kNW; ++w) __stcg(&dirs[((int64_t)s * kNW + w) * G + sl], acc[w]);
-      }
       send_u = up;
       send_h = h16p[RPL - 1];
     }
     diag = sl == 0 ? BB : rh;
+  };
+  const int steps = R + G - 1;
+  // steps in blocks of 4: the trace pass keeps a block's direction words in
+  // registers and writes each word index as one 16-byte store
+  uint32_t hist[TRACE ? 4 : 1][kNW];
+  for (int s0 = 0; s0 < steps; s0 += 4) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (s0 + u < steps) step(s0 + u, hist[TRACE ? u : 0]);
+    if (TRACE) {
+#pragma unroll
+      for (int w = 0; w < kNW; ++w) {
+        // words past the last step are never read
+        const uint4 v = make_uint4(hist[0][w], hist[1][w], hist[2][w], hist[3][w]);
+        __stcg(reinterpret_cast<uint4*>(dirs + (int64_t)w * S8 + s0), v);
+      }
+    }
+    // Early stop: after step s = kSufSteps * m + G - 1 every cell left lies
+    // right of column kSufSteps * m, and the bound pass's suffix maximum
+    // suf[m] bounds them all.  Once it is below the score reached so far
+    // for every pair of the warp, no cell left can be (or tie) the first
+    // maximum, and the traceback never reaches them.  ((G - 1) % 4 == 3,
+    // so such an s ends a block.)
+    const int s = s0 + 3;
+    if (a.suf && s >= kSufSteps + G - 1 && ((s - (G - 1)) & (kSufSteps - 1)) == 0) {
+      const int m = (s - (G - 1)) / kSufSteps;
+      uint32_t v = bestv[0];
+      if (TRACE) {
+#pragma unroll
+        for (int k = 1; k < RPL; ++k) v = __vimax_s16x2_relu(v, bestv[k]);
+      }
+#pragma unroll
+      for (int d = G / 2; d > 0; d >>= 1) v = __vimax_s16x2_relu(v, __shfl_xor_sync(0xffffffffu, v, d, G));
+      const uint32_t v0 = v & 0xFFFFu, v1 = v >> 16;
+      const int s0v = v0 > B ? (int)((v0 - B) >> 4) : 0, s1v = v1 > B ? (int)((v1 - B) >> 4) : 0;
+      const bool done0 = !has0 || (int)a.suf[(int64_t)p0 * kSufBlocks + m] < s0v;
+      const bool done1 = !has1 || (int)a.suf[(int64_t)p1 * kSufBlocks + m] < s1v;
+      if (__all_sync(0xffffffffu, done0 && done1)) break;
+    }
   }
   if (!TRACE) {
     // maximum of the group, per packed pair
@@ -247,15 +299,17 @@ __global__ void __launch_bounds__(kPkWarps * 32) sw_packed_kernel(FastArgs a) {
 // cells, against six ALU operations of the exact pass.  Rows past the query
 // (all mismatch) stay strictly below the maximum of the rows above, as in the
 // exact pass.  Writes a.ub[p] = the bound.
+constexpr int kBdWarps = 4;
+
 template <int G, int RPL>
-__global__ void __launch_bounds__(kPkWarps * 32) sw_bound_kernel(FastArgs a) {
+__global__ void __launch_bounds__(kBdWarps * 32) sw_bound_kernel(FastArgs a) {
   constexpr int kGroups = 32 / G;
   constexpr int kPairs = 2 * kGroups;
-  extern __shared__ uint32_t wsel_all[];
+  extern __shared__ uint16_t wsel16_all[];  // [warps * groups][R + 1]
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int g = lane / G, sl = lane % G;
   const int64_t nlist = *a.count - a.list_offset;
-  const int64_t warp = (int64_t)blockIdx.x * kPkWarps + wib;
+  const int64_t warp = (int64_t)blockIdx.x * kBdWarps + wib;
   if (warp * kPairs >= nlist) return;  // whole warp
   const int64_t base = warp * kPairs + 2 * g;
   const int Q = a.Q, R = a.R;
@@ -267,10 +321,10 @@ __global__ void __launch_bounds__(kPkWarps * 32) sw_bound_kernel(FastArgs a) {
   const char* q1 = a.q + (int64_t)p1 * a.q_stride;
   const char* w0 = a.w + (int64_t)p0 * a.w_stride;
   const char* w1 = a.w + (int64_t)p1 * a.w_stride;
-  uint32_t* wsel = wsel_all + (wib * kGroups + g) * (R + 1);
+  uint16_t* wsel = wsel16_all + (wib * kGroups + g) * (R + 1);
   for (int c = sl; c < R; c += G) {
     uint32_t s0 = base_class((uint8_t)w0[c]), s1 = base_class((uint8_t)w1[c]);
-    wsel[c + 1] = s0 | ((s0 | 8u) << 4) | ((4u + s1) << 8) | (((4u + s1) | 8u) << 12);
+    wsel[c + 1] = (uint16_t)(s0 | ((s0 | 8u) << 4) | ((4u + s1) << 8) | (((4u + s1) | 8u) << 12));
   }
   __syncwarp();
   const uint32_t Z = (uint32_t)(-a.gap_ext);
@@ -294,44 +348,83 @@ __global__ void __launch_bounds__(kPkWarps * 32) sw_bound_kernel(FastArgs a) {
     }
     h[k] = 0;  // H[i][0] = 0
   }
+  const uint32_t not_first = sl == 0 ? 0u : 1u;  // row 0 above lane 0: H = 0
+  const uint16_t* wcol = wsel + 1 - sl;          // lane sl holds column s - sl + 1
+  // maximum of the lane's cells per block of kSufSteps wavefront steps
+  uint32_t* blk = reinterpret_cast<uint32_t*>(wsel16_all + kBdWarps * kGroups * (R + 1)) +
+                  (wib * 32 + lane) * kSufBlocks;
   uint32_t best = ZZ, send = 0, prev_up = 0;
-  const int steps = R + G - 1;
-  for (int s = 0; s < steps; ++s) {
-    uint32_t up = __shfl_up_sync(0xffffffffu, send, 1, G);
-    if (sl == 0) up = 0;  // row 0
+  // one wavefront step; `check` only in the G - 1 steps at either end, where
+  // some lanes are outside the window
+  auto step = [&](int s, bool check) {
+    uint32_t up = __shfl_up_sync(0xffffffffu, send, 1, G) * not_first;
     // the diagonal of the lane's first row is the lane above's last row one
     // column back: what arrived as `up` one step earlier
     uint32_t dg = prev_up;
     prev_up = up;
-    const int j = s - sl + 1;
-    if (j >= 1 && j <= R) {
-      const uint32_t ws = wsel[j];
-      uint32_t hpair = 0;
-#pragma unroll
-      for (int k = 0; k < RPL; ++k) {
-        const uint32_t sc = prmt(prof0[k], prof1[k], ws);
-        const uint32_t t = __vimax3_s16x2(up, h[k], ZZ);
-        const uint32_t hz = __viaddmax_s16x2(dg, sc, t);
-        dg = h[k];
-        up = hz + EE;
-        h[k] = up;
-        if (k & 1) {
-          best = __vimax3_s16x2(best, hpair, hz);
-        } else if (k == RPL - 1) {
-          best = __vimax_s16x2_relu(best, hz);
-        } else {
-          hpair = hz;
-        }
-      }
-      send = up;
+    if (check) {
+      const int j = s - sl + 1;
+      if (j < 1 || j > R) return;
     }
-  }
-  uint32_t v = best;
+    const uint32_t ws = wcol[s];
+    uint32_t hpair = 0;
 #pragma unroll
-  for (int d = G / 2; d > 0; d >>= 1) v = __vimax_s16x2_relu(v, __shfl_xor_sync(0xffffffffu, v, d, G));
-  if (sl == 0) {
-    if (has0) a.ub[p0] = (int32_t)(v & 0xFFFFu) - (int32_t)Z;
-    if (has1) a.ub[p1] = (int32_t)(v >> 16) - (int32_t)Z;
+    for (int k = 0; k < RPL; ++k) {
+      const uint32_t sc = prmt(prof0[k], prof1[k], ws);
+      const uint32_t t = __vimax3_s16x2(up, h[k], ZZ);
+      const uint32_t hz = __viaddmax_s16x2(dg, sc, t);
+      dg = h[k];
+      up = hz + EE;
+      h[k] = up;
+      if (k & 1) {
+        best = __vimax3_s16x2(best, hpair, hz);
+      } else if (k == RPL - 1) {
+        best = __vimax_s16x2_relu(best, hz);
+      } else {
+        hpair = hz;
+      }
+    }
+    send = up;
+  };
+  const int steps = R + G - 1;
+  auto run = [&](int s0, int s1, bool check) {
+    for (int s = s0; s < s1; ++s) {
+      step(s, check);
+      if ((s & (kSufSteps - 1)) == kSufSteps - 1) {
+        blk[s / kSufSteps] = best;
+        best = ZZ;
+      }
+    }
+  };
+  if (R >= G) {
+    run(0, G - 1, true);
+    run(G - 1, R, false);
+    run(R, steps, true);
+  } else {
+    run(0, steps, true);
+  }
+  const int nblk = (steps + kSufSteps - 1) / kSufSteps;
+  if (steps % kSufSteps) blk[nblk - 1] = best;
+  // suffix maxima over blocks, across the group's lanes: suf[m] bounds every
+  // cell the wavefront reaches at step kSufSteps * m or later, which covers
+  // all cells right of column kSufSteps * m
+  uint32_t suf = ZZ;
+  for (int b = nblk - 1; b >= 0; --b) {
+    suf = __vimax_s16x2_relu(suf, blk[b]);
+    uint32_t v = suf;
+#pragma unroll
+    for (int d = G / 2; d > 0; d >>= 1) v = __vimax_s16x2_relu(v, __shfl_xor_sync(0xffffffffu, v, d, G));
+    if (sl == 0) {
+      const int32_t v0 = (int32_t)(v & 0xFFFFu) - (int32_t)Z, v1 = (int32_t)(v >> 16) - (int32_t)Z;
+      if (a.suf) {
+        if (has0) a.suf[(int64_t)p0 * kSufBlocks + b] = (uint16_t)v0;
+        if (has1) a.suf[(int64_t)p1 * kSufBlocks + b] = (uint16_t)v1;
+      }
+      if (b == 0) {
+        if (has0) a.ub[p0] = v0;
+        if (has1) a.ub[p1] = v1;
+      }
+    }
   }
 }
 
@@ -342,7 +435,7 @@ template <int G, int RPL>
 __global__ void __launch_bounds__(256) sw_walk_kernel(FastArgs a) {
   constexpr int kGroups = 32 / G;
   constexpr int kPairs = 2 * kGroups;
-  constexpr int kNW = (RPL + 3) / 4;
+  constexpr int kNW = DirLayout<RPL>::kWords;
   const int64_t nlist = *a.count - a.list_offset;
   const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= nlist || idx >= a.chunk) return;
@@ -351,19 +444,25 @@ __global__ void __launch_bounds__(256) sw_walk_kernel(FastArgs a) {
   const int g = (int)((idx % kPairs) >> 1);
   const int hp = (int)(idx & 1);
   const int R = a.R;
-  const uint32_t* dirs = a.dirs + (warp * kGroups + g) * (int64_t)(R + G - 1) * kNW * G;
+  const int S8 = steps8(R, G);
+  const uint32_t* dirs = a.dirs + (warp * kGroups + g) * (int64_t)G * kNW * S8;
   const char* qg = a.q + (int64_t)p * a.q_stride;
   const char* wg = a.w + (int64_t)p * a.w_stride;
   const int W = R + 1;
   const int shift_half = 16 * hp;
-  auto dir_at = [&](int cell) -> uint32_t {
-    // 8 NONE, 4 DIAG, 2 UP, 1 LEFT
-    const int i = cell / W, jj = cell % W;
-    if (i == 0 || jj == 0) return 8u;
+  // the direction word last read: consecutive cells of a walk mostly share
+  // it or sit next to it
+  int64_t last = -1;
+  uint32_t word = 0;
+  // 2 DIAG, 1 UP, 0 LEFT or NONE
+  auto code_at = [&](int i, int jj) -> uint32_t {
     const int ln = (i - 1) / RPL, k = (i - 1) % RPL;
-    const int step = jj + ln - 1;
-    const uint32_t word = __ldcg(&dirs[((int64_t)step * kNW + (k >> 2)) * G + ln]);
-    return (word >> (shift_half + 4 * (k & 3))) & 0xFu;
+    const int64_t at = (int64_t)(ln * kNW + (k >> 3)) * S8 + (jj + ln - 1);
+    if (at != last) {
+      word = __ldcg(&dirs[at]);
+      last = at;
+    }
+    return (word >> (shift_half + 2 * (k & 7))) & 3u;
   };
   // consensus bytes are gathered four at a time and stored as words
   uint32_t* qcw = reinterpret_cast<uint32_t*>(a.qcons + (int64_t)p * a.cons_stride);
@@ -379,11 +478,42 @@ __global__ void __launch_bounds__(256) sw_walk_kernel(FastArgs a) {
       racc = qacc = 0;
     }
   };
+  // Directions of the reference's kernel (NONE, DIAG, UP, LEFT) from the
+  // 2-bit codes and the cell's score h, which the walk carries: a cell
+  // with code 0 is NONE exactly when h = 0 (any other cell has h > 0).
+  enum : int { kNone = 0, kDiag = 1, kUp = 2, kLeft = 3 };
+  auto dir_of = [](uint32_t code, int h) -> int {
+    return code == 2u ? kDiag : code == 1u ? kUp : (h == 0 ? kNone : kLeft);
+  };
+  const int m = a.match, x = a.mismatch, o = a.gap_open, e = a.gap_ext;
+  auto upc = [](char c) -> char { return (unsigned)(c - 'a') < 26u ? (char)(c - 32) : c; };
   const int2 b = a.best[p];
-  int cur = b.y, cr = cur / W, cc = cur % W, nxt;
-  uint32_t d0 = dir_at(cur);
-  nxt = d0 == 2u ? cur - W : d0 == 1u ? cur - 1 : d0 == 4u ? cur - W - 1 : cur;
-  int nr = nxt / W, nc = nxt % W;
+  int cr = b.y / W, cc = b.y % W;
+  int h = b.x;                       // score of (cr, cc)
+  int d = (cr == 0 || cc == 0) ? kNone : dir_of(code_at(cr, cc), h);
+  // predecessor (nr, nc) of (cr, cc) and its score nh
+  int nr = cr, nc = cc, nh = h, nd = kNone;
+  auto advance = [&]() {
+    nr = cr - ((d == kDiag || d == kUp) ? 1 : 0);
+    nc = cc - ((d == kDiag || d == kLeft) ? 1 : 0);
+    if (d == kNone) {
+      nh = h;
+      nd = kNone;
+      return;
+    }
+    const uint32_t pc = (nr == 0 || nc == 0) ? 0u : code_at(nr, nc);
+    if (d == kDiag) {
+      const char qc = upc(qg[cr - 1]), rc = upc(wg[cc - 1]);
+      const int sub = (qc == rc || qc == 'N' || rc == 'N') ? m : x;
+      nh = h - sub;
+    } else {
+      // the gap costs gap_ext when the predecessor itself moved the same way
+      const bool same = nr != 0 && nc != 0 && (d == kUp ? pc == 1u : pc == 0u);
+      nh = h - (same ? e : o);
+    }
+    nd = (nr == 0 || nc == 0) ? kNone : dir_of(pc, nh);
+  };
+  advance();
   int tick = -1, nref = -1, start = 0;
   while ((cr != nr || cc != nc) && nc != 0 && nr != 0) {
     ++tick;
@@ -391,11 +521,9 @@ __global__ void __launch_bounds__(256) sw_walk_kernel(FastArgs a) {
     if (nc != cc) { rch = wg[cc - 1]; ++nref; }
     emit(tick, rch, nr == cr ? '-' : qg[cr - 1]);
     start = cc;
-    cur = nxt; cr = nr; cc = nc;
-    const uint32_t dd = dir_at(cur);
-    if (dd == 8u) break;
-    nxt = dd == 2u ? cur - W : dd == 1u ? cur - 1 : cur - W - 1;
-    nr = nxt / W; nc = nxt % W;
+    cr = nr; cc = nc; h = nh; d = nd;
+    if (d == kNone) break;
+    advance();
   }
   if ((cr != nr || cc != nc) && (nc == 0 || nr == 0)) {
     ++tick;
@@ -459,28 +587,43 @@ int launch_shape(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {
   return 0;
 }
 
+// lanes per group and rows per lane of the bound pass: three registers per
+// row (against four in the exact passes) leave room for longer strips, which
+// spread the per-step work over more cells
+Shape bound_shape_for(int Q) {
+  if (Q <= 32) return {4, 8};
+  if (Q <= 64) return {4, 16};
+  if (Q <= 100) return {4, 25};
+  if (Q <= 128) return {4, 32};
+  if (Q <= 200) return {8, 25};
+  if (Q <= 256) return {8, 32};
+  return {0, 0};
+}
+
 int launch_bound(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {
-  const Shape s = shape_for(a.Q);
+  const Shape s = bound_shape_for(a.Q);
   if (s.G == 0 || max_pairs <= 0) return 0;
   const int pairs_per_warp = 2 * (32 / s.G);
   const int64_t warps = (max_pairs + pairs_per_warp - 1) / pairs_per_warp;
-  const unsigned grid = (unsigned)((warps + kPkWarps - 1) / kPkWarps);
-  const size_t smem = (size_t)kPkWarps * (32 / s.G) * (a.R + 1) * sizeof(uint32_t);
+  const unsigned grid = (unsigned)((warps + kBdWarps - 1) / kBdWarps);
+  if (a.R + s.G - 1 > kSufSteps * kSufBlocks) return 0;
+  const size_t smem = (size_t)kBdWarps * (32 / s.G) * (a.R + 1) * sizeof(uint16_t) +
+                      (size_t)kBdWarps * 32 * kSufBlocks * sizeof(uint32_t) + 16;
 #define SWIFT_BD(G_, R_)                                                  \
   if (s.G == G_ && s.RPL == R_) {                                          \
     if (smem > 48 * 1024)                                                  \
       cudaFuncSetAttribute(sw_bound_kernel<G_, R_>,                        \
                            cudaFuncAttributeMaxDynamicSharedMemorySize,    \
                            (int)smem);                                     \
-    sw_bound_kernel<G_, R_><<<grid, kPkWarps * 32, smem, st>>>(a);         \
+    sw_bound_kernel<G_, R_><<<grid, kBdWarps * 32, smem, st>>>(a);         \
     return 1;                                                              \
   }
-  SWIFT_BD(8, 4)
-  SWIFT_BD(8, 8)
-  SWIFT_BD(8, 13)
-  SWIFT_BD(8, 16)
-  SWIFT_BD(16, 13)
-  SWIFT_BD(16, 16)
+  SWIFT_BD(4, 8)
+  SWIFT_BD(4, 16)
+  SWIFT_BD(4, 25)
+  SWIFT_BD(4, 32)
+  SWIFT_BD(8, 25)
+  SWIFT_BD(8, 32)
 #undef SWIFT_BD
   return 0;
 }
@@ -522,7 +665,7 @@ int64_t trace_scratch_words(int Q, int R, int64_t pairs) {
   const Shape s = shape_for(Q);
   if (s.G == 0) return 0;
   const int64_t groups = (pairs + 1) / 2 + 32;  // round up to whole warps
-  return groups * (int64_t)(R + s.G - 1) * ((s.RPL + 3) / 4) * s.G;
+  return groups * (int64_t)s.G * ((s.RPL + 7) / 8) * steps8(R, s.G);
 }
 
 int launch_sw_score(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {
