@@ -567,6 +567,7 @@ int swift_index_build(swift_ctx* ctx, const char* ref, size_t len, int32_t k, in
     dr[i].bpl = hr.recs[i].bpl;
     dr[i].name_len = hr.recs[i].name_len;
     memcpy(dr[i].name, hr.recs[i].name, kNameMax);
+    dr[i].regular = hr.recs[i].regular ? 1 : 0;
     tbase[i + 1] = tbase[i] + hr.recs[i].cat_len / (uint64_t)k;
   }
   const uint64_t n_tuples = tbase[nr];
@@ -936,6 +937,7 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
   memset(&pa, 0, sizeof(pa));
   pa.ref_file = idx->d_file;
   pa.ref_file_len = idx->file_len;
+  pa.cat = (const char*)idx->d_cat;
   pa.recs = idx->d_recs;
   pa.reads = rd->d_bytes;
   pa.rd = rd->d_rd;
@@ -1113,7 +1115,10 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
     launch_prune(st, fa, aln, ex_list, cnt + 3);
     CKLAUNCH();
     ++launches;
-    const int64_t ex_max = std::max<int64_t>(h_cnt[0] - h_cnt[2], 0);
+    // the kept count sizes the exact pass's grid
+    CK(cudaMemcpyAsync(h_cnt, cnt, sizeof(h_cnt), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    const int64_t ex_max = h_cnt[3];
     rc = sort_by_stop(ex_list, cnt + 3, ex_max, sorted);
     if (rc != SWIFT_OK) return rc;
     fa2.list = sorted;

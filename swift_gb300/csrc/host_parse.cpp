@@ -52,6 +52,32 @@ bool bytes_ok(const char* s, size_t len, bool header, std::string* err,
   return true;
 }
 
+// Records whose windows can be copied from the concatenation (see
+// RefRecord::regular); the device computes offsets in 32 bits, so the
+// record must also end below 4 GiB.
+void mark_regular(HostRef* hr) {
+  size_t li = 0;
+  const size_t nl = hr->line_len.size();
+  for (RefRecord& q : hr->recs) {
+    const uint64_t end = q.cat_start + q.cat_len;
+    size_t first = li;
+    while (li < nl && hr->line_dst[li] < end) ++li;
+    const size_t n = li - first;
+    bool ok = q.seq_off + q.cat_len + (q.bpl ? q.cat_len / q.bpl : 0) + 1 < (1ull << 32);
+    if (n == 0) {
+      ok = false;
+    } else if (q.bpl == 0) {
+      ok = ok && n == 1 && hr->line_src[first] == q.seq_off;
+    } else {
+      for (size_t t = 0; ok && t < n; ++t) {
+        ok = hr->line_src[first + t] == q.seq_off + t * (uint64_t)(q.bpl + 1) &&
+             (t + 1 < n ? hr->line_len[first + t] == q.bpl : hr->line_len[first + t] <= q.bpl);
+      }
+    }
+    q.regular = ok;
+  }
+}
+
 }  // namespace
 
 int parse_reference(const char* b, size_t n, HostRef* out, std::string* err) {
@@ -117,6 +143,7 @@ int parse_reference(const char* b, size_t n, HostRef* out, std::string* err) {
     *err = "reference: no sequence header";
     return SWIFT_E_INPUT;
   }
+  mark_regular(&r);
   return SWIFT_OK;
 }
 

@@ -34,6 +34,10 @@ struct RefRecord {
   uint64_t cat_start;  // start in the concatenated sequence
   uint64_t cat_len;    // bases in the record
   char name[kNameMax];
+  // every sequence line but the last holds bpl bytes, the last at most bpl,
+  // and lines follow each other directly: file offset seq_off + c + c / bpl
+  // then is concatenated position c, so a window is a contiguous copy
+  bool regular;
 };
 
 struct HostRef {
@@ -65,7 +69,8 @@ struct DevRecord {        // per reference sequence
   uint32_t bpl;
   uint32_t name_len;
   char name[kNameMax];
-  char pad[6];
+  uint8_t regular;        // see RefRecord::regular
+  char pad[5];
 };
 
 struct DevRead {          // per read
@@ -167,6 +172,7 @@ int parse_error(uint32_t code, uint64_t off, std::string* msg);
 struct PairArgs {
   const char* ref_file;
   uint64_t ref_file_len;
+  const char* cat;            // concatenated record sequences
   const DevRecord* recs;
   const char* reads;
   const DevRead* rd;

@@ -28,6 +28,44 @@ __device__ __forceinline__ char comp_char(char c) {
   return c == 'A' ? 'T' : c == 'C' ? 'G' : c == 'G' ? 'C' : 'A';
 }
 
+// getRefSeq2's walk over the file bytes: up to 300 characters from file
+// offset off, newlines dropped, stopping at a header line or end of file.
+// The first kPre 32-byte rounds are loaded up front so the warp waits for
+// memory once, not once per round.
+__device__ int fetch_window(const PairArgs& a, uint32_t off, char* tmp, int lane) {
+  constexpr int kPre = 11;
+  char pre[kPre];
+#pragma unroll
+  for (int t = 0; t < kPre; ++t) {
+    const uint64_t p = (uint64_t)off + 32 * t + lane;
+    pre[t] = p < a.ref_file_len ? a.ref_file[p] : '\0';
+  }
+  int got = 0;
+  bool done = false;
+  // one 32-byte round: drop newlines, stop at a header line or end of file
+  auto round = [&](char c, uint64_t p) {
+    const bool stop = p >= a.ref_file_len || c == '>';
+    const uint32_t stop_bal = __ballot_sync(0xffffffffu, stop);
+    const int first_stop = stop_bal ? __ffs(stop_bal) - 1 : 32;
+    const bool keep = lane < first_stop && c != '\n';
+    const uint32_t keep_bal = __ballot_sync(0xffffffffu, keep);
+    const int rank = __popc(keep_bal & ((1u << lane) - 1));
+    if (keep && got + rank < kWin) tmp[got + rank] = c;
+    got += __popc(keep_bal);
+    if (got > kWin) got = kWin;
+    done = first_stop < 32 || got >= kWin;
+  };
+#pragma unroll
+  for (int t = 0; t < kPre; ++t) {
+    if (!done) round(pre[t], (uint64_t)off + 32 * t + lane);
+  }
+  for (uint64_t pos = (uint64_t)off + 32 * kPre; !done; pos += 32) {
+    const uint64_t p = pos + (uint64_t)lane;
+    round(p < a.ref_file_len ? a.ref_file[p] : '\0', p);
+  }
+  return got;
+}
+
 __global__ void __launch_bounds__(kPairWarps * 32) build_pairs_kernel(PairArgs a) {
   __shared__ char tmp_all[kPairWarps][kWinPad + 32];
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -39,24 +77,19 @@ __global__ void __launch_bounds__(kPairWarps * 32) build_pairs_kernel(PairArgs a
   const DevRecord& rec = a.recs[ri];
   const uint32_t off = (uint32_t)rec.seq_off + (uint32_t)dist +
                        (rec.bpl > 0 ? (uint32_t)dist / rec.bpl : 0u);
-  // fetch up to 300 window characters
   int got = 0;
-  uint64_t pos = off;
-  while (got < kWin) {
-    uint64_t p = pos + (uint64_t)lane;
-    char c = p < a.ref_file_len ? a.ref_file[p] : '\0';
-    bool eof = p >= a.ref_file_len;
-    bool stop = eof || c == '>';
-    uint32_t stop_bal = __ballot_sync(0xffffffffu, stop);
-    int first_stop = stop_bal ? __ffs(stop_bal) - 1 : 32;
-    bool keep = lane < first_stop && c != '\n';
-    uint32_t keep_bal = __ballot_sync(0xffffffffu, keep);
-    int rank = __popc(keep_bal & ((1u << lane) - 1));
-    if (keep && got + rank < kWin) tmp[got + rank] = c;
-    got += __popc(keep_bal);
-    if (got > kWin) got = kWin;
-    if (first_stop < 32) break;
-    pos += 32;
+  if (rec.regular) {
+    // the window is concatenated positions dist .. dist + 299 of the record
+    const uint64_t avail = rec.cat_len > (uint64_t)dist ? rec.cat_len - (uint64_t)dist : 0;
+    got = avail < (uint64_t)kWin ? (int)avail : kWin;
+    const char* src = a.cat + rec.cat_start + dist;
+#pragma unroll
+    for (int t = 0; t < (kWin + 31) / 32; ++t) {
+      const int i = lane + 32 * t;
+      if (i < got) tmp[i] = src[i];
+    }
+  } else {
+    got = fetch_window(a, off, tmp, lane);
   }
   __syncwarp();
   // N trimming (see the restatement notes at the top of this file)

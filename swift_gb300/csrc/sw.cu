@@ -42,20 +42,12 @@ struct DirWord<4> { using T = uint8_t; };
 template <>
 struct DirWord<8> { using T = uint16_t; };
 
+// One pair on one warp; base is the warp's shared-memory slice.
 template <int RPL>
-__global__ void __launch_bounds__(kSwWarps * 32) sw_generic_kernel(SwArgs a, int per_warp_bytes) {
+__device__ __forceinline__ void generic_pair(const SwArgs& a, int64_t pair, uint8_t* base,
+                                             int lane) {
   using DW = typename DirWord<RPL>::T;
-  extern __shared__ __align__(16) uint8_t smem[];
-  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  int64_t pair = (int64_t)blockIdx.x * kSwWarps + wib;
-  if (a.list) {
-    if (pair >= *a.count) return;
-    pair = a.list[pair];
-  } else if (pair >= a.n) {
-    return;
-  }
   const int Q = a.Q, R = a.R;
-  uint8_t* base = smem + (size_t)wib * per_warp_bytes;
   uint8_t* wsh = base;                                  // R bytes (rounded to 16)
   DW* dirs = reinterpret_cast<DW*>(base + ((R + 15) & ~15));  // (R+1) x 32
   const char* qg = a.q + pair * a.q_stride;
@@ -182,6 +174,21 @@ __global__ void __launch_bounds__(kSwWarps * 32) sw_generic_kernel(SwArgs a, int
   a.aln[pair] = out;
 }
 
+// Warps stride over the pairs (the list's length is known on the device
+// only, so the grid is capped rather than sized by it).
+template <int RPL>
+__global__ void __launch_bounds__(kSwWarps * 32) sw_generic_kernel(SwArgs a, int per_warp_bytes) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  uint8_t* base = smem + (size_t)wib * per_warp_bytes;
+  const int64_t n = a.list ? (int64_t)*a.count : a.n;
+  for (int64_t i = (int64_t)blockIdx.x * kSwWarps + wib; i < n;
+       i += (int64_t)gridDim.x * kSwWarps) {
+    generic_pair<RPL>(a, a.list ? (int64_t)a.list[i] : i, base, lane);
+    __syncwarp();
+  }
+}
+
 template <int RPL>
 int per_warp_bytes(int R) {
   return ((R + 15) & ~15) + (R + 1) * 32 * (RPL / 4);
@@ -202,8 +209,14 @@ int launch_generic(cudaStream_t st, const SwArgs& a, std::string* err) {
     *err = "window too long for the on-chip traceback";
     return SWIFT_E_LIMIT;
   }
-  unsigned grid = (unsigned)((a.n + kSwWarps - 1) / kSwWarps);
-  sw_generic_kernel<RPL><<<grid, kSwWarps * 32, smem, st>>>(a, pw);
+  int64_t blocks = (a.n + kSwWarps - 1) / kSwWarps;
+  if (a.list) {  // the list's length is on the device: a few waves stride over it
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && sms > 0)
+      blocks = std::min<int64_t>(blocks, (int64_t)sms * 16);
+  }
+  sw_generic_kernel<RPL><<<(unsigned)blocks, kSwWarps * 32, smem, st>>>(a, pw);
   return SWIFT_OK;
 }
 

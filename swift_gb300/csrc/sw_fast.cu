@@ -92,16 +92,12 @@ struct DirLayout {
 __host__ __device__ constexpr int steps8(int R, int G) { return (R + G - 1 + 7) & ~7; }
 
 template <int G, int RPL, bool TRACE>
-__global__ void __launch_bounds__(kPkWarps * 32) sw_packed_kernel(FastArgs a) {
+__device__ __forceinline__ void packed_item(const FastArgs& a, const int64_t warp, const int64_t nlist,
+                                            uint32_t* wsel_all, const int wib, const int lane) {
   constexpr int kGroups = 32 / G;      // groups per warp
   constexpr int kPairs = 2 * kGroups;  // pairs per warp
   constexpr int kNW = DirLayout<RPL>::kWords;
-  extern __shared__ uint32_t wsel_all[];  // [warps * groups][R + 1]
-  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int g = lane / G, sl = lane % G;
-  const int64_t nlist = *a.count - a.list_offset;
-  const int64_t warp = (int64_t)blockIdx.x * kPkWarps + wib;
-  if (warp * kPairs >= nlist) return;  // whole warp
   const int64_t base = warp * kPairs + 2 * g;
   const int Q = a.Q, R = a.R;
   const int32_t* list = a.list + a.list_offset;
@@ -289,6 +285,17 @@ __global__ void __launch_bounds__(kPkWarps * 32) sw_packed_kernel(FastArgs a) {
   }
 }
 
+// One work item of kPairs pairs per warp.
+template <int G, int RPL, bool TRACE>
+__global__ void __launch_bounds__(kPkWarps * 32, (TRACE || RPL > 13) ? 2 : 3) sw_packed_kernel(FastArgs a) {
+  constexpr int kPairs = 2 * (32 / G);
+  extern __shared__ uint32_t wsel_all[];  // [warps * groups][R + 1]
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t nlist = *a.count - a.list_offset;
+  const int64_t warp = (int64_t)blockIdx.x * kPkWarps + wib;
+  if (warp * kPairs < nlist) packed_item<G, RPL, TRACE>(a, warp, nlist, wsel_all, wib, lane);
+}
+
 // Upper bound of every pair's score: the same recurrence with every gap
 // charged gap_ext (>= gap_open), so by induction each cell is at least the
 // reference's cell and the maximum is an upper bound of the score.  Without
@@ -354,9 +361,14 @@ __global__ void __launch_bounds__(kBdWarps * 32) sw_bound_kernel(FastArgs a) {
   uint32_t* blk = reinterpret_cast<uint32_t*>(wsel16_all + kBdWarps * kGroups * (R + 1)) +
                   (wib * 32 + lane) * kSufBlocks;
   uint32_t best = ZZ, send = 0, prev_up = 0;
-  // one wavefront step; `check` only in the G - 1 steps at either end, where
-  // some lanes are outside the window
-  auto step = [&](int s, bool check) {
+  // One wavefront step; `check` only in the G - 1 steps at either end, where
+  // some lanes are outside the window.  The running maximum takes only the
+  // cells of `track` steps: a lane holds whole rows, and the cell right of
+  // an untracked cell, one step later, is at least its value + gap_ext, so
+  // the maximum of tracked cells - gap_ext bounds every cell.  The last
+  // column of every row is tracked (the last main step and the checked
+  // steps).
+  auto step = [&](int s, bool check, bool track) {
     uint32_t up = __shfl_up_sync(0xffffffffu, send, 1, G) * not_first;
     // the diagonal of the lane's first row is the lane above's last row one
     // column back: what arrived as `up` one step earlier
@@ -376,7 +388,8 @@ __global__ void __launch_bounds__(kBdWarps * 32) sw_bound_kernel(FastArgs a) {
       dg = h[k];
       up = hz + EE;
       h[k] = up;
-      if (k & 1) {
+      if (!track) {
+      } else if (k & 1) {
         best = __vimax3_s16x2(best, hpair, hz);
       } else if (k == RPL - 1) {
         best = __vimax_s16x2_relu(best, hz);
@@ -387,21 +400,38 @@ __global__ void __launch_bounds__(kBdWarps * 32) sw_bound_kernel(FastArgs a) {
     send = up;
   };
   const int steps = R + G - 1;
-  auto run = [&](int s0, int s1, bool check) {
-    for (int s = s0; s < s1; ++s) {
-      step(s, check);
-      if ((s & (kSufSteps - 1)) == kSufSteps - 1) {
-        blk[s / kSufSteps] = best;
-        best = ZZ;
-      }
+  auto flush = [&](int s) {
+    if ((s & (kSufSteps - 1)) == kSufSteps - 1) {
+      blk[s / kSufSteps] = best;
+      best = ZZ;
     }
   };
   if (R >= G) {
-    run(0, G - 1, true);
-    run(G - 1, R, false);
-    run(R, steps, true);
+    for (int s = 0; s < G - 1; ++s) {
+      step(s, true, true);
+      flush(s);
+    }
+    // steady state in pairs of steps, the maximum taken on the second
+    int s = G - 1;
+    for (; s + 1 < R - 1; s += 2) {
+      step(s, false, false);
+      flush(s);
+      step(s + 1, false, true);
+      flush(s + 1);
+    }
+    for (; s < R; ++s) {
+      step(s, false, true);
+      flush(s);
+    }
+    for (s = R; s < steps; ++s) {
+      step(s, true, true);
+      flush(s);
+    }
   } else {
-    run(0, steps, true);
+    for (int s = 0; s < steps; ++s) {
+      step(s, true, true);
+      flush(s);
+    }
   }
   const int nblk = (steps + kSufSteps - 1) / kSufSteps;
   if (steps % kSufSteps) blk[nblk - 1] = best;
@@ -415,7 +445,8 @@ __global__ void __launch_bounds__(kBdWarps * 32) sw_bound_kernel(FastArgs a) {
 #pragma unroll
     for (int d = G / 2; d > 0; d >>= 1) v = __vimax_s16x2_relu(v, __shfl_xor_sync(0xffffffffu, v, d, G));
     if (sl == 0) {
-      const int32_t v0 = (int32_t)(v & 0xFFFFu) - (int32_t)Z, v1 = (int32_t)(v >> 16) - (int32_t)Z;
+      // tracked maximum (H + Z) - Z, plus Z = -gap_ext for the untracked cells
+      const int32_t v0 = (int32_t)(v & 0xFFFFu), v1 = (int32_t)(v >> 16);
       if (a.suf) {
         if (has0) a.suf[(int64_t)p0 * kSufBlocks + b] = (uint16_t)v0;
         if (has1) a.suf[(int64_t)p1 * kSufBlocks + b] = (uint16_t)v1;

@@ -272,6 +272,45 @@ def test_align_messy_inputs(ctx, oracle):
     assert got == want, first_diff(got, want)
 
 
+def test_align_line_layouts(ctx, oracle):
+    # windows come from the concatenated sequence when every line but the
+    # last has the record's width, and from the file bytes otherwise; both
+    # must follow the reference's file-offset arithmetic
+    rng = random.Random(61)
+    seqs = [bytes(rng.choice(b"ACGT") for _ in range(rng.randint(3000, 6000))) for _ in range(7)]
+    def lines(s, widths, eol=b"\n"):
+        out, i, t = [], 0, 0
+        while i < len(s):
+            w = widths[min(t, len(widths) - 1)] if callable(widths) is False else widths(t)
+            out.append(s[i:i + w] + eol)
+            i += w
+            t += 1
+        return b"".join(out)
+    recs = [
+        b">uniform\n" + lines(seqs[0], [60]),
+        b">long_middle\n" + lines(seqs[1], lambda t: 75 if t == 10 else 60),
+        b">blank_line\n" + lines(seqs[2][:1500], [60]) + b"\n" + lines(seqs[2][1500:], [60]),
+        b">single\n" + seqs[3] + b"\n",
+        b">long_last\n" + lines(seqs[4][:-100], [50]) + seqs[4][-100:] + b"\n",
+        b">crlf\n" + lines(seqs[5], [61], b"\r\n"),
+        b">uniform_no_eol\n" + lines(seqs[6], [70])[:-1],
+    ]
+    ref = b"".join(recs)
+    reads = []
+    for r, sq in enumerate(seqs):
+        for t in range(60):
+            a = rng.randrange(0, len(sq) - 100)
+            rd = bytearray(sq[a:a + 100])
+            if t % 2:
+                rd = bytearray(rd[::-1].translate(bytes.maketrans(b"ACGT", b"TGCA")))
+            reads.append(b">r%d_%d\n" % (r, t) + bytes(rd) + b"\n")
+    reads = b"".join(reads)
+    ix = ctx.index(ref)
+    got = ctx.align(ix, reads)
+    want = oracle.align(ref, reads, oparams(ctx, oracle))
+    assert got == want, first_diff(got, want)
+
+
 def test_align_scoring_and_seed_parameters(ctx, oracle, sg):
     ref, reads = small_case(n_reads=300, seed=77)
     for kw in [dict(seed_len=10, ignore_thres=50), dict(match=3, mismatch=-2, gap_open=-6,
