@@ -40,6 +40,8 @@ struct swift_index {
   uint64_t cat_len = 0;
   uint32_t* d_count = nullptr;
   uint32_t* d_offsets = nullptr;
+  uint4* d_groups = nullptr;   // compact bucket directory for seeding
+  uint32_t* d_cstart = nullptr;
   uint2* d_post = nullptr;
   int64_t total = 0;
   int64_t nb = 0;
@@ -277,6 +279,8 @@ int run_seed(swift_ctx* ctx, const swift_index* idx, const swift_reads* rd, int 
   a.rd = rd->d_rd;
   a.n_reads = n;
   a.offsets = idx->d_offsets;
+  a.groups = idx->d_groups;
+  a.cstart = idx->d_cstart;
   a.postings = idx->d_post;
   a.k = idx->k;
   a.max_hits = max_hits;
@@ -626,6 +630,17 @@ int swift_index_build(swift_ctx* ctx, const char* ref, size_t len, int32_t k, in
                           ix->d_count, ix->d_offsets, d_cursor, ix->d_post);
     launch_order_buckets(st, ix->d_offsets, ix->nb, ix->d_post);
     CKI(cudaGetLastError());
+    const int64_t ng = (ix->nb + 63) / 64;
+    uint32_t *d_bits32, *d_gcnt, *d_grank, *d_nocc;
+    CKI(sc.get(&d_bits32, (size_t)(ix->nb + 31) / 32));
+    CKI(sc.get(&d_gcnt, (size_t)ng));
+    CKI(sc.get(&d_grank, (size_t)ng));
+    CKI(sc.get(&d_nocc, 1));
+    CKI(cudaMalloc(&ix->d_groups, (size_t)ng * sizeof(uint4)));
+    CKI(cudaMalloc(&ix->d_cstart, ((size_t)total + 1) * sizeof(uint32_t)));
+    build_bucket_directory(st, ix->d_offsets, ix->nb, d_bits32, d_gcnt, d_grank, tmp, d_nocc,
+                           ix->d_groups, ix->d_cstart);
+    CKI(cudaGetLastError());
   }
   CKI(cudaStreamSynchronize(st));
 #undef CKI
@@ -642,6 +657,8 @@ int swift_index_destroy(swift_index* ix) {
   cudaFree(ix->d_packed);
   cudaFree(ix->d_count);
   cudaFree(ix->d_offsets);
+  cudaFree(ix->d_groups);
+  cudaFree(ix->d_cstart);
   cudaFree(ix->d_post);
   delete ix;
   return SWIFT_OK;

@@ -145,6 +145,64 @@ __global__ void order_buckets_kernel(const uint32_t* __restrict__ offsets, int64
   }
 }
 
+// Compact bucket directory for seeding.  The bucket-start table has 4^k
+// entries (64 MiB at k = 12) and seeding looks up one entry per query
+// position at random; most buckets are empty.  The directory keeps, per
+// group of 64 buckets, the occupancy bits and the number of occupied buckets
+// before the group (16 bytes), and the starts of occupied buckets only:
+// a few tens of MB for a 50 Mbp reference, which stay in L2.
+__global__ void bucket_bits_kernel(const uint32_t* __restrict__ offsets, int64_t nb,
+                                   uint32_t* __restrict__ bits32) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t w = warp; w * 32 < nb; w += nwarps) {
+    const int64_t h = w * 32 + lane;
+    const bool occ = h < nb && offsets[h + 1] > offsets[h];
+    const uint32_t b = __ballot_sync(0xffffffffu, occ);
+    if (lane == 0) bits32[w] = b;
+  }
+}
+
+__global__ void group_count_kernel(const uint32_t* __restrict__ bits32, int64_t nw32, int64_t ng,
+                                   uint32_t* __restrict__ gcnt) {
+  int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (; g < ng; g += stride) {
+    const uint32_t lo = bits32[2 * g], hi = 2 * g + 1 < nw32 ? bits32[2 * g + 1] : 0u;
+    gcnt[g] = (uint32_t)(__popc(lo) + __popc(hi));
+  }
+}
+
+__global__ void group_pack_kernel(const uint32_t* __restrict__ bits32, int64_t nw32,
+                                  const uint32_t* __restrict__ grank, int64_t ng,
+                                  uint4* __restrict__ groups) {
+  int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (; g < ng; g += stride) {
+    const uint32_t lo = bits32[2 * g], hi = 2 * g + 1 < nw32 ? bits32[2 * g + 1] : 0u;
+    groups[g] = make_uint4(lo, hi, grank[g], 0u);
+  }
+}
+
+__global__ void compact_starts_kernel(const uint32_t* __restrict__ offsets, int64_t nb,
+                                      const uint4* __restrict__ groups,
+                                      const uint32_t* __restrict__ n_occ,
+                                      uint32_t* __restrict__ cstart) {
+  int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  if (h == 0) cstart[*n_occ] = offsets[nb];
+  for (; h < nb; h += stride) {
+    const uint32_t b = offsets[h];
+    if (offsets[h + 1] > b) {
+      const uint4 g = groups[h >> 6];
+      const uint64_t bits = ((uint64_t)g.y << 32) | g.x;
+      const uint32_t r = g.z + (uint32_t)__popcll(bits & ((1ull << (h & 63)) - 1));
+      cstart[r] = b;
+    }
+  }
+}
+
 static inline unsigned grid_for(int64_t n, int threads, unsigned cap = 152u * 32u) {
   int64_t g = (n + threads - 1) / threads;
   if (g < 1) g = 1;
@@ -185,6 +243,18 @@ void launch_scatter_tuples(cudaStream_t st, const uint32_t* packed, const DevRec
   if (n_tuples == 0) return;
   scatter_tuples_kernel<<<grid_for((int64_t)n_tuples, 256), 256, 0, st>>>(
       packed, recs, tbase, n_recs, n_tuples, k, thres, count, offsets, cursor, post);
+}
+
+int build_bucket_directory(cudaStream_t st, const uint32_t* offsets, int64_t nb, uint32_t* bits32,
+                           uint32_t* gcnt, uint32_t* grank, void* scan_tmp, uint32_t* n_occ,
+                           uint4* groups, uint32_t* cstart) {
+  const int64_t nw32 = (nb + 31) / 32, ng = (nb + 63) / 64;
+  bucket_bits_kernel<<<grid_for(nw32 * 32, 256), 256, 0, st>>>(offsets, nb, bits32);
+  group_count_kernel<<<grid_for(ng, 256), 256, 0, st>>>(bits32, nw32, ng, gcnt);
+  int k = exclusive_scan_u32(st, gcnt, grank, ng, scan_tmp, n_occ);
+  group_pack_kernel<<<grid_for(ng, 256), 256, 0, st>>>(bits32, nw32, grank, ng, groups);
+  compact_starts_kernel<<<grid_for(nb, 256), 256, 0, st>>>(offsets, nb, groups, n_occ, cstart);
+  return k + 4;
 }
 
 void launch_order_buckets(cudaStream_t st, const uint32_t* offsets, int64_t nb, uint2* post) {

@@ -109,6 +109,13 @@ void launch_count_tuples(cudaStream_t st, const uint32_t* packed, const DevRecor
                          uint32_t* count);
 void launch_threshold(cudaStream_t st, const uint32_t* count, int64_t nb, uint32_t thres,
                       uint32_t* eff);
+// Compact bucket directory (index.cu): groups[g] = (occupancy bits of
+// buckets 64 g .. 64 g + 63 as lo, hi words, occupied buckets before the
+// group, 0); cstart[r] = start of the r-th occupied bucket, cstart[n_occ] =
+// total.  Scratch: bits32 (nb / 32), gcnt and grank (nb / 64), scan_tmp.
+int build_bucket_directory(cudaStream_t st, const uint32_t* offsets, int64_t nb, uint32_t* bits32,
+                           uint32_t* gcnt, uint32_t* grank, void* scan_tmp, uint32_t* n_occ,
+                           uint4* groups, uint32_t* cstart);
 void launch_scatter_tuples(cudaStream_t st, const uint32_t* packed, const DevRecord* recs,
                            const uint64_t* tbase, int n_recs, uint64_t n_tuples, int k,
                            uint32_t thres, const uint32_t* count, const uint32_t* offsets,
@@ -129,6 +136,8 @@ struct SeedArgs {
   const DevRead* rd;
   int64_t n_reads;
   const uint32_t* offsets;    // bucket starts, 4^k + 1 entries
+  const uint4* groups;        // compact bucket directory (index.cu)
+  const uint32_t* cstart;
   const uint2* postings;      // (ref_pos, ref_idx)
   int k;
   int max_hits;
@@ -211,8 +220,8 @@ int launch_sw(cudaStream_t st, const SwArgs& a, std::string* err);
 
 // sw_fast.cu: packed 16-bit passes (score of every pair; trace of printed pairs)
 // Bound-pass suffix maxima: blocks of wavefront steps, blocks per pair.
-constexpr int kSufSteps = 32;
-constexpr int kSufBlocks = 16;
+constexpr int kSufSteps = 16;
+constexpr int kSufBlocks = 32;
 struct FastArgs {
   const char* q;
   const char* w;

@@ -83,11 +83,18 @@ __global__ void __launch_bounds__(kSeedWarps * 32) seed_warp_kernel(SeedArgs a) 
     int i = lane + 32 * m;
     beg[m] = cnt[m] = 0;
     if (i < nq) {
-      uint32_t h = hash_at(codes, i, k);
-      uint32_t b = __ldg(&a.offsets[h]), e = __ldg(&a.offsets[h + 1]);
-      beg[m] = b;
-      cnt[m] = e - b;
-      my += e - b;
+      const uint32_t h = hash_at(codes, i, k);
+      // compact bucket directory: occupancy bits and rank, then the start
+      // of occupied buckets only
+      const uint4 grp = __ldg(&a.groups[h >> 6]);
+      const uint64_t bits = ((uint64_t)grp.y << 32) | grp.x;
+      if ((bits >> (h & 63)) & 1u) {
+        const uint32_t r = grp.z + (uint32_t)__popcll(bits & ((1ull << (h & 63)) - 1));
+        const uint32_t b = __ldg(&a.cstart[r]), e = __ldg(&a.cstart[r + 1]);
+        beg[m] = b;
+        cnt[m] = e - b;
+        my += e - b;
+      }
     }
   }
   uint32_t incl = my;
