@@ -80,6 +80,9 @@ typedef struct {
                             needed no exact score                            */
   int64_t retraced_pairs;/* printed pairs traced after selection (bounded
                             selection: the read's candidate was not best)    */
+  double first_pass_ms;  /* the packed path's first kernel alone: the score
+                            bound (default) or the exact score pass          */
+  int64_t first_pass_cells; /* DP cells that kernel covered               */
 } swift_stats;
 
 void swift_params_default(swift_params *p);

@@ -58,7 +58,8 @@ class Stats(C.Structure):
         ("seed_overflow_strands", C.c_int64), ("sw_generic_pairs", C.c_int64),
         ("launches", C.c_int64), ("host_parse_ms", C.c_double), ("h2d_ms", C.c_double),
         ("d2h_ms", C.c_double), ("traced_pairs", C.c_int64), ("bound_pruned", C.c_int64),
-        ("retraced_pairs", C.c_int64),
+        ("retraced_pairs", C.c_int64), ("first_pass_ms", C.c_double),
+        ("first_pass_cells", C.c_int64),
     ]
 
     def as_dict(self):

@@ -22,7 +22,7 @@ struct swift_ctx {
   bool own_stream = false;
   std::string err;
   int64_t total_mem = 0;
-  cudaEvent_t ev[8] = {};
+  cudaEvent_t ev[10] = {};
   char* d_text = nullptr;
   size_t text_len = 0, text_cap = 0;
   int sw_path = 0;  // 0 bounded selection, 1 generic kernel only, 2 exact score of every pair
@@ -488,7 +488,7 @@ int swift_ctx_create(int device, void* stream, swift_ctx** out) {
     e = cudaMemGetInfo(&fr, &tot);
     ctx->total_mem = (int64_t)tot;
   }
-  for (int i = 0; i < 8 && e == cudaSuccess; ++i) e = cudaEventCreate(&ctx->ev[i]);
+  for (int i = 0; i < 10 && e == cudaSuccess; ++i) e = cudaEventCreate(&ctx->ev[i]);
   if (e != cudaSuccess) {
     delete ctx;
     return SWIFT_E_CUDA;
@@ -503,7 +503,7 @@ int swift_ctx_destroy(swift_ctx* ctx) {
   cudaSetDevice(ctx->device);
   if (ctx->st) cudaStreamSynchronize(ctx->st);
   if (ctx->d_text) cudaFree(ctx->d_text);
-  for (int i = 0; i < 8; ++i)
+  for (int i = 0; i < 10; ++i)
     if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
   if (ctx->own_stream) cudaStreamDestroy(ctx->st);
   delete ctx;
@@ -1036,12 +1036,14 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
   }
   fa2.ub = ub;
   fa2.suf = suf;
+  CK(cudaEventRecord(ctx->ev[7], st));
   if (fast_ok && nproc > 0) {
     fa2.list = fast_list;
     fa2.count = cnt;
     launches += bounded ? launch_sw_bound(st, fa2, nproc) : launch_sw_score(st, fa2, nproc);
     CKLAUNCH();
   }
+  CK(cudaEventRecord(ctx->ev[8], st));
   if (nproc > 0) {
     sa.list = gen_list;
     sa.count = cnt + 1;
@@ -1192,6 +1194,9 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
     s.pairs_ms = t;
     cudaEventElapsedTime(&t, ctx->ev[2], ctx->ev[3]);
     s.sw_ms = t;
+    cudaEventElapsedTime(&t, ctx->ev[7], ctx->ev[8]);
+    s.first_pass_ms = t;
+    s.first_pass_cells = fast_ok ? (int64_t)h_cnt[0] * Q * kWin : 0;
     cudaEventElapsedTime(&t, ctx->ev[3], ctx->ev[6]);
     s.select_ms = t;
     cudaEventElapsedTime(&t, ctx->ev[6], ctx->ev[4]);
