@@ -162,6 +162,39 @@ int swift_sw_batch_noalloc(swift_ctx *ctx, const char *qry, const char *ref, int
                            int32_t *start, int32_t *end, int32_t *len, char *qcons,
                            char *rcons);
 
+/* Statistics of one swift_sw_pairs call. */
+typedef struct {
+  double ms;               /* device time of the call (CUDA events)           */
+  int64_t pairs, cells;    /* cells = sum over pairs of q_len * r_len         */
+  int64_t segments;        /* groups of one shape, one launch set each        */
+  int64_t generic_pairs;   /* pairs on the int32 kernel                       */
+  int64_t launches;        /* kernels this library launched                   */
+} swift_pairs_stats;
+
+/* Phase 2 on explicit pairs of varying lengths: the batched form of
+ * alignSequences (src/align.cu:2904-2921, whose pairs all share one query
+ * and window length).  Pair i aligns qry[q_off[i], q_off[i] + q_len[i])
+ * against ref[r_off[i], r_off[i] + r_len[i]) with the reference kernel's
+ * recurrence, tie rules and traceback.  Outputs per pair: score, start,
+ * end, length and, when qcons/rcons are not NULL, the reversed consensus
+ * strings at qcons/rcons + i * cons_stride (cons_stride >= q_len + r_len + 2
+ * for every pair, a multiple of 4).  1 <= q_len <= 256; 1 <= r_len <= 1024
+ * (768 when q_len > 128).  Inputs all host or all device memory; outputs
+ * likewise.
+ *   mode 0 (batched): pairs sorted by (q_len, r_len) on the device, one set
+ *          of launches per shape: packed 16-bit passes for pairs of ACGT
+ *          bytes, the int32 kernel for the rest;
+ *   mode 1 (plain): every pair padded to the largest shape, one launch of
+ *          the int32 kernel, as the reference runs a batch.  Padding leaves
+ *          results unchanged when mismatch and both gap penalties are
+ *          negative (otherwise mode 1 is refused, SWIFT_E_ARG); bytes 0x00
+ *          and 0x01 are the padding and are refused in pairs (SWIFT_E_INPUT). */
+int swift_sw_pairs(swift_ctx *ctx, const char *qry, const int64_t *q_off, const int32_t *q_len,
+                   const char *ref, const int64_t *r_off, const int32_t *r_len, int64_t n_pairs,
+                   int32_t match, int32_t mismatch, int32_t gap_open, int32_t gap_ext,
+                   int32_t *score, int32_t *start, int32_t *end, int32_t *len, char *qcons,
+                   char *rcons, int64_t cons_stride, int32_t mode, swift_pairs_stats *stats);
+
 /* The whole pipeline on a reads FASTA in host memory: seeding, windows,
  * Smith-Waterman, best alignment per read, default records.  *out receives
  * a buffer owned by the library (free with swift_free). */

@@ -25,7 +25,7 @@ EXPORTS = [
     "swift_seed", "swift_sw_batch", "swift_align", "swift_reads_upload",
     "swift_reads_destroy", "swift_align_resident", "swift_fetch_output",
     "swift_align_files", "swift_free", "swift_peak_dpx", "swift_align_into",
-    "swift_sw_batch_noalloc",
+    "swift_sw_batch_noalloc", "swift_sw_pairs",
 ]
 
 
@@ -46,6 +46,14 @@ class Params(C.Structure):
 class Match(C.Structure):
     _fields_ = [("read", C.c_int32), ("strand", C.c_int32), ("ref_idx", C.c_int32),
                 ("shift", C.c_int32), ("ref_pos", C.c_int32)]
+
+
+class PairsStats(C.Structure):
+    _fields_ = [("ms", C.c_double), ("pairs", C.c_int64), ("cells", C.c_int64),
+                ("segments", C.c_int64), ("generic_pairs", C.c_int64), ("launches", C.c_int64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class Stats(C.Structure):
@@ -95,6 +103,8 @@ def lib():
         L.swift_align.argtypes = [vp, vp, vp, sz, C.POINTER(Params), C.POINTER(vp),
                                   C.POINTER(sz), C.POINTER(Stats)]
         L.swift_sw_batch_noalloc.argtypes = L.swift_sw_batch.argtypes
+        L.swift_sw_pairs.argtypes = [vp, vp, vp, vp, vp, vp, vp, i64, i32, i32, i32, i32,
+                                     vp, vp, vp, vp, vp, vp, i64, i32, C.POINTER(PairsStats)]
         L.swift_align_into.argtypes = [vp, vp, vp, sz, C.POINTER(Params), vp, sz, C.POINTER(sz),
                                        C.POINTER(Stats)]
         L.swift_reads_upload.argtypes = [vp, C.c_char_p, sz, C.POINTER(vp)]
@@ -199,6 +209,40 @@ class Context:
             out.append(dict(score=float(score[i]), start=int(start[i]), end=int(end[i]), len=L,
                             qcons=bytes(qc[i, :max(L, 0)]), rcons=bytes(rc[i, :max(L, 0)])))
         return out
+
+    def sw_pairs(self, qry: bytes, q_off, q_len, ref: bytes, r_off, r_len, match=2, mismatch=-1,
+                 gap_open=-10, gap_ext=-1, mode=0, consensus=True):
+        """Pairs of varying lengths (host buffers): pair i aligns
+        qry[q_off[i]:q_off[i]+q_len[i]] against ref[r_off[i]:r_off[i]+r_len[i]].
+        Returns (dict of numpy arrays, stats); consensus strings as lists of
+        bytes when asked for."""
+        import numpy as np
+        q_off = np.ascontiguousarray(q_off, dtype=np.int64)
+        r_off = np.ascontiguousarray(r_off, dtype=np.int64)
+        q_len = np.ascontiguousarray(q_len, dtype=np.int32)
+        r_len = np.ascontiguousarray(r_len, dtype=np.int32)
+        n = len(q_len)
+        qb = np.frombuffer(qry, dtype=np.uint8) if len(qry) else np.zeros(1, np.uint8)
+        rb = np.frombuffer(ref, dtype=np.uint8) if len(ref) else np.zeros(1, np.uint8)
+        out = {k: np.zeros(max(n, 1), np.int32) for k in ("score", "start", "end", "len")}
+        cs = 0
+        qc = rc = None
+        if consensus and n:
+            cs = (int((q_len + r_len).max()) + 2 + 3) & ~3
+            qc = np.zeros((n, cs), np.uint8)
+            rc = np.zeros((n, cs), np.uint8)
+        st = PairsStats()
+        self._check(lib().swift_sw_pairs(
+            self._h, qb.ctypes.data, q_off.ctypes.data, q_len.ctypes.data, rb.ctypes.data,
+            r_off.ctypes.data, r_len.ctypes.data, n, match, mismatch, gap_open, gap_ext,
+            out["score"].ctypes.data, out["start"].ctypes.data, out["end"].ctypes.data,
+            out["len"].ctypes.data, qc.ctypes.data if qc is not None else None,
+            rc.ctypes.data if rc is not None else None, cs, mode, C.byref(st)))
+        res = {k: v[:n] for k, v in out.items()}
+        if qc is not None:
+            res["qcons"] = [bytes(qc[i, :max(int(res["len"][i]), 0)]) for i in range(n)]
+            res["rcons"] = [bytes(rc[i, :max(int(res["len"][i]), 0)]) for i in range(n)]
+        return res, st.as_dict()
 
     # -- whole pipeline ----------------------------------------------------------
     def align(self, index: "Index", reads_fasta, params: Params | None = None,

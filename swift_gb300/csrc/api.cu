@@ -896,6 +896,335 @@ int swift_sw_batch_noalloc(swift_ctx* ctx, const char* qry, const char* ref, int
   return SWIFT_OK;
 }
 
+static bool device_ptr(const void* p) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+__global__ void aln_to_i32_kernel(const DevAln* __restrict__ aln, int64_t n, int32_t* score,
+                                  int32_t* start, int32_t* end, int32_t* len) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const DevAln a = aln[i];
+  score[i] = a.score;
+  start[i] = a.start;
+  end[i] = a.end;
+  len[i] = a.len;
+}
+
+int swift_sw_pairs(swift_ctx* ctx, const char* qry, const int64_t* q_off, const int32_t* q_len,
+                   const char* ref, const int64_t* r_off, const int32_t* r_len, int64_t n,
+                   int32_t m, int32_t x, int32_t o, int32_t e, int32_t* score, int32_t* start,
+                   int32_t* end, int32_t* len, char* qcons, char* rcons, int64_t cs, int32_t mode,
+                   swift_pairs_stats* stats) {
+  if (!ctx || !qry || !q_off || !q_len || !ref || !r_off || !r_len || !score || !start || !end ||
+      !len)
+    return fail(ctx, SWIFT_E_ARG, "null argument");
+  if ((qcons == nullptr) != (rcons == nullptr)) return fail(ctx, SWIFT_E_ARG, "qcons and rcons: both or neither");
+  if (n < 0) return fail(ctx, SWIFT_E_ARG, "negative pair count");
+  if (mode != 0 && mode != 1) return fail(ctx, SWIFT_E_ARG, "mode must be 0 (batched) or 1 (plain)");
+  if (mode == 1 && !(x < 0 && o < 0 && e < 0))
+    return fail(ctx, SWIFT_E_ARG,
+                "plain mode pads pairs, which is exact only with negative mismatch and gap penalties");
+  if (qcons && (cs <= 0 || cs % 4 != 0)) return fail(ctx, SWIFT_E_ARG, "cons_stride must be a positive multiple of 4");
+  swift_pairs_stats ps;
+  memset(&ps, 0, sizeof(ps));
+  ps.pairs = n;
+  if (n == 0) {
+    if (stats) *stats = ps;
+    return SWIFT_OK;
+  }
+  CK(cudaSetDevice(ctx->device));
+  cudaStream_t st = ctx->st;
+  Scratch sc(st);
+  const bool in_dev = device_ptr(qry);
+  if (in_dev != device_ptr(ref) || in_dev != device_ptr(q_off) || in_dev != device_ptr(q_len) ||
+      in_dev != device_ptr(r_off) || in_dev != device_ptr(r_len))
+    return fail(ctx, SWIFT_E_ARG, "inputs must be all host or all device memory");
+  const bool out_dev = device_ptr(score);
+  if (out_dev != device_ptr(start) || out_dev != device_ptr(end) || out_dev != device_ptr(len) ||
+      (qcons && (out_dev != device_ptr(qcons) || out_dev != device_ptr(rcons))))
+    return fail(ctx, SWIFT_E_ARG, "outputs must be all host or all device memory");
+  // inputs on the device
+  const char *dq = qry, *dr = ref;
+  const int64_t *dqo = q_off, *dro = r_off;
+  const int32_t *dql = q_len, *drl = r_len;
+  if (!in_dev) {
+    int64_t qext = 0, rext = 0;
+    for (int64_t i = 0; i < n; ++i) {
+      if (q_len[i] < 1 || r_len[i] < 1 || q_off[i] < 0 || r_off[i] < 0)
+        return fail(ctx, SWIFT_E_ARG, "pair lengths must be >= 1 and offsets >= 0");
+      qext = std::max<int64_t>(qext, q_off[i] + q_len[i]);
+      rext = std::max<int64_t>(rext, r_off[i] + r_len[i]);
+    }
+    char *tq, *tr;
+    int64_t *tqo, *tro;
+    int32_t *tql, *trl;
+    CK(sc.get(&tq, (size_t)qext));
+    CK(sc.get(&tr, (size_t)rext));
+    CK(sc.get(&tqo, (size_t)n));
+    CK(sc.get(&tro, (size_t)n));
+    CK(sc.get(&tql, (size_t)n));
+    CK(sc.get(&trl, (size_t)n));
+    CK(cudaMemcpyAsync(tq, qry, qext, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(tr, ref, rext, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(tqo, q_off, n * 8, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(tro, r_off, n * 8, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(tql, q_len, n * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(trl, r_len, n * 4, cudaMemcpyHostToDevice, st));
+    dq = tq; dr = tr; dqo = tqo; dro = tro; dql = tql; drl = trl;
+  }
+  CK(cudaEventRecord(ctx->ev[0], st));
+  // shape limits over all pairs
+  int32_t* mx;
+  CK(sc.get(&mx, 4));
+  const int32_t mx0[4] = {0, 0, 0x7fffffff, 0};
+  CK(cudaMemcpyAsync(mx, mx0, sizeof(mx0), cudaMemcpyHostToDevice, st));
+  launch_var_max_len(st, dql, drl, n, mx);
+  CKLAUNCH();
+  int32_t h_mx[4];
+  CK(cudaMemcpyAsync(h_mx, mx, sizeof(h_mx), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  const int maxQ = h_mx[0], maxR = h_mx[1];
+  if (h_mx[2] < 1) return fail(ctx, SWIFT_E_ARG, "pair lengths must be >= 1");
+  if (maxQ > kMaxQ || maxR > kMaxR || (maxQ > 128 && maxR > 768))
+    return fail(ctx, SWIFT_E_LIMIT, "q_len <= 256 and r_len <= 1024 (768 when q_len > 128)");
+  if (qcons && cs < (int64_t)h_mx[3] + 2) return fail(ctx, SWIFT_E_ARG, "cons_stride below q_len + r_len + 2");
+  const int64_t q_stride = ((int64_t)maxQ + 16) & ~(int64_t)15;
+  const int64_t w_stride = ((int64_t)maxR + 16) & ~(int64_t)15;
+  int bias0 = 0;
+  // chunks bound the fixed-stride copies and the traceback scratch
+  const int64_t chunk = 4 << 20;
+  const int64_t nc = std::min<int64_t>(n, chunk);
+  char *qbuf, *wbuf;
+  DevAln* aln;
+  int2* best2;
+  uint32_t *key, *hist, *hstart, *fill, *occ, *segpos, *nseg_d, *bad;
+  int32_t *sorted, *seg_key, *seg_start, *seg_count;
+  void* tmp;
+  CK(sc.get(&qbuf, (size_t)(nc * q_stride)));
+  CK(sc.get(&wbuf, (size_t)(nc * w_stride)));
+  CK(sc.get(&aln, (size_t)nc));
+  CK(sc.get(&best2, (size_t)nc));
+  CK(sc.get(&key, (size_t)nc));
+  CK(sc.get(&sorted, (size_t)nc));
+  CK(sc.get(&hist, kVarKeys));
+  CK(sc.get(&hstart, kVarKeys + 1));
+  CK(sc.get(&fill, kVarKeys));
+  CK(sc.get(&occ, kVarKeys));
+  CK(sc.get(&segpos, kVarKeys + 1));
+  CK(sc.get(&nseg_d, 2));
+  CK(sc.get(&bad, 1));
+  CK(cudaMemsetAsync(bad, 0, sizeof(uint32_t), st));
+  CK(sc.get(&seg_key, kVarKeys));
+  CK(sc.get(&seg_start, kVarKeys));
+  CK(sc.get(&seg_count, kVarKeys));
+  CK(sc.get((uint8_t**)&tmp, scan_temp_bytes(std::max<int64_t>(kVarKeys, nc))));
+  // outputs staged on the device when the caller's are host memory
+  int32_t *os = score, *ost = start, *oe = end, *ol = len;
+  char *oqc = qcons, *orc = rcons;
+  if (!out_dev) {
+    CK(sc.get(&os, (size_t)nc));
+    CK(sc.get(&ost, (size_t)nc));
+    CK(sc.get(&oe, (size_t)nc));
+    CK(sc.get(&ol, (size_t)nc));
+    if (qcons) {
+      CK(sc.get(&oqc, (size_t)(nc * cs)));
+      CK(sc.get(&orc, (size_t)(nc * cs)));
+    }
+  }
+  uint32_t* dirs = nullptr;
+  int64_t dirs_words = 0;
+  int launches = 0;
+  for (int64_t c0 = 0; c0 < n; c0 += chunk) {
+    const int64_t cn = std::min(chunk, n - c0);
+    char* cq = qcons ? (out_dev ? qcons + c0 * cs : oqc) : nullptr;
+    char* cr = qcons ? (out_dev ? rcons + c0 * cs : orc) : nullptr;
+    VarPairArgs va;
+    memset(&va, 0, sizeof(va));
+    va.qry = dq;
+    va.q_off = dqo + c0;
+    va.q_len = dql + c0;
+    va.ref = dr;
+    va.r_off = dro + c0;
+    va.r_len = drl + c0;
+    va.n = cn;
+    va.qbuf = qbuf;
+    va.wbuf = wbuf;
+    va.q_stride = q_stride;
+    va.w_stride = w_stride;
+    va.fast_ok = mode == 0 && fast_params_ok(64, 300, m, x, o, e, &bias0);
+    va.fast_max_r = kFastMaxR;
+    va.key = key;
+    va.hist = hist;
+    va.bad = bad;
+    CK(cudaMemsetAsync(hist, 0, kVarKeys * sizeof(uint32_t), st));
+    launch_pack_var(st, va);
+    CKLAUNCH();
+    ++launches;
+    if (mode == 1) {
+      // padding bytes must not occur in the pairs (see pack_var_kernel)
+      uint32_t h_bad = 0;
+      CK(cudaMemcpyAsync(&h_bad, bad, 4, cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+      if (h_bad)
+        return fail(ctx, SWIFT_E_INPUT, "plain mode: bytes 0x00 and 0x01 are reserved for padding");
+      SwArgs sa;
+      memset(&sa, 0, sizeof(sa));
+      sa.q = qbuf;
+      sa.w = wbuf;
+      sa.q_stride = q_stride;
+      sa.w_stride = w_stride;
+      sa.Q = maxQ;
+      sa.R = maxR;
+      sa.match = m;
+      sa.mismatch = x;
+      sa.gap_open = o;
+      sa.gap_ext = e;
+      sa.n = cn;
+      sa.aln = aln;
+      sa.qcons = cq;
+      sa.rcons = cr;
+      sa.cons_stride = cs;
+      int rc = launch_sw(st, sa, &ctx->err);
+      if (rc != SWIFT_OK) return rc;
+      CKLAUNCH();
+      ++launches;
+      ps.segments += 1;
+      ps.generic_pairs += cn;
+    } else {
+      // counting sort by shape key; the segment table goes to the host
+      int k = exclusive_scan_u32(st, hist, hstart, kVarKeys, tmp, hstart + kVarKeys);
+      launch_var_occupied(st, hist, occ);
+      k += exclusive_scan_u32(st, occ, segpos, kVarKeys, tmp, nseg_d);
+      launch_var_segments(st, hist, hstart, segpos, seg_key, seg_start, seg_count);
+      CK(cudaMemsetAsync(fill, 0, kVarKeys * sizeof(uint32_t), st));
+      launch_var_scatter(st, key, cn, hstart, fill, sorted);
+      CKLAUNCH();
+      launches += k + 3;
+      uint32_t nseg = 0;
+      CK(cudaMemcpyAsync(&nseg, nseg_d, 4, cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+      std::vector<int32_t> hk(nseg), hs(nseg), hc(nseg);
+      if (nseg) {
+        CK(cudaMemcpyAsync(hk.data(), seg_key, nseg * 4, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(hs.data(), seg_start, nseg * 4, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(hc.data(), seg_count, nseg * 4, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+      }
+      ps.segments += nseg;
+      for (uint32_t s = 0; s < nseg; ++s) {
+        const int Q = (hk[s] >> 11) & 511, R = hk[s] & 2047;
+        const bool gen = (hk[s] >> 20) & 1;
+        const int64_t cnt = hc[s];
+        int32_t* list = sorted + hs[s];
+        int bias = 0;
+        if (gen || !fast_params_ok(Q, R, m, x, o, e, &bias)) {
+          SwArgs sa;
+          memset(&sa, 0, sizeof(sa));
+          sa.q = qbuf;
+          sa.w = wbuf;
+          sa.q_stride = q_stride;
+          sa.w_stride = w_stride;
+          sa.Q = Q;
+          sa.R = R;
+          sa.match = m;
+          sa.mismatch = x;
+          sa.gap_open = o;
+          sa.gap_ext = e;
+          sa.n = cnt;
+          sa.aln = aln;
+          sa.qcons = cq;
+          sa.rcons = cr;
+          sa.cons_stride = cs;
+          sa.list = list;
+          sa.count = seg_count + s;
+          int rc = launch_sw(st, sa, &ctx->err);
+          if (rc != SWIFT_OK) return rc;
+          CKLAUNCH();
+          ++launches;
+          ps.generic_pairs += cnt;
+          continue;
+        }
+        // packed trace pass + walk, in sub-chunks that bound the direction scratch
+        const int64_t sub = 262144;
+        const int64_t words = trace_scratch_words(Q, R, std::min(cnt, sub));
+        if (words > dirs_words) {
+          CK(sc.get(&dirs, (size_t)words));
+          dirs_words = words;
+        }
+        FastArgs fa;
+        memset(&fa, 0, sizeof(fa));
+        fa.q = qbuf;
+        fa.w = wbuf;
+        fa.q_stride = q_stride;
+        fa.w_stride = w_stride;
+        fa.Q = Q;
+        fa.R = R;
+        fa.match = m;
+        fa.mismatch = x;
+        fa.gap_open = o;
+        fa.gap_ext = e;
+        fa.bias = bias;
+        fa.aln = aln;
+        fa.best = best2;
+        fa.dirs = dirs;
+        fa.qcons = cq;
+        fa.rcons = cr;
+        fa.cons_stride = cs;
+        fa.list = list;
+        fa.count = seg_count + s;
+        for (int64_t off = 0; off < cnt; off += sub) {
+          fa.list_offset = off;
+          const int kk = launch_sw_trace(st, fa, std::min(sub, cnt - off));
+          if (kk == 0) return fail(ctx, SWIFT_E_DEVICE, "trace pass could not launch");
+          launches += kk;
+          CKLAUNCH();
+        }
+      }
+    }
+    aln_to_i32_kernel<<<(unsigned)((cn + 255) / 256), 256, 0, st>>>(
+        aln, cn, out_dev ? score + c0 : os, out_dev ? start + c0 : ost, out_dev ? end + c0 : oe,
+        out_dev ? len + c0 : ol);
+    CKLAUNCH();
+    ++launches;
+    if (!out_dev) {
+      CK(cudaMemcpyAsync(score + c0, os, cn * 4, cudaMemcpyDeviceToHost, st));
+      CK(cudaMemcpyAsync(start + c0, ost, cn * 4, cudaMemcpyDeviceToHost, st));
+      CK(cudaMemcpyAsync(end + c0, oe, cn * 4, cudaMemcpyDeviceToHost, st));
+      CK(cudaMemcpyAsync(len + c0, ol, cn * 4, cudaMemcpyDeviceToHost, st));
+      if (qcons) {
+        CK(cudaMemcpyAsync(qcons + c0 * cs, oqc, cn * cs, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(rcons + c0 * cs, orc, cn * cs, cudaMemcpyDeviceToHost, st));
+      }
+      CK(cudaStreamSynchronize(st));  // the staging buffers are reused by the next chunk
+    }
+  }
+  CK(cudaEventRecord(ctx->ev[1], st));
+  CK(cudaEventSynchronize(ctx->ev[1]));
+  float t = 0;
+  cudaEventElapsedTime(&t, ctx->ev[0], ctx->ev[1]);
+  ps.ms = t;
+  ps.launches = launches + 1;
+  if (stats) {
+    // cells need the lengths on the host
+    if (!in_dev) {
+      for (int64_t i = 0; i < n; ++i) ps.cells += (int64_t)q_len[i] * r_len[i];
+    } else {
+      std::vector<int32_t> a(n), b(n);
+      CK(cudaMemcpy(a.data(), q_len, n * 4, cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(b.data(), r_len, n * 4, cudaMemcpyDeviceToHost));
+      for (int64_t i = 0; i < n; ++i) ps.cells += (int64_t)a[i] * b[i];
+    }
+    *stats = ps;
+  }
+  return SWIFT_OK;
+}
+
 int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_reads* rd,
                          const swift_params* p, size_t* out_len, swift_stats* stats) {
   if (!ctx || !idx || !rd || !p) return fail(ctx, SWIFT_E_ARG, "null argument");

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -218,6 +219,35 @@ constexpr int64_t kStaticSwPairs = SWIFT_SW_NOALLOC_MAX_PAIRS;
 int static_sw_scratch(int device, DevAln** out, std::string* err);
 int launch_sw(cudaStream_t st, const SwArgs& a, std::string* err);
 
+// pairs_var.cu: explicit pairs of varying lengths, sorted by shape
+constexpr uint32_t kVarKeys = 1u << 21;  // shape keys: generic bit, Q (9 bits), R (11 bits)
+struct VarPairArgs {
+  const char* qry;            // query bytes of pair i at qry + q_off[i], q_len[i] of them
+  const int64_t* q_off;
+  const int32_t* q_len;
+  const char* ref;            // window bytes at ref + r_off[i], r_len[i] of them
+  const int64_t* r_off;
+  const int32_t* r_len;
+  int64_t n;
+  char* qbuf;                 // fixed strides, NUL padded
+  char* wbuf;
+  int64_t q_stride, w_stride;
+  bool fast_ok;               // scoring the packed passes take
+  int fast_max_r;
+  uint32_t* key;              // per pair
+  uint32_t* hist;             // per key
+  uint32_t* bad;              // set when a pair holds byte 0x00 or 0x01
+};
+void launch_var_max_len(cudaStream_t st, const int32_t* q_len, const int32_t* r_len, int64_t n,
+                        int32_t* out);
+void launch_pack_var(cudaStream_t st, const VarPairArgs& a);
+void launch_var_occupied(cudaStream_t st, const uint32_t* hist, uint32_t* occ);
+void launch_var_segments(cudaStream_t st, const uint32_t* hist, const uint32_t* start,
+                         const uint32_t* seg_pos, int32_t* seg_key, int32_t* seg_start,
+                         int32_t* seg_count);
+void launch_var_scatter(cudaStream_t st, const uint32_t* key, int64_t n, const uint32_t* start,
+                        uint32_t* fill, int32_t* sorted);
+
 // sw_fast.cu: packed 16-bit passes (score of every pair; trace of printed pairs)
 // Bound-pass suffix maxima: blocks of wavefront steps, blocks per pair.
 constexpr int kSufSteps = 16;
@@ -245,6 +275,7 @@ struct FastArgs {
   int64_t cons_stride;
 };
 bool fast_params_ok(int Q, int R, int m, int x, int o, int e, int* bias);
+constexpr int kFastMaxR = 512;  // window columns the packed passes take
 int64_t trace_scratch_words(int Q, int R, int64_t pairs);
 int launch_sw_score(cudaStream_t st, const FastArgs& a, int64_t max_pairs);
 int launch_sw_trace(cudaStream_t st, const FastArgs& a, int64_t max_pairs);

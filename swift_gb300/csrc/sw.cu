@@ -140,8 +140,16 @@ __device__ __forceinline__ void generic_pair(const SwArgs& a, int64_t pair, uint
     int ln = (i - 1) / RPL, k = (i - 1) % RPL;
     return ((uint32_t)dirs[jj * 32 + ln] >> (2 * k)) & 3u;
   };
-  char* qc = a.qcons + pair * a.cons_stride;
-  char* rc = a.rcons + pair * a.cons_stride;
+  // consensus strings are optional (coordinates only when the caller passes none)
+  const bool cons = a.qcons != nullptr;
+  char* qc = cons ? a.qcons + pair * a.cons_stride : nullptr;
+  char* rc = cons ? a.rcons + pair * a.cons_stride : nullptr;
+  auto put = [&](int t, char r, char q) {
+    if (cons) {
+      rc[t] = r;
+      qc[t] = q;
+    }
+  };
   int cur = cell_max, cr = cur / W, cc = cur % W, nxt;
   uint32_t d0 = dir_at(cur);
   nxt = d0 == kUp ? cur - W : d0 == kLeft ? cur - 1 : d0 == kDiag ? cur - W - 1 : cur;
@@ -149,9 +157,9 @@ __device__ __forceinline__ void generic_pair(const SwArgs& a, int64_t pair, uint
   int tick = -1, nref = -1, start = 0;
   while ((cr != nr || cc != nc) && nc != 0 && nr != 0) {
     ++tick;
-    if (nc == cc) rc[tick] = '-';
-    else { rc[tick] = wg[cc - 1]; ++nref; }
-    qc[tick] = nr == cr ? '-' : qg[cr - 1];
+    char rch = '-';
+    if (nc != cc) { rch = wg[cc - 1]; ++nref; }
+    put(tick, rch, nr == cr ? '-' : qg[cr - 1]);
     start = cc;
     cur = nxt; cr = nr; cc = nc;
     uint32_t dd = dir_at(cur);
@@ -161,9 +169,9 @@ __device__ __forceinline__ void generic_pair(const SwArgs& a, int64_t pair, uint
   }
   if ((cr != nr || cc != nc) && (nc == 0 || nr == 0)) {
     ++tick;
-    if (nc == cc) rc[tick] = '-';
-    else { rc[tick] = wg[cc - 1]; ++nref; }
-    qc[tick] = nr == cr ? '-' : qg[cr - 1];
+    char rch = '-';
+    if (nc != cc) { rch = wg[cc - 1]; ++nref; }
+    put(tick, rch, nr == cr ? '-' : qg[cr - 1]);
     start = cc;
   }
   DevAln out;

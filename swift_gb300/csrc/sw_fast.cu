@@ -52,7 +52,6 @@ namespace swift {
 namespace {
 
 constexpr int kPkWarps = 8;
-constexpr int kFastMaxR = 512;  // window columns the packed passes take
 
 __device__ __forceinline__ uint32_t base_class(uint32_t c) {
   uint32_t u = c & 0xDFu;
@@ -496,16 +495,20 @@ __global__ void __launch_bounds__(256) sw_walk_kernel(FastArgs a) {
     return (word >> (shift_half + 2 * (k & 7))) & 3u;
   };
   // consensus bytes are gathered four at a time and stored as words
-  uint32_t* qcw = reinterpret_cast<uint32_t*>(a.qcons + (int64_t)p * a.cons_stride);
-  uint32_t* rcw = reinterpret_cast<uint32_t*>(a.rcons + (int64_t)p * a.cons_stride);
+  // (consensus strings are optional: coordinates only when qcons is null)
+  const bool cons = a.qcons != nullptr;
+  uint32_t* qcw = cons ? reinterpret_cast<uint32_t*>(a.qcons + (int64_t)p * a.cons_stride) : nullptr;
+  uint32_t* rcw = cons ? reinterpret_cast<uint32_t*>(a.rcons + (int64_t)p * a.cons_stride) : nullptr;
   uint32_t qacc = 0, racc = 0;
   auto emit = [&](int tick, char r, char q) {
     const int sh = 8 * (tick & 3);
     racc |= (uint32_t)(uint8_t)r << sh;
     qacc |= (uint32_t)(uint8_t)q << sh;
     if ((tick & 3) == 3) {
-      rcw[tick >> 2] = racc;
-      qcw[tick >> 2] = qacc;
+      if (cons) {
+        rcw[tick >> 2] = racc;
+        qcw[tick >> 2] = qacc;
+      }
       racc = qacc = 0;
     }
   };
@@ -563,7 +566,7 @@ __global__ void __launch_bounds__(256) sw_walk_kernel(FastArgs a) {
     emit(tick, rch, nr == cr ? '-' : qg[cr - 1]);
     start = cc;
   }
-  if (tick >= 0 && (tick & 3) != 3) {
+  if (cons && tick >= 0 && (tick & 3) != 3) {
     rcw[tick >> 2] = racc;
     qcw[tick >> 2] = qacc;
   }

@@ -1,0 +1,140 @@
+"""Pairs of varying lengths (swift_sw_pairs) against the oracle, pair by pair.
+
+Each pair is aligned on its own query and window lengths; the batched mode
+(shape-sorted launches, packed passes for ACGT pairs) and the plain mode
+(everything padded to the largest shape, int32 kernel) must both reproduce
+the oracle's score, coordinates and consensus strings exactly.
+"""
+import random
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def sg():
+    from swift_gb300 import build as b
+    b.build()
+    import swift_gb300
+    return swift_gb300
+
+
+@pytest.fixture(scope="module")
+def ctx(sg):
+    return sg.Context(0)
+
+
+@pytest.fixture(scope="module")
+def oracle():
+    from oracle import oracle as O
+    O.build()
+    return O
+
+
+def make_pairs(n, seed, q_range=(20, 250), extra=(20, 140), odd_every=9):
+    """Reads with a mutated copy inside their window; every odd_every-th pair
+    carries N, lowercase or IUPAC bytes (the int32 kernel's pairs)."""
+    rng = random.Random(seed)
+    qs, ws = [], []
+    for i in range(n):
+        Q = rng.randint(*q_range)
+        R = min(1024 if Q <= 128 else 768, Q + rng.randint(*extra))
+        w = bytearray(rng.choice(b"ACGT") for _ in range(R))
+        a = rng.randrange(0, max(1, R - Q))
+        q = bytearray(w[a:a + Q])
+        while len(q) < Q:
+            q.append(rng.choice(b"ACGT"))
+        for k in range(Q):
+            r = rng.random()
+            if r < 0.03:
+                q[k] = rng.choice(b"ACGT")
+        if rng.random() < 0.2:  # an indel
+            k = rng.randrange(1, Q - 1)
+            q = q[:k] + q[k + 1:] + bytearray([rng.choice(b"ACGT")]) if rng.random() < 0.5 \
+                else q[:k] + bytearray([rng.choice(b"ACGT")]) + q[k:-1]
+        if i % 4 == 3:  # a decoy window
+            w = bytearray(rng.choice(b"ACGT") for _ in range(R))
+        if odd_every and i % odd_every == 5:
+            q[rng.randrange(Q)] = ord("N")
+            w[rng.randrange(R)] = rng.choice(b"nRy")
+            q[: Q // 4] = q[: Q // 4].lower()
+        qs.append(bytes(q))
+        ws.append(bytes(w))
+    return qs, ws
+
+
+def pack(items):
+    off = np.zeros(len(items), np.int64)
+    ln = np.array([len(x) for x in items], np.int32)
+    off[1:] = np.cumsum(ln[:-1])
+    return b"".join(items), off, ln
+
+
+def check_against_oracle(res, qs, ws, oracle, params):
+    m, x, o, e = params
+    for i, (q, w) in enumerate(zip(qs, ws)):
+        want = oracle.sw(q, w, m=m, x=x, o=o, e=e)
+        got = (int(res["score"][i]), int(res["start"][i]), int(res["end"][i]), int(res["len"][i]))
+        assert got == (int(want["score"]), want["start"], want["end"], want["len"]), (i, got, want)
+        if "qcons" in res:
+            assert res["qcons"][i] == want["qcons"] and res["rcons"][i] == want["rcons"], i
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_pairs_vs_oracle(ctx, oracle, mode):
+    qs, ws = make_pairs(1500, seed=7 + mode)
+    qb, qo, ql = pack(qs)
+    wb, wo, wl = pack(ws)
+    res, st = ctx.sw_pairs(qb, qo, ql, wb, wo, wl, mode=mode)
+    check_against_oracle(res, qs, ws, oracle, (2, -1, -10, -1))
+    assert st["pairs"] == len(qs) and st["cells"] == int((ql.astype(np.int64) * wl).sum())
+    if mode == 0:
+        assert st["segments"] > 10 and 0 < st["generic_pairs"] < len(qs)
+
+
+def test_pairs_modes_agree_and_coordinates_only(ctx, oracle):
+    qs, ws = make_pairs(3000, seed=21, q_range=(36, 128), extra=(128, 128), odd_every=0)
+    qb, qo, ql = pack(qs)
+    wb, wo, wl = pack(ws)
+    a, sa = ctx.sw_pairs(qb, qo, ql, wb, wo, wl, mode=0)
+    b, _ = ctx.sw_pairs(qb, qo, ql, wb, wo, wl, mode=1)
+    c, _ = ctx.sw_pairs(qb, qo, ql, wb, wo, wl, mode=0, consensus=False)
+    for k in ("score", "start", "end", "len"):
+        assert np.array_equal(a[k], b[k]) and np.array_equal(a[k], c[k]), k
+    assert a["qcons"] == b["qcons"] and a["rcons"] == b["rcons"]
+    assert sa["generic_pairs"] == 0  # every pair on the packed passes
+    check_against_oracle(a, qs[:400], ws[:400], oracle, (2, -1, -10, -1))
+
+
+def test_pairs_shared_buffers_and_parameters(ctx, oracle):
+    # pairs may share query and window bytes (a read against many regions)
+    rng = random.Random(5)
+    ref = bytes(rng.choice(b"ACGT") for _ in range(20000))
+    reads = [ref[p:p + L] for p, L in ((1000, 80), (5000, 150), (12000, 40))]
+    qb, qo_r, ql_r = pack(reads)
+    q_off, q_len, r_off, r_len = [], [], [], []
+    for r in range(3):
+        for t in range(40):
+            pos = rng.randrange(0, 20000 - 300)
+            q_off.append(qo_r[r]); q_len.append(ql_r[r])
+            r_off.append(pos); r_len.append(rng.randint(50, 300))
+    qs = [qb[a:a + b] for a, b in zip(q_off, q_len)]
+    ws = [ref[a:a + b] for a, b in zip(r_off, r_len)]
+    for params in [(2, -1, -10, -1), (3, -2, -5, -2), (1, -3, -4, -1)]:
+        res, _ = ctx.sw_pairs(qb, q_off, q_len, ref, r_off, r_len, *params)
+        check_against_oracle(res, qs, ws, oracle, params)
+
+
+def test_pairs_limits(ctx, sg):
+    qb, wb = b"A" * 300, b"A" * 2000
+    for ql, wl, code in [(257, 100, -5), (200, 800, -5), (0, 10, -1)]:
+        with pytest.raises(sg.SwiftError) as e:
+            ctx.sw_pairs(qb, [0], [ql], wb, [0], [wl])
+        assert e.value.code == code
+    with pytest.raises(sg.SwiftError) as e:  # plain mode needs negative penalties
+        ctx.sw_pairs(qb, [0], [10], wb, [0], [10], 2, 1, -10, -1, mode=1)
+    assert e.value.code == -1
+    res, st = ctx.sw_pairs(b"", [], [], b"", [], [])
+    assert st["pairs"] == 0 and len(res["score"]) == 0
