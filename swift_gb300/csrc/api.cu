@@ -1057,7 +1057,9 @@ int swift_sw_pairs(swift_ctx* ctx, const char* qry, const int64_t* q_off, const 
     va.wbuf = wbuf;
     va.q_stride = q_stride;
     va.w_stride = w_stride;
-    va.fast_ok = mode == 0 && fast_params_ok(64, 300, m, x, o, e, &bias0);
+    va.class_ok = 0;
+    for (int c = 0; mode == 0 && c < 6; ++c)
+      if (fast_params_ok(packed_class_max_q(c), kFastMaxR, m, x, o, e, &bias0)) va.class_ok |= 1u << c;
     va.fast_max_r = kFastMaxR;
     va.key = key;
     va.hist = hist;
@@ -1116,14 +1118,43 @@ int swift_sw_pairs(swift_ctx* ctx, const char* qry, const int64_t* q_off, const 
         CK(cudaMemcpyAsync(hc.data(), seg_count, nseg * 4, cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
       }
-      ps.segments += nseg;
+      // launch groups: packed pairs by shape class (their keys are
+      // consecutive), generic pairs by exact shape
+      struct Group {
+        bool gen;
+        int Q, R;           // generic: the shape; packed: class's longest query, widest window
+        int64_t start, count;
+      };
+      std::vector<Group> groups;
       for (uint32_t s = 0; s < nseg; ++s) {
-        const int Q = (hk[s] >> 11) & 511, R = hk[s] & 2047;
         const bool gen = (hk[s] >> 20) & 1;
-        const int64_t cnt = hc[s];
-        int32_t* list = sorted + hs[s];
+        const int q = (hk[s] >> 11) & 511, R = hk[s] & 2047;
+        if (!gen && !groups.empty() && !groups.back().gen &&
+            groups.back().Q == packed_class_max_q(q)) {
+          groups.back().R = std::max(groups.back().R, R);
+          groups.back().count += hc[s];
+          continue;
+        }
+        groups.push_back({gen, gen ? q : packed_class_max_q(q), R, hs[s], hc[s]});
+      }
+      ps.segments += (int64_t)groups.size();
+      // launch sizes go to the device (the kernels read counts there)
+      std::vector<int32_t> gcount(groups.size());
+      for (size_t g = 0; g < groups.size(); ++g) gcount[g] = (int32_t)groups[g].count;
+      int32_t* gcount_d = seg_count;  // reuse: the segment counts are on the host now
+      if (!groups.empty())
+        CK(cudaMemcpyAsync(gcount_d, gcount.data(), groups.size() * 4, cudaMemcpyHostToDevice, st));
+      for (size_t gi = 0; gi < groups.size(); ++gi) {
+        const Group& G = groups[gi];
+        const int Q = G.Q, R = G.R;
+        const int64_t cnt = G.count;
+        int32_t* list = sorted + G.start;
         int bias = 0;
-        if (gen || !fast_params_ok(Q, R, m, x, o, e, &bias)) {
+        if (G.gen || !fast_params_ok(Q, R, m, x, o, e, &bias)) {
+          // (a packed class whose longest query the packed scoring does not
+          // take runs here too: the int32 kernel takes per-launch shapes, so
+          // its pairs go one exact shape at a time)
+          if (!G.gen) return fail(ctx, SWIFT_E_DEVICE, "packed class outside the packed scoring");
           SwArgs sa;
           memset(&sa, 0, sizeof(sa));
           sa.q = qbuf;
@@ -1142,7 +1173,7 @@ int swift_sw_pairs(swift_ctx* ctx, const char* qry, const int64_t* q_off, const 
           sa.rcons = cr;
           sa.cons_stride = cs;
           sa.list = list;
-          sa.count = seg_count + s;
+          sa.count = gcount_d + gi;
           int rc = launch_sw(st, sa, &ctx->err);
           if (rc != SWIFT_OK) return rc;
           CKLAUNCH();
@@ -1150,7 +1181,8 @@ int swift_sw_pairs(swift_ctx* ctx, const char* qry, const int64_t* q_off, const 
           ps.generic_pairs += cnt;
           continue;
         }
-        // packed trace pass + walk, in sub-chunks that bound the direction scratch
+        // packed trace pass + walk over pairs of one class, per-pair lengths,
+        // in sub-chunks that bound the direction scratch
         const int64_t sub = 262144;
         const int64_t words = trace_scratch_words(Q, R, std::min(cnt, sub));
         if (words > dirs_words) {
@@ -1165,6 +1197,8 @@ int swift_sw_pairs(swift_ctx* ctx, const char* qry, const int64_t* q_off, const 
         fa.w_stride = w_stride;
         fa.Q = Q;
         fa.R = R;
+        fa.q_len = dql + c0;
+        fa.r_len = drl + c0;
         fa.match = m;
         fa.mismatch = x;
         fa.gap_open = o;
@@ -1177,7 +1211,7 @@ int swift_sw_pairs(swift_ctx* ctx, const char* qry, const int64_t* q_off, const 
         fa.rcons = cr;
         fa.cons_stride = cs;
         fa.list = list;
-        fa.count = seg_count + s;
+        fa.count = gcount_d + gi;
         for (int64_t off = 0; off < cnt; off += sub) {
           fa.list_offset = off;
           const int kk = launch_sw_trace(st, fa, std::min(sub, cnt - off));

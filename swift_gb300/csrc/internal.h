@@ -232,7 +232,7 @@ struct VarPairArgs {
   char* qbuf;                 // fixed strides, NUL padded
   char* wbuf;
   int64_t q_stride, w_stride;
-  bool fast_ok;               // scoring the packed passes take
+  uint32_t class_ok;          // bit c: the packed passes take this scoring for class c
   int fast_max_r;
   uint32_t* key;              // per pair
   uint32_t* hist;             // per key
@@ -263,6 +263,8 @@ struct FastArgs {
   const int32_t* count;       // number of ids (device)
   int64_t list_offset;        // first id of this launch
   DevAln* aln;                // score pass: .score; trace pass: all fields
+  const int32_t* q_len;       // trace pass: per-pair query and window lengths
+  const int32_t* r_len;       // (pairs of one launch may differ), or null
   int32_t* ub;                // bound pass: upper bound of the score per pair
   uint16_t* suf;              // bound pass: per pair, kSufBlocks suffix maxima of
                               // kSufSteps-step blocks (read by the exact passes
@@ -276,6 +278,14 @@ struct FastArgs {
 };
 bool fast_params_ok(int Q, int R, int m, int x, int o, int e, int* bias);
 constexpr int kFastMaxR = 512;  // window columns the packed passes take
+// Packed shape class of a query length (the (lanes, rows) shapes of the
+// packed passes, shortest first), and the longest query of each class.
+__host__ __device__ inline int packed_class(int Q) {
+  return Q <= 32 ? 0 : Q <= 64 ? 1 : Q <= 104 ? 2 : Q <= 128 ? 3 : Q <= 208 ? 4 : Q <= 256 ? 5 : -1;
+}
+__host__ __device__ inline int packed_class_max_q(int c) {
+  return c == 0 ? 32 : c == 1 ? 64 : c == 2 ? 104 : c == 3 ? 128 : c == 4 ? 208 : 256;
+}
 int64_t trace_scratch_words(int Q, int R, int64_t pairs);
 int launch_sw_score(cudaStream_t st, const FastArgs& a, int64_t max_pairs);
 int launch_sw_trace(cudaStream_t st, const FastArgs& a, int64_t max_pairs);

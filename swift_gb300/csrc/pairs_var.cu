@@ -2,11 +2,13 @@
 // fixed-stride buffers and sorted by shape, so every launch of the existing
 // Smith-Waterman passes covers pairs of one (Q, R).
 //
-// Shape key: bits 0-10 window length R (<= 1024), bits 11-19 query length Q
-// (<= 256), bit 20 set when the pair needs the generic kernel (a byte
-// outside ACGTacgt, or a shape or scoring the packed passes do not take).
-// Pairs of one key form a segment; a counting sort over the 2^21 keys gives
-// the segments in key order.
+// Shape key: bits 0-10 window length R (<= 1024); for pairs of the packed
+// passes bits 11-19 hold the packed shape class of Q, for the others (a
+// byte outside ACGTacgt, or a shape or scoring the packed passes do not
+// take) bit 20 is set and bits 11-19 hold Q itself.  A counting sort over
+// the 2^21 keys orders the pairs by key: packed pairs of one class form one
+// launch (sorted by window length, so a warp's pairs sweep similar widths),
+// generic pairs one launch per exact shape.
 #include "internal.h"
 
 namespace swift {
@@ -52,8 +54,11 @@ __global__ void __launch_bounds__(kVarWarps * 32) pack_var_kernel(VarPairArgs a)
   bad = __any_sync(0xffffffffu, bad);
   if (lane == 0 && bad) atomicOr(a.bad, 1u);
   if (lane == 0) {
-    const bool gen = odd || !a.fast_ok || R > a.fast_max_r || Q < 1 || R < 1;
-    const uint32_t key = ((gen ? 1u : 0u) << 20) | ((uint32_t)Q << 11) | (uint32_t)R;
+    const int cls = packed_class(Q);
+    const bool gen = odd || R > a.fast_max_r || Q < 1 || R < 1 || cls < 0 ||
+                     !((a.class_ok >> cls) & 1u);
+    const uint32_t key = gen ? (1u << 20) | ((uint32_t)Q << 11) | (uint32_t)R
+                             : ((uint32_t)cls << 11) | (uint32_t)R;
     a.key[i] = key;
     atomicAdd(&a.hist[key], 1u);
   }

@@ -90,7 +90,12 @@ struct DirLayout {
 };
 __host__ __device__ constexpr int steps8(int R, int G) { return (R + G - 1 + 7) & ~7; }
 
-template <int G, int RPL, bool TRACE>
+// VAR: pairs of one launch may differ in length (a.q_len / a.r_len per pair):
+// rows past a pair's query are all-mismatch rows as usual, the warp sweeps
+// the longest window of its pairs, and columns past a pair's own window are
+// kept out of its first-maximum bookkeeping (their cells are computed but
+// never reach the maximum, the traceback or the result).
+template <int G, int RPL, bool TRACE, bool VAR>
 __device__ __forceinline__ void packed_item(const FastArgs& a, const int64_t warp, const int64_t nlist,
                                             uint32_t* wsel_all, const int wib, const int lane) {
   constexpr int kGroups = 32 / G;      // groups per warp
@@ -98,18 +103,22 @@ __device__ __forceinline__ void packed_item(const FastArgs& a, const int64_t war
   constexpr int kNW = DirLayout<RPL>::kWords;
   const int g = lane / G, sl = lane % G;
   const int64_t base = warp * kPairs + 2 * g;
-  const int Q = a.Q, R = a.R;
   const int32_t* list = a.list + a.list_offset;
   const bool has0 = base < nlist, has1 = base + 1 < nlist;
   const int32_t p0 = has0 ? list[base] : list[nlist - 1];
   const int32_t p1 = has1 ? list[base + 1] : p0;
+  const int Q0 = VAR ? a.q_len[p0] : a.Q, Q1 = VAR ? a.q_len[p1] : a.Q;
+  const int R0 = VAR ? a.r_len[p0] : a.R, R1 = VAR ? a.r_len[p1] : a.R;
+  // columns the warp sweeps
+  const int R = VAR ? (int)__reduce_max_sync(0xffffffffu, (unsigned)max(R0, R1)) : a.R;
   const char* q0 = a.q + (int64_t)p0 * a.q_stride;
   const char* q1 = a.q + (int64_t)p1 * a.q_stride;
   const char* w0 = a.w + (int64_t)p0 * a.w_stride;
   const char* w1 = a.w + (int64_t)p1 * a.w_stride;
-  uint32_t* wsel = wsel_all + (wib * kGroups + g) * (R + 1);
+  uint32_t* wsel = wsel_all + (wib * kGroups + g) * (a.R + 1);
   for (int c = sl; c < R; c += G) {
-    uint32_t s0 = base_class((uint8_t)w0[c]), s1 = base_class((uint8_t)w1[c]);
+    uint32_t s0 = (!VAR || c < R0) ? base_class((uint8_t)w0[c]) : 0u;
+    uint32_t s1 = (!VAR || c < R1) ? base_class((uint8_t)w1[c]) : 0u;
     wsel[c + 1] = s0 | ((s0 | 8u) << 4) | ((4u + s1) << 8) | (((4u + s1) | 8u) << 12);
   }
   __syncwarp();
@@ -130,13 +139,9 @@ __device__ __forceinline__ void packed_item(const FastArgs& a, const int64_t war
 #pragma unroll
   for (int k = 0; k < RPL; ++k) {
     const int i = sl * RPL + k;
-    if (i < Q) {
-      const uint32_t c0 = base_class((uint8_t)q0[i]), c1 = base_class((uint8_t)q1[i]);
-      prof0[k] = all_x ^ ((sm ^ sx) << (8 * c0));
-      prof1[k] = all_x ^ ((sm ^ sx) << (8 * c1));
-    } else {
-      prof0[k] = prof1[k] = all_x;  // past the query: mismatch everywhere
-    }
+    // past the query: mismatch everywhere
+    prof0[k] = i < Q0 ? all_x ^ ((sm ^ sx) << (8 * base_class((uint8_t)q0[i]))) : all_x;
+    prof1[k] = i < Q1 ? all_x ^ ((sm ^ sx) << (8 * base_class((uint8_t)q1[i]))) : all_x;
     h16p[k] = BB;  // H[i][0] = 0
     xl[k] = BB;    // column 0 is NONE
     if (TRACE) {
@@ -145,7 +150,7 @@ __device__ __forceinline__ void packed_item(const FastArgs& a, const int64_t war
     }
   }
   if (!TRACE) bestv[0] = BB;
-  const int S8 = steps8(R, G);
+  const int S8 = steps8(a.R, G);  // the launch's layout (the walk's too)
   uint32_t* dirs = nullptr;
   if (TRACE) dirs = a.dirs + ((warp * kGroups + g) * G + sl) * (int64_t)kNW * S8;
   uint32_t send_u = BB, send_h = BB, diag = BB;
@@ -160,6 +165,8 @@ __device__ __forceinline__ void packed_item(const FastArgs& a, const int64_t war
     if (j >= 1 && j <= R) {
       const uint32_t ws = wsel[j];
       const uint32_t jj = (uint32_t)j * 0x00010001u;
+      // VAR: halves whose window ends before column j
+      const uint32_t cm = VAR ? ((j <= R0 ? 0x0000FFFFu : 0u) | (j <= R1 ? 0xFFFF0000u : 0u)) : ~0u;
       uint32_t dg = diag;
       uint32_t hpair = 0;  // score pass: even row waiting for its odd partner
 #pragma unroll
@@ -175,7 +182,7 @@ __device__ __forceinline__ void packed_item(const FastArgs& a, const int64_t war
         up = (hx & 0x00020002u) * KU + h16;
         xl[k] = (hx & 0x00010001u) * KL + h16;
         if (TRACE) {
-          const uint32_t m = gt_mask(h16, bestv[k]);
+          const uint32_t m = VAR ? gt_mask(h16, bestv[k]) & cm : gt_mask(h16, bestv[k]);
           bestv[k] = sel(m, h16, bestv[k]);
           bestc[k] = sel(m, jj, bestc[k]);
           // bits 1 (UP) and 2 (DIAG) of each half's code to 2 * (k & 7)
@@ -254,7 +261,7 @@ __device__ __forceinline__ void packed_item(const FastArgs& a, const int64_t war
   for (int hp = 0; hp < 2; ++hp) {
     const int sh = 16 * hp;
     uint32_t bv = 0, bc = 0, br = 0x7fffffffu;
-    const int nrows = Q - sl * RPL;
+    const int nrows = (hp ? Q1 : Q0) - sl * RPL;
 #pragma unroll
     for (int k = 0; k < RPL; ++k) {
       const uint32_t v = (bestv[k] >> sh) & 0xFFFFu;
@@ -276,7 +283,7 @@ __device__ __forceinline__ void packed_item(const FastArgs& a, const int64_t war
       }
     }
     scorem[hp] = bv > B ? (int)((bv - B) >> 4) : 0;
-    cellm[hp] = scorem[hp] > 0 ? (int32_t)(br * (uint32_t)(R + 1) + bc) : 0;
+    cellm[hp] = scorem[hp] > 0 ? (int32_t)(br * (uint32_t)((hp ? R1 : R0) + 1) + bc) : 0;
   }
   if (sl < 2 && (sl == 0 ? has0 : has1)) {
     const int32_t p = sl == 0 ? p0 : p1;
@@ -285,14 +292,14 @@ __device__ __forceinline__ void packed_item(const FastArgs& a, const int64_t war
 }
 
 // One work item of kPairs pairs per warp.
-template <int G, int RPL, bool TRACE>
+template <int G, int RPL, bool TRACE, bool VAR>
 __global__ void __launch_bounds__(kPkWarps * 32, (TRACE || RPL > 13) ? 2 : 3) sw_packed_kernel(FastArgs a) {
   constexpr int kPairs = 2 * (32 / G);
   extern __shared__ uint32_t wsel_all[];  // [warps * groups][R + 1]
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t nlist = *a.count - a.list_offset;
   const int64_t warp = (int64_t)blockIdx.x * kPkWarps + wib;
-  if (warp * kPairs < nlist) packed_item<G, RPL, TRACE>(a, warp, nlist, wsel_all, wib, lane);
+  if (warp * kPairs < nlist) packed_item<G, RPL, TRACE, VAR>(a, warp, nlist, wsel_all, wib, lane);
 }
 
 // Upper bound of every pair's score: the same recurrence with every gap
@@ -478,7 +485,7 @@ __global__ void __launch_bounds__(256) sw_walk_kernel(FastArgs a) {
   const uint32_t* dirs = a.dirs + (warp * kGroups + g) * (int64_t)G * kNW * S8;
   const char* qg = a.q + (int64_t)p * a.q_stride;
   const char* wg = a.w + (int64_t)p * a.w_stride;
-  const int W = R + 1;
+  const int W = (a.r_len ? a.r_len[p] : R) + 1;  // the pair's own window for cell indices
   const int shift_half = 16 * hp;
   // the direction word last read: consecutive cells of a walk mostly share
   // it or sit next to it
@@ -593,7 +600,7 @@ Shape shape_for(int Q) {
   return {0, 0};
 }
 
-template <bool TRACE>
+template <bool TRACE, bool VAR>
 int launch_shape(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {
   const Shape s = shape_for(a.Q);
   if (s.G == 0 || max_pairs <= 0) return 0;
@@ -605,10 +612,10 @@ int launch_shape(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {
 #define SWIFT_PK(G_, R_)                                                  \
   if (s.G == G_ && s.RPL == R_) {                                          \
     if (smem > 48 * 1024)                                                  \
-      cudaFuncSetAttribute(sw_packed_kernel<G_, R_, TRACE>,                \
+      cudaFuncSetAttribute(sw_packed_kernel<G_, R_, TRACE, VAR>,           \
                            cudaFuncAttributeMaxDynamicSharedMemorySize,    \
                            (int)smem);                                     \
-    sw_packed_kernel<G_, R_, TRACE><<<grid, tb, smem, st>>>(a);            \
+    sw_packed_kernel<G_, R_, TRACE, VAR><<<grid, tb, smem, st>>>(a);       \
     return 1;                                                              \
   }
   SWIFT_PK(8, 4)
@@ -703,7 +710,7 @@ int64_t trace_scratch_words(int Q, int R, int64_t pairs) {
 }
 
 int launch_sw_score(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {
-  return launch_shape<false>(st, a, max_pairs);
+  return launch_shape<false, false>(st, a, max_pairs);
 }
 
 int launch_sw_bound(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {
@@ -714,7 +721,7 @@ int launch_sw_trace(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {
   if (a.cons_stride % 4 != 0) return 0;  // the walk stores 32-bit words
   FastArgs b = a;
   b.chunk = max_pairs;
-  int k = launch_shape<true>(st, b, max_pairs);
+  int k = a.q_len ? launch_shape<true, true>(st, b, max_pairs) : launch_shape<true, false>(st, b, max_pairs);
   return k + launch_walk(st, b, max_pairs);
 }
 

@@ -139,6 +139,43 @@ def reads_fasta(names, reads) -> bytes:
     return b"".join(parts)
 
 
+def pairs_workload(n_reads: int, seed: int = 1, max_regions: int = 64, flank: int = 64,
+                   ref=None):
+    """Batched Phase-2 workload of varying lengths: reads with L ~ U[36, 250]
+    (1 % substitutions, 0.1 % indels), each against n ~ U{1..max_regions}
+    regions: its true region and n - 1 decoys at uniform positions, each
+    region [pos - flank, pos + L + flank) clipped to its sequence.  Returns
+    (reference bytes, reads bytes, q_off, q_len, r_off, r_len) with offsets
+    into the two byte strings (the reference without line breaks)."""
+    if ref is None:
+        _, seqs = make_reference(50_000_000, 24, sigma=0.8, repeat_frac=0.10, n_units=500,
+                                 unit_len=300, divergence=0.03, seed=0)
+    else:
+        seqs = ref
+    rng = _rng(seed + 100)
+    _, reads, origins = make_reads(seqs, n_reads, sub_p=0.01, indel_p=0.001, seed=seed,
+                                   len_range=(36, 250))
+    lens = np.array([len(x) for x in seqs], dtype=np.int64)
+    cum = np.concatenate([[0], np.cumsum(lens)])
+    rl = np.array([len(r) for r in reads], dtype=np.int64)
+    roff = np.concatenate([[0], np.cumsum(rl)[:-1]])
+    n_reg = rng.integers(1, max_regions + 1, n_reads)
+    read_of = np.repeat(np.arange(n_reads), n_reg)
+    first = np.concatenate([[0], np.cumsum(n_reg)[:-1]])
+    is_true = np.zeros(len(read_of), dtype=bool)
+    is_true[first] = True
+    pos = rng.integers(0, cum[-1], len(read_of))  # decoys: uniform
+    tsid = np.array([o[0] for o in origins], dtype=np.int64)
+    toff = np.array([o[1] for o in origins], dtype=np.int64)
+    pos[first] = cum[tsid] + toff
+    sid = np.searchsorted(cum, pos, side="right") - 1
+    L = rl[read_of]
+    lo = np.maximum(pos - flank, cum[sid])
+    hi = np.minimum(pos + L + flank, cum[sid + 1])
+    return (np.concatenate(seqs).tobytes(), b"".join(reads), roff[read_of], L.astype(np.int32),
+            lo.astype(np.int64), (hi - lo).astype(np.int32))
+
+
 def workload(name: str, n_reads: int | None = None):
     """(reference FASTA, reads FASTA, description) of a named workload."""
     if name == "small":

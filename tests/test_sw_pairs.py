@@ -138,3 +138,19 @@ def test_pairs_limits(ctx, sg):
     assert e.value.code == -1
     res, st = ctx.sw_pairs(b"", [], [], b"", [], [])
     assert st["pairs"] == 0 and len(res["score"]) == 0
+
+
+def test_pairs_batched_workload_vs_oracle(ctx, oracle):
+    # the batched workload's shapes: reads of 36-250 bp against 1-64 regions
+    # each (true region and decoys, 64 bp flanks), on a small reference
+    from swift_gb300 import synth
+    _, seqs = synth.make_reference(2_000_000, 3, sigma=0.5, repeat_frac=0.1, seed=41)
+    ref, reads, qo, ql, ro, rl = synth.pairs_workload(150, seed=42, ref=seqs)
+    res, st = ctx.sw_pairs(reads, qo, ql, ref, ro, rl)
+    assert 1 <= st["segments"] <= 6  # one launch set per packed shape class
+    qs = [reads[a:a + b] for a, b in zip(qo, ql)]
+    ws = [ref[a:a + b] for a, b in zip(ro, rl)]
+    check_against_oracle(res, qs, ws, oracle, (2, -1, -10, -1))
+    plain, _ = ctx.sw_pairs(reads, qo, ql, ref, ro, rl, mode=1, consensus=False)
+    for k in ("score", "start", "end", "len"):
+        assert np.array_equal(plain[k], res[k]), k
