@@ -47,7 +47,7 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="scale", choices=["scale", "small", "batched"])
+    ap.add_argument("--workload", default="scale", choices=["scale", "small", "batched", "serving"])
     ap.add_argument("--reads", type=int, default=None)
     ap.add_argument("--cpu-sample", type=int, default=20000)
     ap.add_argument("--no-e2e", action="store_true")
@@ -219,6 +219,83 @@ def bench_batched(args, rank, world, local):
     return 0
 
 
+def bench_serving(args, rank, world, local, workers=4, pool_size=240, per_load=500):
+    """Serving: a 200 Mbp reference (24 sequences) resident; requests of
+    log-uniform size in [1, 10000] reads, read length per request U[50, 199]
+    (the reference's query buffer caps reads at 199 bases); first the
+    saturation throughput (every request of the pool queued at once), then
+    Poisson arrivals at fractions of it, with per-request latency from
+    submission to result (p50 / p99)."""
+    import numpy as np
+    import swift_gb300 as sg
+    from swift_gb300 import build as b, synth
+    import torch
+    torch.cuda.set_device(local)
+    b.build()
+    names, seqs = synth.make_reference(200_000_000, 24, sigma=0.8, repeat_frac=0.10,
+                                       n_units=500, unit_len=300, divergence=0.03, seed=0)
+    ctx = sg.Context(local)
+    idx = ctx.index(synth.fasta_bytes(names, seqs))
+    rng = np.random.default_rng(3 + rank)
+    sizes = np.floor(np.exp(rng.uniform(0, np.log(10001), pool_size))).astype(int).clip(1, 10000)
+    # reads drawn once at 199 bases, each request cut to its own length
+    _, rs_all, _ = synth.make_reads(seqs, int(sizes.sum()), 199, 0.01, 0.001, 0.05, seed=1000)
+    pool, at = [], 0
+    for t, n in enumerate(sizes):
+        L = int(rng.integers(50, 200))
+        rs = [r[:L] for r in rs_all[at:at + int(n)]]
+        at += int(n)
+        pool.append((int(n), synth.reads_fasta([f"s{t}_{i}" for i in range(int(n))], rs)))
+    srv = sg.Server(idx, device=local, workers=workers)
+    for n, r in pool[:8]:  # warm-up
+        srv.wait(srv.submit(r))
+    # saturation: the whole pool queued at once
+    t0 = time.perf_counter()
+    tickets = [srv.submit(r) for _, r in pool]
+    for t in tickets:
+        srv.wait(t)
+    sat_s = time.perf_counter() - t0
+    total_reads = sum(n for n, _ in pool)
+    sat_rps = total_reads / sat_s
+    mean_reads = total_reads / len(pool)
+    loads = []
+    for frac in (0.3, 0.6, 0.9):
+        rate = frac * sat_rps / mean_reads  # requests per second
+        gaps = rng.exponential(1.0 / rate, per_load)
+        picks = rng.integers(0, len(pool), per_load)
+        lat, done_reads = [], 0
+        start = time.perf_counter()
+        due = start
+        tks = []
+        for g, k in zip(gaps, picks):
+            due += g
+            now = time.perf_counter()
+            if due > now:
+                time.sleep(due - now)
+            tks.append((srv.submit(pool[k][1]), pool[k][0]))
+        for t, n in tks:
+            _, st = srv.wait(t)
+            lat.append(st["total_ms"])
+            done_reads += n
+        el = time.perf_counter() - start
+        loads.append({"offered_fraction": frac, "offered_reads_per_s": frac * sat_rps,
+                      "achieved_reads_per_s": done_reads / el, "requests": per_load,
+                      "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99))})
+    srv.close()
+    if rank == 0:
+        print(json.dumps({
+            "metric": "serving reads/s at saturation; p50/p99 request latency under Poisson load",
+            "value": sat_rps, "unit": "reads/s", "n_gpus": world, "steps": len(loads),
+            "warmup": 8, "ms_per_step": sat_s * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int16x2", "data": "synthetic",
+            "config": {"workload": "serving: 200 Mbp / 24 seqs resident; %d-request pool, sizes "
+                       "log-uniform [1, 10000] reads (mean %.0f), read length U[50, 199] per "
+                       "request; %d concurrent pipelines" % (pool_size, mean_reads, workers)},
+            "latency": loads,
+        }))
+    return 0
+
+
 def main():
     args = parse_args()
     rank, world, local = dist_env()
@@ -245,6 +322,8 @@ def main():
 
     if args.workload == "batched":
         return bench_batched(args, rank, world, local)
+    if args.workload == "serving":
+        return bench_serving(args, rank, world, local)
     import torch
     import swift_gb300 as sg
     from swift_gb300 import build as b

@@ -227,6 +227,32 @@ int swift_fetch_output(swift_ctx *ctx, char *dst, size_t cap);
 int swift_align_files(swift_ctx *ctx, const char *qry_path, const char *ref_path,
                       const char *out_path, const swift_params *p);
 
+/* Serving loop.  No counterpart in the reference (a one-shot CLI).  The
+ * index stays resident while requests, one reads FASTA each, queue up and
+ * run on `workers` concurrent pipelines (a context and stream each, on the
+ * given device).  A request starts when its estimated device memory fits
+ * within mem_budget bytes beside the requests in flight (0: half of the
+ * free memory at creation); one larger than the budget runs alone.  Each
+ * result is byte-identical to swift_align on that request alone. */
+typedef struct swift_server swift_server;
+typedef struct {
+  double queue_ms;   /* submit to start (host clock)                          */
+  double run_ms;     /* start to result                                       */
+  double total_ms;   /* submit to result: the request's latency               */
+  double device_ms;  /* the pipeline's device time (CUDA events)              */
+  int64_t reads, out_bytes;
+} swift_request_stats;
+int swift_server_create(int device, const swift_index *idx, const swift_params *p,
+                        int32_t workers, int64_t mem_budget, swift_server **out);
+/* Queues a copy of the reads; *ticket identifies the request. */
+int swift_server_submit(swift_server *s, const char *reads_fasta, size_t len, int64_t *ticket);
+/* Blocks until the request is done and returns its status; *out (free with
+ * swift_free) holds the records; err receives the message of a failure. */
+int swift_server_wait(swift_server *s, int64_t ticket, char **out, size_t *out_len,
+                      swift_request_stats *stats, char *err, size_t err_cap);
+/* Runs the queued requests to completion, then frees everything. */
+int swift_server_destroy(swift_server *s);
+
 /* Measured peak cell-update rate of the packed-int16 max-plus instruction
  * on this GPU (2 cells per __vimax3_s16x2_relu lane instruction): the
  * denominator of the Smith-Waterman roofline. */

@@ -25,7 +25,8 @@ EXPORTS = [
     "swift_seed", "swift_sw_batch", "swift_align", "swift_reads_upload",
     "swift_reads_destroy", "swift_align_resident", "swift_fetch_output",
     "swift_align_files", "swift_free", "swift_peak_dpx", "swift_align_into",
-    "swift_sw_batch_noalloc", "swift_sw_pairs",
+    "swift_sw_batch_noalloc", "swift_sw_pairs", "swift_server_create", "swift_server_submit",
+    "swift_server_wait", "swift_server_destroy",
 ]
 
 
@@ -51,6 +52,14 @@ class Match(C.Structure):
 class PairsStats(C.Structure):
     _fields_ = [("ms", C.c_double), ("pairs", C.c_int64), ("cells", C.c_int64),
                 ("segments", C.c_int64), ("generic_pairs", C.c_int64), ("launches", C.c_int64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class RequestStats(C.Structure):
+    _fields_ = [("queue_ms", C.c_double), ("run_ms", C.c_double), ("total_ms", C.c_double),
+                ("device_ms", C.c_double), ("reads", C.c_int64), ("out_bytes", C.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -103,6 +112,11 @@ def lib():
         L.swift_align.argtypes = [vp, vp, vp, sz, C.POINTER(Params), C.POINTER(vp),
                                   C.POINTER(sz), C.POINTER(Stats)]
         L.swift_sw_batch_noalloc.argtypes = L.swift_sw_batch.argtypes
+        L.swift_server_create.argtypes = [i32, vp, C.POINTER(Params), i32, i64, C.POINTER(vp)]
+        L.swift_server_submit.argtypes = [vp, C.c_char_p, sz, C.POINTER(i64)]
+        L.swift_server_wait.argtypes = [vp, i64, C.POINTER(vp), C.POINTER(sz),
+                                        C.POINTER(RequestStats), C.c_char_p, sz]
+        L.swift_server_destroy.argtypes = [vp]
         L.swift_sw_pairs.argtypes = [vp, vp, vp, vp, vp, vp, vp, i64, i32, i32, i32, i32,
                                      vp, vp, vp, vp, vp, vp, i64, i32, C.POINTER(PairsStats)]
         L.swift_align_into.argtypes = [vp, vp, vp, sz, C.POINTER(Params), vp, sz, C.POINTER(sz),
@@ -293,6 +307,52 @@ class Context:
         p = params or default_params()
         self._check(lib().swift_align_files(self._h, qry_path.encode(), ref_path.encode(),
                                             out_path.encode(), C.byref(p)))
+
+
+class Server:
+    """Serving loop over a resident index: submit reads, wait for records."""
+
+    def __init__(self, index: "Index", device: int = 0, params: Params | None = None,
+                 workers: int = 4, mem_budget: int = 0):
+        self._index = index  # keeps the index alive
+        p = params or default_params(seed_len=index.seed_len, ignore_thres=index.ignore_thres)
+        h = C.c_void_p()
+        rc = lib().swift_server_create(device, index._h, C.byref(p), workers, mem_budget,
+                                       C.byref(h))
+        if rc != SWIFT_OK:
+            raise SwiftError(rc, "server creation failed")
+        self._h = h
+
+    def submit(self, reads_fasta: bytes) -> int:
+        t = C.c_int64()
+        rc = lib().swift_server_submit(self._h, reads_fasta, len(reads_fasta), C.byref(t))
+        if rc != SWIFT_OK:
+            raise SwiftError(rc, "submit failed")
+        return t.value
+
+    def wait(self, ticket: int):
+        """Returns (records bytes, stats dict); raises SwiftError for a failed request."""
+        out, n, st = C.c_void_p(), C.c_size_t(), RequestStats()
+        err = C.create_string_buffer(512)
+        rc = lib().swift_server_wait(self._h, ticket, C.byref(out), C.byref(n), C.byref(st),
+                                     err, 512)
+        data = C.string_at(out, n.value) if out.value and n.value else b""
+        if out.value:
+            lib().swift_free(out)
+        if rc != SWIFT_OK:
+            raise SwiftError(rc, err.value.decode(errors="replace"))
+        return data, st.as_dict()
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().swift_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Index:

@@ -51,7 +51,7 @@ def make_reference(total_bp: int, n_seqs: int = 1, sigma: float = 0.0,
         w = rng.lognormal(0.0, sigma, n_seqs)
     lens = np.floor(w / w.sum() * total_bp).astype(np.int64)
     lens[0] += total_bp - lens.sum()
-    cat = ACGT[rng.integers(0, 4, total_bp)]
+    cat = ACGT[rng.integers(0, 4, total_bp, dtype=np.uint8)]
     if repeat_frac > 0:
         units = ACGT[rng.integers(0, 4, (n_units, unit_len))]
         n_slots = total_bp // unit_len
