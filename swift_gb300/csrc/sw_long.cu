@@ -1,0 +1,307 @@
+// Phase 2 for long pairs (queries up to 4096, windows up to 8192 bases):
+// one CTA per pair, the reference kernel's recurrence and tie rules
+// (src/smithWaterman.cu:510-645, 911-1026) in int32 cells.
+//
+// Cells use the packed passes' encoding, Hx = 16 H + onehot(direction) + B,
+// so one add-max chain gives H and the reference's direction with its tie
+// precedence, and the next cells' gap penalties come from the code bits; at
+// these lengths 16 H exceeds 16 bits, so a cell is one 32-bit lane.
+//
+// Layout.  The 256 threads own consecutive strips of RPL query rows (RPL =
+// 4, 8, 12 or 16, the smallest that covers the query).  Within a warp, lane
+// t sweeps the window one column behind lane t-1 (shuffles carry the bottom
+// row down).  Between warps, lane 31 writes its bottom row's H and UP
+// candidate per column to a shared ring that lane 0 of the next warp reads;
+// warp w runs two 32-column stages behind warp w-1, one __syncthreads per
+// stage, so every value is written before it is read and a ring of 128
+// columns is never overrun.  Each thread streams its 2-bit direction codes
+// per wavefront step to global scratch (four steps per 16-byte store);
+// sw_long_walk_kernel then walks the reference's traceback, one thread per
+// pair, carrying the cell score to tell NONE from LEFT.
+#include "internal.h"
+
+namespace swift {
+namespace {
+
+constexpr int kLW = 8;           // warps per CTA
+constexpr int kLT = kLW * 32;    // threads per CTA
+constexpr int kStage = 32;       // wavefront steps per stage
+constexpr int kRing = 128;       // ring columns between neighbouring warps
+constexpr int kWild = 0x100;     // 'N' matches every byte
+
+__device__ __forceinline__ int upcase(uint8_t c) {
+  return (unsigned)(c - 'a') < 26u ? c - 'a' + 'A' : c;
+}
+
+template <int RPL>
+__global__ void __launch_bounds__(kLT) sw_long_kernel(LongArgs a) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int64_t item = (int64_t)blockIdx.x;
+  if (item >= a.n) return;
+  const int32_t p = a.list[item];
+  const int Q = a.q_len[p], R = a.r_len[p];
+  const char* qg = a.qry + a.q_off[p];
+  const char* wg = a.ref + a.r_off[p];
+  // shared: up-cased window (int16 per column), rings for the 7 warp boundaries
+  int16_t* wu = reinterpret_cast<int16_t*>(smem);                    // [R + 1]
+  int32_t* ring = reinterpret_cast<int32_t*>(smem + ((2 * (a.max_r + 1) + 15) & ~15));
+  // ring[(b * 2 + 0) * kRing + col % kRing]: UP candidate of boundary b's upper row
+  // ring[(b * 2 + 1) * kRing + col % kRing]: its H (code bits cleared)
+  for (int c = tid; c < R; c += kLT) {
+    const int u = upcase((uint8_t)wg[c]);
+    wu[c + 1] = (int16_t)(u == 'N' ? kWild : u);
+  }
+  const int B = a.bias;
+  const int B8 = B + 8;
+  const int CU = 16 * a.gap_open + 2, CL = 16 * a.gap_open + 1;
+  const int KU = 8 * (a.gap_ext - a.gap_open), KL = 16 * (a.gap_ext - a.gap_open);
+  const int SM = 16 * a.match + 4, SX = 16 * a.mismatch + 4;
+  int qv[RPL], h16p[RPL], xl[RPL], bestv[RPL], bestc[RPL];
+#pragma unroll
+  for (int k = 0; k < RPL; ++k) {
+    const int i = tid * RPL + k;
+    if (i < Q) {
+      const int u = upcase((uint8_t)qg[i]);
+      qv[k] = u == 'N' ? kWild : u;
+    } else {
+      qv[k] = -1;  // past the query: matches nothing (kept out of the maximum)
+    }
+    h16p[k] = B;
+    xl[k] = B;
+    bestv[k] = B;
+    bestc[k] = 0;
+  }
+  const int S4 = (R + 31 + 3) & ~3;  // steps of one thread's direction words
+  uint32_t* dirs = a.dirs + ((int64_t)item * kLT + tid) * a.dir_stride;
+  __syncthreads();
+  int send_u = B, send_h = B, diag = B;
+  uint32_t hist[4];
+  const int steps = R + 31;                          // a warp's wavefront
+  const int n_stages = 2 * (kLW - 1) + (steps + kStage - 1) / kStage;
+  for (int stage = 0; stage < n_stages; ++stage) {
+    const int s_lo = (stage - 2 * warp) * kStage;
+    if (s_lo >= 0 && s_lo < steps) {
+#pragma unroll 1
+      for (int s0 = s_lo; s0 < s_lo + kStage; s0 += 4) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int s = s0 + u;
+          hist[u] = 0;
+          int up = __shfl_up_sync(0xffffffffu, send_u, 1);
+          const int rh = __shfl_up_sync(0xffffffffu, send_h, 1);
+          const int j = s - lane + 1;  // this lane's column
+          if (lane == 0) {
+            if (warp == 0) {
+              up = B;  // row 0
+            } else if (j >= 1 && j <= R) {
+              up = ring[((warp - 1) * 2 + 0) * kRing + j % kRing];
+            }
+          }
+          if (j >= 1 && j <= R) {
+            const int rv = wu[j];
+            int dg = diag;
+            uint32_t acc = 0;
+#pragma unroll
+            for (int k = 0; k < RPL; ++k) {
+              const bool hit = qv[k] == rv || qv[k] == kWild || (rv == kWild && qv[k] >= 0);
+              const int sc = hit ? SM : SX;
+              const int m3 = __vimax3_s32(xl[k] + CL, up + CU, B8);
+              const int hx = __viaddmax_s32(dg, sc, m3);
+              dg = h16p[k];
+              const int h16 = hx & ~15;
+              h16p[k] = h16;
+              up = (hx & 2) * KU + h16;
+              xl[k] = (hx & 1) * KL + h16;
+              if (h16 > bestv[k]) {
+                bestv[k] = h16;
+                bestc[k] = j;
+              }
+              acc |= (uint32_t)((hx >> 1) & 3) << (2 * k);  // 2 DIAG, 1 UP, 0 LEFT / NONE
+            }
+            hist[u] = acc;
+            send_u = up;
+            send_h = h16p[RPL - 1];
+            if (lane == 31 && warp + 1 < kLW) {
+              ring[(warp * 2 + 0) * kRing + j % kRing] = up;
+              ring[(warp * 2 + 1) * kRing + j % kRing] = send_h;
+            }
+          }
+          // the diagonal of the next step: lane above's bottom H at this
+          // column (lane 0: from the ring; column 0 is H = 0)
+          if (lane == 0) {
+            diag = (warp == 0 || j < 1 || j > R) ? B : ring[((warp - 1) * 2 + 1) * kRing + j % kRing];
+          } else {
+            diag = rh;
+          }
+        }
+        if (s0 < S4) {
+          const uint4 v = make_uint4(hist[0], hist[1], hist[2], hist[3]);
+          __stcg(reinterpret_cast<uint4*>(dirs + s0), v);
+        }
+      }
+    }
+    __syncthreads();
+  }
+  // first maximum in row-major order: per thread, then over the CTA
+  int bv = 0, br = 0x7fffffff, bc = 0;
+#pragma unroll
+  for (int k = 0; k < RPL; ++k) {
+    const int i = tid * RPL + k;
+    if (i < Q && bestv[k] > bv) {
+      bv = bestv[k];
+      br = i + 1;
+      bc = bestc[k];
+    }
+  }
+  __shared__ int red_v[kLW], red_r[kLW], red_c[kLW];
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) {
+    const int ov = __shfl_xor_sync(0xffffffffu, bv, d);
+    const int orr = __shfl_xor_sync(0xffffffffu, br, d);
+    const int oc = __shfl_xor_sync(0xffffffffu, bc, d);
+    if (ov > bv || (ov == bv && orr < br)) {
+      bv = ov;
+      br = orr;
+      bc = oc;
+    }
+  }
+  if (lane == 0) {
+    red_v[warp] = bv;
+    red_r[warp] = br;
+    red_c[warp] = bc;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    for (int w = 1; w < kLW; ++w) {
+      if (red_v[w] > bv || (red_v[w] == bv && red_r[w] < br)) {
+        bv = red_v[w];
+        br = red_r[w];
+        bc = red_c[w];
+      }
+    }
+    const int score = bv > B ? (bv - B) >> 4 : 0;
+    a.best[p] = make_int2(score, score > 0 ? br * (R + 1) + bc : 0);
+  }
+}
+
+// Traceback walk over the long kernel's direction codes, one thread per
+// pair (the same rules as sw_walk_kernel).
+template <int RPL>
+__global__ void __launch_bounds__(128) sw_long_walk_kernel(LongArgs a) {
+  const int64_t item = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (item >= a.n) return;
+  const int32_t p = a.list[item];
+  const int R = a.r_len[p];
+  const char* qg = a.qry + a.q_off[p];
+  const char* wg = a.ref + a.r_off[p];
+  const uint32_t* dirs = a.dirs + (int64_t)item * kLT * a.dir_stride;
+  const int W = R + 1;
+  int64_t last = -1;
+  uint32_t word = 0;
+  auto code_at = [&](int i, int jj) -> uint32_t {
+    const int t = (i - 1) / RPL, k = (i - 1) % RPL, ln = t & 31;
+    const int64_t at = (int64_t)t * a.dir_stride + (jj + ln - 1);
+    if (at != last) {
+      word = __ldcg(&dirs[at]);
+      last = at;
+    }
+    return (word >> (2 * k)) & 3u;
+  };
+  enum : int { kNone = 0, kDiag = 1, kUp = 2, kLeft = 3 };
+  auto dir_of = [](uint32_t code, int h) -> int {
+    return code == 2u ? kDiag : code == 1u ? kUp : (h == 0 ? kNone : kLeft);
+  };
+  const int m = a.match, x = a.mismatch, o = a.gap_open, e = a.gap_ext;
+  char* qc = a.qcons ? a.qcons + (int64_t)p * a.cons_stride : nullptr;
+  char* rc = a.rcons ? a.rcons + (int64_t)p * a.cons_stride : nullptr;
+  const int2 b = a.best[p];
+  int cr = b.y / W, cc = b.y % W;
+  int h = b.x;
+  int d = (cr == 0 || cc == 0) ? kNone : dir_of(code_at(cr, cc), h);
+  int nr = cr, nc = cc, nh = h, nd = kNone;
+  auto advance = [&]() {
+    nr = cr - ((d == kDiag || d == kUp) ? 1 : 0);
+    nc = cc - ((d == kDiag || d == kLeft) ? 1 : 0);
+    if (d == kNone) {
+      nh = h;
+      nd = kNone;
+      return;
+    }
+    const uint32_t pc = (nr == 0 || nc == 0) ? 0u : code_at(nr, nc);
+    if (d == kDiag) {
+      const int qb = upcase((uint8_t)qg[cr - 1]), rb = upcase((uint8_t)wg[cc - 1]);
+      nh = h - ((qb == rb || qb == 'N' || rb == 'N') ? m : x);
+    } else {
+      // the gap costs gap_ext when the predecessor itself moved the same way
+      const bool same = nr != 0 && nc != 0 && (d == kUp ? pc == 1u : pc == 0u);
+      nh = h - (same ? e : o);
+    }
+    nd = (nr == 0 || nc == 0) ? kNone : dir_of(pc, nh);
+  };
+  advance();
+  int tick = -1, nref = -1, start = 0;
+  auto emit = [&](char r, char q) {
+    ++tick;
+    if (qc) {
+      rc[tick] = r;
+      qc[tick] = q;
+    }
+  };
+  while ((cr != nr || cc != nc) && nc != 0 && nr != 0) {
+    char rch = '-';
+    if (nc != cc) { rch = wg[cc - 1]; ++nref; }
+    emit(rch, nr == cr ? '-' : qg[cr - 1]);
+    start = cc;
+    cr = nr; cc = nc; h = nh; d = nd;
+    if (d == kNone) break;
+    advance();
+  }
+  if ((cr != nr || cc != nc) && (nc == 0 || nr == 0)) {
+    char rch = '-';
+    if (nc != cc) { rch = wg[cc - 1]; ++nref; }
+    emit(rch, nr == cr ? '-' : qg[cr - 1]);
+    start = cc;
+  }
+  DevAln out;
+  out.score = b.x;
+  out.start = start;
+  out.end = start + nref;
+  out.len = tick + 1;
+  a.aln[p] = out;
+}
+
+template <int RPL>
+int launch_long_rpl(cudaStream_t st, const LongArgs& a) {
+  const size_t smem = ((2 * (a.max_r + 1) + 15) & ~15) + (size_t)(kLW - 1) * 2 * kRing * 4;
+  sw_long_kernel<RPL><<<(unsigned)a.n, kLT, smem, st>>>(a);
+  sw_long_walk_kernel<RPL><<<(unsigned)((a.n + 127) / 128), 128, 0, st>>>(a);
+  return 2;
+}
+
+}  // namespace
+
+int long_rows_per_lane(int Q) {
+  return Q <= 4 * kLT ? 4 : Q <= 8 * kLT ? 8 : Q <= 12 * kLT ? 12 : Q <= 16 * kLT ? 16 : 0;
+}
+
+int64_t long_dir_stride(int max_r) { return (int64_t)((max_r + 31 + 3) & ~3); }
+
+int64_t long_scratch_words(int max_r, int64_t pairs) {
+  return pairs * kLT * long_dir_stride(max_r);
+}
+
+int launch_sw_long(cudaStream_t st, const LongArgs& a, int rpl) {
+  if (a.n <= 0) return 0;
+  // shared memory: window (2 B per column) + rings, 23 KB at the longest window
+  if (((2 * (a.max_r + 1) + 15) & ~15) + (kLW - 1) * 2 * kRing * 4 > 48 * 1024) return 0;
+  switch (rpl) {
+    case 4: return launch_long_rpl<4>(st, a);
+    case 8: return launch_long_rpl<8>(st, a);
+    case 12: return launch_long_rpl<12>(st, a);
+    case 16: return launch_long_rpl<16>(st, a);
+    default: return 0;
+  }
+}
+
+}  // namespace swift
