@@ -178,14 +178,16 @@ typedef struct {
  * recurrence, tie rules and traceback.  Outputs per pair: score, start,
  * end, length and, when qcons/rcons are not NULL, the reversed consensus
  * strings at qcons/rcons + i * cons_stride (cons_stride >= q_len + r_len + 2
- * for every pair, a multiple of 4).  1 <= q_len <= 256; 1 <= r_len <= 1024
- * (768 when q_len > 128).  Inputs all host or all device memory; outputs
- * likewise.
+ * for every pair, a multiple of 4).  1 <= q_len <= 4096, 1 <= r_len <= 8192;
+ * pairs beyond 256 x 1024 (or q_len > 128 with r_len > 768) run on the long
+ * kernel, one CTA each, which needs negative mismatch and gap penalties.
+ * Inputs all host or all device memory; outputs likewise.
  *   mode 0 (batched): pairs sorted by (q_len, r_len) on the device, one set
  *          of launches per shape: packed 16-bit passes for pairs of ACGT
  *          bytes, the int32 kernel for the rest;
  *   mode 1 (plain): every pair padded to the largest shape, one launch of
- *          the int32 kernel, as the reference runs a batch.  Padding leaves
+ *          the int32 kernel, as the reference runs a batch (pairs up to
+ *          256 x 1024 only).  Padding leaves
  *          results unchanged when mismatch and both gap penalties are
  *          negative (otherwise mode 1 is refused, SWIFT_E_ARG); bytes 0x00
  *          and 0x01 are the padding and are refused in pairs (SWIFT_E_INPUT). */

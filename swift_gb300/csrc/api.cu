@@ -981,21 +981,30 @@ int swift_sw_pairs(swift_ctx* ctx, const char* qry, const int64_t* q_off, const 
   CK(cudaEventRecord(ctx->ev[0], st));
   // shape limits over all pairs
   int32_t* mx;
-  CK(sc.get(&mx, 4));
-  const int32_t mx0[4] = {0, 0, 0x7fffffff, 0};
+  CK(sc.get(&mx, 8));
+  const int32_t mx0[8] = {0, 0, 0x7fffffff, 0, 0, 0, 0, 0};
   CK(cudaMemcpyAsync(mx, mx0, sizeof(mx0), cudaMemcpyHostToDevice, st));
   launch_var_max_len(st, dql, drl, n, mx);
   CKLAUNCH();
-  int32_t h_mx[4];
+  int32_t h_mx[8];
   CK(cudaMemcpyAsync(h_mx, mx, sizeof(h_mx), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   const int maxQ = h_mx[0], maxR = h_mx[1];
+  const int64_t n_long = h_mx[6];
   if (h_mx[2] < 1) return fail(ctx, SWIFT_E_ARG, "pair lengths must be >= 1");
-  if (maxQ > kMaxQ || maxR > kMaxR || (maxQ > 128 && maxR > 768))
-    return fail(ctx, SWIFT_E_LIMIT, "q_len <= 256 and r_len <= 1024 (768 when q_len > 128)");
+  if (maxQ > kLongMaxQ || maxR > kLongMaxR)
+    return fail(ctx, SWIFT_E_LIMIT, "q_len <= 4096 and r_len <= 8192");
+  if (mode == 1 && n_long > 0)
+    return fail(ctx, SWIFT_E_LIMIT,
+                "plain mode takes q_len <= 256 and r_len <= 1024 (768 when q_len > 128)");
+  if (n_long > 0 && !(x < 0 && o < 0 && e < 0))
+    return fail(ctx, SWIFT_E_ARG,
+                "pairs longer than 256 x 1024 need negative mismatch and gap penalties");
   if (qcons && cs < (int64_t)h_mx[3] + 2) return fail(ctx, SWIFT_E_ARG, "cons_stride below q_len + r_len + 2");
-  const int64_t q_stride = ((int64_t)maxQ + 16) & ~(int64_t)15;
-  const int64_t w_stride = ((int64_t)maxR + 16) & ~(int64_t)15;
+  // fixed strides for the pairs of the warp-per-pair kernels (long pairs are
+  // read in place)
+  const int64_t q_stride = ((int64_t)h_mx[4] + 16) & ~(int64_t)15;
+  const int64_t w_stride = ((int64_t)h_mx[5] + 16) & ~(int64_t)15;
   int bias0 = 0;
   // chunks bound the fixed-stride copies and the traceback scratch
   const int64_t chunk = 4 << 20;
@@ -1126,7 +1135,14 @@ int swift_sw_pairs(swift_ctx* ctx, const char* qry, const int64_t* q_off, const 
         int64_t start, count;
       };
       std::vector<Group> groups;
+      std::vector<std::pair<int64_t, int64_t>> long_groups;  // (start, count) per rows class
+      std::vector<int> long_class;
       for (uint32_t s = 0; s < nseg; ++s) {
+        if ((uint32_t)hk[s] >= kVarLongKey) {
+          long_groups.push_back({hs[s], hc[s]});
+          long_class.push_back((int)((uint32_t)hk[s] - kVarLongKey));
+          continue;
+        }
         const bool gen = (hk[s] >> 20) & 1;
         const int q = (hk[s] >> 11) & 511, R = hk[s] & 2047;
         if (!gen && !groups.empty() && !groups.back().gen &&
@@ -1219,6 +1235,53 @@ int swift_sw_pairs(swift_ctx* ctx, const char* qry, const int64_t* q_off, const 
           launches += kk;
           CKLAUNCH();
         }
+      }
+      // long pairs: one CTA each, in batches of whole waves that bound the
+      // direction scratch (8.4 MB per pair at the longest window)
+      for (size_t lg = 0; lg < long_groups.size(); ++lg) {
+        const int rpl = 4 * (long_class[lg] + 1);
+        const int64_t cnt = long_groups[lg].second;
+        const int max_r = kLongMaxR;
+        int dev_sms = 0;
+        cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device);
+        const int64_t wave = std::max(2 * dev_sms, 1);
+        const int64_t per = std::max<int64_t>(1, (int64_t)(3.0e9 / 4) / (256 * long_dir_stride(max_r)));
+        const int64_t batch = std::min(cnt, std::max(wave, per / wave * wave));
+        const int64_t words = long_scratch_words(max_r, batch);
+        if (words > dirs_words) {
+          CK(sc.get(&dirs, (size_t)words));
+          dirs_words = words;
+        }
+        LongArgs la;
+        memset(&la, 0, sizeof(la));
+        la.qry = dq;
+        la.q_off = dqo + c0;
+        la.q_len = dql + c0;
+        la.ref = dr;
+        la.r_off = dro + c0;
+        la.r_len = drl + c0;
+        la.max_r = max_r;
+        la.match = m;
+        la.mismatch = x;
+        la.gap_open = o;
+        la.gap_ext = e;
+        la.bias = ((-(16 * o + 1)) + 15) & ~15;
+        la.dirs = dirs;
+        la.dir_stride = long_dir_stride(max_r);
+        la.best = best2;
+        la.aln = aln;
+        la.qcons = cq;
+        la.rcons = cr;
+        la.cons_stride = cs;
+        for (int64_t off = 0; off < cnt; off += batch) {
+          la.list = sorted + long_groups[lg].first + off;
+          la.n = std::min(batch, cnt - off);
+          const int kk = launch_sw_long(st, la, rpl);
+          if (kk == 0) return fail(ctx, SWIFT_E_DEVICE, "long pass could not launch");
+          launches += kk;
+          CKLAUNCH();
+        }
+        ps.segments += 1;
       }
     }
     aln_to_i32_kernel<<<(unsigned)((cn + 255) / 256), 256, 0, st>>>(

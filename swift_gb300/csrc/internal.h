@@ -221,6 +221,12 @@ int launch_sw(cudaStream_t st, const SwArgs& a, std::string* err);
 
 // pairs_var.cu: explicit pairs of varying lengths, sorted by shape
 constexpr uint32_t kVarKeys = 1u << 21;  // shape keys: generic bit, Q (9 bits), R (11 bits)
+// the top four keys: long pairs (sw_long.cu) by rows-per-lane class
+constexpr uint32_t kVarLongKey = kVarKeys - 4;
+// pairs beyond the warp-per-pair kernels' shapes go to the long kernel
+__host__ __device__ inline bool var_pair_long(int Q, int R) {
+  return Q > 256 || R > 1024 || (Q > 128 && R > 768);
+}
 struct VarPairArgs {
   const char* qry;            // query bytes of pair i at qry + q_off[i], q_len[i] of them
   const int64_t* q_off;
@@ -247,6 +253,33 @@ void launch_var_segments(cudaStream_t st, const uint32_t* hist, const uint32_t* 
                          int32_t* seg_count);
 void launch_var_scatter(cudaStream_t st, const uint32_t* key, int64_t n, const uint32_t* start,
                         uint32_t* fill, int32_t* sorted);
+
+// sw_long.cu: long pairs (queries up to 4096, windows up to 8192), one CTA each
+constexpr int kLongMaxQ = 4096;
+constexpr int kLongMaxR = 8192;
+struct LongArgs {
+  const char* qry;            // pair i: qry + q_off[i], q_len[i] bytes; ref likewise
+  const int64_t* q_off;
+  const int32_t* q_len;
+  const char* ref;
+  const int64_t* r_off;
+  const int32_t* r_len;
+  const int32_t* list;        // pair ids of this launch
+  int64_t n;
+  int max_r;                  // longest window of the launch
+  int match, mismatch, gap_open, gap_ext, bias;
+  uint32_t* dirs;             // direction scratch: n x 256 threads x dir_stride words
+  int64_t dir_stride;
+  int2* best;                 // per pair: (score, first maximum cell)
+  DevAln* aln;
+  char* qcons;                // optional reversed consensus strings
+  char* rcons;
+  int64_t cons_stride;
+};
+int long_rows_per_lane(int Q);           // 4, 8, 12 or 16; 0 beyond 4096
+int64_t long_dir_stride(int max_r);
+int64_t long_scratch_words(int max_r, int64_t pairs);
+int launch_sw_long(cudaStream_t st, const LongArgs& a, int rpl);
 
 // sw_fast.cu: packed 16-bit passes (score of every pair; trace of printed pairs)
 // Bound-pass suffix maxima: blocks of wavefront steps, blocks per pair.

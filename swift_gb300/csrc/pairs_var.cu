@@ -33,6 +33,15 @@ __global__ void __launch_bounds__(kVarWarps * 32) pack_var_kernel(VarPairArgs a)
   const int64_t i = (int64_t)blockIdx.x * kVarWarps + wib;
   if (i >= a.n) return;
   const int Q = a.q_len[i], R = a.r_len[i];
+  if (var_pair_long(Q, R)) {  // read in place by the long kernel
+    if (lane == 0) {
+      const int c = Q <= 1024 ? 0 : Q <= 2048 ? 1 : Q <= 3072 ? 2 : 3;
+      const uint32_t key = kVarLongKey + (uint32_t)c;
+      a.key[i] = key;
+      atomicAdd(&a.hist[key], 1u);
+    }
+    return;
+  }
   const char* qs = a.qry + a.q_off[i];
   const char* ws = a.ref + a.r_off[i];
   char* qd = a.qbuf + i * a.q_stride;
@@ -92,21 +101,33 @@ __global__ void var_scatter_kernel(const uint32_t* __restrict__ key, int64_t n,
   sorted[start[k] + atomicAdd(&fill[k], 1u)] = (int32_t)i;
 }
 
-// out: max q_len, max r_len, min length, max q_len + r_len
+// out: max q_len, max r_len, min length, max q_len + r_len, then max q_len
+// and r_len over the pairs of the warp-per-pair kernels (not long), count
+// of long pairs
 __global__ void max_len_kernel(const int32_t* __restrict__ q_len, const int32_t* __restrict__ r_len,
                                int64_t n, int32_t* out) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  int mq = 0, mr = 0, lo = 0x7fffffff, ms = 0;
+  int mq = 0, mr = 0, lo = 0x7fffffff, ms = 0, sq = 0, sr = 0, nl = 0;
   for (; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    mq = max(mq, q_len[i]);
-    mr = max(mr, r_len[i]);
-    lo = min(lo, min(q_len[i], r_len[i]));
-    ms = max(ms, q_len[i] + r_len[i]);
+    const int Q = q_len[i], R = r_len[i];
+    mq = max(mq, Q);
+    mr = max(mr, R);
+    lo = min(lo, min(Q, R));
+    ms = max(ms, Q + R);
+    if (var_pair_long(Q, R)) {
+      ++nl;
+    } else {
+      sq = max(sq, Q);
+      sr = max(sr, R);
+    }
   }
   atomicMax(&out[0], mq);
   atomicMax(&out[1], mr);
   atomicMin(&out[2], lo);
   atomicMax(&out[3], ms);
+  atomicMax(&out[4], sq);
+  atomicMax(&out[5], sr);
+  atomicAdd(&out[6], nl);
 }
 
 }  // namespace
