@@ -47,7 +47,8 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="scale", choices=["scale", "small", "batched", "serving"])
+    ap.add_argument("--workload", default="scale",
+                    choices=["scale", "small", "batched", "serving", "long"])
     ap.add_argument("--reads", type=int, default=None)
     ap.add_argument("--cpu-sample", type=int, default=20000)
     ap.add_argument("--no-e2e", action="store_true")
@@ -165,8 +166,13 @@ def bench_batched(args, rank, world, local):
     device = local
     torch.cuda.set_device(device)
     b.build()
-    n_reads = args.reads or 1_000_000
-    ref, reads, qo, ql, ro, rl = synth.pairs_workload(n_reads, seed=1 + rank)
+    long = args.workload == "long"
+    if long:
+        n_reads = args.reads or 20_000
+        ref, reads, qo, ql, ro, rl = synth.long_workload(n_reads, seed=1 + rank)
+    else:
+        n_reads = args.reads or 1_000_000
+        ref, reads, qo, ql, ro, rl = synth.pairs_workload(n_reads, seed=1 + rank)
     stream = torch.cuda.Stream(device)
     torch.cuda.set_stream(stream)
     ctx = sg.Context(device, stream.cuda_stream)
@@ -193,24 +199,30 @@ def bench_batched(args, rank, world, local):
         sts = [run(n, 0) for _ in range(args.steps)]
     ms = statistics.median(s["ms"] for s in sts)
     cells = sts[-1]["cells"]
-    # plain mode on the first pairs (about a tenth of the cells: one padded launch is slow)
-    n_plain = max(1, n // 10)
-    run(n_plain, 1)
-    sp = [run(n_plain, 1) for _ in range(max(1, min(args.steps, 2)))]
-    ms_p = statistics.median(s["ms"] for s in sp)
-    plain_gcups = sp[-1]["cells"] / (ms_p * 1e-3) / 1e9
     gcups = cells / (ms * 1e-3) / 1e9
+    plain_gcups = ms_p = n_plain = None
+    if not long:  # plain mode takes pairs up to 256 x 1024 only
+        # plain mode on the first pairs (about a tenth of the cells: one padded launch is slow)
+        n_plain = max(1, n // 10)
+        run(n_plain, 1)
+        sp = [run(n_plain, 1) for _ in range(max(1, min(args.steps, 2)))]
+        ms_p = statistics.median(s["ms"] for s in sp)
+        plain_gcups = sp[-1]["cells"] / (ms_p * 1e-3) / 1e9
     if rank == 0:
+        wl_desc = ("long: %d queries L ~ U[1000,4000] (3%% subs, 0.5%% indels) x one region "
+                   "U[max(2000, L+200), 8000] on a 100 Mbp uniform reference" % n_reads) if long else \
+                  ("batched: %d reads L ~ U[36,250] x U{1..64} regions "
+                   "(true + decoys, 64 bp flanks) on the 50 Mbp reference" % n_reads)
         print(json.dumps({
-            "metric": "SW GCUPS on read x region pairs of varying length (batched), bit-exact",
+            "metric": ("SW GCUPS on long query x region pairs, bit-exact" if long else
+                       "SW GCUPS on read x region pairs of varying length (batched), bit-exact"),
             "value": gcups, "unit": "GCUPS", "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "int16x2", "data": "synthetic",
-            "config": {"workload": "batched: %d reads L ~ U[36,250] x U{1..64} regions "
-                       "(true + decoys, 64 bp flanks) on the 50 Mbp reference" % n_reads,
-                       "pairs": n, "cells": cells, "segments": sts[-1]["segments"],
-                       "generic_pairs": sts[-1]["generic_pairs"]},
-            "plain": {"gcups": plain_gcups, "pairs": n_plain, "ms": ms_p,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32" if long else "int16x2",
+            "data": "synthetic",
+            "config": {"workload": wl_desc, "pairs": n, "cells": cells,
+                       "segments": sts[-1]["segments"], "generic_pairs": sts[-1]["generic_pairs"]},
+            "plain": None if long else {"gcups": plain_gcups, "pairs": n_plain, "ms": ms_p,
                       "note": "every pair padded to the largest shape, one int32 launch"},
             "batched_vs_plain": gcups / plain_gcups if plain_gcups else None,
             "gpu_launches": int(sum(s["launches"] for s in sts)),
@@ -320,7 +332,7 @@ def main():
         print(json.dumps(line))
         return 0
 
-    if args.workload == "batched":
+    if args.workload in ("batched", "long"):
         return bench_batched(args, rank, world, local)
     if args.workload == "serving":
         return bench_serving(args, rank, world, local)

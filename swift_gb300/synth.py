@@ -176,6 +176,41 @@ def pairs_workload(n_reads: int, seed: int = 1, max_regions: int = 64, flank: in
             lo.astype(np.int64), (hi - lo).astype(np.int32))
 
 
+def long_workload(n_queries: int = 20_000, seed: int = 1, ref_bp: int = 100_000_000):
+    """Long-region Phase-2 workload: a uniform reference; queries of
+    L ~ U[1000, 4000] bases (3 % substitutions, 0.5 % indels of 1-3 bases)
+    from uniform positions, each against one region of length
+    U[max(2000, L + 200), 8000] that contains the query's origin.  Returns
+    (reference bytes, queries bytes, q_off, q_len, r_off, r_len)."""
+    rng = _rng(seed)
+    ref = ACGT[rng.integers(0, 4, ref_bp, dtype=np.uint8)]
+    L = rng.integers(1000, 4001, n_queries)
+    RL = np.array([int(rng.integers(max(2000, l + 200), 8001)) for l in L])
+    pos = rng.integers(0, ref_bp - 8200, n_queries)
+    qs = []
+    for i in range(n_queries):
+        s = ref[pos[i]:pos[i] + L[i]].copy()
+        code = np.searchsorted(ACGT, s)
+        sub = rng.random(L[i]) < 0.03
+        s = np.where(sub, ACGT[(code + rng.integers(1, 4, L[i])) % 4], s)
+        buf = bytearray(s.tobytes())
+        for _ in range(int(rng.binomial(L[i], 0.005))):
+            at = int(rng.integers(0, len(buf)))
+            size = int(rng.integers(1, 4))
+            if rng.random() < 0.5:
+                buf[at:at] = ACGT[rng.integers(0, 4, size)].tobytes()
+            else:
+                del buf[at:at + size]
+        while len(buf) < L[i]:
+            buf += ACGT[rng.integers(0, 4, 1)].tobytes()
+        qs.append(bytes(buf[:L[i]]))
+    lead = np.array([int(rng.integers(0, RL[i] - L[i] + 1)) for i in range(n_queries)])
+    r_off = np.clip(pos - lead, 0, ref_bp - RL)
+    q_off = np.concatenate([[0], np.cumsum(L)[:-1]])
+    return (ref.tobytes(), b"".join(qs), q_off.astype(np.int64), L.astype(np.int32),
+            r_off.astype(np.int64), RL.astype(np.int32))
+
+
 def workload(name: str, n_reads: int | None = None):
     """(reference FASTA, reads FASTA, description) of a named workload."""
     if name == "small":

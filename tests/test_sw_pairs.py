@@ -128,8 +128,8 @@ def test_pairs_shared_buffers_and_parameters(ctx, oracle):
 
 
 def test_pairs_limits(ctx, sg):
-    qb, wb = b"A" * 300, b"A" * 2000
-    for ql, wl, code in [(257, 100, -5), (200, 800, -5), (0, 10, -1)]:
+    qb, wb = b"A" * 5000, b"A" * 9000
+    for ql, wl, code in [(4097, 100, -5), (200, 8193, -5), (0, 10, -1)]:
         with pytest.raises(sg.SwiftError) as e:
             ctx.sw_pairs(qb, [0], [ql], wb, [0], [wl])
         assert e.value.code == code
@@ -154,3 +154,50 @@ def test_pairs_batched_workload_vs_oracle(ctx, oracle):
     plain, _ = ctx.sw_pairs(reads, qo, ql, ref, ro, rl, mode=1, consensus=False)
     for k in ("score", "start", "end", "len"):
         assert np.array_equal(plain[k], res[k]), k
+
+
+def test_long_pairs_vs_oracle(ctx, oracle):
+    # long queries and windows (the long-region shapes: queries to 4000,
+    # windows to 8000) next to short pairs in one call
+    rng = random.Random(91)
+    qs, ws = [], []
+    for Q, R in [(300, 600), (1000, 2000), (1500, 1200), (2100, 4000), (3000, 3500),
+                 (4000, 8000), (257, 300), (150, 1000), (64, 2000), (3500, 5000)]:
+        w = bytearray(rng.choice(b"ACGT") for _ in range(R))
+        a = rng.randrange(0, max(1, R - Q))
+        q = bytearray(w[a:a + Q])
+        while len(q) < Q:
+            q.append(rng.choice(b"ACGT"))
+        for k in range(Q):
+            if rng.random() < 0.03:
+                q[k] = rng.choice(b"ACGT")
+        for _ in range(Q // 400):  # indels, length kept
+            k = rng.randrange(1, Q - 3)
+            if rng.random() < 0.5:
+                q = q[:k] + q[k + 2:] + bytearray(b"AC")
+            else:
+                q = q[:k] + bytearray(b"GT") + q[k:-2]
+        q[rng.randrange(Q)] = ord("N")
+        w[rng.randrange(R)] = ord("n")
+        qs.append(bytes(q))
+        ws.append(bytes(w))
+    sq, sw_ = make_pairs(40, seed=92)
+    qs += sq
+    ws += sw_
+    qb, qo, ql = pack(qs)
+    wb, wo, wl = pack(ws)
+    res, st = ctx.sw_pairs(qb, qo, ql, wb, wo, wl)
+    check_against_oracle(res, qs, ws, oracle, (2, -1, -10, -1))
+    res2, _ = ctx.sw_pairs(qb, qo, ql, wb, wo, wl, 3, -2, -5, -2)
+    check_against_oracle(res2, qs, ws, oracle, (3, -2, -5, -2))
+
+
+def test_long_workload_vs_oracle(ctx, oracle):
+    # the long-region workload's shapes on a small reference
+    from swift_gb300 import synth
+    ref, qry, qo, ql, ro, rl = synth.long_workload(24, seed=93, ref_bp=2_000_000)
+    res, st = ctx.sw_pairs(qry, qo, ql, ref, ro, rl)
+    qs = [qry[a:a + b] for a, b in zip(qo, ql)]
+    ws = [ref[a:a + b] for a, b in zip(ro, rl)]
+    check_against_oracle(res, qs, ws, oracle, (2, -1, -10, -1))
+    assert (res["score"] > 1000).all()  # every query aligns across its region
