@@ -1236,52 +1236,80 @@ int swift_sw_pairs(swift_ctx* ctx, const char* qry, const int64_t* q_off, const 
           CKLAUNCH();
         }
       }
-      // long pairs: one CTA each, in batches of whole waves that bound the
-      // direction scratch (8.4 MB per pair at the longest window)
-      for (size_t lg = 0; lg < long_groups.size(); ++lg) {
-        const int rpl = 4 * (long_class[lg] + 1);
-        const int64_t cnt = long_groups[lg].second;
-        const int max_r = kLongMaxR;
-        int dev_sms = 0;
-        cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device);
-        const int64_t wave = std::max(2 * dev_sms, 1);
-        const int64_t per = std::max<int64_t>(1, (int64_t)(3.0e9 / 4) / (256 * long_dir_stride(max_r)));
-        const int64_t batch = std::min(cnt, std::max(wave, per / wave * wave));
-        const int64_t words = long_scratch_words(max_r, batch);
-        if (words > dirs_words) {
-          CK(sc.get(&dirs, (size_t)words));
-          dirs_words = words;
+      // long pairs: one CTA each, largest first, in launches of many waves
+      // (the block scheduler fills SMs freed by small pairs) whose direction
+      // slots, sized per pair, fit a scratch budget
+      if (!long_groups.empty()) {
+        std::vector<int32_t> hql(cn), hrl(cn);
+        CK(cudaMemcpyAsync(hql.data(), dql + c0, cn * 4, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(hrl.data(), drl + c0, cn * 4, cudaMemcpyDeviceToHost, st));
+        std::vector<int32_t> ids;
+        for (size_t lg = 0; lg < long_groups.size(); ++lg) {
+          const int64_t cnt = long_groups[lg].second;
+          ids.resize(cnt);
+          CK(cudaMemcpyAsync(ids.data(), sorted + long_groups[lg].first, cnt * 4,
+                             cudaMemcpyDeviceToHost, st));
+          CK(cudaStreamSynchronize(st));
+          std::sort(ids.begin(), ids.end(), [&](int32_t u, int32_t v) {
+            const int64_t cu = (int64_t)hql[u] * hrl[u], cv = (int64_t)hql[v] * hrl[v];
+            return cu != cv ? cu > cv : u < v;
+          });
+          const int rpl = 4 * (long_class[lg] + 1);
+          const int64_t budget_words = (int64_t)(12.0e9 / 4);
+          int64_t b0 = 0;
+          while (b0 < cnt) {
+            // one launch: items b0 .. b1 - 1 with their slot offsets
+            std::vector<int64_t> off;
+            int64_t words = 0, b1 = b0;
+            while (b1 < cnt && (b1 == b0 || words + long_slot_words(hrl[ids[b1]]) <= budget_words)) {
+              off.push_back(words);
+              words += long_slot_words(hrl[ids[b1]]);
+              ++b1;
+            }
+            const int64_t nb = b1 - b0;
+            if (words > dirs_words) {
+              CK(sc.get(&dirs, (size_t)words));
+              dirs_words = words;
+            }
+            int32_t* dlist;
+            int64_t* doff;
+            CK(sc.get(&dlist, (size_t)nb));
+            CK(sc.get(&doff, (size_t)nb));
+            CK(cudaMemcpyAsync(dlist, ids.data() + b0, nb * 4, cudaMemcpyHostToDevice, st));
+            CK(cudaMemcpyAsync(doff, off.data(), nb * 8, cudaMemcpyHostToDevice, st));
+            LongArgs la;
+            memset(&la, 0, sizeof(la));
+            la.qry = dq;
+            la.q_off = dqo + c0;
+            la.q_len = dql + c0;
+            la.ref = dr;
+            la.r_off = dro + c0;
+            la.r_len = drl + c0;
+            la.list = dlist;
+            la.n = nb;
+            la.max_r = kLongMaxR;
+            la.match = m;
+            la.mismatch = x;
+            la.gap_open = o;
+            la.gap_ext = e;
+            la.bias = ((-(16 * o + 1)) + 15) & ~15;
+            la.dirs = dirs;
+            la.dir_off = doff;
+            la.best = best2;
+            la.aln = aln;
+            la.qcons = cq;
+            la.rcons = cr;
+            la.cons_stride = cs;
+            const int kk = launch_sw_long(st, la, rpl);
+            if (kk == 0) return fail(ctx, SWIFT_E_DEVICE, "long pass could not launch");
+            launches += kk;
+            CKLAUNCH();
+            // (copies from pageable host memory are staged before they
+            // return; the next launch reuses the scratch in stream order)
+            b0 = b1;
+          }
+          ps.segments += 1;
         }
-        LongArgs la;
-        memset(&la, 0, sizeof(la));
-        la.qry = dq;
-        la.q_off = dqo + c0;
-        la.q_len = dql + c0;
-        la.ref = dr;
-        la.r_off = dro + c0;
-        la.r_len = drl + c0;
-        la.max_r = max_r;
-        la.match = m;
-        la.mismatch = x;
-        la.gap_open = o;
-        la.gap_ext = e;
-        la.bias = ((-(16 * o + 1)) + 15) & ~15;
-        la.dirs = dirs;
-        la.dir_stride = long_dir_stride(max_r);
-        la.best = best2;
-        la.aln = aln;
-        la.qcons = cq;
-        la.rcons = cr;
-        la.cons_stride = cs;
-        for (int64_t off = 0; off < cnt; off += batch) {
-          la.list = sorted + long_groups[lg].first + off;
-          la.n = std::min(batch, cnt - off);
-          const int kk = launch_sw_long(st, la, rpl);
-          if (kk == 0) return fail(ctx, SWIFT_E_DEVICE, "long pass could not launch");
-          launches += kk;
-          CKLAUNCH();
-        }
-        ps.segments += 1;
       }
     }
     aln_to_i32_kernel<<<(unsigned)((cn + 255) / 256), 256, 0, st>>>(

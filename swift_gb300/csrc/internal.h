@@ -268,8 +268,8 @@ struct LongArgs {
   int64_t n;
   int max_r;                  // longest window of the launch
   int match, mismatch, gap_open, gap_ext, bias;
-  uint32_t* dirs;             // direction scratch: n x 256 threads x dir_stride words
-  int64_t dir_stride;
+  uint32_t* dirs;             // direction scratch: the slot of item i at dirs + dir_off[i],
+  const int64_t* dir_off;     // long_slot_words(R of its pair) words
   int2* best;                 // per pair: (score, first maximum cell)
   DevAln* aln;
   char* qcons;                // optional reversed consensus strings
@@ -277,8 +277,7 @@ struct LongArgs {
   int64_t cons_stride;
 };
 int long_rows_per_lane(int Q);           // 4, 8, 12 or 16; 0 beyond 4096
-int64_t long_dir_stride(int max_r);
-int64_t long_scratch_words(int max_r, int64_t pairs);
+int64_t long_slot_words(int R);          // direction words of one pair (16-byte multiple)
 int launch_sw_long(cudaStream_t st, const LongArgs& a, int rpl);
 
 // sw_fast.cu: packed 16-bit passes (score of every pair; trace of printed pairs)

@@ -73,7 +73,8 @@ __global__ void __launch_bounds__(kLT) sw_long_kernel(LongArgs a) {
     bestc[k] = 0;
   }
   const int S4 = (R + 31 + 3) & ~3;  // steps of one thread's direction words
-  uint32_t* dirs = a.dirs + ((int64_t)item * kLT + tid) * a.dir_stride;
+  // the pair's own slot: 256 threads x S4 words from dir_off[item]
+  uint32_t* dirs = a.dirs + a.dir_off[item] + (int64_t)tid * S4;
   __syncthreads();
   int send_u = B, send_h = B, diag = B;
   uint32_t hist[4];
@@ -195,17 +196,22 @@ __global__ void __launch_bounds__(128) sw_long_walk_kernel(LongArgs a) {
   const int R = a.r_len[p];
   const char* qg = a.qry + a.q_off[p];
   const char* wg = a.ref + a.r_off[p];
-  const uint32_t* dirs = a.dirs + (int64_t)item * kLT * a.dir_stride;
+  const int S4 = (R + 31 + 3) & ~3;
+  const uint32_t* dirs = a.dirs + a.dir_off[item];
   const int W = R + 1;
+  // four consecutive steps of one thread per load: a diagonal run of the
+  // walk stays in one thread's rows and moves one step back per cell
   int64_t last = -1;
-  uint32_t word = 0;
+  uint4 words = make_uint4(0, 0, 0, 0);
   auto code_at = [&](int i, int jj) -> uint32_t {
     const int t = (i - 1) / RPL, k = (i - 1) % RPL, ln = t & 31;
-    const int64_t at = (int64_t)t * a.dir_stride + (jj + ln - 1);
-    if (at != last) {
-      word = __ldcg(&dirs[at]);
-      last = at;
+    const int64_t at = (int64_t)t * S4 + (jj + ln - 1);
+    if ((at & ~(int64_t)3) != last) {
+      last = at & ~(int64_t)3;
+      words = __ldcg(reinterpret_cast<const uint4*>(dirs + last));
     }
+    const int q = (int)(at & 3);
+    const uint32_t word = q == 0 ? words.x : q == 1 ? words.y : q == 2 ? words.z : words.w;
     return (word >> (2 * k)) & 3u;
   };
   enum : int { kNone = 0, kDiag = 1, kUp = 2, kLeft = 3 };
@@ -285,11 +291,7 @@ int long_rows_per_lane(int Q) {
   return Q <= 4 * kLT ? 4 : Q <= 8 * kLT ? 8 : Q <= 12 * kLT ? 12 : Q <= 16 * kLT ? 16 : 0;
 }
 
-int64_t long_dir_stride(int max_r) { return (int64_t)((max_r + 31 + 3) & ~3); }
-
-int64_t long_scratch_words(int max_r, int64_t pairs) {
-  return pairs * kLT * long_dir_stride(max_r);
-}
+int64_t long_slot_words(int R) { return (int64_t)kLT * ((R + 31 + 3) & ~3); }
 
 int launch_sw_long(cudaStream_t st, const LongArgs& a, int rpl) {
   if (a.n <= 0) return 0;
