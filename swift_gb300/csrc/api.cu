@@ -1066,6 +1066,7 @@ int swift_sw_pairs(swift_ctx* ctx, const char* qry, const int64_t* q_off, const 
     va.wbuf = wbuf;
     va.q_stride = q_stride;
     va.w_stride = w_stride;
+    va.long_prof = long_prof_ok(m, x, o, kLongMaxQ);
     va.class_ok = 0;
     for (int c = 0; mode == 0 && c < 6; ++c)
       if (fast_params_ok(packed_class_max_q(c), kFastMaxR, m, x, o, e, &bias0)) va.class_ok |= 1u << c;
@@ -1140,7 +1141,7 @@ int swift_sw_pairs(swift_ctx* ctx, const char* qry, const int64_t* q_off, const 
       for (uint32_t s = 0; s < nseg; ++s) {
         if ((uint32_t)hk[s] >= kVarLongKey) {
           long_groups.push_back({hs[s], hc[s]});
-          long_class.push_back((int)((uint32_t)hk[s] - kVarLongKey));
+          long_class.push_back((int)((uint32_t)hk[s] - kVarLongKey));  // 2 class + profile bit
           continue;
         }
         const bool gen = (hk[s] >> 20) & 1;
@@ -1254,7 +1255,8 @@ int swift_sw_pairs(swift_ctx* ctx, const char* qry, const int64_t* q_off, const 
             const int64_t cu = (int64_t)hql[u] * hrl[u], cv = (int64_t)hql[v] * hrl[v];
             return cu != cv ? cu > cv : u < v;
           });
-          const int rpl = 4 * (long_class[lg] + 1);
+          const int rpl = 4 * ((long_class[lg] >> 1) + 1);
+          const bool prof = long_class[lg] & 1;
           const int64_t budget_words = (int64_t)(12.0e9 / 4);
           int64_t b0 = 0;
           while (b0 < cnt) {
@@ -1292,7 +1294,7 @@ int swift_sw_pairs(swift_ctx* ctx, const char* qry, const int64_t* q_off, const 
             la.mismatch = x;
             la.gap_open = o;
             la.gap_ext = e;
-            la.bias = ((-(16 * o + 1)) + 15) & ~15;
+            la.bias = long_bias(o);
             la.dirs = dirs;
             la.dir_off = doff;
             la.best = best2;
@@ -1300,7 +1302,7 @@ int swift_sw_pairs(swift_ctx* ctx, const char* qry, const int64_t* q_off, const 
             la.qcons = cq;
             la.rcons = cr;
             la.cons_stride = cs;
-            const int kk = launch_sw_long(st, la, rpl);
+            const int kk = launch_sw_long(st, la, rpl, prof);
             if (kk == 0) return fail(ctx, SWIFT_E_DEVICE, "long pass could not launch");
             launches += kk;
             CKLAUNCH();

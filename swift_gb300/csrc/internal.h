@@ -221,8 +221,9 @@ int launch_sw(cudaStream_t st, const SwArgs& a, std::string* err);
 
 // pairs_var.cu: explicit pairs of varying lengths, sorted by shape
 constexpr uint32_t kVarKeys = 1u << 21;  // shape keys: generic bit, Q (9 bits), R (11 bits)
-// the top four keys: long pairs (sw_long.cu) by rows-per-lane class
-constexpr uint32_t kVarLongKey = kVarKeys - 4;
+// the top eight keys: long pairs (sw_long.cu) by rows-per-lane class (key
+// bits 2-1) and whether they hold only ACGTN bytes (bit 0)
+constexpr uint32_t kVarLongKey = kVarKeys - 8;
 // pairs beyond the warp-per-pair kernels' shapes go to the long kernel
 __host__ __device__ inline bool var_pair_long(int Q, int R) {
   return Q > 256 || R > 1024 || (Q > 128 && R > 768);
@@ -239,6 +240,7 @@ struct VarPairArgs {
   char* wbuf;
   int64_t q_stride, w_stride;
   uint32_t class_ok;          // bit c: the packed passes take this scoring for class c
+  bool long_prof;             // the long kernel's profile path takes this scoring
   int fast_max_r;
   uint32_t* key;              // per pair
   uint32_t* hist;             // per key
@@ -278,7 +280,13 @@ struct LongArgs {
 };
 int long_rows_per_lane(int Q);           // 4, 8, 12 or 16; 0 beyond 4096
 int64_t long_slot_words(int R);          // direction words of one pair (16-byte multiple)
-int launch_sw_long(cudaStream_t st, const LongArgs& a, int rpl);
+// the long kernel's cell bias for a gap-open penalty, and whether its
+// profile path takes a scoring for queries up to max_q rows; prof: every
+// pair of the launch holds only ACGTN bytes (either case) and
+// long_prof_ok(...) holds
+int long_bias(int gap_open);
+bool long_prof_ok(int m, int x, int gap_open, int max_q);
+int launch_sw_long(cudaStream_t st, const LongArgs& a, int rpl, bool prof);
 
 // sw_fast.cu: packed 16-bit passes (score of every pair; trace of printed pairs)
 // Bound-pass suffix maxima: blocks of wavefront steps, blocks per pair.

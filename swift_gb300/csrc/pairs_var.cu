@@ -34,9 +34,15 @@ __global__ void __launch_bounds__(kVarWarps * 32) pack_var_kernel(VarPairArgs a)
   if (i >= a.n) return;
   const int Q = a.q_len[i], R = a.r_len[i];
   if (var_pair_long(Q, R)) {  // read in place by the long kernel
+    bool other = false;  // a byte outside ACGTN (either case)
+    const char* qs = a.qry + a.q_off[i];
+    const char* ws = a.ref + a.r_off[i];
+    for (int t = lane; t < Q; t += 32) other |= !acgt((uint8_t)qs[t]) && ((uint8_t)qs[t] & 0xDFu) != 'N';
+    for (int t = lane; t < R; t += 32) other |= !acgt((uint8_t)ws[t]) && ((uint8_t)ws[t] & 0xDFu) != 'N';
+    other = __any_sync(0xffffffffu, other);
     if (lane == 0) {
       const int c = Q <= 1024 ? 0 : Q <= 2048 ? 1 : Q <= 3072 ? 2 : 3;
-      const uint32_t key = kVarLongKey + (uint32_t)c;
+      const uint32_t key = kVarLongKey + 2 * (uint32_t)c + ((other || !a.long_prof) ? 0u : 1u);
       a.key[i] = key;
       atomicAdd(&a.hist[key], 1u);
     }

@@ -18,6 +18,8 @@
 // per wavefront step to global scratch (four steps per 16-byte store);
 // sw_long_walk_kernel then walks the reference's traceback, one thread per
 // pair, carrying the cell score to tell NONE from LEFT.
+#include <type_traits>
+
 #include "internal.h"
 
 namespace swift {
@@ -33,8 +35,28 @@ __device__ __forceinline__ int upcase(uint8_t c) {
   return (unsigned)(c - 'a') < 26u ? c - 'a' + 'A' : c;
 }
 
-template <int RPL>
-__global__ void __launch_bounds__(kLT) sw_long_kernel(LongArgs a) {
+constexpr int kColMask = (1 << 17) - 1;
+
+__device__ __forceinline__ uint32_t prmt_b(uint32_t a, uint32_t b, uint32_t s) {
+  uint32_t d;
+  asm("prmt.b32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(s));
+  return d;
+}
+
+// base class of an ACGTN pair byte: A 0, C 1, G 2, T 3, N 4 (either case)
+__device__ __forceinline__ int class5(uint8_t c) {
+  const int u = upcase(c);
+  return u == 'C' ? 1 : u == 'G' ? 2 : u == 'T' ? 3 : u == 'N' ? 4 : 0;
+}
+
+// PROF: the pair holds only ACGTN bytes (either case) and 16 m Q stays below
+// 2^18.  Then the substitution score is one byte permute of a per-row
+// profile (window classes A, C, G, T, N), and a row's first maximum is one
+// max over keys 2^17 H' + (2^17 - 1 - column), H' = H + B / 16 (16 H + B
+// times 2^13, whose low 17 bits are zero): the largest H, and on equal H the
+// smallest column.  Other pairs compare bytes.
+template <int RPL, bool PROF>
+__global__ void __launch_bounds__(kLT, 2) sw_long_kernel(LongArgs a) {
   extern __shared__ __align__(16) uint8_t smem[];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int64_t item = (int64_t)blockIdx.x;
@@ -49,8 +71,13 @@ __global__ void __launch_bounds__(kLT) sw_long_kernel(LongArgs a) {
   // ring[(b * 2 + 0) * kRing + col % kRing]: UP candidate of boundary b's upper row
   // ring[(b * 2 + 1) * kRing + col % kRing]: its H (code bits cleared)
   for (int c = tid; c < R; c += kLT) {
-    const int u = upcase((uint8_t)wg[c]);
-    wu[c + 1] = (int16_t)(u == 'N' ? kWild : u);
+    if (PROF) {  // byte-permute selector: the class's byte, sign-extended
+      const uint32_t k = (uint32_t)class5((uint8_t)wg[c]);
+      wu[c + 1] = (int16_t)(k | ((k | 8u) << 4) | ((k | 8u) << 8) | ((k | 8u) << 12));
+    } else {
+      const int u = upcase((uint8_t)wg[c]);
+      wu[c + 1] = (int16_t)(u == 'N' ? kWild : u);
+    }
   }
   const int B = a.bias;
   const int B8 = B + 8;
@@ -58,18 +85,33 @@ __global__ void __launch_bounds__(kLT) sw_long_kernel(LongArgs a) {
   const int KU = 8 * (a.gap_ext - a.gap_open), KL = 16 * (a.gap_ext - a.gap_open);
   const int SM = 16 * a.match + 4, SX = 16 * a.mismatch + 4;
   int qv[RPL], h16p[RPL], xl[RPL], bestv[RPL], bestc[RPL];
+  uint32_t pf0[PROF ? RPL : 1], pf1[PROF ? RPL : 1];
+  const uint32_t sm8 = (uint32_t)(uint8_t)(int8_t)SM, sx8 = (uint32_t)(uint8_t)(int8_t)SX;
 #pragma unroll
   for (int k = 0; k < RPL; ++k) {
     const int i = tid * RPL + k;
-    if (i < Q) {
-      const int u = upcase((uint8_t)qg[i]);
-      qv[k] = u == 'N' ? kWild : u;
+    if (PROF) {
+      // scores against window classes A C G T (pf0) and N (pf1 byte 0);
+      // rows past the query mismatch everything (and stay out of the maximum)
+      const int qc = i < Q ? class5((uint8_t)qg[i]) : -1;
+      uint32_t v0 = 0;
+#pragma unroll
+      for (int w = 0; w < 4; ++w)
+        v0 |= ((qc == w || qc == 4) ? sm8 : sx8) << (8 * w);
+      pf0[k] = v0;
+      pf1[k] = qc >= 0 ? sm8 : sx8;
+      bestv[k] = B * 8192 + kColMask;  // H = 0 at column 0: no H = 0 cell beats it
     } else {
-      qv[k] = -1;  // past the query: matches nothing (kept out of the maximum)
+      if (i < Q) {
+        const int u = upcase((uint8_t)qg[i]);
+        qv[k] = u == 'N' ? kWild : u;
+      } else {
+        qv[k] = -1;  // past the query: matches nothing (kept out of the maximum)
+      }
+      bestv[k] = B;
     }
     h16p[k] = B;
     xl[k] = B;
-    bestv[k] = B;
     bestc[k] = 0;
   }
   const int S4 = (R + 31 + 3) & ~3;  // steps of one thread's direction words
@@ -77,7 +119,72 @@ __global__ void __launch_bounds__(kLT) sw_long_kernel(LongArgs a) {
   uint32_t* dirs = a.dirs + a.dir_off[item] + (int64_t)tid * S4;
   __syncthreads();
   int send_u = B, send_h = B, diag = B;
-  uint32_t hist[4];
+  // One wavefront step: this lane's column j against its RPL rows.  FULL:
+  // every lane's column lies in 1..R (a warp-uniform fact of the step), so
+  // no lane is masked and the rows' state updates in place.
+  auto step = [&](const int s, auto full) -> uint32_t {
+    constexpr bool kFull = decltype(full)::value;
+    int up = __shfl_up_sync(0xffffffffu, send_u, 1);
+    const int rh = __shfl_up_sync(0xffffffffu, send_h, 1);
+    const int j = s - lane + 1;  // this lane's column
+    const bool in = kFull || (j >= 1 && j <= R);
+    if (lane == 0) {
+      if (warp == 0) {
+        up = B;  // row 0
+      } else if (in) {
+        up = ring[((warp - 1) * 2 + 0) * kRing + (j & (kRing - 1))];
+      }
+    }
+    uint32_t acc = 0;
+    if (in) {
+      const int rv = wu[j];
+      const int cj = kColMask - j;
+      int dg = diag;
+#pragma unroll
+      for (int k = 0; k < RPL; ++k) {
+        int sc;
+        if (PROF) {
+          sc = (int)prmt_b(pf0[k], pf1[k], (uint32_t)(uint16_t)rv);
+        } else {
+          const bool hit = qv[k] == rv || qv[k] == kWild || (rv == kWild && qv[k] >= 0);
+          sc = hit ? SM : SX;
+        }
+        const int m3 = __vimax3_s32(xl[k] + CL, up + CU, B8);
+        const int hx = __viaddmax_s32(dg, sc, m3);
+        dg = h16p[k];
+        const int h16 = hx & ~15;
+        h16p[k] = h16;
+        up = (hx & 2) * KU + h16;
+        xl[k] = (hx & 1) * KL + h16;
+        if (PROF) {
+          bestv[k] = max(bestv[k], h16 * 8192 + cj);
+        } else if (h16 > bestv[k]) {
+          bestv[k] = h16;
+          bestc[k] = j;
+        }
+        // 2 DIAG, 1 UP, 0 LEFT / NONE: code bits 2..1 to bits 2k+1..2k
+        if (k == 0) {
+          acc |= ((uint32_t)hx >> 1) & 3u;
+        } else {
+          acc |= ((uint32_t)hx << (2 * k - 1)) & (3u << (2 * k));
+        }
+      }
+      send_u = up;
+      send_h = h16p[RPL - 1];
+      if (lane == 31 && warp + 1 < kLW) {
+        ring[(warp * 2 + 0) * kRing + (j & (kRing - 1))] = up;
+        ring[(warp * 2 + 1) * kRing + (j & (kRing - 1))] = send_h;
+      }
+    }
+    // the diagonal of the next step: lane above's bottom H at this column
+    // (lane 0: from the ring; column 0 is H = 0)
+    if (lane == 0) {
+      diag = (warp == 0 || !in) ? B : ring[((warp - 1) * 2 + 1) * kRing + (j & (kRing - 1))];
+    } else {
+      diag = rh;
+    }
+    return acc;
+  };
   const int steps = R + 31;                          // a warp's wavefront
   const int n_stages = 2 * (kLW - 1) + (steps + kStage - 1) / kStage;
   for (int stage = 0; stage < n_stages; ++stage) {
@@ -85,61 +192,19 @@ __global__ void __launch_bounds__(kLT) sw_long_kernel(LongArgs a) {
     if (s_lo >= 0 && s_lo < steps) {
 #pragma unroll 1
       for (int s0 = s_lo; s0 < s_lo + kStage; s0 += 4) {
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const int s = s0 + u;
-          hist[u] = 0;
-          int up = __shfl_up_sync(0xffffffffu, send_u, 1);
-          const int rh = __shfl_up_sync(0xffffffffu, send_h, 1);
-          const int j = s - lane + 1;  // this lane's column
-          if (lane == 0) {
-            if (warp == 0) {
-              up = B;  // row 0
-            } else if (j >= 1 && j <= R) {
-              up = ring[((warp - 1) * 2 + 0) * kRing + j % kRing];
-            }
-          }
-          if (j >= 1 && j <= R) {
-            const int rv = wu[j];
-            int dg = diag;
-            uint32_t acc = 0;
-#pragma unroll
-            for (int k = 0; k < RPL; ++k) {
-              const bool hit = qv[k] == rv || qv[k] == kWild || (rv == kWild && qv[k] >= 0);
-              const int sc = hit ? SM : SX;
-              const int m3 = __vimax3_s32(xl[k] + CL, up + CU, B8);
-              const int hx = __viaddmax_s32(dg, sc, m3);
-              dg = h16p[k];
-              const int h16 = hx & ~15;
-              h16p[k] = h16;
-              up = (hx & 2) * KU + h16;
-              xl[k] = (hx & 1) * KL + h16;
-              if (h16 > bestv[k]) {
-                bestv[k] = h16;
-                bestc[k] = j;
-              }
-              acc |= (uint32_t)((hx >> 1) & 3) << (2 * k);  // 2 DIAG, 1 UP, 0 LEFT / NONE
-            }
-            hist[u] = acc;
-            send_u = up;
-            send_h = h16p[RPL - 1];
-            if (lane == 31 && warp + 1 < kLW) {
-              ring[(warp * 2 + 0) * kRing + j % kRing] = up;
-              ring[(warp * 2 + 1) * kRing + j % kRing] = send_h;
-            }
-          }
-          // the diagonal of the next step: lane above's bottom H at this
-          // column (lane 0: from the ring; column 0 is H = 0)
-          if (lane == 0) {
-            diag = (warp == 0 || j < 1 || j > R) ? B : ring[((warp - 1) * 2 + 1) * kRing + j % kRing];
-          } else {
-            diag = rh;
-          }
+        uint4 v;
+        if (s0 >= 31 && s0 + 3 <= R - 1) {  // lane 31 past column 0, lane 0 short of R + 1
+          v.x = step(s0, std::true_type());
+          v.y = step(s0 + 1, std::true_type());
+          v.z = step(s0 + 2, std::true_type());
+          v.w = step(s0 + 3, std::true_type());
+        } else {
+          v.x = step(s0, std::false_type());
+          v.y = step(s0 + 1, std::false_type());
+          v.z = step(s0 + 2, std::false_type());
+          v.w = step(s0 + 3, std::false_type());
         }
-        if (s0 < S4) {
-          const uint4 v = make_uint4(hist[0], hist[1], hist[2], hist[3]);
-          __stcg(reinterpret_cast<uint4*>(dirs + s0), v);
-        }
+        if (s0 < S4) __stcg(reinterpret_cast<uint4*>(dirs + s0), v);
       }
     }
     __syncthreads();
@@ -149,10 +214,11 @@ __global__ void __launch_bounds__(kLT) sw_long_kernel(LongArgs a) {
 #pragma unroll
   for (int k = 0; k < RPL; ++k) {
     const int i = tid * RPL + k;
-    if (i < Q && bestv[k] > bv) {
-      bv = bestv[k];
+    const int v = PROF ? (bestv[k] >> 17) << 4 : bestv[k];
+    if (i < Q && v > bv) {
+      bv = v;
       br = i + 1;
-      bc = bestc[k];
+      bc = PROF ? kColMask - (bestv[k] & kColMask) : bestc[k];
     }
   }
   __shared__ int red_v[kLW], red_r[kLW], red_c[kLW];
@@ -278,9 +344,12 @@ __global__ void __launch_bounds__(128) sw_long_walk_kernel(LongArgs a) {
 }
 
 template <int RPL>
-int launch_long_rpl(cudaStream_t st, const LongArgs& a) {
+int launch_long_rpl(cudaStream_t st, const LongArgs& a, bool prof) {
   const size_t smem = ((2 * (a.max_r + 1) + 15) & ~15) + (size_t)(kLW - 1) * 2 * kRing * 4;
-  sw_long_kernel<RPL><<<(unsigned)a.n, kLT, smem, st>>>(a);
+  if (prof)
+    sw_long_kernel<RPL, true><<<(unsigned)a.n, kLT, smem, st>>>(a);
+  else
+    sw_long_kernel<RPL, false><<<(unsigned)a.n, kLT, smem, st>>>(a);
   sw_long_walk_kernel<RPL><<<(unsigned)((a.n + 127) / 128), 128, 0, st>>>(a);
   return 2;
 }
@@ -293,15 +362,25 @@ int long_rows_per_lane(int Q) {
 
 int64_t long_slot_words(int R) { return (int64_t)kLT * ((R + 31 + 3) & ~3); }
 
-int launch_sw_long(cudaStream_t st, const LongArgs& a, int rpl) {
+int long_bias(int gap_open) { return ((-(16 * gap_open + 1)) + 15) & ~15; }
+
+bool long_prof_ok(int m, int x, int gap_open, int max_q) {
+  return 16 * m + 4 <= 127 && 16 * x + 4 >= -128 &&
+         16ll * m * max_q + long_bias(gap_open) + 16 < (1ll << 18);
+}
+
+int launch_sw_long(cudaStream_t st, const LongArgs& a, int rpl, bool prof) {
   if (a.n <= 0) return 0;
   // shared memory: window (2 B per column) + rings, 23 KB at the longest window
   if (((2 * (a.max_r + 1) + 15) & ~15) + (kLW - 1) * 2 * kRing * 4 > 48 * 1024) return 0;
+  if (prof && (a.bias != long_bias(a.gap_open) ||
+               !long_prof_ok(a.match, a.mismatch, a.gap_open, 256 * rpl)))
+    return 0;
   switch (rpl) {
-    case 4: return launch_long_rpl<4>(st, a);
-    case 8: return launch_long_rpl<8>(st, a);
-    case 12: return launch_long_rpl<12>(st, a);
-    case 16: return launch_long_rpl<16>(st, a);
+    case 4: return launch_long_rpl<4>(st, a, prof);
+    case 8: return launch_long_rpl<8>(st, a, prof);
+    case 12: return launch_long_rpl<12>(st, a, prof);
+    case 16: return launch_long_rpl<16>(st, a, prof);
     default: return 0;
   }
 }

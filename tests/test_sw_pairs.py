@@ -179,8 +179,17 @@ def test_long_pairs_vs_oracle(ctx, oracle):
                 q = q[:k] + bytearray(b"GT") + q[k:-2]
         q[rng.randrange(Q)] = ord("N")
         w[rng.randrange(R)] = ord("n")
+        if Q in (1000, 3000):  # lowercase runs (still ACGTN pairs)
+            q[: Q // 5] = q[: Q // 5].lower()
+            w[R // 2:] = w[R // 2:].lower()
+        if Q in (1500, 3500):  # IUPAC bytes: the byte-compare path
+            q[rng.randrange(Q)] = ord("R")
+            w[rng.randrange(R)] = ord("y")
         qs.append(bytes(q))
         ws.append(bytes(w))
+    # no cell above zero, and a single matching base: first-maximum ties
+    qs += [b"A" * 300, b"A" * 1100]
+    ws += [b"C" * 900, b"C" * 700 + b"A" + b"C" * 600]
     sq, sw_ = make_pairs(40, seed=92)
     qs += sq
     ws += sw_
@@ -190,6 +199,10 @@ def test_long_pairs_vs_oracle(ctx, oracle):
     check_against_oracle(res, qs, ws, oracle, (2, -1, -10, -1))
     res2, _ = ctx.sw_pairs(qb, qo, ql, wb, wo, wl, 3, -2, -5, -2)
     check_against_oracle(res2, qs, ws, oracle, (3, -2, -5, -2))
+    # a match score whose largest cells leave the profile path's key range
+    # for 4000-row queries, and a large gap-open bias
+    res3, _ = ctx.sw_pairs(qb, qo, ql, wb, wo, wl, 5, -3, -40, -2)
+    check_against_oracle(res3, qs, ws, oracle, (5, -3, -40, -2))
 
 
 def test_long_workload_vs_oracle(ctx, oracle):
