@@ -26,6 +26,8 @@ struct swift_ctx {
   char* d_text = nullptr;
   size_t text_len = 0, text_cap = 0;
   int sw_path = 0;  // 0 bounded selection, 1 generic kernel only, 2 exact score of every pair
+  cudaStream_t side = nullptr;  // second stream for concurrent launches, made on first use
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
 };
 
 struct swift_index {
@@ -96,6 +98,38 @@ struct Scratch {
     ptrs.push_back(p);
     *out = (T*)p;
     return cudaSuccess;
+  }
+};
+
+// Work after side_fork may run on ctx->side as well as ctx->st; SideJoin
+// orders ctx->st after it again (at join(), or when it leaves scope, so an
+// early error return still joins before the scratch is freed on ctx->st).
+int side_fork(swift_ctx* ctx) {
+  if (!ctx->side) {
+    if (cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->join_ev, cudaEventDisableTiming) != cudaSuccess)
+      return fail(ctx, SWIFT_E_CUDA, "side stream: " + std::string(cudaGetErrorString(cudaGetLastError())));
+  }
+  if (cudaEventRecord(ctx->fork_ev, ctx->st) != cudaSuccess ||
+      cudaStreamWaitEvent(ctx->side, ctx->fork_ev, 0) != cudaSuccess)
+    return fail(ctx, SWIFT_E_CUDA, "side stream fork failed");
+  return SWIFT_OK;
+}
+
+struct SideJoin {
+  swift_ctx* ctx;
+  bool armed = false;
+  explicit SideJoin(swift_ctx* c) : ctx(c) {}
+  int join() {
+    armed = false;
+    if (cudaEventRecord(ctx->join_ev, ctx->side) != cudaSuccess ||
+        cudaStreamWaitEvent(ctx->st, ctx->join_ev, 0) != cudaSuccess)
+      return fail(ctx, SWIFT_E_CUDA, "side stream join failed");
+    return SWIFT_OK;
+  }
+  ~SideJoin() {
+    if (armed) join();
   }
 };
 
@@ -505,6 +539,12 @@ int swift_ctx_destroy(swift_ctx* ctx) {
   if (ctx->d_text) cudaFree(ctx->d_text);
   for (int i = 0; i < 10; ++i)
     if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
+  if (ctx->side) {
+    cudaStreamSynchronize(ctx->side);
+    cudaStreamDestroy(ctx->side);
+    cudaEventDestroy(ctx->fork_ev);
+    cudaEventDestroy(ctx->join_ev);
+  }
   if (ctx->own_stream) cudaStreamDestroy(ctx->st);
   delete ctx;
   return SWIFT_OK;
@@ -1046,9 +1086,10 @@ int swift_sw_pairs(swift_ctx* ctx, const char* qry, const int64_t* q_off, const 
       CK(sc.get(&orc, (size_t)(nc * cs)));
     }
   }
-  uint32_t* dirs = nullptr;
-  int64_t dirs_words = 0;
+  uint32_t* dirs[2] = {nullptr, nullptr};
+  int64_t dirs_words[2] = {0, 0};
   int launches = 0;
+  SideJoin joined(ctx);  // after sc: joins the side stream before sc frees
   for (int64_t c0 = 0; c0 < n; c0 += chunk) {
     const int64_t cn = std::min(chunk, n - c0);
     char* cq = qcons ? (out_dev ? qcons + c0 * cs : oqc) : nullptr;
@@ -1202,9 +1243,9 @@ int swift_sw_pairs(swift_ctx* ctx, const char* qry, const int64_t* q_off, const 
         // in sub-chunks that bound the direction scratch
         const int64_t sub = 262144;
         const int64_t words = trace_scratch_words(Q, R, std::min(cnt, sub));
-        if (words > dirs_words) {
-          CK(sc.get(&dirs, (size_t)words));
-          dirs_words = words;
+        if (words > dirs_words[0]) {
+          CK(sc.get(&dirs[0], (size_t)words));
+          dirs_words[0] = words;
         }
         FastArgs fa;
         memset(&fa, 0, sizeof(fa));
@@ -1223,7 +1264,7 @@ int swift_sw_pairs(swift_ctx* ctx, const char* qry, const int64_t* q_off, const 
         fa.bias = bias;
         fa.aln = aln;
         fa.best = best2;
-        fa.dirs = dirs;
+        fa.dirs = dirs[0];
         fa.qcons = cq;
         fa.rcons = cr;
         fa.cons_stride = cs;
@@ -1239,78 +1280,111 @@ int swift_sw_pairs(swift_ctx* ctx, const char* qry, const int64_t* q_off, const 
       }
       // long pairs: one CTA each, largest first, in launches of many waves
       // (the block scheduler fills SMs freed by small pairs) whose direction
-      // slots, sized per pair, fit a scratch budget
+      // slots, sized per pair, fit one of two scratch regions.  Launches
+      // alternate between the context stream and a side stream, each
+      // launch's walk on its own stream: a walk (a few threads per SM)
+      // overlaps the next launch's fill, and a region is reused only after
+      // the walk that read it.
       if (!long_groups.empty()) {
         std::vector<int32_t> hql(cn), hrl(cn);
         CK(cudaMemcpyAsync(hql.data(), dql + c0, cn * 4, cudaMemcpyDeviceToHost, st));
         CK(cudaMemcpyAsync(hrl.data(), drl + c0, cn * 4, cudaMemcpyDeviceToHost, st));
-        std::vector<int32_t> ids;
+        int64_t n_long = 0;
+        for (const auto& g : long_groups) n_long += g.second;
+        std::vector<int32_t> ids(n_long);
+        int64_t at = 0;
+        for (const auto& g : long_groups) {
+          CK(cudaMemcpyAsync(ids.data() + at, sorted + g.first, g.second * 4,
+                             cudaMemcpyDeviceToHost, st));
+          at += g.second;
+        }
+        CK(cudaStreamSynchronize(st));
+        struct LongBatch {
+          int rpl;
+          bool prof;
+          int64_t b0, nb, words;
+        };
+        std::vector<LongBatch> batches;
+        std::vector<int64_t> off(n_long);
+        const int64_t region_words = (int64_t)(8.0e9 / 4);
+        int64_t max_words = 0;
+        at = 0;
         for (size_t lg = 0; lg < long_groups.size(); ++lg) {
           const int64_t cnt = long_groups[lg].second;
-          ids.resize(cnt);
-          CK(cudaMemcpyAsync(ids.data(), sorted + long_groups[lg].first, cnt * 4,
-                             cudaMemcpyDeviceToHost, st));
-          CK(cudaStreamSynchronize(st));
-          std::sort(ids.begin(), ids.end(), [&](int32_t u, int32_t v) {
+          int32_t* g = ids.data() + at;
+          std::sort(g, g + cnt, [&](int32_t u, int32_t v) {
             const int64_t cu = (int64_t)hql[u] * hrl[u], cv = (int64_t)hql[v] * hrl[v];
             return cu != cv ? cu > cv : u < v;
           });
           const int rpl = 4 * ((long_class[lg] >> 1) + 1);
           const bool prof = long_class[lg] & 1;
-          const int64_t budget_words = (int64_t)(12.0e9 / 4);
           int64_t b0 = 0;
           while (b0 < cnt) {
-            // one launch: items b0 .. b1 - 1 with their slot offsets
-            std::vector<int64_t> off;
             int64_t words = 0, b1 = b0;
-            while (b1 < cnt && (b1 == b0 || words + long_slot_words(hrl[ids[b1]]) <= budget_words)) {
-              off.push_back(words);
-              words += long_slot_words(hrl[ids[b1]]);
+            while (b1 < cnt && (b1 == b0 || words + long_slot_words(hrl[g[b1]]) <= region_words)) {
+              off[at + b1] = words;
+              words += long_slot_words(hrl[g[b1]]);
               ++b1;
             }
-            const int64_t nb = b1 - b0;
-            if (words > dirs_words) {
-              CK(sc.get(&dirs, (size_t)words));
-              dirs_words = words;
-            }
-            int32_t* dlist;
-            int64_t* doff;
-            CK(sc.get(&dlist, (size_t)nb));
-            CK(sc.get(&doff, (size_t)nb));
-            CK(cudaMemcpyAsync(dlist, ids.data() + b0, nb * 4, cudaMemcpyHostToDevice, st));
-            CK(cudaMemcpyAsync(doff, off.data(), nb * 8, cudaMemcpyHostToDevice, st));
-            LongArgs la;
-            memset(&la, 0, sizeof(la));
-            la.qry = dq;
-            la.q_off = dqo + c0;
-            la.q_len = dql + c0;
-            la.ref = dr;
-            la.r_off = dro + c0;
-            la.r_len = drl + c0;
-            la.list = dlist;
-            la.n = nb;
-            la.max_r = kLongMaxR;
-            la.match = m;
-            la.mismatch = x;
-            la.gap_open = o;
-            la.gap_ext = e;
-            la.bias = long_bias(o);
-            la.dirs = dirs;
-            la.dir_off = doff;
-            la.best = best2;
-            la.aln = aln;
-            la.qcons = cq;
-            la.rcons = cr;
-            la.cons_stride = cs;
-            const int kk = launch_sw_long(st, la, rpl, prof);
-            if (kk == 0) return fail(ctx, SWIFT_E_DEVICE, "long pass could not launch");
-            launches += kk;
-            CKLAUNCH();
-            // (copies from pageable host memory are staged before they
-            // return; the next launch reuses the scratch in stream order)
+            batches.push_back({rpl, prof, at + b0, b1 - b0, words});
+            max_words = std::max(max_words, words);
             b0 = b1;
           }
+          at += cnt;
           ps.segments += 1;
+        }
+        int32_t* dlist;
+        int64_t* doff;
+        CK(sc.get(&dlist, (size_t)n_long));
+        CK(sc.get(&doff, (size_t)n_long));
+        CK(cudaMemcpyAsync(dlist, ids.data(), n_long * 4, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(doff, off.data(), n_long * 8, cudaMemcpyHostToDevice, st));
+        const int n_regions = batches.size() > 1 ? 2 : 1;
+        for (int r = 0; r < n_regions; ++r) {
+          if (max_words > dirs_words[r]) {
+            CK(sc.get(&dirs[r], (size_t)max_words));
+            dirs_words[r] = max_words;
+          }
+        }
+        if (n_regions > 1) {
+          const int rc = side_fork(ctx);
+          if (rc != SWIFT_OK) return rc;
+          joined.armed = true;
+        }
+        for (size_t b = 0; b < batches.size(); ++b) {
+          const LongBatch& lb = batches[b];
+          cudaStream_t bs = (b & 1) ? ctx->side : st;
+          LongArgs la;
+          memset(&la, 0, sizeof(la));
+          la.qry = dq;
+          la.q_off = dqo + c0;
+          la.q_len = dql + c0;
+          la.ref = dr;
+          la.r_off = dro + c0;
+          la.r_len = drl + c0;
+          la.list = dlist + lb.b0;
+          la.n = lb.nb;
+          la.max_r = kLongMaxR;
+          la.match = m;
+          la.mismatch = x;
+          la.gap_open = o;
+          la.gap_ext = e;
+          la.bias = long_bias(o);
+          la.dirs = dirs[b & 1];
+          la.dir_off = doff + lb.b0;
+          la.best = best2;
+          la.aln = aln;
+          la.qcons = cq;
+          la.rcons = cr;
+          la.cons_stride = cs;
+          const int kk = launch_sw_long(bs, la, lb.rpl, lb.prof);
+          if (kk == 0) return fail(ctx, SWIFT_E_DEVICE, "long pass could not launch");
+          launches += kk;
+          CKLAUNCH();
+        }
+        if (joined.armed) {
+          const int rc = joined.join();
+          if (rc != SWIFT_OK) return rc;
         }
       }
     }

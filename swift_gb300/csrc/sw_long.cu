@@ -186,10 +186,14 @@ __global__ void __launch_bounds__(kLT, 2) sw_long_kernel(LongArgs a) {
     return acc;
   };
   const int steps = R + 31;                          // a warp's wavefront
-  const int n_stages = 2 * (kLW - 1) + (steps + kStage - 1) / kStage;
+  // warps whose rows all lie past the query compute nothing (their lanes'
+  // rows are out of the maximum, and the walk never reads them); the stage
+  // count follows the last warp that computes
+  const int act = min(kLW, (Q + 32 * RPL - 1) / (32 * RPL));
+  const int n_stages = 2 * (act - 1) + (steps + kStage - 1) / kStage;
   for (int stage = 0; stage < n_stages; ++stage) {
     const int s_lo = (stage - 2 * warp) * kStage;
-    if (s_lo >= 0 && s_lo < steps) {
+    if (warp < act && s_lo >= 0 && s_lo < steps) {
 #pragma unroll 1
       for (int s0 = s_lo; s0 < s_lo + kStage; s0 += 4) {
         uint4 v;
