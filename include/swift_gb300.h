@@ -55,6 +55,11 @@ typedef struct {
   int32_t qry_len;       /* -s; <= 0: length of the first read             */
   int64_t device_mem;    /* bytes used to size Phase-2 batches the way the
                             reference does from its device; 0: this GPU's  */
+  int32_t out_format;    /* -f: 1 SAM records of every alignment
+                            (printOutputSam, src/output.cu:98-130); any
+                            other value the default record of the best one
+                            per read (printOutput, src/output.cu:154-201)  */
+  int32_t reserved;      /* 0                                              */
 } swift_params;
 
 /* One Phase-1 record (one line of the reference's match file,

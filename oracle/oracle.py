@@ -31,6 +31,7 @@ class Params(C.Structure):
         ("qry_len", C.c_int),
         ("device_mem", C.c_longlong),
         ("threads", C.c_int),
+        ("out_format", C.c_int),
     ]
 
 
@@ -55,7 +56,7 @@ class Aln(C.Structure):
 
 
 def default_params(**kw) -> Params:
-    p = Params(12, 1000, 3, 2, -1, -10, -1, 0, 0, os.cpu_count() or 1)
+    p = Params(12, 1000, 3, 2, -1, -10, -1, 0, 0, os.cpu_count() or 1, 0)
     for k, v in kw.items():
         setattr(p, k, v)
     return p

@@ -34,6 +34,8 @@ def lib():
         L.ref_pipeline.argtypes = [C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p,
                                    C.c_longlong, i, i, f, f, f, f]
         L.ref_pipeline.restype = C.c_long
+        L.ref_pipeline_fmt.argtypes = L.ref_pipeline.argtypes + [i]
+        L.ref_pipeline_fmt.restype = C.c_long
         _lib = L
     return _lib
 
@@ -97,10 +99,11 @@ def map_query(seq: bytes, rev: bytes, is_rev: int, max_hits: int = 3):
 
 
 def pipeline(ref: bytes, reads: bytes, device_mem: int, seed_len=12, thres=1000,
-             m=2, x=-1, o=-10, e=-1) -> bytes:
+             m=2, x=-1, o=-10, e=-1, out_format=0) -> bytes:
+    """The reference's pipeline file to file; out_format 1: SAM records."""
     rp, qp, op, mp = (_tmp(n) for n in ("p_ref.fa", "p_reads.fa", "p_out.txt", "p_match.txt"))
     open(rp, "wb").write(ref)
     open(qp, "wb").write(reads)
-    lib().ref_pipeline(rp.encode(), qp.encode(), op.encode(), mp.encode(), device_mem,
-                       seed_len, thres, m, x, o, e)
+    lib().ref_pipeline_fmt(rp.encode(), qp.encode(), op.encode(), mp.encode(), device_mem,
+                           seed_len, thres, m, x, o, e, out_format)
     return open(op, "rb").read()

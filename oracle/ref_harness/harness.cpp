@@ -219,11 +219,13 @@ static void choose_best(char *names, int name_len, float *score, int size) {
 
 /* The SSAHA -> GPU Smith-Waterman -> best alignment pipeline with the
  * reference's functions, file to file.  device_mem sizes the Phase-2
- * batches as the reference does from its GPU.  Returns the number of
- * match records. */
-long ref_pipeline(const char *ref_file, const char *qry_file, const char *out_file,
-                  const char *match_file, long long device_mem, int seed_len, int thres,
-                  float m, float x, float o, float e) {
+ * batches as the reference does from its GPU; out_format 1 prints every
+ * record with printOutputSam instead of the best ones with printOutput
+ * (the branch of src/align.cu:756-768).  Returns the number of match
+ * records. */
+long ref_pipeline_fmt(const char *ref_file, const char *qry_file, const char *out_file,
+                      const char *match_file, long long device_mem, int seed_len, int thres,
+                      float m, float x, float o, float e, int out_format) {
   preprocessCreate();
   int num_qrs = getSeqCount((char *)qry_file);
   int qry_len = getSeqSize((char *)qry_file);
@@ -304,9 +306,14 @@ long ref_pipeline(const char *ref_file, const char *qry_file, const char *out_fi
                         en.data(), ln.data(), rcons.data(), qcons.data()};
     const int T = Q + 1 > R ? Q + 1 : R;
     for (long j = 0; j < cnt; ++j) run_block(T, (int)j);
-    choose_best(qname.data(), MAX_SEQ_NAME_LENGTH, score.data(), (int)cnt);
-    printOutput((int)cnt, qname.data(), rname.data(), score.data(), dist.data(), st.data(),
-                en.data(), ln.data(), comb, qcons.data(), rcons.data(), of);
+    if (out_format == SAM_OUTPUT_FORMAT) {
+      printOutputSam((int)cnt, qname.data(), rname.data(), score.data(), st.data(), en.data(),
+                     ln.data(), comb, qcons.data(), rcons.data(), of);
+    } else {
+      choose_best(qname.data(), MAX_SEQ_NAME_LENGTH, score.data(), (int)cnt);
+      printOutput((int)cnt, qname.data(), rname.data(), score.data(), dist.data(), st.data(),
+                  en.data(), ln.data(), comb, qcons.data(), rcons.data(), of);
+    }
   }
   fclose(mf);
   fclose(of);
@@ -315,6 +322,13 @@ long ref_pipeline(const char *ref_file, const char *qry_file, const char *out_fi
   for (int j = 0; j < nt; ++j) qryDelete(slot[j]);
   refMapFree();
   return num_matches;
+}
+
+long ref_pipeline(const char *ref_file, const char *qry_file, const char *out_file,
+                  const char *match_file, long long device_mem, int seed_len, int thres,
+                  float m, float x, float o, float e) {
+  return ref_pipeline_fmt(ref_file, qry_file, out_file, match_file, device_mem, seed_len, thres,
+                          m, x, o, e, DEFAULT_OUTPUT_FORMAT);
 }
 
 }  // extern "C"

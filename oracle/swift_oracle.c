@@ -841,6 +841,39 @@ static void so_print_record(so_sb *sb, const so_pair *x) {
   so_sb_put(sb, "\n", 1);
 }
 
+/* printCigar (src/output.cu:33-81): runs over the consensus from its last
+ * byte to its first; '-' in the reference consensus is D, else '-' in the
+ * query consensus is I, else M. */
+static void so_print_cigar(so_sb *sb, const char *qc, const char *rc, int len) {
+  int run = 0;
+  char op = ' ', buf[16];
+  for (int z = len - 1; z >= 0; --z) {
+    char c = rc[z] == '-' ? 'D' : qc[z] == '-' ? 'I' : 'M';
+    if (run > 0 && c != op) {
+      int n = snprintf(buf, sizeof(buf), "%d%c", run, op);
+      so_sb_put(sb, buf, (size_t)n);
+      run = 0;
+    }
+    op = c;
+    ++run;
+  }
+  if (run > 0) {
+    int n = snprintf(buf, sizeof(buf), "%d%c", run, op);
+    so_sb_put(sb, buf, (size_t)n);
+  }
+}
+
+/* printOutputSam (src/output.cu:98-130): one line per record, window start */
+static void so_print_sam(so_sb *sb, const so_pair *x) {
+  char hdr[512];
+  int hn = snprintf(hdr, sizeof(hdr), "%s\t*\t%s\t%d\t255\t", x->qname, x->rname, x->a.start);
+  so_sb_put(sb, hdr, (size_t)hn);
+  so_print_cigar(sb, x->qc, x->rc, x->a.len);
+  so_sb_put(sb, "\t*\t0\t0\t", 7);
+  for (int z = x->a.len - 1; z >= 0; --z) so_sb_put(sb, &x->qc[z], 1);
+  so_sb_put(sb, "\t*\n", 3);
+}
+
 struct so_session {
   so_ref r;
   so_index *ix;
@@ -954,6 +987,13 @@ int so_session_align(so_session *ss, const char *reads, size_t reads_len,
     for (int t = 0; t < threads; ++t) pthread_join(th[t], NULL);
     free(th);
     pthread_mutex_destroy(&jb.mu);
+    if (p->out_format == 1) {  /* SAM: every record, no selection (src/align.cu:756-761) */
+      for (long j = 0; j < cnt; ++j) so_print_sam(&sb, &pp[j]);
+      free(pp);
+      free(cons);
+      done += cnt;
+      continue;
+    }
     /* chooseBestAlignment over this batch (src/align.cu:844-905) */
     long start = 0;
     while (start < cnt) {

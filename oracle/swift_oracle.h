@@ -32,6 +32,8 @@ typedef struct {
   long long device_mem;/* device bytes that size the Phase-2 batches the way
                         getNumQueriesPerIteration does; <= 0: one batch */
   int threads;       /* worker threads (>= 1)                                */
+  int out_format;    /* -f: 1 SAM (printOutputSam, src/output.cu:98-130,
+                        every record); other values printOutput           */
 } so_params;
 
 typedef struct {

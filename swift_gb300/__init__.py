@@ -41,6 +41,7 @@ class Params(C.Structure):
         ("seed_len", C.c_int32), ("ignore_thres", C.c_int32), ("max_hits", C.c_int32),
         ("match", C.c_int32), ("mismatch", C.c_int32), ("gap_open", C.c_int32),
         ("gap_ext", C.c_int32), ("qry_len", C.c_int32), ("device_mem", C.c_int64),
+        ("out_format", C.c_int32), ("reserved", C.c_int32),
     ]
 
 

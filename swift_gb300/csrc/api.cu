@@ -502,6 +502,8 @@ void swift_params_default(swift_params* p) {
   p->gap_ext = -1;
   p->qry_len = 0;
   p->device_mem = 0;
+  p->out_format = 0;
+  p->reserved = 0;
 }
 
 int swift_ctx_create(int device, void* stream, swift_ctx** out) {
@@ -1506,7 +1508,9 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
   int bias = 0;
   const bool fast_ok =
       ctx->sw_path != 1 && fast_params_ok(Q, kWin, p->match, p->mismatch, p->gap_open, p->gap_ext, &bias);
-  const bool bounded = fast_ok && ctx->sw_path == 0;
+  // SAM output prints every record: no selection, every pair traced
+  const bool sam = p->out_format == 1;
+  const bool bounded = fast_ok && ctx->sw_path == 0 && !sam;
   // counters: 0 packed-path pairs, 1 generic pairs, 2 trace list,
   // 3 exact-score list, 4 second trace list, 5 printed records
   // counters 8.. : histogram and fill of the early-stop sort (two uses)
@@ -1567,7 +1571,7 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
   fa2.ub = ub;
   fa2.suf = suf;
   CK(cudaEventRecord(ctx->ev[7], st));
-  if (fast_ok && nproc > 0) {
+  if (fast_ok && nproc > 0 && !sam) {
     fa2.list = fast_list;
     fa2.count = cnt;
     launches += bounded ? launch_sw_bound(st, fa2, nproc) : launch_sw_score(st, fa2, nproc);
@@ -1647,6 +1651,17 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
     launches += 2;
     return SWIFT_OK;
   };
+  if (sam) {
+    // every record is printed: trace every packed-path pair (the trace pass
+    // scores it as well)
+    CK(cudaEventRecord(ctx->ev[6], st));
+    if (fast_ok && nproc > 0) {
+      CK(cudaMemcpyAsync(h_cnt, cnt, sizeof(h_cnt), cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+      rc = trace_list(fast_list, cnt, h_cnt[0]);
+      if (rc != SWIFT_OK) return rc;
+    }
+  }
   if (bounded && nproc > 0) {
     // candidates: traced first, then pairs their scores cannot rule out get
     // exact scores
@@ -1676,11 +1691,13 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
     launches += launch_sw_score(st, fa2, ex_max);
     CKLAUNCH();
   }
-  launch_select(st, fa);
-  CKLAUNCH();
-  launches += nproc > 0 ? 1 : 0;
-  if (!bounded) CK(cudaEventRecord(ctx->ev[6], st));
-  if (nproc > 0) {
+  if (!sam) {
+    launch_select(st, fa);
+    CKLAUNCH();
+    launches += nproc > 0 ? 1 : 0;
+  }
+  if (!bounded && !sam) CK(cudaEventRecord(ctx->ev[6], st));
+  if (nproc > 0 && !sam) {
     // printed packed-path pairs not traced yet
     int32_t* list2 = bounded ? gen_list : tb_list;  // generic list no longer needed
     traceback_list_kernel<<<(unsigned)((nproc + 255) / 256), 256, 0, st>>>(
@@ -1694,7 +1711,10 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
     if (bounded) pruned = std::max<int64_t>(h_cnt[0] - h_cnt[2] - h_cnt[3], 0);
   }
   CK(cudaEventRecord(ctx->ev[4], st));
-  launch_format_sizes(st, fa);
+  if (sam)
+    launch_sam_sizes(st, fa);
+  else
+    launch_format_sizes(st, fa);
   CKLAUNCH();
   int scan_k = exclusive_scan_u64(st, bytes, offs, nproc, tmp, tot_d);
   CKLAUNCH();
@@ -1710,7 +1730,10 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
     ctx->text_cap = cap;
   }
   fa.text = ctx->d_text;
-  launch_format_write(st, fa);
+  if (sam)
+    launch_sam_write(st, fa);
+  else
+    launch_format_write(st, fa);
   CKLAUNCH();
   CK(cudaEventRecord(ctx->ev[5], st));
   CK(cudaEventSynchronize(ctx->ev[5]));
@@ -1740,9 +1763,9 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
     s.cells = nproc * (int64_t)Q * kWin;
     s.out_bytes = (int64_t)total;
     s.seed_overflow_strands = so.overflow;
-    s.printed = h_cnt[5];
+    s.printed = sam ? nproc : h_cnt[5];
     s.sw_generic_pairs = h_cnt[1];
-    s.traced_pairs = h_cnt[2] + h_cnt[4];
+    s.traced_pairs = sam ? h_cnt[0] : h_cnt[2] + h_cnt[4];
     s.bound_pruned = pruned;
     s.retraced_pairs = bounded ? h_cnt[4] : 0;
     // build_pairs + the Smith-Waterman passes and select (launches) +

@@ -41,7 +41,7 @@ int main(int argc, char** argv) {
   const char *q = nullptr, *q2 = nullptr, *r = nullptr, *o = nullptr;
   swift_params p;
   swift_params_default(&p);
-  int fmt = 0, cpu = 0;
+  int cpu = 0;
   if (argc == 1) {
     printf("%s\n", usage_text());
     return 0;
@@ -61,7 +61,7 @@ int main(int argc, char** argv) {
     else if (!strcmp(a, "-M")) p.mismatch = atoi(take());
     else if (!strcmp(a, "-O")) p.gap_open = atoi(take());
     else if (!strcmp(a, "-E")) p.gap_ext = atoi(take());
-    else if (!strcmp(a, "-f")) fmt = atoi(take());
+    else if (!strcmp(a, "-f")) p.out_format = atoi(take());
     else if (!strcmp(a, "-t")) p.ignore_thres = atoi(take());
     else if (!strcmp(a, "-l")) p.seed_len = atoi(take());
     else if (!strcmp(a, "-cpu")) cpu = 1;
@@ -77,9 +77,9 @@ int main(int argc, char** argv) {
     printf("%s\n", usage_text());
     return 0;
   }
-  if (q2 || fmt != 0 || cpu) {
+  if (q2 || cpu) {
     fprintf(stderr, "swift: %s is not supported by this build\n",
-            q2 ? "paired-end alignment (-q2)" : fmt != 0 ? "SAM output (-f 1)" : "-cpu");
+            q2 ? "paired-end alignment (-q2)" : "-cpu");
     return 2;
   }
   swift_ctx* ctx = nullptr;

@@ -356,5 +356,8 @@ void launch_candidates(cudaStream_t st, const FormatArgs& a, int32_t* list, int3
 void launch_prune(cudaStream_t st, const FormatArgs& a, DevAln* aln, int32_t* list, int32_t* cnt);
 void launch_format_sizes(cudaStream_t st, const FormatArgs& a);
 void launch_format_write(cudaStream_t st, const FormatArgs& a);
+// SAM output: every record, sizes then text (keep is not read)
+void launch_sam_sizes(cudaStream_t st, const FormatArgs& a);
+void launch_sam_write(cudaStream_t st, const FormatArgs& a);
 
 }  // namespace swift

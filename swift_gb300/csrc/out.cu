@@ -7,7 +7,8 @@
 // group; the group keeps its first record with the maximum score (maximum
 // starting from 0.0 with strict comparison) and drops the others.
 //
-// Formatting restates printOutput (src/output.cu:154-201):
+// Formatting restates printOutput (src/output.cu:154-201), or for SAM output
+// printOutputSam (src/output.cu:98-130, below):
 //   "\n****************************************\n"
 //   "Qry: %s | Ref: %s | Score: %.1f | AlignStart: %d | AlignEnd: %d | "
 //   "AlignLength: %d\n"
@@ -248,7 +249,115 @@ __global__ void __launch_bounds__(kFmtWarps * 32) format_write_kernel(FormatArgs
   }
 }
 
+// SAM records (printOutputSam, src/output.cu:98-130): every record of the
+// batch, no best selection, one line each:
+//   qname "\t*\t" rname "\t" alignStart "\t255\t" CIGAR "\t*\t0\t0\t"
+//   reversed query consensus "\t*\n"
+// alignStart is the window coordinate (no reference distance added).  The
+// CIGAR (printCigar, src/output.cu:33-81) walks the consensus from its last
+// byte to its first: '-' in the reference consensus is D, else '-' in the
+// query consensus is I, else M; each run prints as its length and letter.
+__device__ __forceinline__ char cigar_op(char r, char q) {
+  return r == '-' ? 'D' : q == '-' ? 'I' : 'M';
+}
+
+__device__ int cigar_bytes(const char* rc, const char* qc, int L) {
+  int n = 0, run = 0;
+  char op = ' ';
+  for (int z = L - 1; z >= 0; --z) {
+    const char c = cigar_op(rc[z], qc[z]);
+    if (run > 0 && c != op) {
+      n += ndigits(run) + 1;
+      run = 0;
+    }
+    op = c;
+    ++run;
+  }
+  if (run > 0) n += ndigits(run) + 1;
+  return n;
+}
+
+__global__ void sam_sizes_kernel(FormatArgs a) {
+  int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= a.n) return;
+  const DevPair p = a.pairs[j];
+  const DevAln al = a.aln[j];
+  const int L = al.len > 0 ? al.len : 0;
+  uint64_t n = qname_len(a, p) + 3 + a.recs[p.ref_idx].name_len + 1 + ndigits(al.start) + 5;
+  n += cigar_bytes(a.rcons + j * a.cons_stride, a.qcons + j * a.cons_stride, L);
+  n += 7 + L + 3;
+  a.bytes[j] = n;
+}
+
+// header + CIGAR: names (<= 50 bytes each), 11 digits, 9 literal bytes, and
+// at most 2 bytes of CIGAR per consensus byte (<= 556 of them)
+constexpr int kSamHead = 1280;
+
+__global__ void __launch_bounds__(kFmtWarps * 32) sam_write_kernel(FormatArgs a) {
+  __shared__ char head_all[kFmtWarps][kSamHead];
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t j = (int64_t)blockIdx.x * kFmtWarps + wib;
+  if (j >= a.n) return;
+  const DevPair p = a.pairs[j];
+  const DevAln al = a.aln[j];
+  const int L = al.len > 0 ? al.len : 0;
+  const char* rc = a.rcons + j * a.cons_stride;
+  const char* qc = a.qcons + j * a.cons_stride;
+  char* head = head_all[wib];
+  int hn = 0;
+  if (lane == 0) {
+    char* o = head;
+    const int ql = qname_len(a, p);
+    for (int i = 0; i < ql; ++i) *o++ = qname_at(a, p, i);
+    o = put_str(o, "\t*\t");
+    const DevRecord& rec = a.recs[p.ref_idx];
+    for (uint32_t i = 0; i < rec.name_len; ++i) *o++ = rec.name[i];
+    *o++ = '\t';
+    o = put_int(o, al.start);
+    o = put_str(o, "\t255\t");
+    int run = 0;
+    char op = ' ';
+    for (int z = L - 1; z >= 0; --z) {
+      const char c = cigar_op(rc[z], qc[z]);
+      if (run > 0 && c != op) {
+        o = put_int(o, run);
+        *o++ = op;
+        run = 0;
+      }
+      op = c;
+      ++run;
+    }
+    if (run > 0) {
+      o = put_int(o, run);
+      *o++ = op;
+    }
+    o = put_str(o, "\t*\t0\t0\t");
+    hn = (int)(o - head);
+  }
+  hn = __shfl_sync(0xffffffffu, hn, 0);
+  __syncwarp();
+  char* out = a.text + a.offs[j];
+  for (int i = lane; i < hn; i += 32) out[i] = head[i];
+  out += hn;
+  for (int z = lane; z < L; z += 32) out[z] = qc[L - 1 - z];
+  if (lane == 0) {
+    out[L] = '\t';
+    out[L + 1] = '*';
+    out[L + 2] = '\n';
+  }
+}
+
 }  // namespace
+
+void launch_sam_sizes(cudaStream_t st, const FormatArgs& a) {
+  if (a.n <= 0) return;
+  sam_sizes_kernel<<<(unsigned)((a.n + 255) / 256), 256, 0, st>>>(a);
+}
+
+void launch_sam_write(cudaStream_t st, const FormatArgs& a) {
+  if (a.n <= 0) return;
+  sam_write_kernel<<<(unsigned)((a.n + kFmtWarps - 1) / kFmtWarps), kFmtWarps * 32, 0, st>>>(a);
+}
 
 void launch_select(cudaStream_t st, const FormatArgs& a) {
   if (a.n <= 0) return;

@@ -26,6 +26,7 @@ sys.path.insert(0, ROOT)
 from oracle import ref as R  # noqa: E402
 
 DEVICE_MEM = 288_000_000_000  # bytes; sizes Phase-2 batches as on a GB300
+SAM_SMALL_MEM = 100_000_000 + 24 * 1220  # Phase-2 batches of 24 records at Q = 100
 
 
 def mutate(rng, s, p_sub=0.05, p_indel=0.02):
@@ -114,7 +115,12 @@ def main():
     open(os.path.join(HERE, "pipeline_reads.fa"), "wb").write(reads)
     open(os.path.join(HERE, "pipeline_out.txt"), "wb").write(out)
     json.dump(dict(device_mem=DEVICE_MEM), open(os.path.join(HERE, "pipeline_meta.json"), "w"))
-    print("wrote fixtures:", len(out), "bytes of pipeline output")
+    # SAM records (-f 1) of the same inputs (every record printed, so the
+    # Phase-2 batch size does not change them)
+    sam = R.pipeline(ref, reads, DEVICE_MEM, out_format=1)
+    assert R.pipeline(ref, reads, SAM_SMALL_MEM, out_format=1) == sam
+    open(os.path.join(HERE, "pipeline_out_sam.txt"), "wb").write(sam)
+    print("wrote fixtures:", len(out), "bytes of pipeline output,", len(sam), "of SAM output")
 
 
 if __name__ == "__main__":

@@ -46,6 +46,27 @@ def test_oracle_pipeline(oracle):
     assert got == load("pipeline_out.txt", "rb")
 
 
+def test_oracle_pipeline_sam(oracle):
+    # the reference's printOutputSam records of the same inputs
+    meta = load("pipeline_meta.json")
+    got = oracle.align(load("pipeline_ref.fa", "rb"), load("pipeline_reads.fa", "rb"),
+                       oracle.default_params(device_mem=meta["device_mem"], out_format=1))
+    assert got == load("pipeline_out_sam.txt", "rb")
+
+
+@pytest.mark.gpu
+def test_gpu_pipeline_sam():
+    import swift_gb300 as sg
+    meta = load("pipeline_meta.json")
+    ctx = sg.Context(0)
+    ix = ctx.index(load("pipeline_ref.fa", "rb"))
+    want = load("pipeline_out_sam.txt", "rb")
+    for dm in (meta["device_mem"], 100_000_000 + 24 * 1220):  # one batch; batches of 24
+        got = ctx.align(ix, load("pipeline_reads.fa", "rb"),
+                        sg.default_params(device_mem=dm, out_format=1))
+        assert got == want
+
+
 @pytest.mark.gpu
 def test_gpu_sw_pairs():
     import swift_gb300 as sg

@@ -465,3 +465,85 @@ def test_packed_path_query_lengths(ctx, oracle, sg, Q):
     got = ctx.align(ix, reads)
     want = oracle.align(ref, reads, oparams(ctx, oracle))
     assert got == want, first_diff(got, want)
+
+
+# ---------------------------------------------------------------------------
+# SAM output (-f 1): every record, CIGAR from the reversed consensus
+
+@pytest.mark.parametrize("n_reads", [1, 17, 250])
+def test_sam_read_counts(ctx, oracle, sg, n_reads):
+    ref, reads = small_case(n_reads=n_reads, seed=140 + n_reads)
+    ix = ctx.index(ref)
+    got, st = ctx.align(ix, reads, sg.default_params(out_format=1), stats=True)
+    want = oracle.align(ref, reads, oparams(ctx, oracle, out_format=1))
+    assert got == want, first_diff(got, want)
+    assert st["printed"] == st["records"] == got.count(b"\n")
+
+
+def test_sam_messy_inputs_and_paths(ctx, oracle, sg):
+    # lowercase and N in the reference, random reads with N (generic kernel
+    # pairs), both strands; the packed and generic paths print the same SAM
+    fa = messy_reference(seed=18)
+    seqs, cur = [], None
+    for line in fa.split(b"\n"):
+        if line.startswith(b">"):
+            cur = bytearray()
+            seqs.append(cur)
+        elif cur is not None:
+            cur += line
+    rng = random.Random(19)
+    parts = []
+    for i in range(400):
+        s = seqs[rng.randrange(len(seqs))]
+        a = rng.randrange(0, len(s) - 100)
+        r = bytes(s[a:a + 100])
+        if i % 3 == 1:
+            r = oracle.revcomp(r)
+        if i % 7 == 3:
+            r = bytes(rng.choice(b"ACGTN") for _ in range(100))
+        parts.append(b">read_%d\n%s\n" % (i, r))
+    reads = b"".join(parts)
+    ix = ctx.index(fa)
+    p = sg.default_params(out_format=1)
+    got, st = ctx.align(ix, reads, p, stats=True)
+    want = oracle.align(fa, reads, oparams(ctx, oracle, out_format=1))
+    assert got == want, first_diff(got, want)
+    assert st["sw_generic_pairs"] > 0 and st["traced_pairs"] > 0
+    ctx.set_sw_path(1)
+    try:
+        assert ctx.align(ix, reads, p) == want
+    finally:
+        ctx.set_sw_path(0)
+
+
+def test_sam_scoring_and_query_lengths(ctx, oracle, sg):
+    from swift_gb300 import synth
+    for Q, kw in [(36, dict(match=3, mismatch=-2, gap_open=-6, gap_ext=-2)), (150, {}),
+                  (199, dict(max_hits=1))]:
+        names, seqs = synth.make_reference(80_000, 2, sigma=0.3, seed=500 + Q)
+        ref = synth.fasta_bytes(names, seqs)
+        rn, rs, _ = synth.make_reads(seqs, 300, Q, 0.03, 0.01, 0.05, seed=501 + Q)
+        reads = synth.reads_fasta(rn, rs)
+        ix = ctx.index(ref)
+        got = ctx.align(ix, reads, sg.default_params(out_format=1, **kw))
+        want = oracle.align(ref, reads, oparams(ctx, oracle, out_format=1, **kw))
+        assert got == want, (Q, kw, first_diff(got, want))
+
+
+def test_sam_cli(ctx, oracle, sg):
+    ref, reads = small_case(n_reads=120, seed=57)
+    with tempfile.TemporaryDirectory() as d:
+        rp, qp, op = (os.path.join(d, f) for f in ("ref.fa", "reads.fa", "out.sam"))
+        open(rp, "wb").write(ref)
+        open(qp, "wb").write(reads)
+        r = subprocess.run([sg.CLI_PATH, "-q", qp, "-r", rp, "-o", op, "-f", "1"],
+                           capture_output=True)
+        assert r.returncode == 0, r.stderr
+        got = open(op, "rb").read()
+        # any other -f value prints the default records, as the reference does
+        r = subprocess.run([sg.CLI_PATH, "-q", qp, "-r", rp, "-o", op, "-f", "2"],
+                           capture_output=True)
+        assert r.returncode == 0, r.stderr
+        got2 = open(op, "rb").read()
+    assert got == oracle.align(ref, reads, oparams(ctx, oracle, out_format=1))
+    assert got2 == oracle.align(ref, reads, oparams(ctx, oracle))

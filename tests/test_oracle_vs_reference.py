@@ -116,3 +116,29 @@ def test_pipeline_random(oracle):
     want = R.pipeline(ref, reads, dm)
     got = oracle.align(ref, reads, oracle.default_params(device_mem=dm))
     assert got == want
+
+
+def test_pipeline_sam_random(oracle):
+    # SAM records (-f 1): every record of every batch, CIGAR from the
+    # reversed consensus; small batches so the stale repeats and batch ends
+    # are in the output, reads with indels so D and I runs appear
+    rng = random.Random(10)
+    seqs = [rand_seq(rng, n) for n in (6000, 4000, 3000)]
+    ref = b"".join(b">chr%d\n" % i + b"\n".join(s[j:j + 60] for j in range(0, len(s), 60)) + b"\n"
+                   for i, s in enumerate(seqs))
+    reads = []
+    for i in range(29):
+        s = seqs[rng.randrange(3)]
+        a = rng.randrange(0, len(s) - 110)
+        r = mutate(rng, s[a:a + 110], 0.03, 0.02)[:90].ljust(90, b"C")
+        if i % 3 == 1:
+            r = oracle.revcomp(r)
+        if i % 7 == 3:
+            r = r[:40] + b"N" + r[41:]
+        reads.append(b">read_%d\n%s\n" % (i, r))
+    reads = b"".join(reads)
+    for dm in (288_000_000_000, 100_000_000 + 17 * 1000):
+        want = R.pipeline(ref, reads, dm, out_format=1)
+        got = oracle.align(ref, reads, oracle.default_params(device_mem=dm, out_format=1))
+        assert got == want
+        assert want.count(b"\n") > 29 and b"D" in want and b"I" in want
