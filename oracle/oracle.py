@@ -32,6 +32,7 @@ class Params(C.Structure):
         ("device_mem", C.c_longlong),
         ("threads", C.c_int),
         ("out_format", C.c_int),
+        ("seeder", C.c_int),
     ]
 
 
@@ -56,7 +57,7 @@ class Aln(C.Structure):
 
 
 def default_params(**kw) -> Params:
-    p = Params(12, 1000, 3, 2, -1, -10, -1, 0, 0, os.cpu_count() or 1, 0)
+    p = Params(12, 1000, 3, 2, -1, -10, -1, 0, 0, os.cpu_count() or 1, 0, 0)
     for k, v in kw.items():
         setattr(p, k, v)
     return p
@@ -95,6 +96,8 @@ def lib():
                                 C.POINTER(Params), C.POINTER(C.c_void_p),
                                 C.POINTER(C.c_int), C.c_char_p, C.c_size_t]
         L.so_free.argtypes = [C.c_void_p]
+        L.so_lt13_map.argtypes = [C.c_char_p, C.c_size_t, C.c_int, C.c_int, C.c_char_p, C.c_int,
+                                  C.c_void_p, C.c_void_p, C.c_char_p, C.c_size_t]
         L.so_session_create.argtypes = [C.c_char_p, C.c_size_t, C.POINTER(Params),
                                         C.POINTER(C.c_void_p), C.c_char_p, C.c_size_t]
         L.so_session_align.argtypes = [C.c_void_p, C.c_char_p, C.c_size_t,
@@ -234,6 +237,17 @@ def phase1(ref: bytes, reads: bytes, params: Params | None = None):
            for i in range(n.value)]
     lib().so_free(out)
     return res
+
+
+def lt13_map(ref: bytes, seq: bytes, k: int = 12, thres: int = 1000):
+    """lt13 seed-and-extend hits of one query strand: [(ref_idx, ref_pos)]."""
+    ri = (C.c_int32 * 3)()
+    rp = (C.c_int32 * 3)()
+    err = C.create_string_buffer(512)
+    n = lib().so_lt13_map(ref, len(ref), k, thres, seq, len(seq), ri, rp, err, 512)
+    if n < 0:
+        raise OracleError(err.value.decode())
+    return [(ri[i], rp[i]) for i in range(n)]
 
 
 class Session:

@@ -34,7 +34,7 @@ def lib():
         L.ref_pipeline.argtypes = [C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p,
                                    C.c_longlong, i, i, f, f, f, f]
         L.ref_pipeline.restype = C.c_long
-        L.ref_pipeline_fmt.argtypes = L.ref_pipeline.argtypes + [i]
+        L.ref_pipeline_fmt.argtypes = L.ref_pipeline.argtypes + [i, i]
         L.ref_pipeline_fmt.restype = C.c_long
         _lib = L
     return _lib
@@ -99,11 +99,38 @@ def map_query(seq: bytes, rev: bytes, is_rev: int, max_hits: int = 3):
 
 
 def pipeline(ref: bytes, reads: bytes, device_mem: int, seed_len=12, thres=1000,
-             m=2, x=-1, o=-10, e=-1, out_format=0) -> bytes:
-    """The reference's pipeline file to file; out_format 1: SAM records."""
+             m=2, x=-1, o=-10, e=-1, out_format=0, seeder=0) -> bytes:
+    """The reference's pipeline file to file; out_format 1: SAM records;
+    seeder 1: the lt13 seed-and-extend Phase 1 of search2Queries."""
+    return pipeline_with_matches(ref, reads, device_mem, seed_len, thres, m, x, o, e,
+                                 out_format, seeder)[0]
+
+
+def _pipeline_in_process(rp, qp, op, mp, device_mem, seed_len, thres, m, x, o, e, out_format,
+                         seeder):
+    lib().ref_pipeline_fmt(rp.encode(), qp.encode(), op.encode(), mp.encode(), device_mem,
+                           seed_len, thres, m, x, o, e, out_format, seeder)
+
+
+def pipeline_with_matches(ref: bytes, reads: bytes, device_mem: int, seed_len=12, thres=1000,
+                          m=2, x=-1, o=-10, e=-1, out_format=0, seeder=0):
+    """(output bytes, Phase-1 records [(name, strand, ref_idx, shift, ref_pos)])."""
     rp, qp, op, mp = (_tmp(n) for n in ("p_ref.fa", "p_reads.fa", "p_out.txt", "p_match.txt"))
     open(rp, "wb").write(ref)
     open(qp, "wb").write(reads)
-    lib().ref_pipeline_fmt(rp.encode(), qp.encode(), op.encode(), mp.encode(), device_mem,
-                           seed_len, thres, m, x, o, e, out_format)
-    return open(op, "rb").read()
+    args = (rp, qp, op, mp, device_mem, seed_len, thres, m, x, o, e, out_format, seeder)
+    if seeder == 1:
+        # lookupTable13Create keeps _maxRefPosComposite in a file-static that
+        # it never resets: one reference per process, as in the reference
+        import subprocess
+        import sys
+        code = ("import sys; sys.path.insert(0, %r); from oracle import ref as R; "
+                "R._pipeline_in_process(*%r)" % (os.path.dirname(HERE), args))
+        subprocess.run([sys.executable, "-c", code], check=True, capture_output=True)
+    else:
+        _pipeline_in_process(*args)
+    recs = []
+    for line in open(mp, "rb").read().splitlines():
+        f = line.split(b"\t")
+        recs.append((f[0].decode(), int(f[1]), int(f[2]), int(f[3]), int(f[4])))
+    return open(op, "rb").read(), recs

@@ -11,9 +11,14 @@
  *     run sequentially with mapHits6's random picks pinned to the first ones;
  *   - the per-batch loop of alignQueries3 (src/align.cu:574-808) and the
  *     batch sizing of getNumQueriesPerIteration (src/align.cu:2767-2793);
- *   - chooseBestAlignment (src/align.cu:844-905) with the first maximum kept.
- * The GPU kernel smithWaterman (src/smithWaterman.cu:360-395) runs on the
- * CPU: one fiber per CUDA thread, __syncthreads() yields to the next fiber.
+ *   - chooseBestAlignment (src/align.cu:844-905) with the first maximum kept;
+ *   - the query loop of search2Queries (src/search2.cu:176-256) and its
+ *     printHeuristicMatches (src/search2.cu:339-377), both static there.
+ * The GPU kernels smithWaterman (src/smithWaterman.cu:360-395) and
+ * lookupTable13MapQry2_gpu (src/lookupTable13.cu:646-868) run on the CPU:
+ * one fiber per CUDA thread, __syncthreads() yields to the next fiber.
+ * lookupTable13MapQry2_gpu reads its block's shared random seed without
+ * setting it; the harness zeroes the block's shared variables first.
  */
 #include <math.h>
 #include <stdio.h>
@@ -25,6 +30,7 @@
 
 #include "common.h"
 #include "input.h"
+#include "lookupTable13.h"
 #include "lookupTable5.h"
 #include "mapHits6.h"
 #include "output.h"
@@ -45,14 +51,28 @@ void smithWaterman_cpu(float *HMatrix, int *rowBacktracker, int *colBacktracker,
 
 /* ---- shim runtime (declared in shim.h) ------------------------------- */
 struct ref_dim3 threadIdx, blockIdx, blockDim, gridDim;
-int arr_shr[1];
+/* dynamic shared memory of one block: lookupTable13MapQry2_gpu takes
+ * idealArrSize x 21 + 16 bytes (src/search2.cu:122-137), under 48 KB */
+int arr_shr[12800];
 
 cudaError_t cudaGetLastError(void) { return 0; }
 const char *cudaGetErrorString(cudaError_t) { return "no error"; }
-cudaError_t cudaMalloc(void **, size_t) { abort(); }
-cudaError_t cudaFree(void *) { abort(); }
-cudaError_t cudaMemcpy(void *, const void *, size_t, enum cudaMemcpyKind) { abort(); }
-cudaError_t cudaMemset(void *, int, size_t) { abort(); }
+cudaError_t cudaMalloc(void **p, size_t n) {
+  *p = calloc(n + 65536, 1);
+  return 0;
+}
+cudaError_t cudaFree(void *p) {
+  free(p);
+  return 0;
+}
+cudaError_t cudaMemcpy(void *d, const void *s, size_t n, enum cudaMemcpyKind) {
+  memcpy(d, s, n);
+  return 0;
+}
+cudaError_t cudaMemset(void *d, int v, size_t n) {
+  memset(d, v, n);
+  return 0;
+}
 
 static unsigned g_rand = 0;
 /* stands in for rand() in array.cu (arrGetRandomNums): 0, 1, 2, ... so the
@@ -79,10 +99,15 @@ struct KernelArgs {
 };
 static KernelArgs g_args;
 
-static void fiber_entry(int tid) {
+static void sw_body() {
   KernelArgs &a = g_args;
   smithWaterman(a.ref, a.R, a.qry, a.Q, a.m, a.x, a.o, a.e, a.score, a.start, a.end, a.len,
                 a.rcons, a.qcons, 1, 1);
+}
+static void (*g_body)() = sw_body;
+
+static void fiber_entry(int tid) {
+  g_body();
   g_done[tid] = 1;
 }
 
@@ -217,6 +242,79 @@ static void choose_best(char *names, int name_len, float *score, int size) {
   }
 }
 
+/* ---- lt13 seeding: search2Queries' loop, one CPU block per strand ---- */
+extern "C" char __start_ref13shr[], __stop_ref13shr[];
+
+struct L13Args {
+  int *keys, *vals, *ntup, *map;
+  char *qrs;
+  uchar *qlen;
+  int *qdist;
+  char *ri;
+  int *rp;
+  int k;
+};
+static L13Args g_l13;
+
+static void l13_body() {
+  L13Args &a = g_l13;
+  lookupTable13MapQry2_gpu(a.keys, a.vals, a.ntup, a.map, a.qrs, a.qlen, a.qdist,
+                           MAX_QRY_SEQ_LENGTH, a.ri, a.rp, 3, a.k, 0, 2304);
+}
+
+/* Writes the match file of search2Queries for the reads file: per read,
+ * forward then reverse-complement hits (reference index != -1), shift 0.
+ * Returns the number of records. */
+static long l13_phase1(const char *ref_file, const char *qry_file, FILE *mf, int seed_len,
+                       int thres) {
+  int total = 0;
+  lookupTable13Create(ref_file, seed_len, thres, &total);
+  int *keys, *vals, *ntup, *map, nk, nv, maxc;
+  lookupTable13CpyHashTableToGPU(&keys, &nk, &vals, &nv, &ntup, &map, &maxc);
+  lookupTable13CpyConstMemToGPU();
+  FILE *qf = fopen(qry_file, "r");
+  Query *q = qryCreate2();
+  std::vector<char> qrs(2 * MAX_QRY_SEQ_LENGTH + 64, 0);
+  uchar qlen[2];
+  int qdist[2] = {0, 0};
+  char ri[2 * 3];
+  int rp[2 * 3];
+  long n = 0;
+  while (qryGetNext2(qf, q) != NULL) {
+    strcpy(qrs.data(), q->seq);
+    qlen[0] = (uchar)q->length;
+    strcpy(qrs.data() + MAX_QRY_SEQ_LENGTH, q->revCompSeq);
+    qlen[1] = (uchar)q->length;
+    qdist[1] = qlen[0];
+    memset(ri, -1, sizeof(ri));
+    memset(rp, -1, sizeof(rp));
+    g_l13 = L13Args{keys, vals, ntup, map, qrs.data(), qlen, qdist, ri, rp, seed_len};
+    g_body = l13_body;
+    for (int b = 0; b < 2; ++b) {
+      memset(__start_ref13shr, 0, (size_t)(__stop_ref13shr - __start_ref13shr));
+      memset(arr_shr, 0, sizeof(arr_shr));
+      run_block(64, b);
+    }
+    g_body = sw_body;
+    for (int b = 0; b < 2; ++b)
+      for (int j = 0; j < 3; ++j) {
+        int kk = b * 3 + j;
+        if (ri[kk] != -1) {
+          fprintf(mf, "%s\t%d\t%d\t%d\t%d\t%lu\t%lu\n", q->name, b, ri[kk], 0, rp[kk],
+                  q->nameOffset, q->seqOffset);
+          ++n;
+        }
+      }
+  }
+  fclose(qf);
+  qryDelete(q);
+  cudaFree(keys);
+  cudaFree(vals);
+  cudaFree(ntup);
+  cudaFree(map);
+  return n;
+}
+
 /* The SSAHA -> GPU Smith-Waterman -> best alignment pipeline with the
  * reference's functions, file to file.  device_mem sizes the Phase-2
  * batches as the reference does from its GPU; out_format 1 prints every
@@ -225,36 +323,40 @@ static void choose_best(char *names, int name_len, float *score, int size) {
  * records. */
 long ref_pipeline_fmt(const char *ref_file, const char *qry_file, const char *out_file,
                       const char *match_file, long long device_mem, int seed_len, int thres,
-                      float m, float x, float o, float e, int out_format) {
+                      float m, float x, float o, float e, int out_format, int seeder) {
   preprocessCreate();
   int num_qrs = getSeqCount((char *)qry_file);
   int qry_len = getSeqSize((char *)qry_file);
   refMapCreate(ref_file);
-  int total = 0;
-  lookupTable5Create(ref_file, seed_len, MAX_NUM_HITS_SINGLE_END, thres, &total);
   FILE *mf = fopen(match_file, "w");
-  FILE *qf = fopen(qry_file, "r");
+  long num_matches = 0;
   const int nt = NUM_THREADS;
   Query *slot[NUM_THREADS];
   for (int j = 0; j < nt; ++j) slot[j] = qryCreate2();
-  char ri[MAX_NUM_HITS_SINGLE_END];
-  int sh[MAX_NUM_HITS_SINGLE_END], rp[MAX_NUM_HITS_SINGLE_END];
-  long num_matches = 0;
-  for (int i = 0; i < num_qrs; i += nt) {
-    for (int j = 0; j < nt; ++j) qryGetNext2(qf, slot[j]);
-    for (int j = 0; j < nt; ++j) {
-      for (int strand = 0; strand < 2; ++strand) {
-        g_rand = 0;
-        int n = lookupTable5MapQry(slot[j], slot[j]->length, strand, ri, sh, rp);
-        for (int h = 0; h < n; ++h)
-          fprintf(mf, "%s\t%d\t%d\t%d\t%d\t%lu\t%lu\n", slot[j]->name, strand, ri[h], sh[h], rp[h],
-                  slot[j]->nameOffset, slot[j]->seqOffset);
-        num_matches += n;
+  if (seeder == 1) {
+    num_matches = l13_phase1(ref_file, qry_file, mf, seed_len, thres);
+  } else {
+    int total = 0;
+    lookupTable5Create(ref_file, seed_len, MAX_NUM_HITS_SINGLE_END, thres, &total);
+    FILE *qf = fopen(qry_file, "r");
+    char ri[MAX_NUM_HITS_SINGLE_END];
+    int sh[MAX_NUM_HITS_SINGLE_END], rp[MAX_NUM_HITS_SINGLE_END];
+    for (int i = 0; i < num_qrs; i += nt) {
+      for (int j = 0; j < nt; ++j) qryGetNext2(qf, slot[j]);
+      for (int j = 0; j < nt; ++j) {
+        for (int strand = 0; strand < 2; ++strand) {
+          g_rand = 0;
+          int n = lookupTable5MapQry(slot[j], slot[j]->length, strand, ri, sh, rp);
+          for (int h = 0; h < n; ++h)
+            fprintf(mf, "%s\t%d\t%d\t%d\t%d\t%lu\t%lu\n", slot[j]->name, strand, ri[h], sh[h],
+                    rp[h], slot[j]->nameOffset, slot[j]->seqOffset);
+          num_matches += n;
+        }
       }
     }
+    fclose(qf);
   }
   fclose(mf);
-  fclose(qf);
   /* Phase 2 */
   const int R = REF_LENGTH, Q = qry_len, comb = R + Q + 2;
   long per_iter;
@@ -328,7 +430,7 @@ long ref_pipeline(const char *ref_file, const char *qry_file, const char *out_fi
                   const char *match_file, long long device_mem, int seed_len, int thres,
                   float m, float x, float o, float e) {
   return ref_pipeline_fmt(ref_file, qry_file, out_file, match_file, device_mem, seed_len, thres,
-                          m, x, o, e, DEFAULT_OUTPUT_FORMAT);
+                          m, x, o, e, DEFAULT_OUTPUT_FORMAT, 0);
 }
 
 }  // extern "C"

@@ -5,8 +5,16 @@
  * CUDA qualifiers become nothing (or 'static' for __shared__ inside the
  * Smith-Waterman kernel, so that one CPU "block" of fibers shares them);
  * threadIdx/blockIdx/blockDim are globals set by the fiber scheduler;
- * __syncthreads() yields to the next fiber.  CUDA runtime calls that the
- * harness never reaches are declared so the files compile; they abort.
+ * __syncthreads() yields to the next fiber.  Device memory is host memory:
+ * cudaMalloc returns zeroed memory with 64 KB of zeroed slack after it (so
+ * reads just past an allocation see 0), cudaMemcpy and cudaMemcpyToSymbol
+ * copy, cudaFree frees.
+ *
+ * REF_L13 (lookupTable13.cu): the block's __shared__ variables go to the
+ * section ref13shr, which the harness zeroes before every block, calloc
+ * leaves room for the one-past-the-end write of lookupTable13Create, and
+ * the file's __constant__ tables get names of their own (constant memory
+ * is per module in CUDA; lookupTable5.cu defines the same names).
  */
 #ifndef REF_SHIM_H_
 #define REF_SHIM_H_
@@ -27,7 +35,14 @@
 #define __device__
 #define __host__
 #define __constant__
-#ifdef REF_SHARED_STATIC
+#if defined(REF_L13)
+#define __shared__ static __attribute__((section("ref13shr")))
+static inline void *ref13_calloc(size_t n, size_t sz) { return calloc(n + 1024, sz); }
+#define calloc ref13_calloc
+/* __constant__ arrays are per module in CUDA; lookupTable5.cu has its own */
+#define hashCodes_gpu ref13_hashCodes_gpu
+#define powerVals_gpu ref13_powerVals_gpu
+#elif defined(REF_SHARED_STATIC)
 #define __shared__ static
 /* the kernel file defines its own toupper; keep libc's declaration apart */
 #define toupper ref_sw_toupper
@@ -46,6 +61,7 @@ extern "C" int ref_rand(void);
 static inline int max(int a, int b) { return a > b ? a : b; }
 static inline int min(int a, int b) { return a < b ? a : b; }
 static inline short max(short a, short b) { return a > b ? a : b; }
+static inline long long max(long long a, long long b) { return a > b ? a : b; }
 static inline short min(short a, short b) { return a < b ? a : b; }
 
 struct ref_dim3 {
@@ -69,8 +85,9 @@ cudaError_t cudaFree(void *);
 cudaError_t cudaMemcpy(void *, const void *, size_t, enum cudaMemcpyKind);
 cudaError_t cudaMemset(void *, int, size_t);
 template <class T>
-cudaError_t cudaMemcpyToSymbol(const T &, const void *, size_t, size_t = 0,
+cudaError_t cudaMemcpyToSymbol(const T &sym, const void *src, size_t n, size_t off = 0,
                                enum cudaMemcpyKind = cudaMemcpyHostToDevice) {
-  abort();
+  memcpy((char *)&sym + off, src, n);
+  return 0;
 }
 #endif

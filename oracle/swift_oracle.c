@@ -716,6 +716,13 @@ static int so_run_phase1(const so_index *ix, const so_reads *rd, int max_hits,
   return 0;
 }
 
+typedef struct so_lt13_s so_lt13;
+static int so_lt13_build(const so_ref *r, const so_index *ix, so_lt13 **out, char *err,
+                         size_t errlen);
+static void so_lt13_free(so_lt13 *t);
+static int so_run_phase1_lt13(const so_lt13 *t, const so_reads *rd, int threads,
+                              so_match **out, int *n_out);
+
 int so_phase1(const char *ref, size_t ref_len, const char *reads,
               size_t reads_len, const so_params *p, so_match **out, int *n_out,
               char *err, size_t errlen) {
@@ -726,12 +733,343 @@ int so_phase1(const char *ref, size_t ref_len, const char *reads,
   if (rc == 0) rc = so_index_from_ref(&r, p->seed_len, p->ignore_thres, &ix, err, errlen);
   if (rc == 0) rc = so_reads_parse(reads, reads_len, &rd, err, errlen);
   if (rc == 0) {
-    rc = so_run_phase1(ix, &rd, p->max_hits, p->threads, out, n_out);
+    if (p->seeder == 1) {
+      so_lt13 *t = NULL;
+      rc = so_lt13_build(&r, ix, &t, err, errlen);
+      if (rc == 0) rc = so_run_phase1_lt13(t, &rd, p->threads, out, n_out);
+      so_lt13_free(t);
+    } else {
+      rc = so_run_phase1(ix, &rd, p->max_hits, p->threads, out, n_out);
+    }
     free(rd.r);
   }
   so_index_free(ix);
   so_ref_free(&r);
   return rc;
+}
+
+/* ------------------------------------------------------------------ */
+/* lt13 seed-and-extend seeder: the Phase 1 of the reference CLI's GPU   */
+/* default (search2Queries, src/search2.cu:48-259), restated per query   */
+/* strand in the order the kernel's single block computes it.            */
+
+#define SO_L13_ARR 2304     /* idealArrSize at 48 KB of shared memory per
+                               block (src/search2.cu:122-137)             */
+#define SO_L13_THREADS 64   /* dimBlock.x (src/search2.cu:151)            */
+#define SO_L13_ITERS (SO_L13_ARR / SO_L13_THREADS)
+#define SO_L13_POS_BITS 25  /* REF_POS_BITS2 (src/lookupTable13.cu:32)    */
+#define SO_L13_POS_MASK 33554431
+#define SO_L13_HITS 3       /* maxNumHits = 3 (src/search2.cu:62)         */
+#define SO_L13_KEEP 1000    /* the k > 1000 reset (src/lookupTable13.cu:800) */
+
+struct so_lt13_s {
+  const so_index *ix;   /* keys = lookup, numTuplesPerHash = actual      */
+  int k, nrefs;
+  int32_t *vals;        /* _refPos2: total + 1 composites, [0] = -1      */
+  long *tbase, *ntup;   /* per reference: first tuple id, tuple count    */
+  int32_t *map;         /* refPosHashMap per tuple id (0: never written) */
+  long long max_comp;   /* _maxRefPosComposite: entries of the device copy */
+};
+
+static void so_lt13_free(so_lt13 *t) {
+  if (!t) return;
+  free(t->vals);
+  free(t->tbase);
+  free(t->ntup);
+  free(t->map);
+  free(t);
+}
+
+/* lookupTable13Create (src/lookupTable13.cu:64-242) on top of the SSAHA
+ * index of the same tuples: composites refIdx << 25 | pos / k replace the
+ * positions, and refPosHashMap holds the hash of every tuple written to the
+ * temporary file (the first thres occurrences of each hash).  The map has
+ * _maxRefPosComposite entries on the device, one short of the largest
+ * composite written (src/lookupTable13.cu:182,374-377); reads at or past
+ * that length are undefined in the reference and are 0 here, the value of
+ * every entry never written. */
+static int so_lt13_build(const so_ref *r, const so_index *ix, so_lt13 **out, char *err,
+                         size_t errlen) {
+  const int k = ix->k;
+  if (r->n > 64) {
+    so_err(err, errlen, "lt13 seeding: more than 64 reference sequences (the composite "
+           "position keeps the index in the bits of an int above bit 25)");
+    return -1;
+  }
+  if (ix->thres > SO_L13_ARR - SO_L13_KEEP - 2 * SO_L13_THREADS) {
+    so_err(err, errlen, "lt13 seeding: ignore threshold above %d (the kernel's shared "
+           "arrays would overflow)", SO_L13_ARR - SO_L13_KEEP - 2 * SO_L13_THREADS);
+    return -1;
+  }
+  so_lt13 *t = (so_lt13 *)calloc(1, sizeof(so_lt13));
+  t->ix = ix;
+  t->k = k;
+  t->nrefs = r->n;
+  t->tbase = (long *)calloc((size_t)r->n + 1, sizeof(long));
+  t->ntup = (long *)calloc((size_t)r->n + 1, sizeof(long));
+  long nt = 0;
+  for (int i = 0; i < r->n; ++i) {
+    t->tbase[i] = nt;
+    t->ntup[i] = (long)(r->recs[i].cat_len / (size_t)k);
+    if (t->ntup[i] >= (1L << SO_L13_POS_BITS) - 64) {
+      so_err(err, errlen, "lt13 seeding: a sequence of %ld tuples does not fit the "
+             "composite position", t->ntup[i]);
+      so_lt13_free(t);
+      return -1;
+    }
+    nt += t->ntup[i];
+  }
+  t->vals = (int32_t *)malloc(((size_t)ix->total + 1) * sizeof(int32_t));
+  t->vals[0] = -1;
+  for (int i = 1; i <= ix->total; ++i)
+    t->vals[i] = ((int32_t)ix->ref_idx[i] << SO_L13_POS_BITS) + ix->ref_pos[i] / k;
+  t->map = (int32_t *)calloc((size_t)(nt > 0 ? nt : 1), sizeof(int32_t));
+  int *seen = (int *)calloc((size_t)ix->nb, sizeof(int));
+  for (int ri = 0; ri < r->n; ++ri) {
+    const char *s = r->cat + r->recs[ri].cat_start;
+    for (long c = 0; c < t->ntup[ri]; ++c) {
+      int h = so_hash(s + c * k, k);
+      if (++seen[h] <= ix->thres) {
+        t->map[t->tbase[ri] + c] = h;
+        long long comp = ((long long)ri << SO_L13_POS_BITS) + c;
+        if (comp > t->max_comp) t->max_comp = comp;
+      }
+    }
+  }
+  free(seen);
+  *out = t;
+  return 0;
+}
+
+static int32_t so_lt13_map_at(const so_lt13 *t, long long v) {
+  if (v < 0 || v >= t->max_comp) return 0;
+  int r = (int)(v >> SO_L13_POS_BITS);
+  long c = (long)(v & SO_L13_POS_MASK);
+  if (r >= t->nrefs || c >= t->ntup[r]) return 0;
+  return t->map[t->tbase[r] + c];
+}
+
+/* getRandNum13_gpu (src/lookupTable13.cu:907-911): K&R's generator on the
+ * block's shared seed, which the reference never initialises; it starts at
+ * 0 here for every query strand. */
+static int so_l13_rand(uint32_t *seed) {
+  *seed = *seed * 1103515245u + 12345u;
+  return (int)((*seed / 65536u) % 32768u);
+}
+
+/* One query strand: lookupTable13MapQry2_gpu (src/lookupTable13.cu:646-868)
+ * with the block's 64 threads run in order.  Writes up to 3 hits (records
+ * whose reference index is not -1, src/search2.cu:339-377). */
+static int so_lt13_query(const so_lt13 *t, const char *seq, int Q, int32_t *ri, int32_t *rp) {
+  const so_index *ix = t->ix;
+  const int k = t->k;
+  char qs[SO_L13_ARR];            /* qrySeq_shr: the strand, zeros after it */
+  int nm[SO_L13_ARR], pos[SO_L13_ARR], pos3[SO_L13_ARR];
+  int qh[SO_L13_ARR];
+  memset(qs, 0, sizeof(qs));
+  memcpy(qs, seq, (size_t)Q);
+  for (int i = 0; i < SO_L13_ARR; ++i) {
+    nm[i] = -1;
+    pos[i] = -1;
+    pos3[i] = -1;
+  }
+  /* getHash13_gpu at every offset the kernel hashes (zeros hash as A) */
+  const int n_tup = Q - k + 1;
+  const int last = (Q / k) * k;
+  int hmax = n_tup + 2 > last ? n_tup + 2 : last;
+  if (hmax < 0) hmax = 0;
+  for (int x = 0; x < hmax && x + k <= SO_L13_ARR; ++x) qh[x] = so_hash(qs + x, k);
+  int count = 0, maxm = 0;
+  int inc = -1;
+  while (inc <= n_tup) {
+    ++inc;
+    const int h = qh[inc];
+    const int nh = ix->actual[h];
+    const int iters = (nh + SO_L13_THREADS - 1) / SO_L13_THREADS;
+    const int key = ix->lookup[h];
+    /* seed and extend every hit of the tuple (src/lookupTable13.cu:722-771) */
+    for (int j = 0; j < iters * SO_L13_THREADS; ++j) {
+      const int idx = count + j;
+      long long val = j < nh ? t->vals[key + j] : -1;
+      if (val < 0) {
+        nm[idx] = 0;
+        continue;
+      }
+      const int start_val = (int)val;
+      int matches = 0, mm = 0, mm2 = 0, inc2 = inc;
+      int32_t rth = so_lt13_map_at(t, val);
+      while (inc2 < last) {
+        if (rth == qh[inc2]) {
+          ++val;
+          rth = so_lt13_map_at(t, val);
+          inc2 += k;
+          ++matches;
+          mm = 0;
+          mm2 = 0;
+        } else if (mm < k - 1) {
+          ++inc2;
+          ++mm;
+        } else if (mm2 == 0) {
+          ++val;
+          rth = so_lt13_map_at(t, val);
+          inc2 -= mm;
+          mm = 0;
+          ++mm2;
+        } else {
+          break;
+        }
+      }
+      nm[idx] = matches;
+      pos[idx] = start_val;
+    }
+    /* the tail clear (src/lookupTable13.cu:774-783): thread 0 clears from
+     * offset for gap entries, the block from offset in steps of 64 */
+    const int offset = count + nh;
+    const int gap = (SO_L13_ARR - offset) % SO_L13_THREADS;
+    for (int i = offset; i < offset + gap; ++i) nm[i] = -1;
+    const int it3 = (SO_L13_ARR - offset) / SO_L13_THREADS;
+    for (int i = offset; i < offset + it3 * SO_L13_THREADS; ++i) nm[i] = -1;
+    /* keep the biggest matches (src/lookupTable13.cu:786-803) */
+    int kk = count;
+    for (int j = count; j < offset; ++j) {
+      if (maxm <= nm[j]) {
+        if (maxm < nm[j]) {
+          maxm = nm[j];
+          kk = 0;
+        }
+        nm[j] = -1;
+        nm[kk] = maxm;
+        pos[kk] = pos[j];
+        ++kk;
+      }
+    }
+    if (kk > SO_L13_KEEP) kk = 0;
+    count = kk;
+  }
+  /* final selection (src/lookupTable13.cu:808-839): the maximum over
+   * [0, count], then the entries equal to it in thread-strided order */
+  int fm = 0;
+  for (int i = 0; i <= count; ++i)
+    if (nm[i] > fm) fm = nm[i];
+  int n3 = 0;
+  for (int th = 0; th < SO_L13_THREADS; ++th)
+    for (int i = 0; i < SO_L13_ITERS; ++i) {
+      const int p = i * SO_L13_THREADS + th;
+      if (nm[p] == fm) pos3[n3++] = pos[p];
+    }
+  int pick[SO_L13_HITS];
+  if (n3 > SO_L13_HITS) {
+    /* arrGetRandomNums13_gpu (src/lookupTable13.cu:882-898) */
+    uint32_t seed = 0;
+    int got = 0;
+    while (got < SO_L13_HITS) {
+      int v = so_l13_rand(&seed) % n3;
+      int dup = 0;
+      for (int i = 0; i < got; ++i) dup |= pick[i] == v;
+      if (!dup) pick[got++] = v;
+    }
+  } else {
+    for (int i = 0; i < SO_L13_HITS; ++i) pick[i] = i;
+  }
+  int n = 0;
+  for (int i = 0; i < SO_L13_HITS; ++i) {
+    const int v = pos3[pick[i]];
+    const int8_t r8 = (int8_t)(v >> SO_L13_POS_BITS);
+    if (r8 == -1) continue;
+    ri[n] = r8;
+    rp[n] = (v & SO_L13_POS_MASK) * k;
+    ++n;
+  }
+  return n;
+}
+
+int so_lt13_map(const char *fasta, size_t len, int k, int thres, const char *seq,
+                int seq_len, int32_t *ri, int32_t *rp, char *err, size_t errlen) {
+  so_ref r;
+  so_index *ix = NULL;
+  so_lt13 *t = NULL;
+  int rc = so_ref_parse(fasta, len, &r, err, errlen);
+  if (rc == 0) rc = so_index_from_ref(&r, k, thres, &ix, err, errlen);
+  if (rc == 0) rc = so_lt13_build(&r, ix, &t, err, errlen);
+  if (rc == 0) rc = so_lt13_query(t, seq, seq_len, ri, rp);
+  so_lt13_free(t);
+  so_index_free(ix);
+  so_ref_free(&r);
+  return rc;
+}
+
+typedef struct {
+  const so_lt13 *t;
+  const so_reads *rd;
+  int32_t *ri, *rp;  /* per read: 2 x 3 entries */
+  int *cnt;          /* per read: [fwd, rev] */
+  long next;
+  pthread_mutex_t mu;
+} so_l13_job;
+
+static void *so_l13_worker(void *arg) {
+  so_l13_job *jb = (so_l13_job *)arg;
+  char rev[SO_QSEQ_MAX + 1];
+  for (;;) {
+    pthread_mutex_lock(&jb->mu);
+    long i = jb->next;
+    jb->next += 64;
+    pthread_mutex_unlock(&jb->mu);
+    if (i >= jb->rd->n) break;
+    long e = i + 64 < jb->rd->n ? i + 64 : jb->rd->n;
+    for (; i < e; ++i) {
+      const so_read *r = &jb->rd->r[i];
+      size_t b0 = (size_t)i * 2 * SO_L13_HITS;
+      jb->cnt[2 * i] = so_lt13_query(jb->t, r->seq, r->len, jb->ri + b0, jb->rp + b0);
+      so_revcomp(r->seq, r->len, rev);
+      jb->cnt[2 * i + 1] = so_lt13_query(jb->t, rev, r->len, jb->ri + b0 + SO_L13_HITS,
+                                         jb->rp + b0 + SO_L13_HITS);
+    }
+  }
+  return NULL;
+}
+
+/* search2Queries' records (src/search2.cu:176-256, 339-377): every read in
+ * file order, forward strand then reverse complement, shift 0. */
+static int so_run_phase1_lt13(const so_lt13 *t, const so_reads *rd, int threads,
+                              so_match **out, int *n_out) {
+  so_l13_job jb;
+  memset(&jb, 0, sizeof(jb));
+  jb.t = t;
+  jb.rd = rd;
+  size_t nr = (size_t)(rd->n > 0 ? rd->n : 1);
+  jb.ri = (int32_t *)malloc(nr * 2 * SO_L13_HITS * sizeof(int32_t));
+  jb.rp = (int32_t *)malloc(nr * 2 * SO_L13_HITS * sizeof(int32_t));
+  jb.cnt = (int *)calloc(nr * 2, sizeof(int));
+  pthread_mutex_init(&jb.mu, NULL);
+  if (threads < 1) threads = 1;
+  pthread_t *th = (pthread_t *)malloc((size_t)threads * sizeof(pthread_t));
+  for (int i = 0; i < threads; ++i) pthread_create(&th[i], NULL, so_l13_worker, &jb);
+  for (int i = 0; i < threads; ++i) pthread_join(th[i], NULL);
+  free(th);
+  pthread_mutex_destroy(&jb.mu);
+  long nm = 0;
+  for (long i = 0; i < rd->n; ++i) nm += jb.cnt[2 * i] + jb.cnt[2 * i + 1];
+  so_match *m = (so_match *)malloc((size_t)(nm > 0 ? nm : 1) * sizeof(so_match));
+  long q = 0;
+  for (long i = 0; i < rd->n; ++i)
+    for (int strand = 0; strand < 2; ++strand) {
+      size_t b0 = (size_t)i * 2 * SO_L13_HITS + (size_t)strand * SO_L13_HITS;
+      for (int h = 0; h < jb.cnt[2 * i + strand]; ++h) {
+        m[q].slot_read = (int32_t)i;
+        m[q].strand = strand;
+        m[q].ref_idx = jb.ri[b0 + h];
+        m[q].shift = 0;
+        m[q].ref_pos = jb.rp[b0 + h];
+        ++q;
+      }
+    }
+  free(jb.ri);
+  free(jb.rp);
+  free(jb.cnt);
+  *out = m;
+  *n_out = (int)nm;
+  return 0;
 }
 
 /* ------------------------------------------------------------------ */
@@ -877,6 +1215,7 @@ static void so_print_sam(so_sb *sb, const so_pair *x) {
 struct so_session {
   so_ref r;
   so_index *ix;
+  so_lt13 *l13;  /* seeder 1 only */
   so_params p;
 };
 
@@ -886,6 +1225,7 @@ int so_session_create(const char *ref, size_t ref_len, const so_params *p,
   s->p = *p;
   int rc = so_ref_parse(ref, ref_len, &s->r, err, errlen);
   if (rc == 0) rc = so_index_from_ref(&s->r, p->seed_len, p->ignore_thres, &s->ix, err, errlen);
+  if (rc == 0 && p->seeder == 1) rc = so_lt13_build(&s->r, s->ix, &s->l13, err, errlen);
   if (rc != 0) {
     so_session_free(s);
     return rc;
@@ -896,6 +1236,7 @@ int so_session_create(const char *ref, size_t ref_len, const so_params *p,
 
 void so_session_free(so_session *s) {
   if (!s) return;
+  so_lt13_free(s->l13);
   so_index_free(s->ix);
   so_ref_free(&s->r);
   free(s);
@@ -920,7 +1261,9 @@ int so_session_align(so_session *ss, const char *reads, size_t reads_len,
   int nm = 0;
   memset(&rd, 0, sizeof(rd));
   int rc = so_reads_parse(reads, reads_len, &rd, err, errlen);
-  if (rc == 0) rc = so_run_phase1(ss->ix, &rd, p->max_hits, p->threads, &m, &nm);
+  if (rc == 0)
+    rc = p->seeder == 1 ? so_run_phase1_lt13(ss->l13, &rd, p->threads, &m, &nm)
+                        : so_run_phase1(ss->ix, &rd, p->max_hits, p->threads, &m, &nm);
   if (rc != 0) {
     free(rd.r);
     return rc;

@@ -34,6 +34,8 @@ typedef struct {
   int threads;       /* worker threads (>= 1)                                */
   int out_format;    /* -f: 1 SAM (printOutputSam, src/output.cu:98-130,
                         every record); other values printOutput           */
+  int seeder;        /* 0 SSAHA (searchQueries3); 1 lt13 seed-and-extend
+                        (search2Queries, the GPU default of src/main.cu)   */
 } so_params;
 
 typedef struct {
@@ -109,6 +111,13 @@ void so_session_free(so_session *s);
 
 /* Phase 1 only: the match-file records in file order (including the
  * trailing-batch repeats of searchQueries3).  *out is malloc'ed. */
+/* lt13 seed-and-extend mapping of one query strand (lookupTable13MapQry2_gpu,
+ * src/lookupTable13.cu:646-868) on the index built from fasta with seed
+ * length k and threshold thres: up to 3 (ref_idx, ref_pos) hits in the
+ * printed order.  Returns the count, or < 0 with err set. */
+int so_lt13_map(const char *fasta, size_t len, int k, int thres, const char *seq,
+                int seq_len, int32_t *ri, int32_t *rp, char *err, size_t errlen);
+
 int so_phase1(const char *ref, size_t ref_len, const char *reads,
               size_t reads_len, const so_params *p, so_match **out,
               int *n_out, char *err, size_t errlen);

@@ -142,3 +142,70 @@ def test_pipeline_sam_random(oracle):
         got = oracle.align(ref, reads, oracle.default_params(device_mem=dm, out_format=1))
         assert got == want
         assert want.count(b"\n") > 29 and b"D" in want and b"I" in want
+
+
+def _lt13_case(rng, n_refs, ref_len, n_reads, read_len, unit=None, n_frac=0.0):
+    seqs = []
+    for i in range(n_refs):
+        if unit:  # copies of one unit with light divergence: many equal hits
+            u = rand_seq(rng, unit)
+            s = bytearray()
+            while len(s) < ref_len:
+                s += mutate(rng, u, 0.02, 0.0)
+            s = bytes(s[:ref_len])
+        else:
+            s = rand_seq(rng, ref_len)
+        seqs.append(s)
+    if n_frac:
+        seqs = [bytes(c if rng.random() > n_frac else ord("N") for c in s) for s in seqs]
+    ref = b"".join(b">c%d\n" % i + b"\n".join(s[j:j + 60] for j in range(0, len(s), 60)) + b"\n"
+                   for i, s in enumerate(seqs))
+    reads = []
+    for i in range(n_reads):
+        s = seqs[rng.randrange(n_refs)]
+        # the first read is the shortest: Phase 2 aligns every read on the
+        # first read's length (reads shorter than that read stale buffers)
+        L = read_len if isinstance(read_len, int) else (
+            read_len[0] if i == 0 else rng.randint(*read_len))
+        if i % 5 == 4:  # a read at a sequence end (extensions walk past it)
+            a = len(s) - L + rng.randrange(0, 8)
+            r = (s[a:] + rand_seq(rng, L))[:L]
+        else:
+            a = rng.randrange(0, len(s) - L - 20)
+            r = mutate(rng, s[a:a + L + 10], 0.03, 0.01)[:L].ljust(L, b"G")
+        if i % 2:
+            r = oracle_revcomp(r)
+        if i % 7 == 3:
+            r = r[:L // 2].lower() + b"N" + r[L // 2 + 1:]
+        reads.append(b">q%d\n%s\n" % (i, r))
+    return ref, b"".join(reads)
+
+
+def oracle_revcomp(s):
+    comp = {ord("A"): ord("T"), ord("C"): ord("G"), ord("G"): ord("C")}
+    return bytes(comp.get(c, ord("A")) for c in reversed(s))
+
+
+@pytest.mark.parametrize("seed,case", list(enumerate([
+    dict(n_refs=2, ref_len=9000, n_reads=40, read_len=100, k=12, t=1000),
+    dict(n_refs=4, ref_len=3000, n_reads=40, read_len=(13, 150), k=12, t=1000, n_frac=0.01),
+    dict(n_refs=1, ref_len=12000, n_reads=30, read_len=90, k=8, t=300, unit=120),
+    dict(n_refs=3, ref_len=6000, n_reads=30, read_len=(8, 60), k=6, t=1000, unit=40),
+    dict(n_refs=2, ref_len=5000, n_reads=30, read_len=100, k=10, t=5),
+])))
+def test_lt13_phase1_and_pipeline(oracle, seed, case):
+    # the reference's lookupTable13MapQry2_gpu (run on CPU fibers) against the
+    # oracle's restatement: Phase-1 records and the whole default output
+    rng = random.Random(1300 + seed)
+    kw = {k: v for k, v in case.items() if k not in ("k", "t")}
+    ref, reads = _lt13_case(rng, **kw)
+    dm = 288_000_000_000
+    out, recs = R.pipeline_with_matches(ref, reads, dm, seed_len=case["k"], thres=case["t"],
+                                        seeder=1)
+    p = oracle.default_params(device_mem=dm, seed_len=case["k"], ignore_thres=case["t"],
+                              seeder=1)
+    names = [l[1:].decode() for l in reads.split(b"\n") if l.startswith(b">")]
+    got = [(names[r], s, ri, sh, rp) for r, s, ri, sh, rp in oracle.phase1(ref, reads, p)]
+    assert got == recs
+    assert oracle.align(ref, reads, p) == out
+    assert len(recs) > 0
