@@ -59,7 +59,10 @@ typedef struct {
                             (printOutputSam, src/output.cu:98-130); any
                             other value the default record of the best one
                             per read (printOutput, src/output.cu:154-201)  */
-  int32_t reserved;      /* 0                                              */
+  int32_t seeder;        /* Phase 1: 0 SSAHA seeding (searchQueries3,
+                            src/search.cu:275-382); 1 lt13 seed-and-extend
+                            (search2Queries, src/search2.cu:48-259), the
+                            GPU default of the reference CLI               */
 } swift_params;
 
 /* One Phase-1 record (one line of the reference's match file,
@@ -130,6 +133,17 @@ int swift_index_export(swift_ctx *ctx, const swift_index *idx, int32_t *lookup,
 int swift_seed(swift_ctx *ctx, const swift_index *idx, const char *reads_fasta,
                size_t len, int32_t max_hits, swift_match *out, int64_t cap,
                int64_t *n);
+
+/* Phase 1 of the reference CLI's GPU default: lt13 seed-and-extend
+ * (replaces search2Queries, src/search2.cu:48-259, with
+ * lookupTable13Create and lookupTable13MapQry2_gpu,
+ * src/lookupTable13.cu:64-242,646-868).  Up to 3 records per read strand,
+ * every read once in file order (forward, then reverse complement), shift 0.
+ * The index's extra tables are built on first use.  SWIFT_E_LIMIT for more
+ * than 64 reference sequences, an ignore threshold above 1176 or a
+ * sequence of 2^25 - 64 tuples or more.  Output as swift_seed. */
+int swift_seed_lt13(swift_ctx *ctx, const swift_index *idx, const char *reads_fasta,
+                    size_t len, swift_match *out, int64_t cap, int64_t *n);
 
 /* Phase 2 on explicit pairs, the alignSequences contract: n pairs, query i
  * at qry + i*(Q+1) (Q bytes used), window i at ref + i*(R+1) (R bytes

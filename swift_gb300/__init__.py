@@ -22,7 +22,7 @@ EXPORTS = [
     "swift_params_default", "swift_ctx_create", "swift_ctx_destroy", "swift_last_error",
     "swift_ctx_info", "swift_ctx_set_sw_path",
     "swift_index_build", "swift_index_destroy", "swift_index_info", "swift_index_export",
-    "swift_seed", "swift_sw_batch", "swift_align", "swift_reads_upload",
+    "swift_seed", "swift_seed_lt13", "swift_sw_batch", "swift_align", "swift_reads_upload",
     "swift_reads_destroy", "swift_align_resident", "swift_fetch_output",
     "swift_align_files", "swift_free", "swift_peak_dpx", "swift_align_into",
     "swift_sw_batch_noalloc", "swift_sw_pairs", "swift_server_create", "swift_server_submit",
@@ -41,7 +41,7 @@ class Params(C.Structure):
         ("seed_len", C.c_int32), ("ignore_thres", C.c_int32), ("max_hits", C.c_int32),
         ("match", C.c_int32), ("mismatch", C.c_int32), ("gap_open", C.c_int32),
         ("gap_ext", C.c_int32), ("qry_len", C.c_int32), ("device_mem", C.c_int64),
-        ("out_format", C.c_int32), ("reserved", C.c_int32),
+        ("out_format", C.c_int32), ("seeder", C.c_int32),
     ]
 
 
@@ -108,6 +108,7 @@ def lib():
         L.swift_index_info.argtypes = [vp, vp, C.POINTER(i32), C.POINTER(i64), C.POINTER(i64)]
         L.swift_index_export.argtypes = [vp, vp, vp, vp, vp, vp]
         L.swift_seed.argtypes = [vp, vp, C.c_char_p, sz, i32, vp, i64, C.POINTER(i64)]
+        L.swift_seed_lt13.argtypes = [vp, vp, C.c_char_p, sz, vp, i64, C.POINTER(i64)]
         L.swift_sw_batch.argtypes = [vp, vp, vp, i32, i32, i64, i32, i32, i32, i32,
                                      vp, vp, vp, vp, vp, vp]
         L.swift_align.argtypes = [vp, vp, vp, sz, C.POINTER(Params), C.POINTER(vp),
@@ -196,6 +197,16 @@ class Context:
         arr = (Match * max(n.value, 1))()
         self._check(lib().swift_seed(self._h, index._h, reads_fasta, len(reads_fasta), max_hits,
                                      arr, n.value, C.byref(n)))
+        return [(m.read, m.strand, m.ref_idx, m.shift, m.ref_pos) for m in arr[: n.value]]
+
+    def seed_lt13(self, index: "Index", reads_fasta: bytes):
+        """lt13 seed-and-extend records (search2Queries)."""
+        n = C.c_int64()
+        self._check(lib().swift_seed_lt13(self._h, index._h, reads_fasta, len(reads_fasta),
+                                          None, 0, C.byref(n)))
+        arr = (Match * max(n.value, 1))()
+        self._check(lib().swift_seed_lt13(self._h, index._h, reads_fasta, len(reads_fasta),
+                                          arr, n.value, C.byref(n)))
         return [(m.read, m.strand, m.ref_idx, m.shift, m.ref_pos) for m in arr[: n.value]]
 
     # -- Phase 2 on explicit pairs (alignSequences) ------------------------------

@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -47,6 +48,14 @@ struct swift_index {
   uint2* d_post = nullptr;
   int64_t total = 0;
   int64_t nb = 0;
+  // lt13 seeding (seed13.cu), built on first use
+  std::mutex lt13_mu;
+  bool lt13_ready = false;
+  int32_t* d_vals13 = nullptr;   // composite per posting
+  int32_t* d_map13 = nullptr;    // refPosHashMap per tuple id
+  int64_t* d_tbase13 = nullptr;  // per reference: first tuple id, tuples
+  int64_t* d_ntup13 = nullptr;
+  int64_t max_comp13 = 0;
 };
 
 struct swift_reads {
@@ -294,19 +303,132 @@ struct SeedOut {
   int64_t launches = 0;
 };
 
+// The lt13 tables of an index (seed13.cu), built once on first use: the
+// composite of every posting, and refPosHashMap per tuple id, which keeps a
+// tuple's hash when it is among the first thres occurrences of that hash in
+// file order (lookupTable13Create, src/lookupTable13.cu:101-140).  The
+// hashes come from the device; the occurrence ranks are counted on the host
+// in one pass over the tuples.
+int ensure_lt13(swift_ctx* ctx, const swift_index* cidx) {
+  swift_index* idx = const_cast<swift_index*>(cidx);
+  std::lock_guard<std::mutex> lk(idx->lt13_mu);
+  if (idx->lt13_ready) return SWIFT_OK;
+  const int nr = (int)idx->recs.size();
+  if (nr > kMaxRefs13)
+    return fail(ctx, SWIFT_E_LIMIT, "lt13 seeding: more than 64 reference sequences (the "
+                                    "composite position keeps the index above bit 25 of an int)");
+  if (idx->thres > kMaxThres13)
+    return fail(ctx, SWIFT_E_LIMIT, "lt13 seeding: ignore threshold above 1176 (the reference "
+                                    "kernel's shared arrays would overflow)");
+  const int k = idx->k;
+  std::vector<int64_t> tb(nr + 1, 0), nt(std::max(nr, 1), 0);
+  std::vector<uint64_t> tbu(nr + 1, 0);
+  for (int r = 0; r < nr; ++r) {
+    nt[r] = (int64_t)(idx->recs[r].cat_len / (uint64_t)k);
+    if (nt[r] >= (1 << 25) - 64)
+      return fail(ctx, SWIFT_E_LIMIT, "lt13 seeding: a sequence's tuples do not fit the "
+                                      "composite position");
+    tb[r + 1] = tb[r] + nt[r];
+    tbu[r + 1] = (uint64_t)tb[r + 1];
+  }
+  const int64_t n_tup = tb[nr];
+  cudaStream_t st = ctx->st;
+  std::vector<uint32_t> hash((size_t)std::max<int64_t>(n_tup, 1));
+  {
+    Scratch sc(st);
+    uint64_t* d_tb;
+    uint32_t* d_hash;
+    CK(sc.get(&d_tb, (size_t)nr + 1));
+    CK(sc.get(&d_hash, (size_t)std::max<int64_t>(n_tup, 1)));
+    CK(cudaMemcpyAsync(d_tb, tbu.data(), (nr + 1) * 8, cudaMemcpyHostToDevice, st));
+    launch_tuple_hash13(st, idx->d_packed, idx->d_recs, d_tb, nr, (uint64_t)n_tup, k, d_hash);
+    CKLAUNCH();
+    CK(cudaMemcpyAsync(hash.data(), d_hash, n_tup * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+  }
+  std::vector<int32_t> map((size_t)std::max<int64_t>(n_tup, 1), 0);
+  std::vector<uint16_t> seen((size_t)idx->nb, 0);
+  int64_t max_comp = 0;
+  for (int r = 0; r < nr; ++r)
+    for (int64_t c = 0; c < nt[r]; ++c) {
+      const int64_t t = tb[r] + c;
+      const uint32_t h = hash[t];
+      if (seen[h] < 65535) ++seen[h];
+      if (seen[h] <= (uint32_t)idx->thres) {
+        map[t] = (int32_t)h;
+        max_comp = std::max<int64_t>(max_comp, ((int64_t)r << 25) + c);
+      }
+    }
+  CK(cudaMalloc(&idx->d_map13, (size_t)std::max<int64_t>(n_tup, 1) * 4));
+  CK(cudaMalloc(&idx->d_vals13, (size_t)std::max<int64_t>(idx->total, 1) * 4));
+  CK(cudaMalloc(&idx->d_tbase13, (size_t)std::max(nr, 1) * 8));
+  CK(cudaMalloc(&idx->d_ntup13, (size_t)std::max(nr, 1) * 8));
+  CK(cudaMemcpyAsync(idx->d_map13, map.data(), n_tup * 4, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(idx->d_tbase13, tb.data(), nr * 8, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(idx->d_ntup13, nt.data(), nr * 8, cudaMemcpyHostToDevice, st));
+  launch_composites13(st, idx->d_post, idx->total, k, idx->d_vals13);
+  CKLAUNCH();
+  CK(cudaStreamSynchronize(st));
+  idx->max_comp13 = max_comp;
+  idx->lt13_ready = true;
+  return SWIFT_OK;
+}
+
 // Phase 1 for resident reads: fills the match arrays (allocated in sc).
+// seeder 0: SSAHA (searchQueries3, with its stale trailing batch); 1: lt13
+// seed-and-extend (search2Queries: every read once, 3 hits per strand).
 int run_seed(swift_ctx* ctx, const swift_index* idx, const swift_reads* rd, int max_hits,
-             Scratch& sc, SeedOut* out) {
+             int seeder, Scratch& sc, SeedOut* out) {
   const int64_t n = rd->n;
   const int64_t ns = 2 * n;
   cudaStream_t st = ctx->st;
+  if (seeder == 1) {
+    const int rc13 = ensure_lt13(ctx, idx);
+    if (rc13 != SWIFT_OK) return rc13;
+    max_hits = 3;  // search2Queries fixes maxNumHits at 3 (src/search2.cu:62)
+  }
   int3* best;
   int32_t *nbest, *ovl, *novl;
   CK(sc.get(&best, (size_t)std::max<int64_t>(ns, 1) * max_hits));
   CK(sc.get(&nbest, (size_t)std::max<int64_t>(ns, 1)));
   CK(sc.get(&ovl, (size_t)std::max<int64_t>(ns, 1)));
-  CK(sc.get(&novl, 1));
-  CK(cudaMemsetAsync(novl, 0, sizeof(int32_t), st));
+  CK(sc.get(&novl, 2));
+  CK(cudaMemsetAsync(novl, 0, 2 * sizeof(int32_t), st));
+  if (seeder == 1) {
+    Seed13Args s13;
+    memset(&s13, 0, sizeof(s13));
+    s13.reads = rd->d_bytes;
+    s13.rd = rd->d_rd;
+    s13.n_reads = n;
+    s13.offsets = idx->d_offsets;
+    s13.vals = idx->d_vals13;
+    s13.map = idx->d_map13;
+    s13.tbase = idx->d_tbase13;
+    s13.ntup = idx->d_ntup13;
+    s13.nrefs = (int)idx->recs.size();
+    s13.max_comp = idx->max_comp13;
+    s13.k = idx->k;
+    s13.best = best;
+    s13.nbest = nbest;
+    s13.overflow_list = ovl;
+    s13.n_overflow = novl;
+    launch_seed13(st, s13, false);
+    CKLAUNCH();
+    out->launches += ns > 0 ? 1 : 0;
+    int32_t h_novl = 0;
+    CK(cudaMemcpyAsync(&h_novl, novl, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    out->overflow = h_novl;
+    if (h_novl > 0) {  // strands redone with the reference's full array sizes
+      s13.list = ovl;
+      s13.n_list = h_novl;
+      s13.n_overflow = novl + 1;
+      launch_seed13(st, s13, true);
+      CKLAUNCH();
+      out->launches += 1;
+    }
+  }
+  if (seeder != 1) {
   SeedArgs a;
   memset(&a, 0, sizeof(a));
   a.reads = rd->d_bytes;
@@ -359,6 +481,7 @@ int run_seed(swift_ctx* ctx, const swift_index* idx, const swift_reads* rd, int 
     CKLAUNCH();
     out->launches += 1;
   }
+  }  // SSAHA seeding
   // per-read record counts -> offsets
   uint64_t *cnt, *roff, *tot_d;
   void* tmp;
@@ -372,7 +495,9 @@ int run_seed(swift_ctx* ctx, const swift_index* idx, const swift_reads* rd, int 
   CKLAUNCH();
   uint64_t total_in = 0;
   CK(cudaMemcpyAsync(&total_in, tot_d, sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
-  const std::vector<int32_t>& rep = rd->repeats;
+  // the stale trailing batch of searchQueries3; search2Queries has none
+  const std::vector<int32_t> no_rep;
+  const std::vector<int32_t>& rep = seeder == 1 ? no_rep : rd->repeats;
   std::vector<uint64_t> rep_cnt(rep.size()), rep_off(rep.size());
   std::vector<int32_t> rep_nb(2 * rep.size());
   for (size_t i = 0; i < rep.size(); ++i)
@@ -503,7 +628,7 @@ void swift_params_default(swift_params* p) {
   p->qry_len = 0;
   p->device_mem = 0;
   p->out_format = 0;
-  p->reserved = 0;
+  p->seeder = 0;
 }
 
 int swift_ctx_create(int device, void* stream, swift_ctx** out) {
@@ -702,6 +827,10 @@ int swift_index_destroy(swift_index* ix) {
   cudaFree(ix->d_groups);
   cudaFree(ix->d_cstart);
   cudaFree(ix->d_post);
+  cudaFree(ix->d_vals13);
+  cudaFree(ix->d_map13);
+  cudaFree(ix->d_tbase13);
+  cudaFree(ix->d_ntup13);
   delete ix;
   return SWIFT_OK;
 }
@@ -755,8 +884,10 @@ int swift_reads_destroy(swift_reads* r) {
   return SWIFT_OK;
 }
 
-int swift_seed(swift_ctx* ctx, const swift_index* idx, const char* reads, size_t len,
-               int32_t max_hits, swift_match* out, int64_t cap, int64_t* n) {
+namespace {
+
+int seed_records(swift_ctx* ctx, const swift_index* idx, const char* reads, size_t len,
+                 int32_t max_hits, int seeder, swift_match* out, int64_t cap, int64_t* n) {
   if (!ctx || !idx || !reads || !n) return fail(ctx, SWIFT_E_ARG, "null argument");
   if (max_hits < 1 || max_hits > 64) return fail(ctx, SWIFT_E_ARG, "max_hits outside 1..64");
   CK(cudaSetDevice(ctx->device));
@@ -766,7 +897,7 @@ int swift_seed(swift_ctx* ctx, const swift_index* idx, const char* reads, size_t
   {
     Scratch sc(ctx->st);
     SeedOut so;
-    rc = run_seed(ctx, idx, rd, max_hits, sc, &so);
+    rc = run_seed(ctx, idx, rd, max_hits, seeder, sc, &so);
     if (rc == SWIFT_OK) {
       *n = so.n;
       int64_t w = std::min<int64_t>(so.n, cap);
@@ -796,6 +927,19 @@ int swift_seed(swift_ctx* ctx, const swift_index* idx, const char* reads, size_t
   swift_reads_destroy(rd);
   return rc;
 }
+
+}  // namespace
+
+int swift_seed(swift_ctx* ctx, const swift_index* idx, const char* reads, size_t len,
+               int32_t max_hits, swift_match* out, int64_t cap, int64_t* n) {
+  return seed_records(ctx, idx, reads, len, max_hits, 0, out, cap, n);
+}
+
+int swift_seed_lt13(swift_ctx* ctx, const swift_index* idx, const char* reads, size_t len,
+                    swift_match* out, int64_t cap, int64_t* n) {
+  return seed_records(ctx, idx, reads, len, 3, 1, out, cap, n);
+}
+
 
 int swift_sw_batch(swift_ctx* ctx, const char* qry, const char* ref, int32_t Q, int32_t R,
                    int64_t n, int32_t m, int32_t x, int32_t o, int32_t e, float* score,
@@ -1447,7 +1591,8 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
   memset(&s, 0, sizeof(s));
   CK(cudaEventRecord(ctx->ev[0], st));
   SeedOut so;
-  int rc = run_seed(ctx, idx, rd, p->max_hits, sc, &so);
+  if (p->seeder != 0 && p->seeder != 1) return fail(ctx, SWIFT_E_ARG, "seeder must be 0 or 1");
+  int rc = run_seed(ctx, idx, rd, p->max_hits, p->seeder, sc, &so);
   if (rc != SWIFT_OK) return rc;
   CK(cudaEventRecord(ctx->ev[1], st));
   const int64_t nm = so.n;

@@ -41,6 +41,10 @@ int main(int argc, char** argv) {
   const char *q = nullptr, *q2 = nullptr, *r = nullptr, *o = nullptr;
   swift_params p;
   swift_params_default(&p);
+  // Phase 1 of the reference's GPU branch is search2Queries (lt13
+  // seed-and-extend, src/main.cu:135-150); -seeder 0 selects the SSAHA
+  // seeding of searchQueries3 instead (not a reference flag)
+  p.seeder = 1;
   int cpu = 0;
   if (argc == 1) {
     printf("%s\n", usage_text());
@@ -65,6 +69,7 @@ int main(int argc, char** argv) {
     else if (!strcmp(a, "-t")) p.ignore_thres = atoi(take());
     else if (!strcmp(a, "-l")) p.seed_len = atoi(take());
     else if (!strcmp(a, "-cpu")) cpu = 1;
+    else if (!strcmp(a, "-seeder")) p.seeder = atoi(take());
     else if (!strcmp(a, "-v")) {
       printf("Version: %s\n", "0.11.2");
       return 0;

@@ -149,6 +149,36 @@ struct SeedArgs {
   uint64_t* scratch;          // overflow path: per-strand hash tables
 };
 void launch_seed(cudaStream_t st, const SeedArgs& a);
+
+// seed13.cu: lt13 seed-and-extend seeding (search2Queries)
+constexpr int kMaxRefs13 = 64;      // refIdx << 25 in an int
+constexpr int kFullArr13 = 2304;    // the reference block's shared arrays (idealArrSize)
+constexpr int kFullStage13 = 1280;  // staged hits of one tuple offset (ignore threshold <= 1176)
+constexpr int kMaxThres13 = 1176;   // kFullArr13 - 1000 kept - 2 x 64 padding
+struct Seed13Args {
+  const char* reads;
+  const DevRead* rd;
+  int64_t n_reads;
+  const uint32_t* offsets;    // bucket starts of the SSAHA index
+  const int32_t* vals;        // composites per posting
+  const int32_t* map;         // refPosHashMap per tuple id
+  const int64_t* tbase;       // per reference: first tuple id
+  const int64_t* ntup;        // per reference: tuples
+  int nrefs;
+  int64_t max_comp;
+  int k;
+  const int32_t* list;        // strands to map (null: all 2 x n_reads)
+  int64_t n_list;
+  int3* best;                 // per strand: 3 x (ref_idx, 0, ref_pos)
+  int32_t* nbest;
+  int32_t* overflow_list;     // strands whose entries outgrow the fast kernel
+  int32_t* n_overflow;
+};
+void launch_seed13(cudaStream_t st, const Seed13Args& a, bool full);
+void launch_tuple_hash13(cudaStream_t st, const uint32_t* packed, const DevRecord* recs,
+                         const uint64_t* tbase, int n_recs, uint64_t n_tuples, int k,
+                         uint32_t* out);
+void launch_composites13(cudaStream_t st, const uint2* post, int64_t n, int k, int32_t* vals);
 void launch_seed_overflow(cudaStream_t st, const SeedArgs& a, int n_overflow,
                           const uint64_t* tab_off, const uint32_t* tab_size);
 int seed_smem_cap();

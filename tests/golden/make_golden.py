@@ -120,6 +120,10 @@ def main():
     sam = R.pipeline(ref, reads, DEVICE_MEM, out_format=1)
     assert R.pipeline(ref, reads, SAM_SMALL_MEM, out_format=1) == sam
     open(os.path.join(HERE, "pipeline_out_sam.txt"), "wb").write(sam)
+    # the reference CLI's GPU default Phase 1 (lt13 seed-and-extend) on the
+    # same inputs, through the default records
+    lt13 = R.pipeline(ref, reads, DEVICE_MEM, seeder=1)
+    open(os.path.join(HERE, "pipeline_out_lt13.txt"), "wb").write(lt13)
     print("wrote fixtures:", len(out), "bytes of pipeline output,", len(sam), "of SAM output")
 
 

@@ -54,6 +54,25 @@ def test_oracle_pipeline_sam(oracle):
     assert got == load("pipeline_out_sam.txt", "rb")
 
 
+def test_oracle_pipeline_lt13(oracle):
+    # the reference's lookupTable13 kernel (run on CPU fibers) made this file
+    meta = load("pipeline_meta.json")
+    got = oracle.align(load("pipeline_ref.fa", "rb"), load("pipeline_reads.fa", "rb"),
+                       oracle.default_params(device_mem=meta["device_mem"], seeder=1))
+    assert got == load("pipeline_out_lt13.txt", "rb")
+
+
+@pytest.mark.gpu
+def test_gpu_pipeline_lt13():
+    import swift_gb300 as sg
+    meta = load("pipeline_meta.json")
+    ctx = sg.Context(0)
+    ix = ctx.index(load("pipeline_ref.fa", "rb"))
+    got = ctx.align(ix, load("pipeline_reads.fa", "rb"),
+                    sg.default_params(device_mem=meta["device_mem"], seeder=1))
+    assert got == load("pipeline_out_lt13.txt", "rb")
+
+
 @pytest.mark.gpu
 def test_gpu_pipeline_sam():
     import swift_gb300 as sg

@@ -401,11 +401,17 @@ def test_cli_matches_oracle(ctx, oracle, sg):
         rp, qp, op = (os.path.join(d, f) for f in ("ref.fa", "reads.fa", "out.txt"))
         open(rp, "wb").write(ref)
         open(qp, "wb").write(reads)
+        # the reference CLI's GPU branch: lt13 seed-and-extend Phase 1
         r = subprocess.run([sg.CLI_PATH, "-q", qp, "-r", rp, "-o", op], capture_output=True)
         assert r.returncode == 0, r.stderr
         got = open(op, "rb").read()
-    want = oracle.align(ref, reads, oparams(ctx, oracle))
-    assert got == want
+        # SSAHA seeding (searchQueries3)
+        r = subprocess.run([sg.CLI_PATH, "-q", qp, "-r", rp, "-o", op, "-seeder", "0"],
+                           capture_output=True)
+        assert r.returncode == 0, r.stderr
+        got0 = open(op, "rb").read()
+    assert got == oracle.align(ref, reads, oparams(ctx, oracle, seeder=1))
+    assert got0 == oracle.align(ref, reads, oparams(ctx, oracle))
 
 
 def test_packed_and_generic_paths_agree(ctx, oracle):
@@ -545,5 +551,5 @@ def test_sam_cli(ctx, oracle, sg):
                            capture_output=True)
         assert r.returncode == 0, r.stderr
         got2 = open(op, "rb").read()
-    assert got == oracle.align(ref, reads, oparams(ctx, oracle, out_format=1))
-    assert got2 == oracle.align(ref, reads, oparams(ctx, oracle))
+    assert got == oracle.align(ref, reads, oparams(ctx, oracle, out_format=1, seeder=1))
+    assert got2 == oracle.align(ref, reads, oparams(ctx, oracle, seeder=1))

@@ -209,3 +209,22 @@ def test_lt13_phase1_and_pipeline(oracle, seed, case):
     assert got == recs
     assert oracle.align(ref, reads, p) == out
     assert len(recs) > 0
+
+
+def test_lt13_kept_entries_reset(oracle):
+    # 1100 exact copies of a 12-base unit, k = 6, threshold 1100: one query
+    # tuple keeps more than 1000 entries, so the kernel's reset fires
+    rng = random.Random(78)
+    u = rand_seq(rng, 12)
+    s = u * 1100
+    ref = b">rep\n" + b"\n".join(s[j:j + 60] for j in range(0, len(s), 60)) + b"\n"
+    reads = b"".join(b">r%d\n%s\n" % (i, s[a:a + 90])
+                     for i, a in enumerate(rng.randrange(0, 13000) for _ in range(12)))
+    reads += b">tail\n" + s[-50:] + rand_seq(rng, 40) + b"\n"
+    dm = 288_000_000_000
+    out, recs = R.pipeline_with_matches(ref, reads, dm, seed_len=6, thres=1100, seeder=1)
+    p = oracle.default_params(device_mem=dm, seed_len=6, ignore_thres=1100, seeder=1)
+    names = [l[1:].decode() for l in reads.split(b"\n") if l.startswith(b">")]
+    got = [(names[r], st, ri, sh, rp) for r, st, ri, sh, rp in oracle.phase1(ref, reads, p)]
+    assert got == recs
+    assert oracle.align(ref, reads, p) == out
