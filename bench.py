@@ -33,6 +33,12 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "reads/s (SSAHA seeding + Smith-Waterman + best per read + records), bit-exact"
+METRIC_LT13 = ("reads/s (lt13 seed-and-extend seeding + Smith-Waterman + best per read + "
+               "records), bit-exact")
+
+
+def metric_for(args):
+    return METRIC_LT13 if args.seeder == "lt13" else METRIC
 # DRAM bytes per pair of the bound pass, read + written, from one ncu capture
 # (413 MB for 825,653 pairs of the scale workload with 200 K reads), and the
 # algorithmic bytes: 112 B query + 304 B window read, 64 B suffix maxima +
@@ -52,6 +58,9 @@ def parse_args():
     ap.add_argument("--reads", type=int, default=None)
     ap.add_argument("--cpu-sample", type=int, default=20000)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--seeder", default="ssaha", choices=["ssaha", "lt13"],
+                    help="Phase 1: SSAHA seeding (searchQueries3) or lt13 seed-and-extend "
+                         "(search2Queries, the reference CLI's GPU default)")
     return ap.parse_args()
 
 
@@ -138,11 +147,12 @@ def sample_reads(reads: bytes, n: int) -> bytes:
     return b"\n".join(lines[: 2 * n]) + b"\n"
 
 
-def cpu_reference(ref: bytes, reads: bytes, n_sample: int, steps: int, warmup: int):
+def cpu_reference(ref: bytes, reads: bytes, n_sample: int, steps: int, warmup: int,
+                  seeder: int = 0):
     """The reference algorithm on the host cores (oracle port), reads/s."""
     from oracle import oracle as O
     threads = os.cpu_count() or 1
-    sess = O.Session(ref, O.default_params(threads=threads))
+    sess = O.Session(ref, O.default_params(threads=threads, seeder=seeder))
     sample = sample_reads(reads, n_sample)
     for _ in range(warmup):
         sess.align(sample)
@@ -317,13 +327,15 @@ def main():
         ref, reads, n, desc = make_workload(args, 0)
         steps, warm = max(args.steps, 1), max(args.warmup, 0)
         n_sample = min(args.cpu_sample, n)
-        rps, threads, dt = cpu_reference(ref, reads, n_sample, steps, min(warm, 1))
+        rps, threads, dt = cpu_reference(ref, reads, n_sample, steps, min(warm, 1),
+                                         1 if args.seeder == "lt13" else 0)
         line = {
-            "impl": "reference", "metric": METRIC, "value": rps, "unit": "reads/s",
+            "impl": "reference", "metric": metric_for(args), "value": rps, "unit": "reads/s",
             "n_gpus": args.gpus, "steps": steps, "warmup": warm,
             "ms_per_step": dt * 1e3 / steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-            "config": {"workload": desc, "sample_reads_per_step": n_sample},
+            "config": {"workload": desc, "seeder": args.seeder,
+                       "sample_reads_per_step": n_sample},
             "cpu_baseline": {"value": rps, "unit": "reads/s", "cores": threads, "kind": "port",
                              "sample": f"{n_sample} reads of the workload per step"},
             "e2e": {"value": rps, "unit": "reads/s", "h2d_bytes_per_step": 0,
@@ -356,9 +368,11 @@ def main():
     index_s = time.perf_counter() - t0
     rd = ctx.reads(reads)
     peak_cells = ctx.peak_dpx_cells_per_s()
+    seeder = 1 if args.seeder == "lt13" else 0
+    params = sg.default_params(seeder=seeder)
     stats = []
     for _ in range(max(args.warmup, 3)):
-        out_n, st = ctx.align_resident(idx, rd)
+        out_n, st = ctx.align_resident(idx, rd, params)
     # timed region: K steps bracketed by barrier + synchronize
     if world > 1:
         torch.distributed.barrier()
@@ -367,7 +381,7 @@ def main():
     with ClockSampler(device) as clk:
         e0.record(stream)
         for _ in range(args.steps):
-            out_n, st = ctx.align_resident(idx, rd)
+            out_n, st = ctx.align_resident(idx, rd, params)
             stats.append(st)
         e1.record(stream)
         torch.cuda.synchronize()
@@ -392,14 +406,14 @@ def main():
         cap = int(out_n * 1.1) + (1 << 20)
         out_pinned = torch.empty(cap, dtype=torch.uint8, pin_memory=True)
         for _ in range(2):
-            ctx.align_into(idx, pinned.data_ptr(), len(reads), out_pinned.data_ptr(), cap)
+            ctx.align_into(idx, pinned.data_ptr(), len(reads), out_pinned.data_ptr(), cap, params)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         out_bytes = 0
         host = []
         for _ in range(args.steps):
             out_bytes, est = ctx.align_into(idx, pinned.data_ptr(), len(reads),
-                                            out_pinned.data_ptr(), cap)
+                                            out_pinned.data_ptr(), cap, params)
             host.append(est)
         torch.cuda.synchronize()
         e2e_s = time.perf_counter() - t0
@@ -412,7 +426,7 @@ def main():
         return 0
     cpu = None
     try:
-        rps, threads, dt = cpu_reference(ref, reads, min(args.cpu_sample, n), 1, 0)
+        rps, threads, dt = cpu_reference(ref, reads, min(args.cpu_sample, n), 1, 0, seeder)
         cpu = {"value": rps, "unit": "reads/s", "cores": threads, "kind": "port",
                "sample": f"{min(args.cpu_sample, n)} reads of the workload, index prebuilt"}
     except Exception as ex:  # the baseline must not break the GPU line
@@ -424,12 +438,13 @@ def main():
     peak = peak_cells / 1e9
     fast_pairs = stats[-1]["records"] - stats[-1]["sw_generic_pairs"]
     line = {
-        "metric": METRIC, "value": value, "unit": "reads/s", "n_gpus": world,
+        "metric": metric_for(args), "value": value, "unit": "reads/s", "n_gpus": world,
         "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "int16x2" if stats[-1]["sw_generic_pairs"] < stats[-1]["records"] else "int32",
         "data": "synthetic",
-        "config": {"workload": desc, "l2": "inputs larger than L2 (reads %.0f MB, index %.0f MB)"
+        "config": {"workload": desc, "seeder": args.seeder,
+                   "l2": "inputs larger than L2 (reads %.0f MB, index %.0f MB)"
                    % (len(reads) / 1e6, (2 * 4 ** 12 * 4 + 8 * idx.info()["total"]) / 1e6),
                    "records_per_step": stats[-1]["records"],
                    "printed_per_step": stats[-1]["printed"],
@@ -442,6 +457,7 @@ def main():
         "phase_ms": {k: statistics.median(s[k] for s in stats)
                      for k in ("seed_ms", "pairs_ms", "sw_ms", "select_ms", "traceback_ms",
                                "format_ms", "total_ms")},
+        "seed_overflow_strands": stats[-1]["seed_overflow_strands"],
         "roofline": {"bound": "dpx", "kernel": "sw_bound_kernel (score bound of every pair)",
                      "achieved": achieved, "peak": peak,
                      "unit": "Gcells/s", "frac": achieved / peak if peak and achieved else None,

@@ -400,7 +400,8 @@ int run_seed(swift_ctx* ctx, const swift_index* idx, const swift_reads* rd, int 
     s13.reads = rd->d_bytes;
     s13.rd = rd->d_rd;
     s13.n_reads = n;
-    s13.offsets = idx->d_offsets;
+    s13.groups = idx->d_groups;
+    s13.cstart = idx->d_cstart;
     s13.vals = idx->d_vals13;
     s13.map = idx->d_map13;
     s13.tbase = idx->d_tbase13;

@@ -159,7 +159,8 @@ struct Seed13Args {
   const char* reads;
   const DevRead* rd;
   int64_t n_reads;
-  const uint32_t* offsets;    // bucket starts of the SSAHA index
+  const uint4* groups;        // compact bucket directory of the SSAHA index
+  const uint32_t* cstart;
   const int32_t* vals;        // composites per posting
   const int32_t* map;         // refPosHashMap per tuple id
   const int64_t* tbase;       // per reference: first tuple id

@@ -70,9 +70,11 @@ __device__ __forceinline__ int rand13(uint32_t* seed) {
 template <int CAP, int GCAP>
 struct WarpBuf {
   char q[kQBuf];
+  uint32_t packed[kQBuf / 16 + 2];  // 2-bit codes of q, 16 per word
   int32_t qh[kQBuf];
   int32_t hoff[kQBuf + 1];   // exclusive prefix of hits per tuple offset
   uint32_t hstart[kQBuf];    // bucket start per tuple offset
+  int16_t ht[kQBuf];         // tuple offsets with hits, in order
   int16_t snm[GCAP];         // staged extension results
   int32_t spos[GCAP];
   int16_t nm[CAP];           // numMatches_shr (live part)
@@ -124,24 +126,39 @@ __global__ void __launch_bounds__(kWarps * 32) seed13_kernel(Seed13Args a) {
     const int n_inc = n_tup >= -1 ? n_tup + 2 : 0;  // offsets 0 .. Q - k + 2
     const int last = (Q / k) * k;
     const int xh = max(n_inc, last);
+    // getHash13_gpu: sum 4^i code(q[x + i]) is the 2k-bit little-endian
+    // field at bit 2x of the packed codes
+    for (int w = lane; w < kQBuf / 16 + 2; w += 32) {
+      uint32_t v = 0;
+      if (w < kQBuf / 16)
+        for (int i = 0; i < 16; ++i) v |= code13((uint8_t)b.q[16 * w + i]) << (2 * i);
+      b.packed[w] = v;
+    }
+    __syncwarp();
+    const uint64_t hmask = (1ull << (2 * k)) - 1;
     for (int x = lane; x < xh; x += 32) {
-      uint32_t h = 0, p = 1;
-      for (int i = 0; i < k; ++i) {
-        h += p * code13((uint8_t)b.q[x + i]);
-        p <<= 2;
-      }
-      b.qh[x] = (int32_t)h;
+      const int wi = x >> 4;
+      const uint64_t two = (uint64_t)b.packed[wi] | ((uint64_t)b.packed[wi + 1] << 32);
+      b.qh[x] = (int32_t)((two >> (2 * (x & 15))) & hmask);
     }
     __syncwarp();
     // hits per tuple offset and their prefix
-    int carry = 0;
+    int carry = 0, nht = 0;
     for (int x0 = 0; x0 < n_inc; x0 += 32) {
       const int x = x0 + lane;
       int nh = 0;
       if (x < n_inc) {
+        // compact bucket directory: occupancy bits and rank per 64 buckets,
+        // then the starts of occupied buckets
         const uint32_t h = (uint32_t)b.qh[x];
-        const uint32_t s0 = a.offsets[h];
-        nh = (int)(a.offsets[h + 1] - s0);
+        const uint4 grp = __ldg(&a.groups[h >> 6]);
+        const uint64_t bits = ((uint64_t)grp.y << 32) | grp.x;
+        uint32_t s0 = 0;
+        if ((bits >> (h & 63)) & 1u) {
+          const uint32_t r = grp.z + (uint32_t)__popcll(bits & ((1ull << (h & 63)) - 1));
+          s0 = __ldg(&a.cstart[r]);
+          nh = (int)(__ldg(&a.cstart[r + 1]) - s0);
+        }
         b.hstart[x] = s0;
       }
       int incl = nh;
@@ -152,22 +169,32 @@ __global__ void __launch_bounds__(kWarps * 32) seed13_kernel(Seed13Args a) {
       }
       if (x < n_inc) b.hoff[x] = carry + incl - nh;
       carry += __shfl_sync(0xffffffffu, incl, 31);
+      // tuple offsets with hits, in order
+      const uint32_t hb = __ballot_sync(0xffffffffu, nh > 0);
+      if (nh > 0) b.ht[nht + __popc(hb & ((1u << lane) - 1))] = (int16_t)x;
+      nht += __popc(hb);
     }
     if (lane == 0) b.hoff[n_inc] = carry;
     __syncwarp();
     // 2-3. extensions in rounds of whole tuples that fit the staging arrays,
-    // then the block's bookkeeping by lane 0
+    // then the block's bookkeeping by lane 0.  Only tuple offsets with hits
+    // change the state: an offset without hits clears the entries past
+    // count, which the next offset with hits overwrites or clears too, so
+    // only a run of them after the last offset with hits is felt (live =
+    // count at the end).
     int count = 0, maxm = 0, live = 0;
     bool over = false;
-    int t0 = 0;
-    while (t0 < n_inc && !over) {
-      int t1 = t0 + 1;
-      if (b.hoff[t1] - b.hoff[t0] > GCAP) {
+    int u0 = 0;
+    while (u0 < nht && !over) {
+      const int base = b.hoff[b.ht[u0]];
+      int u1 = u0 + 1;
+      if (b.hoff[b.ht[u0] + 1] - base > GCAP) {
         over = true;
         break;
       }
-      while (t1 < n_inc && b.hoff[t1 + 1] - b.hoff[t0] <= GCAP) ++t1;
-      const int g0 = b.hoff[t0], g1 = b.hoff[t1];
+      while (u1 < nht && b.hoff[b.ht[u1] + 1] - base <= GCAP) ++u1;
+      const int g0 = base, g1 = b.hoff[b.ht[u1 - 1] + 1];
+      const int t0 = b.ht[u0], t1 = b.ht[u1 - 1] + 1;
       for (int g = g0 + lane; g < g1; g += 32) {
         int lo = t0, hi = t1 - 1;  // the tuple offset holding hit g
         while (lo < hi) {
@@ -206,7 +233,8 @@ __global__ void __launch_bounds__(kWarps * 32) seed13_kernel(Seed13Args a) {
       }
       __syncwarp();
       if (lane == 0) {
-        for (int t = t0; t < t1 && !over; ++t) {
+        for (int u = u0; u < u1 && !over; ++u) {
+          const int t = b.ht[u];
           const int nh = b.hoff[t + 1] - b.hoff[t];
           const int offset = count + nh;
           if (offset > CAP) {
@@ -239,7 +267,11 @@ __global__ void __launch_bounds__(kWarps * 32) seed13_kernel(Seed13Args a) {
       }
       over = __shfl_sync(0xffffffffu, over ? 1 : 0, 0) != 0;
       __syncwarp();
-      t0 = t1;
+      u0 = u1;
+    }
+    if (lane == 0 && nht > 0 && b.ht[nht - 1] < n_inc - 1) {
+      for (int p = count; p < live; ++p) b.nm[p] = -1;
+      live = min(live, count);
     }
     // 4. final selection (lane 0)
     if (lane == 0) {
@@ -270,7 +302,7 @@ __global__ void __launch_bounds__(kWarps * 32) seed13_kernel(Seed13Args a) {
         for (int i = 0; i < n_pick; ++i) {
           int32_t v = -1;
           int c = 0;
-          for (int t = 0; t < kRefThreads && v < 0; ++t)
+          for (int t = 0; t < min(kRefThreads, live) && v < 0; ++t)
             for (int p = t; p < live; p += kRefThreads)
               if (b.nm[p] == fm) {
                 if (c == pick[i]) {
