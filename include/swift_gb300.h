@@ -119,6 +119,22 @@ int swift_index_build(swift_ctx *ctx, const char *ref_fasta, size_t len,
                       int32_t seed_len, int32_t ignore_thres,
                       swift_index **out);
 int swift_index_destroy(swift_index *idx);
+
+/* Index persistence for warm starts.  swift_index_save writes the index to
+ * one binary file: what lookupTable13Create2 reads back in the reference
+ * (bucket starts and counts, composite values, refPosHashMap;
+ * src/lookupTable13.cu:257-322, there three text files) together with the
+ * reference bytes, sequence records, SSAHA postings, bucket directory and
+ * packed sequence, so swift_index_load rebuilds the index on the context's
+ * device without parsing or hashing the reference again.  The lt13 tables
+ * are included when they were built.  Loading refuses (SWIFT_E_INPUT) a
+ * file whose magic, version, section sizes or checksum do not match;
+ * SWIFT_E_ARG when the file cannot be opened. */
+int swift_index_save(swift_ctx *ctx, const swift_index *idx, const char *path);
+int swift_index_load(swift_ctx *ctx, const char *path, swift_index **out);
+/* The seed length and ignore threshold an index was built with. */
+int swift_index_params(swift_ctx *ctx, const swift_index *idx, int32_t *seed_len,
+                       int32_t *ignore_thres);
 /* Index contents in the reference layout (src/lookupTable5.cu:199-231):
  * lookup[h] is the 1-based start of bucket h or 0; ref_idx/ref_pos have
  * total+1 entries with slot 0 = -1.  Any pointer may be NULL. */

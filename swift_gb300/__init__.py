@@ -22,7 +22,8 @@ EXPORTS = [
     "swift_params_default", "swift_ctx_create", "swift_ctx_destroy", "swift_last_error",
     "swift_ctx_info", "swift_ctx_set_sw_path",
     "swift_index_build", "swift_index_destroy", "swift_index_info", "swift_index_export",
-    "swift_seed", "swift_seed_lt13", "swift_sw_batch", "swift_align", "swift_reads_upload",
+    "swift_seed", "swift_seed_lt13", "swift_index_save", "swift_index_load",
+    "swift_index_params", "swift_sw_batch", "swift_align", "swift_reads_upload",
     "swift_reads_destroy", "swift_align_resident", "swift_fetch_output",
     "swift_align_files", "swift_free", "swift_peak_dpx", "swift_align_into",
     "swift_sw_batch_noalloc", "swift_sw_pairs", "swift_server_create", "swift_server_submit",
@@ -109,6 +110,9 @@ def lib():
         L.swift_index_export.argtypes = [vp, vp, vp, vp, vp, vp]
         L.swift_seed.argtypes = [vp, vp, C.c_char_p, sz, i32, vp, i64, C.POINTER(i64)]
         L.swift_seed_lt13.argtypes = [vp, vp, C.c_char_p, sz, vp, i64, C.POINTER(i64)]
+        L.swift_index_save.argtypes = [vp, vp, C.c_char_p]
+        L.swift_index_load.argtypes = [vp, C.c_char_p, C.POINTER(vp)]
+        L.swift_index_params.argtypes = [vp, vp, C.POINTER(i32), C.POINTER(i32)]
         L.swift_sw_batch.argtypes = [vp, vp, vp, i32, i32, i64, i32, i32, i32, i32,
                                      vp, vp, vp, vp, vp, vp]
         L.swift_align.argtypes = [vp, vp, vp, sz, C.POINTER(Params), C.POINTER(vp),
@@ -370,14 +374,31 @@ class Server:
 class Index:
     """Device-resident reference (FASTA bytes, 2-bit codes) and SSAHA index."""
 
-    def __init__(self, ctx: Context, ref_fasta: bytes, seed_len=12, ignore_thres=1000):
-        h = C.c_void_p()
-        ctx._check(lib().swift_index_build(ctx._h, ref_fasta, len(ref_fasta), seed_len,
-                                           ignore_thres, C.byref(h)))
+    def __init__(self, ctx: Context, ref_fasta: bytes | None, seed_len=12, ignore_thres=1000,
+                 _handle=None):
+        if _handle is None:
+            h = C.c_void_p()
+            ctx._check(lib().swift_index_build(ctx._h, ref_fasta, len(ref_fasta), seed_len,
+                                               ignore_thres, C.byref(h)))
+        else:
+            h = _handle
+            k, t = C.c_int32(), C.c_int32()
+            ctx._check(lib().swift_index_params(ctx._h, h, C.byref(k), C.byref(t)))
+            seed_len, ignore_thres = k.value, t.value
         self._h = h
         self.ctx = ctx
         self.seed_len = seed_len
         self.ignore_thres = ignore_thres
+
+    @classmethod
+    def load(cls, ctx: Context, path: str) -> "Index":
+        """An index saved by Index.save, rebuilt on ctx's device."""
+        h = C.c_void_p()
+        ctx._check(lib().swift_index_load(ctx._h, path.encode(), C.byref(h)))
+        return cls(ctx, None, _handle=h)
+
+    def save(self, path: str):
+        self.ctx._check(lib().swift_index_save(self.ctx._h, self._h, path.encode()))
 
     def info(self):
         nr, tot, nb = C.c_int32(), C.c_int64(), C.c_int64()

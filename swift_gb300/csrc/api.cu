@@ -12,63 +12,11 @@
 #include <string>
 #include <vector>
 
+#include "handles.h"
 #include "internal.h"
 
 
 using namespace swift;
-
-struct swift_ctx {
-  int device = 0;
-  cudaStream_t st = nullptr;
-  bool own_stream = false;
-  std::string err;
-  int64_t total_mem = 0;
-  cudaEvent_t ev[10] = {};
-  char* d_text = nullptr;
-  size_t text_len = 0, text_cap = 0;
-  int sw_path = 0;  // 0 bounded selection, 1 generic kernel only, 2 exact score of every pair
-  cudaStream_t side = nullptr;  // second stream for concurrent launches, made on first use
-  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
-};
-
-struct swift_index {
-  int device = 0;
-  int k = 12, thres = 1000;
-  char* d_file = nullptr;
-  uint64_t file_len = 0;
-  DevRecord* d_recs = nullptr;
-  std::vector<RefRecord> recs;
-  uint8_t* d_cat = nullptr;
-  uint32_t* d_packed = nullptr;
-  uint64_t cat_len = 0;
-  uint32_t* d_count = nullptr;
-  uint32_t* d_offsets = nullptr;
-  uint4* d_groups = nullptr;   // compact bucket directory for seeding
-  uint32_t* d_cstart = nullptr;
-  uint2* d_post = nullptr;
-  int64_t total = 0;
-  int64_t nb = 0;
-  // lt13 seeding (seed13.cu), built on first use
-  std::mutex lt13_mu;
-  bool lt13_ready = false;
-  int32_t* d_vals13 = nullptr;   // composite per posting
-  int32_t* d_map13 = nullptr;    // refPosHashMap per tuple id
-  int64_t* d_tbase13 = nullptr;  // per reference: first tuple id, tuples
-  int64_t* d_ntup13 = nullptr;
-  int64_t max_comp13 = 0;
-};
-
-struct swift_reads {
-  int device = 0;
-  char* d_bytes = nullptr;
-  uint64_t len = 0;
-  DevRead* d_rd = nullptr;
-  int64_t n = 0;          // reads
-  int64_t n_gt = 0;       // '>' bytes (getSeqCount)
-  int32_t first_len = 0;  // getSeqSize
-  int32_t min_len = 0, max_len = 0;
-  std::vector<int32_t> repeats;
-};
 
 namespace {
 
@@ -370,6 +318,7 @@ int ensure_lt13(swift_ctx* ctx, const swift_index* cidx) {
   CKLAUNCH();
   CK(cudaStreamSynchronize(st));
   idx->max_comp13 = max_comp;
+  idx->n_tup13 = n_tup;
   idx->lt13_ready = true;
   return SWIFT_OK;
 }
