@@ -96,6 +96,11 @@ def lib():
                                 C.POINTER(Params), C.POINTER(C.c_void_p),
                                 C.POINTER(C.c_int), C.c_char_p, C.c_size_t]
         L.so_free.argtypes = [C.c_void_p]
+        L.so_phase1_paired.argtypes = [C.c_char_p, C.c_size_t] * 3 + [
+            C.POINTER(Params), C.POINTER(C.c_void_p), C.POINTER(C.c_long), C.c_char_p, C.c_size_t]
+        L.so_align_paired.argtypes = [C.c_char_p, C.c_size_t] * 3 + [
+            C.POINTER(Params), C.c_uint, C.c_uint, C.POINTER(C.c_void_p), C.POINTER(C.c_size_t),
+            C.c_char_p, C.c_size_t]
         L.so_lt13_map.argtypes = [C.c_char_p, C.c_size_t, C.c_int, C.c_int, C.c_char_p, C.c_int,
                                   C.c_void_p, C.c_void_p, C.c_char_p, C.c_size_t]
         L.so_session_create.argtypes = [C.c_char_p, C.c_size_t, C.POINTER(Params),
@@ -277,3 +282,35 @@ class Session:
         if getattr(self, "_h", None):
             lib().so_session_free(self._h)
             self._h = None
+
+
+def phase1_paired(ref: bytes, reads1: bytes, reads2: bytes, params: Params | None = None):
+    """Paired-end Phase-1 records: (id, rev, mate, ref_idx, shift, offset, read)."""
+    p = params or default_params()
+    out = C.c_void_p()
+    n = C.c_long()
+    err = C.create_string_buffer(512)
+    rc = lib().so_phase1_paired(ref, len(ref), reads1, len(reads1), reads2, len(reads2),
+                                C.byref(p), C.byref(out), C.byref(n), err, 512)
+    if rc != 0:
+        raise OracleError(err.value.decode())
+    a = C.cast(out, C.POINTER(C.c_int32))
+    res = [tuple(a[7 * i + f] for f in range(7)) for i in range(n.value)]
+    lib().so_free(out)
+    return res
+
+
+def align_paired(ref: bytes, reads1: bytes, reads2: bytes, params: Params | None = None,
+                 min_frag: int = 99, max_frag: int = 600) -> bytes:
+    """The paired-end pipeline's output (MIN/MAX_FRAG_SIZE defaults)."""
+    p = params or default_params()
+    out = C.c_void_p()
+    n = C.c_size_t()
+    err = C.create_string_buffer(512)
+    rc = lib().so_align_paired(ref, len(ref), reads1, len(reads1), reads2, len(reads2),
+                               C.byref(p), min_frag, max_frag, C.byref(out), C.byref(n), err, 512)
+    if rc != 0:
+        raise OracleError(err.value.decode())
+    res = C.string_at(out, n.value)
+    lib().so_free(out)
+    return res

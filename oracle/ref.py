@@ -36,6 +36,9 @@ def lib():
         L.ref_pipeline.restype = C.c_long
         L.ref_pipeline_fmt.argtypes = L.ref_pipeline.argtypes + [i, i]
         L.ref_pipeline_fmt.restype = C.c_long
+        L.ref_pipeline_paired.argtypes = [C.c_char_p] * 5 + [C.c_longlong, i, f, f, f, f, i,
+                                                             C.c_uint, C.c_uint]
+        L.ref_pipeline_paired.restype = C.c_long
         _lib = L
     return _lib
 
@@ -133,4 +136,23 @@ def pipeline_with_matches(ref: bytes, reads: bytes, device_mem: int, seed_len=12
     for line in open(mp, "rb").read().splitlines():
         f = line.split(b"\t")
         recs.append((f[0].decode(), int(f[1]), int(f[2]), int(f[3]), int(f[4])))
+    return open(op, "rb").read(), recs
+
+
+def pipeline_paired(ref: bytes, reads1: bytes, reads2: bytes, device_mem: int, seed_len=12,
+                    m=2, x=-1, o=-10, e=-1, out_format=0, min_frag=99, max_frag=600):
+    """The reference's paired-end pipeline (-q/-q2) file to file:
+    (output bytes, Phase-1 records [(id, name, rev, mate, ref_idx, shift, offset)])."""
+    rp, q1, q2, op, mp = (_tmp(n) for n in ("pe_ref.fa", "pe_1.fa", "pe_2.fa", "pe_out.txt",
+                                            "pe_match.txt"))
+    open(rp, "wb").write(ref)
+    open(q1, "wb").write(reads1)
+    open(q2, "wb").write(reads2)
+    lib().ref_pipeline_paired(rp.encode(), q1.encode(), q2.encode(), op.encode(), mp.encode(),
+                              device_mem, seed_len, m, x, o, e, out_format, min_frag, max_frag)
+    recs = []
+    for line in open(mp, "rb").read().splitlines():
+        f = line.split(b"\t")
+        recs.append((int(f[0]), f[1].decode(), int(f[2]), int(f[3]), int(f[4]), int(f[5]),
+                     int(f[6])))
     return open(op, "rb").read(), recs

@@ -13,7 +13,12 @@
  *     batch sizing of getNumQueriesPerIteration (src/align.cu:2767-2793);
  *   - chooseBestAlignment (src/align.cu:844-905) with the first maximum kept;
  *   - the query loop of search2Queries (src/search2.cu:176-256) and its
- *     printHeuristicMatches (src/search2.cu:339-377), both static there.
+ *     printHeuristicMatches (src/search2.cu:339-377), both static there;
+ *   - the paired-end loops of searchQueries_paired2 (src/search.cu:2084-2200,
+ *     with printHeuristicMatches3, src/search.cu:1848-1860) and
+ *     alignQueries_paired2 (src/align.cu:1879-2110), calling the reference's
+ *     lookupTable2, getOffsets_paired2, getSeq, chooseBestAlignment_paired3
+ *     and printOutput_paired2.
  * The GPU kernels smithWaterman (src/smithWaterman.cu:360-395) and
  * lookupTable13MapQry2_gpu (src/lookupTable13.cu:646-868) run on the CPU:
  * one fiber per CUDA thread, __syncthreads() yields to the next fiber.
@@ -30,7 +35,9 @@
 
 #include "common.h"
 #include "input.h"
+#include "hitList.h"
 #include "lookupTable13.h"
+#include "lookupTable2.h"
 #include "lookupTable5.h"
 #include "mapHits6.h"
 #include "output.h"
@@ -78,6 +85,8 @@ static unsigned g_rand = 0;
 /* stands in for rand() in array.cu (arrGetRandomNums): 0, 1, 2, ... so the
  * random biggest-cluster picks of mapHits6 become the first ones */
 extern "C" int ref_rand(void) { return (int)(g_rand++); }
+extern "C" int ref_rand_zero(void) { return 0; }
+long long ref_device_mem = 288000000000LL;
 
 static ucontext_t g_main;
 static std::vector<ucontext_t> g_fib;
@@ -431,6 +440,133 @@ long ref_pipeline(const char *ref_file, const char *qry_file, const char *out_fi
                   float m, float x, float o, float e) {
   return ref_pipeline_fmt(ref_file, qry_file, out_file, match_file, device_mem, seed_len, thres,
                           m, x, o, e, DEFAULT_OUTPUT_FORMAT, 0);
+}
+
+}  // extern "C"
+
+/* prototypes of align.cu's exported functions, C++ linkage as the reference
+ * compiles them (align.h also declares its static helpers) */
+int getMemPerRefQryPair(int refLength, int queryLength);
+int getNumQueriesPerIteration_paired(cudaDeviceProp *deviceProp, int memPerRefQueryPair,
+                                     int numTotalQueries);
+void chooseBestAlignment_paired3_wrap(char *qryName, int qryNameLen, uint *revComp,
+                                      char *refName, int refNameLen, float *score,
+                                      int *refDistance, int *alignStart, int *alignEnd, int size,
+                                      uint minFragSize, uint maxFragSize);
+void getNumQrsPerIter_paired_wrap(const char *file, int maxNumQrsPerIter, int **numQrsPerIter,
+                                  int *arrSize);
+
+extern "C" {
+
+/* The paired-end pipeline of src/main.cu:172-212 (GPU branch), file to
+ * file.  Returns the number of match records. */
+long ref_pipeline_paired(const char *ref_file, const char *q1_file, const char *q2_file,
+                         const char *out_file, const char *match_file, long long device_mem,
+                         int seed_len, float m, float x, float o, float e, int out_format,
+                         unsigned min_frag, unsigned max_frag) {
+  preprocessCreate();
+  const int num_qrs = getSeqCount((char *)q1_file);
+  const int qry_len = getSeqSize((char *)q1_file);
+  refMapCreate(ref_file);
+  /* Phase 1: searchQueries_paired2 */
+  lookupTable2Create(ref_file, seed_len, MAX_NUM_HITS_PAIRED_END, TUPLE_IGNORE_THRES);
+  Query *qry1 = qryCreate2(), *qry2 = qryCreate2();
+  FILE *mf = fopen(match_file, "w");
+  FILE *f1 = fopen(q1_file, "r"), *f2 = fopen(q2_file, "r");
+  long num_matches = 0;
+  for (int i = 0, id = 0; i < num_qrs; ++i) {
+    qry1 = qryGetNext2(f1, qry1);
+    qry2 = qryGetNext2(f2, qry2);
+    ++id;
+    Query *mate[2] = {qry1, qry2};
+    for (int mi = 0; mi < 2; ++mi)
+      for (int rc = 0; rc < 2; ++rc) {
+        g_rand = 0;
+        HitList *best = lookupTable2MapQry(mate[mi], (uint)qry_len, (uint)rc);
+        for (HitList *h = best; h != NULL; h = h->next) {
+          fprintf(mf, "%d\t%s\t%d\t%d\t%d\t%d\t%d\t%u\t%u\n", id, mate[mi]->name, rc, mi + 1,
+                  h->index, h->shift, h->offset, (uint)mate[mi]->nameOffset,
+                  (uint)mate[mi]->seqOffset);
+          ++num_matches;
+        }
+        if (best != NULL) hitListDelete(best);
+      }
+  }
+  fclose(mf);
+  fclose(f1);
+  fclose(f2);
+  lookupTable2Delete();
+  /* Phase 2: alignQueries_paired2 */
+  ref_device_mem = device_mem;
+  const int Q = qry_len, R = 3 * qry_len, comb = R + Q + 2;
+  cudaDeviceProp prop;
+  cudaGetDeviceProperties(&prop, 0);
+  const int max_qrs = getNumQueriesPerIteration_paired(&prop, getMemPerRefQryPair(R, Q),
+                                                       (int)num_matches);
+  int *per_iter = NULL, n_iter = 0;
+  getNumQrsPerIter_paired_wrap(match_file, max_qrs, &per_iter, &n_iter);
+  const size_t cap = max_qrs > 0 ? (size_t)max_qrs : 1;
+  std::vector<float> score(cap);
+  std::vector<int> dist(cap), st(cap), en(cap), ln(cap), qidx(cap);
+  std::vector<uint> rev(cap);
+  std::vector<char> rcons(cap * comb), qcons(cap * comb);
+  std::vector<char> qname(cap * MAX_SEQ_NAME_LENGTH), rname(cap * MAX_SEQ_NAME_LENGTH);
+  std::vector<char> qseq(cap * (Q + 1), 0), rseq(cap * (R + 1), 0);
+  std::vector<char> tmpq(Q + 1, 0);
+  mf = fopen(match_file, "r");
+  f1 = fopen(q1_file, "r");
+  f2 = fopen(q2_file, "r");
+  FILE *rfp = fopen(ref_file, "r");
+  FILE *of = fopen(out_file, "w");
+  for (int it = 0; it < n_iter; ++it) {
+    const int cnt = per_iter[it];
+    memset(rseq.data(), 0, rseq.size());
+    for (int j = 0; j < cnt; ++j) {
+      uint qno, qso, rno, rso, rfo;
+      int mate, ridx;
+      getOffsets_paired2(mf, &qno, &qso, &mate, &rno, &rso, &rfo, &dist[j], &rev[j], &ridx,
+                         &qidx[j]);
+      dist[j] = dist[j] - Q > 0 ? dist[j] - Q : 0;
+      refMapGetOffsets(ridx, dist[j], &rno, &rfo);
+      getSeq(rfp, rfo, rseq.data() + (size_t)j * (R + 1), R);
+      getSeqName(rfp, rno, rname.data() + (size_t)j * MAX_SEQ_NAME_LENGTH);
+      FILE *qf = mate == 1 ? f1 : f2;
+      if (rev[j] == 1) {
+        getSeq(qf, qso, tmpq.data(), Q);
+        qryGetReverseComplement(tmpq.data(), Q, qseq.data() + (size_t)j * (Q + 1));
+        getSeqName(qf, qno, qname.data() + (size_t)j * MAX_SEQ_NAME_LENGTH);
+        strcat(qname.data() + (size_t)j * MAX_SEQ_NAME_LENGTH, "*");
+      } else {
+        getSeq(qf, qso, qseq.data() + (size_t)j * (Q + 1), Q);
+        getSeqName(qf, qno, qname.data() + (size_t)j * MAX_SEQ_NAME_LENGTH);
+      }
+    }
+    for (int j = 0; j < cnt; ++j) score[j] = 0;
+    g_args = KernelArgs{rseq.data(), R, qseq.data(), Q, m, x, o, e, score.data(), st.data(),
+                        en.data(), ln.data(), rcons.data(), qcons.data()};
+    const int T = Q + 1 > R ? Q + 1 : R;
+    for (int j = 0; j < cnt; ++j) run_block(T, j);
+    if (out_format == SAM_OUTPUT_FORMAT) {
+      printOutputSam(cnt, qname.data(), rname.data(), score.data(), st.data(), en.data(),
+                     ln.data(), comb, qcons.data(), rcons.data(), of);
+    } else {
+      chooseBestAlignment_paired3_wrap(qname.data(), MAX_QRY_NAME_LENGTH, rev.data(),
+                                       rname.data(), MAX_REF_NAME_LENGTH, score.data(),
+                                       dist.data(), st.data(), en.data(), cnt, min_frag,
+                                       max_frag);
+      printOutput_paired2(cnt, qidx.data(), qname.data(), rname.data(), score.data(),
+                          dist.data(), st.data(), en.data(), ln.data(), comb, qcons.data(),
+                          rcons.data(), of);
+    }
+  }
+  fclose(mf);
+  fclose(f1);
+  fclose(f2);
+  fclose(rfp);
+  fclose(of);
+  free(per_iter);
+  refMapFree();
+  return num_matches;
 }
 
 }  // extern "C"

@@ -50,6 +50,12 @@ static inline void *ref13_calloc(size_t n, size_t sz) { return calloc(n + 1024, 
 #define __shared__
 #endif
 
+#ifdef REF_ALIGN
+/* align.cu: device queries answered for one device, rand() pinned to 0 */
+extern "C" int ref_rand_zero(void);
+#define rand ref_rand_zero
+#endif
+
 #ifdef REF_PIN_RAND
 /* array.cu: rand() -> a counter 0, 1, 2, ... reset before each call of
  * interest, which pins mapHits6's random picks to the first clusters */
@@ -71,6 +77,28 @@ extern struct ref_dim3 threadIdx, blockIdx, blockDim, gridDim;
 void __syncthreads(void);
 
 typedef int cudaError_t;
+typedef struct ref_dim3 dim3;
+/* the device align.cu sizes its batches from: ref_device_mem bytes */
+extern long long ref_device_mem;
+struct cudaDeviceProp {
+  size_t totalGlobalMem;
+  int maxGridSize[3];
+  int regsPerBlock;
+  int maxThreadsPerBlock;
+  size_t sharedMemPerBlock;
+};
+static inline cudaError_t cudaGetDeviceProperties(struct cudaDeviceProp *p, int) {
+  memset(p, 0, sizeof(*p));
+  p->totalGlobalMem = (size_t)ref_device_mem;
+  p->maxGridSize[0] = 2147483647;
+  p->regsPerBlock = 65536;
+  p->maxThreadsPerBlock = 1024;
+  p->sharedMemPerBlock = 49152;
+  return 0;
+}
+static inline cudaError_t cudaGetDevice(int *d) { *d = 0; return 0; }
+static inline cudaError_t cudaGetDeviceCount(int *n) { *n = 1; return 0; }
+static inline cudaError_t cudaSetDevice(int) { return 0; }
 enum cudaMemcpyKind {
   cudaMemcpyHostToHost,
   cudaMemcpyHostToDevice,

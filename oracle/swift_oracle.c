@@ -1371,3 +1371,640 @@ int so_session_align(so_session *ss, const char *reads, size_t reads_len,
   *out_len = sb.n;
   return 0;
 }
+
+/* ------------------------------------------------------------------ */
+/* Paired-end pipeline (-q2): the GPU branch of src/main.cu:172-212.    */
+/* Phase 1 searchQueries_paired2 (src/search.cu:2084-2200) on           */
+/* lookupTable2 (src/lookupTable2.cu:75-300): non-overlapping tuples    */
+/* stored as FILE offsets, mapped back by refMapGetIndexAndPos          */
+/* (src/refMap.cu:166-242).  Phase 2 alignQueries_paired2               */
+/* (src/align.cu:1879-2110): windows of 3Q by getSeq, mate pairs chosen */
+/* by chooseBestAlignment_paired3 (src/align.cu:1248-1422), records by  */
+/* printOutput_paired2 (src/output.cu:300-362).                          */
+
+#define SO_PE_THRES 1000   /* TUPLE_IGNORE_THRES, src/common.h:75          */
+#define SO_PE_HITS 3       /* MAX_NUM_HITS_PAIRED_END, src/common.h:63     */
+
+typedef struct {
+  int k, nb;
+  int *lookup, *repeats;
+  uint32_t *fileoff;       /* total + 1; [0] unused                        */
+} so_pe_index;
+
+static void so_pe_index_free(so_pe_index *t) {
+  if (!t) return;
+  free(t->lookup);
+  free(t->repeats);
+  free(t->fileoff);
+  free(t);
+}
+
+/* lookupTable2Create's loop over the reference lines (src/lookupTable2.cu:
+ * 99-168): tuples at 0, k, 2k of each line buffer (carried bases first),
+ * file offset = header end + bases + line count, one less for the first
+ * tuple written after a carry. */
+static so_pe_index *so_pe_index_build(const char *b, size_t n, int k) {
+  so_pe_index *t = (so_pe_index *)calloc(1, sizeof(so_pe_index));
+  t->k = k;
+  t->nb = 1 << (2 * k);
+  t->lookup = (int *)calloc((size_t)t->nb, sizeof(int));
+  t->repeats = (int *)calloc((size_t)t->nb, sizeof(int));
+  int *nrep = (int *)calloc((size_t)t->nb, sizeof(int));
+  size_t cap = 1024, nw = 0;
+  int *wh = (int *)malloc(cap * sizeof(int));
+  uint32_t *wo = (uint32_t *)malloc(cap * sizeof(uint32_t));
+  char *line = (char *)malloc(2 * SO_LINE_MAX + 16);
+  long total = 0;
+  int offset = 0, num_bases = 0, num_nl = 0;
+  uint32_t ref_pos = 0;
+  size_t pos = 0, c;
+  while ((c = so_chunk(b, n, pos)) > 0) {
+    memcpy(line + offset, b + pos, c);
+    line[offset + c] = '\0';
+    pos += c;
+    int ll = offset + (int)c;
+    if (line[ll - 1] == '\n') line[--ll] = '\0';
+    if (ll == 0) {
+      offset = 0;
+    } else if (line[offset] == '>') {
+      offset = 0;
+      num_bases = 0;
+      num_nl = 0;
+      ref_pos = (uint32_t)pos;  /* ftell after the header line */
+    } else {
+      int iters = ll - k + 1, i;
+      for (i = 0; i < iters; i += k) {
+        int h = so_hash(line + i, k);
+        ++t->repeats[h];
+        if (t->repeats[h] <= SO_PE_THRES) {
+          ++nrep[h];
+          ++total;
+          if (nw == cap) {
+            cap *= 2;
+            wh = (int *)realloc(wh, cap * sizeof(int));
+            wo = (uint32_t *)realloc(wo, cap * sizeof(uint32_t));
+          }
+          wh[nw] = h;
+          if (offset > 0) {
+            wo[nw] = ref_pos + (uint32_t)num_bases + (uint32_t)i + (uint32_t)num_nl - 1u;
+            offset = 0;
+          } else {
+            wo[nw] = ref_pos + (uint32_t)num_bases + (uint32_t)i + (uint32_t)num_nl;
+          }
+          ++nw;
+        } else if (t->repeats[h] == nrep[h] + 1) {
+          nrep[h] = 0;
+          total -= SO_PE_THRES;
+        }
+      }
+      num_bases += ll;
+      ++num_nl;
+      offset = ll - i;
+      memmove(line, line + i, (size_t)(offset > 0 ? offset : 0));
+      if (offset < 0) offset = 0;
+      num_bases -= offset;
+    }
+  }
+  t->fileoff = (uint32_t *)calloc((size_t)total + 1, sizeof(uint32_t));
+  t->fileoff[0] = UINT32_MAX;
+  int start = 1;
+  for (int h = 0; h < t->nb; ++h)
+    if (t->repeats[h] > 0 && t->repeats[h] <= SO_PE_THRES) {
+      t->lookup[h] = start;
+      start += t->repeats[h];
+    }
+  for (size_t w = 0; w < nw; ++w) {
+    int h = wh[w];
+    if (t->repeats[h] <= SO_PE_THRES) {
+      int idx = t->lookup[h] + nrep[h] - 1;
+      t->fileoff[idx] = wo[w];
+      --nrep[h];
+    }
+  }
+  free(wh);
+  free(wo);
+  free(line);
+  free(nrep);
+  return t;
+}
+
+/* refMapGetIndexAndPos (src/refMap.cu:166-242) */
+static void so_pe_index_pos(const so_ref *r, uint32_t off, int *index, int *pos) {
+  int idx = -1;
+  if (r->recs[0].seq_off == off) {
+    *index = 0;
+    *pos = 0;
+    return;
+  }
+  if (r->n == 1) {
+    idx = 0;
+  } else {
+    for (int i = 1; i < r->n; ++i) {
+      if (r->recs[i - 1].seq_off == off) {
+        *index = i - 1;
+        *pos = 0;
+        return;
+      } else if (r->recs[i].seq_off > off) {
+        idx = i - 1;
+        break;
+      }
+    }
+    if (idx == -1) idx = r->n - 1;
+  }
+  const uint32_t so = (uint32_t)r->recs[idx].seq_off;
+  const uint32_t bpl = r->recs[idx].bpl;
+  if (bpl == 0) {
+    *pos = (int)(off - so);
+  } else {
+    uint32_t tmp = so;
+    int nl = 0;
+    while (tmp + bpl + 1 <= off) {
+      tmp += bpl + 1;
+      ++nl;
+    }
+    *pos = (int)(off - so) - nl;
+  }
+  *index = idx;
+}
+
+typedef struct {
+  int8_t index;
+  int32_t shift, offset;
+  long order;
+} so_pe_hit;
+
+static int so_pe_hit_cmp(const void *a, const void *b) {
+  const so_pe_hit *x = (const so_pe_hit *)a, *y = (const so_pe_hit *)b;
+  if (x->index != y->index) return x->index < y->index ? -1 : 1;
+  if (x->shift != y->shift) return x->shift < y->shift ? -1 : 1;
+  if (x->offset != y->offset) return x->offset < y->offset ? -1 : 1;
+  return x->order < y->order ? -1 : x->order > y->order; /* a stable merge sort */
+}
+
+/* lookupTable2MapQry (src/lookupTable2.cu:247-300) with getBestScoringPosition
+ * (src/lookupTable2.cu:308-452): the first node of the first min(3, n) largest
+ * clusters (the random picks pinned to the first ones) */
+static int so_pe_map(const so_pe_index *t, const so_ref *r, const char *seq, int Q,
+                     int8_t *ri, int32_t *sh, int32_t *off) {
+  const int k = t->k;
+  int nq = Q - k + 1;
+  long cap = 0, nh = 0;
+  for (int i = 0; i < nq; ++i) {
+    int h = so_hash(seq + i, k);
+    if (t->repeats[h] > SO_PE_THRES) continue;
+    cap += t->repeats[h];
+  }
+  so_pe_hit *hits = (so_pe_hit *)malloc((size_t)(cap > 0 ? cap : 1) * sizeof(so_pe_hit));
+  for (int i = 0; i < nq; ++i) {
+    int h = so_hash(seq + i, k);
+    if (t->repeats[h] > SO_PE_THRES) continue;
+    int s0 = t->lookup[h], e0 = s0 + t->repeats[h] - 1;
+    for (int j = s0; j <= e0; ++j) {
+      int idx, p;
+      so_pe_index_pos(r, t->fileoff[j], &idx, &p);
+      hits[nh].index = (int8_t)idx;
+      hits[nh].shift = p - i;
+      hits[nh].offset = p;
+      hits[nh].order = nh;
+      ++nh;
+    }
+  }
+  int n = 0;
+  if (nh == 1) {
+    ri[0] = hits[0].index;
+    sh[0] = hits[0].shift;
+    off[0] = hits[0].offset;
+    n = 1;
+  } else if (nh > 1) {
+    qsort(hits, (size_t)nh, sizeof(so_pe_hit), so_pe_hit_cmp);
+    int maxsz = 0, nmax = 0;
+    for (long a = 0; a < nh;) {
+      long e = a;
+      while (e + 1 < nh && hits[e + 1].index == hits[a].index && hits[e + 1].shift == hits[a].shift) ++e;
+      int sz = (int)(e - a + 1);
+      if (sz > maxsz) {
+        maxsz = sz;
+        nmax = 1;
+      } else if (sz == maxsz) {
+        ++nmax;
+      }
+      a = e + 1;
+    }
+    int want = nmax < SO_PE_HITS ? nmax : SO_PE_HITS;
+    for (long a = 0; a < nh && n < want;) {
+      long e = a;
+      while (e + 1 < nh && hits[e + 1].index == hits[a].index && hits[e + 1].shift == hits[a].shift) ++e;
+      if ((int)(e - a + 1) == maxsz) {
+        ri[n] = hits[a].index;
+        sh[n] = hits[a].shift;
+        off[n] = hits[a].offset;
+        ++n;
+      }
+      a = e + 1;
+    }
+  }
+  free(hits);
+  return n;
+}
+
+typedef struct {
+  int32_t id, mate, rev, read;   /* read: index in its mate file */
+  int32_t ref_idx, shift, offset;
+} so_pe_match;
+
+/* searchQueries_paired2's records: per pair id, mate 1 forward, mate 1
+ * reverse, mate 2 forward, mate 2 reverse; Q = getSeqSize of file 1. */
+static int so_pe_phase1(const so_ref *r, const so_pe_index *t, const so_reads *r1,
+                        const so_reads *r2, int Q, so_pe_match **out, long *n_out) {
+  long cap = 64, n = 0;
+  so_pe_match *m = (so_pe_match *)malloc((size_t)cap * sizeof(so_pe_match));
+  char rev[SO_QSEQ_MAX + 1];
+  int8_t ri[SO_PE_HITS];
+  int32_t sh[SO_PE_HITS], of[SO_PE_HITS];
+  for (int i = 0; i < r1->n; ++i) {
+    const so_read *mate[2] = {&r1->r[i], &r2->r[i]};
+    for (int mi = 0; mi < 2; ++mi)
+      for (int rc = 0; rc < 2; ++rc) {
+        const so_read *q = mate[mi];
+        const char *seq = q->seq;
+        if (rc) {
+          so_revcomp(q->seq, q->len, rev);
+          seq = rev;
+        }
+        int nh = so_pe_map(t, r, seq, Q, ri, sh, of);
+        for (int h = 0; h < nh; ++h) {
+          if (n == cap) {
+            cap *= 2;
+            m = (so_pe_match *)realloc(m, (size_t)cap * sizeof(so_pe_match));
+          }
+          m[n].id = i + 1;
+          m[n].mate = mi + 1;
+          m[n].rev = rc;
+          m[n].read = i;
+          m[n].ref_idx = ri[h];
+          m[n].shift = sh[h];
+          m[n].offset = of[h];
+          ++n;
+        }
+      }
+  }
+  *out = m;
+  *n_out = n;
+  return 0;
+}
+
+/* getNumQrsPerIter_paired (src/align.cu:1812-1852) over the record ids */
+static int so_pe_batches(const so_pe_match *m, long n, int max_per, int **out) {
+  int old_count = 0, count = 0, old_id = 0, is_new = 0, size = 0;
+  int *arr = NULL;
+  for (long r = 0; r < n; ++r) {
+    ++count;
+    int id = m[r].id;
+    if (is_new) {
+      is_new = 0;
+      if (id == old_id)
+        arr[size - 1] = old_count;
+      else
+        count = 1;
+    } else if (id != old_id) {
+      old_count = count - 1;
+    }
+    if (count == max_per) {
+      arr = (int *)realloc(arr, (size_t)(size + 1) * sizeof(int));
+      arr[size++] = count;
+      count = count - old_count;
+      is_new = 1;
+    }
+    old_id = id;
+  }
+  if (!is_new && count <= max_per) {
+    arr = (int *)realloc(arr, (size_t)(size + 1) * sizeof(int));
+    arr[size++] = count;
+  }
+  *out = arr;
+  return size;
+}
+
+/* getSeq (src/input.cu:163-204): up to len bytes from the file offset on,
+ * across lines, stopping at a '>' line; out is left untouched when nothing
+ * is read (the caller zeroes it first). */
+static void so_get_seq(const char *b, size_t n, size_t off, char *out, int len) {
+  int cnt = 0, first = 1;
+  size_t pos = off, c;
+  while ((c = so_chunk(b, n, pos)) > 0) {
+    const char *l = b + pos;
+    pos += c;
+    if (l[0] == '>') break;
+    int ll = (int)c - (l[c - 1] == '\n');
+    cnt += ll;
+    if (cnt > len) ll -= cnt - len;
+    if (first) {
+      memcpy(out, l, (size_t)ll);
+      out[ll] = '\0';
+      first = 0;
+    } else {
+      size_t cur = strlen(out);
+      memcpy(out + cur, l, (size_t)ll);
+      out[cur + ll] = '\0';
+    }
+    if (cnt >= len) break;
+  }
+}
+
+/* getMatePairName (src/align.cu:1434-1467): names end in 1 or 2 (the
+ * library refuses others: the reference leaves the previous name there) */
+static void so_pe_mate_name(const char *q, char *mate) {
+  int len = (int)strlen(q) - 1;
+  if (len < 0) return;
+  if (q[len] == '*') {
+    if (len >= 1 && (q[len - 1] == '1' || q[len - 1] == '2')) {
+      memcpy(mate, q, (size_t)(len - 1));
+      mate[len - 1] = q[len - 1] == '1' ? '2' : '1';
+      mate[len] = '\0';
+    }
+  } else if (q[len] == '1' || q[len] == '2') {
+    memcpy(mate, q, (size_t)len);
+    mate[len] = q[len] == '1' ? '2' : '1';
+    mate[len + 1] = '\0';
+  }
+}
+
+typedef struct {
+  char qname[SO_NAME_MAX + 1];
+  const char *rname;
+  int ref_dist, rev, id;
+  char *q, *w;
+  so_aln a;
+  float score;
+  char *qc, *rc;
+} so_pe_pair;
+
+/* chooseBestAlignment_paired3 (src/align.cu:1248-1422): its rand() pinned
+ * to 0 (the first best pair); more than 6 tied pairs fit (the reference's
+ * arrays of 6 would overflow) */
+static void so_pe_choose(so_pe_pair *x, int size, unsigned min_frag, unsigned max_frag,
+                         char *mate) {
+  int start = 0, end = size - 1;
+  while (start < size) {
+    for (int i = start + 1; i < size; ++i)
+      if (so_name_cmp(x[i].qname, x[i - 1].qname, SO_NAME_MAX) != 0) {
+        end = i - 1;
+        break;
+      }
+    if (end < start) end = size - 1;
+    so_pe_mate_name(x[start].qname, mate);
+    int start2 = end + 1, end2 = size - 1, has = 0;
+    if (start2 < size) {
+      for (int i = start2; i < size; ++i) {
+        if (so_name_cmp(mate, x[i].qname, SO_NAME_MAX) != 0) {
+          end2 = i - 1;
+          break;
+        } else {
+          has = 1;
+        }
+      }
+      if (end2 < start2) {
+        if (has) {
+          end2 = size - 1;
+        } else {
+          for (int i = start; i <= end; ++i) x[i].score = -1.0f;
+          start = start2;
+          continue;
+        }
+      }
+    } else {
+      for (int i = start; i <= end; ++i) x[i].score = -1.0f;
+      start = start2;
+      continue;
+    }
+    float max_score = 0.0f;
+    for (int pass = 0; pass < 2; ++pass) {
+      int found = -1, found2 = -1;
+      for (int i = start; i <= end; ++i)
+        for (int j = start2; j <= end2; ++j) {
+          if (!((x[i].rev == 0 && x[j].rev == 1) || (x[j].rev == 0 && x[i].rev == 1))) continue;
+          float sum = x[i].score + x[j].score;
+          if (pass == 0 ? !(max_score < sum) : !(sum == max_score)) continue;
+          int ok = 1;
+          if (strcmp(x[i].rname, x[j].rname) == 0) {
+            int d;
+            if (x[i].rev == 0 && x[j].rev == 1)
+              d = (x[j].ref_dist + x[j].a.end) - (x[i].ref_dist + x[i].a.start);
+            else
+              d = (x[i].ref_dist + x[i].a.end) - (x[j].ref_dist + x[j].a.start);
+            ok = (unsigned)d >= min_frag && (unsigned)d <= max_frag;
+          }
+          if (!ok) continue;
+          if (pass == 0) {
+            max_score = sum;
+          } else if (found < 0) {
+            found = i;
+            found2 = j;
+          }
+        }
+      if (pass == 1) {
+        for (int i = start; i <= end; ++i)
+          if (found < 0 || i != found) x[i].score = -1.0f;
+        for (int i = start2; i <= end2; ++i)
+          if (found < 0 || i != found2) x[i].score = -1.0f;
+      }
+    }
+    start = end2 + 1;
+  }
+}
+
+/* printOutput_paired2 (src/output.cu:300-362) */
+static void so_pe_print(so_sb *sb, const so_pe_pair *x, int size) {
+  int old = -1;
+  for (int y = 0; y < size; ++y) {
+    if (x[y].score == -1.0f) continue;
+    if (x[y].id != old) {
+      old = x[y].id;
+      so_sb_put(sb, "\n*************************************\n", 39);
+    } else {
+      so_sb_put(sb, "\n", 1);
+    }
+    char hdr[512];
+    int len = x[y].a.len;
+    int hn = snprintf(hdr, sizeof(hdr),
+                      "Qry: %s | Ref: %s | Score: %.1f | AlignStart: %d | AlignEnd: %d | "
+                      "AlignLength: %d\n",
+                      x[y].qname, x[y].rname, x[y].score, x[y].a.start + x[y].ref_dist,
+                      x[y].a.end + x[y].ref_dist, len);
+    so_sb_put(sb, hdr, (size_t)hn);
+    so_sb_put(sb, "R: ", 3);
+    for (int z = len - 1; z >= 0; --z) so_sb_put(sb, &x[y].rc[z], 1);
+    so_sb_put(sb, "\n   ", 4);
+    for (int z = len - 1; z >= 0; --z) {
+      char rc = x[y].rc[z], qc = x[y].qc[z];
+      int ur = (unsigned)(rc - 'a') < 26u ? rc - 32 : rc;
+      int uq = (unsigned)(qc - 'a') < 26u ? qc - 32 : qc;
+      char ch = (ur == uq || rc == 'N' || qc == 'N') ? '|'
+                : (rc == '-' || qc == '-')          ? '-'
+                                                    : '.';
+      so_sb_put(sb, &ch, 1);
+    }
+    so_sb_put(sb, "\nQ: ", 4);
+    for (int z = len - 1; z >= 0; --z) so_sb_put(sb, &x[y].qc[z], 1);
+    so_sb_put(sb, "\n", 1);
+  }
+}
+
+int so_phase1_paired(const char *ref, size_t ref_len, const char *reads1, size_t len1,
+                     const char *reads2, size_t len2, const so_params *p, int32_t **out,
+                     long *n_out, char *err, size_t errlen) {
+  so_ref r;
+  so_reads a, b;
+  memset(&a, 0, sizeof(a));
+  memset(&b, 0, sizeof(b));
+  int rc = so_ref_parse(ref, ref_len, &r, err, errlen);
+  if (rc == 0) rc = so_reads_parse(reads1, len1, &a, err, errlen);
+  if (rc == 0) rc = so_reads_parse(reads2, len2, &b, err, errlen);
+  if (rc == 0 && a.n != b.n) {
+    so_err(err, errlen, "paired reads: %d and %d reads", a.n, b.n);
+    rc = -1;
+  }
+  if (rc == 0) {
+    int Q = p->qry_len > 0 ? p->qry_len : a.first_len;
+    so_pe_index *t = so_pe_index_build(ref, ref_len, p->seed_len);
+    so_pe_match *m = NULL;
+    long n = 0;
+    so_pe_phase1(&r, t, &a, &b, Q, &m, &n);
+    int32_t *o = (int32_t *)malloc((size_t)(n > 0 ? n : 1) * 7 * sizeof(int32_t));
+    for (long i = 0; i < n; ++i) {
+      int32_t *f = o + 7 * i;
+      f[0] = m[i].id;
+      f[1] = m[i].rev;
+      f[2] = m[i].mate;
+      f[3] = m[i].ref_idx;
+      f[4] = m[i].shift;
+      f[5] = m[i].offset;
+      f[6] = m[i].read;
+    }
+    free(m);
+    so_pe_index_free(t);
+    *out = o;
+    *n_out = n;
+  }
+  free(a.r);
+  free(b.r);
+  so_ref_free(&r);
+  return rc;
+}
+
+int so_align_paired(const char *ref, size_t ref_len, const char *reads1, size_t len1,
+                    const char *reads2, size_t len2, const so_params *p, unsigned min_frag,
+                    unsigned max_frag, char **out, size_t *out_len, char *err, size_t errlen) {
+  so_ref r;
+  so_reads rd[2];
+  memset(rd, 0, sizeof(rd));
+  int rc = so_ref_parse(ref, ref_len, &r, err, errlen);
+  if (rc == 0) rc = so_reads_parse(reads1, len1, &rd[0], err, errlen);
+  if (rc == 0) rc = so_reads_parse(reads2, len2, &rd[1], err, errlen);
+  if (rc == 0 && rd[0].n != rd[1].n) {
+    so_err(err, errlen, "paired reads: %d and %d reads", rd[0].n, rd[1].n);
+    rc = -1;
+  }
+  const int Q = p->qry_len > 0 ? p->qry_len : rd[0].first_len;
+  if (rc == 0 && (Q < 1 || 3 * Q > 1024)) {
+    so_err(err, errlen, "query length %d outside 1..341", Q);
+    rc = -1;
+  }
+  if (rc != 0) {
+    free(rd[0].r);
+    free(rd[1].r);
+    so_ref_free(&r);
+    return rc;
+  }
+  const int R = 3 * Q, comb = R + Q + 2;
+  so_pe_index *t = so_pe_index_build(ref, ref_len, p->seed_len);
+  so_pe_match *m = NULL;
+  long nm = 0;
+  so_pe_phase1(&r, t, &rd[0], &rd[1], Q, &m, &nm);
+  so_pe_index_free(t);
+  /* getNumQueriesPerIteration_paired (src/align.cu:2804-2824) */
+  long max_per;
+  {
+    int mem_pair = (R + 1) + (Q + 1) + 4 + 4 + 4 + 2 + 2 * comb;
+    long gm = (long)(p->device_mem - SO_MEM_MARGIN);
+    max_per = p->device_mem > 0 ? (int)floor((float)gm / mem_pair) : nm;
+    if (max_per > nm) max_per = nm;
+  }
+  int *per = NULL;
+  int n_it = max_per > 0 ? so_pe_batches(m, nm, (int)max_per, &per) : 0;
+  so_sb sb = {0};
+  char mate[SO_NAME_MAX + 2];
+  memset(mate, 0, sizeof(mate));
+  long done = 0;
+  for (int it = 0; it < n_it; ++it) {
+    int cnt = per[it];
+    so_pe_pair *x = (so_pe_pair *)calloc((size_t)(cnt > 0 ? cnt : 1), sizeof(so_pe_pair));
+    char *buf = (char *)calloc((size_t)(cnt > 0 ? cnt : 1), (size_t)(Q + 1 + R + 1 + 2 * comb));
+    for (int j = 0; j < cnt; ++j) {
+      const so_pe_match *mm = &m[done + j];
+      so_pe_pair *y = &x[j];
+      char *slot = buf + (size_t)j * (Q + 1 + R + 1 + 2 * comb);
+      y->q = slot;
+      y->w = slot + Q + 1;
+      y->qc = y->w + R + 1;
+      y->rc = y->qc + comb;
+      y->id = mm->id;
+      y->rev = mm->rev;
+      int dist = mm->offset - Q;
+      if (dist < 0) dist = 0;
+      y->ref_dist = dist;
+      const so_rec *rec = &r.recs[mm->ref_idx];
+      unsigned woff = (unsigned)rec->seq_off + (unsigned)dist +
+                      (rec->bpl > 0 ? (unsigned)dist / rec->bpl : 0u);
+      so_get_seq(r.file, r.file_len, woff, y->w, R);
+      y->rname = rec->name;
+      const so_read *rr = &rd[mm->mate - 1].r[mm->read];
+      char tmp[SO_QSEQ_MAX + 2];
+      int L = rr->len < Q ? rr->len : Q;
+      memcpy(tmp, rr->seq, (size_t)L);
+      tmp[L] = '\0';
+      strcpy(y->qname, rr->name);
+      if (mm->rev) {
+        so_revcomp(tmp, Q, y->q);
+        strcat(y->qname, "*");
+      } else {
+        memcpy(y->q, tmp, (size_t)L + 1);
+      }
+    }
+    for (int j = 0; j < cnt; ++j) {
+      so_pe_pair *y = &x[j];
+      so_sw(y->q, Q, y->w, R, p->match, p->mismatch, p->gap_open, p->gap_ext, &y->a, y->qc,
+            y->rc, NULL);
+      y->score = y->a.score;
+    }
+    if (p->out_format == 1) {
+      for (int j = 0; j < cnt; ++j) {
+        so_pair tmp;
+        memset(&tmp, 0, sizeof(tmp));
+        strcpy(tmp.qname, x[j].qname);
+        tmp.rname = x[j].rname;
+        tmp.a = x[j].a;
+        tmp.qc = x[j].qc;
+        tmp.rc = x[j].rc;
+        so_print_sam(&sb, &tmp);
+      }
+    } else {
+      so_pe_choose(x, cnt, min_frag, max_frag, mate);
+      so_pe_print(&sb, x, cnt);
+    }
+    free(x);
+    free(buf);
+    done += cnt;
+  }
+  free(per);
+  free(m);
+  free(rd[0].r);
+  free(rd[1].r);
+  so_ref_free(&r);
+  so_sb_put(&sb, "", 0);
+  if (!sb.b) sb.b = (char *)malloc(1);
+  sb.b[sb.n] = '\0';
+  *out = sb.b;
+  *out_len = sb.n;
+  return 0;
+}

@@ -124,6 +124,17 @@ int so_phase1(const char *ref, size_t ref_len, const char *reads,
 
 void so_free(void *);
 
+/* Paired-end pipeline (-q2, src/main.cu:172-212): Phase-1 records as 7
+ * ints each (id, rev, mate, ref_idx, shift, offset, read index), and the
+ * whole output (out_format 1: SAM).  Reads files must hold the same number
+ * of reads. */
+int so_phase1_paired(const char *ref, size_t ref_len, const char *reads1, size_t len1,
+                     const char *reads2, size_t len2, const so_params *p, int32_t **out,
+                     long *n_out, char *err, size_t errlen);
+int so_align_paired(const char *ref, size_t ref_len, const char *reads1, size_t len1,
+                    const char *reads2, size_t len2, const so_params *p, unsigned min_frag,
+                    unsigned max_frag, char **out, size_t *out_len, char *err, size_t errlen);
+
 #ifdef __cplusplus
 }
 #endif

@@ -228,3 +228,81 @@ def test_lt13_kept_entries_reset(oracle):
     got = [(names[r], st, ri, sh, rp) for r, st, ri, sh, rp in oracle.phase1(ref, reads, p)]
     assert got == recs
     assert oracle.align(ref, reads, p) == out
+
+
+def _paired_case(rng, n_refs, ref_len, n_pairs, L, widths=(60,), repeats=False, frag=(150, 700),
+                 lowcomplex=False):
+    comp = bytes.maketrans(b"ACGT", b"TGCA")
+    seqs = []
+    for i in range(n_refs):
+        if repeats:
+            u = rand_seq(rng, 200)
+            s = bytearray()
+            while len(s) < ref_len:
+                s += mutate(rng, u, 0.02, 0.0) if rng.random() < 0.6 else rand_seq(rng, 200)
+            s = bytes(s[:ref_len])
+        else:
+            s = rand_seq(rng, ref_len)
+        if i % 2 == 1:
+            s = s[:500].lower() + s[500:]
+        if lowcomplex and i == 0:  # a 12-mer over the 1000-occurrence threshold
+            s = s[:3000] + b"ACGTTGCAACGT" * 1200 + s[3000:]
+        seqs.append(s)
+    recs = []
+    for i, s in enumerate(seqs):
+        w = widths[i % len(widths)]
+        lines = [s[j:j + w] for j in range(0, len(s), w)]
+        if i == 1 and len(lines) > 8:  # a blank line and a longer line in the middle
+            lines[3] = lines[3] + lines[4]
+            del lines[4]
+            lines.insert(6, b"")
+        recs.append(b">ref%d\n" % i + b"\n".join(lines) + b"\n")
+    ref = b"".join(recs)
+    r1, r2 = [], []
+    for i in range(n_pairs):
+        si = rng.randrange(n_refs)
+        s = seqs[si]
+        f = rng.randint(*frag)
+        a = rng.randrange(0, max(1, len(s) - f - 5))
+        m1 = mutate(rng, s[a:a + L + 5], 0.02, 0.01)[:L].ljust(L, b"A")
+        m2 = mutate(rng, s[a + f - L:a + f + 5], 0.02, 0.01)[:L].ljust(L, b"C")
+        m2 = m2.translate(comp)[::-1]
+        if i % 5 == 2:
+            m1, m2 = m2, m1
+        if i % 7 == 3:  # mate 2 from another sequence
+            o = seqs[(si + 1) % n_refs]
+            b = rng.randrange(0, len(o) - L)
+            m2 = o[b:b + L].upper()
+        if i % 11 == 5:
+            m1 = rand_seq(rng, L)
+        if i % 13 == 6:
+            m1 = m1[:20] + b"N" + m1[21:]
+        r1.append(b">pair%d/1\n%s\n" % (i, m1))
+        r2.append(b">pair%d/2\n%s\n" % (i, m2))
+    return ref, b"".join(r1), b"".join(r2)
+
+
+@pytest.mark.parametrize("seed,case", list(enumerate([
+    dict(n_refs=1, ref_len=20000, n_pairs=30, L=100),
+    dict(n_refs=3, ref_len=8000, n_pairs=40, L=90, widths=(60, 70, 50)),
+    dict(n_refs=2, ref_len=12000, n_pairs=40, L=100, repeats=True),
+    dict(n_refs=2, ref_len=6000, n_pairs=30, L=60, frag=(50, 900)),
+    dict(n_refs=2, ref_len=9000, n_pairs=40, L=100, widths=(50, 62), lowcomplex=True),
+])))
+@pytest.mark.parametrize("dm,fmt", [(288_000_000_000, 0), (100_000_000 + 37 * 1700, 0),
+                                    (288_000_000_000, 1)])
+def test_paired_pipeline(oracle, seed, case, dm, fmt):
+    # the reference's searchQueries_paired2 (lookupTable2, hit lists, the
+    # cluster picks) and alignQueries_paired2 (getSeq windows of 3Q, the
+    # kernel on fibers, chooseBestAlignment_paired3, printOutput_paired2)
+    # against the oracle: records and output, one batch and small batches
+    rng = random.Random(1400 + seed)
+    ref, r1, r2 = _paired_case(rng, **case)
+    out, recs = R.pipeline_paired(ref, r1, r2, dm, out_format=fmt)
+    p = oracle.default_params(device_mem=dm, out_format=fmt)
+    names = [[l[1:].decode() for l in r.split(b"\n") if l.startswith(b">")] for r in (r1, r2)]
+    got = [(i, names[m - 1][rd], rv, m, ri, sh, of)
+           for i, rv, m, ri, sh, of, rd in oracle.phase1_paired(ref, r1, r2, p)]
+    assert got == recs
+    assert oracle.align_paired(ref, r1, r2, p) == out
+    assert len(recs) > 0 and len(out) > 0
