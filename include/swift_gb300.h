@@ -261,6 +261,26 @@ int swift_fetch_output(swift_ctx *ctx, char *dst, size_t cap);
 
 /* File-to-file pipeline, the CLI: reads the two FASTA files and writes the
  * default output records to out_path. */
+/* Paired-end alignment (-q / -q2), the GPU branch of src/main.cu:172-212:
+ * replaces searchQueries_paired2 (src/search.cu:2084-2200, lookupTable2
+ * seeding of both mates and their reverse complements, 3 hits each) and
+ * alignQueries_paired2 (src/align.cu:1879-2110: windows of 3Q bases from
+ * getSeq, chooseBestAlignment_paired3 keeping the best mate pair whose
+ * fragment length lies in [min_frag, max_frag] on one reference,
+ * printOutput_paired2 records; out_format 1: SAM records of every hit).
+ * The reference's MIN/MAX_FRAG_SIZE are 99 and 600 (src/common.h:66-68).
+ * Both reads buffers hold the same number of reads, every read at least
+ * the query length (first read of reads1, or qry_len), names ending in 1
+ * or 2 (SWIFT_E_INPUT otherwise).  The lookupTable2 positions are built on
+ * the index at first use (with the reference's fixed 1000-repeat threshold).
+ * The output is malloc'ed (swift_free).  Of the stats, seed_ms (both
+ * files), pairs_ms, sw_ms, select_ms (host pairing), format_ms and
+ * total_ms, reads (both mates), records, printed and cells are set. */
+int swift_align_paired(swift_ctx *ctx, const swift_index *idx, const char *reads1,
+                       size_t len1, const char *reads2, size_t len2, const swift_params *p,
+                       uint32_t min_frag, uint32_t max_frag, char **out, size_t *out_len,
+                       swift_stats *stats);
+
 int swift_align_files(swift_ctx *ctx, const char *qry_path, const char *ref_path,
                       const char *out_path, const swift_params *p);
 

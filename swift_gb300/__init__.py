@@ -23,7 +23,7 @@ EXPORTS = [
     "swift_ctx_info", "swift_ctx_set_sw_path",
     "swift_index_build", "swift_index_destroy", "swift_index_info", "swift_index_export",
     "swift_seed", "swift_seed_lt13", "swift_index_save", "swift_index_load",
-    "swift_index_params", "swift_sw_batch", "swift_align", "swift_reads_upload",
+    "swift_index_params", "swift_align_paired", "swift_sw_batch", "swift_align", "swift_reads_upload",
     "swift_reads_destroy", "swift_align_resident", "swift_fetch_output",
     "swift_align_files", "swift_free", "swift_peak_dpx", "swift_align_into",
     "swift_sw_batch_noalloc", "swift_sw_pairs", "swift_server_create", "swift_server_submit",
@@ -113,6 +113,9 @@ def lib():
         L.swift_index_save.argtypes = [vp, vp, C.c_char_p]
         L.swift_index_load.argtypes = [vp, C.c_char_p, C.POINTER(vp)]
         L.swift_index_params.argtypes = [vp, vp, C.POINTER(i32), C.POINTER(i32)]
+        L.swift_align_paired.argtypes = [vp, vp, C.c_char_p, sz, C.c_char_p, sz, C.POINTER(Params),
+                                         C.c_uint32, C.c_uint32, C.POINTER(vp), C.POINTER(sz),
+                                         vp]
         L.swift_sw_batch.argtypes = [vp, vp, vp, i32, i32, i64, i32, i32, i32, i32,
                                      vp, vp, vp, vp, vp, vp]
         L.swift_align.argtypes = [vp, vp, vp, sz, C.POINTER(Params), C.POINTER(vp),
@@ -292,6 +295,21 @@ class Context:
         data = C.string_at(out, n.value) if n.value else b""
         lib().swift_free(out)
         return (data, st.as_dict()) if stats else data
+
+    def align_paired(self, index: "Index", reads1: bytes, reads2: bytes,
+                     params: Params | None = None, min_frag: int = 99, max_frag: int = 600,
+                     stats: bool = False):
+        """Paired-end alignment (-q / -q2); the output text (and stats)."""
+        p = params or default_params(seed_len=index.seed_len, ignore_thres=index.ignore_thres)
+        out = C.c_void_p()
+        n = C.c_size_t()
+        st = Stats()
+        self._check(lib().swift_align_paired(self._h, index._h, reads1, len(reads1), reads2,
+                                             len(reads2), C.byref(p), min_frag, max_frag,
+                                             C.byref(out), C.byref(n), C.byref(st)))
+        text = C.string_at(out, n.value)
+        lib().swift_free(out)
+        return (text, st.as_dict()) if stats else text
 
     def align_into(self, index: "Index", reads_ptr: int, nbytes: int, out_ptr: int, cap: int,
                    params: Params | None = None):

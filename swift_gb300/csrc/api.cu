@@ -251,6 +251,191 @@ struct SeedOut {
   int64_t launches = 0;
 };
 
+// lookupTable2's position of every posting (src/lookupTable2.cu:75-218,
+// searchQueries_paired2's index): the same tuples and bucket order as an
+// SSAHA index with the 1000-repeat threshold, each stored there as a FILE
+// offset (header end + bases + line count, one less for the first tuple
+// written after a line that carried bases over) and read back through
+// refMapGetIndexAndPos (src/refMap.cu:166-242), which counts newlines with
+// the record's bases-per-line.  The line walk runs on the host over the
+// reference bytes once; the postings keep their order.
+int ensure_lt2(swift_ctx* ctx, const swift_index* cidx) {
+  swift_index* idx = const_cast<swift_index*>(cidx);
+  std::lock_guard<std::mutex> lk(idx->pe_mu);
+  if (idx->pe_ready) return SWIFT_OK;
+  constexpr int kThres = 1000;  // TUPLE_IGNORE_THRES (src/common.h:75)
+  std::vector<char> file(idx->file_len + 1, 0);
+  CK(cudaMemcpy(file.data(), idx->d_file, idx->file_len, cudaMemcpyDeviceToHost));
+  const swift_index* src = idx;
+  if (idx->thres != kThres) {
+    const int rc = swift_index_build(ctx, file.data(), idx->file_len, idx->k, kThres,
+                                     &idx->pe_sub);
+    if (rc != SWIFT_OK) return rc;
+    src = idx->pe_sub;
+  }
+  const int k = idx->k;
+  const int nr = (int)idx->recs.size();
+  std::vector<int64_t> tb(nr + 1, 0);
+  for (int r = 0; r < nr; ++r) tb[r + 1] = tb[r] + (int64_t)(idx->recs[r].cat_len / (uint64_t)k);
+  std::vector<int32_t> ppos((size_t)std::max<int64_t>(tb[nr], 1), 0);
+  std::vector<int8_t> pidx((size_t)std::max<int64_t>(tb[nr], 1), 0);
+  // refMapGetIndexAndPos
+  auto index_pos = [&](uint32_t off, int* index, int* pos) {
+    if ((uint32_t)idx->recs[0].seq_off == off) {
+      *index = 0;
+      *pos = 0;
+      return;
+    }
+    int id = -1;
+    if (nr == 1) {
+      id = 0;
+    } else {
+      for (int i = 1; i < nr; ++i) {
+        if ((uint32_t)idx->recs[i - 1].seq_off == off) {
+          *index = i - 1;
+          *pos = 0;
+          return;
+        } else if ((uint32_t)idx->recs[i].seq_off > off) {
+          id = i - 1;
+          break;
+        }
+      }
+      if (id == -1) id = nr - 1;
+    }
+    const uint32_t so = (uint32_t)idx->recs[id].seq_off, bpl = idx->recs[id].bpl;
+    if (bpl == 0) {
+      *pos = (int)(off - so);
+    } else {
+      const uint32_t nl = off >= so ? (off - so) / (bpl + 1) : 0;
+      *pos = (int)(off - so) - (int)nl;
+    }
+    *index = id;
+  };
+  // the line walk of lookupTable2Create (lines as fgets cuts them)
+  {
+    std::vector<uint16_t> seen((size_t)idx->nb, 0);
+    std::vector<char> line(2 * 100000 + 16);
+    const size_t n = idx->file_len;
+    int offset = 0, num_bases = 0, num_nl = 0, ri = -1;
+    uint32_t ref_pos = 0;
+    size_t pos = 0;
+    auto code = [](char c) -> uint32_t {
+      const uint32_t u = (uint8_t)c & 0xDFu;
+      return u == 'C' ? 1u : u == 'G' ? 2u : u == 'T' ? 3u : 0u;
+    };
+    while (pos < n) {
+      size_t lim = std::min<size_t>(n - pos, 100000 - 1);
+      const char* nlp = (const char*)memchr(file.data() + pos, '\n', lim);
+      const size_t c = nlp ? (size_t)(nlp - (file.data() + pos)) + 1 : lim;
+      memcpy(line.data() + offset, file.data() + pos, c);
+      pos += c;
+      int ll = offset + (int)c;
+      if (line[ll - 1] == '\n') --ll;
+      if (ll == 0) {
+        offset = 0;
+      } else if (line[offset] == '>') {
+        offset = 0;
+        num_bases = 0;
+        num_nl = 0;
+        ++ri;
+        ref_pos = (uint32_t)pos;
+      } else {
+        const int iters = ll - k + 1;
+        int i;
+        for (i = 0; i < iters; i += k) {
+          uint32_t h = 0;
+          for (int t = k - 1; t >= 0; --t) h = (h << 2) | code(line[i + t]);
+          if (seen[h] < 65535) ++seen[h];
+          if (seen[h] <= kThres) {
+            uint32_t off = ref_pos + (uint32_t)num_bases + (uint32_t)i + (uint32_t)num_nl;
+            if (offset > 0) {
+              off -= 1u;
+              offset = 0;
+            }
+            const int64_t c0 = (int64_t)num_bases + i;  // position in the record
+            if (ri >= 0 && ri < nr && c0 / k < tb[ri + 1] - tb[ri]) {
+              int id2, p2;
+              index_pos(off, &id2, &p2);
+              ppos[tb[ri] + c0 / k] = p2;
+              pidx[tb[ri] + c0 / k] = (int8_t)id2;
+            }
+          }
+        }
+        num_bases += ll;
+        ++num_nl;
+        offset = ll - i;
+        if (offset > 0) memmove(line.data(), line.data() + i, (size_t)offset);
+        else offset = 0;
+        num_bases -= offset;
+      }
+    }
+  }
+  std::vector<uint2> post((size_t)std::max<int64_t>(src->total, 1));
+  if (src->total)
+    CK(cudaMemcpy(post.data(), src->d_post, src->total * sizeof(uint2), cudaMemcpyDeviceToHost));
+  for (int64_t i = 0; i < src->total; ++i) {
+    const uint32_t r = post[i].y, c0 = post[i].x;
+    const int64_t t = tb[r] + c0 / (uint32_t)k;
+    post[i] = make_uint2((uint32_t)ppos[t], (uint32_t)(int32_t)pidx[t]);
+  }
+  CK(cudaMalloc(&idx->d_post_pe, (size_t)std::max<int64_t>(src->total, 1) * sizeof(uint2)));
+  if (src->total)
+    CK(cudaMemcpy(idx->d_post_pe, post.data(), src->total * sizeof(uint2), cudaMemcpyHostToDevice));
+  idx->pe_ready = true;
+  return SWIFT_OK;
+}
+
+// SSAHA seeding of every strand of a.rd (lookupTable5MapQry +
+// mapHits6GetBestHits per strand): the on-chip kernel, then the strands it
+// handed over (more hits than its shared tables hold) on the overflow
+// kernel.  a.best / a.nbest / a.overflow_list / a.n_overflow (zeroed) are
+// the caller's.
+int seed_ssaha(swift_ctx* ctx, Scratch& sc, SeedArgs a, SeedOut* out) {
+  cudaStream_t st = ctx->st;
+  const int64_t n = a.n_reads, ns = 2 * n;
+  int32_t* ovl = a.overflow_list;
+  int32_t* novl = a.n_overflow;
+  int32_t* nbest = a.nbest;
+  launch_seed(st, a);
+  CKLAUNCH();
+  out->launches += n > 0 ? 1 : 0;
+  int32_t h_novl = 0;
+  CK(cudaMemcpyAsync(&h_novl, novl, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  out->overflow += h_novl;
+  if (h_novl > 0) {
+    std::vector<int32_t> list(h_novl), nb(ns);
+    CK(cudaMemcpyAsync(list.data(), ovl, h_novl * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(nb.data(), nbest, ns * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    std::vector<uint64_t> toff(h_novl);
+    std::vector<uint32_t> tsz(h_novl);
+    uint64_t tot = 0;
+    for (int i = 0; i < h_novl; ++i) {
+      uint32_t hits = (uint32_t)(-nb[list[i]]);
+      uint32_t S = 64;
+      while (S < 2 * hits) S <<= 1;
+      toff[i] = tot;
+      tsz[i] = S;
+      tot += 2 * (uint64_t)S;  // S keys (8 B) + 2 S counters (4 B)
+    }
+    uint64_t* scratch;
+    uint64_t* d_toff;
+    uint32_t* d_tsz;
+    CK(sc.get(&scratch, tot));
+    CK(sc.get(&d_toff, h_novl));
+    CK(sc.get(&d_tsz, h_novl));
+    CK(cudaMemsetAsync(scratch, 0, tot * sizeof(uint64_t), st));
+    CK(cudaMemcpyAsync(d_toff, toff.data(), h_novl * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(d_tsz, tsz.data(), h_novl * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    a.scratch = scratch;
+    launch_seed_overflow(st, a, h_novl, d_toff, d_tsz);
+    CKLAUNCH();
+    out->launches += 1;
+  }
+  return SWIFT_OK;
+}
+
 // The lt13 tables of an index (seed13.cu), built once on first use: the
 // composite of every posting, and refPosHashMap per tuple id, which keeps a
 // tuple's hash when it is among the first thres occurrences of that hash in
@@ -379,59 +564,24 @@ int run_seed(swift_ctx* ctx, const swift_index* idx, const swift_reads* rd, int 
     }
   }
   if (seeder != 1) {
-  SeedArgs a;
-  memset(&a, 0, sizeof(a));
-  a.reads = rd->d_bytes;
-  a.rd = rd->d_rd;
-  a.n_reads = n;
-  a.offsets = idx->d_offsets;
-  a.groups = idx->d_groups;
-  a.cstart = idx->d_cstart;
-  a.postings = idx->d_post;
-  a.k = idx->k;
-  a.max_hits = max_hits;
-  a.best = best;
-  a.nbest = nbest;
-  a.overflow_list = ovl;
-  a.n_overflow = novl;
-  launch_seed(st, a);
-  CKLAUNCH();
-  out->launches += n > 0 ? 1 : 0;
-  int32_t h_novl = 0;
-  CK(cudaMemcpyAsync(&h_novl, novl, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-  CK(cudaStreamSynchronize(st));
-  out->overflow = h_novl;
-  if (h_novl > 0) {
-    std::vector<int32_t> list(h_novl), nb(ns);
-    CK(cudaMemcpyAsync(list.data(), ovl, h_novl * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(nb.data(), nbest, ns * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    std::vector<uint64_t> toff(h_novl);
-    std::vector<uint32_t> tsz(h_novl);
-    uint64_t tot = 0;
-    for (int i = 0; i < h_novl; ++i) {
-      uint32_t hits = (uint32_t)(-nb[list[i]]);
-      uint32_t S = 64;
-      while (S < 2 * hits) S <<= 1;
-      toff[i] = tot;
-      tsz[i] = S;
-      tot += 2 * (uint64_t)S;  // S keys (8 B) + 2 S counters (4 B)
-    }
-    uint64_t* scratch;
-    uint64_t* d_toff;
-    uint32_t* d_tsz;
-    CK(sc.get(&scratch, tot));
-    CK(sc.get(&d_toff, h_novl));
-    CK(sc.get(&d_tsz, h_novl));
-    CK(cudaMemsetAsync(scratch, 0, tot * sizeof(uint64_t), st));
-    CK(cudaMemcpyAsync(d_toff, toff.data(), h_novl * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(d_tsz, tsz.data(), h_novl * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
-    a.scratch = scratch;
-    launch_seed_overflow(st, a, h_novl, d_toff, d_tsz);
-    CKLAUNCH();
-    out->launches += 1;
+    SeedArgs a;
+    memset(&a, 0, sizeof(a));
+    a.reads = rd->d_bytes;
+    a.rd = rd->d_rd;
+    a.n_reads = n;
+    a.offsets = idx->d_offsets;
+    a.groups = idx->d_groups;
+    a.cstart = idx->d_cstart;
+    a.postings = idx->d_post;
+    a.k = idx->k;
+    a.max_hits = max_hits;
+    a.best = best;
+    a.nbest = nbest;
+    a.overflow_list = ovl;
+    a.n_overflow = novl;
+    const int rcs = seed_ssaha(ctx, sc, a, out);
+    if (rcs != SWIFT_OK) return rcs;
   }
-  }  // SSAHA seeding
   // per-read record counts -> offsets
   uint64_t *cnt, *roff, *tot_d;
   void* tmp;
@@ -781,6 +931,8 @@ int swift_index_destroy(swift_index* ix) {
   cudaFree(ix->d_map13);
   cudaFree(ix->d_tbase13);
   cudaFree(ix->d_ntup13);
+  cudaFree(ix->d_post_pe);
+  if (ix->pe_sub) swift_index_destroy(ix->pe_sub);
   delete ix;
   return SWIFT_OK;
 }
@@ -1943,6 +2095,443 @@ int swift_align_into(swift_ctx* ctx, const swift_index* idx, const char* reads, 
   }
   swift_reads_destroy(rd);
   return rc;
+}
+
+int swift_align_paired(swift_ctx* ctx, const swift_index* idx, const char* reads1, size_t len1,
+                       const char* reads2, size_t len2, const swift_params* p,
+                       uint32_t min_frag, uint32_t max_frag, char** out, size_t* out_len,
+                       swift_stats* stats) {
+  if (!ctx || !idx || !reads1 || !reads2 || !p || !out || !out_len)
+    return fail(ctx, SWIFT_E_ARG, "null argument");
+  if (p->seed_len != idx->k) return fail(ctx, SWIFT_E_ARG, "seed length differs from the index's");
+  CK(cudaSetDevice(ctx->device));
+  cudaStream_t st = ctx->st;
+  swift_stats s;
+  memset(&s, 0, sizeof(s));
+  CK(cudaEventRecord(ctx->ev[0], st));
+  swift_reads *rd1 = nullptr, *rd2 = nullptr;
+  int rc = upload_reads(ctx, reads1, len1, &rd1);
+  if (rc != SWIFT_OK) return rc;
+  rc = upload_reads(ctx, reads2, len2, &rd2);
+  if (rc != SWIFT_OK) {
+    swift_reads_destroy(rd1);
+    return rc;
+  }
+  struct Guard {
+    swift_reads *a, *b;
+    ~Guard() {
+      swift_reads_destroy(a);
+      swift_reads_destroy(b);
+    }
+  } guard{rd1, rd2};
+  const int64_t n = rd1->n;
+  if (rd2->n != n) return fail(ctx, SWIFT_E_INPUT, "the two reads files hold different numbers of reads");
+  const int Q = p->qry_len > 0 ? p->qry_len : rd1->first_len;
+  if (Q < 1 || Q > kReadMax) return fail(ctx, SWIFT_E_LIMIT, "query length outside 1..199");
+  if (n > 0 && (rd1->min_len < Q || rd2->min_len < Q))
+    return fail(ctx, SWIFT_E_INPUT, "a read is shorter than the query length; the reference "
+                                    "aligns such reads against stale buffer contents");
+  // mate names end in 1 or 2 (getMatePairName; otherwise the reference
+  // pairs against the name it found before)
+  {
+    std::vector<DevRead> h1(n), h2(n);
+    if (n) {
+      CK(cudaMemcpy(h1.data(), rd1->d_rd, n * sizeof(DevRead), cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(h2.data(), rd2->d_rd, n * sizeof(DevRead), cudaMemcpyDeviceToHost));
+    }
+    for (int64_t i = 0; i < n; ++i)
+      for (int f = 0; f < 2; ++f) {
+        const DevRead& r = f == 0 ? h1[i] : h2[i];
+        const char* b = f == 0 ? reads1 : reads2;
+        const char last = r.name_len > 0 ? b[r.name_off + r.name_len] : 0;
+        if (last != '1' && last != '2')
+          return fail(ctx, SWIFT_E_INPUT, "paired-end read names must end in 1 or 2");
+      }
+  }
+  rc = ensure_lt2(ctx, idx);
+  if (rc != SWIFT_OK) return rc;
+  const swift_index* src = idx->pe_sub ? idx->pe_sub : idx;
+  Scratch sc(st);
+  // Phase 1: both files' strands on the lookupTable2 positions
+  constexpr int kHits = 3;  // MAX_NUM_HITS_PAIRED_END (src/common.h:63)
+  const int64_t ns = 2 * n;
+  int3 *best1, *best2;
+  int32_t *nb1, *nb2, *ovl, *novl;
+  CK(sc.get(&best1, (size_t)std::max<int64_t>(ns, 1) * kHits));
+  CK(sc.get(&best2, (size_t)std::max<int64_t>(ns, 1) * kHits));
+  CK(sc.get(&nb1, (size_t)std::max<int64_t>(ns, 1)));
+  CK(sc.get(&nb2, (size_t)std::max<int64_t>(ns, 1)));
+  CK(sc.get(&ovl, (size_t)std::max<int64_t>(ns, 1)));
+  CK(sc.get(&novl, 2));
+  SeedOut so;
+  for (int f = 0; f < 2; ++f) {
+    CK(cudaMemsetAsync(novl, 0, 2 * sizeof(int32_t), st));
+    SeedArgs a;
+    memset(&a, 0, sizeof(a));
+    const swift_reads* r = f == 0 ? rd1 : rd2;
+    a.reads = r->d_bytes;
+    a.rd = r->d_rd;
+    a.n_reads = n;
+    a.groups = src->d_groups;
+    a.cstart = src->d_cstart;
+    a.offsets = src->d_offsets;
+    a.postings = idx->d_post_pe;
+    a.k = idx->k;
+    a.max_hits = kHits;
+    a.fixed_len = Q;
+    a.best = f == 0 ? best1 : best2;
+    a.nbest = f == 0 ? nb1 : nb2;
+    a.overflow_list = ovl;
+    a.n_overflow = novl;
+    rc = seed_ssaha(ctx, sc, a, &so);
+    if (rc != SWIFT_OK) return rc;
+  }
+  // records in searchQueries_paired2's order
+  PairedArgs pa;
+  memset(&pa, 0, sizeof(pa));
+  pa.n_pairs = n;
+  pa.max_hits = kHits;
+  pa.nbest1 = nb1;
+  pa.nbest2 = nb2;
+  pa.best1 = best1;
+  pa.best2 = best2;
+  uint64_t *cnt, *roff, *tot_d;
+  void* tmp;
+  CK(sc.get(&cnt, (size_t)std::max<int64_t>(n, 1)));
+  CK(sc.get(&roff, (size_t)std::max<int64_t>(n, 1)));
+  CK(sc.get(&tot_d, 1));
+  CK(sc.get((uint8_t**)&tmp, scan_temp_bytes(n)));
+  launch_pe_records(st, pa, cnt);
+  CKLAUNCH();
+  int launches = (int)so.launches + (n > 0 ? 1 : 0) + exclusive_scan_u64(st, cnt, roff, n, tmp, tot_d);
+  uint64_t nrec = 0;
+  CK(cudaMemcpyAsync(&nrec, tot_d, 8, cudaMemcpyDeviceToHost, st));
+  std::vector<uint64_t> h_cnt((size_t)std::max<int64_t>(n, 1));
+  if (n) CK(cudaMemcpyAsync(h_cnt.data(), cnt, n * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  const size_t nr = (size_t)std::max<uint64_t>(nrec, 1);
+  CK(sc.get(&pa.m_id, nr));
+  CK(sc.get(&pa.m_mate, nr));
+  CK(sc.get(&pa.m_rev, nr));
+  CK(sc.get(&pa.m_read, nr));
+  CK(sc.get(&pa.m_ri, nr));
+  CK(sc.get(&pa.m_shift, nr));
+  CK(sc.get(&pa.m_off, nr));
+  pa.roff = roff;
+  pa.n_rec = (int64_t)nrec;
+  launch_pe_fill(st, pa);
+  CKLAUNCH();
+  ++launches;
+  CK(cudaEventRecord(ctx->ev[1], st));
+  // both reads buffers back to back for names and queries
+  char* d_reads;
+  DevRead* d_rd;
+  CK(sc.get(&d_reads, len1 + len2 + 64));
+  CK(sc.get(&d_rd, (size_t)std::max<int64_t>(2 * n, 1)));
+  CK(cudaMemcpyAsync(d_reads, rd1->d_bytes, len1, cudaMemcpyDeviceToDevice, st));
+  CK(cudaMemcpyAsync(d_reads + len1, rd2->d_bytes, len2, cudaMemcpyDeviceToDevice, st));
+  if (n) CK(cudaMemcpyAsync(d_rd, rd1->d_rd, n * sizeof(DevRead), cudaMemcpyDeviceToDevice, st));
+  launch_shift_reads(st, rd2->d_rd, n, len1, d_rd + n);
+  CKLAUNCH();
+  // Phase 2 pairs: query Q, window 3Q
+  const int R = 3 * Q;
+  const int64_t cs = (int64_t)Q + R + 2;
+  char *qbuf, *wbuf, *qcons, *rcons;
+  float* score;
+  int32_t *ast, *aen, *aln_len;
+  DevPair* pairs;
+  DevAln* aln;
+  CK(sc.get(&qbuf, nr * (Q + 1)));
+  CK(sc.get(&wbuf, nr * (R + 1)));
+  CK(sc.get(&qcons, nr * cs));
+  CK(sc.get(&rcons, nr * cs));
+  CK(sc.get(&score, nr));
+  CK(sc.get(&ast, nr));
+  CK(sc.get(&aen, nr));
+  CK(sc.get(&aln_len, nr));
+  CK(sc.get(&pairs, nr));
+  CK(sc.get(&aln, nr));
+  CK(cudaMemsetAsync(wbuf, 0, nr * (R + 1), st));
+  pa.Q = Q;
+  pa.ref_file = idx->d_file;
+  pa.ref_file_len = idx->file_len;
+  pa.recs = idx->d_recs;
+  pa.reads = d_reads;
+  pa.rd = d_rd;
+  pa.pairs = pairs;
+  pa.qbuf = qbuf;
+  pa.wbuf = wbuf;
+  launch_pe_pairs(st, pa);
+  CKLAUNCH();
+  ++launches;
+  CK(cudaEventRecord(ctx->ev[2], st));
+  if (nrec > 0) {
+    rc = swift_sw_batch(ctx, qbuf, wbuf, Q, R, (int64_t)nrec, p->match, p->mismatch, p->gap_open,
+                        p->gap_ext, score, ast, aen, aln_len, qcons, rcons);
+    if (rc != SWIFT_OK) return rc;
+  }
+  launch_aln_from_arrays(st, score, ast, aen, aln_len, (int64_t)nrec, aln);
+  CKLAUNCH();
+  CK(cudaEventRecord(ctx->ev[3], st));
+  // selection (chooseBestAlignment_paired3 per batch) on the host over the
+  // per-record scores, names and coordinates; printing flags to the device
+  const bool sam = p->out_format == 1;
+  FormatArgs fa;
+  memset(&fa, 0, sizeof(fa));
+  fa.reads = d_reads;
+  fa.rd = d_rd;
+  fa.recs = idx->d_recs;
+  fa.pairs = pairs;
+  fa.aln = aln;
+  fa.qcons = qcons;
+  fa.rcons = rcons;
+  fa.cons_stride = cs;
+  fa.n = (int64_t)nrec;
+  int32_t* keep;
+  int8_t* sep;
+  uint64_t *bytes, *offs, *tot2;
+  void* tmp2;
+  CK(sc.get(&keep, nr));
+  CK(sc.get(&sep, nr));
+  CK(sc.get(&bytes, nr));
+  CK(sc.get(&offs, nr));
+  CK(sc.get(&tot2, 1));
+  CK(sc.get((uint8_t**)&tmp2, scan_temp_bytes((int64_t)nrec)));
+  int64_t printed = (int64_t)nrec;
+  if (!sam && nrec > 0) {
+    std::vector<int32_t> h_id(nrec), h_mate(nrec), h_rev(nrec), h_read(nrec), h_ri(nrec),
+        h_st(nrec), h_en(nrec);
+    std::vector<float> h_sc(nrec);
+    std::vector<DevPair> h_pairs(nrec);
+    CK(cudaMemcpyAsync(h_id.data(), pa.m_id, nrec * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(h_mate.data(), pa.m_mate, nrec * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(h_rev.data(), pa.m_rev, nrec * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(h_read.data(), pa.m_read, nrec * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(h_ri.data(), pa.m_ri, nrec * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(h_st.data(), ast, nrec * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(h_en.data(), aen, nrec * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(h_sc.data(), score, nrec * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(h_pairs.data(), pairs, nrec * sizeof(DevPair), cudaMemcpyDeviceToHost, st));
+    std::vector<DevRead> h_rd(2 * n);
+    CK(cudaMemcpyAsync(h_rd.data(), d_rd, 2 * n * sizeof(DevRead), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    // query name of a record (the read's header text, '*' for reverse)
+    std::vector<std::string> qn(nrec);
+    for (uint64_t j = 0; j < nrec; ++j) {
+      const DevRead& r = h_rd[h_pairs[j].read];
+      const char* b = h_pairs[j].read < n ? reads1 + r.name_off : reads2 + (r.name_off - len1);
+      qn[j].assign(b + 1, (size_t)r.name_len);
+      if (h_rev[j]) qn[j] += '*';
+    }
+    // qryNameCmp (src/align.cu:1501-1519) on names under 50 bytes
+    auto name_cmp = [](const std::string& a, const std::string& b) -> int {
+      size_t i = 0;
+      for (; i < kNameMax; ++i) {
+        const char ca = i < a.size() ? a[i] : 0, cb = i < b.size() ? b[i] : 0;
+        if (ca == 0 && cb == 0) return 0;
+        if (ca == 0 || cb == 0) break;
+        if (ca != cb) return -1;
+      }
+      if (i >= kNameMax) return -1;
+      auto at = [](const std::string& s, size_t k) { return k < s.size() ? s[k] : '\0'; };
+      if ((at(a, i) == '*' && at(a, i + 1) == 0) || (at(b, i) == '*' && at(b, i + 1) == 0)) return 0;
+      return -1;
+    };
+    // getMatePairName (src/align.cu:1434-1467)
+    auto mate_name = [](const std::string& q) {
+      std::string m = q;
+      if (!q.empty() && q.back() == '*') m.pop_back();
+      if (!m.empty()) m.back() = m.back() == '1' ? '2' : '1';
+      return m;
+    };
+    // batches: getNumQueriesPerIteration_paired + getNumQrsPerIter_paired
+    const int64_t dev_mem = p->device_mem > 0 ? p->device_mem : ctx->total_mem;
+    int64_t max_per;
+    {
+      const int mem_pair = (R + 1) + (Q + 1) + 4 + 4 + 4 + 2 + 2 * (int)cs;
+      const long gm = (long)(dev_mem - 100000000LL);
+      max_per = (int)floor((float)gm / mem_pair);
+      if (max_per > (int64_t)nrec) max_per = (int64_t)nrec;
+    }
+    std::vector<int64_t> per;
+    if (max_per > 0) {
+      int64_t old_count = 0, count = 0, old_id = 0;
+      bool is_new = false;
+      for (uint64_t r = 0; r < nrec; ++r) {
+        ++count;
+        const int64_t id = h_id[r];
+        if (is_new) {
+          is_new = false;
+          if (id == old_id) per.back() = old_count;
+          else count = 1;
+        } else if (id != old_id) {
+          old_count = count - 1;
+        }
+        if (count == max_per) {
+          per.push_back(count);
+          count -= old_count;
+          is_new = true;
+        }
+        old_id = id;
+      }
+      if (!is_new && count <= max_per) per.push_back(count);
+    }
+    std::vector<float> sc2(h_sc);
+    std::vector<int32_t> h_keep(nrec, 0);
+    std::vector<int8_t> h_sep(nrec, 0);
+    std::vector<int32_t> dist(nrec);
+    for (uint64_t j = 0; j < nrec; ++j) dist[j] = h_pairs[j].ref_dist;
+    uint64_t b0 = 0;
+    printed = 0;
+    for (int64_t cntb : per) {
+      const int64_t size = cntb;
+      // chooseBestAlignment_paired3 (src/align.cu:1248-1422), its rand() pinned to 0
+      int64_t start = 0, end = size - 1;
+      auto X = [&](int64_t i) { return b0 + (uint64_t)i; };
+      while (start < size) {
+        for (int64_t i = start + 1; i < size; ++i)
+          if (name_cmp(qn[X(i)], qn[X(i - 1)]) != 0) {
+            end = i - 1;
+            break;
+          }
+        if (end < start) end = size - 1;
+        const std::string mate = mate_name(qn[X(start)]);
+        int64_t start2 = end + 1, end2 = size - 1;
+        bool has = false;
+        if (start2 < size) {
+          for (int64_t i = start2; i < size; ++i) {
+            if (name_cmp(mate, qn[X(i)]) != 0) {
+              end2 = i - 1;
+              break;
+            } else {
+              has = true;
+            }
+          }
+          if (end2 < start2) {
+            if (has) {
+              end2 = size - 1;
+            } else {
+              for (int64_t i = start; i <= end; ++i) sc2[X(i)] = -1.0f;
+              start = start2;
+              continue;
+            }
+          }
+        } else {
+          for (int64_t i = start; i <= end; ++i) sc2[X(i)] = -1.0f;
+          start = start2;
+          continue;
+        }
+        auto ok_pair = [&](int64_t i, int64_t j) {
+          const uint64_t a = X(i), b = X(j);
+          if (strcmp(idx->recs[h_ri[a]].name, idx->recs[h_ri[b]].name) != 0) return true;
+          int d;
+          if (h_rev[a] == 0 && h_rev[b] == 1)
+            d = (dist[b] + h_en[b]) - (dist[a] + h_st[a]);
+          else
+            d = (dist[a] + h_en[a]) - (dist[b] + h_st[b]);
+          return (uint32_t)d >= min_frag && (uint32_t)d <= max_frag;
+        };
+        float max_score = 0.0f;
+        for (int64_t i = start; i <= end; ++i)
+          for (int64_t j = start2; j <= end2; ++j) {
+            const uint64_t a = X(i), b = X(j);
+            if (!((h_rev[a] == 0 && h_rev[b] == 1) || (h_rev[b] == 0 && h_rev[a] == 1))) continue;
+            const float sum = sc2[a] + sc2[b];
+            if (max_score < sum && ok_pair(i, j)) max_score = sum;
+          }
+        int64_t f1 = -1, f2 = -1;
+        for (int64_t i = start; i <= end && f1 < 0; ++i)
+          for (int64_t j = start2; j <= end2; ++j) {
+            const uint64_t a = X(i), b = X(j);
+            if (!((h_rev[a] == 0 && h_rev[b] == 1) || (h_rev[b] == 0 && h_rev[a] == 1))) continue;
+            if (sc2[a] + sc2[b] == max_score && ok_pair(i, j)) {
+              f1 = i;
+              f2 = j;
+              break;
+            }
+          }
+        for (int64_t i = start; i <= end; ++i)
+          if (f1 < 0 || i != f1) sc2[X(i)] = -1.0f;
+        for (int64_t i = start2; i <= end2; ++i)
+          if (f1 < 0 || i != f2) sc2[X(i)] = -1.0f;
+        start = end2 + 1;
+      }
+      // printOutput_paired2 (src/output.cu:300-362): a record opens with a
+      // line of '*' when its pair id differs from the last printed one
+      int64_t old = -1;
+      for (int64_t y = 0; y < size; ++y) {
+        const uint64_t r = X(y);
+        if (sc2[r] == -1.0f) continue;
+        h_keep[r] = 1;
+        h_sep[r] = h_id[r] != old ? 1 : 0;
+        old = h_id[r];
+        ++printed;
+      }
+      b0 += (uint64_t)size;
+    }
+    CK(cudaMemcpyAsync(keep, h_keep.data(), nrec * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(sep, h_sep.data(), nrec, cudaMemcpyHostToDevice, st));
+    fa.keep = keep;
+    fa.pe_sep = sep;
+  }
+  CK(cudaEventRecord(ctx->ev[4], st));
+  fa.bytes = bytes;
+  fa.offs = offs;
+  if (sam)
+    launch_sam_sizes(st, fa);
+  else
+    launch_format_sizes(st, fa);
+  CKLAUNCH();
+  launches += (nrec > 0 ? 1 : 0) + exclusive_scan_u64(st, bytes, offs, (int64_t)nrec, tmp2, tot2);
+  uint64_t total = 0;
+  CK(cudaMemcpyAsync(&total, tot2, 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  char* d_text;
+  CK(sc.get(&d_text, (size_t)total + 16));
+  fa.text = d_text;
+  if (sam)
+    launch_sam_write(st, fa);
+  else
+    launch_format_write(st, fa);
+  CKLAUNCH();
+  launches += nrec > 0 ? 1 : 0;
+  CK(cudaEventRecord(ctx->ev[5], st));
+  char* h = (char*)malloc(total + 1);
+  if (!h) return fail(ctx, SWIFT_E_NOMEM, "host output buffer");
+  if (total) {
+    const cudaError_t e = cudaMemcpyAsync(h, d_text, total, cudaMemcpyDeviceToHost, st);
+    if (e != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess) {
+      free(h);
+      return fail(ctx, SWIFT_E_CUDA, "output copy");
+    }
+  }
+  h[total] = '\0';
+  *out = h;
+  *out_len = total;
+  if (stats) {
+    float t;
+    cudaEventElapsedTime(&t, ctx->ev[0], ctx->ev[1]);
+    s.seed_ms = t;
+    cudaEventElapsedTime(&t, ctx->ev[1], ctx->ev[2]);
+    s.pairs_ms = t;
+    cudaEventElapsedTime(&t, ctx->ev[2], ctx->ev[3]);
+    s.sw_ms = t;
+    cudaEventElapsedTime(&t, ctx->ev[3], ctx->ev[4]);
+    s.select_ms = t;
+    cudaEventElapsedTime(&t, ctx->ev[4], ctx->ev[5]);
+    s.format_ms = t;
+    cudaEventElapsedTime(&t, ctx->ev[0], ctx->ev[5]);
+    s.total_ms = t;
+    s.reads = 2 * n;
+    s.records = (int64_t)nrec;
+    s.printed = printed;
+    s.cells = (int64_t)nrec * Q * R;
+    s.out_bytes = (int64_t)total;
+    s.seed_overflow_strands = so.overflow;
+    s.launches = launches;
+    *stats = s;
+  }
+  return SWIFT_OK;
 }
 
 static int read_file(const char* path, std::vector<char>* buf, std::string* err) {

@@ -1,12 +1,27 @@
 // swift — command-line front end with the reference's flags and usage text
 // (src/main.cu:42-431).  Single-end alignment runs the device pipeline:
-// SSAHA seeding -> Smith-Waterman over 300-base windows -> best alignment per
-// read -> default output records.
+// seeding (lt13 seed-and-extend, as the reference's GPU branch, or SSAHA) ->
+// Smith-Waterman over 300-base windows -> best alignment per read -> output
+// records.  With -q2, the paired-end pipeline (src/main.cu:172-212).
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
+#include <vector>
+
 #include "../../include/swift_gb300.h"
+
+static bool slurp(const char* path, std::vector<char>* out) {
+  FILE* f = fopen(path, "rb");
+  if (!f) return false;
+  fseek(f, 0, SEEK_END);
+  const long n = ftell(f);
+  fseek(f, 0, SEEK_SET);
+  out->resize(n > 0 ? (size_t)n : 0);
+  const bool ok = n <= 0 || fread(out->data(), 1, (size_t)n, f) == (size_t)n;
+  fclose(f);
+  return ok;
+}
 
 static const char* usage_text() {
   return "\nUSAGE:\n"
@@ -46,6 +61,7 @@ int main(int argc, char** argv) {
   // seeding of searchQueries3 instead (not a reference flag)
   p.seeder = 1;
   int cpu = 0;
+  unsigned min_frag = 99, max_frag = 600;  // MIN/MAX_FRAG_SIZE (src/common.h:66-68)
   if (argc == 1) {
     printf("%s\n", usage_text());
     return 0;
@@ -59,8 +75,9 @@ int main(int argc, char** argv) {
     else if (!strcmp(a, "-r")) r = take();
     else if (!strcmp(a, "-o")) o = take();
     else if (!strcmp(a, "-s")) p.qry_len = atoi(take());
-    else if (!strcmp(a, "-n") || !strcmp(a, "-S") || !strcmp(a, "-N") || !strcmp(a, "-ms") ||
-             !strcmp(a, "-MS")) take();
+    else if (!strcmp(a, "-n") || !strcmp(a, "-S") || !strcmp(a, "-N")) take();
+    else if (!strcmp(a, "-ms")) min_frag = (unsigned)atoi(take());
+    else if (!strcmp(a, "-MS")) max_frag = (unsigned)atoi(take());
     else if (!strcmp(a, "-m")) p.match = atoi(take());
     else if (!strcmp(a, "-M")) p.mismatch = atoi(take());
     else if (!strcmp(a, "-O")) p.gap_open = atoi(take());
@@ -82,15 +99,39 @@ int main(int argc, char** argv) {
     printf("%s\n", usage_text());
     return 0;
   }
-  if (q2 || cpu) {
-    fprintf(stderr, "swift: %s is not supported by this build\n",
-            q2 ? "paired-end alignment (-q2)" : "-cpu");
+  if (cpu) {
+    fprintf(stderr, "swift: -cpu is not supported by this build\n");
     return 2;
   }
   swift_ctx* ctx = nullptr;
   if (swift_ctx_create(0, nullptr, &ctx) != SWIFT_OK) {
     fprintf(stderr, "swift: no CUDA device\n");
     return 1;
+  }
+  if (q2) {
+    std::vector<char> ref, r1, r2;
+    if (!slurp(r, &ref) || !slurp(q, &r1) || !slurp(q2, &r2)) {
+      fprintf(stderr, "swift: cannot read an input file\n");
+      swift_ctx_destroy(ctx);
+      return 1;
+    }
+    swift_index* idx = nullptr;
+    char* text = nullptr;
+    size_t n = 0;
+    int rc = swift_index_build(ctx, ref.data(), ref.size(), p.seed_len, p.ignore_thres, &idx);
+    if (rc == SWIFT_OK)
+      rc = swift_align_paired(ctx, idx, r1.data(), r1.size(), r2.data(), r2.size(), &p, min_frag,
+                              max_frag, &text, &n, nullptr);
+    if (rc == SWIFT_OK) {
+      FILE* f = fopen(o, "wb");
+      if (!f || (n && fwrite(text, 1, n, f) != n)) rc = SWIFT_E_ARG;
+      if (f) fclose(f);
+    }
+    if (rc != SWIFT_OK) fprintf(stderr, "swift: %s\n", swift_last_error(ctx));
+    swift_free(text);
+    swift_index_destroy(idx);
+    swift_ctx_destroy(ctx);
+    return rc == SWIFT_OK ? 0 : 1;
   }
   int rc = swift_align_files(ctx, q, r, o, &p);
   if (rc != SWIFT_OK) fprintf(stderr, "swift: %s\n", swift_last_error(ctx));

@@ -50,6 +50,14 @@ struct swift_index {
   int64_t* d_ntup13 = nullptr;
   int64_t max_comp13 = 0;
   int64_t n_tup13 = 0;           // tuples over all references
+  // paired-end seeding (lookupTable2 positions), built on first use: the
+  // postings of an index with the 1000-repeat threshold (this one, or
+  // pe_sub when this one has another threshold) with lookupTable2's
+  // positions
+  std::mutex pe_mu;
+  bool pe_ready = false;
+  swift_index* pe_sub = nullptr;
+  uint2* d_post_pe = nullptr;
 };
 
 struct swift_reads {

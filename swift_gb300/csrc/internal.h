@@ -142,6 +142,8 @@ struct SeedArgs {
   const uint2* postings;      // (ref_pos, ref_idx)
   int k;
   int max_hits;
+  int fixed_len;              // > 0: every strand has this many bases (the
+                              // strand string's first fixed_len; paired end)
   int3* best;                 // per strand: max_hits x (ri, shift, rp)
   int32_t* nbest;             // per strand
   int32_t* overflow_list;     // strands too big for the on-chip path
@@ -229,6 +231,33 @@ struct PairArgs {
   int Qs;                     // query stride
 };
 void launch_build_pairs(cudaStream_t st, const PairArgs& a);
+
+// paired.cu: paired-end records and pairs
+struct PairedArgs {
+  int64_t n_pairs;            // reads per file
+  int max_hits;
+  const int32_t *nbest1, *nbest2;   // per strand of each file
+  const int3 *best1, *best2;
+  const uint64_t* roff;       // per pair: first record
+  int64_t n_rec;
+  int32_t *m_id, *m_mate, *m_rev, *m_read, *m_ri, *m_shift, *m_off;
+  int Q;
+  const char* ref_file;
+  uint64_t ref_file_len;
+  const DevRecord* recs;
+  const char* reads;          // both reads files, the second after the first
+  const DevRead* rd;          // file 1's reads, then file 2's
+  DevPair* pairs;
+  char* qbuf;                 // n_rec x (Q + 1)
+  char* wbuf;                 // n_rec x (3Q + 1), zeroed by the caller
+};
+void launch_pe_records(cudaStream_t st, const PairedArgs& a, uint64_t* cnt);
+void launch_pe_fill(cudaStream_t st, const PairedArgs& a);
+void launch_pe_pairs(cudaStream_t st, const PairedArgs& a);
+void launch_aln_from_arrays(cudaStream_t st, const float* score, const int32_t* start,
+                            const int32_t* end, const int32_t* len, int64_t n, DevAln* aln);
+void launch_shift_reads(cudaStream_t st, const DevRead* in, int64_t n, uint64_t by,
+                        DevRead* out);
 
 // sw.cu
 struct SwArgs {
@@ -381,6 +410,9 @@ struct FormatArgs {
   char* text;
   const int32_t* ub;          // bounded selection: upper bound per packed-path pair
   int32_t* cand;              // bounded selection: the group's candidate per pair
+  const int8_t* pe_sep;       // paired-end records (printOutput_paired2): 1 opens a
+                              // pair with a line of 37 '*', 0 a blank line; null:
+                              // the single-end record's 40 '*'
 };
 void launch_select(cudaStream_t st, const FormatArgs& a);
 void launch_candidates(cudaStream_t st, const FormatArgs& a, int32_t* list, int32_t* cnt);

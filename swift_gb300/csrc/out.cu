@@ -172,7 +172,7 @@ __device__ uint64_t record_bytes(const FormatArgs& a, int64_t j) {
   const DevPair p = a.pairs[j];
   const DevAln al = a.aln[j];
   const int dist = p.ref_dist;
-  uint64_t n = 42;
+  uint64_t n = a.pe_sep ? (a.pe_sep[j] ? 39 : 1) : 42;
   n += kLitQry + qname_len(a, p) + kLitRef + a.recs[p.ref_idx].name_len;
   n += kLitScore + ndigits(al.score) + 2;
   n += kLitStart + ndigits(al.start + dist) + kLitEnd + ndigits(al.end + dist);
@@ -200,7 +200,13 @@ __global__ void __launch_bounds__(kFmtWarps * 32) format_write_kernel(FormatArgs
   char* hdr = hdr_all[wib];
   int hn = 0;
   if (lane == 0) {
-    char* o = put_str(hdr, "\n****************************************\n");  // 42 bytes
+    char* o;
+    if (!a.pe_sep)
+      o = put_str(hdr, "\n****************************************\n");  // 42 bytes
+    else if (a.pe_sep[j])
+      o = put_str(hdr, "\n*************************************\n");  // 39 bytes
+    else
+      o = put_str(hdr, "\n");
     o = put_str(o, "Qry: ");
     const int ql = qname_len(a, p);
     for (int i = 0; i < ql; ++i) *o++ = qname_at(a, p, i);

@@ -1,0 +1,162 @@
+// Paired-end Phase 1 records and Phase 2 pairs on the device (the GPU branch
+// of src/main.cu:172-212).
+//
+// Records (searchQueries_paired2, src/search.cu:2084-2200): per pair id, the
+// hits of mate 1 forward, mate 1 reverse complement, mate 2 forward, mate 2
+// reverse complement, each strand's best clusters from the SSAHA seeding
+// kernel run on the lookupTable2 positions (api.cu builds them).
+//
+// Pairs (alignQueries_paired2, src/align.cu:1976-2043): the window is
+// getSeq's (src/input.cu:163-204) 3Q bytes from the file offset of
+// max(0, offset - Q) in the record (refMapGetOffsets): lines read on from
+// there, newlines dropped, stopping before a line that starts with '>' or
+// after 3Q bytes; no N trimming.  The query is the first Q bases of the
+// mate's read line, reverse-complemented for reverse-strand records
+// (qryGetReverseComplement over those Q bases).
+#include "internal.h"
+
+namespace swift {
+namespace {
+
+__global__ void pe_count_kernel(const int32_t* __restrict__ nb1, const int32_t* __restrict__ nb2,
+                                int64_t n, uint64_t* __restrict__ cnt) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) cnt[i] = (uint64_t)(nb1[2 * i] + nb1[2 * i + 1] + nb2[2 * i] + nb2[2 * i + 1]);
+}
+
+__global__ void pe_fill_kernel(PairedArgs a) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n_pairs) return;
+  uint64_t o = a.roff[i];
+  for (int mate = 0; mate < 2; ++mate) {
+    const int32_t* nb = mate == 0 ? a.nbest1 : a.nbest2;
+    const int3* best = mate == 0 ? a.best1 : a.best2;
+    for (int s = 0; s < 2; ++s) {
+      const int64_t sid = 2 * i + s;
+      for (int h = 0; h < nb[sid]; ++h) {
+        const int3 b = best[sid * a.max_hits + h];
+        a.m_id[o] = (int32_t)(i + 1);
+        a.m_mate[o] = mate + 1;
+        a.m_rev[o] = s;
+        a.m_read[o] = (int32_t)i;
+        a.m_ri[o] = b.x;
+        a.m_shift[o] = b.y;
+        a.m_off[o] = b.z;
+        ++o;
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ char revcomp_base(char c) {
+  return c == 'A' ? 'T' : c == 'C' ? 'G' : c == 'G' ? 'C' : 'A';
+}
+
+// one thread per record
+__global__ void pe_pairs_kernel(PairedArgs a) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= a.n_rec) return;
+  const int Q = a.Q, R = 3 * a.Q;
+  const int mate = a.m_mate[j], rev = a.m_rev[j], read = a.m_read[j], ri = a.m_ri[j];
+  int dist = a.m_off[j] - Q;
+  if (dist < 0) dist = 0;
+  const DevRecord& rec = a.recs[ri];
+  const uint32_t woff = (uint32_t)rec.seq_off + (uint32_t)dist +
+                        (rec.bpl > 0 ? (uint32_t)dist / rec.bpl : 0u);
+  // getSeq over the reference file bytes
+  char* w = a.wbuf + j * (int64_t)(R + 1);
+  int got = 0;
+  uint64_t pos = woff;
+  const uint64_t n = a.ref_file_len;
+  bool line_start = true;
+  while (pos < n && got < R) {
+    const char c = a.ref_file[pos];
+    if (line_start && c == '>') break;
+    line_start = false;
+    if (c == '\n') {
+      line_start = true;
+    } else {
+      w[got++] = c;
+    }
+    ++pos;
+  }
+  // query: the mate's read, first Q bases
+  const int64_t cr = mate == 1 ? (int64_t)read : a.n_pairs + read;
+  const DevRead rr = a.rd[cr];
+  const char* s = a.reads + rr.seq_off;
+  char* q = a.qbuf + j * (int64_t)(Q + 1);
+  if (rev) {
+    for (int t = 0; t < Q; ++t) q[t] = revcomp_base(s[Q - 1 - t]);
+  } else {
+    for (int t = 0; t < Q; ++t) q[t] = s[t];
+  }
+  q[Q] = '\0';
+  DevPair p;
+  p.read = (int32_t)cr;
+  p.strand = rev;
+  p.ref_idx = ri;
+  p.ref_dist = dist;
+  p.win_len = got;
+  p.flags = 0;
+  a.pairs[j] = p;
+}
+
+__global__ void aln_from_arrays_kernel(const float* __restrict__ score,
+                                       const int32_t* __restrict__ start,
+                                       const int32_t* __restrict__ end,
+                                       const int32_t* __restrict__ len, int64_t n,
+                                       DevAln* __restrict__ aln) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  DevAln d;
+  d.score = (int32_t)score[i];
+  d.start = start[i];
+  d.end = end[i];
+  d.len = len[i];
+  aln[i] = d;
+}
+
+// the second reads file's records after the first's: offsets shifted by the
+// first buffer's length
+__global__ void shift_reads_kernel(const DevRead* __restrict__ in, int64_t n, uint64_t by,
+                                   DevRead* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  DevRead r = in[i];
+  r.name_off += by;
+  r.seq_off += by;
+  out[i] = r;
+}
+
+}  // namespace
+
+void launch_pe_records(cudaStream_t st, const PairedArgs& a, uint64_t* cnt) {
+  if (a.n_pairs <= 0) return;
+  pe_count_kernel<<<(unsigned)((a.n_pairs + 255) / 256), 256, 0, st>>>(a.nbest1, a.nbest2,
+                                                                       a.n_pairs, cnt);
+}
+
+void launch_pe_fill(cudaStream_t st, const PairedArgs& a) {
+  if (a.n_pairs <= 0) return;
+  pe_fill_kernel<<<(unsigned)((a.n_pairs + 255) / 256), 256, 0, st>>>(a);
+}
+
+void launch_pe_pairs(cudaStream_t st, const PairedArgs& a) {
+  if (a.n_rec <= 0) return;
+  pe_pairs_kernel<<<(unsigned)((a.n_rec + 127) / 128), 128, 0, st>>>(a);
+}
+
+void launch_aln_from_arrays(cudaStream_t st, const float* score, const int32_t* start,
+                            const int32_t* end, const int32_t* len, int64_t n, DevAln* aln) {
+  if (n <= 0) return;
+  aln_from_arrays_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(score, start, end, len, n,
+                                                                       aln);
+}
+
+void launch_shift_reads(cudaStream_t st, const DevRead* in, int64_t n, uint64_t by,
+                        DevRead* out) {
+  if (n <= 0) return;
+  shift_reads_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(in, n, by, out);
+}
+
+}  // namespace swift

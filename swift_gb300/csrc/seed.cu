@@ -67,7 +67,7 @@ __global__ void __launch_bounds__(kSeedWarps * 32) seed_warp_kernel(SeedArgs a) 
   uint8_t* codes = codes_all[wib];
   const DevRead rd = a.rd[read];
   const int L = rd.len, k = a.k;
-  const int nq = L - k + 1;
+  const int nq = (a.fixed_len > 0 ? a.fixed_len : L) - k + 1;
   if (nq <= 0) {
     if (lane == 0) a.nbest[sid] = 0;
     return;
@@ -215,7 +215,7 @@ __global__ void __launch_bounds__(kOvThreads) seed_overflow_kernel(SeedArgs a,
   const int64_t read = sid >> 1;
   const int strand = (int)(sid & 1);
   const DevRead rd = a.rd[read];
-  const int L = rd.len, k = a.k, nq = L - k + 1;
+  const int L = rd.len, k = a.k, nq = (a.fixed_len > 0 ? a.fixed_len : L) - k + 1;
   const uint32_t S = tab_size[blockIdx.x];
   uint64_t* tk = a.scratch + tab_off[blockIdx.x];
   uint32_t* tc = reinterpret_cast<uint32_t*>(tk + S);
