@@ -54,7 +54,9 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="scale",
-                    choices=["scale", "small", "batched", "serving", "long"])
+                    choices=["scale", "small", "batched", "serving", "long", "paired"])
+    ap.add_argument("--format", default="default", choices=["default", "sam"],
+                    help="output records: the default text or SAM (-f 1)")
     ap.add_argument("--reads", type=int, default=None)
     ap.add_argument("--cpu-sample", type=int, default=20000)
     ap.add_argument("--no-e2e", action="store_true")
@@ -318,6 +320,105 @@ def bench_serving(args, rank, world, local, workers=4, pool_size=240, per_load=5
     return 0
 
 
+def bench_paired(args, rank, world, local):
+    """Paired-end alignment (-q / -q2) end to end through swift_align_paired
+    (host reads in, host text out): the scale reference, 500 K read pairs,
+    fragments U[200, 500], 100 bp mates, 1 % substitutions."""
+    import torch
+    import swift_gb300 as sg
+    from swift_gb300 import build as b
+    from swift_gb300 import synth
+    from oracle import oracle as O
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    n = args.reads or 500_000
+    names, seqs = synth.make_reference(50_000_000, 24, sigma=0.8, repeat_frac=0.10,
+                                       n_units=500, unit_len=300, divergence=0.03, seed=0)
+    ref = synth.fasta_bytes(names, seqs)
+    r1, r2 = synth.paired_reads(seqs, n, 100, (200, 500), 0.01, seed=1 + rank)
+    desc = ("paired: scale reference (50 Mbp / 24 seqs), %d read pairs, 100 bp mates, "
+            "fragments U[200,500], 1%% substitutions" % n)
+    metric = ("read pairs/s (paired end: lookupTable2 seeding + Smith-Waterman + mate pairing "
+              "+ records), bit-exact")
+    fmt = 1 if args.format == "sam" else 0
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        k = min(args.cpu_sample, n, 5000)
+        s1 = sample_reads(r1, k)
+        s2 = sample_reads(r2, k)
+        p = O.default_params(out_format=fmt)
+        t0 = time.perf_counter()
+        steps = max(args.steps, 1)
+        for _ in range(steps):
+            O.align_paired(ref, s1, s2, p)
+        dt = time.perf_counter() - t0
+        v = k * steps / dt
+        print(json.dumps({
+            "impl": "reference", "metric": metric, "value": v, "unit": "read pairs/s",
+            "n_gpus": args.gpus, "steps": steps, "warmup": 0, "ms_per_step": dt * 1e3 / steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic", "config": {"workload": desc, "sample_pairs_per_step": k},
+            "cpu_baseline": {"value": v, "unit": "read pairs/s", "cores": 1, "kind": "port",
+                             "sample": f"{k} read pairs per step (index built inside)"},
+            "e2e": {"value": v, "unit": "read pairs/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}))
+        return 0
+    torch.cuda.set_device(local)
+    b.build()
+    ctx = sg.Context(local)
+    idx = ctx.index(ref)
+    p = sg.default_params(out_format=fmt)
+    for _ in range(max(args.warmup, 3)):
+        text, st = ctx.align_paired(idx, r1, r2, p, stats=True)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    stats = []
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            text, st = ctx.align_paired(idx, r1, r2, p, stats=True)
+            stats.append(st)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([dt], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        dt = float(t.item())
+        torch.distributed.barrier()
+    if rank != 0:
+        return 0
+    value = n * world * args.steps / dt
+    dev_ms = statistics.median(s["total_ms"] for s in stats)
+    k = min(args.cpu_sample, n, 2000)
+    t0 = time.perf_counter()
+    O.align_paired(ref, sample_reads(r1, k), sample_reads(r2, k), O.default_params(out_format=fmt))
+    cdt = time.perf_counter() - t0
+    line = {
+        "metric": metric, "value": value, "unit": "read pairs/s", "n_gpus": world,
+        "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": dt * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int16x2",
+        "data": "synthetic",
+        "config": {"workload": desc, "format": args.format,
+                   "records_per_step": stats[-1]["records"],
+                   "printed_per_step": stats[-1]["printed"]},
+        "phase_ms": {kk: statistics.median(s[kk] for s in stats)
+                     for kk in ("seed_ms", "pairs_ms", "sw_ms", "select_ms", "format_ms",
+                                "total_ms")},
+        "device_pairs_per_s": n / (dev_ms * 1e-3),
+        "cpu_baseline": {"value": k / cdt, "unit": "read pairs/s", "cores": 1, "kind": "port",
+                         "sample": f"{k} read pairs, index built inside"},
+        "e2e": {"value": value, "unit": "read pairs/s", "h2d_bytes_per_step": len(r1) + len(r2),
+                "d2h_bytes_per_step": len(text)},
+        "gpu_launches": int(sum(s["launches"] for s in stats)),
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     args = parse_args()
     rank, world, local = dist_env()
@@ -346,6 +447,8 @@ def main():
 
     if args.workload in ("batched", "long"):
         return bench_batched(args, rank, world, local)
+    if args.workload == "paired":
+        return bench_paired(args, rank, world, local)
     if args.workload == "serving":
         return bench_serving(args, rank, world, local)
     import torch
@@ -369,7 +472,21 @@ def main():
     rd = ctx.reads(reads)
     peak_cells = ctx.peak_dpx_cells_per_s()
     seeder = 1 if args.seeder == "lt13" else 0
-    params = sg.default_params(seeder=seeder)
+    params = sg.default_params(seeder=seeder, out_format=1 if args.format == "sam" else 0)
+    # warm start: the index written to a file and read back (its load time)
+    index_load_s = None
+    try:
+        import tempfile
+        with tempfile.TemporaryDirectory() as d:
+            path = os.path.join(d, "ref.swidx")
+            idx.save(path)
+            t0 = time.perf_counter()
+            idx2 = sg.Index.load(ctx, path)
+            torch.cuda.synchronize()
+            index_load_s = time.perf_counter() - t0
+            idx2.close()
+    except Exception:
+        pass
     stats = []
     for _ in range(max(args.warmup, 3)):
         out_n, st = ctx.align_resident(idx, rd, params)
@@ -443,7 +560,7 @@ def main():
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "int16x2" if stats[-1]["sw_generic_pairs"] < stats[-1]["records"] else "int32",
         "data": "synthetic",
-        "config": {"workload": desc, "seeder": args.seeder,
+        "config": {"workload": desc, "seeder": args.seeder, "format": args.format,
                    "l2": "inputs larger than L2 (reads %.0f MB, index %.0f MB)"
                    % (len(reads) / 1e6, (2 * 4 ** 12 * 4 + 8 * idx.info()["total"]) / 1e6),
                    "records_per_step": stats[-1]["records"],
@@ -452,7 +569,7 @@ def main():
                    "traced_pairs_per_step": stats[-1]["traced_pairs"],
                    "retraced_pairs_per_step": stats[-1]["retraced_pairs"],
                    "bound_pruned_pairs_per_step": stats[-1]["bound_pruned"],
-                   "index_build_s": index_s},
+                   "index_build_s": index_s, "index_load_s": index_load_s},
         "sw_gcups": gcups,
         "phase_ms": {k: statistics.median(s[k] for s in stats)
                      for k in ("seed_ms", "pairs_ms", "sw_ms", "select_ms", "traceback_ms",

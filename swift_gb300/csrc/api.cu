@@ -2233,25 +2233,21 @@ int swift_align_paired(swift_ctx* ctx, const swift_index* idx, const char* reads
   if (n) CK(cudaMemcpyAsync(d_rd, rd1->d_rd, n * sizeof(DevRead), cudaMemcpyDeviceToDevice, st));
   launch_shift_reads(st, rd2->d_rd, n, len1, d_rd + n);
   CKLAUNCH();
-  // Phase 2 pairs: query Q, window 3Q
+  // Phase 2 pairs: query Q, window 3Q; the packed passes trace pairs of
+  // ACGT bytes with full windows, the generic kernel the others
   const int R = 3 * Q;
-  const int64_t cs = (int64_t)Q + R + 2;
+  const int64_t qs = (Q + 16) & ~15, ws = (R + 16) & ~15;
+  const int64_t cs = ((int64_t)Q + R + 2 + 15) & ~(int64_t)15;  // the walk stores words
   char *qbuf, *wbuf, *qcons, *rcons;
-  float* score;
-  int32_t *ast, *aen, *aln_len;
   DevPair* pairs;
   DevAln* aln;
-  CK(sc.get(&qbuf, nr * (Q + 1)));
-  CK(sc.get(&wbuf, nr * (R + 1)));
+  CK(sc.get(&qbuf, nr * qs));
+  CK(sc.get(&wbuf, nr * ws));
   CK(sc.get(&qcons, nr * cs));
   CK(sc.get(&rcons, nr * cs));
-  CK(sc.get(&score, nr));
-  CK(sc.get(&ast, nr));
-  CK(sc.get(&aen, nr));
-  CK(sc.get(&aln_len, nr));
   CK(sc.get(&pairs, nr));
   CK(sc.get(&aln, nr));
-  CK(cudaMemsetAsync(wbuf, 0, nr * (R + 1), st));
+  CK(cudaMemsetAsync(wbuf, 0, nr * ws, st));
   pa.Q = Q;
   pa.ref_file = idx->d_file;
   pa.ref_file_len = idx->file_len;
@@ -2261,17 +2257,86 @@ int swift_align_paired(swift_ctx* ctx, const swift_index* idx, const char* reads
   pa.pairs = pairs;
   pa.qbuf = qbuf;
   pa.wbuf = wbuf;
+  pa.q_stride = qs;
+  pa.w_stride = ws;
   launch_pe_pairs(st, pa);
   CKLAUNCH();
   ++launches;
   CK(cudaEventRecord(ctx->ev[2], st));
+  int bias = 0;
+  const bool fast_ok = fast_params_ok(Q, R, p->match, p->mismatch, p->gap_open, p->gap_ext, &bias);
+  int32_t *fast_list, *gen_list, *lcnt;
+  CK(sc.get(&fast_list, nr));
+  CK(sc.get(&gen_list, nr));
+  CK(sc.get(&lcnt, 2));
+  CK(cudaMemsetAsync(lcnt, 0, 2 * sizeof(int32_t), st));
   if (nrec > 0) {
-    rc = swift_sw_batch(ctx, qbuf, wbuf, Q, R, (int64_t)nrec, p->match, p->mismatch, p->gap_open,
-                        p->gap_ext, score, ast, aen, aln_len, qcons, rcons);
+    partition_pairs_kernel<<<(unsigned)((nrec + 255) / 256), 256, 0, st>>>(
+        pairs, (int64_t)nrec, fast_ok ? 0 : 1, fast_list, lcnt, gen_list, lcnt + 1);
+    CKLAUNCH();
+    ++launches;
+    SwArgs sa;
+    memset(&sa, 0, sizeof(sa));
+    sa.q = qbuf;
+    sa.w = wbuf;
+    sa.q_stride = qs;
+    sa.w_stride = ws;
+    sa.Q = Q;
+    sa.R = R;
+    sa.match = p->match;
+    sa.mismatch = p->mismatch;
+    sa.gap_open = p->gap_open;
+    sa.gap_ext = p->gap_ext;
+    sa.n = (int64_t)nrec;
+    sa.aln = aln;
+    sa.qcons = qcons;
+    sa.rcons = rcons;
+    sa.cons_stride = cs;
+    sa.list = gen_list;
+    sa.count = lcnt + 1;
+    rc = launch_sw(st, sa, &ctx->err);
     if (rc != SWIFT_OK) return rc;
+    CKLAUNCH();
+    ++launches;
+    if (fast_ok) {
+      int32_t h_fast = 0;
+      CK(cudaMemcpyAsync(&h_fast, lcnt, 4, cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+      const int64_t chunk = 262144;
+      int2* best2;
+      uint32_t* dirs;
+      CK(sc.get(&best2, nr));
+      CK(sc.get(&dirs, (size_t)trace_scratch_words(Q, R, std::min<int64_t>(std::max(h_fast, 1), chunk))));
+      FastArgs fa2;
+      memset(&fa2, 0, sizeof(fa2));
+      fa2.q = qbuf;
+      fa2.w = wbuf;
+      fa2.q_stride = qs;
+      fa2.w_stride = ws;
+      fa2.Q = Q;
+      fa2.R = R;
+      fa2.match = p->match;
+      fa2.mismatch = p->mismatch;
+      fa2.gap_open = p->gap_open;
+      fa2.gap_ext = p->gap_ext;
+      fa2.bias = bias;
+      fa2.aln = aln;
+      fa2.qcons = qcons;
+      fa2.rcons = rcons;
+      fa2.cons_stride = cs;
+      fa2.best = best2;
+      fa2.list = fast_list;
+      fa2.count = lcnt;
+      fa2.dirs = dirs;
+      for (int64_t off = 0; off < h_fast; off += chunk) {
+        fa2.list_offset = off;
+        const int kk = launch_sw_trace(st, fa2, std::min<int64_t>(chunk, h_fast - off));
+        if (kk == 0) return fail(ctx, SWIFT_E_DEVICE, "trace pass could not launch");
+        launches += kk;
+        CKLAUNCH();
+      }
+    }
   }
-  launch_aln_from_arrays(st, score, ast, aen, aln_len, (int64_t)nrec, aln);
-  CKLAUNCH();
   CK(cudaEventRecord(ctx->ev[3], st));
   // selection (chooseBestAlignment_paired3 per batch) on the host over the
   // per-record scores, names and coordinates; printing flags to the device
@@ -2299,22 +2364,23 @@ int swift_align_paired(swift_ctx* ctx, const swift_index* idx, const char* reads
   CK(sc.get((uint8_t**)&tmp2, scan_temp_bytes((int64_t)nrec)));
   int64_t printed = (int64_t)nrec;
   if (!sam && nrec > 0) {
-    std::vector<int32_t> h_id(nrec), h_mate(nrec), h_rev(nrec), h_read(nrec), h_ri(nrec),
-        h_st(nrec), h_en(nrec);
+    std::vector<int32_t> h_id(nrec), h_rev(nrec), h_ri(nrec), h_st(nrec), h_en(nrec);
     std::vector<float> h_sc(nrec);
     std::vector<DevPair> h_pairs(nrec);
+    std::vector<DevAln> h_aln(nrec);
     CK(cudaMemcpyAsync(h_id.data(), pa.m_id, nrec * 4, cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(h_mate.data(), pa.m_mate, nrec * 4, cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(h_rev.data(), pa.m_rev, nrec * 4, cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(h_read.data(), pa.m_read, nrec * 4, cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(h_ri.data(), pa.m_ri, nrec * 4, cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(h_st.data(), ast, nrec * 4, cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(h_en.data(), aen, nrec * 4, cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(h_sc.data(), score, nrec * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(h_aln.data(), aln, nrec * sizeof(DevAln), cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(h_pairs.data(), pairs, nrec * sizeof(DevPair), cudaMemcpyDeviceToHost, st));
     std::vector<DevRead> h_rd(2 * n);
     CK(cudaMemcpyAsync(h_rd.data(), d_rd, 2 * n * sizeof(DevRead), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
+    for (uint64_t j = 0; j < nrec; ++j) {
+      h_rev[j] = h_pairs[j].strand;
+      h_ri[j] = h_pairs[j].ref_idx;
+      h_sc[j] = (float)h_aln[j].score;
+      h_st[j] = h_aln[j].start;
+      h_en[j] = h_aln[j].end;
+    }
     // query name of a record (the read's header text, '*' for reverse)
     std::vector<std::string> qn(nrec);
     for (uint64_t j = 0; j < nrec; ++j) {

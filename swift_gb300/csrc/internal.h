@@ -248,8 +248,9 @@ struct PairedArgs {
   const char* reads;          // both reads files, the second after the first
   const DevRead* rd;          // file 1's reads, then file 2's
   DevPair* pairs;
-  char* qbuf;                 // n_rec x (Q + 1)
-  char* wbuf;                 // n_rec x (3Q + 1), zeroed by the caller
+  char* qbuf;                 // n_rec x q_stride
+  char* wbuf;                 // n_rec x w_stride, zeroed by the caller
+  int64_t q_stride, w_stride; // >= Q + 1 and 3Q + 1, multiples of 16
 };
 void launch_pe_records(cudaStream_t st, const PairedArgs& a, uint64_t* cnt);
 void launch_pe_fill(cudaStream_t st, const PairedArgs& a);

@@ -64,7 +64,8 @@ __global__ void pe_pairs_kernel(PairedArgs a) {
   const uint32_t woff = (uint32_t)rec.seq_off + (uint32_t)dist +
                         (rec.bpl > 0 ? (uint32_t)dist / rec.bpl : 0u);
   // getSeq over the reference file bytes
-  char* w = a.wbuf + j * (int64_t)(R + 1);
+  char* w = a.wbuf + j * a.w_stride;
+  bool odd = false;  // a byte outside ACGT or a short window: the generic kernel
   int got = 0;
   uint64_t pos = woff;
   const uint64_t n = a.ref_file_len;
@@ -77,6 +78,7 @@ __global__ void pe_pairs_kernel(PairedArgs a) {
       line_start = true;
     } else {
       w[got++] = c;
+      odd |= !(c == 'A' || c == 'C' || c == 'G' || c == 'T');
     }
     ++pos;
   }
@@ -84,20 +86,21 @@ __global__ void pe_pairs_kernel(PairedArgs a) {
   const int64_t cr = mate == 1 ? (int64_t)read : a.n_pairs + read;
   const DevRead rr = a.rd[cr];
   const char* s = a.reads + rr.seq_off;
-  char* q = a.qbuf + j * (int64_t)(Q + 1);
+  char* q = a.qbuf + j * a.q_stride;
   if (rev) {
     for (int t = 0; t < Q; ++t) q[t] = revcomp_base(s[Q - 1 - t]);
   } else {
     for (int t = 0; t < Q; ++t) q[t] = s[t];
   }
-  q[Q] = '\0';
+  for (int t = 0; t < Q; ++t) odd |= !(q[t] == 'A' || q[t] == 'C' || q[t] == 'G' || q[t] == 'T');
+  for (int64_t t = Q; t < a.q_stride; ++t) q[t] = '\0';
   DevPair p;
   p.read = (int32_t)cr;
   p.strand = rev;
   p.ref_idx = ri;
   p.ref_dist = dist;
   p.win_len = got;
-  p.flags = 0;
+  p.flags = (odd || got != R) ? 1 : 0;
   a.pairs[j] = p;
 }
 

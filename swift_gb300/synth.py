@@ -132,6 +132,48 @@ def make_reads(seqs, n_reads: int, read_len: int = 100, sub_p: float = 0.01,
     return names, out, origins
 
 
+def paired_reads(seqs, n_pairs: int, read_len: int = 100, frag: tuple[int, int] = (200, 500),
+                 sub_p: float = 0.01, seed: int = 1):
+    """Paired-end reads: fragments of length U[frag] from uniform positions;
+    mate 1 the fragment's first read_len bases, mate 2 the reverse complement
+    of its last read_len bases, substitutions at sub_p; names r<i>/1 and
+    r<i>/2.  Returns (reads FASTA 1, reads FASTA 2)."""
+    rng = _rng(seed)
+    lens = np.array([len(s) for s in seqs], dtype=np.int64)
+    cum = np.concatenate([[0], np.cumsum(lens)])
+    f = rng.integers(frag[0], frag[1] + 1, n_pairs)
+    pos = rng.integers(0, cum[-1], n_pairs)
+    sid = np.searchsorted(cum, pos, side="right") - 1
+    off = pos - cum[sid]
+    bad = off + f > lens[sid]
+    while bad.any():
+        pos[bad] = rng.integers(0, cum[-1], bad.sum())
+        sid[bad] = np.searchsorted(cum, pos[bad], side="right") - 1
+        off[bad] = pos[bad] - cum[sid[bad]]
+        bad = off + f > lens[sid]
+    cat = np.concatenate(seqs)
+    L = read_len
+    m1 = cat[pos[:, None] + np.arange(L)[None, :]]
+    m2 = cat[(pos + f - L)[:, None] + np.arange(L)[None, :]]
+    comp = np.zeros(256, np.uint8)
+    for a, c in zip(b"ACGT", b"TGCA"):
+        comp[a] = c
+    m2 = comp[m2[:, ::-1]]
+    for m in (m1, m2):
+        code = np.searchsorted(ACGT, m)
+        sub = rng.random(m.shape) < sub_p
+        m[:] = np.where(sub, ACGT[(code + rng.integers(1, 4, m.shape)) % 4], m)
+
+    def fasta(mat, mate):
+        body = np.empty((n_pairs, L + 1), np.uint8)
+        body[:, :L] = mat
+        body[:, L] = ord("\n")
+        rows = [b">r%d/%d\n" % (i, mate) + body[i].tobytes() for i in range(n_pairs)]
+        return b"".join(rows)
+
+    return fasta(m1, 1), fasta(m2, 2)
+
+
 def reads_fasta(names, reads) -> bytes:
     parts = []
     for n, r in zip(names, reads):
