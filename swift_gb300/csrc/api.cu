@@ -2362,181 +2362,105 @@ int swift_align_paired(swift_ctx* ctx, const swift_index* idx, const char* reads
   CK(sc.get(&offs, nr));
   CK(sc.get(&tot2, 1));
   CK(sc.get((uint8_t**)&tmp2, scan_temp_bytes((int64_t)nrec)));
-  int64_t printed = (int64_t)nrec;
-  if (!sam && nrec > 0) {
-    std::vector<int32_t> h_id(nrec), h_rev(nrec), h_ri(nrec), h_st(nrec), h_en(nrec);
-    std::vector<float> h_sc(nrec);
-    std::vector<DevPair> h_pairs(nrec);
-    std::vector<DevAln> h_aln(nrec);
-    CK(cudaMemcpyAsync(h_id.data(), pa.m_id, nrec * 4, cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(h_aln.data(), aln, nrec * sizeof(DevAln), cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(h_pairs.data(), pairs, nrec * sizeof(DevPair), cudaMemcpyDeviceToHost, st));
-    std::vector<DevRead> h_rd(2 * n);
-    CK(cudaMemcpyAsync(h_rd.data(), d_rd, 2 * n * sizeof(DevRead), cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    for (uint64_t j = 0; j < nrec; ++j) {
-      h_rev[j] = h_pairs[j].strand;
-      h_ri[j] = h_pairs[j].ref_idx;
-      h_sc[j] = (float)h_aln[j].score;
-      h_st[j] = h_aln[j].start;
-      h_en[j] = h_aln[j].end;
-    }
-    // query name of a record (the read's header text, '*' for reverse)
-    std::vector<std::string> qn(nrec);
-    for (uint64_t j = 0; j < nrec; ++j) {
-      const DevRead& r = h_rd[h_pairs[j].read];
-      const char* b = h_pairs[j].read < n ? reads1 + r.name_off : reads2 + (r.name_off - len1);
-      qn[j].assign(b + 1, (size_t)r.name_len);
-      if (h_rev[j]) qn[j] += '*';
-    }
-    // qryNameCmp (src/align.cu:1501-1519) on names under 50 bytes
-    auto name_cmp = [](const std::string& a, const std::string& b) -> int {
-      size_t i = 0;
-      for (; i < kNameMax; ++i) {
-        const char ca = i < a.size() ? a[i] : 0, cb = i < b.size() ? b[i] : 0;
-        if (ca == 0 && cb == 0) return 0;
-        if (ca == 0 || cb == 0) break;
-        if (ca != cb) return -1;
-      }
-      if (i >= kNameMax) return -1;
-      auto at = [](const std::string& s, size_t k) { return k < s.size() ? s[k] : '\0'; };
-      if ((at(a, i) == '*' && at(a, i + 1) == 0) || (at(b, i) == '*' && at(b, i + 1) == 0)) return 0;
-      return -1;
-    };
-    // getMatePairName (src/align.cu:1434-1467)
-    auto mate_name = [](const std::string& q) {
-      std::string m = q;
-      if (!q.empty() && q.back() == '*') m.pop_back();
-      if (!m.empty()) m.back() = m.back() == '1' ? '2' : '1';
-      return m;
-    };
-    // batches: getNumQueriesPerIteration_paired + getNumQrsPerIter_paired
+  // Phase-2 batches: getNumQueriesPerIteration_paired (src/align.cu:2804-2824)
+  // and getNumQrsPerIter_paired (src/align.cu:1812-1852) over the record ids,
+  // which follow from the per-pair record counts; records past the last
+  // batch are not aligned in the reference and not printed here
+  std::vector<uint8_t> h_bs(nr, 0);
+  uint64_t covered = 0;
+  {
     const int64_t dev_mem = p->device_mem > 0 ? p->device_mem : ctx->total_mem;
     int64_t max_per;
     {
-      const int mem_pair = (R + 1) + (Q + 1) + 4 + 4 + 4 + 2 + 2 * (int)cs;
+      const int mem_pair = (R + 1) + (Q + 1) + 4 + 4 + 4 + 2 + 2 * (Q + R + 2);
       const long gm = (long)(dev_mem - 100000000LL);
       max_per = (int)floor((float)gm / mem_pair);
       if (max_per > (int64_t)nrec) max_per = (int64_t)nrec;
     }
-    std::vector<int64_t> per;
     if (max_per > 0) {
+      std::vector<int64_t> per;
       int64_t old_count = 0, count = 0, old_id = 0;
       bool is_new = false;
-      for (uint64_t r = 0; r < nrec; ++r) {
-        ++count;
-        const int64_t id = h_id[r];
-        if (is_new) {
-          is_new = false;
-          if (id == old_id) per.back() = old_count;
-          else count = 1;
-        } else if (id != old_id) {
-          old_count = count - 1;
+      for (int64_t i = 0; i < n; ++i)
+        for (uint64_t t = 0; t < h_cnt[i]; ++t) {
+          ++count;
+          const int64_t id = i + 1;
+          if (is_new) {
+            is_new = false;
+            if (id == old_id) per.back() = old_count;
+            else count = 1;
+          } else if (id != old_id) {
+            old_count = count - 1;
+          }
+          if (count == max_per) {
+            per.push_back(count);
+            count -= old_count;
+            is_new = true;
+          }
+          old_id = id;
         }
-        if (count == max_per) {
-          per.push_back(count);
-          count -= old_count;
-          is_new = true;
-        }
-        old_id = id;
-      }
       if (!is_new && count <= max_per) per.push_back(count);
+      for (int64_t c : per) {
+        if (covered < nrec) h_bs[covered] = 1;
+        covered += (uint64_t)c;
+      }
+      covered = std::min<uint64_t>(covered, nrec);
     }
-    std::vector<float> sc2(h_sc);
-    std::vector<int32_t> h_keep(nrec, 0);
-    std::vector<int8_t> h_sep(nrec, 0);
-    std::vector<int32_t> dist(nrec);
-    for (uint64_t j = 0; j < nrec; ++j) dist[j] = h_pairs[j].ref_dist;
-    uint64_t b0 = 0;
-    printed = 0;
-    for (int64_t cntb : per) {
-      const int64_t size = cntb;
-      // chooseBestAlignment_paired3 (src/align.cu:1248-1422), its rand() pinned to 0
-      int64_t start = 0, end = size - 1;
-      auto X = [&](int64_t i) { return b0 + (uint64_t)i; };
-      while (start < size) {
-        for (int64_t i = start + 1; i < size; ++i)
-          if (name_cmp(qn[X(i)], qn[X(i - 1)]) != 0) {
-            end = i - 1;
-            break;
-          }
-        if (end < start) end = size - 1;
-        const std::string mate = mate_name(qn[X(start)]);
-        int64_t start2 = end + 1, end2 = size - 1;
-        bool has = false;
-        if (start2 < size) {
-          for (int64_t i = start2; i < size; ++i) {
-            if (name_cmp(mate, qn[X(i)]) != 0) {
-              end2 = i - 1;
-              break;
-            } else {
-              has = true;
-            }
-          }
-          if (end2 < start2) {
-            if (has) {
-              end2 = size - 1;
-            } else {
-              for (int64_t i = start; i <= end; ++i) sc2[X(i)] = -1.0f;
-              start = start2;
-              continue;
-            }
-          }
-        } else {
-          for (int64_t i = start; i <= end; ++i) sc2[X(i)] = -1.0f;
-          start = start2;
-          continue;
+  }
+  fa.n = (int64_t)covered;
+  int64_t printed = (int64_t)covered;
+  if (!sam && covered > 0) {
+    // reference-name classes (the pairing compares names, not indices)
+    std::vector<int32_t> h_class(idx->recs.size());
+    for (size_t r = 0; r < idx->recs.size(); ++r) {
+      h_class[r] = (int32_t)r;
+      for (size_t q = 0; q < r; ++q)
+        if (strcmp(idx->recs[q].name, idx->recs[r].name) == 0) {
+          h_class[r] = (int32_t)q;
+          break;
         }
-        auto ok_pair = [&](int64_t i, int64_t j) {
-          const uint64_t a = X(i), b = X(j);
-          if (strcmp(idx->recs[h_ri[a]].name, idx->recs[h_ri[b]].name) != 0) return true;
-          int d;
-          if (h_rev[a] == 0 && h_rev[b] == 1)
-            d = (dist[b] + h_en[b]) - (dist[a] + h_st[a]);
-          else
-            d = (dist[a] + h_en[a]) - (dist[b] + h_st[b]);
-          return (uint32_t)d >= min_frag && (uint32_t)d <= max_frag;
-        };
-        float max_score = 0.0f;
-        for (int64_t i = start; i <= end; ++i)
-          for (int64_t j = start2; j <= end2; ++j) {
-            const uint64_t a = X(i), b = X(j);
-            if (!((h_rev[a] == 0 && h_rev[b] == 1) || (h_rev[b] == 0 && h_rev[a] == 1))) continue;
-            const float sum = sc2[a] + sc2[b];
-            if (max_score < sum && ok_pair(i, j)) max_score = sum;
-          }
-        int64_t f1 = -1, f2 = -1;
-        for (int64_t i = start; i <= end && f1 < 0; ++i)
-          for (int64_t j = start2; j <= end2; ++j) {
-            const uint64_t a = X(i), b = X(j);
-            if (!((h_rev[a] == 0 && h_rev[b] == 1) || (h_rev[b] == 0 && h_rev[a] == 1))) continue;
-            if (sc2[a] + sc2[b] == max_score && ok_pair(i, j)) {
-              f1 = i;
-              f2 = j;
-              break;
-            }
-          }
-        for (int64_t i = start; i <= end; ++i)
-          if (f1 < 0 || i != f1) sc2[X(i)] = -1.0f;
-        for (int64_t i = start2; i <= end2; ++i)
-          if (f1 < 0 || i != f2) sc2[X(i)] = -1.0f;
-        start = end2 + 1;
-      }
-      // printOutput_paired2 (src/output.cu:300-362): a record opens with a
-      // line of '*' when its pair id differs from the last printed one
-      int64_t old = -1;
-      for (int64_t y = 0; y < size; ++y) {
-        const uint64_t r = X(y);
-        if (sc2[r] == -1.0f) continue;
-        h_keep[r] = 1;
-        h_sep[r] = h_id[r] != old ? 1 : 0;
-        old = h_id[r];
-        ++printed;
-      }
-      b0 += (uint64_t)size;
     }
-    CK(cudaMemcpyAsync(keep, h_keep.data(), nrec * 4, cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(sep, h_sep.data(), nrec, cudaMemcpyHostToDevice, st));
+    uint8_t* d_bs;
+    int32_t* d_class;
+    uint32_t *run_flag, *run_of, *n_runs_d;
+    int64_t* first;
+    void* tmp3;
+    CK(sc.get(&d_bs, nr));
+    CK(sc.get(&d_class, std::max<size_t>(h_class.size(), 1)));
+    CK(sc.get(&run_flag, nr));
+    CK(sc.get(&run_of, nr));
+    CK(sc.get(&n_runs_d, 1));
+    CK(sc.get(&first, nr));
+    CK(sc.get((uint8_t**)&tmp3, scan_temp_bytes((int64_t)nrec)));
+    CK(cudaMemcpyAsync(d_bs, h_bs.data(), covered, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(d_class, h_class.data(), h_class.size() * 4, cudaMemcpyHostToDevice, st));
+    PairSelArgs ps;
+    memset(&ps, 0, sizeof(ps));
+    ps.n = (int64_t)covered;
+    ps.pairs = pairs;
+    ps.aln = aln;
+    ps.id = pa.m_id;
+    ps.batch_start = d_bs;
+    ps.reads = d_reads;
+    ps.rd = d_rd;
+    ps.ref_class = d_class;
+    ps.min_frag = min_frag;
+    ps.max_frag = max_frag;
+    ps.keep = keep;
+    ps.sep = sep;
+    launch_pe_runs(st, ps, run_flag);
+    CKLAUNCH();
+    launches += 1 + exclusive_scan_u32(st, run_flag, run_of, (int64_t)covered, tmp3, n_runs_d);
+    uint32_t n_runs = 0;
+    CK(cudaMemcpyAsync(&n_runs, n_runs_d, 4, cudaMemcpyDeviceToHost, st));
+    launch_pe_run_first(st, ps, run_flag, run_of, first);
+    CKLAUNCH();
+    CK(cudaStreamSynchronize(st));
+    launch_pe_pair_runs(st, ps, first, (int64_t)n_runs);
+    CKLAUNCH();
+    launch_pe_sep(st, ps);
+    CKLAUNCH();
+    launches += 3;
     fa.keep = keep;
     fa.pe_sep = sep;
   }
@@ -2548,7 +2472,7 @@ int swift_align_paired(swift_ctx* ctx, const swift_index* idx, const char* reads
   else
     launch_format_sizes(st, fa);
   CKLAUNCH();
-  launches += (nrec > 0 ? 1 : 0) + exclusive_scan_u64(st, bytes, offs, (int64_t)nrec, tmp2, tot2);
+  launches += (covered > 0 ? 1 : 0) + exclusive_scan_u64(st, bytes, offs, (int64_t)covered, tmp2, tot2);
   uint64_t total = 0;
   CK(cudaMemcpyAsync(&total, tot2, 8, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
@@ -2560,7 +2484,7 @@ int swift_align_paired(swift_ctx* ctx, const swift_index* idx, const char* reads
   else
     launch_format_write(st, fa);
   CKLAUNCH();
-  launches += nrec > 0 ? 1 : 0;
+  launches += covered > 0 ? 1 : 0;
   CK(cudaEventRecord(ctx->ev[5], st));
   char* h = (char*)malloc(total + 1);
   if (!h) return fail(ctx, SWIFT_E_NOMEM, "host output buffer");

@@ -259,6 +259,26 @@ void launch_aln_from_arrays(cudaStream_t st, const float* score, const int32_t* 
                             const int32_t* end, const int32_t* len, int64_t n, DevAln* aln);
 void launch_shift_reads(cudaStream_t st, const DevRead* in, int64_t n, uint64_t by,
                         DevRead* out);
+// mate pairing (chooseBestAlignment_paired3) and printOutput_paired2 flags
+struct PairSelArgs {
+  int64_t n;                  // records
+  const DevPair* pairs;
+  const DevAln* aln;
+  const int32_t* id;          // pair id per record (non-decreasing)
+  const uint8_t* batch_start; // 1 at the first record of each Phase-2 batch
+  const char* reads;          // both reads files (names)
+  const DevRead* rd;
+  const int32_t* ref_class;   // per reference: its name's class (equal names, equal class)
+  uint32_t min_frag, max_frag;
+  int32_t* keep;              // out: printed
+  int8_t* sep;                // out: 1 opens with the line of '*'
+};
+void launch_pe_runs(cudaStream_t st, const PairSelArgs& a, uint32_t* flag);
+void launch_pe_run_first(cudaStream_t st, const PairSelArgs& a, const uint32_t* flag,
+                         const uint32_t* run_of, int64_t* first);
+void launch_pe_pair_runs(cudaStream_t st, const PairSelArgs& a, const int64_t* first,
+                         int64_t n_runs);
+void launch_pe_sep(cudaStream_t st, const PairSelArgs& a);
 
 // sw.cu
 struct SwArgs {

@@ -131,6 +131,133 @@ __global__ void shift_reads_kernel(const DevRead* __restrict__ in, int64_t n, ui
   out[i] = r;
 }
 
+
+// ---- mate pairing (chooseBestAlignment_paired3, src/align.cu:1248-1422) ----
+// Names end in 1 or 2 (checked on the host), so qryNameCmp is equality of
+// the read names ("core", the trailing '*' of reverse records aside) and the
+// mate name is the core with its last character swapped.  Within a batch the
+// reference walks runs of records with one core: a run whose next run has
+// the mate core is paired with it and the walk resumes after both; otherwise
+// the run is dropped and the walk resumes at the next run.  Whether run r
+// starts a step follows from the last run h < r whose next run is not its
+// mate: steps start at h + 1, h + 3, ...
+
+__device__ __forceinline__ bool core_equal(const PairSelArgs& a, int64_t x, int64_t y) {
+  const DevRead rx = a.rd[a.pairs[x].read], ry = a.rd[a.pairs[y].read];
+  if (rx.name_len != ry.name_len) return false;
+  const char* px = a.reads + rx.name_off + 1;
+  const char* py = a.reads + ry.name_off + 1;
+  for (int i = 0; i < rx.name_len; ++i)
+    if (px[i] != py[i]) return false;
+  return true;
+}
+
+// is the core of record y the mate name of record x's core?
+__device__ __forceinline__ bool core_is_mate(const PairSelArgs& a, int64_t x, int64_t y) {
+  const DevRead rx = a.rd[a.pairs[x].read], ry = a.rd[a.pairs[y].read];
+  if (rx.name_len != ry.name_len || rx.name_len < 1) return false;
+  const char* px = a.reads + rx.name_off + 1;
+  const char* py = a.reads + ry.name_off + 1;
+  const int L = rx.name_len;
+  for (int i = 0; i < L - 1; ++i)
+    if (px[i] != py[i]) return false;
+  return py[L - 1] == (px[L - 1] == '1' ? '2' : '1');
+}
+
+// per record: 1 where a run of one core starts (batch starts included)
+__global__ void pe_run_start_kernel(PairSelArgs a, uint32_t* flag) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= a.n) return;
+  flag[j] = (a.batch_start[j] || !core_equal(a, j, j - 1)) ? 1u : 0u;
+}
+
+// per run: its first record, from the run index of each record
+__global__ void pe_run_first_kernel(PairSelArgs a, const uint32_t* flag, const uint32_t* run_of,
+                                    int64_t* first) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= a.n) return;
+  if (flag[j]) first[run_of[j]] = j;
+}
+
+__device__ __forceinline__ bool opposite(const PairSelArgs& a, int64_t i, int64_t j) {
+  const int ri = a.pairs[i].strand, rj = a.pairs[j].strand;
+  return (ri == 0 && rj == 1) || (rj == 0 && ri == 1);
+}
+
+__device__ __forceinline__ bool frag_ok(const PairSelArgs& a, int64_t i, int64_t j) {
+  const DevPair pi = a.pairs[i], pj = a.pairs[j];
+  if (a.ref_class[pi.ref_idx] != a.ref_class[pj.ref_idx]) return true;  // other reference names
+  const DevAln ai = a.aln[i], aj = a.aln[j];
+  int d;
+  if (pi.strand == 0 && pj.strand == 1)
+    d = (pj.ref_dist + aj.end) - (pi.ref_dist + ai.start);
+  else
+    d = (pi.ref_dist + ai.end) - (pj.ref_dist + aj.start);
+  return (uint32_t)d >= a.min_frag && (uint32_t)d <= a.max_frag;
+}
+
+// per run: the pairing step it starts, if it starts one
+__global__ void pe_pair_runs_kernel(PairSelArgs a, const int64_t* first, int64_t n_runs) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n_runs) return;
+  // m(h): run h's next run lies in its batch and carries its mate core
+  auto run_end = [&](int64_t h) { return h + 1 < n_runs ? first[h + 1] : a.n; };
+  auto mates = [&](int64_t h) {
+    if (h + 1 >= n_runs) return false;
+    const int64_t nx = first[h + 1];
+    if (a.batch_start[nx]) return false;
+    return core_is_mate(a, first[h], nx);
+  };
+  int64_t h = r - 1;
+  while (h >= 0 && !a.batch_start[first[h + 1]] && mates(h)) --h;
+  // runs h + 1 .. r - 1 all pair with their next run: steps alternate
+  if (((r - h - 1) & 1) != 0) return;  // run r is the mate run of r - 1
+  const int64_t s1 = first[r], e1 = run_end(r);
+  if (!mates(r)) {
+    for (int64_t i = s1; i < e1; ++i) a.keep[i] = 0;
+    return;
+  }
+  const int64_t s2 = e1, e2 = run_end(r + 1);
+  int best = 0;
+  for (int64_t i = s1; i < e1; ++i)
+    for (int64_t j = s2; j < e2; ++j) {
+      if (!opposite(a, i, j)) continue;
+      const int sum = a.aln[i].score + a.aln[j].score;
+      if (best < sum && frag_ok(a, i, j)) best = sum;
+    }
+  int64_t f1 = -1, f2 = -1;
+  for (int64_t i = s1; i < e1 && f1 < 0; ++i)
+    for (int64_t j = s2; j < e2; ++j)
+      if (opposite(a, i, j) && a.aln[i].score + a.aln[j].score == best && frag_ok(a, i, j)) {
+        f1 = i;
+        f2 = j;
+        break;
+      }
+  for (int64_t i = s1; i < e1; ++i) a.keep[i] = i == f1 ? 1 : 0;
+  for (int64_t j = s2; j < e2; ++j) a.keep[j] = j == f2 ? 1 : 0;
+}
+
+// printOutput_paired2's separator: a kept record opens with the line of '*'
+// unless a kept record of the same pair id precedes it in the batch (ids are
+// non-decreasing)
+__global__ void pe_sep_kernel(PairSelArgs a) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= a.n) return;
+  int8_t sep = 0;
+  if (a.keep[j]) {
+    sep = 1;
+    if (!a.batch_start[j]) {
+      for (int64_t i = j - 1; i >= 0 && a.id[i] == a.id[j]; --i) {
+        if (a.keep[i]) {
+          sep = 0;
+          break;
+        }
+        if (a.batch_start[i]) break;
+      }
+    }
+  }
+  a.sep[j] = sep;
+}
 }  // namespace
 
 void launch_pe_records(cudaStream_t st, const PairedArgs& a, uint64_t* cnt) {
@@ -154,6 +281,28 @@ void launch_aln_from_arrays(cudaStream_t st, const float* score, const int32_t* 
   if (n <= 0) return;
   aln_from_arrays_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(score, start, end, len, n,
                                                                        aln);
+}
+
+void launch_pe_runs(cudaStream_t st, const PairSelArgs& a, uint32_t* flag) {
+  if (a.n <= 0) return;
+  pe_run_start_kernel<<<(unsigned)((a.n + 255) / 256), 256, 0, st>>>(a, flag);
+}
+
+void launch_pe_run_first(cudaStream_t st, const PairSelArgs& a, const uint32_t* flag,
+                         const uint32_t* run_of, int64_t* first) {
+  if (a.n <= 0) return;
+  pe_run_first_kernel<<<(unsigned)((a.n + 255) / 256), 256, 0, st>>>(a, flag, run_of, first);
+}
+
+void launch_pe_pair_runs(cudaStream_t st, const PairSelArgs& a, const int64_t* first,
+                         int64_t n_runs) {
+  if (n_runs <= 0) return;
+  pe_pair_runs_kernel<<<(unsigned)((n_runs + 127) / 128), 128, 0, st>>>(a, first, n_runs);
+}
+
+void launch_pe_sep(cudaStream_t st, const PairSelArgs& a) {
+  if (a.n <= 0) return;
+  pe_sep_kernel<<<(unsigned)((a.n + 255) / 256), 256, 0, st>>>(a);
 }
 
 void launch_shift_reads(cudaStream_t st, const DevRead* in, int64_t n, uint64_t by,
