@@ -296,11 +296,17 @@ __global__ void sam_sizes_kernel(FormatArgs a) {
 }
 
 // header + CIGAR: names (<= 50 bytes each), 11 digits, 9 literal bytes, and
-// at most 2 bytes of CIGAR per consensus byte (<= 556 of them)
-constexpr int kSamHead = 1280;
+// at most 2 bytes of CIGAR per consensus byte (<= Q + R <= 199 + 597 of them
+// for paired-end windows of 3Q)
+constexpr int kSamHead = 1792;
+
+// consensus bytes of one record, and the run starts of its CIGAR operations
+constexpr int kSamMaxL = 800;
 
 __global__ void __launch_bounds__(kFmtWarps * 32) sam_write_kernel(FormatArgs a) {
   __shared__ char head_all[kFmtWarps][kSamHead];
+  __shared__ char ops_all[kFmtWarps][kSamMaxL];
+  __shared__ uint32_t starts_all[kFmtWarps][kSamMaxL / 32];
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t j = (int64_t)blockIdx.x * kFmtWarps + wib;
   if (j >= a.n) return;
@@ -310,6 +316,19 @@ __global__ void __launch_bounds__(kFmtWarps * 32) sam_write_kernel(FormatArgs a)
   const char* rc = a.rcons + j * a.cons_stride;
   const char* qc = a.qcons + j * a.cons_stride;
   char* head = head_all[wib];
+  char* ops = ops_all[wib];
+  uint32_t* starts = starts_all[wib];
+  // the operations in printing order (last consensus byte first), and a bit
+  // per position that starts a run
+  for (int t = lane; t < L; t += 32) ops[t] = cigar_op(rc[L - 1 - t], qc[L - 1 - t]);
+  __syncwarp();
+  for (int c0 = 0; c0 < L; c0 += 32) {
+    const int t = c0 + lane;
+    const bool st = t < L && (t == 0 || ops[t] != ops[t - 1]);
+    const uint32_t m = __ballot_sync(0xffffffffu, st);
+    if (lane == 0) starts[c0 >> 5] = m;
+  }
+  __syncwarp();
   int hn = 0;
   if (lane == 0) {
     char* o = head;
@@ -321,21 +340,22 @@ __global__ void __launch_bounds__(kFmtWarps * 32) sam_write_kernel(FormatArgs a)
     *o++ = '\t';
     o = put_int(o, al.start);
     o = put_str(o, "\t255\t");
-    int run = 0;
-    char op = ' ';
-    for (int z = L - 1; z >= 0; --z) {
-      const char c = cigar_op(rc[z], qc[z]);
-      if (run > 0 && c != op) {
-        o = put_int(o, run);
-        *o++ = op;
-        run = 0;
+    int prev = -1;
+    for (int c = 0; c < (L + 31) / 32; ++c) {
+      uint32_t m = starts[c];
+      while (m) {
+        const int t = 32 * c + __ffs(m) - 1;
+        m &= m - 1;
+        if (prev >= 0) {
+          o = put_int(o, t - prev);
+          *o++ = ops[prev];
+        }
+        prev = t;
       }
-      op = c;
-      ++run;
     }
-    if (run > 0) {
-      o = put_int(o, run);
-      *o++ = op;
+    if (prev >= 0) {
+      o = put_int(o, L - prev);
+      *o++ = ops[prev];
     }
     o = put_str(o, "\t*\t0\t0\t");
     hn = (int)(o - head);

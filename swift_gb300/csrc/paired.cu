@@ -52,9 +52,13 @@ __device__ __forceinline__ char revcomp_base(char c) {
   return c == 'A' ? 'T' : c == 'C' ? 'G' : c == 'G' ? 'C' : 'A';
 }
 
-// one thread per record
-__global__ void pe_pairs_kernel(PairedArgs a) {
-  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+// one warp per record; the window's bytes are compacted with ballots (each
+// round the warp reads 32 file bytes, drops newlines, stops at a header)
+constexpr int kPeWarps = 8;
+
+__global__ void __launch_bounds__(kPeWarps * 32) pe_pairs_kernel(PairedArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int64_t j = (int64_t)blockIdx.x * kPeWarps + (threadIdx.x >> 5);
   if (j >= a.n_rec) return;
   const int Q = a.Q, R = 3 * a.Q;
   const int mate = a.m_mate[j], rev = a.m_rev[j], read = a.m_read[j], ri = a.m_ri[j];
@@ -63,45 +67,49 @@ __global__ void pe_pairs_kernel(PairedArgs a) {
   const DevRecord& rec = a.recs[ri];
   const uint32_t woff = (uint32_t)rec.seq_off + (uint32_t)dist +
                         (rec.bpl > 0 ? (uint32_t)dist / rec.bpl : 0u);
-  // getSeq over the reference file bytes
+  // getSeq over the reference file bytes ('>' only starts header lines)
   char* w = a.wbuf + j * a.w_stride;
   bool odd = false;  // a byte outside ACGT or a short window: the generic kernel
   int got = 0;
-  uint64_t pos = woff;
-  const uint64_t n = a.ref_file_len;
-  bool line_start = true;
-  while (pos < n && got < R) {
-    const char c = a.ref_file[pos];
-    if (line_start && c == '>') break;
-    line_start = false;
-    if (c == '\n') {
-      line_start = true;
-    } else {
-      w[got++] = c;
+  for (uint64_t pos = woff;; pos += 32) {
+    const uint64_t p = pos + (uint64_t)lane;
+    const char c = p < a.ref_file_len ? a.ref_file[p] : '\0';
+    const bool stop = p >= a.ref_file_len || c == '>';
+    const uint32_t sb = __ballot_sync(0xffffffffu, stop);
+    const int first_stop = sb ? __ffs(sb) - 1 : 32;
+    const bool keep = lane < first_stop && c != '\n';
+    const uint32_t kb = __ballot_sync(0xffffffffu, keep);
+    const int at = got + __popc(kb & ((1u << lane) - 1));
+    if (keep && at < R) {
+      w[at] = c;
       odd |= !(c == 'A' || c == 'C' || c == 'G' || c == 'T');
     }
-    ++pos;
+    got += __popc(kb);
+    if (first_stop < 32 || got >= R) break;
   }
+  if (got > R) got = R;
   // query: the mate's read, first Q bases
   const int64_t cr = mate == 1 ? (int64_t)read : a.n_pairs + read;
   const DevRead rr = a.rd[cr];
   const char* s = a.reads + rr.seq_off;
   char* q = a.qbuf + j * a.q_stride;
-  if (rev) {
-    for (int t = 0; t < Q; ++t) q[t] = revcomp_base(s[Q - 1 - t]);
-  } else {
-    for (int t = 0; t < Q; ++t) q[t] = s[t];
+  for (int t = lane; t < a.q_stride; t += 32) {
+    char c = '\0';
+    if (t < Q) c = rev ? revcomp_base(s[Q - 1 - t]) : s[t];
+    q[t] = c;
+    if (t < Q) odd |= !(c == 'A' || c == 'C' || c == 'G' || c == 'T');
   }
-  for (int t = 0; t < Q; ++t) odd |= !(q[t] == 'A' || q[t] == 'C' || q[t] == 'G' || q[t] == 'T');
-  for (int64_t t = Q; t < a.q_stride; ++t) q[t] = '\0';
-  DevPair p;
-  p.read = (int32_t)cr;
-  p.strand = rev;
-  p.ref_idx = ri;
-  p.ref_dist = dist;
-  p.win_len = got;
-  p.flags = (odd || got != R) ? 1 : 0;
-  a.pairs[j] = p;
+  odd = __any_sync(0xffffffffu, odd);
+  if (lane == 0) {
+    DevPair p;
+    p.read = (int32_t)cr;
+    p.strand = rev;
+    p.ref_idx = ri;
+    p.ref_dist = dist;
+    p.win_len = got;
+    p.flags = (odd || got != R) ? 1 : 0;
+    a.pairs[j] = p;
+  }
 }
 
 __global__ void aln_from_arrays_kernel(const float* __restrict__ score,
@@ -273,7 +281,7 @@ void launch_pe_fill(cudaStream_t st, const PairedArgs& a) {
 
 void launch_pe_pairs(cudaStream_t st, const PairedArgs& a) {
   if (a.n_rec <= 0) return;
-  pe_pairs_kernel<<<(unsigned)((a.n_rec + 127) / 128), 128, 0, st>>>(a);
+  pe_pairs_kernel<<<(unsigned)((a.n_rec + kPeWarps - 1) / kPeWarps), kPeWarps * 32, 0, st>>>(a);
 }
 
 void launch_aln_from_arrays(cudaStream_t st, const float* score, const int32_t* start,
