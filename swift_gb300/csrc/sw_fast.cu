@@ -46,6 +46,7 @@
 // other pairs take sw.cu): query and window bytes in {A,C,G,T,a,c,g,t},
 // window length = R, mismatch, gap_open, gap_ext < 0, gap_ext >= gap_open,
 // |16*score+4| < 128, 16 * match * Q + B stays below 0x7C00.
+#include <type_traits>
 #include "internal.h"
 
 namespace swift {
@@ -154,15 +155,18 @@ __device__ __forceinline__ void packed_item(const FastArgs& a, const int64_t war
   uint32_t* dirs = nullptr;
   if (TRACE) dirs = a.dirs + ((warp * kGroups + g) * G + sl) * (int64_t)kNW * S8;
   uint32_t send_u = BB, send_h = BB, diag = BB;
-  // one wavefront step; acc receives the step's direction words
-  auto step = [&](const int s, uint32_t* acc) {
+  // one wavefront step; acc receives the step's direction words.  `full`
+  // (std::true_type) marks a step whose columns lie inside the window on
+  // every lane of the group: the range check and its merges drop out.
+  auto step = [&](const int s, uint32_t* acc, auto full) {
+    constexpr bool kFull = decltype(full)::value;
     uint32_t up = __shfl_up_sync(0xffffffffu, send_u, 1, G);
     const uint32_t rh = __shfl_up_sync(0xffffffffu, send_h, 1, G);
     if (sl == 0) up = BB;  // row 0: H = 0, NONE
     const int j = s - sl + 1;
 #pragma unroll
     for (int w = 0; w < kNW; ++w) acc[w] = 0;
-    if (j >= 1 && j <= R) {
+    if (kFull || (j >= 1 && j <= R)) {
       const uint32_t ws = wsel[j];
       const uint32_t jj = (uint32_t)j * 0x00010001u;
       // VAR: halves whose window ends before column j
@@ -209,9 +213,16 @@ __device__ __forceinline__ void packed_item(const FastArgs& a, const int64_t war
   // registers and writes each word index as one 16-byte store
   uint32_t hist[TRACE ? 4 : 1][kNW];
   for (int s0 = 0; s0 < steps; s0 += 4) {
+    // steps s0..s0+3 have 1 <= j <= R on every lane when s0 >= G - 1 and
+    // s0 + 3 <= R - 1 (then also s0 + 3 < steps)
+    if (s0 >= G - 1 && s0 + 3 <= R - 1) {
 #pragma unroll
-    for (int u = 0; u < 4; ++u)
-      if (s0 + u < steps) step(s0 + u, hist[TRACE ? u : 0]);
+      for (int u = 0; u < 4; ++u) step(s0 + u, hist[TRACE ? u : 0], std::true_type());
+    } else {
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (s0 + u < steps) step(s0 + u, hist[TRACE ? u : 0], std::false_type());
+    }
     if (TRACE) {
 #pragma unroll
       for (int w = 0; w < kNW; ++w) {
