@@ -45,6 +45,24 @@ def metric_for(args):
 # 4 B bound written.
 BOUND_DRAM_BYTES_PER_PAIR = 413.0e6 / 825653
 BOUND_ALGO_BYTES_PER_PAIR = 112 + 304 + 64 + 4
+# The same for the trace pass, the first kernel when every pair is traced
+# (SAM output): 112 B query + 304 B window read, 8 B first maximum and the
+# direction words written (8 lanes x 2 words x 312 steps x 4 B per two pairs
+# at 100 bp); DRAM bytes from one ncu capture (2.06 GB for 99,996 pairs).
+TRACE_DRAM_BYTES_PER_PAIR = 2.06e9 / 99996
+TRACE_ALGO_BYTES_PER_PAIR = 112 + 304 + 8 + 8 * 2 * 312 * 4 // 2
+FIRST_PASS = {
+    0: ("sw_bound_kernel (score bound of every pair)", BOUND_DRAM_BYTES_PER_PAIR,
+        BOUND_ALGO_BYTES_PER_PAIR,
+        "the formulation issues 3.25 ALU instructions per 2 cells, so 0.31 is its ceiling"),
+    1: ("sw_packed_kernel score pass (exact score of every pair)", None, 112 + 304 + 4,
+        "the exact formulation issues about 6.5 ALU instructions per 2 cells, so about "
+        "0.15 is its ceiling"),
+    2: ("sw_packed_kernel trace pass (every pair traced for SAM output)",
+        TRACE_DRAM_BYTES_PER_PAIR, TRACE_ALGO_BYTES_PER_PAIR,
+        "the trace formulation issues about 10 ALU instructions per 2 cells (first "
+        "maximum of every row, direction bits), so about 0.1 is its ceiling"),
+}
 
 
 def parse_args():
@@ -554,6 +572,7 @@ def main():
     achieved = stats[-1]["first_pass_cells"] / (fp_ms * 1e-3) / 1e9 if fp_ms > 0 else None
     peak = peak_cells / 1e9
     fast_pairs = stats[-1]["records"] - stats[-1]["sw_generic_pairs"]
+    fp_name, fp_dram, fp_algo, fp_note = FIRST_PASS[int(stats[-1]["first_pass_kind"])]
     line = {
         "metric": metric_for(args), "value": value, "unit": "reads/s", "n_gpus": world,
         "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms_step,
@@ -575,16 +594,16 @@ def main():
                      for k in ("seed_ms", "pairs_ms", "sw_ms", "select_ms", "traceback_ms",
                                "format_ms", "total_ms")},
         "seed_overflow_strands": stats[-1]["seed_overflow_strands"],
-        "roofline": {"bound": "dpx", "kernel": "sw_bound_kernel (score bound of every pair)",
+        "roofline": {"bound": "dpx", "kernel": fp_name,
                      "achieved": achieved, "peak": peak,
                      "unit": "Gcells/s", "frac": achieved / peak if peak and achieved else None,
                      "kernel_ms": fp_ms,
-                     "traffic": BOUND_DRAM_BYTES_PER_PAIR * fast_pairs,
-                     "traffic_unit": "bytes per launch",
-                     "algorithmic_bytes": BOUND_ALGO_BYTES_PER_PAIR * fast_pairs,
+                     "traffic": fp_dram * fast_pairs if fp_dram else None,
+                     "traffic_unit": "bytes per launch" if stats[-1]["first_pass_kind"] != 2
+                     else "bytes per pass (262,144-pair launches)",
+                     "algorithmic_bytes": fp_algo * fast_pairs,
                      "peak_source": "measured on this GPU: 2 cells per __vimax3_s16x2_relu "
-                                    "lane instruction (the formulation issues 3.25 ALU "
-                                    "instructions per 2 cells, so 0.31 is its ceiling)"},
+                                    "lane instruction (%s)" % fp_note},
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": int(sum(s["launches"] for s in stats)),

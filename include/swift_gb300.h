@@ -89,8 +89,10 @@ typedef struct {
   int64_t retraced_pairs;/* printed pairs traced after selection (bounded
                             selection: the read's candidate was not best)    */
   double first_pass_ms;  /* the packed path's first kernel alone: the score
-                            bound (default) or the exact score pass          */
+                            bound (default), the exact score pass, or (SAM
+                            output, every pair traced) the trace pass        */
   int64_t first_pass_cells; /* DP cells that kernel covered               */
+  int64_t first_pass_kind;  /* 0 score bound, 1 exact score, 2 trace pass  */
 } swift_stats;
 
 void swift_params_default(swift_params *p);

@@ -78,7 +78,7 @@ class Stats(C.Structure):
         ("launches", C.c_int64), ("host_parse_ms", C.c_double), ("h2d_ms", C.c_double),
         ("d2h_ms", C.c_double), ("traced_pairs", C.c_int64), ("bound_pruned", C.c_int64),
         ("retraced_pairs", C.c_int64), ("first_pass_ms", C.c_double),
-        ("first_pass_cells", C.c_int64),
+        ("first_pass_cells", C.c_int64), ("first_pass_kind", C.c_int64),
     ]
 
     def as_dict(self):

@@ -772,6 +772,7 @@ int swift_ctx_destroy(swift_ctx* ctx) {
     cudaEventDestroy(ctx->fork_ev);
     cudaEventDestroy(ctx->join_ev);
   }
+  for (cudaEvent_t e : ctx->chunk_ev) cudaEventDestroy(e);
   if (ctx->own_stream) cudaStreamDestroy(ctx->st);
   delete ctx;
   return SWIFT_OK;
@@ -1855,8 +1856,9 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
   if (fast_ok && nproc > 0) CK(sc.get(&best2, nn));
   fa2.best = best2;
   // trace pass + walk over list[0, n), in chunks that bound the direction
-  // scratch
-  auto trace_list = [&](int32_t* list, int32_t* count, int64_t n) -> int {
+  // scratch; `timed`: CUDA events around each chunk's trace pass
+  int timed_chunks = 0;
+  auto trace_list = [&](int32_t* list, int32_t* count, int64_t n, bool timed) -> int {
     const int64_t chunk = 262144;
     if (n <= 0) return SWIFT_OK;
     const int64_t words = trace_scratch_words(Q, kWin, std::min(n, chunk));
@@ -1865,9 +1867,23 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
     fa2.list = list;
     fa2.count = count;
     fa2.dirs = dirs;
+    if (timed) {
+      const size_t need = 2 * (size_t)((n + chunk - 1) / chunk);
+      while (ctx->chunk_ev.size() < need) {
+        cudaEvent_t e;
+        CK(cudaEventCreate(&e));
+        ctx->chunk_ev.push_back(e);
+      }
+    }
     for (int64_t off = 0; off < n; off += chunk) {
       fa2.list_offset = off;
-      const int k = launch_sw_trace(st, fa2, std::min(chunk, n - off));
+      cudaEvent_t eb = nullptr, ea = nullptr;
+      if (timed) {
+        eb = ctx->chunk_ev[2 * timed_chunks];
+        ea = ctx->chunk_ev[2 * timed_chunks + 1];
+        ++timed_chunks;
+      }
+      const int k = launch_sw_trace(st, fa2, std::min(chunk, n - off), eb, ea);
       if (k == 0) return fail(ctx, SWIFT_E_DEVICE, "trace pass could not launch");
       launches += k;
       CKLAUNCH();
@@ -1905,7 +1921,7 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
     if (fast_ok && nproc > 0) {
       CK(cudaMemcpyAsync(h_cnt, cnt, sizeof(h_cnt), cudaMemcpyDeviceToHost, st));
       CK(cudaStreamSynchronize(st));
-      rc = trace_list(fast_list, cnt, h_cnt[0]);
+      rc = trace_list(fast_list, cnt, h_cnt[0], true);
       if (rc != SWIFT_OK) return rc;
     }
   }
@@ -1920,7 +1936,7 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
     CK(cudaEventRecord(ctx->ev[6], st));
     rc = sort_by_stop(tb_list, cnt + 2, h_cnt[2], sorted);
     if (rc != SWIFT_OK) return rc;
-    rc = trace_list(sorted, cnt + 2, h_cnt[2]);
+    rc = trace_list(sorted, cnt + 2, h_cnt[2], false);
     if (rc != SWIFT_OK) return rc;
     int32_t* ex_list = fast_list;  // free once the bound pass has run
     launch_prune(st, fa, aln, ex_list, cnt + 3);
@@ -1953,7 +1969,7 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
     ++launches;
     CK(cudaMemcpyAsync(h_cnt, cnt, sizeof(h_cnt), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    rc = trace_list(list2, cnt + 4, h_cnt[4]);
+    rc = trace_list(list2, cnt + 4, h_cnt[4], false);
     if (rc != SWIFT_OK) return rc;
     if (bounded) pruned = std::max<int64_t>(h_cnt[0] - h_cnt[2] - h_cnt[3], 0);
   }
@@ -1994,8 +2010,20 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
     s.pairs_ms = t;
     cudaEventElapsedTime(&t, ctx->ev[2], ctx->ev[3]);
     s.sw_ms = t;
-    cudaEventElapsedTime(&t, ctx->ev[7], ctx->ev[8]);
-    s.first_pass_ms = t;
+    if (sam) {
+      // no score pass: the trace pass over every packed-path pair
+      double sum = 0;
+      for (int c = 0; c < timed_chunks; ++c) {
+        cudaEventElapsedTime(&t, ctx->chunk_ev[2 * c], ctx->chunk_ev[2 * c + 1]);
+        sum += t;
+      }
+      s.first_pass_ms = sum;
+      s.first_pass_kind = 2;
+    } else {
+      cudaEventElapsedTime(&t, ctx->ev[7], ctx->ev[8]);
+      s.first_pass_ms = t;
+      s.first_pass_kind = bounded ? 0 : 1;
+    }
     s.first_pass_cells = fast_ok ? (int64_t)h_cnt[0] * Q * kWin : 0;
     cudaEventElapsedTime(&t, ctx->ev[3], ctx->ev[6]);
     s.select_ms = t;

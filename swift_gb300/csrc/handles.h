@@ -22,6 +22,7 @@ struct swift_ctx {
   int sw_path = 0;  // 0 bounded selection, 1 generic kernel only, 2 exact score of every pair
   cudaStream_t side = nullptr;  // second stream for concurrent launches, made on first use
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+  std::vector<cudaEvent_t> chunk_ev;  // per-chunk timing of the trace pass, grown on use
 };
 
 struct swift_index {

@@ -409,7 +409,9 @@ __host__ __device__ inline int packed_class_max_q(int c) {
 }
 int64_t trace_scratch_words(int Q, int R, int64_t pairs);
 int launch_sw_score(cudaStream_t st, const FastArgs& a, int64_t max_pairs);
-int launch_sw_trace(cudaStream_t st, const FastArgs& a, int64_t max_pairs);
+// before / after (optional) are recorded around the trace pass alone
+int launch_sw_trace(cudaStream_t st, const FastArgs& a, int64_t max_pairs,
+                    cudaEvent_t before = nullptr, cudaEvent_t after = nullptr);
 int launch_sw_bound(cudaStream_t st, const FastArgs& a, int64_t max_pairs);
 int measure_dpx_peak(cudaStream_t st, int device, double* lane_instr_per_s);
 

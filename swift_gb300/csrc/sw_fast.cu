@@ -176,10 +176,11 @@ __device__ __forceinline__ void packed_item(const FastArgs& a, const int64_t war
 #pragma unroll
       for (int k = 0; k < RPL; ++k) {
         const uint32_t sc = prmt(prof0[k], prof1[k], ws);
-        // LEFT and UP candidates (plain adds, issued on the FMA pipe), the
-        // NONE floor, then DIAG with the signed substitution score
-        const uint32_t m3 = __vimax3_s16x2(xl[k] + CL, up + CU, B8);
-        const uint32_t hx = __viaddmax_s16x2(dg, sc, m3);
+        // DIAG (signed substitution score) against LEFT first: neither waits
+        // for the row above, which then enters one three-way max with the
+        // NONE floor (the candidates' plain adds issue on the FMA pipe)
+        const uint32_t dl = __viaddmax_s16x2(dg, sc, xl[k] + CL);
+        const uint32_t hx = __vimax3_s16x2(dl, up + CU, B8);
         dg = h16p[k];
         const uint32_t h16 = hx & 0xFFF0FFF0u;
         h16p[k] = h16;
@@ -728,11 +729,14 @@ int launch_sw_bound(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {
   return launch_bound(st, a, max_pairs);
 }
 
-int launch_sw_trace(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {
+int launch_sw_trace(cudaStream_t st, const FastArgs& a, int64_t max_pairs, cudaEvent_t before,
+                    cudaEvent_t after) {
   if (a.cons_stride % 4 != 0) return 0;  // the walk stores 32-bit words
   FastArgs b = a;
   b.chunk = max_pairs;
+  if (before && cudaEventRecord(before, st) != cudaSuccess) return 0;
   int k = a.q_len ? launch_shape<true, true>(st, b, max_pairs) : launch_shape<true, false>(st, b, max_pairs);
+  if (after && cudaEventRecord(after, st) != cudaSuccess) return 0;
   return k + launch_walk(st, b, max_pairs);
 }
 

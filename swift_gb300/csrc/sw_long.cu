@@ -149,8 +149,9 @@ __global__ void __launch_bounds__(kLT, 2) sw_long_kernel(LongArgs a) {
           const bool hit = qv[k] == rv || qv[k] == kWild || (rv == kWild && qv[k] >= 0);
           sc = hit ? SM : SX;
         }
-        const int m3 = __vimax3_s32(xl[k] + CL, up + CU, B8);
-        const int hx = __viaddmax_s32(dg, sc, m3);
+        // DIAG against LEFT off the chain down the rows, then UP and NONE
+        const int dl = __viaddmax_s32(dg, sc, xl[k] + CL);
+        const int hx = __vimax3_s32(dl, up + CU, B8);
         dg = h16p[k];
         const int h16 = hx & ~15;
         h16p[k] = h16;
