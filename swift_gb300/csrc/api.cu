@@ -90,6 +90,11 @@ struct SideJoin {
   }
 };
 
+// text copied to the host in this many record ranges (align_into), for
+// calls with at least kOutChunkMin records
+constexpr int kOutChunks = 16;
+constexpr int64_t kOutChunkMin = 65536;
+
 void keep_pool(int device) {
   cudaMemPool_t pool;
   if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
@@ -639,13 +644,16 @@ double ms_since(std::chrono::steady_clock::time_point t0) {
   return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
 
+// transient: buffers for one call, from the stream-ordered pool of ctx->st
+// (freed in stream order by swift_reads_destroy)
 int upload_reads(swift_ctx* ctx, const char* b, size_t len, swift_reads** out,
-                 double* parse_ms = nullptr, double* h2d_ms = nullptr) {
+                 double* parse_ms = nullptr, double* h2d_ms = nullptr, bool transient = false) {
   // bytes to the device, then the record structure found there (parse.cu)
   cudaStream_t st = ctx->st;
   swift_reads* r = new swift_reads();
   r->device = ctx->device;
   r->len = len;
+  if (transient) r->pool_st = st;
   auto t0 = std::chrono::steady_clock::now();
   auto bail = [&](int code, const std::string& m) {
     swift_reads_destroy(r);
@@ -656,7 +664,7 @@ int upload_reads(swift_ctx* ctx, const char* b, size_t len, swift_reads** out,
     cudaError_t e_ = (call);                                                              \
     if (e_ != cudaSuccess) return bail(SWIFT_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
   } while (0)
-  CKR(cudaMalloc(&r->d_bytes, len + 64));
+  CKR(transient ? cudaMallocAsync(&r->d_bytes, len + 64, st) : cudaMalloc(&r->d_bytes, len + 64));
   CKR(cudaMemcpyAsync(r->d_bytes, b, len, cudaMemcpyHostToDevice, st));
   CKR(cudaStreamSynchronize(st));
   if (h2d_ms) *h2d_ms = ms_since(t0);
@@ -686,7 +694,8 @@ int upload_reads(swift_ctx* ctx, const char* b, size_t len, swift_reads** out,
     const uint64_t n_lines = n_nl + ((len > 0 && b[len - 1] != '\n') ? 1 : 0);
     uint64_t* nl;
     CKR(sc.get(&nl, std::max<uint64_t>(n_nl, 1)));
-    CKR(cudaMalloc(&r->d_rd, std::max<uint64_t>(n_lines / 2, 1) * sizeof(DevRead)));
+    const size_t rd_bytes = std::max<uint64_t>(n_lines / 2, 1) * sizeof(DevRead);
+    CKR(transient ? cudaMallocAsync(&r->d_rd, rd_bytes, st) : cudaMalloc(&r->d_rd, rd_bytes));
     launch_parse_newlines(st, r->d_bytes, len, off, nl);
     launch_parse_lines(st, r->d_bytes, len, nl, n_nl, n_lines, r->d_rd, sum, err);
     CKR(cudaGetLastError());
@@ -773,6 +782,7 @@ int swift_ctx_destroy(swift_ctx* ctx) {
     cudaEventDestroy(ctx->join_ev);
   }
   for (cudaEvent_t e : ctx->chunk_ev) cudaEventDestroy(e);
+  for (cudaEvent_t e : ctx->copy_ev) cudaEventDestroy(e);
   if (ctx->own_stream) cudaStreamDestroy(ctx->st);
   delete ctx;
   return SWIFT_OK;
@@ -981,8 +991,13 @@ int swift_reads_upload(swift_ctx* ctx, const char* b, size_t len, swift_reads** 
 int swift_reads_destroy(swift_reads* r) {
   if (!r) return SWIFT_OK;
   cudaSetDevice(r->device);
-  cudaFree(r->d_bytes);
-  cudaFree(r->d_rd);
+  if (r->pool_st) {
+    if (r->d_bytes) cudaFreeAsync(r->d_bytes, r->pool_st);
+    if (r->d_rd) cudaFreeAsync(r->d_rd, r->pool_st);
+  } else {
+    cudaFree(r->d_bytes);
+    cudaFree(r->d_rd);
+  }
   delete r;
   return SWIFT_OK;
 }
@@ -995,7 +1010,7 @@ int seed_records(swift_ctx* ctx, const swift_index* idx, const char* reads, size
   if (max_hits < 1 || max_hits > 64) return fail(ctx, SWIFT_E_ARG, "max_hits outside 1..64");
   CK(cudaSetDevice(ctx->device));
   swift_reads* rd = nullptr;
-  int rc = upload_reads(ctx, reads, len, &rd);
+  int rc = upload_reads(ctx, reads, len, &rd, nullptr, nullptr, true);
   if (rc != SWIFT_OK) return rc;
   {
     Scratch sc(ctx->st);
@@ -1675,8 +1690,12 @@ int swift_sw_pairs(swift_ctx* ctx, const char* qry, const int64_t* q_off, const 
   return SWIFT_OK;
 }
 
-int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_reads* rd,
-                         const swift_params* p, size_t* out_len, swift_stats* stats) {
+// host_out (optional, host_cap bytes): the text is also copied there,
+// overlapped with its writing; the copies are complete once ctx->st is
+// synchronised.  Text longer than host_cap is not copied.
+static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swift_reads* rd,
+                               const swift_params* p, size_t* out_len, swift_stats* stats,
+                               char* host_out, size_t host_cap) {
   if (!ctx || !idx || !rd || !p) return fail(ctx, SWIFT_E_ARG, "null argument");
   CK(cudaSetDevice(ctx->device));
   if (p->seed_len != idx->k || p->ignore_thres != idx->thres)
@@ -1984,7 +2003,16 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
   uint64_t total = 0;
   CK(cudaMemcpyAsync(&total, tot_d, 8, cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(h_cnt, cnt, sizeof(h_cnt), cudaMemcpyDeviceToHost, st));
+  // host output: records in kOutChunks ranges, each range's text copied to
+  // the host on the side stream while the next range is written
+  const int n_chunks = host_out && nproc >= kOutChunkMin ? kOutChunks : 1;
+  uint64_t rec_at[kOutChunks + 1], text_at[kOutChunks + 1];
+  for (int c = 0; c <= n_chunks; ++c) rec_at[c] = (uint64_t)nproc * c / n_chunks;
+  for (int c = 1; c < n_chunks; ++c)
+    CK(cudaMemcpyAsync(&text_at[c], offs + rec_at[c], 8, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
+  text_at[0] = 0;
+  text_at[n_chunks] = total;
   if (total + 1 > ctx->text_cap) {
     if (ctx->d_text) cudaFree(ctx->d_text);
     ctx->d_text = nullptr;
@@ -1993,12 +2021,40 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
     ctx->text_cap = cap;
   }
   fa.text = ctx->d_text;
-  if (sam)
-    launch_sam_write(st, fa);
-  else
-    launch_format_write(st, fa);
-  CKLAUNCH();
+  const bool to_host = host_out && total > 0 && total <= host_cap;
+  SideJoin copies(ctx);
+  if (to_host) {
+    rc = side_fork(ctx);
+    if (rc != SWIFT_OK) return rc;
+    copies.armed = true;
+    while (ctx->copy_ev.size() < (size_t)n_chunks) {
+      cudaEvent_t e;
+      CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      ctx->copy_ev.push_back(e);
+    }
+  }
+  for (int c = 0; c < n_chunks; ++c) {
+    fa.first = (int64_t)rec_at[c];
+    fa.n = (int64_t)rec_at[c + 1];
+    if (sam)
+      launch_sam_write(st, fa);
+    else
+      launch_format_write(st, fa);
+    CKLAUNCH();
+    if (to_host && text_at[c + 1] > text_at[c]) {
+      CK(cudaEventRecord(ctx->copy_ev[c], st));
+      CK(cudaStreamWaitEvent(ctx->side, ctx->copy_ev[c], 0));
+      CK(cudaMemcpyAsync(host_out + text_at[c], ctx->d_text + text_at[c],
+                         text_at[c + 1] - text_at[c], cudaMemcpyDeviceToHost, ctx->side));
+    }
+  }
+  fa.first = 0;
+  fa.n = nproc;
   CK(cudaEventRecord(ctx->ev[5], st));
+  if (to_host) {
+    rc = copies.join();
+    if (rc != SWIFT_OK) return rc;
+  }
   CK(cudaEventSynchronize(ctx->ev[5]));
   ctx->text_len = total;
   if (out_len) *out_len = total;
@@ -2044,11 +2100,16 @@ int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_rea
     s.bound_pruned = pruned;
     s.retraced_pairs = bounded ? h_cnt[4] : 0;
     // build_pairs + the Smith-Waterman passes and select (launches) +
-    // format sizes, scan, format write
-    s.launches = so.launches + (nproc > 0 ? 1 + 2 : 0) + launches + scan_k;
+    // format sizes, scan, format write (one per record range)
+    s.launches = so.launches + (nproc > 0 ? 1 + 1 + n_chunks : 0) + launches + scan_k;
     *stats = s;
   }
   return SWIFT_OK;
+}
+
+int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_reads* rd,
+                         const swift_params* p, size_t* out_len, swift_stats* stats) {
+  return align_resident_impl(ctx, idx, rd, p, out_len, stats, nullptr, 0);
 }
 
 int swift_fetch_output(swift_ctx* ctx, char* dst, size_t cap) {
@@ -2064,7 +2125,7 @@ int swift_align(swift_ctx* ctx, const swift_index* idx, const char* reads, size_
   CK(cudaSetDevice(ctx->device));
   swift_reads* rd = nullptr;
   double parse_ms = 0, h2d_ms = 0;
-  int rc = upload_reads(ctx, reads, len, &rd, &parse_ms, &h2d_ms);
+  int rc = upload_reads(ctx, reads, len, &rd, &parse_ms, &h2d_ms, true);
   if (rc != SWIFT_OK) return rc;
   size_t n = 0;
   rc = swift_align_resident(ctx, idx, rd, p, &n, stats);
@@ -2101,20 +2162,19 @@ int swift_align_into(swift_ctx* ctx, const swift_index* idx, const char* reads, 
   CK(cudaSetDevice(ctx->device));
   swift_reads* rd = nullptr;
   double parse_ms = 0, h2d_ms = 0;
-  int rc = upload_reads(ctx, reads, len, &rd, &parse_ms, &h2d_ms);
+  int rc = upload_reads(ctx, reads, len, &rd, &parse_ms, &h2d_ms, true);
   if (rc != SWIFT_OK) return rc;
   size_t n = 0;
-  rc = swift_align_resident(ctx, idx, rd, p, &n, stats);
+  // the text is copied to out while it is written
+  rc = align_resident_impl(ctx, idx, rd, p, &n, stats, out, out ? cap : 0);
   auto t0 = std::chrono::steady_clock::now();
   if (rc == SWIFT_OK) {
     *out_len = n;
-    if (n > cap) {
+    cudaError_t e = cudaStreamSynchronize(ctx->st);
+    if (e != cudaSuccess)
+      rc = fail(ctx, SWIFT_E_CUDA, cudaGetErrorString(e));
+    else if (n > cap)
       rc = fail(ctx, SWIFT_E_LIMIT, "output buffer too small");
-    } else if (n) {
-      cudaError_t e = cudaMemcpyAsync(out, ctx->d_text, n, cudaMemcpyDeviceToHost, ctx->st);
-      if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->st);
-      if (e != cudaSuccess) rc = fail(ctx, SWIFT_E_CUDA, cudaGetErrorString(e));
-    }
   }
   if (stats) {
     stats->host_parse_ms = parse_ms;
@@ -2138,9 +2198,9 @@ int swift_align_paired(swift_ctx* ctx, const swift_index* idx, const char* reads
   memset(&s, 0, sizeof(s));
   CK(cudaEventRecord(ctx->ev[0], st));
   swift_reads *rd1 = nullptr, *rd2 = nullptr;
-  int rc = upload_reads(ctx, reads1, len1, &rd1);
+  int rc = upload_reads(ctx, reads1, len1, &rd1, nullptr, nullptr, true);
   if (rc != SWIFT_OK) return rc;
-  rc = upload_reads(ctx, reads2, len2, &rd2);
+  rc = upload_reads(ctx, reads2, len2, &rd2, nullptr, nullptr, true);
   if (rc != SWIFT_OK) {
     swift_reads_destroy(rd1);
     return rc;

@@ -23,6 +23,7 @@ struct swift_ctx {
   cudaStream_t side = nullptr;  // second stream for concurrent launches, made on first use
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   std::vector<cudaEvent_t> chunk_ev;  // per-chunk timing of the trace pass, grown on use
+  std::vector<cudaEvent_t> copy_ev;   // text ranges ready for their host copy, grown on use
 };
 
 struct swift_index {
@@ -71,4 +72,5 @@ struct swift_reads {
   int32_t first_len = 0;  // getSeqSize
   int32_t min_len = 0, max_len = 0;
   std::vector<int32_t> repeats;
+  cudaStream_t pool_st = nullptr;  // buffers from this stream's pool (one call's reads)
 };

@@ -426,6 +426,7 @@ struct FormatArgs {
   const char* rcons;
   int64_t cons_stride;
   int64_t n;
+  int64_t first;              // write kernels: records [first, n)
   int64_t batch;              // Phase-2 batch size (best-per-read groups stop at batch ends)
   int32_t* keep;              // per record: 1 if printed
   uint64_t* bytes;            // per record: text bytes

@@ -193,7 +193,7 @@ constexpr int kFmtWarps = 8;
 __global__ void __launch_bounds__(kFmtWarps * 32) format_write_kernel(FormatArgs a) {
   __shared__ char hdr_all[kFmtWarps][320];  // header line: at most 257 bytes
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t j = (int64_t)blockIdx.x * kFmtWarps + wib;
+  const int64_t j = a.first + (int64_t)blockIdx.x * kFmtWarps + wib;
   if (j >= a.n || !a.keep[j]) return;
   const DevPair p = a.pairs[j];
   const DevAln al = a.aln[j];
@@ -308,7 +308,7 @@ __global__ void __launch_bounds__(kFmtWarps * 32) sam_write_kernel(FormatArgs a)
   __shared__ char ops_all[kFmtWarps][kSamMaxL];
   __shared__ uint32_t starts_all[kFmtWarps][kSamMaxL / 32];
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t j = (int64_t)blockIdx.x * kFmtWarps + wib;
+  const int64_t j = a.first + (int64_t)blockIdx.x * kFmtWarps + wib;
   if (j >= a.n) return;
   const DevPair p = a.pairs[j];
   const DevAln al = a.aln[j];
@@ -381,8 +381,9 @@ void launch_sam_sizes(cudaStream_t st, const FormatArgs& a) {
 }
 
 void launch_sam_write(cudaStream_t st, const FormatArgs& a) {
-  if (a.n <= 0) return;
-  sam_write_kernel<<<(unsigned)((a.n + kFmtWarps - 1) / kFmtWarps), kFmtWarps * 32, 0, st>>>(a);
+  const int64_t n = a.n - a.first;
+  if (n <= 0) return;
+  sam_write_kernel<<<(unsigned)((n + kFmtWarps - 1) / kFmtWarps), kFmtWarps * 32, 0, st>>>(a);
 }
 
 void launch_select(cudaStream_t st, const FormatArgs& a) {
@@ -406,8 +407,9 @@ void launch_format_sizes(cudaStream_t st, const FormatArgs& a) {
 }
 
 void launch_format_write(cudaStream_t st, const FormatArgs& a) {
-  if (a.n <= 0) return;
-  format_write_kernel<<<(unsigned)((a.n + kFmtWarps - 1) / kFmtWarps), kFmtWarps * 32, 0, st>>>(a);
+  const int64_t n = a.n - a.first;
+  if (n <= 0) return;
+  format_write_kernel<<<(unsigned)((n + kFmtWarps - 1) / kFmtWarps), kFmtWarps * 32, 0, st>>>(a);
 }
 
 }  // namespace swift

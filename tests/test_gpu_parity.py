@@ -395,6 +395,36 @@ def test_align_into_caller_buffer(ctx, oracle, sg):
     assert e.value.code == -5
 
 
+def test_align_into_overlapped_copies(ctx, sg):
+    # enough records for the text to go to the host in record ranges, each
+    # copied while the next is written: the same bytes as the one-piece path
+    import ctypes
+    import torch
+    from swift_gb300 import synth
+    names, seqs = synth.make_reference(600_000, 6, sigma=0.6, repeat_frac=0.1, n_units=30,
+                                       unit_len=300, divergence=0.03, seed=12)
+    ref = synth.fasta_bytes(names, seqs)
+    rn, rs, _ = synth.make_reads(seqs, 60_000, 100, 0.02, 0.002, 0.05, seed=13)
+    reads = synth.reads_fasta(rn, rs)
+    ix = ctx.index(ref)
+    src = torch.empty(len(reads), dtype=torch.uint8, pin_memory=True)
+    src.numpy()[:] = memoryview(reads)
+    for fmt in (0, 1):
+        p = sg.default_params(out_format=fmt)
+        want, st = ctx.align(ix, reads, p, stats=True)
+        assert st["records"] >= 65536
+        out = torch.zeros(len(want), dtype=torch.uint8, pin_memory=True)  # exact size
+        n, st2 = ctx.align_into(ix, src.data_ptr(), len(reads), out.data_ptr(), len(want), p)
+        assert n == len(want) and out.numpy().tobytes() == want, fmt
+        pageable = ctypes.create_string_buffer(len(want) + 1)
+        n, _ = ctx.align_into(ix, src.data_ptr(), len(reads), ctypes.addressof(pageable),
+                              len(pageable), p)
+        assert pageable.raw[:n] == want
+        with pytest.raises(sg.SwiftError) as e:
+            ctx.align_into(ix, src.data_ptr(), len(reads), out.data_ptr(), len(want) - 1, p)
+        assert e.value.code == -5
+
+
 def test_cli_matches_oracle(ctx, oracle, sg):
     ref, reads = small_case(n_reads=300, seed=55)
     with tempfile.TemporaryDirectory() as d:
