@@ -868,6 +868,7 @@ int swift_index_build(swift_ctx* ctx, const char* ref, size_t len, int32_t k, in
   CKI(cudaMalloc(&ix->d_recs, std::max(nr, 1) * sizeof(DevRecord)));
   CKI(cudaMalloc(&ix->d_cat, (size_t)n_words * 16 + 64));
   CKI(cudaMalloc(&ix->d_packed, ((size_t)n_words + 2) * sizeof(uint32_t)));
+  CKI(cudaMalloc(&ix->d_odd, (size_t)odd_bits_words(n_words) * sizeof(uint32_t)));
   CKI(cudaMalloc(&ix->d_count, (size_t)ix->nb * sizeof(uint32_t)));
   CKI(cudaMalloc(&ix->d_offsets, ((size_t)ix->nb + 1) * sizeof(uint32_t)));
   {
@@ -896,6 +897,7 @@ int swift_index_build(swift_ctx* ctx, const char* ref, size_t len, int32_t k, in
     CKI(cudaMemsetAsync(d_cursor, 0, (size_t)ix->nb * sizeof(uint32_t), st));
     launch_compact_lines(st, ix->d_file, d_src, d_dst, d_len, n_lines, ix->d_cat);
     launch_pack2bit(st, ix->d_cat, n_words, ix->d_packed);
+    launch_odd_bits(st, ix->d_cat, n_words, ix->d_odd);
     launch_count_tuples(st, ix->d_packed, ix->d_recs, d_tbase, nr, n_tuples, k, ix->d_count);
     launch_threshold(st, ix->d_count, ix->nb, (uint32_t)thres, d_eff);
     exclusive_scan_u32(st, d_eff, ix->d_offsets, ix->nb, tmp, ix->d_offsets + ix->nb);
@@ -933,6 +935,7 @@ int swift_index_destroy(swift_index* ix) {
   cudaFree(ix->d_recs);
   cudaFree(ix->d_cat);
   cudaFree(ix->d_packed);
+  cudaFree(ix->d_odd);
   cudaFree(ix->d_count);
   cudaFree(ix->d_offsets);
   cudaFree(ix->d_groups);
@@ -1754,6 +1757,7 @@ static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swi
   pa.ref_file = idx->d_file;
   pa.ref_file_len = idx->file_len;
   pa.cat = (const char*)idx->d_cat;
+  pa.odd = idx->d_odd;
   pa.recs = idx->d_recs;
   pa.reads = rd->d_bytes;
   pa.rd = rd->d_rd;

@@ -35,6 +35,7 @@ struct swift_index {
   std::vector<swift::RefRecord> recs;
   uint8_t* d_cat = nullptr;
   uint32_t* d_packed = nullptr;
+  uint32_t* d_odd = nullptr;    // non-ACGT positions of d_cat, one bit each
   uint64_t cat_len = 0;
   uint32_t* d_count = nullptr;
   uint32_t* d_offsets = nullptr;

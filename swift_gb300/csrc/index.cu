@@ -218,6 +218,29 @@ void launch_compact_lines(cudaStream_t st, const char* file, const uint64_t* src
                                                                     cat);
 }
 
+// Bit b of odd[t]: byte 32 t + b of cat is not one of ACGTacgt (the zero
+// padding after the last base counts as such).
+__global__ void odd_bits_kernel(const uint8_t* __restrict__ cat, int64_t n_out,
+                                uint32_t* __restrict__ odd) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (; t < n_out; t += stride) {
+    uint32_t bits = 0;
+    for (int b = 0; b < 32; ++b) {
+      const uint32_t u = cat[32 * t + b] & 0xDFu;
+      if (!(u == 'A' || u == 'C' || u == 'G' || u == 'T')) bits |= 1u << b;
+    }
+    odd[t] = bits;
+  }
+}
+
+void launch_odd_bits(cudaStream_t st, const uint8_t* cat, int64_t n_words, uint32_t* odd) {
+  // the last word reads bytes up to 32 * odd_bits_words(n_words) - 1 <
+  // 16 * n_words + 64
+  const int64_t n_out = odd_bits_words(n_words);
+  odd_bits_kernel<<<grid_for(n_out, 256), 256, 0, st>>>(cat, n_out, odd);
+}
+
 void launch_pack2bit(cudaStream_t st, const uint8_t* cat, int64_t n_words, uint32_t* packed) {
   if (n_words <= 0) return;
   pack2bit_kernel<<<grid_for(n_words, 256), 256, 0, st>>>(cat, n_words, packed);

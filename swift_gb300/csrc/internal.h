@@ -105,6 +105,10 @@ void launch_compact_lines(cudaStream_t st, const char* file, const uint64_t* src
                           const uint64_t* dst, const uint32_t* len, int64_t n_lines,
                           uint8_t* cat);
 void launch_pack2bit(cudaStream_t st, const uint8_t* cat, int64_t n_words, uint32_t* packed);
+// words of the odd-base bitmap of a cat buffer of n_words 16-byte words
+// (the bitmap's reads of cat stay inside the buffer's 64 bytes of padding)
+inline int64_t odd_bits_words(int64_t n_words) { return (n_words * 16 + 31) / 32 + 1; }
+void launch_odd_bits(cudaStream_t st, const uint8_t* cat, int64_t n_words, uint32_t* odd);
 void launch_count_tuples(cudaStream_t st, const uint32_t* packed, const DevRecord* recs,
                          const uint64_t* tbase, int n_recs, uint64_t n_tuples, int k,
                          uint32_t* count);
@@ -216,6 +220,7 @@ struct PairArgs {
   const char* ref_file;
   uint64_t ref_file_len;
   const char* cat;            // concatenated record sequences
+  const uint32_t* odd;        // optional: bit p of odd[p / 32] set where cat[p] is not ACGTacgt
   const DevRecord* recs;
   const char* reads;
   const DevRead* rd;

@@ -78,57 +78,98 @@ __global__ void __launch_bounds__(kPairWarps * 32) build_pairs_kernel(PairArgs a
   const uint32_t off = (uint32_t)rec.seq_off + (uint32_t)dist +
                        (rec.bpl > 0 ? (uint32_t)dist / rec.bpl : 0u);
   int got = 0;
-  if (rec.regular) {
-    // the window is concatenated positions dist .. dist + 299 of the record
-    const uint64_t avail = rec.cat_len > (uint64_t)dist ? rec.cat_len - (uint64_t)dist : 0;
-    got = avail < (uint64_t)kWin ? (int)avail : kWin;
-    const char* src = a.cat + rec.cat_start + dist;
-#pragma unroll
-    for (int t = 0; t < (kWin + 31) / 32; ++t) {
-      const int i = lane + 32 * t;
-      if (i < got) tmp[i] = src[i];
-    }
-  } else {
-    got = fetch_window(a, off, tmp, lane);
-  }
-  __syncwarp();
-  // N trimming (see the restatement notes at the top of this file)
-  int lead = 0;
-  {
-    bool isn = false;
-    for (int base = 0; base < got; base += 32) {
-      int i = base + lane;
-      isn = i < got && (tmp[i] == 'N' || tmp[i] == 'n');
-      uint32_t notn = __ballot_sync(0xffffffffu, !isn && i < got);
-      if (notn) {
-        lead = base + __ffs(notn) - 1;
-        break;
-      }
-      lead = base + 32 < got ? base + 32 : got;
-    }
-  }
-  int len = got;
-  if (lead == 0 && got > 0) {
-    for (int base = ((got - 1) / 32) * 32; base >= 0; base -= 32) {
-      int i = base + lane;
-      bool notn = i < got && !(tmp[i] == 'N' || tmp[i] == 'n');
-      uint32_t b = __ballot_sync(0xffffffffu, notn);
-      if (b) {
-        len = base + 31 - __clz(b) + 1;
-        break;
-      }
-      len = base;
-    }
-  }
-  int wl = len - lead;
-  if (wl < 0) wl = 0;
   char* wout = a.wbuf + j * kWinPad;
   bool odd = false;  // a byte the packed score pass does not take
-  for (int i = lane; i < kWinPad; i += 32) {
-    const char c = i < wl ? tmp[lead + i] : '\0';
-    wout[i] = c;
-    if (i < wl && !is_acgt(c)) odd = true;
+  int wl = 0;
+  // Common case: a whole window inside a record of regular lines with only
+  // ACGTacgt bytes (no N to trim): a straight copy of the concatenated bases,
+  // 16 bytes per lane.
+  bool direct = false;
+  if (rec.regular && a.odd) {
+    const uint64_t avail = rec.cat_len > (uint64_t)dist ? rec.cat_len - (uint64_t)dist : 0;
+    if (avail >= (uint64_t)kWin) {
+      const uint64_t g0 = rec.cat_start + (uint64_t)dist, g1 = g0 + kWin - 1;
+      const uint64_t w0 = g0 >> 5;
+      uint32_t bits = 0;
+      if ((uint64_t)lane <= (g1 >> 5) - w0) {
+        bits = a.odd[w0 + lane];
+        if (lane == 0) bits &= ~0u << (g0 & 31);
+        if (w0 + lane == (g1 >> 5)) bits &= ~0u >> (31 - (g1 & 31));
+      }
+      direct = !__any_sync(0xffffffffu, bits != 0);
+    }
   }
+  if (direct) {
+    static_assert(kWinPad % 16 == 0 && kWin % 4 == 0 && kWinPad - kWin == 4,
+                  "the last lane's fourth word is the padding");
+    if (lane < kWinPad / 16) {
+      // four output words from five aligned loads (the reads past the
+      // window's end stay inside the cat buffer's padding)
+      const uintptr_t ad = (uintptr_t)(a.cat + rec.cat_start + dist + 16 * lane);
+      const uint32_t* wp = reinterpret_cast<const uint32_t*>(ad & ~(uintptr_t)3);
+      const uint32_t sh = (uint32_t)(ad & 3) * 8;
+      uint32_t w[5];
+#pragma unroll
+      for (int q = 0; q < 5; ++q) w[q] = wp[q];
+      uint4 o;
+      o.x = __funnelshift_r(w[0], w[1], sh);
+      o.y = __funnelshift_r(w[1], w[2], sh);
+      o.z = __funnelshift_r(w[2], w[3], sh);
+      o.w = lane == kWinPad / 16 - 1 ? 0u : __funnelshift_r(w[3], w[4], sh);
+      *reinterpret_cast<uint4*>(wout + 16 * lane) = o;
+    }
+    wl = kWin;
+  } else {
+    if (rec.regular) {
+      // the window is concatenated positions dist .. dist + 299 of the record
+      const uint64_t avail = rec.cat_len > (uint64_t)dist ? rec.cat_len - (uint64_t)dist : 0;
+      got = avail < (uint64_t)kWin ? (int)avail : kWin;
+      const char* src = a.cat + rec.cat_start + dist;
+#pragma unroll
+      for (int t = 0; t < (kWin + 31) / 32; ++t) {
+        const int i = lane + 32 * t;
+        if (i < got) tmp[i] = src[i];
+      }
+    } else {
+      got = fetch_window(a, off, tmp, lane);
+    }
+    __syncwarp();
+    // N trimming (see the restatement notes at the top of this file)
+    int lead = 0;
+    {
+      bool isn = false;
+      for (int base = 0; base < got; base += 32) {
+        int i = base + lane;
+        isn = i < got && (tmp[i] == 'N' || tmp[i] == 'n');
+        uint32_t notn = __ballot_sync(0xffffffffu, !isn && i < got);
+        if (notn) {
+          lead = base + __ffs(notn) - 1;
+          break;
+        }
+        lead = base + 32 < got ? base + 32 : got;
+      }
+    }
+    int len = got;
+    if (lead == 0 && got > 0) {
+      for (int base = ((got - 1) / 32) * 32; base >= 0; base -= 32) {
+        int i = base + lane;
+        bool notn = i < got && !(tmp[i] == 'N' || tmp[i] == 'n');
+        uint32_t b = __ballot_sync(0xffffffffu, notn);
+        if (b) {
+          len = base + 31 - __clz(b) + 1;
+          break;
+        }
+        len = base;
+      }
+    }
+    wl = len - lead;
+    if (wl < 0) wl = 0;
+    for (int i = lane; i < kWinPad; i += 32) {
+      const char c = i < wl ? tmp[lead + i] : '\0';
+      wout[i] = c;
+      if (i < wl && !is_acgt(c)) odd = true;
+    }
+  }  // window not copied directly
   // query
   const DevRead rd = a.rd[read];
   const char* s = a.reads + rd.seq_off;

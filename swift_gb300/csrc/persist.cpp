@@ -252,6 +252,7 @@ int swift_index_load(swift_ctx* ctx, const char* path, swift_index** out) {
   CKL(cudaMalloc(&ix->d_post, std::max<uint64_t>(h.total, 1) * sizeof(uint2)));
   CKL(cudaMalloc(&ix->d_cat, nw * 16 + 64));
   CKL(cudaMalloc(&ix->d_packed, (nw + 2) * 4));
+  CKL(cudaMalloc(&ix->d_odd, (size_t)odd_bits_words((int64_t)nw) * 4));
   if (h.has_lt13) {
     ix->n_tup13 = h.n_tup13;
     ix->max_comp13 = h.max_comp13;
@@ -279,6 +280,10 @@ int swift_index_load(swift_ctx* ctx, const char* path, swift_index** out) {
     dr[i].regular = ix->recs[i].regular ? 1 : 0;
   }
   if (nr) CKL(cudaMemcpy(ix->d_recs, dr.data(), nr * sizeof(DevRecord), cudaMemcpyHostToDevice));
+  // derived from the bases, not stored
+  launch_odd_bits(nullptr, ix->d_cat, (int64_t)nw, ix->d_odd);
+  CKL(cudaGetLastError());
+  CKL(cudaDeviceSynchronize());
 #undef CKL
   ix->lt13_ready = h.has_lt13 != 0;
   *out = ix;
