@@ -85,6 +85,10 @@ __device__ __forceinline__ uint32_t sel(uint32_t m, uint32_t a, uint32_t b) {
 // 2 * (k & 7) (first pair) and 16 + 2 * (k & 7) (second pair) of row k are
 // 2 for DIAG, 1 for UP and 0 for LEFT or NONE (NONE is the cell with H = 0,
 // which the traceback knows from the scores).
+// first-maximum tags of the trace pass (see packed_item)
+constexpr uint32_t kTagOld = 0x000F000Fu;
+constexpr int kTagWindow = 12;
+
 template <int RPL>
 struct DirLayout {
   static constexpr int kWords = (RPL + 7) / 8;  // words per lane and step
@@ -146,7 +150,7 @@ __device__ __forceinline__ void packed_item(const FastArgs& a, const int64_t war
     h16p[k] = BB;  // H[i][0] = 0
     xl[k] = BB;    // column 0 is NONE
     if (TRACE) {
-      bestv[k] = BB;
+      bestv[k] = BB | kTagOld;  // H = 0 cells (key B + tag < B + 15) never replace it
       bestc[k] = 0;
     }
   }
@@ -158,7 +162,8 @@ __device__ __forceinline__ void packed_item(const FastArgs& a, const int64_t war
   // one wavefront step; acc receives the step's direction words.  `full`
   // (std::true_type) marks a step whose columns lie inside the window on
   // every lane of the group: the range check and its merges drop out.
-  auto step = [&](const int s, uint32_t* acc, auto full) {
+  // tag: the step's first-maximum tag (trace pass), both halves.
+  auto step = [&](const int s, uint32_t* acc, auto full, const uint32_t tag) {
     constexpr bool kFull = decltype(full)::value;
     uint32_t up = __shfl_up_sync(0xffffffffu, send_u, 1, G);
     const uint32_t rh = __shfl_up_sync(0xffffffffu, send_h, 1, G);
@@ -168,7 +173,6 @@ __device__ __forceinline__ void packed_item(const FastArgs& a, const int64_t war
     for (int w = 0; w < kNW; ++w) acc[w] = 0;
     if (kFull || (j >= 1 && j <= R)) {
       const uint32_t ws = wsel[j];
-      const uint32_t jj = (uint32_t)j * 0x00010001u;
       // VAR: halves whose window ends before column j
       const uint32_t cm = VAR ? ((j <= R0 ? 0x0000FFFFu : 0u) | (j <= R1 ? 0xFFFF0000u : 0u)) : ~0u;
       uint32_t dg = diag;
@@ -187,9 +191,10 @@ __device__ __forceinline__ void packed_item(const FastArgs& a, const int64_t war
         up = (hx & 0x00020002u) * KU + h16;
         xl[k] = (hx & 0x00010001u) * KL + h16;
         if (TRACE) {
-          const uint32_t m = VAR ? gt_mask(h16, bestv[k]) & cm : gt_mask(h16, bestv[k]);
-          bestv[k] = sel(m, h16, bestv[k]);
-          bestc[k] = sel(m, jj, bestc[k]);
+          // first maximum of the row: the key's tag makes an earlier step of
+          // the window win a tie, and the window's last best keeps tag 15
+          const uint32_t key = VAR ? (h16 + tag) & cm : h16 + tag;
+          bestv[k] = __vimax_s16x2_relu(bestv[k], key);  // both non-negative
           // bits 1 (UP) and 2 (DIAG) of each half's code to 2 * (k & 7)
           if ((k & 7) == 0) {
             acc[k >> 3] |= (hx >> 1) & 0x00030003u;
@@ -210,19 +215,43 @@ __device__ __forceinline__ void packed_item(const FastArgs& a, const int64_t war
     diag = sl == 0 ? BB : rh;
   };
   const int steps = R + G - 1;
+  // Trace pass, first maximum of each row: the key of a cell is h16 + tag,
+  // tag = 14 - (its step's offset in a window of kTagWindow steps), so one
+  // max keeps the largest H and, among equal H, the earliest step of the
+  // window.  At the window's end the halves whose tag is not 15 took a new
+  // maximum there: their column (stored + 32, so no half borrows) is
+  // recovered from the tag and the tag is set to 15, above every tag a
+  // later window can give an equal H.
+  int sw = 0;  // first step of the current window
+  auto flush_window = [&]() {
+    if (!TRACE) return;
+    const uint32_t base = (uint32_t)(sw - sl + 1 + 14 + 32) * 0x00010001u;
+#pragma unroll
+    for (int k = 0; k < (TRACE ? RPL : 0); ++k) {
+      const uint32_t tg = bestv[k] & kTagOld;
+      // tags 3..15 shifted to the half exponent: normal numbers, same order
+      const uint32_t m = gt_mask(kTagOld << 10, tg << 10);
+      bestc[k] = sel(m, base - tg, bestc[k]);
+      bestv[k] |= kTagOld;
+    }
+  };
   // steps in blocks of 4: the trace pass keeps a block's direction words in
   // registers and writes each word index as one 16-byte store
   uint32_t hist[TRACE ? 4 : 1][kNW];
   for (int s0 = 0; s0 < steps; s0 += 4) {
     // steps s0..s0+3 have 1 <= j <= R on every lane when s0 >= G - 1 and
     // s0 + 3 <= R - 1 (then also s0 + 3 < steps)
+    // tag of step s0 + u: 14 - (its offset in the window)
+    const uint32_t tag0 = (uint32_t)(14 - (s0 - sw)) * 0x00010001u;
     if (s0 >= G - 1 && s0 + 3 <= R - 1) {
 #pragma unroll
-      for (int u = 0; u < 4; ++u) step(s0 + u, hist[TRACE ? u : 0], std::true_type());
+      for (int u = 0; u < 4; ++u)
+        step(s0 + u, hist[TRACE ? u : 0], std::true_type(), tag0 - (uint32_t)u * 0x00010001u);
     } else {
 #pragma unroll
       for (int u = 0; u < 4; ++u)
-        if (s0 + u < steps) step(s0 + u, hist[TRACE ? u : 0], std::false_type());
+        if (s0 + u < steps)
+          step(s0 + u, hist[TRACE ? u : 0], std::false_type(), tag0 - (uint32_t)u * 0x00010001u);
     }
     if (TRACE) {
 #pragma unroll
@@ -230,6 +259,10 @@ __device__ __forceinline__ void packed_item(const FastArgs& a, const int64_t war
         // words past the last step are never read
         const uint4 v = make_uint4(hist[0][w], hist[1][w], hist[2][w], hist[3][w]);
         __stcg(reinterpret_cast<uint4*>(dirs + (int64_t)w * S8 + s0), v);
+      }
+      if (s0 + 4 - sw == kTagWindow) {
+        flush_window();
+        sw = s0 + 4;
       }
     }
     // Early stop: after step s = kSufSteps * m + G - 1 every cell left lies
@@ -255,6 +288,7 @@ __device__ __forceinline__ void packed_item(const FastArgs& a, const int64_t war
       if (__all_sync(0xffffffffu, done0 && done1)) break;
     }
   }
+  flush_window();
   if (!TRACE) {
     // maximum of the group, per packed pair
     uint32_t v = bestv[0];
@@ -279,7 +313,7 @@ __device__ __forceinline__ void packed_item(const FastArgs& a, const int64_t war
       const uint32_t v = (bestv[k] >> sh) & 0xFFFFu;
       if (k < nrows && v > bv) {
         bv = v;
-        bc = (bestc[k] >> sh) & 0xFFFFu;
+        bc = ((bestc[k] >> sh) & 0xFFFFu) - 32u;
         br = (uint32_t)(sl * RPL + k + 1);
       }
     }
