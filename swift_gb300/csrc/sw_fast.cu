@@ -77,11 +77,13 @@ __device__ __forceinline__ uint32_t sel(uint32_t m, uint32_t a, uint32_t b) {
   return (a & m) | (b & ~m);
 }
 
-// Direction scratch of the trace pass, per group (two pairs): for each lane
-// ln and word w, the words of all wavefront steps are contiguous,
-//     region[(ln * kDirWords + w) * steps8 + step],  steps8 = steps rounded up to 8,
-// so a traceback, which moves one step back on most cells, reads
-// consecutive words.  A word holds 8 rows x 2 pairs x 2 bits: bits
+// Direction scratch of the trace pass, per group (two pairs): per lane ln
+// the words of consecutive wavefront steps, the kDirWords words of a step
+// side by side,
+//     region[(ln * steps8 + step) * kDirWords + w],  steps8 = steps rounded up to 8,
+// so a block of 4 steps is one 16 * kDirWords-byte store and a traceback,
+// which moves one step back on most cells, reads neighbouring words of one
+// stream per lane.  A word holds 8 rows x 2 pairs x 2 bits: bits
 // 2 * (k & 7) (first pair) and 16 + 2 * (k & 7) (second pair) of row k are
 // 2 for DIAG, 1 for UP and 0 for LEFT or NONE (NONE is the cell with H = 0,
 // which the traceback knows from the scores).
@@ -254,11 +256,14 @@ __device__ __forceinline__ void packed_item(const FastArgs& a, const int64_t war
           step(s0 + u, hist[TRACE ? u : 0], std::false_type(), tag0 - (uint32_t)u * 0x00010001u);
     }
     if (TRACE) {
+      // words s0 * kNW .. (s0 + 4) * kNW - 1 of the lane, step-major (words
+      // past the last step are never read)
 #pragma unroll
-      for (int w = 0; w < kNW; ++w) {
-        // words past the last step are never read
-        const uint4 v = make_uint4(hist[0][w], hist[1][w], hist[2][w], hist[3][w]);
-        __stcg(reinterpret_cast<uint4*>(dirs + (int64_t)w * S8 + s0), v);
+      for (int q = 0; q < kNW; ++q) {
+        const int f = 4 * q;
+        const uint4 v = make_uint4(hist[f / kNW][f % kNW], hist[(f + 1) / kNW][(f + 1) % kNW],
+                                   hist[(f + 2) / kNW][(f + 2) % kNW], hist[(f + 3) / kNW][(f + 3) % kNW]);
+        __stcg(reinterpret_cast<uint4*>(dirs + (int64_t)s0 * kNW) + q, v);
       }
       if (s0 + 4 - sw == kTagWindow) {
         flush_window();
@@ -540,7 +545,7 @@ __global__ void __launch_bounds__(256) sw_walk_kernel(FastArgs a) {
   // 2 DIAG, 1 UP, 0 LEFT or NONE
   auto code_at = [&](int i, int jj) -> uint32_t {
     const int ln = (i - 1) / RPL, k = (i - 1) % RPL;
-    const int64_t at = (int64_t)(ln * kNW + (k >> 3)) * S8 + (jj + ln - 1);
+    const int64_t at = ((int64_t)ln * S8 + (jj + ln - 1)) * kNW + (k >> 3);
     if (at != last) {
       word = __ldcg(&dirs[at]);
       last = at;
