@@ -261,8 +261,6 @@ int swift_align_resident(swift_ctx *ctx, const swift_index *idx,
  * cap bytes). */
 int swift_fetch_output(swift_ctx *ctx, char *dst, size_t cap);
 
-/* File-to-file pipeline, the CLI: reads the two FASTA files and writes the
- * default output records to out_path. */
 /* Paired-end alignment (-q / -q2), the GPU branch of src/main.cu:172-212:
  * replaces searchQueries_paired2 (src/search.cu:2084-2200, lookupTable2
  * seeding of both mates and their reverse complements, 3 hits each) and
@@ -276,13 +274,22 @@ int swift_fetch_output(swift_ctx *ctx, char *dst, size_t cap);
  * or 2 (SWIFT_E_INPUT otherwise).  The lookupTable2 positions are built on
  * the index at first use (with the reference's fixed 1000-repeat threshold).
  * The output is malloc'ed (swift_free).  Of the stats, seed_ms (both
- * files), pairs_ms, sw_ms, select_ms (host pairing), format_ms and
+ * files), pairs_ms, sw_ms, select_ms (mate pairing), format_ms and
  * total_ms, reads (both mates), records, printed and cells are set. */
 int swift_align_paired(swift_ctx *ctx, const swift_index *idx, const char *reads1,
                        size_t len1, const char *reads2, size_t len2, const swift_params *p,
                        uint32_t min_frag, uint32_t max_frag, char **out, size_t *out_len,
                        swift_stats *stats);
+/* swift_align_paired into the caller's buffer out (cap bytes; pinned host
+ * memory lets the copies overlap the writing of the text): *out_len is the
+ * text length, SWIFT_E_LIMIT when it exceeds cap. */
+int swift_align_paired_into(swift_ctx *ctx, const swift_index *idx, const char *reads1,
+                            size_t len1, const char *reads2, size_t len2,
+                            const swift_params *p, uint32_t min_frag, uint32_t max_frag,
+                            char *out, size_t cap, size_t *out_len, swift_stats *stats);
 
+/* File-to-file pipeline, the CLI: reads the two FASTA files and writes the
+ * default output records to out_path. */
 int swift_align_files(swift_ctx *ctx, const char *qry_path, const char *ref_path,
                       const char *out_path, const swift_params *p);
 

@@ -23,7 +23,7 @@ EXPORTS = [
     "swift_ctx_info", "swift_ctx_set_sw_path",
     "swift_index_build", "swift_index_destroy", "swift_index_info", "swift_index_export",
     "swift_seed", "swift_seed_lt13", "swift_index_save", "swift_index_load",
-    "swift_index_params", "swift_align_paired", "swift_sw_batch", "swift_align", "swift_reads_upload",
+    "swift_index_params", "swift_align_paired", "swift_align_paired_into", "swift_sw_batch", "swift_align", "swift_reads_upload",
     "swift_reads_destroy", "swift_align_resident", "swift_fetch_output",
     "swift_align_files", "swift_free", "swift_peak_dpx", "swift_align_into",
     "swift_sw_batch_noalloc", "swift_sw_pairs", "swift_server_create", "swift_server_submit",
@@ -116,6 +116,8 @@ def lib():
         L.swift_align_paired.argtypes = [vp, vp, C.c_char_p, sz, C.c_char_p, sz, C.POINTER(Params),
                                          C.c_uint32, C.c_uint32, C.POINTER(vp), C.POINTER(sz),
                                          vp]
+        L.swift_align_paired_into.argtypes = [vp, vp, vp, sz, vp, sz, C.POINTER(Params),
+                                              C.c_uint32, C.c_uint32, vp, sz, C.POINTER(sz), vp]
         L.swift_sw_batch.argtypes = [vp, vp, vp, i32, i32, i64, i32, i32, i32, i32,
                                      vp, vp, vp, vp, vp, vp]
         L.swift_align.argtypes = [vp, vp, vp, sz, C.POINTER(Params), C.POINTER(vp),
@@ -310,6 +312,20 @@ class Context:
         text = C.string_at(out, n.value)
         lib().swift_free(out)
         return (text, st.as_dict()) if stats else text
+
+    def align_paired_into(self, index: "Index", ptr1: int, len1: int, ptr2: int, len2: int,
+                          out_ptr: int, cap: int, params: Params | None = None,
+                          min_frag: int = 99, max_frag: int = 600):
+        """Paired-end alignment with host buffers given by address (for
+        example pinned memory); returns (bytes written, stats)."""
+        p = params or default_params(seed_len=index.seed_len, ignore_thres=index.ignore_thres)
+        n = C.c_size_t()
+        st = Stats()
+        self._check(lib().swift_align_paired_into(self._h, index._h, C.c_void_p(ptr1), len1,
+                                                  C.c_void_p(ptr2), len2, C.byref(p), min_frag,
+                                                  max_frag, C.c_void_p(out_ptr), cap, C.byref(n),
+                                                  C.byref(st)))
+        return n.value, st.as_dict()
 
     def align_into(self, index: "Index", reads_ptr: int, nbytes: int, out_ptr: int, cap: int,
                    params: Params | None = None):

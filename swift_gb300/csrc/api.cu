@@ -95,6 +95,61 @@ struct SideJoin {
 constexpr int kOutChunks = 16;
 constexpr int64_t kOutChunkMin = 65536;
 
+// Text of records [0, n) written in record ranges; with a host buffer each
+// range is copied there on the side stream while the next one is written.
+struct TextChunks {
+  int n_chunks = 1;
+  uint64_t rec_at[kOutChunks + 1] = {}, text_at[kOutChunks + 1] = {};
+  // Queues the copies of the range starts' text offsets (offs: exclusive
+  // scan of the record sizes); they hold after the caller's next
+  // synchronisation of st.
+  int plan(swift_ctx* ctx, cudaStream_t st, const uint64_t* offs, int64_t n, bool to_host) {
+    n_chunks = to_host && n >= kOutChunkMin ? kOutChunks : 1;
+    for (int c = 0; c <= n_chunks; ++c) rec_at[c] = (uint64_t)n * c / n_chunks;
+    for (int c = 1; c < n_chunks; ++c)
+      CK(cudaMemcpyAsync(&text_at[c], offs + rec_at[c], 8, cudaMemcpyDeviceToHost, st));
+    return SWIFT_OK;
+  }
+  // After that synchronisation: the write kernels into text (total bytes),
+  // `done` recorded on st after the last one.  The text goes to host_out
+  // when it fits host_cap; the copies are complete once st is synchronised.
+  int write(swift_ctx* ctx, cudaStream_t st, FormatArgs fa, bool sam, char* text, uint64_t total,
+            char* host_out, size_t host_cap, cudaEvent_t done) {
+    text_at[0] = 0;
+    text_at[n_chunks] = total;
+    fa.text = text;
+    const bool to_host = host_out && total > 0 && total <= host_cap;
+    SideJoin copies(ctx);
+    if (to_host) {
+      const int rc = side_fork(ctx);
+      if (rc != SWIFT_OK) return rc;
+      copies.armed = true;
+      while (ctx->copy_ev.size() < (size_t)n_chunks) {
+        cudaEvent_t e;
+        CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        ctx->copy_ev.push_back(e);
+      }
+    }
+    for (int c = 0; c < n_chunks; ++c) {
+      fa.first = (int64_t)rec_at[c];
+      fa.n = (int64_t)rec_at[c + 1];
+      if (sam)
+        launch_sam_write(st, fa);
+      else
+        launch_format_write(st, fa);
+      CKLAUNCH();
+      if (to_host && text_at[c + 1] > text_at[c]) {
+        CK(cudaEventRecord(ctx->copy_ev[c], st));
+        CK(cudaStreamWaitEvent(ctx->side, ctx->copy_ev[c], 0));
+        CK(cudaMemcpyAsync(host_out + text_at[c], text + text_at[c], text_at[c + 1] - text_at[c],
+                           cudaMemcpyDeviceToHost, ctx->side));
+      }
+    }
+    CK(cudaEventRecord(done, st));
+    return to_host ? copies.join() : SWIFT_OK;
+  }
+};
+
 void keep_pool(int device) {
   cudaMemPool_t pool;
   if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
@@ -2007,16 +2062,10 @@ static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swi
   uint64_t total = 0;
   CK(cudaMemcpyAsync(&total, tot_d, 8, cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(h_cnt, cnt, sizeof(h_cnt), cudaMemcpyDeviceToHost, st));
-  // host output: records in kOutChunks ranges, each range's text copied to
-  // the host on the side stream while the next range is written
-  const int n_chunks = host_out && nproc >= kOutChunkMin ? kOutChunks : 1;
-  uint64_t rec_at[kOutChunks + 1], text_at[kOutChunks + 1];
-  for (int c = 0; c <= n_chunks; ++c) rec_at[c] = (uint64_t)nproc * c / n_chunks;
-  for (int c = 1; c < n_chunks; ++c)
-    CK(cudaMemcpyAsync(&text_at[c], offs + rec_at[c], 8, cudaMemcpyDeviceToHost, st));
+  TextChunks chunks;
+  rc = chunks.plan(ctx, st, offs, nproc, host_out != nullptr);
+  if (rc != SWIFT_OK) return rc;
   CK(cudaStreamSynchronize(st));
-  text_at[0] = 0;
-  text_at[n_chunks] = total;
   if (total + 1 > ctx->text_cap) {
     if (ctx->d_text) cudaFree(ctx->d_text);
     ctx->d_text = nullptr;
@@ -2024,41 +2073,8 @@ static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swi
     CK(cudaMalloc(&ctx->d_text, cap));
     ctx->text_cap = cap;
   }
-  fa.text = ctx->d_text;
-  const bool to_host = host_out && total > 0 && total <= host_cap;
-  SideJoin copies(ctx);
-  if (to_host) {
-    rc = side_fork(ctx);
-    if (rc != SWIFT_OK) return rc;
-    copies.armed = true;
-    while (ctx->copy_ev.size() < (size_t)n_chunks) {
-      cudaEvent_t e;
-      CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-      ctx->copy_ev.push_back(e);
-    }
-  }
-  for (int c = 0; c < n_chunks; ++c) {
-    fa.first = (int64_t)rec_at[c];
-    fa.n = (int64_t)rec_at[c + 1];
-    if (sam)
-      launch_sam_write(st, fa);
-    else
-      launch_format_write(st, fa);
-    CKLAUNCH();
-    if (to_host && text_at[c + 1] > text_at[c]) {
-      CK(cudaEventRecord(ctx->copy_ev[c], st));
-      CK(cudaStreamWaitEvent(ctx->side, ctx->copy_ev[c], 0));
-      CK(cudaMemcpyAsync(host_out + text_at[c], ctx->d_text + text_at[c],
-                         text_at[c + 1] - text_at[c], cudaMemcpyDeviceToHost, ctx->side));
-    }
-  }
-  fa.first = 0;
-  fa.n = nproc;
-  CK(cudaEventRecord(ctx->ev[5], st));
-  if (to_host) {
-    rc = copies.join();
-    if (rc != SWIFT_OK) return rc;
-  }
+  rc = chunks.write(ctx, st, fa, sam, ctx->d_text, total, host_out, host_cap, ctx->ev[5]);
+  if (rc != SWIFT_OK) return rc;
   CK(cudaEventSynchronize(ctx->ev[5]));
   ctx->text_len = total;
   if (out_len) *out_len = total;
@@ -2105,7 +2121,7 @@ static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swi
     s.retraced_pairs = bounded ? h_cnt[4] : 0;
     // build_pairs + the Smith-Waterman passes and select (launches) +
     // format sizes, scan, format write (one per record range)
-    s.launches = so.launches + (nproc > 0 ? 1 + 1 + n_chunks : 0) + launches + scan_k;
+    s.launches = so.launches + (nproc > 0 ? 1 + 1 + chunks.n_chunks : 0) + launches + scan_k;
     *stats = s;
   }
   return SWIFT_OK;
@@ -2189,11 +2205,13 @@ int swift_align_into(swift_ctx* ctx, const swift_index* idx, const char* reads, 
   return rc;
 }
 
-int swift_align_paired(swift_ctx* ctx, const swift_index* idx, const char* reads1, size_t len1,
-                       const char* reads2, size_t len2, const swift_params* p,
-                       uint32_t min_frag, uint32_t max_frag, char** out, size_t* out_len,
-                       swift_stats* stats) {
-  if (!ctx || !idx || !reads1 || !reads2 || !p || !out || !out_len)
+// The text goes to a malloc'd buffer (*out) or, with host_out, into
+// host_out (host_cap bytes) in record ranges overlapped with its writing.
+static int align_paired_impl(swift_ctx* ctx, const swift_index* idx, const char* reads1,
+                             size_t len1, const char* reads2, size_t len2, const swift_params* p,
+                             uint32_t min_frag, uint32_t max_frag, char** out, char* host_out,
+                             size_t host_cap, size_t* out_len, swift_stats* stats) {
+  if (!ctx || !idx || !reads1 || !reads2 || !p || !(out || host_out) || !out_len)
     return fail(ctx, SWIFT_E_ARG, "null argument");
   if (p->seed_len != idx->k) return fail(ctx, SWIFT_E_ARG, "seed length differs from the index's");
   CK(cudaSetDevice(ctx->device));
@@ -2224,21 +2242,18 @@ int swift_align_paired(swift_ctx* ctx, const swift_index* idx, const char* reads
     return fail(ctx, SWIFT_E_INPUT, "a read is shorter than the query length; the reference "
                                     "aligns such reads against stale buffer contents");
   // mate names end in 1 or 2 (getMatePairName; otherwise the reference
-  // pairs against the name it found before)
-  {
-    std::vector<DevRead> h1(n), h2(n);
-    if (n) {
-      CK(cudaMemcpy(h1.data(), rd1->d_rd, n * sizeof(DevRead), cudaMemcpyDeviceToHost));
-      CK(cudaMemcpy(h2.data(), rd2->d_rd, n * sizeof(DevRead), cudaMemcpyDeviceToHost));
-    }
-    for (int64_t i = 0; i < n; ++i)
-      for (int f = 0; f < 2; ++f) {
-        const DevRead& r = f == 0 ? h1[i] : h2[i];
-        const char* b = f == 0 ? reads1 : reads2;
-        const char last = r.name_len > 0 ? b[r.name_off + r.name_len] : 0;
-        if (last != '1' && last != '2')
-          return fail(ctx, SWIFT_E_INPUT, "paired-end read names must end in 1 or 2");
-      }
+  // pairs against the name it found before), checked on the device
+  if (n) {
+    Scratch scn(st);
+    int32_t* d_bad;
+    CK(scn.get(&d_bad, 1));
+    CK(cudaMemsetAsync(d_bad, 0, sizeof(int32_t), st));
+    launch_pe_names(st, rd1->d_bytes, rd1->d_rd, rd2->d_bytes, rd2->d_rd, n, d_bad);
+    CKLAUNCH();
+    int32_t bad = 0;
+    CK(cudaMemcpyAsync(&bad, d_bad, sizeof(bad), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (bad) return fail(ctx, SWIFT_E_INPUT, "paired-end read names must end in 1 or 2");
   }
   rc = ensure_lt2(ctx, idx);
   if (rc != SWIFT_OK) return rc;
@@ -2567,29 +2582,32 @@ int swift_align_paired(swift_ctx* ctx, const swift_index* idx, const char* reads
   launches += (covered > 0 ? 1 : 0) + exclusive_scan_u64(st, bytes, offs, (int64_t)covered, tmp2, tot2);
   uint64_t total = 0;
   CK(cudaMemcpyAsync(&total, tot2, 8, cudaMemcpyDeviceToHost, st));
+  TextChunks chunks;
+  rc = chunks.plan(ctx, st, offs, (int64_t)covered, host_out != nullptr);
+  if (rc != SWIFT_OK) return rc;
   CK(cudaStreamSynchronize(st));
   char* d_text;
   CK(sc.get(&d_text, (size_t)total + 16));
-  fa.text = d_text;
-  if (sam)
-    launch_sam_write(st, fa);
-  else
-    launch_format_write(st, fa);
-  CKLAUNCH();
-  launches += covered > 0 ? 1 : 0;
-  CK(cudaEventRecord(ctx->ev[5], st));
-  char* h = (char*)malloc(total + 1);
-  if (!h) return fail(ctx, SWIFT_E_NOMEM, "host output buffer");
-  if (total) {
-    const cudaError_t e = cudaMemcpyAsync(h, d_text, total, cudaMemcpyDeviceToHost, st);
-    if (e != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess) {
-      free(h);
-      return fail(ctx, SWIFT_E_CUDA, "output copy");
-    }
-  }
-  h[total] = '\0';
-  *out = h;
+  rc = chunks.write(ctx, st, fa, sam, d_text, total, host_out, host_cap, ctx->ev[5]);
+  if (rc != SWIFT_OK) return rc;
+  launches += covered > 0 ? chunks.n_chunks : 0;
   *out_len = total;
+  if (host_out) {
+    CK(cudaStreamSynchronize(st));
+    if (total > host_cap) return fail(ctx, SWIFT_E_LIMIT, "output buffer too small");
+  } else {
+    char* h = (char*)malloc(total + 1);
+    if (!h) return fail(ctx, SWIFT_E_NOMEM, "host output buffer");
+    if (total) {
+      const cudaError_t e = cudaMemcpyAsync(h, d_text, total, cudaMemcpyDeviceToHost, st);
+      if (e != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess) {
+        free(h);
+        return fail(ctx, SWIFT_E_CUDA, "output copy");
+      }
+    }
+    h[total] = '\0';
+    *out = h;
+  }
   if (stats) {
     float t;
     cudaEventElapsedTime(&t, ctx->ev[0], ctx->ev[1]);
@@ -2614,6 +2632,24 @@ int swift_align_paired(swift_ctx* ctx, const swift_index* idx, const char* reads
     *stats = s;
   }
   return SWIFT_OK;
+}
+
+int swift_align_paired(swift_ctx* ctx, const swift_index* idx, const char* reads1, size_t len1,
+                       const char* reads2, size_t len2, const swift_params* p,
+                       uint32_t min_frag, uint32_t max_frag, char** out, size_t* out_len,
+                       swift_stats* stats) {
+  if (!out) return fail(ctx, SWIFT_E_ARG, "null argument");
+  return align_paired_impl(ctx, idx, reads1, len1, reads2, len2, p, min_frag, max_frag, out,
+                           nullptr, 0, out_len, stats);
+}
+
+int swift_align_paired_into(swift_ctx* ctx, const swift_index* idx, const char* reads1,
+                            size_t len1, const char* reads2, size_t len2, const swift_params* p,
+                            uint32_t min_frag, uint32_t max_frag, char* out, size_t cap,
+                            size_t* out_len, swift_stats* stats) {
+  if (!out) return fail(ctx, SWIFT_E_ARG, "null argument");
+  return align_paired_impl(ctx, idx, reads1, len1, reads2, len2, p, min_frag, max_frag, nullptr,
+                           out, cap, out_len, stats);
 }
 
 static int read_file(const char* path, std::vector<char>* buf, std::string* err) {

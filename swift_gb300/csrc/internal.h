@@ -237,6 +237,9 @@ struct PairArgs {
 };
 void launch_build_pairs(cudaStream_t st, const PairArgs& a);
 
+// paired.cu: *bad = 1 when a read name of either file does not end in 1 or 2
+void launch_pe_names(cudaStream_t st, const char* b1, const DevRead* rd1, const char* b2,
+                     const DevRead* rd2, int64_t n, int32_t* bad);
 // paired.cu: paired-end records and pairs
 struct PairedArgs {
   int64_t n_pairs;            // reads per file

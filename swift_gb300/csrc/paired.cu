@@ -266,7 +266,27 @@ __global__ void pe_sep_kernel(PairSelArgs a) {
   }
   a.sep[j] = sep;
 }
+
+// getMatePairName reads the name's last character: 1 or 2 on both files
+__global__ void pe_names_kernel(const char* __restrict__ b1, const DevRead* __restrict__ rd1,
+                                const char* __restrict__ b2, const DevRead* __restrict__ rd2,
+                                int64_t n, int32_t* bad) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+#pragma unroll
+  for (int f = 0; f < 2; ++f) {
+    const DevRead r = f == 0 ? rd1[i] : rd2[i];
+    const char last = r.name_len > 0 ? (f == 0 ? b1 : b2)[r.name_off + r.name_len] : 0;
+    if (last != '1' && last != '2') *bad = 1;
+  }
+}
 }  // namespace
+
+void launch_pe_names(cudaStream_t st, const char* b1, const DevRead* rd1, const char* b2,
+                     const DevRead* rd2, int64_t n, int32_t* bad) {
+  if (n <= 0) return;
+  pe_names_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(b1, rd1, b2, rd2, n, bad);
+}
 
 void launch_pe_records(cudaStream_t st, const PairedArgs& a, uint64_t* cnt) {
   if (a.n_pairs <= 0) return;

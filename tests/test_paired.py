@@ -164,3 +164,37 @@ def test_paired_input_errors(ctx, sg):
             ctx.align_paired(ix, r1, r2)
         assert e.value.code == -2
     assert ctx.align_paired(ix, one, two).startswith(b"\n***")
+
+
+def test_paired_into_caller_buffer(ctx, sg):
+    # enough records for the text to reach the host in record ranges copied
+    # while the next range is written: the same bytes as swift_align_paired
+    import ctypes
+    import torch
+    from swift_gb300 import synth
+    names, seqs = synth.make_reference(2_000_000, 6, sigma=0.6, repeat_frac=0.1, n_units=40,
+                                       unit_len=300, divergence=0.03, seed=21)
+    ref = synth.fasta_bytes(names, seqs)
+    r1, r2 = synth.paired_reads(seqs, 20_000, 100, (200, 500), 0.01, seed=22)
+    ix = ctx.index(ref)
+    pin = []
+    for r in (r1, r2):
+        t = torch.empty(len(r), dtype=torch.uint8, pin_memory=True)
+        t.numpy()[:] = memoryview(r)
+        pin.append(t)
+    for fmt in (0, 1):
+        p = sg.default_params(out_format=fmt)
+        want, st = ctx.align_paired(ix, r1, r2, p, stats=True)
+        assert st["records"] >= 65536
+        out = torch.zeros(len(want), dtype=torch.uint8, pin_memory=True)  # exact size
+        n, _ = ctx.align_paired_into(ix, pin[0].data_ptr(), len(r1), pin[1].data_ptr(), len(r2),
+                                     out.data_ptr(), len(want), p)
+        assert n == len(want) and out.numpy().tobytes() == want, fmt
+        pageable = ctypes.create_string_buffer(len(want) + 1)
+        n, _ = ctx.align_paired_into(ix, pin[0].data_ptr(), len(r1), pin[1].data_ptr(), len(r2),
+                                     ctypes.addressof(pageable), len(pageable), p, 150, 500)
+        assert pageable.raw[:n] == ctx.align_paired(ix, r1, r2, p, 150, 500)
+        with pytest.raises(sg.SwiftError) as e:
+            ctx.align_paired_into(ix, pin[0].data_ptr(), len(r1), pin[1].data_ptr(), len(r2),
+                                  out.data_ptr(), len(want) - 1, p)
+        assert e.value.code == -5
