@@ -39,30 +39,16 @@ METRIC_LT13 = ("reads/s (lt13 seed-and-extend seeding + Smith-Waterman + best pe
 
 def metric_for(args):
     return METRIC_LT13 if args.seeder == "lt13" else METRIC
-# DRAM bytes per pair of the bound pass, read + written, from one ncu capture
-# (413 MB for 825,653 pairs of the scale workload with 200 K reads), and the
-# algorithmic bytes: 112 B query + 304 B window read, 64 B suffix maxima +
-# 4 B bound written.
-BOUND_DRAM_BYTES_PER_PAIR = 413.0e6 / 825653
-BOUND_ALGO_BYTES_PER_PAIR = 112 + 304 + 64 + 4
-# The same for the trace pass, the first kernel when every pair is traced
-# (SAM output): 112 B query + 304 B window read, 8 B first maximum and the
-# direction words written (8 lanes x 2 words x 312 steps x 4 B per two pairs
-# at 100 bp); DRAM bytes from one ncu capture (2.06 GB for 99,996 pairs).
+# The trace pass over whole windows, per pair: algorithmic bytes 112 B query
+# + 304 B window read, 8 B first maximum and the direction words written
+# (8 lanes x 2 words x 312 steps x 4 B per two pairs at 100 bp); DRAM bytes,
+# read + written, from one ncu capture of the candidates' launch.
 TRACE_DRAM_BYTES_PER_PAIR = 2.06e9 / 99996
 TRACE_ALGO_BYTES_PER_PAIR = 112 + 304 + 8 + 8 * 2 * 312 * 4 // 2
-FIRST_PASS = {
-    0: ("sw_bound_kernel (score bound of every pair)", BOUND_DRAM_BYTES_PER_PAIR,
-        BOUND_ALGO_BYTES_PER_PAIR,
-        "the formulation issues 3.25 ALU instructions per 2 cells, so 0.31 is its ceiling"),
-    1: ("sw_packed_kernel score pass (exact score of every pair)", None, 112 + 304 + 4,
-        "the exact formulation issues about 6.5 ALU instructions per 2 cells, so about "
-        "0.15 is its ceiling"),
-    2: ("sw_packed_kernel trace pass (every pair traced for SAM output)",
-        TRACE_DRAM_BYTES_PER_PAIR, TRACE_ALGO_BYTES_PER_PAIR,
-        "the trace formulation issues about 10 ALU instructions per 2 cells (first "
-        "maximum of every row, direction bits), so about 0.1 is its ceiling"),
-}
+TRACE_NOTE = ("the trace formulation issues about 10 ALU instructions per 2 cells (first "
+              "maximum of every row, direction bits), so about 0.1 is its ceiling")
+SCORE_NOTE = ("the exact formulation issues about 6.5 ALU instructions per 2 cells, so about "
+              "0.15 is its ceiling")
 
 
 def parse_args():
@@ -580,12 +566,26 @@ def main():
     except Exception as ex:  # the baseline must not break the GPU line
         cpu = {"value": None, "unit": "reads/s", "cores": os.cpu_count(), "kind": "port",
                "sample": f"failed: {ex}"}
-    # the dominant kernel alone, CUDA events on the library's stream
+    # the dominant kernel alone, CUDA events on the library's stream: the
+    # trace pass over whole windows (the candidates, or every pair for SAM)
+    last = stats[-1]
+    tr_ms = statistics.median(s["trace_ms"] for s in stats)
     fp_ms = statistics.median(s["first_pass_ms"] for s in stats)
-    achieved = stats[-1]["first_pass_cells"] / (fp_ms * 1e-3) / 1e9 if fp_ms > 0 else None
     peak = peak_cells / 1e9
-    fast_pairs = stats[-1]["records"] - stats[-1]["sw_generic_pairs"]
-    fp_name, fp_dram, fp_algo, fp_note = FIRST_PASS[int(stats[-1]["first_pass_kind"])]
+    fast_pairs = last["records"] - last["sw_generic_pairs"]
+    cells_per_pair = last["cells"] // max(last["records"], 1)  # Q x window
+    traced = last["trace_cells"] // cells_per_pair if cells_per_pair else 0
+    if tr_ms > 0:
+        rf_kernel = ("sw_packed_kernel trace pass (%s)"
+                     % ("every packed pair, SAM output" if args.format == "sam"
+                        else "each read's candidate pair, whole windows"))
+        rf_ms, rf_cells = tr_ms, last["trace_cells"]
+        rf_dram, rf_algo, rf_note = TRACE_DRAM_BYTES_PER_PAIR, TRACE_ALGO_BYTES_PER_PAIR, TRACE_NOTE
+        rf_units = traced
+    else:
+        rf_kernel, rf_ms, rf_cells = "sw_packed_kernel score pass", fp_ms, last["first_pass_cells"]
+        rf_dram, rf_algo, rf_note, rf_units = None, 112 + 304 + 4, SCORE_NOTE, fast_pairs
+    achieved = rf_cells / (rf_ms * 1e-3) / 1e9 if rf_ms > 0 else None
     line = {
         "metric": metric_for(args), "value": value, "unit": "reads/s", "n_gpus": world,
         "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms_step,
@@ -607,16 +607,20 @@ def main():
                      for k in ("seed_ms", "pairs_ms", "sw_ms", "select_ms", "traceback_ms",
                                "format_ms", "total_ms")},
         "seed_overflow_strands": stats[-1]["seed_overflow_strands"],
-        "roofline": {"bound": "dpx", "kernel": fp_name,
+        "roofline": {"bound": "dpx", "kernel": rf_kernel,
                      "achieved": achieved, "peak": peak,
                      "unit": "Gcells/s", "frac": achieved / peak if peak and achieved else None,
-                     "kernel_ms": fp_ms,
-                     "traffic": fp_dram * fast_pairs if fp_dram else None,
-                     "traffic_unit": "bytes per launch" if stats[-1]["first_pass_kind"] != 2
-                     else "bytes per pass (262,144-pair launches)",
-                     "algorithmic_bytes": fp_algo * fast_pairs,
+                     "kernel_ms": rf_ms,
+                     "traffic": rf_dram * rf_units if rf_dram else None,
+                     "traffic_unit": "bytes per pass (launches of up to 262,144 pairs)",
+                     "algorithmic_bytes": rf_algo * rf_units,
                      "peak_source": "measured on this GPU: 2 cells per __vimax3_s16x2_relu "
-                                    "lane instruction (%s)" % fp_note},
+                                    "lane instruction (%s)" % rf_note},
+        "lcs_bound": None if last["first_pass_kind"] != 3 else {
+            "kernel": "sw_lcs_kernel (bit-parallel LCS bound of every packed pair)",
+            "kernel_ms": fp_ms, "pairs": fast_pairs,
+            "Gcells_per_s": last["first_pass_cells"] / (fp_ms * 1e-3) / 1e9 if fp_ms > 0 else None,
+            "pairs_left_for_the_relaxed_bound": last["lcs_kept"]},
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": int(sum(s["launches"] for s in stats)),

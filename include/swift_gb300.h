@@ -88,11 +88,16 @@ typedef struct {
                             needed no exact score                            */
   int64_t retraced_pairs;/* printed pairs traced after selection (bounded
                             selection: the read's candidate was not best)    */
-  double first_pass_ms;  /* the packed path's first kernel alone: the score
-                            bound (default), the exact score pass, or (SAM
-                            output, every pair traced) the trace pass        */
+  double first_pass_ms;  /* the packed path's first kernel alone: the LCS
+                            bound (default) or the exact score pass; 0 with
+                            SAM output (every pair traced)                   */
   int64_t first_pass_cells; /* DP cells that kernel covered               */
-  int64_t first_pass_kind;  /* 0 score bound, 1 exact score, 2 trace pass  */
+  int64_t first_pass_kind;  /* 1 exact score, 3 LCS bound                 */
+  double trace_ms;       /* trace-pass launches over whole windows: the
+                            candidates (default) or every packed pair (SAM) */
+  int64_t trace_cells;   /* DP cells of those launches                     */
+  int64_t lcs_kept;      /* pairs the LCS bound could not rule out (they get
+                            the relaxed bound pass)                          */
 } swift_stats;
 
 void swift_params_default(swift_params *p);

@@ -79,6 +79,7 @@ class Stats(C.Structure):
         ("d2h_ms", C.c_double), ("traced_pairs", C.c_int64), ("bound_pruned", C.c_int64),
         ("retraced_pairs", C.c_int64), ("first_pass_ms", C.c_double),
         ("first_pass_cells", C.c_int64), ("first_pass_kind", C.c_int64),
+        ("trace_ms", C.c_double), ("trace_cells", C.c_int64), ("lcs_kept", C.c_int64),
     ]
 
     def as_dict(self):

@@ -1838,12 +1838,14 @@ static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swi
   const bool sam = p->out_format == 1;
   const bool bounded = fast_ok && ctx->sw_path == 0 && !sam;
   // counters: 0 packed-path pairs, 1 generic pairs, 2 trace list,
-  // 3 exact-score list, 4 second trace list, 5 printed records
+  // 3 pairs the LCS bound keeps, 4 second trace list, 5 printed records,
+  // 6 pairs the relaxed bound keeps (exact-score list)
   // counters 8.. : histogram and fill of the early-stop sort (two uses)
-  int32_t *fast_list, *gen_list, *tb_list, *cnt;
+  int32_t *fast_list, *gen_list, *tb_list, *k2_list, *cnt;
   CK(sc.get(&fast_list, nn));
   CK(sc.get(&gen_list, nn));
   CK(sc.get(&tb_list, nn));
+  CK(sc.get(&k2_list, bounded ? nn : 1));
   CK(sc.get(&cnt, 8 + 4 * (kSufBlocks + 1)));
   CK(cudaMemsetAsync(cnt, 0, (8 + 4 * (kSufBlocks + 1)) * sizeof(int32_t), st));
   int launches = 0;
@@ -1900,7 +1902,11 @@ static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swi
   if (fast_ok && nproc > 0 && !sam) {
     fa2.list = fast_list;
     fa2.count = cnt;
-    launches += bounded ? launch_sw_bound(st, fa2, nproc) : launch_sw_score(st, fa2, nproc);
+    // bounded: the LCS bound of every packed pair (the relaxed bound pass
+    // runs later on the pairs it cannot rule out); else exact scores
+    const int k = bounded ? launch_sw_lcs(st, fa2, nproc) : launch_sw_score(st, fa2, nproc);
+    if (k == 0) return fail(ctx, SWIFT_E_DEVICE, "first Smith-Waterman pass could not launch");
+    launches += k;
     CKLAUNCH();
   }
   CK(cudaEventRecord(ctx->ev[8], st));
@@ -2003,31 +2009,50 @@ static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swi
       if (rc != SWIFT_OK) return rc;
     }
   }
+  int64_t lcs_kept = 0, cand_n = 0;
   if (bounded && nproc > 0) {
-    // candidates: traced first, then pairs their scores cannot rule out get
-    // exact scores
+    // candidates (largest LCS bound of their group) traced first, with no
+    // early stop: no relaxed bound has run for them
     launch_candidates(st, fa, tb_list, cnt + 2);
     CKLAUNCH();
     ++launches;
     CK(cudaMemcpyAsync(h_cnt, cnt, sizeof(h_cnt), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     CK(cudaEventRecord(ctx->ev[6], st));
-    rc = sort_by_stop(tb_list, cnt + 2, h_cnt[2], sorted);
+    cand_n = h_cnt[2];
+    fa2.suf = nullptr;
+    rc = trace_list(tb_list, cnt + 2, cand_n, true);
     if (rc != SWIFT_OK) return rc;
-    rc = trace_list(sorted, cnt + 2, h_cnt[2], false);
-    if (rc != SWIFT_OK) return rc;
-    int32_t* ex_list = fast_list;  // free once the bound pass has run
-    launch_prune(st, fa, aln, ex_list, cnt + 3);
+    fa2.suf = suf;
+    // pairs whose LCS bound cannot rule them out against their candidate's
+    // score get the relaxed bound, then the same test again
+    int32_t* k1_list = fast_list;  // free once the LCS pass has run
+    launch_prune(st, fa, aln, k1_list, cnt + 3);
     CKLAUNCH();
     ++launches;
+    CK(cudaMemcpyAsync(h_cnt, cnt, sizeof(h_cnt), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    lcs_kept = h_cnt[3];
+    if (lcs_kept > 0) {
+      fa2.list = k1_list;
+      fa2.count = cnt + 3;
+      fa2.list_offset = 0;
+      const int kb = launch_sw_bound(st, fa2, lcs_kept);
+      if (kb == 0) return fail(ctx, SWIFT_E_DEVICE, "bound pass could not launch");
+      launches += kb;
+      CKLAUNCH();
+      launch_prune_list(st, fa, aln, k1_list, cnt + 3, lcs_kept, k2_list, cnt + 6);
+      CKLAUNCH();
+      ++launches;
+    }
     // the kept count sizes the exact pass's grid
     CK(cudaMemcpyAsync(h_cnt, cnt, sizeof(h_cnt), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    const int64_t ex_max = h_cnt[3];
-    rc = sort_by_stop(ex_list, cnt + 3, ex_max, sorted);
+    const int64_t ex_max = h_cnt[6];
+    rc = sort_by_stop(k2_list, cnt + 6, ex_max, sorted);
     if (rc != SWIFT_OK) return rc;
     fa2.list = sorted;
-    fa2.count = cnt + 3;
+    fa2.count = cnt + 6;
     fa2.list_offset = 0;
     launches += launch_sw_score(st, fa2, ex_max);
     CKLAUNCH();
@@ -2049,7 +2074,7 @@ static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swi
     CK(cudaStreamSynchronize(st));
     rc = trace_list(list2, cnt + 4, h_cnt[4], false);
     if (rc != SWIFT_OK) return rc;
-    if (bounded) pruned = std::max<int64_t>(h_cnt[0] - h_cnt[2] - h_cnt[3], 0);
+    if (bounded) pruned = std::max<int64_t>(h_cnt[0] - h_cnt[2] - h_cnt[6], 0);
   }
   CK(cudaEventRecord(ctx->ev[4], st));
   if (sam)
@@ -2086,21 +2111,22 @@ static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swi
     s.pairs_ms = t;
     cudaEventElapsedTime(&t, ctx->ev[2], ctx->ev[3]);
     s.sw_ms = t;
-    if (sam) {
-      // no score pass: the trace pass over every packed-path pair
-      double sum = 0;
-      for (int c = 0; c < timed_chunks; ++c) {
-        cudaEventElapsedTime(&t, ctx->chunk_ev[2 * c], ctx->chunk_ev[2 * c + 1]);
-        sum += t;
-      }
-      s.first_pass_ms = sum;
-      s.first_pass_kind = 2;
-    } else {
+    // the trace pass over every cell of its pairs: all packed pairs (SAM) or
+    // the candidates (bounded selection; no early stop for them)
+    double trace_sum = 0;
+    for (int c = 0; c < timed_chunks; ++c) {
+      cudaEventElapsedTime(&t, ctx->chunk_ev[2 * c], ctx->chunk_ev[2 * c + 1]);
+      trace_sum += t;
+    }
+    s.trace_ms = trace_sum;
+    s.trace_cells = (sam ? (int64_t)h_cnt[0] : cand_n) * Q * kWin;
+    if (!sam) {
       cudaEventElapsedTime(&t, ctx->ev[7], ctx->ev[8]);
       s.first_pass_ms = t;
-      s.first_pass_kind = bounded ? 0 : 1;
+      s.first_pass_kind = bounded ? 3 : 1;
+      s.first_pass_cells = fast_ok ? (int64_t)h_cnt[0] * Q * kWin : 0;
     }
-    s.first_pass_cells = fast_ok ? (int64_t)h_cnt[0] * Q * kWin : 0;
+    s.lcs_kept = lcs_kept;
     cudaEventElapsedTime(&t, ctx->ev[3], ctx->ev[6]);
     s.select_ms = t;
     cudaEventElapsedTime(&t, ctx->ev[6], ctx->ev[4]);

@@ -421,6 +421,8 @@ int launch_sw_score(cudaStream_t st, const FastArgs& a, int64_t max_pairs);
 int launch_sw_trace(cudaStream_t st, const FastArgs& a, int64_t max_pairs,
                     cudaEvent_t before = nullptr, cudaEvent_t after = nullptr);
 int launch_sw_bound(cudaStream_t st, const FastArgs& a, int64_t max_pairs);
+// sw_lcs.cu: a.ub[p] = match * LCS(query, window) for the listed pairs
+int launch_sw_lcs(cudaStream_t st, const FastArgs& a, int64_t max_pairs);
 int measure_dpx_peak(cudaStream_t st, int device, double* lane_instr_per_s);
 
 // out.cu
@@ -449,6 +451,8 @@ struct FormatArgs {
 void launch_select(cudaStream_t st, const FormatArgs& a);
 void launch_candidates(cudaStream_t st, const FormatArgs& a, int32_t* list, int32_t* cnt);
 void launch_prune(cudaStream_t st, const FormatArgs& a, DevAln* aln, int32_t* list, int32_t* cnt);
+void launch_prune_list(cudaStream_t st, const FormatArgs& a, DevAln* aln, const int32_t* in,
+                       const int32_t* in_cnt, int64_t max_n, int32_t* list, int32_t* cnt);
 void launch_format_sizes(cudaStream_t st, const FormatArgs& a);
 void launch_format_write(cudaStream_t st, const FormatArgs& a);
 // SAM output: every record, sizes then text (keep is not read)
