@@ -46,17 +46,17 @@ __device__ __forceinline__ void load_codes(const char* __restrict__ s, int L, in
   }
 }
 
-__device__ __forceinline__ uint32_t hash_at(const uint8_t* codes, int i, int k) {
-  uint32_t h = 0;
-  for (int t = k - 1; t >= 0; --t) h = (h << 2) | codes[i + t];
-  return h;
-}
+
+// words of 16 packed 2-bit codes covering kReadMax bases, plus one zero word
+constexpr int kPackedWords = (kReadMax + 15) / 16 + 1;
 
 template <int CAP>
 __global__ void __launch_bounds__(kSeedWarps * 32) seed_warp_kernel(SeedArgs a) {
   __shared__ uint64_t keys_all[kSeedWarps][CAP];
   __shared__ uint16_t runlen_all[kSeedWarps][CAP];
-  __shared__ uint8_t codes_all[kSeedWarps][kReadMax + 1];
+  // whole 16-code groups, so the packing below reads inside the array
+  __shared__ __align__(4) uint8_t codes_all[kSeedWarps][16 * kPackedWords];
+  __shared__ uint32_t packed_all[kSeedWarps][kPackedWords];
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t sid = (int64_t)blockIdx.x * kSeedWarps + wib;
   if (sid >= 2 * a.n_reads) return;
@@ -74,6 +74,27 @@ __global__ void __launch_bounds__(kSeedWarps * 32) seed_warp_kernel(SeedArgs a) 
   }
   load_codes(a.reads + rd.seq_off, L, strand, codes, lane);
   __syncwarp();
+  // the codes 2-bit packed, code i at bits 2 (i % 16) of word i / 16, as
+  // the index packs the reference: the hash of [i, i + k) is one funnel
+  // shift (k <= 15)
+  uint32_t* packed = packed_all[wib];
+  if (lane < kPackedWords) {
+    uint32_t pw = 0;
+    if (16 * lane < L) {
+      const uint32_t* c4 = reinterpret_cast<const uint32_t*>(codes + 16 * lane);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        // codes past L are stale bytes: masked below
+        const uint32_t x = c4[q];
+        pw |= ((x & 3u) | ((x >> 6) & 0xCu) | ((x >> 12) & 0x30u) | ((x >> 18) & 0xC0u)) << (8 * q);
+      }
+      const int valid = L - 16 * lane;
+      if (valid < 16) pw &= (1u << (2 * valid)) - 1u;
+    }
+    packed[lane] = pw;
+  }
+  __syncwarp();
+  const uint32_t kmask = (1u << (2 * k)) - 1u;
   // offsets i = lane + 32 m, m < 7 (199 bases at most)
   constexpr int kM = (kReadMax + 31) / 32;
   uint32_t beg[kM], cnt[kM];
@@ -83,7 +104,7 @@ __global__ void __launch_bounds__(kSeedWarps * 32) seed_warp_kernel(SeedArgs a) 
     int i = lane + 32 * m;
     beg[m] = cnt[m] = 0;
     if (i < nq) {
-      const uint32_t h = hash_at(codes, i, k);
+      const uint32_t h = __funnelshift_r(packed[i >> 4], packed[(i >> 4) + 1], 2 * (i & 15)) & kmask;
       // compact bucket directory: occupancy bits and rank, then the start
       // of occupied buckets only
       const uint4 grp = __ldg(&a.groups[h >> 6]);
@@ -131,9 +152,9 @@ __global__ void __launch_bounds__(kSeedWarps * 32) seed_warp_kernel(SeedArgs a) 
   __syncwarp();
   // bitonic sort of keys[0, P)
   for (uint32_t size = 2; size <= P; size <<= 1) {
-    for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+    for (uint32_t stride = size >> 1, ls = __ffs(stride) - 1; stride > 0; stride >>= 1, --ls) {
       for (uint32_t t = lane; t < P / 2; t += 32) {
-        uint32_t i = 2 * stride * (t / stride) + (t % stride);
+        uint32_t i = ((t >> ls) << (ls + 1)) | (t & (stride - 1));
         uint32_t j = i + stride;
         bool asc = (i & size) == 0;
         uint64_t x = keys[i], y = keys[j];
