@@ -42,8 +42,10 @@ def metric_for(args):
 # The trace pass over whole windows, per pair: algorithmic bytes 112 B query
 # + 304 B window read, 8 B first maximum and the direction words written
 # (8 lanes x 2 words x 312 steps x 4 B per two pairs at 100 bp); DRAM bytes,
-# read + written, from one ncu capture of the candidates' launch.
-TRACE_DRAM_BYTES_PER_PAIR = 2.06e9 / 99996
+# read + written, from one ncu capture of the candidates' launch (200,000
+# pairs of the scale workload with 200 K reads: 134.6 MB read, 1922.8 MB
+# written).
+TRACE_DRAM_BYTES_PER_PAIR = (134.6e6 + 1922.8e6) / 200000
 TRACE_ALGO_BYTES_PER_PAIR = 112 + 304 + 8 + 8 * 2 * 312 * 4 // 2
 TRACE_NOTE = ("the trace formulation issues about 10 ALU instructions per 2 cells (first "
               "maximum of every row, direction bits), so about 0.1 is its ceiling")

@@ -52,6 +52,8 @@ constexpr int kPackedWords = (kReadMax + 15) / 16 + 1;
 
 template <int CAP>
 __global__ void __launch_bounds__(kSeedWarps * 32) seed_warp_kernel(SeedArgs a) {
+  // the sort pads n <= CAP keys to the next power of two, which must fit
+  static_assert(CAP >= 32 && (CAP & (CAP - 1)) == 0, "CAP must be a power of two");
   __shared__ uint64_t keys_all[kSeedWarps][CAP];
   __shared__ uint16_t runlen_all[kSeedWarps][CAP];
   // whole 16-code groups, so the packing below reads inside the array
