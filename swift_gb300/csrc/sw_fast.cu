@@ -197,11 +197,13 @@ __device__ __forceinline__ void packed_item(const FastArgs& a, const int64_t war
           // the window win a tie, and the window's last best keeps tag 15
           const uint32_t key = VAR ? (h16 + tag) & cm : h16 + tag;
           bestv[k] = __vimax_s16x2_relu(bestv[k], key);  // both non-negative
-          // bits 1 (UP) and 2 (DIAG) of each half's code to 2 * (k & 7)
+          // bits 1 (UP) and 2 (DIAG) of each half's code to 2 * (k & 7): a
+          // mask, then a multiply-add (the rows' fields do not overlap), which
+          // issues on the FMA pipe
           if ((k & 7) == 0) {
             acc[k >> 3] |= (hx >> 1) & 0x00030003u;
           } else {
-            acc[k >> 3] |= (hx << (2 * (k & 7) - 1)) & (0x00030003u << (2 * (k & 7)));
+            acc[k >> 3] += (hx & 0x00060006u) * (1u << (2 * (k & 7) - 1));
           }
         } else if (k & 1) {
           bestv[0] = __vimax3_s16x2_relu(bestv[0], hpair, h16);
