@@ -51,11 +51,10 @@ __device__ __forceinline__ void load_codes(const char* __restrict__ s, int L, in
 constexpr int kPackedWords = (kReadMax + 15) / 16 + 1;
 
 template <int CAP>
-__global__ void __launch_bounds__(kSeedWarps * 32) seed_warp_kernel(SeedArgs a) {
+__global__ void __launch_bounds__(kSeedWarps * 32, 6) seed_warp_kernel(SeedArgs a) {
   // the sort pads n <= CAP keys to the next power of two, which must fit
   static_assert(CAP >= 32 && (CAP & (CAP - 1)) == 0, "CAP must be a power of two");
   __shared__ uint64_t keys_all[kSeedWarps][CAP];
-  __shared__ uint16_t runlen_all[kSeedWarps][CAP];
   // whole 16-code groups, so the packing below reads inside the array
   __shared__ __align__(4) uint8_t codes_all[kSeedWarps][16 * kPackedWords];
   __shared__ uint32_t packed_all[kSeedWarps][kPackedWords];
@@ -65,7 +64,6 @@ __global__ void __launch_bounds__(kSeedWarps * 32) seed_warp_kernel(SeedArgs a) 
   const int64_t read = sid >> 1;
   const int strand = (int)(sid & 1);
   uint64_t* keys = keys_all[wib];
-  uint16_t* runlen = runlen_all[wib];
   uint8_t* codes = codes_all[wib];
   const DevRead rd = a.rd[read];
   const int L = rd.len, k = a.k;
@@ -168,50 +166,61 @@ __global__ void __launch_bounds__(kSeedWarps * 32) seed_warp_kernel(SeedArgs a) 
       __syncwarp();
     }
   }
-  // run lengths at run starts, scanning chunks back to front
+  // run lengths at run starts, scanning chunks back to front: the biggest
   const uint32_t nch = (n + 31) >> 5;
+  auto starts = [&](uint32_t c) {
+    const uint32_t idx = c * 32 + lane;
+    const bool start = idx < n && (idx == 0 || (keys[idx] >> 8) != (keys[idx - 1] >> 8));
+    return __ballot_sync(0xffffffffu, start);
+  };
+  // the run start ending a run that starts at lane `lane` of a chunk whose
+  // starts are bal, if it lies in the same chunk (else 0)
+  auto next_in_chunk = [&](uint32_t c, uint32_t bal) -> uint32_t {
+    const uint32_t above = lane < 31 ? (bal >> (lane + 1)) << (lane + 1) : 0u;
+    return above ? c * 32 + __ffs(above) - 1 : 0u;
+  };
   uint32_t next = n, biggest = 0;
   for (int c = (int)nch - 1; c >= 0; --c) {
-    uint32_t idx = (uint32_t)c * 32 + lane;
-    bool start = false;
-    if (idx < n) start = idx == 0 || (keys[idx] >> 8) != (keys[idx - 1] >> 8);
-    uint32_t bal = __ballot_sync(0xffffffffu, start);
-    uint32_t above = lane < 31 ? (bal >> (lane + 1)) << (lane + 1) : 0u;
-    uint32_t nx = above ? (uint32_t)c * 32 + __ffs(above) - 1 : next;
-    if (start) {
-      uint32_t len = nx - idx;
-      runlen[idx] = (uint16_t)len;
-      biggest = max(biggest, len);
+    const uint32_t bal = starts(c);
+    if ((bal >> lane) & 1u) {
+      const uint32_t nx = next_in_chunk(c, bal);
+      biggest = max(biggest, (nx ? nx : next) - ((uint32_t)c * 32 + lane));
     }
     if (bal) next = (uint32_t)c * 32 + __ffs(bal) - 1;
   }
-  __syncwarp();
 #pragma unroll
   for (int d = 16; d > 0; d >>= 1) biggest = max(biggest, __shfl_xor_sync(0xffffffffu, biggest, d));
-  // first max_hits runs of the biggest size
+  // first max_hits runs of the biggest size, front to back: a chunk's last
+  // run stays open until the next start (or the end) closes it
   int got = 0;
   int3* out = a.best + sid * a.max_hits;
+  auto emit = [&](uint32_t idx) {  // lane 0; got is warp-uniform
+    if (lane == 0) {
+      const uint64_t key = keys[idx];
+      const int32_t ri = (int32_t)(key >> 40);
+      const int32_t shift = (int32_t)((key >> 8) & 0xffffffffu) - kShiftBias;
+      const int32_t i = (int32_t)(key & 0xff);
+      out[got] = make_int3(ri, shift, shift + i);
+    }
+    ++got;
+  };
+  uint32_t open = ~0u;  // start of the run open at the last chunk boundary
   for (uint32_t c = 0; c < nch && got < a.max_hits; ++c) {
-    uint32_t idx = c * 32 + lane;
-    bool hit = false;
-    if (idx < n) {
-      bool start = idx == 0 || (keys[idx] >> 8) != (keys[idx - 1] >> 8);
-      hit = start && runlen[idx] == biggest;
+    const uint32_t bal = starts(c);
+    if (!bal) continue;
+    if (open != ~0u) {
+      if ((uint32_t)(c * 32 + __ffs(bal) - 1) - open == biggest) emit(open);
+      open = ~0u;
     }
-    uint32_t bal = __ballot_sync(0xffffffffu, hit);
-    while (bal && got < a.max_hits) {
-      int b = __ffs(bal) - 1;
-      bal &= bal - 1;
-      if (lane == b) {
-        uint64_t key = keys[idx];
-        int32_t ri = (int32_t)(key >> 40);
-        int32_t shift = (int32_t)((key >> 8) & 0xffffffffu) - kShiftBias;
-        int32_t i = (int32_t)(key & 0xff);
-        out[got] = make_int3(ri, shift, shift + i);
-      }
-      ++got;
+    const uint32_t nx = next_in_chunk(c, bal);
+    uint32_t hb = __ballot_sync(0xffffffffu, ((bal >> lane) & 1u) && nx && nx - (c * 32 + lane) == biggest);
+    while (hb && got < a.max_hits) {
+      emit(c * 32 + __ffs(hb) - 1);
+      hb &= hb - 1;
     }
+    open = c * 32 + 31 - __clz(bal);
   }
+  if (open != ~0u && got < a.max_hits && n - open == biggest) emit(open);
   if (lane == 0) a.nbest[sid] = got;
 }
 
@@ -314,7 +323,7 @@ __global__ void __launch_bounds__(kOvThreads) seed_overflow_kernel(SeedArgs a,
 
 }  // namespace
 
-constexpr int kSeedCap = 512;  // 8 warps x 512 x 10 B = 40 KB of static shared memory
+constexpr int kSeedCap = 512;  // 8 warps x 512 x 8 B = 32 KB of static shared memory
 
 void launch_seed(cudaStream_t st, const SeedArgs& a) {
   int64_t strands = 2 * a.n_reads;
