@@ -2383,6 +2383,8 @@ static int align_paired_impl(swift_ctx* ctx, const swift_index* idx, const char*
   CK(cudaMemsetAsync(wbuf, 0, nr * ws, st));
   pa.Q = Q;
   pa.ref_file = idx->d_file;
+  pa.cat = (const char*)idx->d_cat;
+  pa.odd = idx->d_odd;
   pa.ref_file_len = idx->file_len;
   pa.recs = idx->d_recs;
   pa.reads = d_reads;

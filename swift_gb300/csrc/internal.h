@@ -252,6 +252,8 @@ struct PairedArgs {
   int Q;
   const char* ref_file;
   uint64_t ref_file_len;
+  const char* cat;            // optional: the index's concatenated sequences and
+  const uint32_t* odd;        // their non-ACGTacgt bitmap (direct window copies)
   const DevRecord* recs;
   const char* reads;          // both reads files, the second after the first
   const DevRead* rd;          // file 1's reads, then file 2's

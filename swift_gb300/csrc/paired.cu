@@ -71,7 +71,44 @@ __global__ void __launch_bounds__(kPeWarps * 32) pe_pairs_kernel(PairedArgs a) {
   char* w = a.wbuf + j * a.w_stride;
   bool odd = false;  // a byte outside ACGT or a short window: the generic kernel
   int got = 0;
-  for (uint64_t pos = woff;; pos += 32) {
+  // Common case: the window inside a record of regular lines with only
+  // ACGTacgt bytes (the bitmap): getSeq's bytes are the concatenated bases,
+  // copied 16 per lane; a lowercase base (bit 0x20 of a letter) is odd here.
+  bool direct = false;
+  if (rec.regular && a.odd && a.w_stride % 16 == 0) {
+    const uint64_t avail = rec.cat_len > (uint64_t)dist ? rec.cat_len - (uint64_t)dist : 0;
+    if (avail >= (uint64_t)R) {
+      const uint64_t g0 = rec.cat_start + (uint64_t)dist, g1 = g0 + R - 1;
+      const uint64_t w0 = g0 >> 5, nw = (g1 >> 5) - w0 + 1;  // at most 20 words (R <= 597)
+      uint32_t bits = 0;
+      if ((uint64_t)lane < nw) {
+        bits = a.odd[w0 + lane];
+        if (lane == 0) bits &= ~0u << (g0 & 31);
+        if ((uint64_t)lane == nw - 1) bits &= ~0u >> (31 - (g1 & 31));
+      }
+      direct = !__any_sync(0xffffffffu, bits != 0);
+    }
+  }
+  if (direct) {
+    for (int c = lane; 16 * c < R; c += 32) {
+      // four output words from five aligned loads (reads past the window's
+      // end stay inside the cat buffer's padding); bytes past R are zero
+      const uintptr_t ad = (uintptr_t)(a.cat + rec.cat_start + dist + 16 * c);
+      const uint32_t* wp = reinterpret_cast<const uint32_t*>(ad & ~(uintptr_t)3);
+      const uint32_t sh = (uint32_t)(ad & 3) * 8;
+      uint32_t x[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int keep = R - 16 * c - 4 * q;  // valid bytes of this word
+        const uint32_t v = __funnelshift_r(wp[q], wp[q + 1], sh);
+        x[q] = keep >= 4 ? v : keep <= 0 ? 0u : v & ((1u << (8 * keep)) - 1u);
+      }
+      odd |= ((x[0] | x[1] | x[2] | x[3]) & 0x20202020u) != 0;
+      *reinterpret_cast<uint4*>(w + 16 * c) = make_uint4(x[0], x[1], x[2], x[3]);
+    }
+    got = R;
+  }
+  for (uint64_t pos = woff; !direct; pos += 32) {
     const uint64_t p = pos + (uint64_t)lane;
     const char c = p < a.ref_file_len ? a.ref_file[p] : '\0';
     const bool stop = p >= a.ref_file_len || c == '>';
