@@ -153,20 +153,14 @@ std::vector<int32_t> phase1_stale_repeats(int64_t n_reads, int64_t n_gt) {
   // (and re-maps) the read it last held.  With well-formed input the first
   // n_reads calls return reads in order; the remaining calls of the last
   // batch repeat the slot's previous read.
+  // Call c < n_reads takes read c into slot c % kP1Slots, so a later call c
+  // repeats the last read r < n_reads with r % kP1Slots == c % kP1Slots.
   std::vector<int32_t> rep;
   if (n_gt <= 0) return rep;
-  int64_t nb = (n_gt + kP1Slots - 1) / kP1Slots;
-  int64_t calls = nb * kP1Slots;
-  int32_t slot[kP1Slots];
-  for (int j = 0; j < kP1Slots; ++j) slot[j] = -1;
-  int64_t next = 0;
-  for (int64_t call = 0; call < calls; ++call) {
-    int j = (int)(call % kP1Slots);
-    if (next < n_reads) {
-      slot[j] = (int32_t)next++;
-    } else if (slot[j] >= 0) {
-      rep.push_back(slot[j]);
-    }
+  const int64_t calls = (n_gt + kP1Slots - 1) / kP1Slots * kP1Slots;
+  for (int64_t call = std::max<int64_t>(n_reads, 0); call < calls; ++call) {
+    const int64_t j = call % kP1Slots;
+    if (n_reads - 1 >= j) rep.push_back((int32_t)(j + (n_reads - 1 - j) / kP1Slots * kP1Slots));
   }
   return rep;
 }
