@@ -176,18 +176,25 @@ __global__ void __launch_bounds__(kPairWarps * 32) build_pairs_kernel(PairArgs a
   const int Q = a.Q;
   const int avail = rd.len < Q ? rd.len : Q;
   char* qout = a.qbuf + j * (int64_t)a.Qs;
-  for (int i = lane; i < a.Qs; i += 32) {
-    char c = '\0';
-    if (i < Q) {
-      if (strand == 0) {
-        c = i < avail ? s[i] : '\0';
-      } else {
-        int src = Q - 1 - i;
-        c = comp_char(src < avail ? s[src] : '\0');
+  // four bytes per lane, one 32-bit store each (Qs is a multiple of 16)
+  for (int i0 = 4 * lane; i0 < a.Qs; i0 += 128) {
+    uint32_t word = 0;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const int i = i0 + b;
+      if (i < Q) {
+        char c;
+        if (strand == 0) {
+          c = i < avail ? s[i] : '\0';
+        } else {
+          const int src = Q - 1 - i;
+          c = comp_char(src < avail ? s[src] : '\0');
+        }
+        if (!is_acgt(c)) odd = true;
+        word |= (uint32_t)(uint8_t)c << (8 * b);
       }
     }
-    qout[i] = c;
-    if (i < Q && !is_acgt(c)) odd = true;
+    *reinterpret_cast<uint32_t*>(qout + i0) = word;
   }
   odd = __any_sync(0xffffffffu, odd) || wl != kWin;
   if (lane == 0) {
