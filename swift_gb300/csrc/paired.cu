@@ -130,11 +130,19 @@ __global__ void __launch_bounds__(kPeWarps * 32) pe_pairs_kernel(PairedArgs a) {
   const DevRead rr = a.rd[cr];
   const char* s = a.reads + rr.seq_off;
   char* q = a.qbuf + j * a.q_stride;
-  for (int t = lane; t < a.q_stride; t += 32) {
-    char c = '\0';
-    if (t < Q) c = rev ? revcomp_base(s[Q - 1 - t]) : s[t];
-    q[t] = c;
-    if (t < Q) odd |= !(c == 'A' || c == 'C' || c == 'G' || c == 'T');
+  // four bytes per lane, one 32-bit store each (q_stride is a multiple of 16)
+  for (int t0 = 4 * lane; t0 < a.q_stride; t0 += 128) {
+    uint32_t word = 0;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const int t = t0 + b;
+      if (t < Q) {
+        const char c = rev ? revcomp_base(s[Q - 1 - t]) : s[t];
+        odd |= !(c == 'A' || c == 'C' || c == 'G' || c == 'T');
+        word |= (uint32_t)(uint8_t)c << (8 * b);
+      }
+    }
+    *reinterpret_cast<uint32_t*>(q + t0) = word;
   }
   odd = __any_sync(0xffffffffu, odd);
   if (lane == 0) {
