@@ -2,12 +2,15 @@
 
 One step = one pass of the whole pipeline over one batch of reads already
 resident on the device: SSAHA seeding of both strands, window construction,
-Smith-Waterman with traceback for every candidate, best alignment per read and
-the default text records (left on the device).  The one-time index build is
-excluded and reported separately.
+Smith-Waterman (LCS and relaxed score bounds, traceback of each read's
+candidate, exact scores of the pairs the bounds keep), best alignment per read
+and the default text records (left on the device).  The one-time index build
+is excluded and reported separately; `e2e` repeats the step through
+swift_align_into with the reads and the text in pinned host memory.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload scale|small] [--reads N]
+                  [--workload scale|batched|long|serving|paired] [--reads N]
+                  [--seeder ssaha|lt13] [--format default|sam] [--no-e2e]
 
 Workload "scale" (default): 50 Mbp reference in 24 sequences (log-normal
 lengths, 10 % diverged repeat copies), 1,000,000 reads x 100 bp (1 % subs,
