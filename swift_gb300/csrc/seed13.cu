@@ -38,7 +38,10 @@ constexpr int kPosMask = (1 << kPosBits) - 1;
 constexpr int kKeep = 1000;      // the k > 1000 reset
 constexpr int kRefThreads = 64;  // the reference block's threads: the final scan's stride
 constexpr int kHits = 3;
-constexpr int kQBuf = 256;       // strand bytes + zero padding (reads <= 199 bases)
+// strand bytes + zero padding: tuple offsets run to Q - k + 2 <= 200 (reads <=
+// 199 bases), hashes read 16 more codes, a multiple of 16 for the packed words
+constexpr int kQBuf = 208;
+static_assert(kQBuf % 16 == 0 && kQBuf >= kReadMax + 3, "strand buffer too small");
 constexpr int kWarps = 4;
 
 __device__ __forceinline__ uint32_t code13(uint8_t c) {
@@ -50,7 +53,7 @@ struct Lt13Shared {
   int nrefs;
   int64_t max_comp;
   int64_t tbase[kMaxRefs13];
-  int64_t ntup[kMaxRefs13];
+  int32_t ntup[kMaxRefs13];  // below 2^25 per reference (the index refuses more)
 };
 
 __device__ __forceinline__ int32_t map_at(const Seed13Args& a, const Lt13Shared& s, int64_t v) {
@@ -94,7 +97,7 @@ __global__ void __launch_bounds__(kWarps * 32) seed13_kernel(Seed13Args a) {
   }
   for (int r = threadIdx.x; r < a.nrefs; r += blockDim.x) {
     sh.tbase[r] = a.tbase[r];
-    sh.ntup[r] = a.ntup[r];
+    sh.ntup[r] = (int32_t)a.ntup[r];
   }
   __syncthreads();
   WarpBuf<CAP, GCAP>& b = bufs[wib];
