@@ -82,6 +82,23 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(x: float) -> float:
+    """The largest x over the ranks of the process group (a job takes as long
+    as its slowest replica): a device tensor on NCCL, a host one on gloo."""
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(units_per_rank: int, world: int, steps: int, seconds: float) -> float:
+    """Whole-job units per second: every replica processes its own units
+    (weak scaling), timed by the slowest one."""
+    return units_per_rank * world * steps / seconds
+
+
 class ClockSampler:
     """nvidia-smi samples of SM clock and throttle reasons during a region."""
 
@@ -406,13 +423,11 @@ def bench_paired(args, rank, world, local):
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
     if world > 1:
-        t = torch.tensor([dt], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        dt = float(t.item())
+        dt = max_over_ranks(dt)
         torch.distributed.barrier()
     if rank != 0:
         return 0
-    value = n * world * args.steps / dt
+    value = job_throughput(n, world, args.steps, dt)
     dev_ms = statistics.median(s["total_ms"] for s in stats)
     k = min(args.cpu_sample, n, 2000)
     t0 = time.perf_counter()
@@ -528,11 +543,9 @@ def main():
         torch.distributed.barrier()
     ms = e0.elapsed_time(e1)
     if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = max_over_ranks(ms)
     ms_step = ms / args.steps
-    value = n * world * args.steps / (ms * 1e-3)
+    value = job_throughput(n, world, args.steps, ms * 1e-3)
     sw_ms = statistics.median(s["sw_ms"] for s in stats)
     seed_ms = statistics.median(s["seed_ms"] for s in stats)
     cells = stats[-1]["cells"]
@@ -556,7 +569,9 @@ def main():
             host.append(est)
         torch.cuda.synchronize()
         e2e_s = time.perf_counter() - t0
-        e2e = {"value": n * world * args.steps / e2e_s, "unit": "reads/s",
+        if world > 1:
+            e2e_s = max_over_ranks(e2e_s)
+        e2e = {"value": job_throughput(n, world, args.steps, e2e_s), "unit": "reads/s",
                "h2d_bytes_per_step": len(reads), "d2h_bytes_per_step": out_bytes,
                "ms_per_step": e2e_s * 1e3 / args.steps,
                "host_ms": {k: statistics.median(h[k] for h in host)
