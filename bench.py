@@ -50,6 +50,10 @@ def metric_for(args):
 # written).
 TRACE_DRAM_BYTES_PER_PAIR = (134.6e6 + 1922.8e6) / 200000
 TRACE_ALGO_BYTES_PER_PAIR = 112 + 304 + 8 + 8 * 2 * 312 * 4 // 2
+# ALU-pipe instructions the trace pass issues per 2 cells (per lane), from
+# the same capture: 909.6 M warp instructions on the ALU pipe (86.05 % of its
+# 2 per SM per cycle over 3.477 M cycles on 152 SMs) for 6.0 G cells.
+TRACE_ALU_PER_2_CELLS = 9.70
 TRACE_NOTE = ("the trace formulation issues about 10 ALU instructions per 2 cells (first "
               "maximum of every row, direction bits), so about 0.1 is its ceiling")
 SCORE_NOTE = ("the exact formulation issues about 6.5 ALU instructions per 2 cells, so about "
@@ -635,7 +639,11 @@ def main():
                      "traffic_unit": "bytes per pass (launches of up to 262,144 pairs)",
                      "algorithmic_bytes": rf_algo * rf_units,
                      "peak_source": "measured on this GPU: 2 cells per __vimax3_s16x2_relu "
-                                    "lane instruction (%s)" % rf_note},
+                                    "lane instruction (%s)" % rf_note,
+                     # the same issue-rate peak per ALU-pipe instruction: how busy the
+                     # pipe that bounds the kernel is kept
+                     "alu_pipe_frac": (achieved / peak * TRACE_ALU_PER_2_CELLS
+                                       if tr_ms > 0 and peak and achieved else None)},
         "lcs_bound": None if last["first_pass_kind"] != 3 else {
             "kernel": "sw_lcs_kernel (bit-parallel LCS bound of every packed pair)",
             "kernel_ms": fp_ms, "pairs": fast_pairs,
