@@ -73,6 +73,9 @@ def parse_args():
     ap.add_argument("--reads", type=int, default=None)
     ap.add_argument("--cpu-sample", type=int, default=20000)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the short runs of the batched, long-region and serving "
+                         "configurations that the default line carries")
     ap.add_argument("--seeder", default="ssaha", choices=["ssaha", "lt13"],
                     help="Phase 1: SSAHA seeding (searchQueries3) or lt13 seed-and-extend "
                          "(search2Queries, the reference CLI's GPU default)")
@@ -161,17 +164,18 @@ def make_workload(args, rank):
     if args.workload == "small":
         names, seqs = synth.make_reference(1_000_000, 1, seed=0)
         n = args.reads or 10_000
-        rn, rs, _ = synth.make_reads(seqs, n, 100, 0.01, 0.001, 0.0, seed=1 + rank)
+        rn, rs, orig = synth.make_reads(seqs, n, 100, 0.01, 0.001, 0.0, seed=1 + rank)
         desc = "small: 1 Mbp / 1 seq, %d x 100 bp reads" % n
     else:
         names, seqs = synth.make_reference(50_000_000, 24, sigma=0.8, repeat_frac=0.10,
                                            n_units=500, unit_len=300, divergence=0.03, seed=0)
         n = args.reads or 1_000_000
-        rn, rs, _ = synth.make_reads(seqs, n, 100, 0.01, 0.001, 0.05, seed=1 + rank)
+        rn, rs, orig = synth.make_reads(seqs, n, 100, 0.01, 0.001, 0.05, seed=1 + rank)
         desc = ("scale: 50 Mbp / 24 seqs (log-normal sigma 0.8, 10%% repeats of 500 x 300 bp "
                 "units at 3%% divergence), %d x 100 bp reads (1%% subs, 0.1%% indels, 5%% random)"
                 % n)
-    return synth.fasta_bytes(names, seqs), synth.reads_fasta(rn, rs), n, desc
+    wl = {"seqs": seqs, "reads": rs, "origins": orig}
+    return synth.fasta_bytes(names, seqs), synth.reads_fasta(rn, rs), n, desc, wl
 
 
 def sample_reads(reads: bytes, n: int) -> bytes:
@@ -180,44 +184,105 @@ def sample_reads(reads: bytes, n: int) -> bytes:
 
 
 def cpu_reference(ref: bytes, reads: bytes, n_sample: int, steps: int, warmup: int,
-                  seeder: int = 0):
-    """The reference algorithm on the host cores (oracle port), reads/s."""
+                  seeder: int = 0, device_mem: int = 0):
+    """The reference algorithm on the host cores (oracle port): reads/s,
+    threads, seconds, and the last run's output (for the parity check)."""
     from oracle import oracle as O
     threads = os.cpu_count() or 1
-    sess = O.Session(ref, O.default_params(threads=threads, seeder=seeder))
+    sess = O.Session(ref, O.default_params(threads=threads, seeder=seeder,
+                                           device_mem=device_mem))
     sample = sample_reads(reads, n_sample)
     for _ in range(warmup):
         sess.align(sample)
     t0 = time.perf_counter()
+    out = b""
     for _ in range(steps):
-        sess.align(sample)
+        out = sess.align(sample)
     dt = time.perf_counter() - t0
-    return n_sample * steps / dt, threads, dt
+    return n_sample * steps / dt, threads, dt, out
 
 
-def bench_batched(args, rank, world, local):
-    """Phase 2 alone on read x region pairs of varying lengths (reads
-    36-250 bp, 1-64 regions each): GCUPS of the shape-sorted batched mode and
-    of the plain mode (every pair padded to the largest shape, one launch),
-    both bit-exact.  Inputs resident on the device; coordinates only."""
+def cpu_model() -> str:
+    """The host CPU's model name (/proc/cpuinfo, else lscpu)."""
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    try:
+        outp = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in outp.splitlines():
+            if line.strip().lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    import platform
+    return platform.machine()
+
+
+def workload_pairs(seqs, reads_list, origins, n: int, seed: int = 7):
+    """The scale workload's Smith-Waterman pairs in the alignSequences layout:
+    each read's first n against the 300-base window the reference builds
+    around its origin (refPos - 100; a random position for random reads)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    Q, R = 100, 300
+    q = np.zeros((n, Q + 1), np.uint8)
+    w = np.zeros((n, R + 1), np.uint8)
+    for i in range(n):
+        q[i, :Q] = np.frombuffer(reads_list[i][:Q], np.uint8)
+        sid, pos = origins[i]
+        if sid < 0:
+            sid = int(rng.integers(0, len(seqs)))
+            pos = int(rng.integers(0, max(1, len(seqs[sid]) - R)))
+        a = max(0, pos - 100)
+        win = np.frombuffer(seqs[sid][a:a + R], np.uint8)
+        w[i, :len(win)] = win
+    return q, w, Q, R
+
+
+def cpu_sw_baseline(q, w, Q, R, n):
+    """The port's Smith-Waterman (the reference kernel's semantics) over n
+    pairs on every host core: GCUPS, threads, seconds."""
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    qb, wb = q[:n].tobytes(), w[:n].tobytes()
+    O.sw_batch(qb, Q, wb, R, min(n, 256), threads=threads)  # warm-up
+    t0 = time.perf_counter()
+    O.sw_batch(qb, Q, wb, R, n, threads=threads)
+    dt = time.perf_counter() - t0
+    return n * Q * R / dt / 1e9, threads, dt
+
+
+def hbm_peak():
+    """Measured HBM copy bandwidth (GB/s) of this machine's GPUs, or the
+    recipe's fallback."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, ValueError, KeyError):
+        return 6800.0, "fallback"
+
+
+def pairs_run(ctx, kind: str, n_reads: int, steps: int, warmup: int, seed: int, seqs=None,
+              plain: bool = True):
+    """Phase 2 alone on explicit pairs through swift_sw_pairs, inputs resident
+    on the device, coordinates only.  kind "batched": reads 36-250 bp x 1-64
+    regions (BASELINE config 2); "long": queries 1-4 kbp x one region of
+    2-8 kbp (config 3).  Returns the measured figures: GCUPS of the
+    shape-sorted batched mode and, for "batched", of the plain mode (every
+    pair padded to the largest shape, one launch) on a tenth of the pairs."""
     import ctypes as C
     import numpy as np
     import torch
     import swift_gb300 as sg
-    from swift_gb300 import build as b, synth
-    device = local
-    torch.cuda.set_device(device)
-    b.build()
-    long = args.workload == "long"
-    if long:
-        n_reads = args.reads or 20_000
-        ref, reads, qo, ql, ro, rl = synth.long_workload(n_reads, seed=1 + rank)
+    from swift_gb300 import synth
+    if kind == "long":
+        ref, reads, qo, ql, ro, rl = synth.long_workload(n_reads, seed=seed)
     else:
-        n_reads = args.reads or 1_000_000
-        ref, reads, qo, ql, ro, rl = synth.pairs_workload(n_reads, seed=1 + rank)
-    stream = torch.cuda.Stream(device)
-    torch.cuda.set_stream(stream)
-    ctx = sg.Context(device, stream.cuda_stream)
+        ref, reads, qo, ql, ro, rl = synth.pairs_workload(n_reads, seed=seed, ref=seqs)
     dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
     d = dict(q=dev(np.frombuffer(reads, np.uint8)), r=dev(np.frombuffer(ref, np.uint8)),
              qo=dev(qo), ql=dev(ql), ro=dev(ro), rl=dev(rl))
@@ -235,52 +300,145 @@ def bench_batched(args, rank, world, local):
             raise sg.SwiftError(rc, sg.lib().swift_last_error(ctx._h).decode())
         return st.as_dict()
 
-    for _ in range(max(args.warmup, 3)):
+    for _ in range(max(warmup, 3)):
         run(n, 0)
-    with ClockSampler(device) as clk:
-        sts = [run(n, 0) for _ in range(args.steps)]
+    sts = [run(n, 0) for _ in range(steps)]
     ms = statistics.median(s["ms"] for s in sts)
     cells = sts[-1]["cells"]
-    gcups = cells / (ms * 1e-3) / 1e9
-    plain_gcups = ms_p = n_plain = None
-    if not long:  # plain mode takes pairs up to 256 x 1024 only
-        # plain mode on the first pairs (about a tenth of the cells: one padded launch is slow)
+    res = {"pairs": n, "cells": cells, "ms": ms, "gcups": cells / (ms * 1e-3) / 1e9,
+           "segments": sts[-1]["segments"], "generic_pairs": sts[-1]["generic_pairs"],
+           "launches": int(sum(s["launches"] for s in sts)), "steps": steps,
+           "warmup": max(warmup, 3)}
+    if kind != "long" and plain:  # plain mode takes pairs up to 256 x 1024 only
         n_plain = max(1, n // 10)
         run(n_plain, 1)
-        sp = [run(n_plain, 1) for _ in range(max(1, min(args.steps, 2)))]
+        sp = [run(n_plain, 1) for _ in range(max(1, min(steps, 2)))]
         ms_p = statistics.median(s["ms"] for s in sp)
-        plain_gcups = sp[-1]["cells"] / (ms_p * 1e-3) / 1e9
+        res["plain"] = {"gcups": sp[-1]["cells"] / (ms_p * 1e-3) / 1e9, "pairs": n_plain,
+                        "ms": ms_p,
+                        "note": "every pair padded to the largest shape, one int32 launch"}
+        res["batched_vs_plain"] = res["gcups"] / res["plain"]["gcups"]
+    res["workload"] = (("long: %d queries L ~ U[1000,4000] (3%% subs, 0.5%% indels) x one region "
+                        "U[max(2000, L+200), 8000] on a 100 Mbp uniform reference" % n_reads)
+                       if kind == "long" else
+                       ("batched: %d reads L ~ U[36,250] x U{1..64} regions (true + decoys, "
+                        "64 bp flanks) on the 50 Mbp reference" % n_reads))
+    return res
+
+
+def bench_batched(args, rank, world, local):
+    """Phase 2 alone on read x region pairs of varying lengths (config 2) or
+    long pairs (config 3), both bit-exact; see pairs_run."""
+    import torch
+    import swift_gb300 as sg
+    from swift_gb300 import build as b
+    device = local
+    torch.cuda.set_device(device)
+    b.build()
+    long = args.workload == "long"
+    stream = torch.cuda.Stream(device)
+    torch.cuda.set_stream(stream)
+    ctx = sg.Context(device, stream.cuda_stream)
+    n_reads = args.reads or (20_000 if long else 1_000_000)
+    with ClockSampler(device) as clk:
+        res = pairs_run(ctx, "long" if long else "batched", n_reads, args.steps, args.warmup,
+                        seed=1 + rank)
     if rank == 0:
-        wl_desc = ("long: %d queries L ~ U[1000,4000] (3%% subs, 0.5%% indels) x one region "
-                   "U[max(2000, L+200), 8000] on a 100 Mbp uniform reference" % n_reads) if long else \
-                  ("batched: %d reads L ~ U[36,250] x U{1..64} regions "
-                   "(true + decoys, 64 bp flanks) on the 50 Mbp reference" % n_reads)
         print(json.dumps({
             "metric": ("SW GCUPS on long query x region pairs, bit-exact" if long else
                        "SW GCUPS on read x region pairs of varying length (batched), bit-exact"),
-            "value": gcups, "unit": "GCUPS", "n_gpus": world, "steps": args.steps,
-            "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True,
+            "value": res["gcups"], "unit": "GCUPS", "n_gpus": world, "steps": args.steps,
+            "warmup": res["warmup"], "ms_per_step": res["ms"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32" if long else "int16x2",
             "data": "synthetic",
-            "config": {"workload": wl_desc, "pairs": n, "cells": cells,
-                       "segments": sts[-1]["segments"], "generic_pairs": sts[-1]["generic_pairs"]},
-            "plain": None if long else {"gcups": plain_gcups, "pairs": n_plain, "ms": ms_p,
-                      "note": "every pair padded to the largest shape, one int32 launch"},
-            "batched_vs_plain": gcups / plain_gcups if plain_gcups else None,
-            "gpu_launches": int(sum(s["launches"] for s in sts)),
+            "config": {"workload": res["workload"], "pairs": res["pairs"], "cells": res["cells"],
+                       "segments": res["segments"], "generic_pairs": res["generic_pairs"]},
+            "plain": res.get("plain"),
+            "batched_vs_plain": res.get("batched_vs_plain"),
+            "gpu_launches": res["launches"],
             "clocks": clk.summary(),
         }))
     return 0
 
 
-def bench_serving(args, rank, world, local, workers=4, pool_size=240, per_load=500):
-    """Serving: a 200 Mbp reference (24 sequences) resident; requests of
-    log-uniform size in [1, 10000] reads, read length per request U[50, 199]
-    (the reference's query buffer caps reads at 199 bases); first the
-    saturation throughput (every request of the pool queued at once), then
-    Poisson arrivals at fractions of it, with per-request latency from
-    submission to result (p50 / p99)."""
+SERVE_MAX_READ = 199  # read lengths of the serving workload: U[50, SERVE_MAX_READ]
+
+
+def serving_pool(seqs, pool_size: int, seed: int, max_len: int = SERVE_MAX_READ):
+    """Requests of the serving workload: log-uniform sizes in [1, 10000]
+    reads, each request's reads of one length U[50, max_len] with the
+    config-0 error model (5 % random reads)."""
     import numpy as np
+    from swift_gb300 import synth
+    rng = np.random.default_rng(seed)
+    sizes = np.floor(np.exp(rng.uniform(0, np.log(10001), pool_size))).astype(int).clip(1, 10000)
+    # reads drawn once at the longest length, each request cut to its own
+    _, rs_all, _ = synth.make_reads(seqs, int(sizes.sum()), max_len, 0.01, 0.001, 0.05,
+                                    seed=seed + 1000)
+    pool, at = [], 0
+    for t, n in enumerate(sizes):
+        L = int(rng.integers(50, max_len + 1))
+        rs = [r[:L] for r in rs_all[at:at + int(n)]]
+        at += int(n)
+        pool.append((int(n), synth.reads_fasta([f"s{t}_{i}" for i in range(int(n))], rs)))
+    return pool
+
+
+def serving_run(idx, device, seqs, pool_size=120, per_load=200, loads=(0.8,), seed=3,
+                workers=4):
+    """Serving on a resident index: the saturation throughput (every request
+    of the pool queued at once), then Poisson arrivals at fractions of it,
+    with per-request latency from submission to result (p50 / p99)."""
+    import numpy as np
+    import swift_gb300 as sg
+    rng = np.random.default_rng(seed + 7)
+    pool = serving_pool(seqs, pool_size, seed)
+    srv = sg.Server(idx, device=device, workers=workers)
+    try:
+        for n, r in pool[:8]:  # warm-up
+            srv.wait(srv.submit(r))
+        t0 = time.perf_counter()
+        tickets = [srv.submit(r) for _, r in pool]
+        for t in tickets:
+            srv.wait(t)
+        sat_s = time.perf_counter() - t0
+        total_reads = sum(n for n, _ in pool)
+        sat_rps = total_reads / sat_s
+        mean_reads = total_reads / len(pool)
+        out = []
+        for frac in loads:
+            rate = frac * sat_rps / mean_reads  # requests per second
+            gaps = rng.exponential(1.0 / rate, per_load)
+            picks = rng.integers(0, len(pool), per_load)
+            lat, done_reads = [], 0
+            start = time.perf_counter()
+            due = start
+            tks = []
+            for g, k in zip(gaps, picks):
+                due += g
+                now = time.perf_counter()
+                if due > now:
+                    time.sleep(due - now)
+                tks.append((srv.submit(pool[k][1]), pool[k][0]))
+            for t, n in tks:
+                _, st = srv.wait(t)
+                lat.append(st["total_ms"])
+                done_reads += n
+            el = time.perf_counter() - start
+            out.append({"offered_fraction": frac, "offered_reads_per_s": frac * sat_rps,
+                        "achieved_reads_per_s": done_reads / el, "requests": per_load,
+                        "p50_ms": float(np.percentile(lat, 50)),
+                        "p99_ms": float(np.percentile(lat, 99))})
+    finally:
+        srv.close()
+    return {"saturation_reads_per_s": sat_rps, "saturation_s": sat_s, "pool_requests": pool_size,
+            "mean_reads_per_request": mean_reads, "workers": workers,
+            "read_length": "U[50, %d] per request" % SERVE_MAX_READ, "latency": out}
+
+
+def bench_serving(args, rank, world, local):
+    """Serving (config 4): a 200 Mbp reference (24 sequences) resident;
+    requests of log-uniform size in [1, 10000] reads; see serving_run."""
     import swift_gb300 as sg
     from swift_gb300 import build as b, synth
     import torch
@@ -290,62 +448,21 @@ def bench_serving(args, rank, world, local, workers=4, pool_size=240, per_load=5
                                        n_units=500, unit_len=300, divergence=0.03, seed=0)
     ctx = sg.Context(local)
     idx = ctx.index(synth.fasta_bytes(names, seqs))
-    rng = np.random.default_rng(3 + rank)
-    sizes = np.floor(np.exp(rng.uniform(0, np.log(10001), pool_size))).astype(int).clip(1, 10000)
-    # reads drawn once at 199 bases, each request cut to its own length
-    _, rs_all, _ = synth.make_reads(seqs, int(sizes.sum()), 199, 0.01, 0.001, 0.05, seed=1000)
-    pool, at = [], 0
-    for t, n in enumerate(sizes):
-        L = int(rng.integers(50, 200))
-        rs = [r[:L] for r in rs_all[at:at + int(n)]]
-        at += int(n)
-        pool.append((int(n), synth.reads_fasta([f"s{t}_{i}" for i in range(int(n))], rs)))
-    srv = sg.Server(idx, device=local, workers=workers)
-    for n, r in pool[:8]:  # warm-up
-        srv.wait(srv.submit(r))
-    # saturation: the whole pool queued at once
-    t0 = time.perf_counter()
-    tickets = [srv.submit(r) for _, r in pool]
-    for t in tickets:
-        srv.wait(t)
-    sat_s = time.perf_counter() - t0
-    total_reads = sum(n for n, _ in pool)
-    sat_rps = total_reads / sat_s
-    mean_reads = total_reads / len(pool)
-    loads = []
-    for frac in (0.3, 0.6, 0.9):
-        rate = frac * sat_rps / mean_reads  # requests per second
-        gaps = rng.exponential(1.0 / rate, per_load)
-        picks = rng.integers(0, len(pool), per_load)
-        lat, done_reads = [], 0
-        start = time.perf_counter()
-        due = start
-        tks = []
-        for g, k in zip(gaps, picks):
-            due += g
-            now = time.perf_counter()
-            if due > now:
-                time.sleep(due - now)
-            tks.append((srv.submit(pool[k][1]), pool[k][0]))
-        for t, n in tks:
-            _, st = srv.wait(t)
-            lat.append(st["total_ms"])
-            done_reads += n
-        el = time.perf_counter() - start
-        loads.append({"offered_fraction": frac, "offered_reads_per_s": frac * sat_rps,
-                      "achieved_reads_per_s": done_reads / el, "requests": per_load,
-                      "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99))})
-    srv.close()
+    with ClockSampler(local) as clk:
+        res = serving_run(idx, local, seqs, pool_size=240, per_load=500,
+                          loads=(0.3, 0.6, 0.8, 0.9), seed=3 + rank)
     if rank == 0:
         print(json.dumps({
             "metric": "serving reads/s at saturation; p50/p99 request latency under Poisson load",
-            "value": sat_rps, "unit": "reads/s", "n_gpus": world, "steps": len(loads),
-            "warmup": 8, "ms_per_step": sat_s * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "int16x2", "data": "synthetic",
+            "value": res["saturation_reads_per_s"], "unit": "reads/s", "n_gpus": world,
+            "steps": len(res["latency"]), "warmup": 8, "ms_per_step": res["saturation_s"] * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int16x2",
+            "data": "synthetic",
             "config": {"workload": "serving: 200 Mbp / 24 seqs resident; %d-request pool, sizes "
-                       "log-uniform [1, 10000] reads (mean %.0f), read length U[50, 199] per "
-                       "request; %d concurrent pipelines" % (pool_size, mean_reads, workers)},
-            "latency": loads,
+                       "log-uniform [1, 10000] reads (mean %.0f), read length %s"
+                       % (res["pool_requests"], res["mean_reads_per_request"],
+                          res["read_length"])},
+            "latency": res["latency"], "clocks": clk.summary(),
         }))
     return 0
 
@@ -466,11 +583,11 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return 0
-        ref, reads, n, desc = make_workload(args, 0)
+        ref, reads, n, desc, _ = make_workload(args, 0)
         steps, warm = max(args.steps, 1), max(args.warmup, 0)
         n_sample = min(args.cpu_sample, n)
-        rps, threads, dt = cpu_reference(ref, reads, n_sample, steps, min(warm, 1),
-                                         1 if args.seeder == "lt13" else 0)
+        rps, threads, dt, _ = cpu_reference(ref, reads, n_sample, steps, min(warm, 1),
+                                            1 if args.seeder == "lt13" else 0)
         line = {
             "impl": "reference", "metric": metric_for(args), "value": rps, "unit": "reads/s",
             "n_gpus": args.gpus, "steps": steps, "warmup": warm,
@@ -479,6 +596,7 @@ def main():
             "config": {"workload": desc, "seeder": args.seeder,
                        "sample_reads_per_step": n_sample},
             "cpu_baseline": {"value": rps, "unit": "reads/s", "cores": threads, "kind": "port",
+                             "cpu_model": cpu_model(),
                              "sample": f"{n_sample} reads of the workload per step"},
             "e2e": {"value": rps, "unit": "reads/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
@@ -501,7 +619,7 @@ def main():
     device = local
     torch.cuda.set_device(device)
     b.build()
-    ref, reads, n, desc = make_workload(args, rank)
+    ref, reads, n, desc, wl = make_workload(args, rank)
     # a dedicated (non-default) stream shared by the library and the events
     stream = torch.cuda.Stream(device)
     torch.cuda.set_stream(stream)
@@ -550,10 +668,11 @@ def main():
         ms = max_over_ranks(ms)
     ms_step = ms / args.steps
     value = job_throughput(n, world, args.steps, ms * 1e-3)
-    sw_ms = statistics.median(s["sw_ms"] for s in stats)
-    seed_ms = statistics.median(s["seed_ms"] for s in stats)
+    # Phase 2 = Smith-Waterman passes + selection + traceback phase
+    p2_ms = statistics.median(s["sw_ms"] + s["select_ms"] + s["traceback_ms"] for s in stats)
     cells = stats[-1]["cells"]
-    gcups = cells / (sw_ms * 1e-3) / 1e9
+    gcups = cells / (p2_ms * 1e-3) / 1e9
+    gcups_computed = stats[-1]["sw_cells_computed"] / (p2_ms * 1e-3) / 1e9
     # end to end through the C ABI: host reads (pinned) in, host text out
     e2e = None
     if not args.no_e2e:
@@ -564,6 +683,8 @@ def main():
         for _ in range(2):
             ctx.align_into(idx, pinned.data_ptr(), len(reads), out_pinned.data_ptr(), cap, params)
         torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
         t0 = time.perf_counter()
         out_bytes = 0
         host = []
@@ -572,6 +693,8 @@ def main():
                                             out_pinned.data_ptr(), cap, params)
             host.append(est)
         torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
         e2e_s = time.perf_counter() - t0
         if world > 1:
             e2e_s = max_over_ranks(e2e_s)
@@ -582,14 +705,41 @@ def main():
                            for k in ("host_parse_ms", "h2d_ms", "d2h_ms", "total_ms")}}
     if rank != 0:
         return 0
-    cpu = None
+    cpu = parity = cpu_sw = None
+    k_cpu = min(args.cpu_sample, n)
+    model = cpu_model()
     try:
-        rps, threads, dt = cpu_reference(ref, reads, min(args.cpu_sample, n), 1, 0, seeder)
+        rps, threads, dt, cpu_out = cpu_reference(ref, reads, k_cpu, 1, 0, seeder,
+                                                  device_mem=ctx.info()["total_mem"])
         cpu = {"value": rps, "unit": "reads/s", "cores": threads, "kind": "port",
-               "sample": f"{min(args.cpu_sample, n)} reads of the workload, index prebuilt"}
+               "cpu_model": model,
+               "sample": f"{k_cpu} reads of the workload, index prebuilt"}
+        # the same sample through the GPU path, byte for byte against the
+        # oracle's output of the CPU baseline run
+        gpu_out = ctx.align(idx, sample_reads(reads, k_cpu), params)
+        parity = {"reads": k_cpu, "bytes": len(cpu_out), "bytes_equal": gpu_out == cpu_out,
+                  "checked_against": "oracle (CPU restatement of the reference path)"}
     except Exception as ex:  # the baseline must not break the GPU line
         cpu = {"value": None, "unit": "reads/s", "cores": os.cpu_count(), "kind": "port",
-               "sample": f"failed: {ex}"}
+               "cpu_model": model, "sample": f"failed: {ex}"}
+    try:
+        # Smith-Waterman alone: the port's routine on every host core against
+        # swift_sw_batch (the alignSequences equivalent) on the same pairs
+        n_sw = min(n, 40_000)
+        q, w, Q, R = workload_pairs(wl["seqs"], wl["reads"], wl["origins"], n_sw)
+        gc, threads, dt = cpu_sw_baseline(q, w, Q, R, n_sw)
+        ctx.sw_batch_arrays(q, w, Q, R)  # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.sw_batch_arrays(q, w, Q, R)
+        gdt = time.perf_counter() - t0
+        cpu_sw = {"gcups": gc, "pairs": n_sw, "shape": f"{Q} x {R}", "cores": threads,
+                  "kind": "port", "cpu_model": model, "seconds": dt,
+                  "gpu_sw_batch_gcups": n_sw * Q * R / gdt / 1e9,
+                  "gpu_note": "swift_sw_batch on the same pairs, host buffers in and out "
+                              "(copies included), every cell computed"}
+    except Exception as ex:
+        cpu_sw = {"gcups": None, "note": f"failed: {ex}"}
     # the dominant kernel alone, CUDA events on the library's stream: the
     # trace pass over whole windows (the candidates, or every pair for SAM)
     last = stats[-1]
@@ -610,6 +760,47 @@ def main():
         rf_kernel, rf_ms, rf_cells = "sw_packed_kernel score pass", fp_ms, last["first_pass_cells"]
         rf_dram, rf_algo, rf_note, rf_units = None, 112 + 304 + 4, SCORE_NOTE, fast_pairs
     achieved = rf_cells / (rf_ms * 1e-3) / 1e9 if rf_ms > 0 else None
+    # seeding against HBM: the survey's sector-model bytes (counted on the
+    # device per strand) over the warp kernels' CUDA-event time
+    seed_rf = None
+    if args.seeder == "ssaha" and last["seed_kernel_ms"] > 0:
+        sk_ms = statistics.median(s["seed_kernel_ms"] for s in stats)
+        hbm, hbm_src = hbm_peak()
+        ach = last["seed_model_bytes"] / (sk_ms * 1e-3) / 1e9
+        seed_rf = {"bound": "hbm", "kernel": "seed_fast_kernel + seed_sort_kernel",
+                   "model_bytes": last["seed_model_bytes"], "kernel_ms": sk_ms,
+                   "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                   "peak_source": hbm_src + " HBM copy bandwidth",
+                   "model": "per read strand ceil(L/4) + 32 B per k-mer lookup + "
+                            "32 * ceil(5 n / 32) B per occupied bucket of n postings + 12 B "
+                            "per hit out; the bucket directory and postings (about 70 MB) "
+                            "stay resident in L2"}
+    # short seeded runs of BASELINE configs 2 and 3 (config 4, serving, below)
+    configs = None
+    if not args.no_configs and args.workload == "scale" and args.format == "default":
+        configs = {}
+        for name, kw in (("batched", dict(n_reads=100_000, seed=11, seqs=wl["seqs"])),
+                         ("long", dict(n_reads=2_000, seed=12))):
+            try:
+                with ClockSampler(device) as cclk:
+                    configs[name] = pairs_run(ctx, name, steps=5, warmup=3, **kw)
+                configs[name]["clocks"] = cclk.summary()
+            except Exception as ex:
+                configs[name] = {"error": str(ex)}
+        try:
+            from swift_gb300 import synth
+            s_names, s_seqs = synth.make_reference(200_000_000, 24, sigma=0.8, repeat_frac=0.10,
+                                                   n_units=500, unit_len=300, divergence=0.03,
+                                                   seed=0)
+            s_idx = ctx.index(synth.fasta_bytes(s_names, s_seqs))
+            with ClockSampler(device) as cclk:
+                configs["serving"] = serving_run(s_idx, device, s_seqs)
+            configs["serving"]["clocks"] = cclk.summary()
+            configs["serving"]["workload"] = ("serving: 200 Mbp / 24 seqs resident; request "
+                                              "sizes log-uniform [1, 10000] reads")
+            s_idx.close()
+        except Exception as ex:
+            configs["serving"] = {"error": str(ex)}
     line = {
         "metric": metric_for(args), "value": value, "unit": "reads/s", "n_gpus": world,
         "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms_step,
@@ -627,6 +818,15 @@ def main():
                    "bound_pruned_pairs_per_step": stats[-1]["bound_pruned"],
                    "index_build_s": index_s, "index_load_s": index_load_s},
         "sw_gcups": gcups,
+        "sw_gcups_kind": ("effective: all Q x R cells of every record / Phase-2 device time "
+                          "(Smith-Waterman passes + selection + traceback phase, %.2f ms); the "
+                          "bounds rule most cells out without computing them" % p2_ms),
+        "sw_gcups_computed": gcups_computed,
+        "sw_gcups_computed_kind": ("DP cells the kernels computed (trace, relaxed bound, exact "
+                                   "score up to its early stop, generic) / the same time"),
+        "parity": parity,
+        "cpu_sw": cpu_sw,
+        "seed_roofline": seed_rf,
         "phase_ms": {k: statistics.median(s[k] for s in stats)
                      for k in ("seed_ms", "pairs_ms", "sw_ms", "select_ms", "traceback_ms",
                                "format_ms", "total_ms")},
@@ -653,6 +853,7 @@ def main():
         "e2e": e2e,
         "gpu_launches": int(sum(s["launches"] for s in stats)),
         "clocks": clk.summary(),
+        "configs": configs,
     }
     print(json.dumps(line))
     return 0

@@ -63,6 +63,11 @@ typedef struct {
                             src/search.cu:275-382); 1 lt13 seed-and-extend
                             (search2Queries, src/search2.cu:48-259), the
                             GPU default of the reference CLI               */
+  int32_t max_read_len;  /* longest read taken, up to 300; 0: the
+                            reference's 199 (its query buffer,
+                            src/common.h:40).  Longer reads are aligned the
+                            same way (query = first qry_len bases, 300-base
+                            windows); SSAHA seeding only                   */
 } swift_params;
 
 /* One Phase-1 record (one line of the reference's match file,
@@ -98,6 +103,15 @@ typedef struct {
   int64_t trace_cells;   /* DP cells of those launches                     */
   int64_t lcs_kept;      /* pairs the LCS bound could not rule out (they get
                             the relaxed bound pass)                          */
+  double seed_kernel_ms; /* SSAHA seeding's warp kernels alone (CUDA events) */
+  int64_t seed_model_bytes; /* their bytes under the seeding roofline's sector
+                            model: per read strand ceil(L/4) + 32 per k-mer
+                            lookup + 32 * ceil(5 n / 32) per occupied bucket
+                            of n postings + 12 per hit written             */
+  int64_t sw_cells_computed; /* DP cells the Smith-Waterman kernels computed:
+                            trace and exact score passes (up to their early
+                            stop), relaxed bound pass, generic kernel; the
+                            LCS bound's bit-parallel columns not counted    */
 } swift_stats;
 
 void swift_params_default(swift_params *p);
@@ -172,10 +186,14 @@ int swift_seed_lt13(swift_ctx *ctx, const swift_index *idx, const char *reads_fa
  * at qry + i*(Q+1) (Q bytes used), window i at ref + i*(R+1) (R bytes
  * used), outputs per pair: score, start, end, length and the reversed
  * consensus strings at qcons/rcons + i*(Q+R+2).  Pointers may be host or
- * device memory.  Q <= 256, R <= 1024. */
+ * device memory (device memory of the context's device; SWIFT_E_ARG for
+ * another device's).  1 <= Q <= 320, 1 <= R <= 1024, every shape in that
+ * range.  The scores are float, as alignSequences takes them; they must be
+ * whole numbers within +-32767 (the reference CLI reads them with atoi),
+ * SWIFT_E_ARG otherwise. */
 int swift_sw_batch(swift_ctx *ctx, const char *qry, const char *ref, int32_t Q,
-                   int32_t R, int64_t n_pairs, int32_t match, int32_t mismatch,
-                   int32_t gap_open, int32_t gap_ext, float *score,
+                   int32_t R, int64_t n_pairs, float match, float mismatch,
+                   float gap_open, float gap_ext, float *score,
                    int32_t *start, int32_t *end, int32_t *len, char *qcons,
                    char *rcons);
 
@@ -186,7 +204,8 @@ int swift_sw_batch(swift_ctx *ctx, const char *qry, const char *ref, int32_t Q,
  * have a request fail or stall in the allocator.  No counterpart in the
  * reference (its alignSequences works on buffers alignQueries3 allocates for
  * every batch).
- *   - every pointer must be device memory (SWIFT_E_ARG otherwise);
+ *   - every pointer must be device memory of the context's device
+ *     (SWIFT_E_ARG otherwise); scores as for swift_sw_batch;
  *   - n_pairs <= SWIFT_SW_NOALLOC_MAX_PAIRS (SWIFT_E_LIMIT otherwise): the
  *     per-pair intermediate results live in a fixed array in the library's
  *     module memory (16 bytes per pair, 1 MiB);
@@ -199,8 +218,8 @@ int swift_sw_batch(swift_ctx *ctx, const char *qry, const char *ref, int32_t Q,
  *     stream are ordered and safe. */
 #define SWIFT_SW_NOALLOC_MAX_PAIRS 65536
 int swift_sw_batch_noalloc(swift_ctx *ctx, const char *qry, const char *ref, int32_t Q,
-                           int32_t R, int64_t n_pairs, int32_t match, int32_t mismatch,
-                           int32_t gap_open, int32_t gap_ext, float *score,
+                           int32_t R, int64_t n_pairs, float match, float mismatch,
+                           float gap_open, float gap_ext, float *score,
                            int32_t *start, int32_t *end, int32_t *len, char *qcons,
                            char *rcons);
 

@@ -81,6 +81,7 @@ def lib():
         for f in ("so_index_start", "so_index_repeats", "so_index_actual"):
             getattr(L, f).argtypes = [C.c_void_p, C.c_int]
         L.so_index_postings.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        L.so_index_buckets.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         L.so_best_hits.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                    C.c_void_p, C.c_void_p, C.c_void_p]
         L.so_map_query.argtypes = [C.c_void_p, C.c_char_p, C.c_int, C.c_int,
@@ -96,6 +97,9 @@ def lib():
                                 C.POINTER(Params), C.POINTER(C.c_void_p),
                                 C.POINTER(C.c_int), C.c_char_p, C.c_size_t]
         L.so_free.argtypes = [C.c_void_p]
+        L.so_sw_batch.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_char_p, C.c_int, C.c_int,
+                                  C.c_long, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                  C.c_void_p]
         L.so_phase1_paired.argtypes = [C.c_char_p, C.c_size_t] * 3 + [
             C.POINTER(Params), C.POINTER(C.c_void_p), C.POINTER(C.c_long), C.c_char_p, C.c_size_t]
         L.so_align_paired.argtypes = [C.c_char_p, C.c_size_t] * 3 + [
@@ -167,6 +171,14 @@ class Index:
         lib().so_index_postings(self._h, ri.ctypes.data, rp.ctypes.data)
         return ri, rp
 
+    def buckets(self):
+        """lookupTable[] and numRepeatsPerTuple[] of every bucket."""
+        import numpy as np
+        look = np.zeros(self.num_buckets, dtype=np.int32)
+        rep = np.zeros(self.num_buckets, dtype=np.int32)
+        lib().so_index_buckets(self._h, look.ctypes.data, rep.ctypes.data)
+        return look, rep
+
     def map_query(self, seq: bytes, max_hits: int = 3):
         import numpy as np
         ri = np.zeros(max_hits, dtype=np.int8)
@@ -211,6 +223,21 @@ def sw(q: bytes, r: bytes, Q: int | None = None, R: int | None = None,
     if want_dirs:
         res["dirs"] = dirs.reshape(Q + 1, R + 1)
     return res
+
+
+def sw_batch(qry: bytes, Q: int, ref: bytes, R: int, n: int, m=2, x=-1, o=-10, e=-1,
+             threads: int | None = None):
+    """so_sw over n pairs in the alignSequences layout (query i at i*(Q+1),
+    window i at i*(R+1)) on host threads; returns (score, start, end, len)
+    arrays."""
+    import numpy as np
+    out = (Aln * max(n, 1))()
+    lib().so_sw_batch(qry, Q, Q + 1, ref, R, R + 1, n, m, x, o, e,
+                      threads or os.cpu_count() or 1, out)
+    a = np.ctypeslib.as_array(out).view(np.dtype([("score", "<f4"), ("start", "<i4"),
+                                                   ("end", "<i4"), ("len", "<i4"),
+                                                   ("cell_max", "<i4")]))[:n]
+    return a["score"].copy(), a["start"].copy(), a["end"].copy(), a["len"].copy()
 
 
 def align(ref: bytes, reads: bytes, params: Params | None = None) -> bytes:

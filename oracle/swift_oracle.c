@@ -361,6 +361,10 @@ void so_index_postings(const so_index *ix, int8_t *ri, int32_t *rp) {
   memcpy(ri, ix->ref_idx, (size_t)ix->total + 1);
   memcpy(rp, ix->ref_pos, ((size_t)ix->total + 1) * sizeof(int32_t));
 }
+void so_index_buckets(const so_index *ix, int32_t *lookup, int32_t *repeats) {
+  memcpy(lookup, ix->lookup, (size_t)ix->nb * sizeof(int32_t));
+  memcpy(repeats, ix->repeats, (size_t)ix->nb * sizeof(int32_t));
+}
 
 /* ------------------------------------------------------------------ */
 /* hits and best clusters                                              */
@@ -522,6 +526,47 @@ void so_sw(const char *q, int Q, const char *r, int R, int m, int x, int o,
   out->end = start + nref;
   out->len = tick + 1;
   if (!dirs) free(dir);
+}
+
+/* so_sw over n pairs (query i at q + i * qs, window i at r + i * rs) on
+ * `threads` host threads, each with its own direction matrix: the CPU
+ * Smith-Waterman baseline, threaded the way the reference's CPU path hands
+ * pairs to threads with one matrix set each (src/align.cu:2395-2422). */
+typedef struct {
+  const char *q, *r;
+  int Q, R, qs, rs, m, x, o, e, T, t;
+  long n;
+  so_aln *out;
+} so_swb;
+
+static void *so_swb_run(void *p) {
+  so_swb *a = (so_swb *)p;
+  uint8_t *dirs = (uint8_t *)malloc((size_t)(a->Q + 1) * (a->R + 1));
+  char *qc = (char *)malloc((size_t)a->Q + a->R + 2);
+  char *rc = (char *)malloc((size_t)a->Q + a->R + 2);
+  for (long i = a->t; i < a->n; i += a->T)
+    so_sw(a->q + i * (long)a->qs, a->Q, a->r + i * (long)a->rs, a->R, a->m, a->x, a->o, a->e,
+          &a->out[i], qc, rc, dirs);
+  free(dirs);
+  free(qc);
+  free(rc);
+  return NULL;
+}
+
+int so_sw_batch(const char *q, int Q, int qs, const char *r, int R, int rs, long n, int m,
+                int x, int o, int e, int threads, so_aln *out) {
+  if (threads < 1) threads = 1;
+  pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * (size_t)threads);
+  so_swb *args = (so_swb *)malloc(sizeof(so_swb) * (size_t)threads);
+  for (int t = 0; t < threads; ++t) {
+    so_swb a = {q, r, Q, R, qs, rs, m, x, o, e, threads, t, n, out};
+    args[t] = a;
+    pthread_create(&th[t], NULL, so_swb_run, &args[t]);
+  }
+  for (int t = 0; t < threads; ++t) pthread_join(th[t], NULL);
+  free(th);
+  free(args);
+  return 0;
 }
 
 /* ------------------------------------------------------------------ */

@@ -68,6 +68,8 @@ int so_index_actual(const so_index *, int h);     /* numActualRepeats[h]   */
 /* refIdx[] and refPos[] of the reference layout: total+1 entries, slot 0 is
  * -1, each bucket in reverse order of occurrence. */
 void so_index_postings(const so_index *, int8_t *ref_idx, int32_t *ref_pos);
+/* lookupTable[] and numRepeatsPerTuple[] of every bucket at once. */
+void so_index_buckets(const so_index *, int32_t *lookup, int32_t *repeats);
 int so_index_num_refs(const so_index *);
 
 /* mapHits6GetBestHits (src/mapHits6.cu:40-70) with the deterministic tie
@@ -90,6 +92,9 @@ void so_revcomp(const char *seq, int len, char *out);
  * not NULL, receives (Q+1)*(R+1) direction codes. */
 void so_sw(const char *q, int Q, const char *r, int R, int m, int x, int o,
            int e, so_aln *out, char *qcons, char *rcons, uint8_t *dirs);
+/* so_sw over n pairs on `threads` host threads (the CPU baseline). */
+int so_sw_batch(const char *q, int Q, int qs, const char *r, int R, int rs, long n, int m,
+                int x, int o, int e, int threads, so_aln *out);
 
 /* The whole spec pipeline: SSAHA seeding (searchQueries3,
  * src/search.cu:275-382) -> GPU-kernel Smith-Waterman over 300-base windows

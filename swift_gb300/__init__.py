@@ -42,7 +42,7 @@ class Params(C.Structure):
         ("seed_len", C.c_int32), ("ignore_thres", C.c_int32), ("max_hits", C.c_int32),
         ("match", C.c_int32), ("mismatch", C.c_int32), ("gap_open", C.c_int32),
         ("gap_ext", C.c_int32), ("qry_len", C.c_int32), ("device_mem", C.c_int64),
-        ("out_format", C.c_int32), ("seeder", C.c_int32),
+        ("out_format", C.c_int32), ("seeder", C.c_int32), ("max_read_len", C.c_int32),
     ]
 
 
@@ -80,6 +80,8 @@ class Stats(C.Structure):
         ("retraced_pairs", C.c_int64), ("first_pass_ms", C.c_double),
         ("first_pass_cells", C.c_int64), ("first_pass_kind", C.c_int64),
         ("trace_ms", C.c_double), ("trace_cells", C.c_int64), ("lcs_kept", C.c_int64),
+        ("seed_kernel_ms", C.c_double), ("seed_model_bytes", C.c_int64),
+        ("sw_cells_computed", C.c_int64),
     ]
 
     def as_dict(self):
@@ -119,7 +121,8 @@ def lib():
                                          vp]
         L.swift_align_paired_into.argtypes = [vp, vp, vp, sz, vp, sz, C.POINTER(Params),
                                               C.c_uint32, C.c_uint32, vp, sz, C.POINTER(sz), vp]
-        L.swift_sw_batch.argtypes = [vp, vp, vp, i32, i32, i64, i32, i32, i32, i32,
+        f32 = C.c_float
+        L.swift_sw_batch.argtypes = [vp, vp, vp, i32, i32, i64, f32, f32, f32, f32,
                                      vp, vp, vp, vp, vp, vp]
         L.swift_align.argtypes = [vp, vp, vp, sz, C.POINTER(Params), C.POINTER(vp),
                                   C.POINTER(sz), C.POINTER(Stats)]
@@ -245,6 +248,23 @@ class Context:
             out.append(dict(score=float(score[i]), start=int(start[i]), end=int(end[i]), len=L,
                             qcons=bytes(qc[i, :max(L, 0)]), rcons=bytes(rc[i, :max(L, 0)])))
         return out
+
+    def sw_batch_arrays(self, q, w, Q: int, R: int, match=2, mismatch=-1, gap_open=-10,
+                        gap_ext=-1):
+        """swift_sw_batch on host arrays already in its layout: q is n x (Q+1)
+        and w n x (R+1) uint8.  Returns (score, start, end, len) arrays; the
+        consensus strings stay in host buffers this call allocates."""
+        import numpy as np
+        n = q.shape[0]
+        score = np.zeros(n, np.float32)
+        start, end, ln = (np.zeros(n, np.int32) for _ in range(3))
+        qc = np.zeros((n, Q + R + 2), np.uint8)
+        rc = np.zeros((n, Q + R + 2), np.uint8)
+        self._check(lib().swift_sw_batch(
+            self._h, q.ctypes.data, w.ctypes.data, Q, R, n, match, mismatch, gap_open, gap_ext,
+            score.ctypes.data, start.ctypes.data, end.ctypes.data, ln.ctypes.data,
+            qc.ctypes.data, rc.ctypes.data))
+        return score, start, end, ln
 
     def sw_pairs(self, qry: bytes, q_off, q_len, ref: bytes, r_off, r_len, match=2, mismatch=-1,
                  gap_open=-10, gap_ext=-1, mode=0, consensus=True):

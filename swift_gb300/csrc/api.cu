@@ -309,6 +309,10 @@ struct SeedOut {
   int64_t n = 0;
   int64_t overflow = 0;
   int64_t launches = 0;
+  // SSAHA seeding: the warp kernels' device time and their sector-model
+  // bytes (counters on the device, read with the call's last results)
+  double kernel_ms = 0;
+  unsigned long long* d_model = nullptr;
 };
 
 // lookupTable2's position of every posting (src/lookupTable2.cu:75-218,
@@ -456,12 +460,27 @@ int seed_ssaha(swift_ctx* ctx, Scratch& sc, SeedArgs a, SeedOut* out) {
   int32_t* ovl = a.overflow_list;
   int32_t* novl = a.n_overflow;
   int32_t* nbest = a.nbest;
+  CK(sc.get(&a.mid_list, (size_t)std::max<int64_t>(ns, 1)));
+  CK(sc.get(&a.n_mid, 1));
+  CK(cudaMemsetAsync(a.n_mid, 0, sizeof(int32_t), st));
+  if (!out->d_model) {
+    CK(sc.get(&out->d_model, kSeedModelSlots));
+    CK(cudaMemsetAsync(out->d_model, 0, kSeedModelSlots * sizeof(unsigned long long), st));
+  }
+  a.model_bytes = out->d_model;
+  CK(cudaEventRecord(ctx->ev[9], st));
   launch_seed(st, a);
   CKLAUNCH();
-  out->launches += n > 0 ? 1 : 0;
+  CK(cudaEventRecord(ctx->ev[10], st));
+  out->launches += n > 0 ? 2 : 0;
   int32_t h_novl = 0;
   CK(cudaMemcpyAsync(&h_novl, novl, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
+  if (n > 0) {
+    float t = 0;
+    cudaEventElapsedTime(&t, ctx->ev[9], ctx->ev[10]);
+    out->kernel_ms += t;
+  }
   out->overflow += h_novl;
   if (h_novl > 0) {
     std::vector<int32_t> list(h_novl), nb(ns);
@@ -702,7 +721,8 @@ double ms_since(std::chrono::steady_clock::time_point t0) {
 // transient: buffers for one call, from the stream-ordered pool of ctx->st
 // (freed in stream order by swift_reads_destroy)
 int upload_reads(swift_ctx* ctx, const char* b, size_t len, swift_reads** out,
-                 double* parse_ms = nullptr, double* h2d_ms = nullptr, bool transient = false) {
+                 double* parse_ms = nullptr, double* h2d_ms = nullptr, bool transient = false,
+                 int max_read = kReadMax) {
   // bytes to the device, then the record structure found there (parse.cu)
   cudaStream_t st = ctx->st;
   swift_reads* r = new swift_reads();
@@ -752,7 +772,7 @@ int upload_reads(swift_ctx* ctx, const char* b, size_t len, swift_reads** out,
     const size_t rd_bytes = std::max<uint64_t>(n_lines / 2, 1) * sizeof(DevRead);
     CKR(transient ? cudaMallocAsync(&r->d_rd, rd_bytes, st) : cudaMalloc(&r->d_rd, rd_bytes));
     launch_parse_newlines(st, r->d_bytes, len, off, nl);
-    launch_parse_lines(st, r->d_bytes, len, nl, n_nl, n_lines, r->d_rd, sum, err);
+    launch_parse_lines(st, r->d_bytes, len, nl, n_nl, n_lines, r->d_rd, sum, err, max_read);
     CKR(cudaGetLastError());
     unsigned long long h_err = 0;
     ParseSummary h_sum;
@@ -761,7 +781,7 @@ int upload_reads(swift_ctx* ctx, const char* b, size_t len, swift_reads** out,
     CKR(cudaStreamSynchronize(st));
     if (h_err != ~0ull) {
       std::string m;
-      const int code = parse_error((uint32_t)(h_err & 0xFF), h_err >> 8, &m);
+      const int code = parse_error((uint32_t)(h_err & 0xFF), h_err >> 8, &m, max_read);
       return bail(code, m);
     }
     r->n = (int64_t)(n_lines / 2);
@@ -793,6 +813,7 @@ void swift_params_default(swift_params* p) {
   p->device_mem = 0;
   p->out_format = 0;
   p->seeder = 0;
+  p->max_read_len = 0;
 }
 
 int swift_ctx_create(int device, void* stream, swift_ctx** out) {
@@ -813,7 +834,7 @@ int swift_ctx_create(int device, void* stream, swift_ctx** out) {
     e = cudaMemGetInfo(&fr, &tot);
     ctx->total_mem = (int64_t)tot;
   }
-  for (int i = 0; i < 10 && e == cudaSuccess; ++i) e = cudaEventCreate(&ctx->ev[i]);
+  for (int i = 0; i < kCtxEvents && e == cudaSuccess; ++i) e = cudaEventCreate(&ctx->ev[i]);
   if (e != cudaSuccess) {
     delete ctx;
     return SWIFT_E_CUDA;
@@ -828,7 +849,7 @@ int swift_ctx_destroy(swift_ctx* ctx) {
   cudaSetDevice(ctx->device);
   if (ctx->st) cudaStreamSynchronize(ctx->st);
   if (ctx->d_text) cudaFree(ctx->d_text);
-  for (int i = 0; i < 10; ++i)
+  for (int i = 0; i < kCtxEvents; ++i)
     if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
   if (ctx->side) {
     cudaStreamSynchronize(ctx->side);
@@ -1043,7 +1064,9 @@ int swift_index_export(swift_ctx* ctx, const swift_index* ix, int32_t* lookup, i
 int swift_reads_upload(swift_ctx* ctx, const char* b, size_t len, swift_reads** out) {
   if (!ctx || !b || !out) return fail(ctx, SWIFT_E_ARG, "null argument");
   CK(cudaSetDevice(ctx->device));
-  return upload_reads(ctx, b, len, out);
+  // reads up to the longest the pipeline takes; each call checks its own
+  // limit (swift_params.max_read_len)
+  return upload_reads(ctx, b, len, out, nullptr, nullptr, false, kSeedReadMax);
 }
 
 int swift_reads_destroy(swift_reads* r) {
@@ -1117,11 +1140,34 @@ int swift_seed_lt13(swift_ctx* ctx, const swift_index* idx, const char* reads, s
 }
 
 
+// alignSequences takes its scores as float (src/align.cu:2904-2921) and the
+// reference CLI parses them with atoi (src/main.cu:309-324), so they are
+// whole numbers: refuse any other value instead of truncating it.
+static int whole_scores(swift_ctx* ctx, float fm, float fx, float fo, float fe, int32_t* m,
+                        int32_t* x, int32_t* o, int32_t* e) {
+  const float in[4] = {fm, fx, fo, fe};
+  int32_t* out[4] = {m, x, o, e};
+  for (int i = 0; i < 4; ++i) {
+    const float v = in[i];
+    if (!(v == v) || v != std::nearbyint(v) || std::fabs(v) > 32767.0f)
+      return fail(ctx, SWIFT_E_ARG,
+                  "scores must be whole numbers within +-32767 (the reference parses them "
+                  "with atoi)");
+    *out[i] = (int32_t)v;
+  }
+  return SWIFT_OK;
+}
+
 int swift_sw_batch(swift_ctx* ctx, const char* qry, const char* ref, int32_t Q, int32_t R,
-                   int64_t n, int32_t m, int32_t x, int32_t o, int32_t e, float* score,
+                   int64_t n, float fm, float fx, float fo, float fe, float* score,
                    int32_t* start, int32_t* end, int32_t* len, char* qcons, char* rcons) {
   if (!ctx || !qry || !ref || !score || !start || !end || !len || !qcons || !rcons)
     return fail(ctx, SWIFT_E_ARG, "null argument");
+  int32_t m, x, o, e;
+  {
+    const int rcw = whole_scores(ctx, fm, fx, fo, fe, &m, &x, &o, &e);
+    if (rcw != SWIFT_OK) return rcw;
+  }
   if (n < 0) return fail(ctx, SWIFT_E_ARG, "negative pair count");
   if (Q < 1 || Q > kMaxQ || R < 1 || R > kMaxR)
     return fail(ctx, SWIFT_E_LIMIT, "Q must be 1..256 and R 1..1024");
@@ -1137,6 +1183,19 @@ int swift_sw_batch(swift_ctx* ctx, const char* qry, const char* ref, int32_t Q, 
     }
     return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
   };
+  {
+    const void* ptrs[] = {qry, ref, score, start, end, len, qcons, rcons};
+    for (const void* q : ptrs) {
+      cudaPointerAttributes at;
+      if (cudaPointerGetAttributes(&at, q) != cudaSuccess) {
+        cudaGetLastError();
+        continue;
+      }
+      if (at.type == cudaMemoryTypeDevice && at.device != ctx->device)
+        return fail(ctx, SWIFT_E_ARG,
+                    "swift_sw_batch: a buffer lives on another device than the context's");
+    }
+  }
   const int64_t cs = (int64_t)Q + R + 2;
   const char* dq = qry;
   const char* dw = ref;
@@ -1202,13 +1261,18 @@ int swift_sw_batch(swift_ctx* ctx, const char* qry, const char* ref, int32_t Q, 
 }
 
 int swift_sw_batch_noalloc(swift_ctx* ctx, const char* qry, const char* ref, int32_t Q,
-                           int32_t R, int64_t n, int32_t m, int32_t x, int32_t o, int32_t e,
+                           int32_t R, int64_t n, float fm, float fx, float fo, float fe,
                            float* score, int32_t* start, int32_t* end, int32_t* len,
                            char* qcons, char* rcons) {
   // Same kernels as swift_sw_batch; the per-pair records go to the static
   // array of sw.cu instead of pool memory, and the host never waits.
   if (!ctx || !qry || !ref || !score || !start || !end || !len || !qcons || !rcons)
     return fail(ctx, SWIFT_E_ARG, "null argument");
+  int32_t m, x, o, e;
+  {
+    const int rcw = whole_scores(ctx, fm, fx, fo, fe, &m, &x, &o, &e);
+    if (rcw != SWIFT_OK) return rcw;
+  }
   if (n < 0) return fail(ctx, SWIFT_E_ARG, "negative pair count");
   if (n > kStaticSwPairs)
     return fail(ctx, SWIFT_E_LIMIT,
@@ -1226,6 +1290,9 @@ int swift_sw_batch_noalloc(swift_ctx* ctx, const char* qry, const char* ref, int
     }
     if (at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged)
       return fail(ctx, SWIFT_E_ARG, "swift_sw_batch_noalloc takes device pointers only");
+    if (at.type == cudaMemoryTypeDevice && at.device != ctx->device)
+      return fail(ctx, SWIFT_E_ARG,
+                  "swift_sw_batch_noalloc: a buffer lives on another device than the context's");
   }
   DevAln* aln = nullptr;
   int rc = static_sw_scratch(ctx->device, &aln, &ctx->err);
@@ -1751,6 +1818,12 @@ int swift_sw_pairs(swift_ctx* ctx, const char* qry, const int64_t* q_off, const 
 // host_out (optional, host_cap bytes): the text is also copied there,
 // overlapped with its writing; the copies are complete once ctx->st is
 // synchronised.  Text longer than host_cap is not copied.
+// The longest read a call takes: the reference's 199 bases unless the
+// parameters allow more (up to kSeedReadMax).
+static int read_limit(const swift_params* p) {
+  return p && p->max_read_len > 0 ? std::min(p->max_read_len, kSeedReadMax) : kReadMax;
+}
+
 static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swift_reads* rd,
                                const swift_params* p, size_t* out_len, swift_stats* stats,
                                char* host_out, size_t host_cap) {
@@ -1759,8 +1832,15 @@ static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swi
   if (p->seed_len != idx->k || p->ignore_thres != idx->thres)
     return fail(ctx, SWIFT_E_ARG, "parameters differ from the index's seed length / threshold");
   if (p->max_hits < 1 || p->max_hits > 64) return fail(ctx, SWIFT_E_ARG, "max_hits outside 1..64");
+  if (p->max_read_len < 0 || p->max_read_len > kSeedReadMax)
+    return fail(ctx, SWIFT_E_ARG, "max_read_len outside 0..300");
+  if (rd->max_len > read_limit(p))
+    return fail(ctx, SWIFT_E_LIMIT,
+                "reads: read longer than " + std::to_string(read_limit(p)) + " bases" +
+                    (read_limit(p) == kReadMax ? " (the reference's query buffer)" : ""));
   const int Q = p->qry_len > 0 ? p->qry_len : rd->first_len;
-  if (Q < 1 || Q > kMaxQ) return fail(ctx, SWIFT_E_LIMIT, "query length outside 1..256");
+  if (Q < 1 || Q > kMaxQ)
+    return fail(ctx, SWIFT_E_LIMIT, "query length outside 1.." + std::to_string(kMaxQ));
   if (rd->n > 0 && rd->min_len < Q)
     return fail(ctx, SWIFT_E_INPUT,
                 "a read is shorter than the query length; the reference aligns such reads "
@@ -1898,6 +1978,10 @@ static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swi
   }
   fa2.ub = ub;
   fa2.suf = suf;
+  unsigned long long* d_cells;
+  CK(sc.get(&d_cells, 1));
+  CK(cudaMemsetAsync(d_cells, 0, sizeof(unsigned long long), st));
+  fa2.cells_done = d_cells;
   CK(cudaEventRecord(ctx->ev[7], st));
   if (fast_ok && nproc > 0 && !sam) {
     fa2.list = fast_list;
@@ -2087,6 +2171,10 @@ static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swi
   uint64_t total = 0;
   CK(cudaMemcpyAsync(&total, tot_d, 8, cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(h_cnt, cnt, sizeof(h_cnt), cudaMemcpyDeviceToHost, st));
+  unsigned long long h_cells = 0, h_model[kSeedModelSlots] = {};
+  CK(cudaMemcpyAsync(&h_cells, d_cells, sizeof(h_cells), cudaMemcpyDeviceToHost, st));
+  if (so.d_model)
+    CK(cudaMemcpyAsync(h_model, so.d_model, sizeof(h_model), cudaMemcpyDeviceToHost, st));
   TextChunks chunks;
   rc = chunks.plan(ctx, st, offs, nproc, host_out != nullptr);
   if (rc != SWIFT_OK) return rc;
@@ -2127,6 +2215,11 @@ static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swi
       s.first_pass_cells = fast_ok ? (int64_t)h_cnt[0] * Q * kWin : 0;
     }
     s.lcs_kept = lcs_kept;
+    s.seed_kernel_ms = so.kernel_ms;
+    for (int i = 0; i < kSeedModelSlots; ++i) s.seed_model_bytes += (int64_t)h_model[i];
+    // the relaxed bound pass and the generic kernel compute every cell of
+    // their pairs; the packed score and trace passes counted theirs
+    s.sw_cells_computed = (int64_t)h_cells + (lcs_kept + (int64_t)h_cnt[1]) * Q * kWin;
     cudaEventElapsedTime(&t, ctx->ev[3], ctx->ev[6]);
     s.select_ms = t;
     cudaEventElapsedTime(&t, ctx->ev[6], ctx->ev[4]);
@@ -2171,7 +2264,7 @@ int swift_align(swift_ctx* ctx, const swift_index* idx, const char* reads, size_
   CK(cudaSetDevice(ctx->device));
   swift_reads* rd = nullptr;
   double parse_ms = 0, h2d_ms = 0;
-  int rc = upload_reads(ctx, reads, len, &rd, &parse_ms, &h2d_ms, true);
+  int rc = upload_reads(ctx, reads, len, &rd, &parse_ms, &h2d_ms, true, read_limit(p));
   if (rc != SWIFT_OK) return rc;
   size_t n = 0;
   rc = swift_align_resident(ctx, idx, rd, p, &n, stats);
@@ -2208,7 +2301,7 @@ int swift_align_into(swift_ctx* ctx, const swift_index* idx, const char* reads, 
   CK(cudaSetDevice(ctx->device));
   swift_reads* rd = nullptr;
   double parse_ms = 0, h2d_ms = 0;
-  int rc = upload_reads(ctx, reads, len, &rd, &parse_ms, &h2d_ms, true);
+  int rc = upload_reads(ctx, reads, len, &rd, &parse_ms, &h2d_ms, true, read_limit(p));
   if (rc != SWIFT_OK) return rc;
   size_t n = 0;
   // the text is copied to out while it is written

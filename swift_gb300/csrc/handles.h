@@ -10,13 +10,15 @@
 
 #include "internal.h"
 
+constexpr int kCtxEvents = 12;
+
 struct swift_ctx {
   int device = 0;
   cudaStream_t st = nullptr;
   bool own_stream = false;
   std::string err;
   int64_t total_mem = 0;
-  cudaEvent_t ev[10] = {};
+  cudaEvent_t ev[kCtxEvents] = {};
   char* d_text = nullptr;
   size_t text_len = 0, text_cap = 0;
   int sw_path = 0;  // 0 bounded selection, 1 generic kernel only, 2 exact score of every pair

@@ -147,6 +147,74 @@ int parse_reference(const char* b, size_t n, HostRef* out, std::string* err) {
   return SWIFT_OK;
 }
 
+int parse_reads_host(const char* b, size_t n, int max_read, HostReads* out, std::string* err) {
+  // The rules of the device parser (parse.cu) in one pass over the lines:
+  // every failure is recorded with its offset and the first in file order
+  // (offset, then code) is reported, as the device's atomicMin does.
+  uint64_t worst = ~0ull;
+  auto report = [&](uint64_t off, uint32_t code) {
+    worst = std::min<uint64_t>(worst, (off << 8) | code);
+  };
+  HostReads r;
+  int32_t mn = INT32_MAX, mx = 0;
+  uint64_t line_start = 0, prev_header = 0;
+  int64_t li = 0;
+  char prev = '\n';
+  const uint64_t n_nl = (uint64_t)std::count(b, b + n, '\n');
+  const uint64_t n_lines = n_nl + ((n > 0 && b[n - 1] != '\n') ? 1 : 0);
+  uint64_t pos = 0;
+  while (li < (int64_t)n_lines) {
+    const char* nlp = (const char*)memchr(b + pos, '\n', n - pos);
+    const uint64_t end = nlp ? (uint64_t)(nlp - b) : n;
+    for (uint64_t i = pos; i < end; ++i) {
+      const uint8_t x = (uint8_t)b[i];
+      if (x == 0 || x >= 128) report(i, kParseBadByte);
+      if (x == '>' && prev != '\n') report(i, kParseGtInLine);
+      prev = (char)x;
+    }
+    prev = '\n';
+    line_start = pos;
+    const uint64_t len = end - line_start;
+    if (len == 0) {
+      report(line_start, kParseEmptyLine);
+    } else {
+      const bool header = b[line_start] == '>';
+      if ((li & 1) == 0) {
+        if (!header) {
+          report(line_start, li == 0 ? kParseSeqNoHeader : kParseMultiLine);
+        } else {
+          if (len - 1 > (uint64_t)(kNameMax - 2)) report(line_start, kParseNameLong);
+          if ((uint64_t)li + 1 >= n_lines) report(line_start, kParseTrailingHeader);
+        }
+        prev_header = line_start;
+      } else if (header) {
+        report(li == 1 ? 0 : prev_header, kParseHeaderNoSeq);
+      } else if (len > (uint64_t)max_read) {
+        report(line_start, kParseReadLong);
+      } else {
+        DevRead d;
+        d.name_off = prev_header;
+        d.seq_off = line_start;
+        d.len = (int32_t)len;
+        d.name_len = (int32_t)(line_start - 1 - prev_header - 1);
+        r.rd.push_back(d);
+        mn = std::min(mn, (int32_t)len);
+        mx = std::max(mx, (int32_t)len);
+        if (li == 1) r.first_len = (int32_t)len - (end == n ? 1 : 0);  // strlen(line) - 1
+      }
+    }
+    pos = end + 1;
+    ++li;
+  }
+  if (worst != ~0ull) return parse_error((uint32_t)(worst & 0xFF), worst >> 8, err, max_read);
+  r.n = (int64_t)(n_lines / 2);
+  r.n_gt = (int64_t)((n_lines + 1) / 2);
+  r.min_len = r.n ? mn : 0;
+  r.max_len = mx;
+  *out = std::move(r);
+  return SWIFT_OK;
+}
+
 std::vector<int32_t> phase1_stale_repeats(int64_t n_reads, int64_t n_gt) {
   // searchQueries3 (src/search.cu:325-357) calls qryGetNext2 in batches of
   // 16 while i < numQrs; a slot whose call finds the end of the file keeps

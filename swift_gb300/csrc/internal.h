@@ -21,7 +21,8 @@ constexpr int kShiftBases = 100;  // REF_LENGTH / 3 (src/align.cu:668)
 constexpr int kMaxRefs = 127;     // refIdx is a char in the reference
 constexpr int kLineMax = 100000;  // MAX_LINE_LENGTH (fgets chunking)
 constexpr int kP1Slots = 16;      // NUM_THREADS of searchQueries3
-constexpr int kMaxQ = 256;        // query rows supported by the SW kernels
+constexpr int kSeedReadMax = 300;  // longest strand the seeding kernels take
+constexpr int kMaxQ = 320;        // query rows supported by the SW kernels
 constexpr int kMaxR = 1024;       // window columns supported by the SW kernels
 
 // ---------------------------------------------------------------------------
@@ -80,6 +81,16 @@ struct DevRead {          // per read
   int32_t len;
   int32_t name_len;
 };
+
+// A reads FASTA parsed on the host with the device parser's rules
+// (parse.cu), reads up to max_read bases: the per-read records (offsets
+// into b) and the lengths the pipeline needs.
+struct HostReads {
+  std::vector<DevRead> rd;
+  int64_t n = 0, n_gt = 0;
+  int32_t first_len = 0, min_len = 0, max_len = 0;
+};
+int parse_reads_host(const char* b, size_t n, int max_read, HostReads* out, std::string* err);
 
 // One Phase-2 pair (one match record).
 struct DevPair {
@@ -150,10 +161,17 @@ struct SeedArgs {
                               // strand string's first fixed_len; paired end)
   int3* best;                 // per strand: max_hits x (ri, shift, rp)
   int32_t* nbest;             // per strand
-  int32_t* overflow_list;     // strands too big for the on-chip path
+  int32_t* overflow_list;     // strands too big for the on-chip paths
   int32_t* n_overflow;
+  int32_t* mid_list;          // strands for the sort kernel (zeroed count)
+  int32_t* n_mid;
+  unsigned long long* model_bytes;  // optional: kSeedModelSlots counters of
+                                    // the roofline's sector-model bytes
   uint64_t* scratch;          // overflow path: per-strand hash tables
 };
+constexpr int kSeedModelSlots = 64;
+// The sort-free kernel over every strand, then the sort kernel over the
+// strands it listed; strands beyond both go to a.overflow_list.
 void launch_seed(cudaStream_t st, const SeedArgs& a);
 
 // seed13.cu: lt13 seed-and-extend seeding (search2Queries)
@@ -212,8 +230,8 @@ void launch_parse_newlines(cudaStream_t st, const char* b, uint64_t n, const uin
                            uint64_t* nl);
 void launch_parse_lines(cudaStream_t st, const char* b, uint64_t n, const uint64_t* nl,
                         uint64_t n_nl, uint64_t n_lines, DevRead* rd, ParseSummary* sum,
-                        unsigned long long* err);
-int parse_error(uint32_t code, uint64_t off, std::string* msg);
+                        unsigned long long* err, int max_read);
+int parse_error(uint32_t code, uint64_t off, std::string* msg, int max_read = kReadMax);
 
 // pairs.cu
 struct PairArgs {
@@ -230,10 +248,13 @@ struct PairArgs {
   const int32_t* m_rp;
   int64_t n;
   int Q;
+  const int32_t* read_q;      // optional: query length per read (reads of
+                              // requests with different query lengths)
+  int32_t* pair_q;            // optional out: each record's query length
   DevPair* pairs;
   char* qbuf;                 // n x Qs
   char* wbuf;                 // n x kWinPad
-  int Qs;                     // query stride
+  int Qs;                     // query stride (>= every query length + 1)
 };
 void launch_build_pairs(cudaStream_t st, const PairArgs& a);
 
@@ -304,6 +325,7 @@ struct SwArgs {
   int64_t cons_stride;
   const int32_t* list;        // optional: pair ids to process ...
   const int32_t* count;       // ... and their number (device); grid sized by n
+  const int32_t* q_len;       // optional: query length per pair (<= Q)
 };
 // Static scratch of swift_sw_batch_noalloc (sw.cu): room for this many pairs.
 constexpr int64_t kStaticSwPairs = SWIFT_SW_NOALLOC_MAX_PAIRS;
@@ -406,16 +428,20 @@ struct FastArgs {
   char* qcons;                // trace pass: reversed consensus strings
   char* rcons;
   int64_t cons_stride;
+  unsigned long long* cells_done;  // optional: score and trace passes add the
+                                   // cells they computed (early stop counted)
 };
 bool fast_params_ok(int Q, int R, int m, int x, int o, int e, int* bias);
 constexpr int kFastMaxR = 512;  // window columns the packed passes take
 // Packed shape class of a query length (the (lanes, rows) shapes of the
 // packed passes, shortest first), and the longest query of each class.
 __host__ __device__ inline int packed_class(int Q) {
-  return Q <= 32 ? 0 : Q <= 64 ? 1 : Q <= 104 ? 2 : Q <= 128 ? 3 : Q <= 208 ? 4 : Q <= 256 ? 5 : -1;
+  return Q <= 32 ? 0 : Q <= 64 ? 1 : Q <= 104 ? 2 : Q <= 128 ? 3 : Q <= 208 ? 4 : Q <= 256 ? 5
+       : Q <= 320 ? 6 : -1;
 }
 __host__ __device__ inline int packed_class_max_q(int c) {
-  return c == 0 ? 32 : c == 1 ? 64 : c == 2 ? 104 : c == 3 ? 128 : c == 4 ? 208 : 256;
+  return c == 0 ? 32 : c == 1 ? 64 : c == 2 ? 104 : c == 3 ? 128 : c == 4 ? 208 : c == 5 ? 256
+       : 320;
 }
 int64_t trace_scratch_words(int Q, int R, int64_t pairs);
 int launch_sw_score(cudaStream_t st, const FastArgs& a, int64_t max_pairs);

@@ -173,7 +173,8 @@ __global__ void __launch_bounds__(kPairWarps * 32) build_pairs_kernel(PairArgs a
   // query
   const DevRead rd = a.rd[read];
   const char* s = a.reads + rd.seq_off;
-  const int Q = a.Q;
+  const int Q = a.read_q ? a.read_q[read] : a.Q;  // the read's request's query length
+  if (a.pair_q && lane == 0) a.pair_q[j] = Q;
   const int avail = rd.len < Q ? rd.len : Q;
   char* qout = a.qbuf + j * (int64_t)a.Qs;
   // four bytes per lane, one 32-bit store each (Qs is a multiple of 16)

@@ -103,7 +103,7 @@ __global__ void tile_newlines(const uint8_t* __restrict__ b, uint64_t n,
 __global__ void lines_to_reads(const uint8_t* __restrict__ b, uint64_t n,
                                const uint64_t* __restrict__ nl, uint64_t n_nl, uint64_t n_lines,
                                DevRead* __restrict__ rd, ParseSummary* sum,
-                               unsigned long long* err) {
+                               unsigned long long* err, int max_read) {
   const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   // the read length of this line, if it is a well-formed sequence line;
   // reduced over the warp before the atomics (one address for all reads)
@@ -130,7 +130,7 @@ __global__ void lines_to_reads(const uint8_t* __restrict__ b, uint64_t n,
       report(err, i == 1 ? 0 : nl[i - 2] + 1, kParseHeaderNoSeq);
       return;
     }
-    if (len > (uint64_t)kReadMax) {
+    if (len > (uint64_t)max_read) {
       report(err, start, kParseReadLong);
       return;
     }
@@ -174,13 +174,13 @@ void launch_parse_newlines(cudaStream_t st, const char* b, uint64_t n, const uin
 
 void launch_parse_lines(cudaStream_t st, const char* b, uint64_t n, const uint64_t* nl,
                         uint64_t n_nl, uint64_t n_lines, DevRead* rd, ParseSummary* sum,
-                        unsigned long long* err) {
+                        unsigned long long* err, int max_read) {
   if (n_lines == 0) return;
   lines_to_reads<<<(unsigned)((n_lines + 255) / 256), 256, 0, st>>>((const uint8_t*)b, n, nl, n_nl,
-                                                                   n_lines, rd, sum, err);
+                                                                   n_lines, rd, sum, err, max_read);
 }
 
-int parse_error(uint32_t code, uint64_t off, std::string* msg) {
+int parse_error(uint32_t code, uint64_t off, std::string* msg, int max_read) {
   const std::string at = " at offset " + std::to_string(off);
   switch (code) {
     case kParseBadByte: *msg = "reads: byte outside 7-bit text" + at; return SWIFT_E_INPUT;
@@ -198,7 +198,9 @@ int parse_error(uint32_t code, uint64_t off, std::string* msg) {
       return SWIFT_E_INPUT;
     case kParseNameLong: *msg = "reads: read name longer than 48 characters" + at; return SWIFT_E_LIMIT;
     case kParseReadLong:
-      *msg = "reads: read longer than 199 bases (the reference's query buffer)" + at;
+      *msg = "reads: read longer than " + std::to_string(max_read) + " bases" +
+             (max_read == kReadMax ? std::string(" (the reference's query buffer)") : std::string()) +
+             at;
       return SWIFT_E_LIMIT;
     default: *msg = "reads: malformed input" + at; return SWIFT_E_INPUT;
   }

@@ -221,6 +221,30 @@ int swift_index_load(swift_ctx* ctx, const char* path, swift_index** out) {
     r.name[kNameMax - 1] = '\0';
     r.regular = fr.regular != 0;
   }
+  {  // every record inside the reference bytes and the concatenated
+     // sequence, records in file order and back to back in the sequence:
+     // the kernels index with these offsets, so a file that passes the
+     // checksum yet holds others is refused here
+    uint64_t cat_at = 0, seq_at = 0;
+    for (uint32_t i = 0; i < h.n_recs; ++i) {
+      const RefRecord& r = ix->recs[i];
+      const bool ok = r.name_off + r.name_len <= h.file_len && r.seq_off <= h.file_len &&
+                      r.seq_off >= seq_at && r.name_off < r.seq_off &&
+                      r.cat_start == cat_at && r.cat_len <= h.cat_len - cat_at &&
+                      r.cat_len <= (h.file_len - r.seq_off) && r.bpl <= h.file_len;
+      if (!ok) {
+        delete ix;
+        return fail(ctx, SWIFT_E_INPUT, "index file: a sequence record lies outside the "
+                                        "reference or out of order");
+      }
+      cat_at = r.cat_start + r.cat_len;
+      seq_at = r.seq_off;
+    }
+    if (cat_at != h.cat_len) {
+      delete ix;
+      return fail(ctx, SWIFT_E_INPUT, "index file: sequence records do not cover the sequence");
+    }
+  }
   const uint64_t nw = n_words_of(ix->cat_len);
   const uint64_t ng = (h.nb + 63) / 64;
   const size_t nr = h.n_recs;

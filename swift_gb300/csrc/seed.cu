@@ -10,19 +10,32 @@
 // any exact sort reproduces the reference; ties between clusters of the same
 // size keep the first ones in sort order.
 //
-// On-chip path: one warp per strand.  The warp hashes the strand's k-mers,
-// counts postings with a warp scan, writes 64-bit keys
-//   key = refIdx << 40 | (shift + 256) << 8 | i
-// into shared memory, sorts them (bitonic), and finds run lengths with
-// ballots.  Strands with more hits than fit on chip go to a per-strand hash
-// table in global scratch (one CTA each).
+// On-chip paths: one warp per strand.  The warp hashes the strand's k-mers
+// (lane t owns the consecutive query offsets t*M .. t*M+M-1, so hits in lane
+// order are hits in offset order), looks each up in the compact bucket
+// directory and counts postings with a warp scan.  Then
+//   - at most 32 hits (most strands): lane t fetches hit t; clusters are the
+//     lanes whose (refIdx, shift) match (__match_any_sync), the biggest size
+//     is a warp max, a cluster's first hit is its lowest lane, and the first
+//     max_hits clusters in key order come from warp minima: no sort at all;
+//   - up to 512 hits: the strand goes to a list for the sort kernel, which
+//     writes 64-bit keys  refIdx << 41 | (shift + 512) << 9 | i  into shared
+//     memory, sorts them (bitonic) and finds run lengths with ballots;
+//   - more: a per-strand hash table in global scratch (one CTA each).
+//
+// Both warp kernels also add up the strand's bytes under the sector model of
+// the seeding roofline (2-bit read, one 32-byte sector per directory lookup,
+// the 5-byte postings of each occupied bucket in whole sectors, 12 bytes per
+// hit out) into model_bytes, when it is given.
 #include "internal.h"
 
 namespace swift {
 namespace {
 
-constexpr int kSeedWarps = 8;          // warps per block, on-chip path
-constexpr int kShiftBias = 256;        // shift >= -(199 - 1) always
+constexpr int kSeedWarps = 8;          // warps per block
+constexpr int kShiftBias = 512;        // shift >= -(kSeedReadMax - 1) always
+constexpr int kFastHits = 32;          // hits of the sort-free path
+constexpr int kSortCap = 512;          // hits of the sort path
 
 __device__ __forceinline__ uint8_t fwd_code(uint8_t c) {
   uint32_t u = c & 0xDFu;
@@ -35,53 +48,35 @@ __device__ __forceinline__ uint8_t rev_code(uint8_t c) {
 }
 
 __device__ __forceinline__ uint64_t make_key(uint32_t ri, int32_t shift, int32_t i) {
-  return ((uint64_t)ri << 40) | ((uint64_t)(uint32_t)(shift + kShiftBias) << 8) | (uint32_t)i;
+  return ((uint64_t)ri << 41) | ((uint64_t)(uint32_t)(shift + kShiftBias) << 9) | (uint32_t)i;
 }
 
-// Loads the strand's 2-bit codes into smem codes[0..L).
-__device__ __forceinline__ void load_codes(const char* __restrict__ s, int L, int strand,
-                                           uint8_t* codes, int lane) {
-  for (int i = lane; i < L; i += 32) {
-    codes[i] = strand == 0 ? fwd_code((uint8_t)s[i]) : rev_code((uint8_t)s[L - 1 - i]);
-  }
-}
+// words of 16 packed 2-bit codes covering kSeedReadMax bases, plus one word
+constexpr int kPackedWords = (kSeedReadMax + 15) / 16 + 1;
+// query offsets per lane at most (contiguous ranges of M = ceil(nq / 32))
+constexpr int kM = (kSeedReadMax + 31) / 32;
 
+struct WarpSmem {
+  uint8_t codes[16 * kPackedWords];  // whole 16-code groups
+  uint32_t packed[kPackedWords];
+};
 
-// words of 16 packed 2-bit codes covering kReadMax bases, plus one zero word
-constexpr int kPackedWords = (kReadMax + 15) / 16 + 1;
-
-template <int CAP>
-__global__ void __launch_bounds__(kSeedWarps * 32, 6) seed_warp_kernel(SeedArgs a) {
-  // the sort pads n <= CAP keys to the next power of two, which must fit
-  static_assert(CAP >= 32 && (CAP & (CAP - 1)) == 0, "CAP must be a power of two");
-  __shared__ uint64_t keys_all[kSeedWarps][CAP];
-  // whole 16-code groups, so the packing below reads inside the array
-  __shared__ __align__(4) uint8_t codes_all[kSeedWarps][16 * kPackedWords];
-  __shared__ uint32_t packed_all[kSeedWarps][kPackedWords];
-  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t sid = (int64_t)blockIdx.x * kSeedWarps + wib;
-  if (sid >= 2 * a.n_reads) return;
-  const int64_t read = sid >> 1;
-  const int strand = (int)(sid & 1);
-  uint64_t* keys = keys_all[wib];
-  uint8_t* codes = codes_all[wib];
-  const DevRead rd = a.rd[read];
-  const int L = rd.len, k = a.k;
-  const int nq = (a.fixed_len > 0 ? a.fixed_len : L) - k + 1;
-  if (nq <= 0) {
-    if (lane == 0) a.nbest[sid] = 0;
-    return;
-  }
-  load_codes(a.reads + rd.seq_off, L, strand, codes, lane);
+// The strand's hits per lane: loads its codes, packs them 2 bits each (code
+// i at bits 2 (i % 16) of word i / 16, as the index packs the reference, so
+// the hash of [i, i + k) is one funnel shift, k <= 15), and looks up the
+// buckets of offsets i0 .. i0 + M - 1 (i0 = lane * M).  Returns the lane's
+// postings; beg / cnt per offset.
+__device__ __forceinline__ uint32_t strand_lookups(const SeedArgs& a, const DevRead& rd, int strand,
+                                                   int L, int nq, int M, WarpSmem& w, int lane,
+                                                   uint32_t (&beg)[kM], uint32_t (&cnt)[kM]) {
+  const char* s = a.reads + rd.seq_off;
+  for (int i = lane; i < L; i += 32)
+    w.codes[i] = strand == 0 ? fwd_code((uint8_t)s[i]) : rev_code((uint8_t)s[L - 1 - i]);
   __syncwarp();
-  // the codes 2-bit packed, code i at bits 2 (i % 16) of word i / 16, as
-  // the index packs the reference: the hash of [i, i + k) is one funnel
-  // shift (k <= 15)
-  uint32_t* packed = packed_all[wib];
   if (lane < kPackedWords) {
     uint32_t pw = 0;
     if (16 * lane < L) {
-      const uint32_t* c4 = reinterpret_cast<const uint32_t*>(codes + 16 * lane);
+      const uint32_t* c4 = reinterpret_cast<const uint32_t*>(w.codes + 16 * lane);
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         // codes past L are stale bytes: masked below
@@ -91,20 +86,19 @@ __global__ void __launch_bounds__(kSeedWarps * 32, 6) seed_warp_kernel(SeedArgs 
       const int valid = L - 16 * lane;
       if (valid < 16) pw &= (1u << (2 * valid)) - 1u;
     }
-    packed[lane] = pw;
+    w.packed[lane] = pw;
   }
   __syncwarp();
-  const uint32_t kmask = (1u << (2 * k)) - 1u;
-  // offsets i = lane + 32 m, m < 7 (199 bases at most)
-  constexpr int kM = (kReadMax + 31) / 32;
-  uint32_t beg[kM], cnt[kM];
+  const uint32_t kmask = (1u << (2 * a.k)) - 1u;
+  const int i0 = lane * M;
   uint32_t my = 0;
 #pragma unroll
   for (int m = 0; m < kM; ++m) {
-    int i = lane + 32 * m;
+    const int i = i0 + m;
     beg[m] = cnt[m] = 0;
-    if (i < nq) {
-      const uint32_t h = __funnelshift_r(packed[i >> 4], packed[(i >> 4) + 1], 2 * (i & 15)) & kmask;
+    if (m < M && i < nq) {
+      const uint32_t h =
+          __funnelshift_r(w.packed[i >> 4], w.packed[(i >> 4) + 1], 2 * (i & 15)) & kmask;
       // compact bucket directory: occupancy bits and rank, then the start
       // of occupied buckets only
       const uint4 grp = __ldg(&a.groups[h >> 6]);
@@ -118,116 +112,240 @@ __global__ void __launch_bounds__(kSeedWarps * 32, 6) seed_warp_kernel(SeedArgs 
       }
     }
   }
+  return my;
+}
+
+// Posting sectors of the lane's lookups under the roofline's sector model.
+__device__ __forceinline__ uint32_t posting_sectors(const uint32_t (&cnt)[kM]) {
+  uint32_t b = 0;
+#pragma unroll
+  for (int m = 0; m < kM; ++m) b += ((5u * cnt[m] + 31u) >> 5) << 5;
+  return b;
+}
+
+// lane 0 adds one strand's model bytes (warp-uniform arguments)
+__device__ __forceinline__ void account(const SeedArgs& a, int lane, int L, int nq,
+                                        uint32_t post_bytes, int hits_out) {
+  if (a.model_bytes && lane == 0)
+    atomicAdd(&a.model_bytes[blockIdx.x & (kSeedModelSlots - 1)],
+              (unsigned long long)((L + 3) / 4 + 32 * max(nq, 0) + post_bytes + 12 * hits_out));
+}
+
+__device__ __forceinline__ int strand_nq(const SeedArgs& a, int L) {
+  return (a.fixed_len > 0 ? a.fixed_len : L) - a.k + 1;
+}
+
+__global__ void __launch_bounds__(kSeedWarps * 32) seed_fast_kernel(SeedArgs a) {
+  __shared__ __align__(16) WarpSmem smem[kSeedWarps];
+  __shared__ uint2 info_all[kSeedWarps][kFastHits];
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t sid = (int64_t)blockIdx.x * kSeedWarps + wib;
+  if (sid >= 2 * a.n_reads) return;
+  const DevRead rd = a.rd[sid >> 1];
+  const int strand = (int)(sid & 1);
+  const int L = rd.len, nq = strand_nq(a, L);
+  if (nq <= 0) {
+    if (lane == 0) a.nbest[sid] = 0;
+    account(a, lane, L, 0, 0, 0);
+    return;
+  }
+  const int M = (nq + 31) >> 5;
+  uint32_t beg[kM], cnt[kM];
+  const uint32_t my = strand_lookups(a, rd, strand, L, nq, M, smem[wib], lane, beg, cnt);
   uint32_t incl = my;
 #pragma unroll
   for (int d = 1; d < 32; d <<= 1) {
-    uint32_t o = __shfl_up_sync(0xffffffffu, incl, d);
+    const uint32_t o = __shfl_up_sync(0xffffffffu, incl, d);
     if (lane >= d) incl += o;
   }
   const uint32_t n = __shfl_sync(0xffffffffu, incl, 31);
-  if (n == 0) {
-    if (lane == 0) a.nbest[sid] = 0;
-    return;
-  }
-  if (n > (uint32_t)CAP) {
+  if (n > (uint32_t)kFastHits) {
+    // the sort kernel (or the hash-table kernel) takes the strand
     if (lane == 0) {
-      int slot = atomicAdd(a.n_overflow, 1);
-      a.overflow_list[slot] = (int32_t)sid;
-      a.nbest[sid] = -(int32_t)n;  // hit count, for sizing the overflow table
+      if (n > (uint32_t)kSortCap) {
+        a.overflow_list[atomicAdd(a.n_overflow, 1)] = (int32_t)sid;
+        a.nbest[sid] = -(int32_t)n;  // hit count, for sizing the overflow table
+      } else {
+        a.mid_list[atomicAdd(a.n_mid, 1)] = (int32_t)sid;
+      }
     }
+    if (n > (uint32_t)kSortCap) account(a, lane, L, nq, 0, 0);  // its lookups
     return;
   }
-  uint32_t pos = incl - my;
+  const uint32_t post = __reduce_add_sync(0xffffffffu, posting_sectors(cnt));
+  // hit t of the strand is posting t - start of the lookup that starts at
+  // the last start at or before t: the starts as one bit mask, each start's
+  // (first posting - start, query offset) in shared memory
+  uint2* info = info_all[wib];
+  uint32_t smask = 0, pos = incl - my;
 #pragma unroll
   for (int m = 0; m < kM; ++m) {
-    int i = lane + 32 * m;
-    for (uint32_t j = 0; j < cnt[m]; ++j) {
-      uint2 p = __ldg(&a.postings[beg[m] + j]);
-      keys[pos++] = make_key(p.y, (int32_t)p.x - i, i);
+    if (cnt[m]) {
+      smask |= 1u << pos;
+      info[pos] = make_uint2(beg[m] - pos, (uint32_t)(lane * M + m));
+      pos += cnt[m];
     }
   }
-  uint32_t P = 32;
-  while (P < n) P <<= 1;
-  for (uint32_t i = n + lane; i < P; i += 32) keys[i] = ~0ull;
+  smask = __reduce_or_sync(0xffffffffu, smask);
   __syncwarp();
-  // bitonic sort of keys[0, P)
-  for (uint32_t size = 2; size <= P; size <<= 1) {
-    for (uint32_t stride = size >> 1, ls = __ffs(stride) - 1; stride > 0; stride >>= 1, --ls) {
-      for (uint32_t t = lane; t < P / 2; t += 32) {
-        uint32_t i = ((t >> ls) << (ls + 1)) | (t & (stride - 1));
-        uint32_t j = i + stride;
-        bool asc = (i & size) == 0;
-        uint64_t x = keys[i], y = keys[j];
-        if ((x > y) == asc) {
-          keys[i] = y;
-          keys[j] = x;
-        }
-      }
-      __syncwarp();
-    }
+  // cluster key (refIdx, shift + bias); lanes without a hit get distinct
+  // keys above every real one
+  uint64_t ck = ~0ull - (uint64_t)lane;
+  uint32_t ri = 0;
+  int32_t shift = 0, qi = 0;
+  if ((uint32_t)lane < n) {
+    const int st = 31 - __clz(smask & (0xffffffffu >> (31 - lane)));
+    const uint2 inf = info[st];
+    const uint2 p = __ldg(&a.postings[inf.x + (uint32_t)lane]);
+    ri = p.y;
+    qi = (int32_t)inf.y;
+    shift = (int32_t)p.x - qi;
+    ck = ((uint64_t)ri << 32) | (uint32_t)(shift + kShiftBias);
   }
-  // run lengths at run starts, scanning chunks back to front: the biggest
-  const uint32_t nch = (n + 31) >> 5;
-  auto starts = [&](uint32_t c) {
-    const uint32_t idx = c * 32 + lane;
-    const bool start = idx < n && (idx == 0 || (keys[idx] >> 8) != (keys[idx - 1] >> 8));
-    return __ballot_sync(0xffffffffu, start);
-  };
-  // the run start ending a run that starts at lane `lane` of a chunk whose
-  // starts are bal, if it lies in the same chunk (else 0)
-  auto next_in_chunk = [&](uint32_t c, uint32_t bal) -> uint32_t {
-    const uint32_t above = lane < 31 ? (bal >> (lane + 1)) << (lane + 1) : 0u;
-    return above ? c * 32 + __ffs(above) - 1 : 0u;
-  };
-  uint32_t next = n, biggest = 0;
-  for (int c = (int)nch - 1; c >= 0; --c) {
-    const uint32_t bal = starts(c);
-    if ((bal >> lane) & 1u) {
-      const uint32_t nx = next_in_chunk(c, bal);
-      biggest = max(biggest, (nx ? nx : next) - ((uint32_t)c * 32 + lane));
-    }
-    if (bal) next = (uint32_t)c * 32 + __ffs(bal) - 1;
-  }
-#pragma unroll
-  for (int d = 16; d > 0; d >>= 1) biggest = max(biggest, __shfl_xor_sync(0xffffffffu, biggest, d));
-  // first max_hits runs of the biggest size, front to back: a chunk's last
-  // run stays open until the next start (or the end) closes it
-  int got = 0;
+  const uint32_t same = __match_any_sync(0xffffffffu, ck);
+  const uint32_t size = (uint32_t)lane < n ? (uint32_t)__popc(same) : 0u;
+  const uint32_t biggest = __reduce_max_sync(0xffffffffu, size);
+  // a cluster's first hit in key order is its lowest lane (offset order, and
+  // two hits of one cluster never share an offset)
+  uint32_t cand = __ballot_sync(0xffffffffu, size == biggest && size > 0 &&
+                                                 (same & ((1u << lane) - 1u)) == 0u);
+  const uint32_t hi = (uint32_t)(ck >> 32), lo = (uint32_t)ck;
   int3* out = a.best + sid * a.max_hits;
-  auto emit = [&](uint32_t idx) {  // lane 0; got is warp-uniform
-    if (lane == 0) {
-      const uint64_t key = keys[idx];
-      const int32_t ri = (int32_t)(key >> 40);
-      const int32_t shift = (int32_t)((key >> 8) & 0xffffffffu) - kShiftBias;
-      const int32_t i = (int32_t)(key & 0xff);
-      out[got] = make_int3(ri, shift, shift + i);
-    }
+  int got = 0;
+  while (cand && got < a.max_hits) {  // the smallest cluster keys first
+    const bool in = (cand >> lane) & 1u;
+    const uint32_t hmin = __reduce_min_sync(0xffffffffu, in ? hi : 0xffffffffu);
+    const uint32_t lmin = __reduce_min_sync(0xffffffffu, in && hi == hmin ? lo : 0xffffffffu);
+    const uint32_t win = __ballot_sync(0xffffffffu, in && hi == hmin && lo == lmin);
+    if (lane == __ffs(win) - 1) out[got] = make_int3((int32_t)ri, shift, shift + qi);
+    cand &= ~win;
     ++got;
-  };
-  uint32_t open = ~0u;  // start of the run open at the last chunk boundary
-  for (uint32_t c = 0; c < nch && got < a.max_hits; ++c) {
-    const uint32_t bal = starts(c);
-    if (!bal) continue;
-    if (open != ~0u) {
-      if ((uint32_t)(c * 32 + __ffs(bal) - 1) - open == biggest) emit(open);
-      open = ~0u;
-    }
-    const uint32_t nx = next_in_chunk(c, bal);
-    uint32_t hb = __ballot_sync(0xffffffffu, ((bal >> lane) & 1u) && nx && nx - (c * 32 + lane) == biggest);
-    while (hb && got < a.max_hits) {
-      emit(c * 32 + __ffs(hb) - 1);
-      hb &= hb - 1;
-    }
-    open = c * 32 + 31 - __clz(bal);
   }
-  if (open != ~0u && got < a.max_hits && n - open == biggest) emit(open);
   if (lane == 0) a.nbest[sid] = got;
+  account(a, lane, L, nq, post, got);
+}
+
+// The sort path over the strands of a.mid_list (between kFastHits and
+// kSortCap hits); warps stride over the list, whose length is on the device.
+template <int CAP>
+__global__ void __launch_bounds__(kSeedWarps * 32, 6) seed_sort_kernel(SeedArgs a) {
+  // the sort pads n <= CAP keys to the next power of two, which must fit
+  static_assert(CAP >= 32 && (CAP & (CAP - 1)) == 0, "CAP must be a power of two");
+  __shared__ uint64_t keys_all[kSeedWarps][CAP];
+  __shared__ __align__(16) WarpSmem smem[kSeedWarps];
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  uint64_t* keys = keys_all[wib];
+  const int64_t n_list = *a.n_mid;
+  for (int64_t t = (int64_t)blockIdx.x * kSeedWarps + wib; t < n_list;
+       t += (int64_t)gridDim.x * kSeedWarps) {
+    const int64_t sid = a.mid_list[t];
+    const DevRead rd = a.rd[sid >> 1];
+    const int strand = (int)(sid & 1);
+    const int L = rd.len, nq = strand_nq(a, L);
+    const int M = (nq + 31) >> 5;
+    uint32_t beg[kM], cnt[kM];
+    const uint32_t my = strand_lookups(a, rd, strand, L, nq, M, smem[wib], lane, beg, cnt);
+    uint32_t incl = my;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t o = __shfl_up_sync(0xffffffffu, incl, d);
+      if (lane >= d) incl += o;
+    }
+    const uint32_t n = __shfl_sync(0xffffffffu, incl, 31);  // in (kFastHits, CAP]
+    const uint32_t post = __reduce_add_sync(0xffffffffu, posting_sectors(cnt));
+    uint32_t pos = incl - my;
+#pragma unroll
+    for (int m = 0; m < kM; ++m) {
+      const int i = lane * M + m;
+      for (uint32_t j = 0; j < cnt[m]; ++j) {
+        const uint2 p = __ldg(&a.postings[beg[m] + j]);
+        keys[pos++] = make_key(p.y, (int32_t)p.x - i, i);
+      }
+    }
+    uint32_t P = 32;
+    while (P < n) P <<= 1;
+    for (uint32_t i = n + lane; i < P; i += 32) keys[i] = ~0ull;
+    __syncwarp();
+    // bitonic sort of keys[0, P)
+    for (uint32_t size = 2; size <= P; size <<= 1) {
+      for (uint32_t stride = size >> 1, ls = __ffs(stride) - 1; stride > 0; stride >>= 1, --ls) {
+        for (uint32_t u = lane; u < P / 2; u += 32) {
+          const uint32_t i = ((u >> ls) << (ls + 1)) | (u & (stride - 1));
+          const uint32_t j = i + stride;
+          const bool asc = (i & size) == 0;
+          const uint64_t x = keys[i], y = keys[j];
+          if ((x > y) == asc) {
+            keys[i] = y;
+            keys[j] = x;
+          }
+        }
+        __syncwarp();
+      }
+    }
+    // run lengths at run starts, scanning chunks back to front: the biggest
+    const uint32_t nch = (n + 31) >> 5;
+    auto starts = [&](uint32_t c) {
+      const uint32_t idx = c * 32 + lane;
+      const bool start = idx < n && (idx == 0 || (keys[idx] >> 9) != (keys[idx - 1] >> 9));
+      return __ballot_sync(0xffffffffu, start);
+    };
+    // the run start ending a run that starts at lane `lane` of a chunk whose
+    // starts are bal, if it lies in the same chunk (else 0)
+    auto next_in_chunk = [&](uint32_t c, uint32_t bal) -> uint32_t {
+      const uint32_t above = lane < 31 ? (bal >> (lane + 1)) << (lane + 1) : 0u;
+      return above ? c * 32 + __ffs(above) - 1 : 0u;
+    };
+    uint32_t next = n, biggest = 0;
+    for (int c = (int)nch - 1; c >= 0; --c) {
+      const uint32_t bal = starts(c);
+      if ((bal >> lane) & 1u) {
+        const uint32_t nx = next_in_chunk(c, bal);
+        biggest = max(biggest, (nx ? nx : next) - ((uint32_t)c * 32 + lane));
+      }
+      if (bal) next = (uint32_t)c * 32 + __ffs(bal) - 1;
+    }
+    biggest = __reduce_max_sync(0xffffffffu, biggest);
+    // first max_hits runs of the biggest size, front to back: a chunk's last
+    // run stays open until the next start (or the end) closes it
+    int got = 0;
+    int3* out = a.best + sid * a.max_hits;
+    auto emit = [&](uint32_t idx) {  // lane 0; got is warp-uniform
+      if (lane == 0) {
+        const uint64_t key = keys[idx];
+        const int32_t ri = (int32_t)(key >> 41);
+        const int32_t shift = (int32_t)((key >> 9) & 0xffffffffu) - kShiftBias;
+        const int32_t i = (int32_t)(key & 0x1ff);
+        out[got] = make_int3(ri, shift, shift + i);
+      }
+      ++got;
+    };
+    uint32_t open = ~0u;  // start of the run open at the last chunk boundary
+    for (uint32_t c = 0; c < nch && got < a.max_hits; ++c) {
+      const uint32_t bal = starts(c);
+      if (!bal) continue;
+      if (open != ~0u) {
+        if ((uint32_t)(c * 32 + __ffs(bal) - 1) - open == biggest) emit(open);
+        open = ~0u;
+      }
+      const uint32_t nx = next_in_chunk(c, bal);
+      uint32_t hb = __ballot_sync(0xffffffffu, ((bal >> lane) & 1u) && nx && nx - (c * 32 + lane) == biggest);
+      while (hb && got < a.max_hits) {
+        emit(c * 32 + __ffs(hb) - 1);
+        hb &= hb - 1;
+      }
+      open = c * 32 + 31 - __clz(bal);
+    }
+    if (open != ~0u && got < a.max_hits && n - open == biggest) emit(open);
+    if (lane == 0) a.nbest[sid] = got;
+    account(a, lane, L, nq, post, got);
+    __syncwarp();  // keys are rewritten by the next strand
+  }
 }
 
 // ---------------------------------------------------------------------------
 // Overflow path: one CTA per strand, open-addressing table over cluster keys
 // (refIdx, shift) with counts and the smallest query offset (kept as
-// 255 - offset under atomicMax so that the table starts all zero).
+// 1023 - offset under atomicMax so that the table starts all zero).
 
 constexpr int kOvThreads = 512;
 
@@ -241,7 +359,7 @@ __device__ __forceinline__ uint32_t mix(uint64_t x) {
 __global__ void __launch_bounds__(kOvThreads) seed_overflow_kernel(SeedArgs a,
                                                                    const uint64_t* tab_off,
                                                                    const uint32_t* tab_size) {
-  __shared__ uint8_t codes[kReadMax + 1];
+  __shared__ uint8_t codes[kSeedReadMax + 1];
   __shared__ uint64_t red[kOvThreads / 32];
   const int64_t sid = a.overflow_list[blockIdx.x];
   const int64_t read = sid >> 1;
@@ -264,14 +382,14 @@ __global__ void __launch_bounds__(kOvThreads) seed_overflow_kernel(SeedArgs a,
     uint32_t b = a.offsets[h], e = a.offsets[h + 1];
     for (uint32_t j = b + lane; j < e; j += 32) {
       uint2 p = a.postings[j];
-      uint64_t ck = make_key(p.y, (int32_t)p.x - i, 0) >> 8;  // nonzero
+      uint64_t ck = make_key(p.y, (int32_t)p.x - i, 0) >> 9;  // nonzero
       uint32_t slot = mix(ck) & (S - 1);
       for (uint32_t probe = 0; probe < S; ++probe) {
         unsigned long long old = atomicCAS((unsigned long long*)&tk[slot], 0ull,
                                            (unsigned long long)ck);
         if (old == 0ull || old == ck) {
           atomicAdd(&tc[slot], 1u);
-          atomicMax(&ti[slot], 255u - (uint32_t)i);  // zero-initialised table
+          atomicMax(&ti[slot], 1023u - (uint32_t)i);  // zero-initialised table
           break;
         }
         slot = (slot + 1) & (S - 1);
@@ -313,7 +431,7 @@ __global__ void __launch_bounds__(kOvThreads) seed_overflow_kernel(SeedArgs a,
       while (tk[slot] != mn) slot = (slot + 1) & (S - 1);
       int32_t ri = (int32_t)(mn >> 32);
       int32_t shift = (int32_t)(mn & 0xffffffffu) - kShiftBias;
-      out[got] = make_int3(ri, shift, shift + (int32_t)(255u - ti[slot]));
+      out[got] = make_int3(ri, shift, shift + (int32_t)(1023u - ti[slot]));
     }
     ++got;
     last = mn;
@@ -323,16 +441,22 @@ __global__ void __launch_bounds__(kOvThreads) seed_overflow_kernel(SeedArgs a,
 
 }  // namespace
 
-constexpr int kSeedCap = 512;  // 8 warps x 512 x 8 B = 32 KB of static shared memory
-
 void launch_seed(cudaStream_t st, const SeedArgs& a) {
-  int64_t strands = 2 * a.n_reads;
+  const int64_t strands = 2 * a.n_reads;
   if (strands == 0) return;
-  unsigned grid = (unsigned)((strands + kSeedWarps - 1) / kSeedWarps);
-  seed_warp_kernel<kSeedCap><<<grid, kSeedWarps * 32, 0, st>>>(a);
+  const unsigned grid = (unsigned)((strands + kSeedWarps - 1) / kSeedWarps);
+  seed_fast_kernel<<<grid, kSeedWarps * 32, 0, st>>>(a);
+  // the sort path over the listed strands: a grid of a few waves strides
+  // over the list (its length is on the device)
+  int dev = 0, sms = 0;
+  int64_t blocks = (strands + kSeedWarps - 1) / kSeedWarps;
+  if (cudaGetDevice(&dev) == cudaSuccess &&
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && sms > 0)
+    blocks = std::min<int64_t>(blocks, (int64_t)sms * 6 * 4);
+  seed_sort_kernel<kSortCap><<<(unsigned)blocks, kSeedWarps * 32, 0, st>>>(a);
 }
 
-int seed_smem_cap() { return kSeedCap; }
+int seed_smem_cap() { return kSortCap; }
 
 void launch_seed_overflow(cudaStream_t st, const SeedArgs& a, int n_overflow,
                           const uint64_t* tab_off, const uint32_t* tab_size) {

@@ -41,13 +41,15 @@ template <>
 struct DirWord<4> { using T = uint8_t; };
 template <>
 struct DirWord<8> { using T = uint16_t; };
+template <>
+struct DirWord<10> { using T = uint32_t; };
 
 // One pair on one warp; base is the warp's shared-memory slice.
 template <int RPL>
 __device__ __forceinline__ void generic_pair(const SwArgs& a, int64_t pair, uint8_t* base,
                                              int lane) {
   using DW = typename DirWord<RPL>::T;
-  const int Q = a.Q, R = a.R;
+  const int Q = a.q_len ? a.q_len[pair] : a.Q, R = a.R;
   uint8_t* wsh = base;                                  // R bytes (rounded to 16)
   DW* dirs = reinterpret_cast<DW*>(base + ((R + 15) & ~15));  // (R+1) x 32
   const char* qg = a.q + pair * a.q_stride;
@@ -183,15 +185,15 @@ __device__ __forceinline__ void generic_pair(const SwArgs& a, int64_t pair, uint
 }
 
 // Warps stride over the pairs (the list's length is known on the device
-// only, so the grid is capped rather than sized by it).
-template <int RPL>
-__global__ void __launch_bounds__(kSwWarps * 32) sw_generic_kernel(SwArgs a, int per_warp_bytes) {
+// only, so the grid is capped rather than sized by it).  W warps per block:
+// fewer for long windows, whose direction words fill more shared memory.
+template <int RPL, int W>
+__global__ void __launch_bounds__(W * 32) sw_generic_kernel(SwArgs a, int per_warp_bytes) {
   extern __shared__ __align__(16) uint8_t smem[];
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   uint8_t* base = smem + (size_t)wib * per_warp_bytes;
   const int64_t n = a.list ? (int64_t)*a.count : a.n;
-  for (int64_t i = (int64_t)blockIdx.x * kSwWarps + wib; i < n;
-       i += (int64_t)gridDim.x * kSwWarps) {
+  for (int64_t i = (int64_t)blockIdx.x * W + wib; i < n; i += (int64_t)gridDim.x * W) {
     generic_pair<RPL>(a, a.list ? (int64_t)a.list[i] : i, base, lane);
     __syncwarp();
   }
@@ -199,33 +201,48 @@ __global__ void __launch_bounds__(kSwWarps * 32) sw_generic_kernel(SwArgs a, int
 
 template <int RPL>
 int per_warp_bytes(int R) {
-  return ((R + 15) & ~15) + (R + 1) * 32 * (RPL / 4);
+  return ((R + 15) & ~15) + (R + 1) * 32 * (int)sizeof(typename DirWord<RPL>::T);
+}
+
+constexpr size_t kGenericSmemMax = 200 * 1024;
+
+template <int RPL, int W>
+int launch_generic_w(cudaStream_t st, const SwArgs& a, int pw) {
+  const size_t smem = (size_t)pw * W;
+  // the opt-in above 48 KB is a per-device function attribute: set it on
+  // every launch (cheap), so a second device or context needs no state here
+  if (smem > 48 * 1024 &&
+      cudaFuncSetAttribute(sw_generic_kernel<RPL, W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem) != cudaSuccess)
+    return SWIFT_E_CUDA;
+  int64_t blocks = (a.n + W - 1) / W;
+  if (a.list) {  // the list's length is on the device: a few waves stride over it
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && sms > 0)
+      blocks = std::min<int64_t>(blocks, (int64_t)sms * 16 * 4 / W);
+  }
+  sw_generic_kernel<RPL, W><<<(unsigned)blocks, W * 32, smem, st>>>(a, pw);
+  return SWIFT_OK;
 }
 
 template <int RPL>
 int launch_generic(cudaStream_t st, const SwArgs& a, std::string* err) {
   int pw = per_warp_bytes<RPL>(a.R);
   pw = (pw + 15) & ~15;
-  size_t smem = (size_t)pw * kSwWarps;
-  static bool configured = false;
-  if (!configured) {
-    cudaFuncSetAttribute(sw_generic_kernel<RPL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         200 * 1024);
-    configured = true;
-  }
-  if (smem > 200 * 1024) {
+  int rc;
+  if ((size_t)pw * kSwWarps <= kGenericSmemMax)
+    rc = launch_generic_w<RPL, kSwWarps>(st, a, pw);
+  else if ((size_t)pw * 2 <= kGenericSmemMax)
+    rc = launch_generic_w<RPL, 2>(st, a, pw);
+  else if ((size_t)pw <= kGenericSmemMax)
+    rc = launch_generic_w<RPL, 1>(st, a, pw);
+  else {
     *err = "window too long for the on-chip traceback";
     return SWIFT_E_LIMIT;
   }
-  int64_t blocks = (a.n + kSwWarps - 1) / kSwWarps;
-  if (a.list) {  // the list's length is on the device: a few waves stride over it
-    int dev = 0, sms = 0;
-    if (cudaGetDevice(&dev) == cudaSuccess &&
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && sms > 0)
-      blocks = std::min<int64_t>(blocks, (int64_t)sms * 16);
-  }
-  sw_generic_kernel<RPL><<<(unsigned)blocks, kSwWarps * 32, smem, st>>>(a, pw);
-  return SWIFT_OK;
+  if (rc != SWIFT_OK) *err = "generic kernel: shared-memory opt-in failed";
+  return rc;
 }
 
 }  // namespace
@@ -263,11 +280,12 @@ int static_sw_scratch(int device, DevAln** out, std::string* err) {
 int launch_sw(cudaStream_t st, const SwArgs& a, std::string* err) {
   if (a.n <= 0) return SWIFT_OK;
   if (a.Q < 1 || a.Q > kMaxQ || a.R < 1 || a.R > kMaxR) {
-    *err = "Smith-Waterman dimensions outside 1..256 x 1..1024";
+    *err = "Smith-Waterman dimensions outside 1..320 x 1..1024";
     return SWIFT_E_LIMIT;
   }
   if (a.Q <= 128) return launch_generic<4>(st, a, err);
-  return launch_generic<8>(st, a, err);
+  if (a.Q <= 256) return launch_generic<8>(st, a, err);
+  return launch_generic<10>(st, a, err);
 }
 
 }  // namespace swift

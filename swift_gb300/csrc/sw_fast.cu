@@ -115,9 +115,11 @@ __device__ __forceinline__ void packed_item(const FastArgs& a, const int64_t war
   const int32_t p0 = has0 ? list[base] : list[nlist - 1];
   const int32_t p1 = has1 ? list[base + 1] : p0;
   const int Q0 = VAR ? a.q_len[p0] : a.Q, Q1 = VAR ? a.q_len[p1] : a.Q;
-  const int R0 = VAR ? a.r_len[p0] : a.R, R1 = VAR ? a.r_len[p1] : a.R;
+  // per-pair windows when r_len is given, else every window is a.R long
+  const bool var_r = VAR && a.r_len != nullptr;
+  const int R0 = var_r ? a.r_len[p0] : a.R, R1 = var_r ? a.r_len[p1] : a.R;
   // columns the warp sweeps
-  const int R = VAR ? (int)__reduce_max_sync(0xffffffffu, (unsigned)max(R0, R1)) : a.R;
+  const int R = var_r ? (int)__reduce_max_sync(0xffffffffu, (unsigned)max(R0, R1)) : a.R;
   const char* q0 = a.q + (int64_t)p0 * a.q_stride;
   const char* q1 = a.q + (int64_t)p1 * a.q_stride;
   const char* w0 = a.w + (int64_t)p0 * a.w_stride;
@@ -176,7 +178,7 @@ __device__ __forceinline__ void packed_item(const FastArgs& a, const int64_t war
     if (kFull || (j >= 1 && j <= R)) {
       const uint32_t ws = wsel[j];
       // VAR: halves whose window ends before column j
-      const uint32_t cm = VAR ? ((j <= R0 ? 0x0000FFFFu : 0u) | (j <= R1 ? 0xFFFF0000u : 0u)) : ~0u;
+      const uint32_t cm = var_r ? ((j <= R0 ? 0x0000FFFFu : 0u) | (j <= R1 ? 0xFFFF0000u : 0u)) : ~0u;
       uint32_t dg = diag;
       uint32_t hpair = 0;  // score pass: even row waiting for its odd partner
 #pragma unroll
@@ -242,6 +244,7 @@ __device__ __forceinline__ void packed_item(const FastArgs& a, const int64_t war
   // steps in blocks of 4: the trace pass keeps a block's direction words in
   // registers and writes each word index as one 16-byte store
   uint32_t hist[TRACE ? 4 : 1][kNW];
+  int s_end = steps;  // wavefront steps the warp ran
   for (int s0 = 0; s0 < steps; s0 += 4) {
     // steps s0..s0+3 have 1 <= j <= R on every lane when s0 >= G - 1 and
     // s0 + 3 <= R - 1 (then also s0 + 3 < steps)
@@ -292,8 +295,20 @@ __device__ __forceinline__ void packed_item(const FastArgs& a, const int64_t war
       const int s0v = v0 > B ? (int)((v0 - B) >> 4) : 0, s1v = v1 > B ? (int)((v1 - B) >> 4) : 0;
       const bool done0 = !has0 || (int)a.suf[(int64_t)p0 * kSufBlocks + m] < s0v;
       const bool done1 = !has1 || (int)a.suf[(int64_t)p1 * kSufBlocks + m] < s1v;
-      if (__all_sync(0xffffffffu, done0 && done1)) break;
+      if (__all_sync(0xffffffffu, done0 && done1)) {
+        s_end = s + 1;
+        break;
+      }
     }
+  }
+  if (a.cells_done) {
+    // cells of the warp's pairs inside the columns every lane finished
+    const int cols = min(s_end - (G - 1), R);
+    const uint32_t c = sl != 0 ? 0u
+                               : (has0 ? (uint32_t)(min(cols, R0) * Q0) : 0u) +
+                                     (has1 ? (uint32_t)(min(cols, R1) * Q1) : 0u);
+    const uint32_t warp_cells = __reduce_add_sync(0xffffffffu, c);
+    if (lane == 0 && warp_cells) atomicAdd(a.cells_done, (unsigned long long)warp_cells);
   }
   flush_window();
   if (!TRACE) {
@@ -383,6 +398,8 @@ __global__ void __launch_bounds__(kBdWarps * 32) sw_bound_kernel(FastArgs a) {
   const bool has0 = base < nlist, has1 = base + 1 < nlist;
   const int32_t p0 = has0 ? list[base] : list[nlist - 1];
   const int32_t p1 = has1 ? list[base + 1] : p0;
+  // each pair's query length (rows past it are all-mismatch rows)
+  const int Q0 = a.q_len ? a.q_len[p0] : Q, Q1 = a.q_len ? a.q_len[p1] : Q;
   const char* q0 = a.q + (int64_t)p0 * a.q_stride;
   const char* q1 = a.q + (int64_t)p1 * a.q_stride;
   const char* w0 = a.w + (int64_t)p0 * a.w_stride;
@@ -405,13 +422,8 @@ __global__ void __launch_bounds__(kBdWarps * 32) sw_bound_kernel(FastArgs a) {
 #pragma unroll
   for (int k = 0; k < RPL; ++k) {
     const int i = sl * RPL + k;
-    if (i < Q) {
-      const uint32_t c0 = base_class((uint8_t)q0[i]), c1 = base_class((uint8_t)q1[i]);
-      prof0[k] = all_x ^ ((sm ^ sx) << (8 * c0));
-      prof1[k] = all_x ^ ((sm ^ sx) << (8 * c1));
-    } else {
-      prof0[k] = prof1[k] = all_x;
-    }
+    prof0[k] = i < Q0 ? all_x ^ ((sm ^ sx) << (8 * base_class((uint8_t)q0[i]))) : all_x;
+    prof1[k] = i < Q1 ? all_x ^ ((sm ^ sx) << (8 * base_class((uint8_t)q1[i]))) : all_x;
     h[k] = 0;  // H[i][0] = 0
   }
   const uint32_t not_first = sl == 0 ? 0u : 1u;  // row 0 above lane 0: H = 0
@@ -642,7 +654,7 @@ struct Shape {
   int G, RPL;
 };
 
-// lanes per group and rows per lane for a query length (Q <= 256)
+// lanes per group and rows per lane for a query length (Q <= 320)
 Shape shape_for(int Q) {
   if (Q <= 32) return {8, 4};
   if (Q <= 64) return {8, 8};
@@ -650,6 +662,7 @@ Shape shape_for(int Q) {
   if (Q <= 128) return {8, 16};
   if (Q <= 208) return {16, 13};
   if (Q <= 256) return {16, 16};
+  if (Q <= 320) return {32, 10};
   return {0, 0};
 }
 
@@ -677,6 +690,7 @@ int launch_shape(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {
   SWIFT_PK(8, 16)
   SWIFT_PK(16, 13)
   SWIFT_PK(16, 16)
+  SWIFT_PK(32, 10)
 #undef SWIFT_PK
   return 0;
 }
@@ -691,6 +705,7 @@ Shape bound_shape_for(int Q) {
   if (Q <= 128) return {4, 32};
   if (Q <= 200) return {8, 25};
   if (Q <= 256) return {8, 32};
+  if (Q <= 320) return {16, 20};
   return {0, 0};
 }
 
@@ -718,6 +733,7 @@ int launch_bound(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {
   SWIFT_BD(4, 32)
   SWIFT_BD(8, 25)
   SWIFT_BD(8, 32)
+  SWIFT_BD(16, 20)
 #undef SWIFT_BD
   return 0;
 }
@@ -737,6 +753,7 @@ int launch_walk(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {
   SWIFT_WK(8, 16)
   SWIFT_WK(16, 13)
   SWIFT_WK(16, 16)
+  SWIFT_WK(32, 10)
 #undef SWIFT_WK
   return 0;
 }
@@ -763,7 +780,8 @@ int64_t trace_scratch_words(int Q, int R, int64_t pairs) {
 }
 
 int launch_sw_score(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {
-  return launch_shape<false, false>(st, a, max_pairs);
+  return a.q_len ? launch_shape<false, true>(st, a, max_pairs)
+                 : launch_shape<false, false>(st, a, max_pairs);
 }
 
 int launch_sw_bound(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {

@@ -57,6 +57,24 @@ __device__ __forceinline__ void add_words<4>(const uint32_t* v, const uint32_t* 
       : "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(u[0]), "r"(u[1]), "r"(u[2]), "r"(u[3]));
 }
 template <>
+__device__ __forceinline__ void add_words<10>(const uint32_t* v, const uint32_t* u, uint32_t* s) {
+  asm("add.cc.u32 %0, %10, %20;\n\t"
+      "addc.cc.u32 %1, %11, %21;\n\t"
+      "addc.cc.u32 %2, %12, %22;\n\t"
+      "addc.cc.u32 %3, %13, %23;\n\t"
+      "addc.cc.u32 %4, %14, %24;\n\t"
+      "addc.cc.u32 %5, %15, %25;\n\t"
+      "addc.cc.u32 %6, %16, %26;\n\t"
+      "addc.cc.u32 %7, %17, %27;\n\t"
+      "addc.cc.u32 %8, %18, %28;\n\t"
+      "addc.u32 %9, %19, %29;"
+      : "=r"(s[0]), "=r"(s[1]), "=r"(s[2]), "=r"(s[3]), "=r"(s[4]), "=r"(s[5]), "=r"(s[6]),
+        "=r"(s[7]), "=r"(s[8]), "=r"(s[9])
+      : "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]),
+        "r"(v[8]), "r"(v[9]), "r"(u[0]), "r"(u[1]), "r"(u[2]), "r"(u[3]), "r"(u[4]), "r"(u[5]),
+        "r"(u[6]), "r"(u[7]), "r"(u[8]), "r"(u[9]));
+}
+template <>
 __device__ __forceinline__ void add_words<8>(const uint32_t* v, const uint32_t* u, uint32_t* s) {
   asm("add.cc.u32 %0, %8, %16;\n\t"
       "addc.cc.u32 %1, %9, %17;\n\t"
@@ -72,7 +90,8 @@ __device__ __forceinline__ void add_words<8>(const uint32_t* v, const uint32_t* 
         "r"(u[0]), "r"(u[1]), "r"(u[2]), "r"(u[3]), "r"(u[4]), "r"(u[5]), "r"(u[6]), "r"(u[7]));
 }
 
-// NW 32-bit words hold the query: Q <= 32 * NW
+// NW 32-bit words hold the query: Q <= 32 * NW (a.Q, the launch's longest;
+// a.q_len, when given, each pair's own)
 template <int NW>
 __global__ void __launch_bounds__(kLcsThreads) sw_lcs_kernel(FastArgs a) {
   __shared__ uint32_t pm_all[4 * NW * kLcsThreads];
@@ -80,7 +99,7 @@ __global__ void __launch_bounds__(kLcsThreads) sw_lcs_kernel(FastArgs a) {
   const int64_t t = (int64_t)blockIdx.x * kLcsThreads + threadIdx.x;
   if (t >= nlist) return;  // no block-wide synchronisation below
   const int32_t p = a.list[a.list_offset + t];
-  const int Q = a.Q, R = a.R;
+  const int Q = a.q_len ? a.q_len[p] : a.Q, R = a.R;
   // query base classes as two bit planes; positions >= Q match nothing
   const uint32_t* q4 = reinterpret_cast<const uint32_t*>(a.q + (int64_t)p * a.q_stride);
   uint32_t b0[NW], b1[NW], qmask[NW];
@@ -164,6 +183,7 @@ int launch_sw_lcs(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {
   SWIFT_LCS(2)
   SWIFT_LCS(4)
   SWIFT_LCS(8)
+  SWIFT_LCS(10)
 #undef SWIFT_LCS
   return 0;
 }

@@ -176,7 +176,35 @@ def test_sw_scoring_parameters(ctx, oracle):
 def test_sw_zero_pairs_and_limits(ctx, sg):
     assert ctx.sw_batch([], [], 10, 10) == []
     with pytest.raises(sg.SwiftError):
-        ctx.sw_batch([b"A" * 10], [b"A" * 10], 300, 10)
+        ctx.sw_batch([b"A" * 10], [b"A" * 10], 400, 10)
+    # scores must be whole numbers (float in alignSequences, atoi in the CLI)
+    with pytest.raises(sg.SwiftError) as e:
+        ctx.sw_batch([b"ACGT"], [b"ACGT"], 4, 4, match=1.5)
+    assert e.value.code == -1
+
+
+@pytest.mark.parametrize("Q,R", [(256, 1024), (129, 787), (128, 1024), (320, 1024), (257, 300)])
+def test_sw_largest_shapes(ctx, oracle, Q, R):
+    # the documented maximum shapes, whose direction words need fewer warps
+    # per block to fit shared memory
+    qs, ws = random_pairs(31 + Q + R, 24, Q, R)
+    got = ctx.sw_batch(qs, ws, Q, R)
+    for i, (q, w) in enumerate(zip(qs, ws)):
+        want = oracle.sw(q, w, Q, R)
+        for key in ("score", "start", "end", "len", "qcons", "rcons"):
+            assert got[i][key] == want[key], (i, key)
+
+
+def test_sw_foreign_device_pointer(ctx, sg):
+    # a device buffer of another GPU than the context's is refused
+    torch = pytest.importorskip("torch")
+    if torch.cuda.device_count() < 2:
+        pytest.skip("one GPU: the check against the context's device cannot be exercised")
+    other = torch.zeros(1 << 12, dtype=torch.uint8, device="cuda:1")
+    p = other.data_ptr()
+    assert sg.lib().swift_sw_batch(ctx._h, p, p, 4, 4, 1, 2, -1, -10, -1, *([p] * 6)) == -1
+    assert sg.lib().swift_sw_batch_noalloc(ctx._h, p, p, 4, 4, 1, 2, -1, -10, -1,
+                                           *([p] * 6)) == -1
 
 
 # ---------------------------------------------------------------------------

@@ -90,3 +90,47 @@ def test_load_refuses_bad_files(sg):
         with pytest.raises(sg.SwiftError) as e:
             sg.Index.load(ctx, os.path.join(d, "missing.swidx"))
         assert e.value.code == -1
+
+
+def _rechecksum(blob: bytearray):
+    """Recomputes the payload checksum of an index file in place (the
+    word-wise FNV-1a-style mix of persist.cpp), so that a patched payload
+    passes the checksum and only the content checks remain."""
+    import numpy as np
+    payload = bytes(blob[96:])
+    h, P, M = 1469598103934665603, 1099511628211, (1 << 64) - 1
+    n8 = len(payload) // 8
+    for w in np.frombuffer(payload[:8 * n8], dtype="<u8").tolist():
+        h = ((h ^ w) * P) & M
+    for b in payload[8 * n8:]:
+        h = ((h ^ b) * P) & M
+    blob[88:96] = h.to_bytes(8, "little")
+
+
+def test_load_refuses_records_outside_the_reference(sg):
+    # a file whose checksum holds but whose sequence records point outside
+    # the reference would steer the kernels' reads out of bounds
+    ref, _ = case(seed=11)
+    ctx = sg.Context(0)
+    ix = ctx.index(ref, 8, 1000)  # k = 8 keeps the file small
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "i.swidx")
+        ix.save(path)
+        blob = bytearray(open(path, "rb").read())
+        ok = bytearray(blob)
+        _rechecksum(ok)
+        assert ok == blob  # the restated checksum is the file's own
+        p = os.path.join(d, "ok.swidx")
+        open(p, "wb").write(bytes(ok))
+        sg.Index.load(ctx, p).close()
+        rec1 = 96 + 96  # second record
+        for name, field, value in [("cat_start", 24, 1 << 40), ("cat_len", 32, 1 << 40),
+                                   ("seq_off", 8, 1 << 50), ("name_off", 0, 1 << 50)]:
+            bad = bytearray(blob)
+            bad[rec1 + field:rec1 + field + 8] = value.to_bytes(8, "little")
+            _rechecksum(bad)
+            p = os.path.join(d, name)
+            open(p, "wb").write(bytes(bad))
+            with pytest.raises(sg.SwiftError) as e:
+                sg.Index.load(ctx, p)
+            assert e.value.code == -2, name

@@ -306,3 +306,30 @@ def test_paired_pipeline(oracle, seed, case, dm, fmt):
     assert got == recs
     assert oracle.align_paired(ref, r1, r2, p) == out
     assert len(recs) > 0 and len(out) > 0
+
+
+def test_cpu_sw_cost_against_the_reference_routine(oracle, capsys):
+    # the CPU baseline times the port's Smith-Waterman; this ties its cost to
+    # the reference's own CPU routine (smithWaterman_cpu,
+    # src/smithWaterman.cu:44-335) on the same 100 x 300 pairs, one thread
+    # each, and checks they agree on score and end
+    import time
+    rng = random.Random(9)
+    pairs = []
+    for _ in range(60):
+        w = rand_seq(rng, 300)
+        pairs.append((mutate(rng, w[80:190])[:100].ljust(100, b"A"), w))
+    t0 = time.perf_counter()
+    ref = [R.sw_cpu(q, w) for q, w in pairs]
+    t_ref = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    port = [oracle.sw(q, w) for q, w in pairs]
+    t_port = time.perf_counter() - t0
+    for a, b in zip(ref, port):
+        assert a["score"] == b["score"] and a["end"] == b["end"]
+    cells = 60 * 100 * 300
+    with capsys.disabled():
+        print(f"\nCPU Smith-Waterman, one thread: reference smithWaterman_cpu "
+              f"{cells / t_ref / 1e6:.0f} Mcells/s, port {cells / t_port / 1e6:.0f} Mcells/s "
+              f"(port / reference = {t_ref / t_port:.2f})")
+    assert t_ref > 0 and t_port > 0

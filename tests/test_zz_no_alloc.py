@@ -1,4 +1,5 @@
-"""swift_sw_batch_noalloc (static scratch, no allocation) against swift_sw_batch.
+"""swift_sw_batch_noalloc (static scratch, no allocation) against swift_sw_batch
+and against the oracle.
 
 Collected last on purpose: it must pass both in a fresh process and after
 every other test has run on the same device.  Both entry points are called
@@ -105,6 +106,25 @@ def test_noalloc_matches_sw_batch_two_calls(sg, ctx):
         assert (want["score"] > 0).mean() > 0.9  # the inputs do align
 
 
+def test_noalloc_matches_oracle(sg, ctx, oracle):
+    # the two entry points share the generic kernel, so the comparison above
+    # alone could not catch an error in it: a few hundred pairs of each call
+    # against the CPU restatement as well, two calls in a row
+    pytest.importorskip("torch")
+    for n, Q, R, params, seed in [(400, 100, 300, (2, -1, -10, -1), 21),
+                                  (300, 150, 260, (3, -2, -6, -2), 22)]:
+        q, w = make_pairs(n, Q, R, seed)
+        got = run_noalloc(sg, ctx, q, w, Q, R, n, params)
+        m, x, o, e = params
+        for i in range(n):
+            want = oracle.sw(bytes(q[i, :Q]), bytes(w[i, :R]), Q, R, m, x, o, e)
+            L = want["len"]
+            assert (float(got["score"][i]), int(got["start"][i]), int(got["end"][i]),
+                    int(got["len"][i])) == (want["score"], want["start"], want["end"], L), i
+            assert bytes(got["qcons"][i, :max(L, 0)]) == want["qcons"], i
+            assert bytes(got["rcons"][i, :max(L, 0)]) == want["rcons"], i
+
+
 def test_noalloc_largest_batch(sg, ctx):
     pytest.importorskip("torch")
     n, Q, R, params = MAX_PAIRS, 40, 60, (2, -1, -10, -1)
@@ -130,8 +150,12 @@ def test_noalloc_rejects(sg, ctx):
                                     p, p, p, p, p, p)
     assert rc == -1
     # sizes beyond the kernel's limits
-    rc = lib.swift_sw_batch_noalloc(ctx._h, p, p, 300, R, 1, 2, -1, -10, -1, p, p, p, p, p, p)
+    rc = lib.swift_sw_batch_noalloc(ctx._h, p, p, 400, R, 1, 2, -1, -10, -1, p, p, p, p, p, p)
     assert rc == -5
+    # scores that are not whole numbers (alignSequences takes floats; the
+    # reference parses them with atoi)
+    rc = lib.swift_sw_batch_noalloc(ctx._h, p, p, Q, R, 1, 2.5, -1, -10, -1, p, p, p, p, p, p)
+    assert rc == -1
     # an empty batch is a no-op
     rc = lib.swift_sw_batch_noalloc(ctx._h, p, p, Q, R, 0, 2, -1, -10, -1, p, p, p, p, p, p)
     assert rc == 0
