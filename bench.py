@@ -361,7 +361,7 @@ def bench_batched(args, rank, world, local):
     return 0
 
 
-SERVE_MAX_READ = 199  # read lengths of the serving workload: U[50, SERVE_MAX_READ]
+SERVE_MAX_READ = 300  # read lengths of the serving workload: U[50, SERVE_MAX_READ]
 
 
 def serving_pool(seqs, pool_size: int, seed: int, max_len: int = SERVE_MAX_READ):
@@ -385,7 +385,7 @@ def serving_pool(seqs, pool_size: int, seed: int, max_len: int = SERVE_MAX_READ)
 
 
 def serving_run(idx, device, seqs, pool_size=120, per_load=200, loads=(0.8,), seed=3,
-                workers=4):
+                workers=2):
     """Serving on a resident index: the saturation throughput (every request
     of the pool queued at once), then Poisson arrivals at fractions of it,
     with per-request latency from submission to result (p50 / p99)."""
@@ -393,7 +393,8 @@ def serving_run(idx, device, seqs, pool_size=120, per_load=200, loads=(0.8,), se
     import swift_gb300 as sg
     rng = np.random.default_rng(seed + 7)
     pool = serving_pool(seqs, pool_size, seed)
-    srv = sg.Server(idx, device=device, workers=workers)
+    srv = sg.Server(idx, device=device, workers=workers,
+                    params=sg.default_params(max_read_len=SERVE_MAX_READ))
     try:
         for n, r in pool[:8]:  # warm-up
             srv.wait(srv.submit(r))

@@ -38,6 +38,7 @@ extern "C" {
 #define SWIFT_E_NOMEM (-4)   /* device or host allocation failed          */
 #define SWIFT_E_LIMIT (-5)   /* size beyond a documented maximum          */
 #define SWIFT_E_DEVICE (-6)  /* a kernel reported an internal error       */
+#define SWIFT_E_CANCELLED (-7) /* serving: the request was cancelled       */
 
 typedef struct swift_ctx swift_ctx;
 typedef struct swift_index swift_index;
@@ -230,7 +231,21 @@ typedef struct {
   int64_t segments;        /* groups of one shape, one launch set each        */
   int64_t generic_pairs;   /* pairs on the int32 kernel                       */
   int64_t launches;        /* kernels this library launched                   */
+  /* the packed shape (lanes, rows per lane) each query class ran with
+   * (classes: queries up to 32, 64, 104, 128, 208, 256, 320 bases; 0: the
+   * class had no packed pairs), the last window bin's; and the device time
+   * this call spent timing candidate shapes                                 */
+  int32_t shape_lanes[8], shape_rows[8];
+  double tune_ms;
 } swift_pairs_stats;
+
+/* Packed-shape choice of swift_sw_pairs: 1 (default) times the candidate
+ * (lanes, rows per lane) shapes of each query class and window bin on a
+ * sample of the call's pairs the first time the context meets them, and
+ * keeps the fastest for the context; 0 uses the fixed default shapes;
+ * k >= 2 runs the (k - 2)-th candidate of every class (the default when it
+ * has fewer).  All give identical results. */
+int swift_ctx_set_tuning(swift_ctx *ctx, int32_t mode);
 
 /* Phase 2 on explicit pairs of varying lengths: the batched form of
  * alignSequences (src/align.cu:2904-2921, whose pairs all share one query
@@ -318,26 +333,47 @@ int swift_align_files(swift_ctx *ctx, const char *qry_path, const char *ref_path
                       const char *out_path, const swift_params *p);
 
 /* Serving loop.  No counterpart in the reference (a one-shot CLI).  The
- * index stays resident while requests, one reads FASTA each, queue up and
- * run on `workers` concurrent pipelines (a context and stream each, on the
- * given device).  A request starts when its estimated device memory fits
- * within mem_budget bytes beside the requests in flight (0: half of the
- * free memory at creation); one larger than the budget runs alone.  Each
- * result is byte-identical to swift_align on that request alone. */
+ * index stays resident while requests, one reads FASTA each, queue up.
+ * Continuous batching: each of `workers` pipelines (a context and stream
+ * each, on the given device) takes every queued request of one query-length
+ * class, oldest first, and runs them as one merged wave (one seeding
+ * launch over all their reads, shared Smith-Waterman launches over all
+ * their pairs); requests that arrive meanwhile join the next wave.  A wave
+ * starts when its estimated device memory fits within mem_budget bytes
+ * beside the waves in flight (0: half of the free memory at creation); a
+ * request larger than the budget runs alone.  Requests are parsed and
+ * checked at submission (reads up to p->max_read_len bases); each result is
+ * byte-identical to swift_align on that request alone. */
 typedef struct swift_server swift_server;
 typedef struct {
-  double queue_ms;   /* submit to start (host clock)                          */
+  double queue_ms;   /* submit to the start of its wave (host clock)          */
   double run_ms;     /* start to result                                       */
   double total_ms;   /* submit to result: the request's latency               */
-  double device_ms;  /* the pipeline's device time (CUDA events)              */
+  double device_ms;  /* its wave's device time (CUDA events)                  */
   int64_t reads, out_bytes;
+  int64_t wave_requests;  /* requests of its wave                             */
+  int64_t wave_reads;     /* reads of its wave                                */
 } swift_request_stats;
 int swift_server_create(int device, const swift_index *idx, const swift_params *p,
                         int32_t workers, int64_t mem_budget, swift_server **out);
-/* Queues a copy of the reads; *ticket identifies the request. */
+/* Queues a copy of the reads; *ticket identifies the request.  A request
+ * that fails its checks is done at once with that error. */
 int swift_server_submit(swift_server *s, const char *reads_fasta, size_t len, int64_t *ticket);
+/* Non-blocking state of a request: SWIFT_SERVE_QUEUED, _RUNNING, _DONE (its
+ * result waits for swift_server_wait) or _CANCELLED; SWIFT_E_ARG for an
+ * unknown ticket. */
+#define SWIFT_SERVE_QUEUED 0
+#define SWIFT_SERVE_RUNNING 1
+#define SWIFT_SERVE_DONE 2
+#define SWIFT_SERVE_CANCELLED 3
+int swift_server_poll(swift_server *s, int64_t ticket, int32_t *state);
+/* Cancels a request that has not started: it leaves the queue and
+ * swift_server_wait returns SWIFT_E_CANCELLED for it.  SWIFT_E_LIMIT once it
+ * runs or is done (its result stands), SWIFT_E_ARG for an unknown ticket. */
+int swift_server_cancel(swift_server *s, int64_t ticket);
 /* Blocks until the request is done and returns its status; *out (free with
- * swift_free) holds the records; err receives the message of a failure. */
+ * swift_free) holds the records; err receives the message of a failure.
+ * The ticket is released. */
 int swift_server_wait(swift_server *s, int64_t ticket, char **out, size_t *out_len,
                       swift_request_stats *stats, char *err, size_t err_cap);
 /* Runs the queued requests to completion, then frees everything. */

@@ -33,6 +33,7 @@ class Params(C.Structure):
         ("threads", C.c_int),
         ("out_format", C.c_int),
         ("seeder", C.c_int),
+        ("max_read_len", C.c_int),
     ]
 
 
@@ -57,7 +58,7 @@ class Aln(C.Structure):
 
 
 def default_params(**kw) -> Params:
-    p = Params(12, 1000, 3, 2, -1, -10, -1, 0, 0, os.cpu_count() or 1, 0, 0)
+    p = Params(12, 1000, 3, 2, -1, -10, -1, 0, 0, os.cpu_count() or 1, 0, 0, 0)
     for k, v in kw.items():
         setattr(p, k, v)
     return p

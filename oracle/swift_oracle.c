@@ -38,6 +38,8 @@
 #define SO_LINE_MAX 100000  /* MAX_LINE_LENGTH, src/common.h:41       */
 #define SO_NAME_MAX 50      /* MAX_QRY_NAME_LENGTH, src/common.h:37    */
 #define SO_QSEQ_MAX 200     /* MAX_QRY_SEQ_LENGTH, src/common.h:40     */
+#define SO_READ_LONGEST 300 /* longest read with so_params.max_read_len */
+#define SO_QMAX 320         /* longest query the restatement takes      */
 #define SO_WIN 300          /* REF_LENGTH, src/common.h:57             */
 #define SO_SHIFT_BASES 100  /* refSeqLength / 3, src/align.cu:668      */
 #define SO_MEM_MARGIN 100000000LL /* GLOBAL_MEM_MARGIN, src/common.h:43 */
@@ -586,8 +588,15 @@ typedef struct {
   int first_len;  /* getSeqSize (src/input.cu:475-496)                         */
 } so_reads;
 
+/* the longest read a run takes: the reference's 199 unless max_read_len
+ * allows more (up to SO_READ_LONGEST) */
+static int so_read_limit(const so_params *p) {
+  if (p->max_read_len <= 0) return SO_QSEQ_MAX - 1;
+  return p->max_read_len < SO_READ_LONGEST ? p->max_read_len : SO_READ_LONGEST;
+}
+
 static int so_reads_parse(const char *b, size_t n, so_reads *rd, char *err,
-                          size_t errlen) {
+                          size_t errlen, int max_read) {
   memset(rd, 0, sizeof(*rd));
   if (so_check_bytes(b, n, "reads", err, errlen)) return -1;
   int cap = 1024;
@@ -628,8 +637,8 @@ static int so_reads_parse(const char *b, size_t n, so_reads *rd, char *err,
                "offset %zu (multi-line reads are not supported)", pos);
         return -1;
       }
-      if (ll >= SO_QSEQ_MAX) {
-        so_err(err, errlen, "reads: read longer than %d bases", SO_QSEQ_MAX - 1);
+      if (ll > max_read) {
+        so_err(err, errlen, "reads: read longer than %d bases", max_read);
         return -1;
       }
       cur.seq = line;
@@ -686,7 +695,7 @@ typedef struct {
 
 static void *so_p1_worker(void *arg) {
   so_p1_job *jb = (so_p1_job *)arg;
-  char rev[SO_QSEQ_MAX + 1];
+  char rev[SO_READ_LONGEST + 1];
   for (;;) {
     pthread_mutex_lock(&jb->mu);
     long i = jb->next;
@@ -776,7 +785,7 @@ int so_phase1(const char *ref, size_t ref_len, const char *reads,
   so_index *ix = NULL;
   int rc = so_ref_parse(ref, ref_len, &r, err, errlen);
   if (rc == 0) rc = so_index_from_ref(&r, p->seed_len, p->ignore_thres, &ix, err, errlen);
-  if (rc == 0) rc = so_reads_parse(reads, reads_len, &rd, err, errlen);
+  if (rc == 0) rc = so_reads_parse(reads, reads_len, &rd, err, errlen, so_read_limit(p));
   if (rc == 0) {
     if (p->seeder == 1) {
       so_lt13 *t = NULL;
@@ -1054,7 +1063,7 @@ typedef struct {
 
 static void *so_l13_worker(void *arg) {
   so_l13_job *jb = (so_l13_job *)arg;
-  char rev[SO_QSEQ_MAX + 1];
+  char rev[SO_READ_LONGEST + 1];
   for (;;) {
     pthread_mutex_lock(&jb->mu);
     long i = jb->next;
@@ -1154,7 +1163,7 @@ typedef struct {
   char qname[SO_NAME_MAX + 1];
   const char *rname;
   int ref_dist;
-  char q[SO_QSEQ_MAX + 2];
+  char q[SO_QMAX + 2];
   char w[SO_WIN + 1];
   so_aln a;
   char *qc, *rc;
@@ -1305,7 +1314,7 @@ int so_session_align(so_session *ss, const char *reads, size_t reads_len,
   so_match *m = NULL;
   int nm = 0;
   memset(&rd, 0, sizeof(rd));
-  int rc = so_reads_parse(reads, reads_len, &rd, err, errlen);
+  int rc = so_reads_parse(reads, reads_len, &rd, err, errlen, so_read_limit(p));
   if (rc == 0)
     rc = p->seeder == 1 ? so_run_phase1_lt13(ss->l13, &rd, p->threads, &m, &nm)
                         : so_run_phase1(ss->ix, &rd, p->max_hits, p->threads, &m, &nm);
@@ -1314,8 +1323,8 @@ int so_session_align(so_session *ss, const char *reads, size_t reads_len,
     return rc;
   }
   int Q = p->qry_len > 0 ? p->qry_len : rd.first_len;
-  if (Q < 1 || Q > SO_QSEQ_MAX) {
-    so_err(err, errlen, "query length %d outside 1..%d", Q, SO_QSEQ_MAX);
+  if (Q < 1 || Q > SO_QMAX) {
+    so_err(err, errlen, "query length %d outside 1..%d", Q, SO_QMAX);
     free(rd.r); free(m);
     return -1;
   }
@@ -1663,7 +1672,7 @@ static int so_pe_phase1(const so_ref *r, const so_pe_index *t, const so_reads *r
                         const so_reads *r2, int Q, so_pe_match **out, long *n_out) {
   long cap = 64, n = 0;
   so_pe_match *m = (so_pe_match *)malloc((size_t)cap * sizeof(so_pe_match));
-  char rev[SO_QSEQ_MAX + 1];
+  char rev[SO_READ_LONGEST + 1];
   int8_t ri[SO_PE_HITS];
   int32_t sh[SO_PE_HITS], of[SO_PE_HITS];
   for (int i = 0; i < r1->n; ++i) {
@@ -1903,8 +1912,8 @@ int so_phase1_paired(const char *ref, size_t ref_len, const char *reads1, size_t
   memset(&a, 0, sizeof(a));
   memset(&b, 0, sizeof(b));
   int rc = so_ref_parse(ref, ref_len, &r, err, errlen);
-  if (rc == 0) rc = so_reads_parse(reads1, len1, &a, err, errlen);
-  if (rc == 0) rc = so_reads_parse(reads2, len2, &b, err, errlen);
+  if (rc == 0) rc = so_reads_parse(reads1, len1, &a, err, errlen, SO_QSEQ_MAX - 1);
+  if (rc == 0) rc = so_reads_parse(reads2, len2, &b, err, errlen, SO_QSEQ_MAX - 1);
   if (rc == 0 && a.n != b.n) {
     so_err(err, errlen, "paired reads: %d and %d reads", a.n, b.n);
     rc = -1;
@@ -1944,8 +1953,8 @@ int so_align_paired(const char *ref, size_t ref_len, const char *reads1, size_t 
   so_reads rd[2];
   memset(rd, 0, sizeof(rd));
   int rc = so_ref_parse(ref, ref_len, &r, err, errlen);
-  if (rc == 0) rc = so_reads_parse(reads1, len1, &rd[0], err, errlen);
-  if (rc == 0) rc = so_reads_parse(reads2, len2, &rd[1], err, errlen);
+  if (rc == 0) rc = so_reads_parse(reads1, len1, &rd[0], err, errlen, SO_QSEQ_MAX - 1);
+  if (rc == 0) rc = so_reads_parse(reads2, len2, &rd[1], err, errlen, SO_QSEQ_MAX - 1);
   if (rc == 0 && rd[0].n != rd[1].n) {
     so_err(err, errlen, "paired reads: %d and %d reads", rd[0].n, rd[1].n);
     rc = -1;
@@ -2004,7 +2013,7 @@ int so_align_paired(const char *ref, size_t ref_len, const char *reads1, size_t 
       so_get_seq(r.file, r.file_len, woff, y->w, R);
       y->rname = rec->name;
       const so_read *rr = &rd[mm->mate - 1].r[mm->read];
-      char tmp[SO_QSEQ_MAX + 2];
+      char tmp[SO_QMAX + 2];
       int L = rr->len < Q ? rr->len : Q;
       memcpy(tmp, rr->seq, (size_t)L);
       tmp[L] = '\0';

@@ -36,6 +36,8 @@ typedef struct {
                         every record); other values printOutput           */
   int seeder;        /* 0 SSAHA (searchQueries3); 1 lt13 seed-and-extend
                         (search2Queries, the GPU default of src/main.cu)   */
+  int max_read_len;  /* longest read taken, up to 300; <= 0: the reference's
+                        199 (MAX_QRY_SEQ_LENGTH - 1, src/common.h:40)       */
 } so_params;
 
 typedef struct {

@@ -15,19 +15,21 @@ LIB_PATH = os.path.join(HERE, "libswift_gb300.so")
 CLI_PATH = os.path.join(HERE, "swift")
 
 SWIFT_OK = 0
-ERRORS = {-1: "argument", -2: "input", -3: "cuda", -4: "memory", -5: "limit", -6: "device"}
+ERRORS = {-1: "argument", -2: "input", -3: "cuda", -4: "memory", -5: "limit", -6: "device",
+          -7: "cancelled"}
+SERVE_STATES = {0: "queued", 1: "running", 2: "done", 3: "cancelled"}
 
 # Exported C symbols (kept in step with include/swift_gb300.h).
 EXPORTS = [
     "swift_params_default", "swift_ctx_create", "swift_ctx_destroy", "swift_last_error",
-    "swift_ctx_info", "swift_ctx_set_sw_path",
+    "swift_ctx_info", "swift_ctx_set_sw_path", "swift_ctx_set_tuning",
     "swift_index_build", "swift_index_destroy", "swift_index_info", "swift_index_export",
     "swift_seed", "swift_seed_lt13", "swift_index_save", "swift_index_load",
     "swift_index_params", "swift_align_paired", "swift_align_paired_into", "swift_sw_batch", "swift_align", "swift_reads_upload",
     "swift_reads_destroy", "swift_align_resident", "swift_fetch_output",
     "swift_align_files", "swift_free", "swift_peak_dpx", "swift_align_into",
     "swift_sw_batch_noalloc", "swift_sw_pairs", "swift_server_create", "swift_server_submit",
-    "swift_server_wait", "swift_server_destroy",
+    "swift_server_wait", "swift_server_destroy", "swift_server_poll", "swift_server_cancel",
 ]
 
 
@@ -53,15 +55,23 @@ class Match(C.Structure):
 
 class PairsStats(C.Structure):
     _fields_ = [("ms", C.c_double), ("pairs", C.c_int64), ("cells", C.c_int64),
-                ("segments", C.c_int64), ("generic_pairs", C.c_int64), ("launches", C.c_int64)]
+                ("segments", C.c_int64), ("generic_pairs", C.c_int64), ("launches", C.c_int64),
+                ("shape_lanes", C.c_int32 * 8), ("shape_rows", C.c_int32 * 8),
+                ("tune_ms", C.c_double)]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        d = {k: getattr(self, k) for k, _ in self._fields_}
+        d["shapes"] = {q: (self.shape_lanes[c], self.shape_rows[c])
+                       for c, q in enumerate((32, 64, 104, 128, 208, 256, 320))
+                       if self.shape_lanes[c]}
+        del d["shape_lanes"], d["shape_rows"]
+        return d
 
 
 class RequestStats(C.Structure):
     _fields_ = [("queue_ms", C.c_double), ("run_ms", C.c_double), ("total_ms", C.c_double),
-                ("device_ms", C.c_double), ("reads", C.c_int64), ("out_bytes", C.c_int64)]
+                ("device_ms", C.c_double), ("reads", C.c_int64), ("out_bytes", C.c_int64),
+                ("wave_requests", C.c_int64), ("wave_reads", C.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -107,6 +117,7 @@ def lib():
         L.swift_last_error.restype = C.c_char_p
         L.swift_ctx_info.argtypes = [vp, C.POINTER(i64), C.POINTER(i32)]
         L.swift_ctx_set_sw_path.argtypes = [vp, i32]
+        L.swift_ctx_set_tuning.argtypes = [vp, i32]
         L.swift_index_build.argtypes = [vp, C.c_char_p, sz, i32, i32, C.POINTER(vp)]
         L.swift_index_destroy.argtypes = [vp]
         L.swift_index_info.argtypes = [vp, vp, C.POINTER(i32), C.POINTER(i64), C.POINTER(i64)]
@@ -132,6 +143,8 @@ def lib():
         L.swift_server_wait.argtypes = [vp, i64, C.POINTER(vp), C.POINTER(sz),
                                         C.POINTER(RequestStats), C.c_char_p, sz]
         L.swift_server_destroy.argtypes = [vp]
+        L.swift_server_poll.argtypes = [vp, i64, C.POINTER(i32)]
+        L.swift_server_cancel.argtypes = [vp, i64]
         L.swift_sw_pairs.argtypes = [vp, vp, vp, vp, vp, vp, vp, i64, i32, i32, i32, i32,
                                      vp, vp, vp, vp, vp, vp, i64, i32, C.POINTER(PairsStats)]
         L.swift_align_into.argtypes = [vp, vp, vp, sz, C.POINTER(Params), vp, sz, C.POINTER(sz),
@@ -181,6 +194,11 @@ class Context:
         """0: bounded selection (default); 1: generic kernel only; 2: exact score
         of every packed-path pair.  All give identical output."""
         self._check(lib().swift_ctx_set_sw_path(self._h, path))
+
+    def set_tuning(self, mode: int):
+        """swift_sw_pairs' packed shapes: 1 autotuned (default), 0 fixed
+        defaults, k >= 2 the (k-2)-th candidate of every class."""
+        self._check(lib().swift_ctx_set_tuning(self._h, mode))
 
     def peak_dpx_cells_per_s(self) -> float:
         v = C.c_double()
@@ -384,7 +402,7 @@ class Server:
     """Serving loop over a resident index: submit reads, wait for records."""
 
     def __init__(self, index: "Index", device: int = 0, params: Params | None = None,
-                 workers: int = 4, mem_budget: int = 0):
+                 workers: int = 2, mem_budget: int = 0):
         self._index = index  # keeps the index alive
         p = params or default_params(seed_len=index.seed_len, ignore_thres=index.ignore_thres)
         h = C.c_void_p()
@@ -400,6 +418,23 @@ class Server:
         if rc != SWIFT_OK:
             raise SwiftError(rc, "submit failed")
         return t.value
+
+    def poll(self, ticket: int) -> str:
+        """'queued', 'running', 'done' or 'cancelled', without blocking."""
+        st = C.c_int32()
+        rc = lib().swift_server_poll(self._h, ticket, C.byref(st))
+        if rc != SWIFT_OK:
+            raise SwiftError(rc, "unknown ticket")
+        return SERVE_STATES[st.value]
+
+    def cancel(self, ticket: int) -> bool:
+        """Cancels a request that has not started; False once it runs or is done."""
+        rc = lib().swift_server_cancel(self._h, ticket)
+        if rc == -5:
+            return False
+        if rc != SWIFT_OK:
+            raise SwiftError(rc, "unknown ticket")
+        return True
 
     def wait(self, ticket: int):
         """Returns (records bytes, stats dict); raises SwiftError for a failed request."""

@@ -292,6 +292,25 @@ __global__ void read_counts_kernel(const int32_t* __restrict__ nbest, int64_t n_
   if (r < n_reads) cnt[r] = (uint64_t)(nbest[2 * r] + nbest[2 * r + 1]);
 }
 
+// Record counts of a wave's record slots (each slot one read's records).
+__global__ void slot_counts_kernel(const int32_t* __restrict__ nbest,
+                                   const int32_t* __restrict__ slot_read, int64_t n_slots,
+                                   uint64_t* __restrict__ cnt) {
+  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v < n_slots) {
+    const int64_t r = slot_read[v];
+    cnt[v] = (uint64_t)(nbest[2 * r] + nbest[2 * r + 1]);
+  }
+}
+
+// out[i] = v[at[i]] for i < n (at[i] == len: total, the value past the end)
+__global__ void gather_u64_kernel(const uint64_t* __restrict__ v, int64_t len,
+                                  const uint64_t* __restrict__ total, const int64_t* __restrict__ at,
+                                  int64_t n, uint64_t* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = at[i] >= len ? *total : v[at[i]];
+}
+
 __global__ void aln_to_ref_layout_kernel(const DevAln* __restrict__ aln, int64_t n, float* score,
                                          int32_t* start, int32_t* end, int32_t* len) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -461,8 +480,10 @@ int seed_ssaha(swift_ctx* ctx, Scratch& sc, SeedArgs a, SeedOut* out) {
   int32_t* novl = a.n_overflow;
   int32_t* nbest = a.nbest;
   CK(sc.get(&a.mid_list, (size_t)std::max<int64_t>(ns, 1)));
-  CK(sc.get(&a.n_mid, 1));
-  CK(cudaMemsetAsync(a.n_mid, 0, sizeof(int32_t), st));
+  CK(sc.get(&a.big_list, (size_t)std::max<int64_t>(ns, 1)));
+  CK(sc.get(&a.n_mid, 2));
+  CK(cudaMemsetAsync(a.n_mid, 0, 2 * sizeof(int32_t), st));
+  a.n_big = a.n_mid + 1;
   if (!out->d_model) {
     CK(sc.get(&out->d_model, kSeedModelSlots));
     CK(cudaMemsetAsync(out->d_model, 0, kSeedModelSlots * sizeof(unsigned long long), st));
@@ -472,7 +493,7 @@ int seed_ssaha(swift_ctx* ctx, Scratch& sc, SeedArgs a, SeedOut* out) {
   launch_seed(st, a);
   CKLAUNCH();
   CK(cudaEventRecord(ctx->ev[10], st));
-  out->launches += n > 0 ? 2 : 0;
+  out->launches += n > 0 ? 3 : 0;
   int32_t h_novl = 0;
   CK(cudaMemcpyAsync(&h_novl, novl, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
@@ -591,7 +612,7 @@ int ensure_lt13(swift_ctx* ctx, const swift_index* cidx) {
 // seeder 0: SSAHA (searchQueries3, with its stale trailing batch); 1: lt13
 // seed-and-extend (search2Queries: every read once, 3 hits per strand).
 int run_seed(swift_ctx* ctx, const swift_index* idx, const swift_reads* rd, int max_hits,
-             int seeder, Scratch& sc, SeedOut* out) {
+             int seeder, Scratch& sc, SeedOut* out, std::vector<WaveReq>* wave = nullptr) {
   const int64_t n = rd->n;
   const int64_t ns = 2 * n;
   cudaStream_t st = ctx->st;
@@ -648,6 +669,7 @@ int run_seed(swift_ctx* ctx, const swift_index* idx, const swift_reads* rd, int 
     a.reads = rd->d_bytes;
     a.rd = rd->d_rd;
     a.n_reads = n;
+    a.max_len = rd->max_len;
     a.offsets = idx->d_offsets;
     a.groups = idx->d_groups;
     a.cstart = idx->d_cstart;
@@ -660,6 +682,63 @@ int run_seed(swift_ctx* ctx, const swift_index* idx, const swift_reads* rd, int 
     a.n_overflow = novl;
     const int rcs = seed_ssaha(ctx, sc, a, out);
     if (rcs != SWIFT_OK) return rcs;
+  }
+  if (wave) {
+    // a merged wave: each request's records in its order (its reads, then
+    // the stale reads of its own 16-read loop), requests one after another
+    const size_t W = wave->size();
+    std::vector<int32_t> slots;
+    std::vector<int64_t> slot_base(W + 1);
+    for (size_t r = 0; r < W; ++r) {
+      slot_base[r] = (int64_t)slots.size();
+      const WaveReq& q = (*wave)[r];
+      for (int64_t i = 0; i < q.n; ++i) slots.push_back((int32_t)(q.read0 + i));
+      if (seeder != 1) slots.insert(slots.end(), q.repeats.begin(), q.repeats.end());
+    }
+    slot_base[W] = (int64_t)slots.size();
+    const int64_t nv = (int64_t)slots.size();
+    int32_t* d_slots;
+    int64_t* d_sb;
+    uint64_t *cnt, *roff, *tot_d, *d_rec0;
+    void* tmp;
+    CK(sc.get(&d_slots, (size_t)std::max<int64_t>(nv, 1)));
+    CK(sc.get(&d_sb, W + 1));
+    CK(sc.get(&cnt, (size_t)std::max<int64_t>(nv, 1)));
+    CK(sc.get(&roff, (size_t)std::max<int64_t>(nv, 1)));
+    CK(sc.get(&tot_d, 1));
+    CK(sc.get(&d_rec0, W + 1));
+    CK(sc.get((uint8_t**)&tmp, scan_temp_bytes(nv)));
+    if (nv) CK(cudaMemcpyAsync(d_slots, slots.data(), nv * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(d_sb, slot_base.data(), (W + 1) * 8, cudaMemcpyHostToDevice, st));
+    if (nv) slot_counts_kernel<<<(unsigned)((nv + 255) / 256), 256, 0, st>>>(nbest, d_slots, nv, cnt);
+    CKLAUNCH();
+    out->launches += (nv > 0 ? 1 : 0) + exclusive_scan_u64(st, cnt, roff, nv, tmp, tot_d);
+    gather_u64_kernel<<<(unsigned)((W + 1 + 255) / 256), 256, 0, st>>>(roff, nv, tot_d, d_sb,
+                                                                       (int64_t)W + 1, d_rec0);
+    CKLAUNCH();
+    ++out->launches;
+    std::vector<uint64_t> rec0(W + 1);
+    CK(cudaMemcpyAsync(rec0.data(), d_rec0, (W + 1) * 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    const uint64_t total = rec0[W];
+    for (size_t r = 0; r < W; ++r) {
+      (*wave)[r].rec0 = (int64_t)rec0[r];
+      (*wave)[r].nm = (int64_t)(rec0[r + 1] - rec0[r]);
+    }
+    const size_t tn = std::max<uint64_t>(total, 1);
+    CK(sc.get(&out->m_read, tn));
+    CK(sc.get(&out->m_strand, tn));
+    CK(sc.get(&out->m_ri, tn));
+    CK(sc.get(&out->m_sh, tn));
+    CK(sc.get(&out->m_rp, tn));
+    if (nv > 0)  // every slot as a "repeat" entry: read slots[v] at offset roff[v]
+      fill_matches_kernel<<<(unsigned)((nv + 255) / 256), 256, 0, st>>>(
+          nbest, best, max_hits, 0, nullptr, d_slots, roff, nv, out->m_read, out->m_strand,
+          out->m_ri, out->m_sh, out->m_rp);
+    CKLAUNCH();
+    out->launches += nv > 0 ? 1 : 0;
+    out->n = (int64_t)total;
+    return SWIFT_OK;
   }
   // per-read record counts -> offsets
   uint64_t *cnt, *roff, *tot_d;
@@ -869,6 +948,12 @@ const char* swift_last_error(const swift_ctx* ctx) { return ctx ? ctx->err.c_str
 int swift_ctx_set_sw_path(swift_ctx* ctx, int32_t path) {
   if (!ctx || path < 0 || path > 2) return SWIFT_E_ARG;
   ctx->sw_path = path;
+  return SWIFT_OK;
+}
+
+int swift_ctx_set_tuning(swift_ctx* ctx, int32_t mode) {
+  if (!ctx || mode < 0 || mode > 64) return SWIFT_E_ARG;
+  ctx->tuning = mode;
   return SWIFT_OK;
 }
 
@@ -1631,7 +1716,23 @@ int swift_sw_pairs(swift_ctx* ctx, const char* qry, const int64_t* q_off, const 
         // packed trace pass + walk over pairs of one class, per-pair lengths,
         // in sub-chunks that bound the direction scratch
         const int64_t sub = 262144;
-        const int64_t words = trace_scratch_words(Q, R, std::min(cnt, sub));
+        // the class's (lanes, rows per lane) shape: the default, a forced
+        // candidate, or the fastest candidate on a sample of these pairs
+        // (timed once per context, class and window bin)
+        int32_t cg[16], crpl[16];
+        const int ncand = packed_shape_candidates(Q, cg, crpl, 16);
+        int sg = 0, srpl = 0;
+        if (ctx->tuning >= 2 && ctx->tuning - 2 < ncand) {
+          sg = cg[ctx->tuning - 2];
+          srpl = crpl[ctx->tuning - 2];
+        }
+        const int tkey = packed_class(Q) * 64 + (R + 63) / 64;
+        const bool tune = ctx->tuning == 1 && ncand > 1 && !ctx->tuned.count(tkey) &&
+                          cnt >= 4096;
+        int64_t words = 0;
+        for (int c = 0; c < (tune ? ncand : 1); ++c)
+          words = std::max(words, trace_scratch_words(Q, R, std::min(cnt, sub),
+                                                      tune ? cg[c] : sg, tune ? crpl[c] : srpl));
         if (words > dirs_words[0]) {
           CK(sc.get(&dirs[0], (size_t)words));
           dirs_words[0] = words;
@@ -1659,6 +1760,61 @@ int swift_sw_pairs(swift_ctx* ctx, const char* qry, const int64_t* q_off, const 
         fa.cons_stride = cs;
         fa.list = list;
         fa.count = gcount_d + gi;
+        if (tune) {
+          // a sample from the middle of the class (its pairs are sorted by
+          // window length), each candidate warmed once and timed once
+          const int64_t ns = std::min<int64_t>(cnt, 16384);
+          int32_t* ns_d;
+          CK(sc.get(&ns_d, 1));
+          const int32_t ns32 = (int32_t)ns;
+          CK(cudaMemcpyAsync(ns_d, &ns32, 4, cudaMemcpyHostToDevice, st));
+          FastArgs ta = fa;
+          ta.list = list + (cnt - ns) / 2;
+          ta.count = ns_d;
+          ta.list_offset = 0;
+          cudaEvent_t e0 = ctx->ev[9], e1 = ctx->ev[10];
+          float best_ms = 0;
+          int best = 0;
+          for (int c = 0; c < ncand; ++c) {
+            ta.shape_g = cg[c];
+            ta.shape_rpl = crpl[c];
+            float t = 0;
+            for (int rep = 0; rep < 2; ++rep) {
+              CK(cudaEventRecord(e0, st));
+              const int kk = launch_sw_trace(st, ta, ns);
+              if (kk == 0) return fail(ctx, SWIFT_E_DEVICE, "trace pass could not launch");
+              launches += kk;
+              CKLAUNCH();
+              CK(cudaEventRecord(e1, st));
+              CK(cudaEventSynchronize(e1));
+              CK(cudaEventElapsedTime(&t, e0, e1));
+              ps.tune_ms += t;
+            }
+            if (c == 0 || t < best_ms) {
+              best_ms = t;
+              best = c;
+            }
+          }
+          ctx->tuned[tkey] = {cg[best], crpl[best]};
+        }
+        if (ctx->tuning == 1) {
+          auto it = ctx->tuned.find(tkey);
+          if (it != ctx->tuned.end()) {
+            sg = it->second.first;
+            srpl = it->second.second;
+          }
+        }
+        fa.shape_g = sg;
+        fa.shape_rpl = srpl;
+        {
+          int32_t dg[1], dr[1];
+          packed_shape_candidates(Q, dg, dr, 1);
+          const int pc = packed_class(Q);
+          if (pc >= 0 && pc < 8) {
+            ps.shape_lanes[pc] = sg ? sg : dg[0];
+            ps.shape_rows[pc] = sg ? srpl : dr[0];
+          }
+        }
         for (int64_t off = 0; off < cnt; off += sub) {
           fa.list_offset = off;
           const int kk = launch_sw_trace(st, fa, std::min(sub, cnt - off));
@@ -1824,9 +1980,17 @@ static int read_limit(const swift_params* p) {
   return p && p->max_read_len > 0 ? std::min(p->max_read_len, kSeedReadMax) : kReadMax;
 }
 
+// wave: a merged batch of requests (the serving loop), each with its own
+// query length, stale-read tail and Phase-2 batches; the requests must be
+// valid on their own (checked at admission).  Null: rd is one request.
+}  // extern "C"
+int read_limit_of(const swift_params* p) { return read_limit(p); }
+extern "C" {
+
 static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swift_reads* rd,
                                const swift_params* p, size_t* out_len, swift_stats* stats,
-                               char* host_out, size_t host_cap) {
+                               char* host_out, size_t host_cap,
+                               std::vector<WaveReq>* wave = nullptr) {
   if (!ctx || !idx || !rd || !p) return fail(ctx, SWIFT_E_ARG, "null argument");
   CK(cudaSetDevice(ctx->device));
   if (p->seed_len != idx->k || p->ignore_thres != idx->thres)
@@ -1838,10 +2002,23 @@ static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swi
     return fail(ctx, SWIFT_E_LIMIT,
                 "reads: read longer than " + std::to_string(read_limit(p)) + " bases" +
                     (read_limit(p) == kReadMax ? " (the reference's query buffer)" : ""));
-  const int Q = p->qry_len > 0 ? p->qry_len : rd->first_len;
+  if (read_limit(p) > kReadMax && p->seeder == 1 && rd->max_len > kReadMax)
+    return fail(ctx, SWIFT_E_LIMIT, "lt13 seeding takes reads of up to 199 bases");
+  // the longest query of the call (every query when not a wave)
+  int Q = p->qry_len > 0 ? p->qry_len : rd->first_len;
+  bool uniform_q = true;
+  if (wave) {
+    if (wave->empty()) return fail(ctx, SWIFT_E_ARG, "empty wave");
+    Q = 0;
+    for (const WaveReq& q : *wave) {
+      if (q.Q < 1 || q.Q > kMaxQ) return fail(ctx, SWIFT_E_ARG, "wave: query length out of range");
+      Q = std::max(Q, (int)q.Q);
+      uniform_q = uniform_q && q.Q == (*wave)[0].Q;
+    }
+  }
   if (Q < 1 || Q > kMaxQ)
     return fail(ctx, SWIFT_E_LIMIT, "query length outside 1.." + std::to_string(kMaxQ));
-  if (rd->n > 0 && rd->min_len < Q)
+  if (!wave && rd->n > 0 && rd->min_len < Q)
     return fail(ctx, SWIFT_E_INPUT,
                 "a read is shorter than the query length; the reference aligns such reads "
                 "against stale buffer contents");
@@ -1852,18 +2029,33 @@ static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swi
   CK(cudaEventRecord(ctx->ev[0], st));
   SeedOut so;
   if (p->seeder != 0 && p->seeder != 1) return fail(ctx, SWIFT_E_ARG, "seeder must be 0 or 1");
-  int rc = run_seed(ctx, idx, rd, p->max_hits, p->seeder, sc, &so);
+  int rc = run_seed(ctx, idx, rd, p->max_hits, p->seeder, sc, &so, wave);
   if (rc != SWIFT_OK) return rc;
   CK(cudaEventRecord(ctx->ev[1], st));
   const int64_t nm = so.n;
   const int64_t dev_mem = p->device_mem > 0 ? p->device_mem : ctx->total_mem;
+  // records the batches of getNumQueriesPerIteration cover: all of them,
+  // unless the float ceil of the batch count comes out one short
+  auto processed = [](int64_t nrec, int64_t per) -> int64_t {
+    const int it = phase2_iterations(nrec, per);
+    if (it <= 0) return 0;
+    const int64_t maxs = (int64_t)it * per;
+    const int64_t last = nrec < maxs ? nrec - (int64_t)(it - 1) * per : per;
+    return (int64_t)(it - 1) * per + last;
+  };
   const int64_t per_iter = phase2_batch(dev_mem, Q, nm);
-  const int n_iter = phase2_iterations(nm, per_iter);
-  int64_t nproc = 0;
-  if (n_iter > 0) {
-    const int64_t maxs = (int64_t)n_iter * per_iter;
-    const int64_t last = nm < maxs ? nm - (int64_t)(n_iter - 1) * per_iter : per_iter;
-    nproc = (int64_t)(n_iter - 1) * per_iter + last;
+  int64_t nproc = wave ? nm : processed(nm, per_iter);
+  // a wave's batch boundaries: each request's own batches (of its own
+  // query length), so its best-per-read groups end where they end alone
+  std::vector<uint8_t> h_bs;
+  if (wave) {
+    h_bs.assign((size_t)std::max<int64_t>(nm, 1), 0);
+    for (const WaveReq& q : *wave) {
+      const int64_t per = phase2_batch(dev_mem, q.Q, q.nm);
+      if (processed(q.nm, per) != q.nm)
+        return fail(ctx, SWIFT_E_LIMIT, "wave: a request's batches do not cover its records");
+      for (int64_t k = 0; k < q.nm; k += std::max<int64_t>(per, 1)) h_bs[q.rec0 + k] = 1;
+    }
   }
   const int Qs = (Q + 16) & ~15;
   // consensus stride: Q + R + 2 bytes, rounded to 16 so the walk kernel can
@@ -1906,6 +2098,25 @@ static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swi
   pa.qbuf = qbuf;
   pa.wbuf = wbuf;
   pa.Qs = Qs;
+  // a wave of several query lengths: each record's own, for the pair
+  // builder and every Smith-Waterman pass (rows past it match nothing)
+  int32_t* pair_q = nullptr;
+  uint8_t* d_bs = nullptr;
+  if (wave) {
+    CK(sc.get(&d_bs, nn));
+    if (nm) CK(cudaMemcpyAsync(d_bs, h_bs.data(), nm, cudaMemcpyHostToDevice, st));
+    if (!uniform_q) {
+      std::vector<int32_t> h_rq((size_t)std::max<int64_t>(rd->n, 1), 0);
+      for (const WaveReq& q : *wave)
+        std::fill(h_rq.begin() + q.read0, h_rq.begin() + q.read0 + q.n, q.Q);
+      int32_t* d_rq;
+      CK(sc.get(&d_rq, h_rq.size()));
+      CK(cudaMemcpyAsync(d_rq, h_rq.data(), h_rq.size() * 4, cudaMemcpyHostToDevice, st));
+      CK(sc.get(&pair_q, nn));
+      pa.read_q = d_rq;
+      pa.pair_q = pair_q;
+    }
+  }
   launch_build_pairs(st, pa);
   CKLAUNCH();
   CK(cudaEventRecord(ctx->ev[2], st));
@@ -1952,6 +2163,7 @@ static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swi
   sa.qcons = qcons;
   sa.rcons = rcons;
   sa.cons_stride = cs;
+  sa.q_len = pair_q;
   FastArgs fa2;
   memset(&fa2, 0, sizeof(fa2));
   fa2.q = qbuf;
@@ -1969,6 +2181,7 @@ static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swi
   fa2.qcons = qcons;
   fa2.rcons = rcons;
   fa2.cons_stride = cs;
+  fa2.q_len = pair_q;
   int32_t *ub = nullptr, *cand = nullptr;
   uint16_t* suf = nullptr;
   if (bounded) {
@@ -2015,6 +2228,7 @@ static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swi
   fa.cons_stride = cs;
   fa.n = nproc;
   fa.batch = per_iter > 0 ? per_iter : 1;
+  fa.batch_start = d_bs;
   fa.keep = keep;
   fa.bytes = bytes;
   fa.offs = offs;
@@ -2173,12 +2387,36 @@ static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swi
   CK(cudaMemcpyAsync(h_cnt, cnt, sizeof(h_cnt), cudaMemcpyDeviceToHost, st));
   unsigned long long h_cells = 0, h_model[kSeedModelSlots] = {};
   CK(cudaMemcpyAsync(&h_cells, d_cells, sizeof(h_cells), cudaMemcpyDeviceToHost, st));
+  // a wave: each request's text starts at its first record's offset
+  std::vector<uint64_t> h_t0;
+  if (wave) {
+    const size_t W = wave->size();
+    std::vector<int64_t> at(W + 1);
+    for (size_t r = 0; r < W; ++r) at[r] = (*wave)[r].rec0;
+    at[W] = nproc;
+    int64_t* d_at;
+    uint64_t* d_t0;
+    CK(sc.get(&d_at, W + 1));
+    CK(sc.get(&d_t0, W + 1));
+    CK(cudaMemcpyAsync(d_at, at.data(), (W + 1) * 8, cudaMemcpyHostToDevice, st));
+    gather_u64_kernel<<<(unsigned)((W + 1 + 255) / 256), 256, 0, st>>>(offs, nproc, tot_d, d_at,
+                                                                       (int64_t)W + 1, d_t0);
+    CKLAUNCH();
+    ++launches;
+    h_t0.resize(W + 1);
+    CK(cudaMemcpyAsync(h_t0.data(), d_t0, (W + 1) * 8, cudaMemcpyDeviceToHost, st));
+  }
   if (so.d_model)
     CK(cudaMemcpyAsync(h_model, so.d_model, sizeof(h_model), cudaMemcpyDeviceToHost, st));
   TextChunks chunks;
   rc = chunks.plan(ctx, st, offs, nproc, host_out != nullptr);
   if (rc != SWIFT_OK) return rc;
   CK(cudaStreamSynchronize(st));
+  if (wave)
+    for (size_t r = 0; r < wave->size(); ++r) {
+      (*wave)[r].text0 = h_t0[r];
+      (*wave)[r].text1 = h_t0[r + 1];
+    }
   if (total + 1 > ctx->text_cap) {
     if (ctx->d_text) cudaFree(ctx->d_text);
     ctx->d_text = nullptr;
@@ -2245,6 +2483,52 @@ static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swi
   }
   return SWIFT_OK;
 }
+
+// One merged wave of the serving loop (server.cpp): the requests' reads
+// FASTA bytes back to back in host memory with their per-read records
+// (offsets into those bytes), every request valid on its own.  The text of
+// all requests goes to host_out when it fits host_cap (the caller splits it
+// with each request's text0 / text1), else it stays on the device for
+// swift_fetch_output.
+}  // extern "C"
+int run_wave(swift_ctx* ctx, const swift_index* idx, const swift_params* p, const char* bytes,
+             size_t len, const std::vector<DevRead>& rd, std::vector<WaveReq>* wave,
+             char* host_out, size_t host_cap, size_t* out_len, swift_stats* stats) {
+  if (!ctx || !idx || !p || !wave || (!bytes && len)) return fail(ctx, SWIFT_E_ARG, "null argument");
+  CK(cudaSetDevice(ctx->device));
+  cudaStream_t st = ctx->st;
+  swift_reads* r = new swift_reads();
+  r->device = ctx->device;
+  r->len = len;
+  r->pool_st = st;
+  r->n = (int64_t)rd.size();
+  r->n_gt = r->n;
+  int32_t mn = INT32_MAX, mx = 0;
+  for (const DevRead& d : rd) {
+    mn = std::min(mn, d.len);
+    mx = std::max(mx, d.len);
+  }
+  r->min_len = r->n ? mn : 0;
+  r->max_len = mx;
+  r->first_len = r->n ? rd[0].len : 0;
+  int rc = SWIFT_OK;
+  if (cudaMallocAsync(&r->d_bytes, len + 64, st) != cudaSuccess ||
+      cudaMallocAsync(&r->d_rd, std::max<size_t>(rd.size(), 1) * sizeof(DevRead), st) != cudaSuccess ||
+      (len && cudaMemcpyAsync(r->d_bytes, bytes, len, cudaMemcpyHostToDevice, st) != cudaSuccess) ||
+      (!rd.empty() && cudaMemcpyAsync(r->d_rd, rd.data(), rd.size() * sizeof(DevRead),
+                                      cudaMemcpyHostToDevice, st) != cudaSuccess)) {
+    rc = fail(ctx, SWIFT_E_CUDA, std::string("wave upload: ") + cudaGetErrorString(cudaGetLastError()));
+  } else {
+    rc = align_resident_impl(ctx, idx, r, p, out_len, stats, host_out, host_cap, wave);
+    if (rc == SWIFT_OK) {
+      const cudaError_t e = cudaStreamSynchronize(st);  // the host copies of the text
+      if (e != cudaSuccess) rc = fail(ctx, SWIFT_E_CUDA, cudaGetErrorString(e));
+    }
+  }
+  swift_reads_destroy(r);
+  return rc;
+}
+extern "C" {
 
 int swift_align_resident(swift_ctx* ctx, const swift_index* idx, const swift_reads* rd,
                          const swift_params* p, size_t* out_len, swift_stats* stats) {
@@ -2398,6 +2682,7 @@ static int align_paired_impl(swift_ctx* ctx, const swift_index* idx, const char*
     a.reads = r->d_bytes;
     a.rd = r->d_rd;
     a.n_reads = n;
+    a.max_len = r->max_len;
     a.groups = src->d_groups;
     a.cstart = src->d_cstart;
     a.offsets = src->d_offsets;

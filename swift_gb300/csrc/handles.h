@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -26,6 +27,10 @@ struct swift_ctx {
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   std::vector<cudaEvent_t> chunk_ev;  // per-chunk timing of the trace pass, grown on use
   std::vector<cudaEvent_t> copy_ev;   // text ranges ready for their host copy, grown on use
+  // swift_sw_pairs: 1 autotune the packed shape per (query class, window
+  // bin), 0 default shapes, k >= 2 the (k-2)-th candidate of every class
+  int tuning = 1;
+  std::map<int, std::pair<int, int>> tuned;  // (class, window bin) -> (lanes, rows per lane)
 };
 
 struct swift_index {
@@ -77,3 +82,9 @@ struct swift_reads {
   std::vector<int32_t> repeats;
   cudaStream_t pool_st = nullptr;  // buffers from this stream's pool (one call's reads)
 };
+
+// api.cu: one merged wave of serving requests (server.cpp); see its comment.
+int run_wave(swift_ctx* ctx, const swift_index* idx, const swift_params* p, const char* bytes,
+             size_t len, const std::vector<swift::DevRead>& rd, std::vector<swift::WaveReq>* wave,
+             char* host_out, size_t host_cap, size_t* out_len, swift_stats* stats);
+int read_limit_of(const swift_params* p);

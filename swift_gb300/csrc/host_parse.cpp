@@ -157,7 +157,7 @@ int parse_reads_host(const char* b, size_t n, int max_read, HostReads* out, std:
   };
   HostReads r;
   int32_t mn = INT32_MAX, mx = 0;
-  uint64_t line_start = 0, prev_header = 0;
+  uint64_t line_start = 0, prev_start = 0;  // this line's and the previous line's start
   int64_t li = 0;
   char prev = '\n';
   const uint64_t n_nl = (uint64_t)std::count(b, b + n, '\n');
@@ -186,23 +186,23 @@ int parse_reads_host(const char* b, size_t n, int max_read, HostReads* out, std:
           if (len - 1 > (uint64_t)(kNameMax - 2)) report(line_start, kParseNameLong);
           if ((uint64_t)li + 1 >= n_lines) report(line_start, kParseTrailingHeader);
         }
-        prev_header = line_start;
-      } else if (header) {
-        report(li == 1 ? 0 : prev_header, kParseHeaderNoSeq);
+      } else if (header) {  // the line before has no sequence line
+        report(li == 1 ? 0 : prev_start, kParseHeaderNoSeq);
       } else if (len > (uint64_t)max_read) {
         report(line_start, kParseReadLong);
       } else {
         DevRead d;
-        d.name_off = prev_header;
+        d.name_off = prev_start;
         d.seq_off = line_start;
         d.len = (int32_t)len;
-        d.name_len = (int32_t)(line_start - 1 - prev_header - 1);
+        d.name_len = (int32_t)(line_start - 1 - prev_start - 1);
         r.rd.push_back(d);
         mn = std::min(mn, (int32_t)len);
         mx = std::max(mx, (int32_t)len);
         if (li == 1) r.first_len = (int32_t)len - (end == n ? 1 : 0);  // strlen(line) - 1
       }
     }
+    prev_start = line_start;
     pos = end + 1;
     ++li;
   }

@@ -52,6 +52,17 @@ struct HostRef {
 
 int parse_reference(const char* b, size_t n, HostRef* out, std::string* err);
 
+// One request of a merged wave (the serving loop): its reads in the wave's
+// reads buffers and what is its own when it runs alone.  rec0 / nm and
+// text0 / text1 are filled by the pipeline.
+struct WaveReq {
+  int64_t read0 = 0, n = 0;       // its reads: wave reads [read0, read0 + n)
+  int32_t Q = 0;                  // its query length
+  std::vector<int32_t> repeats;   // stale reads of its 16-read loop (wave read ids)
+  int64_t rec0 = 0, nm = 0;       // its records in the wave's record arrays
+  uint64_t text0 = 0, text1 = 0;  // its text in the wave's output
+};
+
 // Phase-1 slot schedule of searchQueries3: read index per slot call, -1 for
 // a slot never filled.  Returns the list of reads whose records follow the
 // in-order ones (slots that re-ran a stale read after end of file).
@@ -163,15 +174,19 @@ struct SeedArgs {
   int32_t* nbest;             // per strand
   int32_t* overflow_list;     // strands too big for the on-chip paths
   int32_t* n_overflow;
-  int32_t* mid_list;          // strands for the sort kernel (zeroed count)
+  int max_len;                // longest read (sizes the per-lane offsets)
+  int32_t* mid_list;          // strands for the hash-table kernel (zeroed count)
   int32_t* n_mid;
+  int32_t* big_list;          // strands for the sort kernel (zeroed count)
+  int32_t* n_big;
   unsigned long long* model_bytes;  // optional: kSeedModelSlots counters of
                                     // the roofline's sector-model bytes
   uint64_t* scratch;          // overflow path: per-strand hash tables
 };
 constexpr int kSeedModelSlots = 64;
-// The sort-free kernel over every strand, then the sort kernel over the
-// strands it listed; strands beyond both go to a.overflow_list.
+// The sort-free kernel over every strand, then the hash-table and sort
+// kernels over the strands it listed; strands beyond those go to
+// a.overflow_list.
 void launch_seed(cudaStream_t st, const SeedArgs& a);
 
 // seed13.cu: lt13 seed-and-extend seeding (search2Queries)
@@ -430,6 +445,8 @@ struct FastArgs {
   int64_t cons_stride;
   unsigned long long* cells_done;  // optional: score and trace passes add the
                                    // cells they computed (early stop counted)
+  int shape_g, shape_rpl;     // optional: the (lanes, rows per lane) shape of the
+                              // exact passes and walk; 0: the default for Q
 };
 bool fast_params_ok(int Q, int R, int m, int x, int o, int e, int* bias);
 constexpr int kFastMaxR = 512;  // window columns the packed passes take
@@ -443,7 +460,10 @@ __host__ __device__ inline int packed_class_max_q(int c) {
   return c == 0 ? 32 : c == 1 ? 64 : c == 2 ? 104 : c == 3 ? 128 : c == 4 ? 208 : c == 5 ? 256
        : 320;
 }
-int64_t trace_scratch_words(int Q, int R, int64_t pairs);
+int64_t trace_scratch_words(int Q, int R, int64_t pairs, int shape_g = 0, int shape_rpl = 0);
+// The compiled shapes the autotuner tries for queries up to Q (the default
+// first); returns how many.
+int packed_shape_candidates(int Q, int32_t* g, int32_t* rpl, int cap);
 int launch_sw_score(cudaStream_t st, const FastArgs& a, int64_t max_pairs);
 // before / after (optional) are recorded around the trace pass alone
 int launch_sw_trace(cudaStream_t st, const FastArgs& a, int64_t max_pairs,
@@ -466,6 +486,8 @@ struct FormatArgs {
   int64_t n;
   int64_t first;              // write kernels: records [first, n)
   int64_t batch;              // Phase-2 batch size (best-per-read groups stop at batch ends)
+  const uint8_t* batch_start; // optional: 1 at each record that opens a batch (per
+                              // request of a wave); replaces the uniform batch size
   int32_t* keep;              // per record: 1 if printed
   uint64_t* bytes;            // per record: text bytes
   uint64_t* offs;             // per record: text offset

@@ -50,14 +50,23 @@ __device__ bool names_equal(const FormatArgs& a, const DevPair& s, const DevPair
   return (s0 == '*' && s1 == '\0') || (t0 == '*' && t1 == '\0');
 }
 
+// Record j opens a Phase-2 batch: every a.batch records, or where the wave's
+// per-request flags say so.
+__device__ __forceinline__ bool opens_batch(const FormatArgs& a, int64_t j) {
+  return a.batch_start ? a.batch_start[j] != 0 : j % a.batch == 0;
+}
+// last record of the best-per-read group that starts at j
+__device__ __forceinline__ int64_t group_end(const FormatArgs& a, int64_t j) {
+  int64_t e = j;
+  while (e + 1 < a.n && !opens_batch(a, e + 1) && names_equal(a, a.pairs[e + 1], a.pairs[e])) ++e;
+  return e;
+}
+
 __global__ void select_kernel(FormatArgs a) {
   int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= a.n) return;
-  const int64_t bstart = (j / a.batch) * a.batch;
-  const int64_t bend = min(bstart + a.batch, a.n);
-  if (j != bstart && names_equal(a, a.pairs[j], a.pairs[j - 1])) return;  // not a group start
-  int64_t e = j;
-  while (e + 1 < bend && names_equal(a, a.pairs[e + 1], a.pairs[e])) ++e;
+  if (!opens_batch(a, j) && names_equal(a, a.pairs[j], a.pairs[j - 1])) return;  // not a group start
+  const int64_t e = group_end(a, j);
   int mx = 0;
   for (int64_t i = j; i <= e; ++i) mx = max(mx, a.aln[i].score);
   int64_t keep = -1;
@@ -89,11 +98,8 @@ __global__ void candidate_kernel(FormatArgs a, int32_t* list, int32_t* cnt) {
   bool app = false;
   int32_t cand = 0;
   if (j < a.n) {
-    const int64_t bstart = (j / a.batch) * a.batch;
-    const int64_t bend = min(bstart + a.batch, a.n);
-    if (j == bstart || !names_equal(a, a.pairs[j], a.pairs[j - 1])) {
-      int64_t e = j;
-      while (e + 1 < bend && names_equal(a, a.pairs[e + 1], a.pairs[e])) ++e;
+    if (opens_batch(a, j) || !names_equal(a, a.pairs[j], a.pairs[j - 1])) {
+      const int64_t e = group_end(a, j);
       int64_t best = j;
       int bk = -1;
       for (int64_t i = j; i <= e; ++i) {

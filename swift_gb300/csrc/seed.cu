@@ -35,6 +35,9 @@ namespace {
 constexpr int kSeedWarps = 8;          // warps per block
 constexpr int kShiftBias = 512;        // shift >= -(kSeedReadMax - 1) always
 constexpr int kFastHits = 32;          // hits of the sort-free path
+constexpr int kHashCap = 256;          // hits of the hash-table path
+constexpr int kHashSlots = 512;        // its table slots per warp (load <= 1/2)
+constexpr int kHashWarps = 4;          // warps per block of the hash-table path
 constexpr int kSortCap = 512;          // hits of the sort path
 
 __device__ __forceinline__ uint8_t fwd_code(uint8_t c) {
@@ -53,7 +56,9 @@ __device__ __forceinline__ uint64_t make_key(uint32_t ri, int32_t shift, int32_t
 
 // words of 16 packed 2-bit codes covering kSeedReadMax bases, plus one word
 constexpr int kPackedWords = (kSeedReadMax + 15) / 16 + 1;
-// query offsets per lane at most (contiguous ranges of M = ceil(nq / 32))
+// query offsets per lane at most (contiguous ranges of M = ceil(nq / 32));
+// the kernels are instantiated for KM = 3, 5, 7 and 10 and launched with the
+// smallest that covers the call's longest strand
 constexpr int kM = (kSeedReadMax + 31) / 32;
 
 struct WarpSmem {
@@ -66,9 +71,10 @@ struct WarpSmem {
 // the hash of [i, i + k) is one funnel shift, k <= 15), and looks up the
 // buckets of offsets i0 .. i0 + M - 1 (i0 = lane * M).  Returns the lane's
 // postings; beg / cnt per offset.
+template <int KM>
 __device__ __forceinline__ uint32_t strand_lookups(const SeedArgs& a, const DevRead& rd, int strand,
                                                    int L, int nq, int M, WarpSmem& w, int lane,
-                                                   uint32_t (&beg)[kM], uint32_t (&cnt)[kM]) {
+                                                   uint32_t (&beg)[KM], uint32_t (&cnt)[KM]) {
   const char* s = a.reads + rd.seq_off;
   for (int i = lane; i < L; i += 32)
     w.codes[i] = strand == 0 ? fwd_code((uint8_t)s[i]) : rev_code((uint8_t)s[L - 1 - i]);
@@ -93,7 +99,7 @@ __device__ __forceinline__ uint32_t strand_lookups(const SeedArgs& a, const DevR
   const int i0 = lane * M;
   uint32_t my = 0;
 #pragma unroll
-  for (int m = 0; m < kM; ++m) {
+  for (int m = 0; m < KM; ++m) {
     const int i = i0 + m;
     beg[m] = cnt[m] = 0;
     if (m < M && i < nq) {
@@ -116,11 +122,20 @@ __device__ __forceinline__ uint32_t strand_lookups(const SeedArgs& a, const DevR
 }
 
 // Posting sectors of the lane's lookups under the roofline's sector model.
-__device__ __forceinline__ uint32_t posting_sectors(const uint32_t (&cnt)[kM]) {
+template <int KM>
+__device__ __forceinline__ uint32_t posting_sectors(const uint32_t (&cnt)[KM]) {
   uint32_t b = 0;
 #pragma unroll
-  for (int m = 0; m < kM; ++m) b += ((5u * cnt[m] + 31u) >> 5) << 5;
+  for (int m = 0; m < KM; ++m) b += ((5u * cnt[m] + 31u) >> 5) << 5;
   return b;
+}
+
+// 64-bit mixer (the finaliser of MurmurHash3) for table slots
+__device__ __forceinline__ uint32_t cluster_mix(uint64_t x) {
+  x ^= x >> 33;
+  x *= 0xff51afd7ed558ccdull;
+  x ^= x >> 33;
+  return (uint32_t)x;
 }
 
 // lane 0 adds one strand's model bytes (warp-uniform arguments)
@@ -135,6 +150,7 @@ __device__ __forceinline__ int strand_nq(const SeedArgs& a, int L) {
   return (a.fixed_len > 0 ? a.fixed_len : L) - a.k + 1;
 }
 
+template <int KM>
 __global__ void __launch_bounds__(kSeedWarps * 32) seed_fast_kernel(SeedArgs a) {
   __shared__ __align__(16) WarpSmem smem[kSeedWarps];
   __shared__ uint2 info_all[kSeedWarps][kFastHits];
@@ -150,8 +166,8 @@ __global__ void __launch_bounds__(kSeedWarps * 32) seed_fast_kernel(SeedArgs a) 
     return;
   }
   const int M = (nq + 31) >> 5;
-  uint32_t beg[kM], cnt[kM];
-  const uint32_t my = strand_lookups(a, rd, strand, L, nq, M, smem[wib], lane, beg, cnt);
+  uint32_t beg[KM], cnt[KM];
+  const uint32_t my = strand_lookups<KM>(a, rd, strand, L, nq, M, smem[wib], lane, beg, cnt);
   uint32_t incl = my;
 #pragma unroll
   for (int d = 1; d < 32; d <<= 1) {
@@ -160,11 +176,13 @@ __global__ void __launch_bounds__(kSeedWarps * 32) seed_fast_kernel(SeedArgs a) 
   }
   const uint32_t n = __shfl_sync(0xffffffffu, incl, 31);
   if (n > (uint32_t)kFastHits) {
-    // the sort kernel (or the hash-table kernel) takes the strand
+    // the hash-table, sort or overflow kernel takes the strand
     if (lane == 0) {
       if (n > (uint32_t)kSortCap) {
         a.overflow_list[atomicAdd(a.n_overflow, 1)] = (int32_t)sid;
         a.nbest[sid] = -(int32_t)n;  // hit count, for sizing the overflow table
+      } else if (n > (uint32_t)kHashCap) {
+        a.big_list[atomicAdd(a.n_big, 1)] = (int32_t)sid;
       } else {
         a.mid_list[atomicAdd(a.n_mid, 1)] = (int32_t)sid;
       }
@@ -172,14 +190,14 @@ __global__ void __launch_bounds__(kSeedWarps * 32) seed_fast_kernel(SeedArgs a) 
     if (n > (uint32_t)kSortCap) account(a, lane, L, nq, 0, 0);  // its lookups
     return;
   }
-  const uint32_t post = __reduce_add_sync(0xffffffffu, posting_sectors(cnt));
+  const uint32_t post = __reduce_add_sync(0xffffffffu, posting_sectors<KM>(cnt));
   // hit t of the strand is posting t - start of the lookup that starts at
   // the last start at or before t: the starts as one bit mask, each start's
   // (first posting - start, query offset) in shared memory
   uint2* info = info_all[wib];
   uint32_t smask = 0, pos = incl - my;
 #pragma unroll
-  for (int m = 0; m < kM; ++m) {
+  for (int m = 0; m < KM; ++m) {
     if (cnt[m]) {
       smask |= 1u << pos;
       info[pos] = make_uint2(beg[m] - pos, (uint32_t)(lane * M + m));
@@ -225,9 +243,110 @@ __global__ void __launch_bounds__(kSeedWarps * 32) seed_fast_kernel(SeedArgs a) 
   account(a, lane, L, nq, post, got);
 }
 
-// The sort path over the strands of a.mid_list (between kFastHits and
+// The strands of a.mid_list (between kFastHits and kHashCap hits), without a
+// sort: every hit enters a per-warp open-addressing table over its cluster
+// key (refIdx, shift + bias) that counts the cluster and keeps its smallest
+// query offset; the biggest count is a warp max over the table, and the
+// first max_hits clusters of that size in key order come from warp minima.
+// Warps stride over the list, whose length is on the device.
+template <int KM>
+__global__ void __launch_bounds__(kHashWarps * 32) seed_hash_kernel(SeedArgs a) {
+  constexpr unsigned long long kEmpty = ~0ull;  // above every cluster key
+  constexpr int kPerLane = kHashSlots / 32;
+  __shared__ unsigned long long tkey_all[kHashWarps][kHashSlots];
+  __shared__ uint32_t tcnt_all[kHashWarps][kHashSlots];
+  __shared__ uint32_t tmin_all[kHashWarps][kHashSlots];
+  __shared__ __align__(16) WarpSmem smem[kHashWarps];
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  unsigned long long* tkey = tkey_all[wib];
+  uint32_t* tcnt = tcnt_all[wib];
+  uint32_t* tmin = tmin_all[wib];
+  const int64_t n_list = *a.n_mid;
+  for (int64_t t = (int64_t)blockIdx.x * kHashWarps + wib; t < n_list;
+       t += (int64_t)gridDim.x * kHashWarps) {
+    const int64_t sid = a.mid_list[t];
+    const DevRead rd = a.rd[sid >> 1];
+    const int strand = (int)(sid & 1);
+    const int L = rd.len, nq = strand_nq(a, L);
+    const int M = (nq + 31) >> 5;
+    uint32_t beg[KM], cnt[KM];
+    const uint32_t my = strand_lookups<KM>(a, rd, strand, L, nq, M, smem[wib], lane, beg, cnt);
+    const uint32_t n = __reduce_add_sync(0xffffffffu, my);  // in (kFastHits, kHashCap]
+    const uint32_t post = __reduce_add_sync(0xffffffffu, posting_sectors<KM>(cnt));
+    // a power of two at least twice the hits
+    uint32_t T = 64;
+    while (T < 2 * n) T <<= 1;
+    for (uint32_t i = lane; i < T; i += 32) {
+      tkey[i] = kEmpty;
+      tcnt[i] = 0;
+      tmin[i] = 0xffffffffu;
+    }
+    __syncwarp();
+#pragma unroll
+    for (int m = 0; m < KM; ++m) {
+      const uint32_t i = (uint32_t)(lane * M + m);
+      for (uint32_t j = 0; j < cnt[m]; ++j) {
+        const uint2 p = __ldg(&a.postings[beg[m] + j]);
+        const unsigned long long ck =
+            ((unsigned long long)p.y << 32) | (uint32_t)((int32_t)p.x - (int32_t)i + kShiftBias);
+        uint32_t slot = cluster_mix(ck) & (T - 1);
+        for (uint32_t probe = 0; probe < T; ++probe) {  // T > n: a free slot exists
+          const unsigned long long old = atomicCAS(&tkey[slot], kEmpty, ck);
+          if (old == kEmpty || old == ck) {
+            atomicAdd(&tcnt[slot], 1u);
+            atomicMin(&tmin[slot], i);
+            break;
+          }
+          slot = (slot + 1) & (T - 1);
+        }
+      }
+    }
+    __syncwarp();
+    // the biggest cluster, then its clusters as candidate bits of the lane's
+    // slots lane, lane + 32, ...
+    uint32_t big = 0;
+    for (uint32_t i = lane; i < T; i += 32) big = max(big, tcnt[i]);
+    big = __reduce_max_sync(0xffffffffu, big);
+    uint32_t cand = 0;
+#pragma unroll
+    for (int q = 0; q < kPerLane; ++q) {
+      const uint32_t i = lane + 32 * q;
+      if (i < T && tcnt[i] == big) cand |= 1u << q;
+    }
+    int got = 0;
+    int3* out = a.best + sid * a.max_hits;
+    while (got < a.max_hits) {  // the smallest cluster keys first
+      unsigned long long mk = kEmpty;
+      int mq = -1;
+      for (uint32_t c = cand; c; c &= c - 1) {
+        const int q = __ffs(c) - 1;
+        const unsigned long long k = tkey[lane + 32 * q];
+        if (k < mk) {
+          mk = k;
+          mq = q;
+        }
+      }
+      const uint32_t hi = (uint32_t)(mk >> 32), lo = (uint32_t)mk;
+      const uint32_t hmin = __reduce_min_sync(0xffffffffu, hi);
+      if (hmin == 0xffffffffu) break;  // no candidate left
+      const uint32_t lmin = __reduce_min_sync(0xffffffffu, hi == hmin ? lo : 0xffffffffu);
+      const uint32_t win = __ballot_sync(0xffffffffu, mq >= 0 && hi == hmin && lo == lmin);
+      if (lane == __ffs(win) - 1) {
+        const int32_t shift = (int32_t)lo - kShiftBias;
+        out[got] = make_int3((int32_t)hi, shift, shift + (int32_t)tmin[lane + 32 * mq]);
+        cand &= ~(1u << mq);
+      }
+      ++got;
+    }
+    if (lane == 0) a.nbest[sid] = got;
+    account(a, lane, L, nq, post, got);
+    __syncwarp();  // the table is cleared for the next strand
+  }
+}
+
+// The sort path over the strands of a.big_list (between kHashCap and
 // kSortCap hits); warps stride over the list, whose length is on the device.
-template <int CAP>
+template <int CAP, int KM>
 __global__ void __launch_bounds__(kSeedWarps * 32, 6) seed_sort_kernel(SeedArgs a) {
   // the sort pads n <= CAP keys to the next power of two, which must fit
   static_assert(CAP >= 32 && (CAP & (CAP - 1)) == 0, "CAP must be a power of two");
@@ -235,27 +354,27 @@ __global__ void __launch_bounds__(kSeedWarps * 32, 6) seed_sort_kernel(SeedArgs 
   __shared__ __align__(16) WarpSmem smem[kSeedWarps];
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   uint64_t* keys = keys_all[wib];
-  const int64_t n_list = *a.n_mid;
+  const int64_t n_list = *a.n_big;
   for (int64_t t = (int64_t)blockIdx.x * kSeedWarps + wib; t < n_list;
        t += (int64_t)gridDim.x * kSeedWarps) {
-    const int64_t sid = a.mid_list[t];
+    const int64_t sid = a.big_list[t];
     const DevRead rd = a.rd[sid >> 1];
     const int strand = (int)(sid & 1);
     const int L = rd.len, nq = strand_nq(a, L);
     const int M = (nq + 31) >> 5;
-    uint32_t beg[kM], cnt[kM];
-    const uint32_t my = strand_lookups(a, rd, strand, L, nq, M, smem[wib], lane, beg, cnt);
+    uint32_t beg[KM], cnt[KM];
+    const uint32_t my = strand_lookups<KM>(a, rd, strand, L, nq, M, smem[wib], lane, beg, cnt);
     uint32_t incl = my;
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
       const uint32_t o = __shfl_up_sync(0xffffffffu, incl, d);
       if (lane >= d) incl += o;
     }
-    const uint32_t n = __shfl_sync(0xffffffffu, incl, 31);  // in (kFastHits, CAP]
-    const uint32_t post = __reduce_add_sync(0xffffffffu, posting_sectors(cnt));
+    const uint32_t n = __shfl_sync(0xffffffffu, incl, 31);  // in (kHashCap, CAP]
+    const uint32_t post = __reduce_add_sync(0xffffffffu, posting_sectors<KM>(cnt));
     uint32_t pos = incl - my;
 #pragma unroll
-    for (int m = 0; m < kM; ++m) {
+    for (int m = 0; m < KM; ++m) {
       const int i = lane * M + m;
       for (uint32_t j = 0; j < cnt[m]; ++j) {
         const uint2 p = __ldg(&a.postings[beg[m] + j]);
@@ -441,19 +560,37 @@ __global__ void __launch_bounds__(kOvThreads) seed_overflow_kernel(SeedArgs a,
 
 }  // namespace
 
-void launch_seed(cudaStream_t st, const SeedArgs& a) {
+template <int KM>
+void launch_seed_km(cudaStream_t st, const SeedArgs& a) {
   const int64_t strands = 2 * a.n_reads;
-  if (strands == 0) return;
   const unsigned grid = (unsigned)((strands + kSeedWarps - 1) / kSeedWarps);
-  seed_fast_kernel<<<grid, kSeedWarps * 32, 0, st>>>(a);
-  // the sort path over the listed strands: a grid of a few waves strides
-  // over the list (its length is on the device)
+  seed_fast_kernel<KM><<<grid, kSeedWarps * 32, 0, st>>>(a);
+  // the listed strands: grids of a few waves stride over the lists (their
+  // lengths are on the device)
   int dev = 0, sms = 0;
-  int64_t blocks = (strands + kSeedWarps - 1) / kSeedWarps;
+  int64_t cap = 1 << 20;
   if (cudaGetDevice(&dev) == cudaSuccess &&
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && sms > 0)
-    blocks = std::min<int64_t>(blocks, (int64_t)sms * 6 * 4);
-  seed_sort_kernel<kSortCap><<<(unsigned)blocks, kSeedWarps * 32, 0, st>>>(a);
+    cap = (int64_t)sms * 4 * 4;
+  const int64_t hash_blocks = std::min<int64_t>((strands + kHashWarps - 1) / kHashWarps, 2 * cap);
+  seed_hash_kernel<KM><<<(unsigned)hash_blocks, kHashWarps * 32, 0, st>>>(a);
+  const int64_t sort_blocks = std::min<int64_t>((strands + kSeedWarps - 1) / kSeedWarps, cap);
+  seed_sort_kernel<kSortCap, KM><<<(unsigned)sort_blocks, kSeedWarps * 32, 0, st>>>(a);
+}
+
+void launch_seed(cudaStream_t st, const SeedArgs& a) {
+  if (a.n_reads <= 0) return;
+  // offsets per lane of the longest strand
+  const int nq = (a.fixed_len > 0 ? a.fixed_len : a.max_len) - a.k + 1;
+  const int M = std::max(1, (nq + 31) / 32);
+  if (M <= 3)
+    launch_seed_km<3>(st, a);
+  else if (M <= 5)
+    launch_seed_km<5>(st, a);
+  else if (M <= 7)
+    launch_seed_km<7>(st, a);
+  else
+    launch_seed_km<kM>(st, a);
 }
 
 int seed_smem_cap() { return kSortCap; }

@@ -1,10 +1,19 @@
-// Serving loop: the reference and index stay resident on the device while
-// requests (one reads FASTA each) queue up and run on several concurrent
-// pipelines, each a context with its own stream, so a small request does not
-// wait behind a large one and the device overlaps them.  A request is
-// admitted to a pipeline while the estimated device memory of the requests
-// in flight stays within a budget; results are per request and equal to
-// what swift_align returns for that request alone.
+// Serving loop with continuous batching.  The reference and index stay
+// resident on the device.  Requests (one reads FASTA each) are parsed and
+// checked when they are submitted; workers (a context and stream each) take
+// every queued request of one query-length class, oldest first, up to a
+// read cap and a device-memory budget, and run them as ONE merged wave:
+// one seeding launch over all their reads, one set of Smith-Waterman
+// launches over all their pairs, one formatting pass.  Requests that arrive
+// while a wave runs join the next one; with two or more workers the next
+// wave's host work and launches overlap the running one on the device.
+//
+// Each request keeps what is its own when it runs alone (query length,
+// the stale-read tail of its 16-read loop, its Phase-2 batches), so its
+// records are byte-identical to swift_align on that request alone.
+// Requests of one class share the packed Smith-Waterman shape, so merging
+// them adds no cells: each pair's rows past its own query are the
+// all-mismatch rows the shape computes anyway.
 #include <stdlib.h>
 #include <string.h>
 
@@ -17,7 +26,9 @@
 #include <thread>
 #include <vector>
 
-#include "internal.h"
+#include "handles.h"
+
+using namespace swift;
 
 namespace {
 
@@ -27,19 +38,38 @@ double ms_between(Clock::time_point a, Clock::time_point b) {
   return std::chrono::duration<double, std::milli>(b - a).count();
 }
 
+enum : int { kQueued = 0, kRunning = 1, kDone = 2, kCancelled = 3 };
+
 struct Request {
   int64_t ticket = 0;
   std::vector<char> reads;
-  int64_t n_reads = 0;     // '>' count, for the memory estimate
+  HostReads hr;              // its reads, parsed at submission
+  int32_t Q = 0;             // its query length
+  int cls = 0;               // packed shape class of Q: one class per wave
+  std::vector<int32_t> repeats;
   int64_t est_bytes = 0;
+  int64_t n_reads = 0;
   Clock::time_point submitted, started, finished;
-  bool done = false;
+  int state = kQueued;
   int status = SWIFT_OK;
   std::string error;
-  char* out = nullptr;     // malloc'ed text, handed to the caller
+  char* out = nullptr;       // malloc'ed text, handed to the caller
   size_t out_len = 0;
-  swift_stats stats;
+  double device_ms = 0;      // its wave's device time
+  int64_t wave_requests = 0, wave_reads = 0;
 };
+
+// per worker: its context and pinned staging for the wave's bytes and text
+struct Worker {
+  swift_ctx* ctx = nullptr;
+  char* pin_in = nullptr;
+  size_t pin_in_cap = 0;
+  char* pin_out = nullptr;
+  size_t pin_out_cap = 0;
+};
+
+// Reads per wave at most: bounds a wave's device memory and latency.
+constexpr int64_t kWaveMaxReads = 1 << 18;
 
 }  // namespace
 
@@ -49,7 +79,7 @@ struct swift_server {
   swift_params params;
   int64_t budget = 0;      // device bytes for requests in flight
   int64_t in_flight = 0;
-  std::vector<swift_ctx*> ctxs;
+  std::vector<Worker> workers;
   std::vector<std::thread> threads;
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
@@ -69,52 +99,188 @@ int64_t estimate_bytes(int64_t n_reads, size_t len) {
   return n_reads * (6 * 1600 + 12 * 1024) + 4 * (int64_t)len + (96ll << 20);
 }
 
-void worker(swift_server* s, int w) {
-  swift_ctx* ctx = s->ctxs[w];
+// Page-locked host buffer of at least n bytes (grown, never shrunk).
+bool ensure_pinned(char** buf, size_t* cap, size_t n) {
+  if (*cap >= n && *buf) return true;
+  if (*buf) cudaFreeHost(*buf);
+  *buf = nullptr;
+  *cap = 0;
+  const size_t want = n + n / 4 + (1 << 20);
+  if (cudaHostAlloc((void**)buf, want, cudaHostAllocDefault) != cudaSuccess) {
+    cudaGetLastError();
+    *buf = nullptr;
+    return false;
+  }
+  *cap = want;
+  return true;
+}
+
+// Runs the requests of one wave and fills their results (called without
+// the server lock).
+void run_requests(swift_server* s, Worker& w, const std::vector<Request*>& take) {
+  size_t bytes = 0, n_reads = 0;
+  for (const Request* r : take) {
+    bytes += r->reads.size();
+    n_reads += r->hr.rd.size();
+  }
+  std::vector<DevRead> rd;
+  rd.reserve(n_reads);
+  std::vector<WaveReq> wave(take.size());
+  std::string err;
+  int rc = SWIFT_OK;
+  const char* src = nullptr;
+  std::vector<char> host_bytes;  // if no pinned buffer could be had
+  if (ensure_pinned(&w.pin_in, &w.pin_in_cap, bytes)) {
+    src = w.pin_in;
+  } else {
+    host_bytes.resize(std::max<size_t>(bytes, 1));
+    src = host_bytes.data();
+  }
+  char* dst = const_cast<char*>(src);
+  uint64_t at = 0;
+  for (size_t i = 0; i < take.size(); ++i) {
+    const Request* r = take[i];
+    if (!r->reads.empty()) memcpy(dst + at, r->reads.data(), r->reads.size());
+    WaveReq& q = wave[i];
+    q.read0 = (int64_t)rd.size();
+    q.n = (int64_t)r->hr.rd.size();
+    q.Q = r->Q;
+    for (int32_t x : r->repeats) q.repeats.push_back((int32_t)(q.read0 + x));
+    for (DevRead d : r->hr.rd) {
+      d.name_off += at;
+      d.seq_off += at;
+      rd.push_back(d);
+    }
+    at += r->reads.size();
+  }
+  // the text: about the size of the last wave per read, else a first guess
+  size_t out_len = 0;
+  swift_stats st;
+  memset(&st, 0, sizeof(st));
+  const size_t guess = n_reads * 520 + (1 << 20);
+  ensure_pinned(&w.pin_out, &w.pin_out_cap, std::max(guess, w.pin_out_cap));
+  rc = run_wave(w.ctx, s->idx, &s->params, src, bytes, rd, &wave, w.pin_out,
+                w.pin_out ? w.pin_out_cap : 0, &out_len, &st);
+  if (rc != SWIFT_OK) err = swift_last_error(w.ctx);
+  const char* text = nullptr;
+  std::vector<char> fetched;
+  if (rc == SWIFT_OK) {
+    if (w.pin_out && out_len <= w.pin_out_cap) {
+      text = w.pin_out;
+    } else {  // larger than the staging buffer: fetch it from the device
+      fetched.resize(std::max<size_t>(out_len, 1));
+      rc = swift_fetch_output(w.ctx, fetched.data(), out_len);
+      if (rc != SWIFT_OK) err = swift_last_error(w.ctx);
+      text = fetched.data();
+      ensure_pinned(&w.pin_out, &w.pin_out_cap, out_len);
+    }
+  }
+  const auto now = Clock::now();
+  std::lock_guard<std::mutex> lk(s->mu);
+  for (size_t i = 0; i < take.size(); ++i) {
+    Request* r = take[i];
+    r->finished = now;
+    r->status = rc;
+    r->device_ms = st.total_ms;
+    r->wave_requests = (int64_t)take.size();
+    r->wave_reads = (int64_t)n_reads;
+    if (rc == SWIFT_OK) {
+      const size_t len = (size_t)(wave[i].text1 - wave[i].text0);
+      r->out = (char*)malloc(len + 1);
+      if (!r->out) {
+        r->status = SWIFT_E_NOMEM;
+        r->error = "host output buffer";
+      } else {
+        if (len) memcpy(r->out, text + wave[i].text0, len);
+        r->out[len] = '\0';
+        r->out_len = len;
+      }
+    } else {
+      r->error = err;
+    }
+    r->reads.clear();
+    r->reads.shrink_to_fit();
+    r->hr = HostReads();
+    r->state = kDone;
+    s->in_flight -= r->est_bytes;
+  }
+}
+
+void worker(swift_server* s, int wi) {
+  Worker& w = s->workers[wi];
   for (;;) {
-    Request* r = nullptr;
+    std::vector<Request*> take;
     {
       std::unique_lock<std::mutex> lk(s->mu);
-      // first request that fits the budget (a request larger than the
-      // whole budget runs when nothing else is in flight)
+      // the oldest request decides the wave's class; it starts when it fits
+      // the memory budget beside the waves in flight (a request larger than
+      // the whole budget runs when nothing else is in flight)
       s->cv_work.wait(lk, [&] {
         if (s->stop && s->queue.empty()) return true;
-        for (Request* q : s->queue)
-          if (s->in_flight + q->est_bytes <= s->budget || s->in_flight == 0) return true;
-        return false;
+        if (s->queue.empty()) return false;
+        const Request* f = s->queue.front();
+        return s->in_flight + f->est_bytes <= s->budget || s->in_flight == 0;
       });
       if (s->stop && s->queue.empty()) return;
-      for (auto it = s->queue.begin(); it != s->queue.end(); ++it) {
-        if (s->in_flight + (*it)->est_bytes <= s->budget || s->in_flight == 0) {
-          r = *it;
-          s->queue.erase(it);
-          break;
+      const int cls = s->queue.front()->cls;
+      int64_t reads = 0, est = 0;
+      for (auto it = s->queue.begin(); it != s->queue.end();) {
+        Request* r = *it;
+        const bool first = take.empty();
+        if (r->cls == cls &&
+            (first || (reads + (int64_t)r->hr.rd.size() <= kWaveMaxReads &&
+                       s->in_flight + est + r->est_bytes <= s->budget))) {
+          take.push_back(r);
+          reads += (int64_t)r->hr.rd.size();
+          est += r->est_bytes;
+          it = s->queue.erase(it);
+        } else {
+          ++it;
         }
       }
-      s->in_flight += r->est_bytes;
-      r->started = Clock::now();
+      s->in_flight += est;
+      const auto now = Clock::now();
+      for (Request* r : take) {
+        r->started = now;
+        r->state = kRunning;
+      }
     }
-    char* out = nullptr;
-    size_t n = 0;
-    swift_stats st;
-    memset(&st, 0, sizeof(st));
-    const int rc = swift_align(ctx, s->idx, r->reads.data(), r->reads.size(), &s->params, &out, &n, &st);
-    {
-      std::lock_guard<std::mutex> lk(s->mu);
-      r->finished = Clock::now();
-      r->status = rc;
-      if (rc != SWIFT_OK) r->error = swift_last_error(ctx);
-      r->out = out;
-      r->out_len = n;
-      r->stats = st;
-      r->done = true;
-      r->reads.clear();
-      r->reads.shrink_to_fit();
-      s->in_flight -= r->est_bytes;
-    }
+    run_requests(s, w, take);
     s->cv_done.notify_all();
     s->cv_work.notify_all();
   }
+}
+
+// The checks swift_align makes on a request alone, at submission.
+int admit(const swift_server* s, Request* r) {
+  std::string err;
+  const int limit = read_limit_of(&s->params);
+  int rc = parse_reads_host(r->reads.data(), r->reads.size(), limit, &r->hr, &err);
+  if (rc != SWIFT_OK) {
+    r->error = err;
+    return rc;
+  }
+  const swift_params& p = s->params;
+  const int Q = p.qry_len > 0 ? p.qry_len : r->hr.first_len;
+  if (Q < 1 || Q > kMaxQ) {
+    r->error = "query length outside 1.." + std::to_string(kMaxQ);
+    return SWIFT_E_LIMIT;
+  }
+  if (r->hr.n > 0 && r->hr.min_len < Q) {
+    r->error = "a read is shorter than the query length; the reference aligns such reads "
+               "against stale buffer contents";
+    return SWIFT_E_INPUT;
+  }
+  if (p.seeder == 1 && r->hr.max_len > kReadMax) {
+    r->error = "lt13 seeding takes reads of up to 199 bases";
+    return SWIFT_E_LIMIT;
+  }
+  r->Q = Q;
+  r->n_reads = r->hr.n;
+  r->cls = packed_class(Q);
+  if (p.seeder != 1) r->repeats = phase1_stale_repeats(r->hr.n, r->hr.n_gt);
+  r->est_bytes = estimate_bytes(r->hr.n, r->reads.size());
+  return SWIFT_OK;
 }
 
 }  // namespace
@@ -124,6 +290,10 @@ extern "C" {
 int swift_server_create(int device, const swift_index* idx, const swift_params* p,
                         int32_t workers, int64_t mem_budget, swift_server** out) {
   if (!idx || !p || !out || workers < 1 || workers > 64) return SWIFT_E_ARG;
+  if (p->seed_len != idx->k || p->ignore_thres != idx->thres || p->max_hits < 1 ||
+      p->max_hits > 64 || (p->seeder != 0 && p->seeder != 1) || p->max_read_len < 0 ||
+      p->max_read_len > kSeedReadMax)
+    return SWIFT_E_ARG;
   if (cudaSetDevice(device) != cudaSuccess) return SWIFT_E_CUDA;
   swift_server* s = new swift_server();
   s->device = device;
@@ -138,15 +308,17 @@ int swift_server_create(int device, const swift_index* idx, const swift_params* 
     mem_budget = (int64_t)(fr / 2);
   }
   s->budget = mem_budget;
+  s->workers.resize(workers);
   for (int w = 0; w < workers; ++w) {
     swift_ctx* c = nullptr;
     const int rc = swift_ctx_create(device, nullptr, &c);
     if (rc != SWIFT_OK) {
-      for (swift_ctx* x : s->ctxs) swift_ctx_destroy(x);
+      for (Worker& x : s->workers)
+        if (x.ctx) swift_ctx_destroy(x.ctx);
       delete s;
       return rc;
     }
-    s->ctxs.push_back(c);
+    s->workers[w].ctx = c;
   }
   for (int w = 0; w < workers; ++w) s->threads.emplace_back(worker, s, w);
   *out = s;
@@ -157,11 +329,8 @@ int swift_server_submit(swift_server* s, const char* reads, size_t len, int64_t*
   if (!s || (!reads && len) || !ticket) return SWIFT_E_ARG;
   Request* r = new Request();
   r->reads.assign(reads, reads + len);
-  int64_t n = 0;
-  for (size_t i = 0; i < len; ++i) n += reads[i] == '>';
-  r->n_reads = n;
-  r->est_bytes = estimate_bytes(n, len);
   r->submitted = Clock::now();
+  const int rc = admit(s, r);
   {
     std::lock_guard<std::mutex> lk(s->mu);
     if (s->stop) {
@@ -170,10 +339,51 @@ int swift_server_submit(swift_server* s, const char* reads, size_t len, int64_t*
     }
     r->ticket = s->next_ticket++;
     s->all[r->ticket] = r;
-    s->queue.push_back(r);
     *ticket = r->ticket;
+    if (rc != SWIFT_OK) {  // fails alone, at once
+      r->status = rc;
+      r->state = kDone;
+      r->started = r->finished = r->submitted;
+    } else {
+      s->queue.push_back(r);
+    }
   }
-  s->cv_work.notify_one();
+  if (rc != SWIFT_OK)
+    s->cv_done.notify_all();
+  else
+    s->cv_work.notify_all();
+  return SWIFT_OK;
+}
+
+int swift_server_poll(swift_server* s, int64_t ticket, int32_t* state) {
+  if (!s || !state) return SWIFT_E_ARG;
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->all.find(ticket);
+  if (it == s->all.end()) return SWIFT_E_ARG;
+  *state = it->second->state;
+  return SWIFT_OK;
+}
+
+int swift_server_cancel(swift_server* s, int64_t ticket) {
+  if (!s) return SWIFT_E_ARG;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->all.find(ticket);
+    if (it == s->all.end()) return SWIFT_E_ARG;
+    Request* r = it->second;
+    if (r->state != kQueued) return SWIFT_E_LIMIT;  // running or done: too late
+    for (auto q = s->queue.begin(); q != s->queue.end(); ++q)
+      if (*q == r) {
+        s->queue.erase(q);
+        break;
+      }
+    r->state = kCancelled;
+    r->status = SWIFT_E_CANCELLED;
+    r->error = "request cancelled before it started";
+    r->started = r->finished = Clock::now();
+  }
+  s->cv_done.notify_all();
+  s->cv_work.notify_all();  // the queue's head may have changed
   return SWIFT_OK;
 }
 
@@ -186,7 +396,7 @@ int swift_server_wait(swift_server* s, int64_t ticket, char** out, size_t* out_l
     auto it = s->all.find(ticket);
     if (it == s->all.end()) return SWIFT_E_ARG;
     r = it->second;
-    s->cv_done.wait(lk, [&] { return r->done; });
+    s->cv_done.wait(lk, [&] { return r->state == kDone || r->state == kCancelled; });
     s->all.erase(it);
   }
   *out = r->out;
@@ -196,9 +406,11 @@ int swift_server_wait(swift_server* s, int64_t ticket, char** out, size_t* out_l
     st->queue_ms = ms_between(r->submitted, r->started);
     st->run_ms = ms_between(r->started, r->finished);
     st->total_ms = ms_between(r->submitted, r->finished);
-    st->reads = r->stats.reads;
+    st->reads = r->n_reads;
     st->out_bytes = (int64_t)r->out_len;
-    st->device_ms = r->stats.total_ms;
+    st->device_ms = r->device_ms;
+    st->wave_requests = r->wave_requests;
+    st->wave_reads = r->wave_reads;
   }
   if (err && err_cap) {
     strncpy(err, r->error.c_str(), err_cap - 1);
@@ -221,7 +433,11 @@ int swift_server_destroy(swift_server* s) {
     free(kv.second->out);
     delete kv.second;
   }
-  for (swift_ctx* c : s->ctxs) swift_ctx_destroy(c);
+  for (Worker& w : s->workers) {
+    if (w.ctx) swift_ctx_destroy(w.ctx);
+    if (w.pin_in) cudaFreeHost(w.pin_in);
+    if (w.pin_out) cudaFreeHost(w.pin_out);
+  }
   delete s;
   return SWIFT_OK;
 }

@@ -46,6 +46,8 @@
 // other pairs take sw.cu): query and window bytes in {A,C,G,T,a,c,g,t},
 // window length = R, mismatch, gap_open, gap_ext < 0, gap_ext >= gap_open,
 // |16*score+4| < 128, 16 * match * Q + B stays below 0x7C00.
+#include <string.h>
+
 #include <type_traits>
 #include "internal.h"
 
@@ -197,7 +199,7 @@ __device__ __forceinline__ void packed_item(const FastArgs& a, const int64_t war
         if (TRACE) {
           // first maximum of the row: the key's tag makes an earlier step of
           // the window win a tie, and the window's last best keeps tag 15
-          const uint32_t key = VAR ? (h16 + tag) & cm : h16 + tag;
+          const uint32_t key = VAR && var_r ? (h16 + tag) & cm : h16 + tag;
           bestv[k] = __vimax_s16x2_relu(bestv[k], key);  // both non-negative
           // bits 1 (UP) and 2 (DIAG) of each half's code to 2 * (k & 7): a
           // mask, then a multiply-add (the rows' fields do not overlap), which
@@ -552,19 +554,56 @@ __global__ void __launch_bounds__(256) sw_walk_kernel(FastArgs a) {
   const char* wg = a.w + (int64_t)p * a.w_stride;
   const int W = (a.r_len ? a.r_len[p] : R) + 1;  // the pair's own window for cell indices
   const int shift_half = 16 * hp;
-  // the direction word last read: consecutive cells of a walk mostly share
-  // it or sit next to it
-  int64_t last = -1;
-  uint32_t word = 0;
+  // The walk moves to lower addresses one step (kNW words) per diagonal
+  // move inside a lane's rows: the direction words are kept as three
+  // 16-byte blocks in registers, the one holding the cell's word and the two
+  // before it, so one round of loads serves several steps instead of one
+  // dependent load per step.  (The group's region starts 16-byte aligned and
+  // holds at least 16 blocks; blocks below its start are never read.)
+  const uint4* dirs4 = reinterpret_cast<const uint4*>(dirs);
+  int64_t blk = -16;  // first cached block
+  uint4 c0 = make_uint4(0, 0, 0, 0), c1 = c0, c2 = c0;
+  auto pick = [](const uint4& v, int w) -> uint32_t {
+    return w == 0 ? v.x : w == 1 ? v.y : w == 2 ? v.z : v.w;
+  };
   // 2 DIAG, 1 UP, 0 LEFT or NONE
   auto code_at = [&](int i, int jj) -> uint32_t {
     const int ln = (i - 1) / RPL, k = (i - 1) % RPL;
     const int64_t at = ((int64_t)ln * S8 + (jj + ln - 1)) * kNW + (k >> 3);
-    if (at != last) {
-      word = __ldcg(&dirs[at]);
-      last = at;
+    const int64_t b = at >> 2;
+    if (b < blk || b > blk + 2) {
+      blk = b >= 2 ? b - 2 : 0;
+      c0 = __ldg(dirs4 + blk);
+      c1 = __ldg(dirs4 + blk + 1);
+      c2 = __ldg(dirs4 + blk + 2);
     }
+    const int o = (int)(b - blk), w = (int)(at & 3);
+    const uint32_t word = o == 0 ? pick(c0, w) : o == 1 ? pick(c1, w) : pick(c2, w);
     return (word >> (shift_half + 2 * (k & 7))) & 3u;
+  };
+  // query and window bytes in 16-byte blocks too (rows start 16-byte
+  // aligned, strides are multiples of 16)
+  const bool blocks16 = ((a.q_stride | a.w_stride) & 15) == 0;
+  int qb = -1, wb = -1;
+  uint4 q16 = make_uint4(0, 0, 0, 0), w16 = q16;
+  auto byte_of = [&](const uint4& v, int o) -> char {
+    return (char)((pick(v, o >> 2) >> (8 * (o & 3))) & 0xFFu);
+  };
+  auto qbyte = [&](int i) -> char {
+    if (!blocks16) return qg[i];
+    if ((i >> 4) != qb) {
+      qb = i >> 4;
+      q16 = __ldg(reinterpret_cast<const uint4*>(qg) + qb);
+    }
+    return byte_of(q16, i & 15);
+  };
+  auto wbyte = [&](int i) -> char {
+    if (!blocks16) return wg[i];
+    if ((i >> 4) != wb) {
+      wb = i >> 4;
+      w16 = __ldg(reinterpret_cast<const uint4*>(wg) + wb);
+    }
+    return byte_of(w16, i & 15);
   };
   // consensus bytes are gathered four at a time and stored as words
   // (consensus strings are optional: coordinates only when qcons is null)
@@ -609,7 +648,7 @@ __global__ void __launch_bounds__(256) sw_walk_kernel(FastArgs a) {
     }
     const uint32_t pc = (nr == 0 || nc == 0) ? 0u : code_at(nr, nc);
     if (d == kDiag) {
-      const char qc = upc(qg[cr - 1]), rc = upc(wg[cc - 1]);
+      const char qc = upc(qbyte(cr - 1)), rc = upc(wbyte(cc - 1));
       const int sub = (qc == rc || qc == 'N' || rc == 'N') ? m : x;
       nh = h - sub;
     } else {
@@ -624,8 +663,8 @@ __global__ void __launch_bounds__(256) sw_walk_kernel(FastArgs a) {
   while ((cr != nr || cc != nc) && nc != 0 && nr != 0) {
     ++tick;
     char rch = '-';
-    if (nc != cc) { rch = wg[cc - 1]; ++nref; }
-    emit(tick, rch, nr == cr ? '-' : qg[cr - 1]);
+    if (nc != cc) { rch = wbyte(cc - 1); ++nref; }
+    emit(tick, rch, nr == cr ? '-' : qbyte(cr - 1));
     start = cc;
     cr = nr; cc = nc; h = nh; d = nd;
     if (d == kNone) break;
@@ -634,8 +673,8 @@ __global__ void __launch_bounds__(256) sw_walk_kernel(FastArgs a) {
   if ((cr != nr || cc != nc) && (nc == 0 || nr == 0)) {
     ++tick;
     char rch = '-';
-    if (nc != cc) { rch = wg[cc - 1]; ++nref; }
-    emit(tick, rch, nr == cr ? '-' : qg[cr - 1]);
+    if (nc != cc) { rch = wbyte(cc - 1); ++nref; }
+    emit(tick, rch, nr == cr ? '-' : qbyte(cr - 1));
     start = cc;
   }
   if (cons && tick >= 0 && (tick & 3) != 3) {
@@ -666,9 +705,25 @@ Shape shape_for(int Q) {
   return {0, 0};
 }
 
+// the compiled (lanes, rows per lane) shapes of the exact passes
+constexpr Shape kShapes[] = {{8, 4}, {4, 8}, {8, 8}, {4, 16}, {8, 13}, {8, 16},
+                             {16, 8}, {16, 13}, {16, 16}, {32, 7}, {32, 10}};
+constexpr int kNumShapes = (int)(sizeof(kShapes) / sizeof(kShapes[0]));
+
+// The launch's shape: a.shape when set (it must cover a.Q), else the
+// default for a.Q.
+Shape shape_of(const FastArgs& a) {
+  if (a.shape_g > 0) {
+    for (const Shape& c : kShapes)
+      if (c.G == a.shape_g && c.RPL == a.shape_rpl && c.G * c.RPL >= a.Q) return c;
+    return {0, 0};
+  }
+  return shape_for(a.Q);
+}
+
 template <bool TRACE, bool VAR>
 int launch_shape(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {
-  const Shape s = shape_for(a.Q);
+  const Shape s = shape_of(a);
   if (s.G == 0 || max_pairs <= 0) return 0;
   const int pairs_per_warp = 2 * (32 / s.G);
   const int64_t warps = (max_pairs + pairs_per_warp - 1) / pairs_per_warp;
@@ -685,11 +740,15 @@ int launch_shape(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {
     return 1;                                                              \
   }
   SWIFT_PK(8, 4)
+  SWIFT_PK(4, 8)
   SWIFT_PK(8, 8)
+  SWIFT_PK(4, 16)
   SWIFT_PK(8, 13)
   SWIFT_PK(8, 16)
+  SWIFT_PK(16, 8)
   SWIFT_PK(16, 13)
   SWIFT_PK(16, 16)
+  SWIFT_PK(32, 7)
   SWIFT_PK(32, 10)
 #undef SWIFT_PK
   return 0;
@@ -739,7 +798,7 @@ int launch_bound(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {
 }
 
 int launch_walk(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {
-  const Shape s = shape_for(a.Q);
+  const Shape s = shape_of(a);
   if (s.G == 0 || max_pairs <= 0) return 0;
   const unsigned grid = (unsigned)((max_pairs + 255) / 256);
 #define SWIFT_WK(G_, R_)                                      \
@@ -748,11 +807,15 @@ int launch_walk(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {
     return 1;                                                  \
   }
   SWIFT_WK(8, 4)
+  SWIFT_WK(4, 8)
   SWIFT_WK(8, 8)
+  SWIFT_WK(4, 16)
   SWIFT_WK(8, 13)
   SWIFT_WK(8, 16)
+  SWIFT_WK(16, 8)
   SWIFT_WK(16, 13)
   SWIFT_WK(16, 16)
+  SWIFT_WK(32, 7)
   SWIFT_WK(32, 10)
 #undef SWIFT_WK
   return 0;
@@ -772,11 +835,35 @@ bool fast_params_ok(int Q, int R, int m, int x, int o, int e, int* bias) {
   return true;
 }
 
-int64_t trace_scratch_words(int Q, int R, int64_t pairs) {
-  const Shape s = shape_for(Q);
+int64_t trace_scratch_words(int Q, int R, int64_t pairs, int shape_g, int shape_rpl) {
+  FastArgs a;
+  memset(&a, 0, sizeof(a));
+  a.Q = Q;
+  a.shape_g = shape_g;
+  a.shape_rpl = shape_rpl;
+  const Shape s = shape_of(a);
   if (s.G == 0) return 0;
   const int64_t groups = (pairs + 1) / 2 + 32;  // round up to whole warps
   return groups * (int64_t)s.G * ((s.RPL + 7) / 8) * steps8(R, s.G);
+}
+
+int packed_shape_candidates(int Q, int32_t* g, int32_t* rpl, int cap) {
+  // the default, then the other shapes covering Q without more than about
+  // twice its rows
+  const Shape d = shape_for(Q);
+  if (d.G == 0 || cap < 1) return 0;
+  int n = 0;
+  g[n] = d.G;
+  rpl[n] = d.RPL;
+  ++n;
+  for (const Shape& c : kShapes)
+    if (c.G * c.RPL >= Q && c.G * c.RPL <= 2 * Q + 32 && !(c.G == d.G && c.RPL == d.RPL) &&
+        n < cap) {
+      g[n] = c.G;
+      rpl[n] = c.RPL;
+      ++n;
+    }
+  return n;
 }
 
 int launch_sw_score(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {

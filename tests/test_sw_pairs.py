@@ -156,6 +156,41 @@ def test_pairs_batched_workload_vs_oracle(ctx, oracle):
         assert np.array_equal(plain[k], res[k]), k
 
 
+def test_pairs_every_shape_and_autotuner_agree(ctx, oracle, sg):
+    # every (lanes, rows per lane) candidate of each query class, and the
+    # autotuner's choice, give the default shapes' results exactly
+    from swift_gb300 import synth
+    _, seqs = synth.make_reference(2_000_000, 3, sigma=0.5, repeat_frac=0.1, seed=43)
+    ref, reads, qo, ql, ro, rl = synth.pairs_workload(700, seed=44, ref=seqs)
+    c2 = sg.Context(0)
+    try:
+        c2.set_tuning(0)
+        base, _ = c2.sw_pairs(reads, qo, ql, ref, ro, rl)
+        seen = set()
+        for k in range(2, 2 + 12):
+            c2.set_tuning(k)
+            res, st = c2.sw_pairs(reads, qo, ql, ref, ro, rl)
+            seen |= {(q, s) for q, s in st["shapes"].items()}
+            for key in ("score", "start", "end", "len", "qcons", "rcons"):
+                assert res[key] == base[key] if key in ("qcons", "rcons") else \
+                    np.array_equal(res[key], base[key]), (k, key)
+        assert len(seen) > 7  # more than one shape per class ran
+        c2.set_tuning(1)
+        res, st = c2.sw_pairs(reads, qo, ql, ref, ro, rl)
+        assert st["tune_ms"] > 0 and st["shapes"]
+        for key in ("score", "start", "end", "len"):
+            assert np.array_equal(res[key], base[key]), key
+        res2, st2 = c2.sw_pairs(reads, qo, ql, ref, ro, rl)  # choices kept
+        assert st2["tune_ms"] == 0 and st2["shapes"] == st["shapes"]
+    finally:
+        c2.close()
+    rng = random.Random(45)
+    pick = rng.sample(range(len(ql)), 300)
+    sub = {k: np.asarray(base[k])[pick] for k in ("score", "start", "end", "len")}
+    check_against_oracle(sub, [reads[qo[i]:qo[i] + ql[i]] for i in pick],
+                         [ref[ro[i]:ro[i] + rl[i]] for i in pick], oracle, (2, -1, -10, -1))
+
+
 def test_long_pairs_vs_oracle(ctx, oracle):
     # long queries and windows (the long-region shapes: queries to 4000,
     # windows to 8000) next to short pairs in one call
