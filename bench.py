@@ -73,6 +73,8 @@ def parse_args():
     ap.add_argument("--reads", type=int, default=None)
     ap.add_argument("--cpu-sample", type=int, default=20000)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--serve-workers", type=int, default=2,
+                    help="serving: concurrent wave pipelines")
     ap.add_argument("--no-configs", action="store_true",
                     help="skip the short runs of the batched, long-region and serving "
                          "configurations that the default line carries")
@@ -400,9 +402,9 @@ def serving_run(idx, device, seqs, pool_size=120, per_load=200, loads=(0.8,), se
             srv.wait(srv.submit(r))
         t0 = time.perf_counter()
         tickets = [srv.submit(r) for _, r in pool]
-        for t in tickets:
-            srv.wait(t)
+        sat_st = [srv.wait(t)[1] for t in tickets]
         sat_s = time.perf_counter() - t0
+        sat_waves = [x["wave_requests"] for x in sat_st]
         total_reads = sum(n for n, _ in pool)
         sat_rps = total_reads / sat_s
         mean_reads = total_reads / len(pool)
@@ -421,18 +423,26 @@ def serving_run(idx, device, seqs, pool_size=120, per_load=200, loads=(0.8,), se
                 if due > now:
                     time.sleep(due - now)
                 tks.append((srv.submit(pool[k][1]), pool[k][0]))
+            waves = []
             for t, n in tks:
                 _, st = srv.wait(t)
                 lat.append(st["total_ms"])
+                waves.append(st["wave_requests"])
                 done_reads += n
             el = time.perf_counter() - start
             out.append({"offered_fraction": frac, "offered_reads_per_s": frac * sat_rps,
                         "achieved_reads_per_s": done_reads / el, "requests": per_load,
                         "p50_ms": float(np.percentile(lat, 50)),
-                        "p99_ms": float(np.percentile(lat, 99))})
+                        "p99_ms": float(np.percentile(lat, 99)),
+                        "mean_requests_per_wave": float(np.mean(waves))})
     finally:
         srv.close()
     return {"saturation_reads_per_s": sat_rps, "saturation_s": sat_s, "pool_requests": pool_size,
+            "saturation_mean_requests_per_wave": float(np.mean(sat_waves)),
+            "saturation_host_ms": {  # per request: its parse, its wave's pipeline call
+                "parse_median": float(np.median([x["parse_ms"] for x in sat_st])),
+                "wave_median": float(np.median([x["wave_ms"] for x in sat_st])),
+                "device_median": float(np.median([x["device_ms"] for x in sat_st]))},
             "mean_reads_per_request": mean_reads, "workers": workers,
             "read_length": "U[50, %d] per request" % SERVE_MAX_READ, "latency": out}
 
@@ -451,7 +461,7 @@ def bench_serving(args, rank, world, local):
     idx = ctx.index(synth.fasta_bytes(names, seqs))
     with ClockSampler(local) as clk:
         res = serving_run(idx, local, seqs, pool_size=240, per_load=500,
-                          loads=(0.3, 0.6, 0.8, 0.9), seed=3 + rank)
+                          loads=(0.3, 0.6, 0.8, 0.9), seed=3 + rank, workers=args.serve_workers)
     if rank == 0:
         print(json.dumps({
             "metric": "serving reads/s at saturation; p50/p99 request latency under Poisson load",
@@ -463,7 +473,9 @@ def bench_serving(args, rank, world, local):
                        "log-uniform [1, 10000] reads (mean %.0f), read length %s"
                        % (res["pool_requests"], res["mean_reads_per_request"],
                           res["read_length"])},
-            "latency": res["latency"], "clocks": clk.summary(),
+            "latency": res["latency"], "workers": res["workers"],
+            "saturation_mean_requests_per_wave": res["saturation_mean_requests_per_wave"],
+            "saturation_host_ms": res["saturation_host_ms"], "clocks": clk.summary(),
         }))
     return 0
 
@@ -768,7 +780,7 @@ def main():
         sk_ms = statistics.median(s["seed_kernel_ms"] for s in stats)
         hbm, hbm_src = hbm_peak()
         ach = last["seed_model_bytes"] / (sk_ms * 1e-3) / 1e9
-        seed_rf = {"bound": "hbm", "kernel": "seed_fast_kernel + seed_sort_kernel",
+        seed_rf = {"bound": "hbm", "kernel": "seed_fast_kernel + seed_hash_kernel + seed_overflow_kernel",
                    "model_bytes": last["seed_model_bytes"], "kernel_ms": sk_ms,
                    "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
                    "peak_source": hbm_src + " HBM copy bandwidth",

@@ -341,8 +341,9 @@ int swift_align_files(swift_ctx *ctx, const char *qry_path, const char *ref_path
  * their pairs); requests that arrive meanwhile join the next wave.  A wave
  * starts when its estimated device memory fits within mem_budget bytes
  * beside the waves in flight (0: half of the free memory at creation); a
- * request larger than the budget runs alone.  Requests are parsed and
- * checked at submission (reads up to p->max_read_len bases); each result is
+ * request larger than the budget runs alone.  A request is parsed and
+ * checked by the worker that takes it (reads up to p->max_read_len bases);
+ * one that fails finishes at once with swift_align's error; each result is
  * byte-identical to swift_align on that request alone. */
 typedef struct swift_server swift_server;
 typedef struct {
@@ -353,11 +354,13 @@ typedef struct {
   int64_t reads, out_bytes;
   int64_t wave_requests;  /* requests of its wave                             */
   int64_t wave_reads;     /* reads of its wave                                */
+  double parse_ms;        /* host time parsing and checking its reads         */
+  double wave_ms;         /* host time of its wave's pipeline call, from the
+                             upload of the reads to the text on the host      */
 } swift_request_stats;
 int swift_server_create(int device, const swift_index *idx, const swift_params *p,
                         int32_t workers, int64_t mem_budget, swift_server **out);
-/* Queues a copy of the reads; *ticket identifies the request.  A request
- * that fails its checks is done at once with that error. */
+/* Queues a copy of the reads; *ticket identifies the request. */
 int swift_server_submit(swift_server *s, const char *reads_fasta, size_t len, int64_t *ticket);
 /* Non-blocking state of a request: SWIFT_SERVE_QUEUED, _RUNNING, _DONE (its
  * result waits for swift_server_wait) or _CANCELLED; SWIFT_E_ARG for an

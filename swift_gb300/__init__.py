@@ -71,7 +71,8 @@ class PairsStats(C.Structure):
 class RequestStats(C.Structure):
     _fields_ = [("queue_ms", C.c_double), ("run_ms", C.c_double), ("total_ms", C.c_double),
                 ("device_ms", C.c_double), ("reads", C.c_int64), ("out_bytes", C.c_int64),
-                ("wave_requests", C.c_int64), ("wave_reads", C.c_int64)]
+                ("wave_requests", C.c_int64), ("wave_reads", C.c_int64),
+                ("parse_ms", C.c_double), ("wave_ms", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -159,20 +159,30 @@ int parse_reads_host(const char* b, size_t n, int max_read, HostReads* out, std:
   int32_t mn = INT32_MAX, mx = 0;
   uint64_t line_start = 0, prev_start = 0;  // this line's and the previous line's start
   int64_t li = 0;
-  char prev = '\n';
   const uint64_t n_nl = (uint64_t)std::count(b, b + n, '\n');
   const uint64_t n_lines = n_nl + ((n > 0 && b[n - 1] != '\n') ? 1 : 0);
   uint64_t pos = 0;
   while (li < (int64_t)n_lines) {
     const char* nlp = (const char*)memchr(b + pos, '\n', n - pos);
     const uint64_t end = nlp ? (uint64_t)(nlp - b) : n;
-    for (uint64_t i = pos; i < end; ++i) {
+    // eight bytes at a time: a word with no NUL, no byte >= 128 and no '>'
+    // (the line's first byte may be '>') needs no byte-wise look
+    uint64_t i = pos + (pos < end ? 1 : 0);
+    if (pos < end && ((uint8_t)b[pos] == 0 || (uint8_t)b[pos] >= 128))
+      report(pos, kParseBadByte);
+    for (; i + 8 <= end; i += 8) {
+      uint64_t v;
+      memcpy(&v, b + i, 8);
+      const uint64_t k1 = 0x0101010101010101ull, k80 = 0x8080808080808080ull;
+      const uint64_t gt = v ^ 0x3E3E3E3E3E3E3E3Eull;
+      const uint64_t flags = (((v - k1) & ~v) | ((gt - k1) & ~gt) | v) & k80;
+      if (flags) break;  // the byte loop below finds the offending offset
+    }
+    for (; i < end; ++i) {
       const uint8_t x = (uint8_t)b[i];
       if (x == 0 || x >= 128) report(i, kParseBadByte);
-      if (x == '>' && prev != '\n') report(i, kParseGtInLine);
-      prev = (char)x;
+      if (x == '>') report(i, kParseGtInLine);  // not a line's first byte
     }
-    prev = '\n';
     line_start = pos;
     const uint64_t len = end - line_start;
     if (len == 0) {

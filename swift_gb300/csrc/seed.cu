@@ -18,9 +18,9 @@
 //     lanes whose (refIdx, shift) match (__match_any_sync), the biggest size
 //     is a warp max, a cluster's first hit is its lowest lane, and the first
 //     max_hits clusters in key order come from warp minima: no sort at all;
-//   - up to 512 hits: the strand goes to a list for the sort kernel, which
-//     writes 64-bit keys  refIdx << 41 | (shift + 512) << 9 | i  into shared
-//     memory, sorts them (bitonic) and finds run lengths with ballots;
+//   - up to 512 hits: the strand goes to a list for a hash-table kernel
+//     (a table of up to 256 or 1024 slots per warp in shared memory), which
+//     counts the clusters without a sort;
 //   - more: a per-strand hash table in global scratch (one CTA each).
 //
 // Both warp kernels also add up the strand's bytes under the sector model of
@@ -35,10 +35,8 @@ namespace {
 constexpr int kSeedWarps = 8;          // warps per block
 constexpr int kShiftBias = 512;        // shift >= -(kSeedReadMax - 1) always
 constexpr int kFastHits = 32;          // hits of the sort-free path
-constexpr int kHashCap = 256;          // hits of the hash-table path
-constexpr int kHashSlots = 512;        // its table slots per warp (load <= 1/2)
-constexpr int kHashWarps = 4;          // warps per block of the hash-table path
-constexpr int kSortCap = 512;          // hits of the sort path
+constexpr int kMidCap = 128;           // hits of the small hash-table path
+constexpr int kBigCap = 512;           // hits of the large hash-table path
 
 __device__ __forceinline__ uint8_t fwd_code(uint8_t c) {
   uint32_t u = c & 0xDFu;
@@ -178,16 +176,16 @@ __global__ void __launch_bounds__(kSeedWarps * 32) seed_fast_kernel(SeedArgs a) 
   if (n > (uint32_t)kFastHits) {
     // the hash-table, sort or overflow kernel takes the strand
     if (lane == 0) {
-      if (n > (uint32_t)kSortCap) {
+      if (n > (uint32_t)kBigCap) {
         a.overflow_list[atomicAdd(a.n_overflow, 1)] = (int32_t)sid;
         a.nbest[sid] = -(int32_t)n;  // hit count, for sizing the overflow table
-      } else if (n > (uint32_t)kHashCap) {
+      } else if (n > (uint32_t)kMidCap) {
         a.big_list[atomicAdd(a.n_big, 1)] = (int32_t)sid;
       } else {
         a.mid_list[atomicAdd(a.n_mid, 1)] = (int32_t)sid;
       }
     }
-    if (n > (uint32_t)kSortCap) account(a, lane, L, nq, 0, 0);  // its lookups
+    if (n > (uint32_t)kBigCap) account(a, lane, L, nq, 0, 0);  // its lookups
     return;
   }
   const uint32_t post = __reduce_add_sync(0xffffffffu, posting_sectors<KM>(cnt));
@@ -243,121 +241,45 @@ __global__ void __launch_bounds__(kSeedWarps * 32) seed_fast_kernel(SeedArgs a) 
   account(a, lane, L, nq, post, got);
 }
 
-// The strands of a.mid_list (between kFastHits and kHashCap hits), without a
-// sort: every hit enters a per-warp open-addressing table over its cluster
-// key (refIdx, shift + bias) that counts the cluster and keeps its smallest
-// query offset; the biggest count is a warp max over the table, and the
-// first max_hits clusters of that size in key order come from warp minima.
+// The strands of one list (a.mid_list: kFastHits < hits <= kMidCap;
+// a.big_list: kMidCap < hits <= kBigCap), without a sort.  The hits are
+// gathered cooperatively, hit h by lane h mod 32 (each hit's query offset
+// from a per-hit owner array), every posting load of the strand issued
+// before any is used, and kept in registers.  Each hit enters a per-warp
+// open-addressing table over its cluster key (refIdx, shift + bias) that
+// counts the cluster; the biggest count is a warp max over the hits' own
+// counts, and the first max_hits clusters of that size in key order, with
+// each one's smallest query offset, come from warp minima over the hits.
+// A strand's work grows with its hits, not with the table: the table is
+// emptied once per warp and each strand empties only the slots it used.
 // Warps stride over the list, whose length is on the device.
-template <int KM>
-__global__ void __launch_bounds__(kHashWarps * 32) seed_hash_kernel(SeedArgs a) {
+template <int KM, int CAP, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) seed_hash_kernel(SeedArgs a) {
   constexpr unsigned long long kEmpty = ~0ull;  // above every cluster key
-  constexpr int kPerLane = kHashSlots / 32;
-  __shared__ unsigned long long tkey_all[kHashWarps][kHashSlots];
-  __shared__ uint32_t tcnt_all[kHashWarps][kHashSlots];
-  __shared__ uint32_t tmin_all[kHashWarps][kHashSlots];
-  __shared__ __align__(16) WarpSmem smem[kHashWarps];
+  constexpr int kSlots = 2 * CAP;               // a strand takes 2^k >= 1.5 hits + 1
+  constexpr int kRounds = CAP / 32;             // hits per lane at most
+  constexpr int kOffsets = 32 * KM;             // query offsets a strand can have
+  __shared__ unsigned long long tkey_all[WARPS][kSlots];
+  __shared__ uint32_t tcnt_all[WARPS][kSlots];
+  __shared__ uint16_t owner_all[WARPS][CAP];    // hit -> its query offset
+  __shared__ uint32_t off_all[WARPS][kOffsets];  // offset -> first posting - first hit
+  __shared__ __align__(16) WarpSmem smem[WARPS];
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   unsigned long long* tkey = tkey_all[wib];
   uint32_t* tcnt = tcnt_all[wib];
-  uint32_t* tmin = tmin_all[wib];
-  const int64_t n_list = *a.n_mid;
-  for (int64_t t = (int64_t)blockIdx.x * kHashWarps + wib; t < n_list;
-       t += (int64_t)gridDim.x * kHashWarps) {
-    const int64_t sid = a.mid_list[t];
-    const DevRead rd = a.rd[sid >> 1];
-    const int strand = (int)(sid & 1);
-    const int L = rd.len, nq = strand_nq(a, L);
-    const int M = (nq + 31) >> 5;
-    uint32_t beg[KM], cnt[KM];
-    const uint32_t my = strand_lookups<KM>(a, rd, strand, L, nq, M, smem[wib], lane, beg, cnt);
-    const uint32_t n = __reduce_add_sync(0xffffffffu, my);  // in (kFastHits, kHashCap]
-    const uint32_t post = __reduce_add_sync(0xffffffffu, posting_sectors<KM>(cnt));
-    // a power of two at least twice the hits
-    uint32_t T = 64;
-    while (T < 2 * n) T <<= 1;
-    for (uint32_t i = lane; i < T; i += 32) {
-      tkey[i] = kEmpty;
-      tcnt[i] = 0;
-      tmin[i] = 0xffffffffu;
-    }
-    __syncwarp();
-#pragma unroll
-    for (int m = 0; m < KM; ++m) {
-      const uint32_t i = (uint32_t)(lane * M + m);
-      for (uint32_t j = 0; j < cnt[m]; ++j) {
-        const uint2 p = __ldg(&a.postings[beg[m] + j]);
-        const unsigned long long ck =
-            ((unsigned long long)p.y << 32) | (uint32_t)((int32_t)p.x - (int32_t)i + kShiftBias);
-        uint32_t slot = cluster_mix(ck) & (T - 1);
-        for (uint32_t probe = 0; probe < T; ++probe) {  // T > n: a free slot exists
-          const unsigned long long old = atomicCAS(&tkey[slot], kEmpty, ck);
-          if (old == kEmpty || old == ck) {
-            atomicAdd(&tcnt[slot], 1u);
-            atomicMin(&tmin[slot], i);
-            break;
-          }
-          slot = (slot + 1) & (T - 1);
-        }
-      }
-    }
-    __syncwarp();
-    // the biggest cluster, then its clusters as candidate bits of the lane's
-    // slots lane, lane + 32, ...
-    uint32_t big = 0;
-    for (uint32_t i = lane; i < T; i += 32) big = max(big, tcnt[i]);
-    big = __reduce_max_sync(0xffffffffu, big);
-    uint32_t cand = 0;
-#pragma unroll
-    for (int q = 0; q < kPerLane; ++q) {
-      const uint32_t i = lane + 32 * q;
-      if (i < T && tcnt[i] == big) cand |= 1u << q;
-    }
-    int got = 0;
-    int3* out = a.best + sid * a.max_hits;
-    while (got < a.max_hits) {  // the smallest cluster keys first
-      unsigned long long mk = kEmpty;
-      int mq = -1;
-      for (uint32_t c = cand; c; c &= c - 1) {
-        const int q = __ffs(c) - 1;
-        const unsigned long long k = tkey[lane + 32 * q];
-        if (k < mk) {
-          mk = k;
-          mq = q;
-        }
-      }
-      const uint32_t hi = (uint32_t)(mk >> 32), lo = (uint32_t)mk;
-      const uint32_t hmin = __reduce_min_sync(0xffffffffu, hi);
-      if (hmin == 0xffffffffu) break;  // no candidate left
-      const uint32_t lmin = __reduce_min_sync(0xffffffffu, hi == hmin ? lo : 0xffffffffu);
-      const uint32_t win = __ballot_sync(0xffffffffu, mq >= 0 && hi == hmin && lo == lmin);
-      if (lane == __ffs(win) - 1) {
-        const int32_t shift = (int32_t)lo - kShiftBias;
-        out[got] = make_int3((int32_t)hi, shift, shift + (int32_t)tmin[lane + 32 * mq]);
-        cand &= ~(1u << mq);
-      }
-      ++got;
-    }
-    if (lane == 0) a.nbest[sid] = got;
-    account(a, lane, L, nq, post, got);
-    __syncwarp();  // the table is cleared for the next strand
+  uint16_t* owner = owner_all[wib];
+  uint32_t* off = off_all[wib];
+  const bool big = CAP > kMidCap;
+  const int64_t n_list = big ? *a.n_big : *a.n_mid;
+  const int32_t* list = big ? a.big_list : a.mid_list;
+  for (int i = lane; i < kSlots; i += 32) {
+    tkey[i] = kEmpty;
+    tcnt[i] = 0;
   }
-}
-
-// The sort path over the strands of a.big_list (between kHashCap and
-// kSortCap hits); warps stride over the list, whose length is on the device.
-template <int CAP, int KM>
-__global__ void __launch_bounds__(kSeedWarps * 32, 6) seed_sort_kernel(SeedArgs a) {
-  // the sort pads n <= CAP keys to the next power of two, which must fit
-  static_assert(CAP >= 32 && (CAP & (CAP - 1)) == 0, "CAP must be a power of two");
-  __shared__ uint64_t keys_all[kSeedWarps][CAP];
-  __shared__ __align__(16) WarpSmem smem[kSeedWarps];
-  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  uint64_t* keys = keys_all[wib];
-  const int64_t n_list = *a.n_big;
-  for (int64_t t = (int64_t)blockIdx.x * kSeedWarps + wib; t < n_list;
-       t += (int64_t)gridDim.x * kSeedWarps) {
-    const int64_t sid = a.big_list[t];
+  __syncwarp();
+  for (int64_t t = (int64_t)blockIdx.x * WARPS + wib; t < n_list;
+       t += (int64_t)gridDim.x * WARPS) {
+    const int64_t sid = list[t];
     const DevRead rd = a.rd[sid >> 1];
     const int strand = (int)(sid & 1);
     const int L = rd.len, nq = strand_nq(a, L);
@@ -370,94 +292,109 @@ __global__ void __launch_bounds__(kSeedWarps * 32, 6) seed_sort_kernel(SeedArgs 
       const uint32_t o = __shfl_up_sync(0xffffffffu, incl, d);
       if (lane >= d) incl += o;
     }
-    const uint32_t n = __shfl_sync(0xffffffffu, incl, 31);  // in (kHashCap, CAP]
+    const uint32_t n = __shfl_sync(0xffffffffu, incl, 31);  // in the list's range
     const uint32_t post = __reduce_add_sync(0xffffffffu, posting_sectors<KM>(cnt));
+    // hit h (h in [first, first + cnt) of offset i) is posting off[i] + h
     uint32_t pos = incl - my;
 #pragma unroll
     for (int m = 0; m < KM; ++m) {
-      const int i = lane * M + m;
-      for (uint32_t j = 0; j < cnt[m]; ++j) {
-        const uint2 p = __ldg(&a.postings[beg[m] + j]);
-        keys[pos++] = make_key(p.y, (int32_t)p.x - i, i);
+      if (cnt[m]) {
+        const uint32_t i = (uint32_t)(lane * M + m);
+        off[i] = beg[m] - pos;
+        for (uint32_t j = 0; j < cnt[m]; ++j) owner[pos + j] = (uint16_t)i;
+        pos += cnt[m];
       }
     }
-    uint32_t P = 32;
-    while (P < n) P <<= 1;
-    for (uint32_t i = n + lane; i < P; i += 32) keys[i] = ~0ull;
+    uint32_t T = 64;  // table slots of this strand: load <= 2/3
+    while (T < n + n / 2 + 1) T <<= 1;
     __syncwarp();
-    // bitonic sort of keys[0, P)
-    for (uint32_t size = 2; size <= P; size <<= 1) {
-      for (uint32_t stride = size >> 1, ls = __ffs(stride) - 1; stride > 0; stride >>= 1, --ls) {
-        for (uint32_t u = lane; u < P / 2; u += 32) {
-          const uint32_t i = ((u >> ls) << (ls + 1)) | (u & (stride - 1));
-          const uint32_t j = i + stride;
-          const bool asc = (i & size) == 0;
-          const uint64_t x = keys[i], y = keys[j];
-          if ((x > y) == asc) {
-            keys[i] = y;
-            keys[j] = x;
+    uint2 ph[kRounds];
+    uint32_t ih[kRounds], sl[kRounds];
+#pragma unroll
+    for (int r = 0; r < kRounds; ++r) {
+      const uint32_t h = lane + 32 * r;
+      ih[r] = 0;
+      sl[r] = 0;
+      ph[r] = make_uint2(0, 0);
+      if (h < n) {
+        ih[r] = owner[h];
+        ph[r] = __ldg(&a.postings[off[ih[r]] + h]);
+      }
+    }
+    auto key_of = [&](int r) -> unsigned long long {
+      return ((unsigned long long)ph[r].y << 32) |
+             (uint32_t)((int32_t)ph[r].x - (int32_t)ih[r] + kShiftBias);
+    };
+#pragma unroll
+    for (int r = 0; r < kRounds; ++r) {
+      if (lane + 32 * r < n) {
+        const unsigned long long ck = key_of(r);
+        uint32_t slot = cluster_mix(ck) & (T - 1);
+        for (uint32_t probe = 0; probe < T; ++probe) {  // T > n: a free slot exists
+          const unsigned long long old = atomicCAS(&tkey[slot], kEmpty, ck);
+          if (old == kEmpty || old == ck) {
+            atomicAdd(&tcnt[slot], 1u);
+            sl[r] = slot;
+            break;
           }
+          slot = (slot + 1) & (T - 1);
         }
-        __syncwarp();
       }
     }
-    // run lengths at run starts, scanning chunks back to front: the biggest
-    const uint32_t nch = (n + 31) >> 5;
-    auto starts = [&](uint32_t c) {
-      const uint32_t idx = c * 32 + lane;
-      const bool start = idx < n && (idx == 0 || (keys[idx] >> 9) != (keys[idx - 1] >> 9));
-      return __ballot_sync(0xffffffffu, start);
-    };
-    // the run start ending a run that starts at lane `lane` of a chunk whose
-    // starts are bal, if it lies in the same chunk (else 0)
-    auto next_in_chunk = [&](uint32_t c, uint32_t bal) -> uint32_t {
-      const uint32_t above = lane < 31 ? (bal >> (lane + 1)) << (lane + 1) : 0u;
-      return above ? c * 32 + __ffs(above) - 1 : 0u;
-    };
-    uint32_t next = n, biggest = 0;
-    for (int c = (int)nch - 1; c >= 0; --c) {
-      const uint32_t bal = starts(c);
-      if ((bal >> lane) & 1u) {
-        const uint32_t nx = next_in_chunk(c, bal);
-        biggest = max(biggest, (nx ? nx : next) - ((uint32_t)c * 32 + lane));
-      }
-      if (bal) next = (uint32_t)c * 32 + __ffs(bal) - 1;
-    }
-    biggest = __reduce_max_sync(0xffffffffu, biggest);
-    // first max_hits runs of the biggest size, front to back: a chunk's last
-    // run stays open until the next start (or the end) closes it
+    __syncwarp();
+    // the biggest cluster over the hits' own counts; its hits as bits
+    uint32_t bigc = 0;
+#pragma unroll
+    for (int r = 0; r < kRounds; ++r)
+      if (lane + 32 * r < n) bigc = max(bigc, tcnt[sl[r]]);
+    bigc = __reduce_max_sync(0xffffffffu, bigc);
+    uint32_t cand = 0;
+#pragma unroll
+    for (int r = 0; r < kRounds; ++r)
+      if (lane + 32 * r < n && tcnt[sl[r]] == bigc) cand |= 1u << r;
+    // the first max_hits cluster keys of that size, smallest first (every
+    // key is above 0), each with its smallest query offset
     int got = 0;
     int3* out = a.best + sid * a.max_hits;
-    auto emit = [&](uint32_t idx) {  // lane 0; got is warp-uniform
+    unsigned long long last = 0;
+    while (got < a.max_hits) {
+      unsigned long long mk = kEmpty;
+#pragma unroll
+      for (int r = 0; r < kRounds; ++r) {
+        if ((cand >> r) & 1u) {
+          const unsigned long long k = key_of(r);
+          if (k > last && k < mk) mk = k;
+        }
+      }
+      const uint32_t hmin = __reduce_min_sync(0xffffffffu, (uint32_t)(mk >> 32));
+      if (hmin == 0xffffffffu) break;  // no cluster left
+      const uint32_t lmin = __reduce_min_sync(
+          0xffffffffu, (uint32_t)(mk >> 32) == hmin ? (uint32_t)mk : 0xffffffffu);
+      const unsigned long long K = ((unsigned long long)hmin << 32) | lmin;
+      uint32_t mi = 0xffffffffu;
+#pragma unroll
+      for (int r = 0; r < kRounds; ++r)
+        if (((cand >> r) & 1u) && key_of(r) == K) mi = min(mi, ih[r]);
+      mi = __reduce_min_sync(0xffffffffu, mi);
       if (lane == 0) {
-        const uint64_t key = keys[idx];
-        const int32_t ri = (int32_t)(key >> 41);
-        const int32_t shift = (int32_t)((key >> 9) & 0xffffffffu) - kShiftBias;
-        const int32_t i = (int32_t)(key & 0x1ff);
-        out[got] = make_int3(ri, shift, shift + i);
+        const int32_t shift = (int32_t)lmin - kShiftBias;
+        out[got] = make_int3((int32_t)hmin, shift, shift + (int32_t)mi);
       }
+      last = K;
       ++got;
-    };
-    uint32_t open = ~0u;  // start of the run open at the last chunk boundary
-    for (uint32_t c = 0; c < nch && got < a.max_hits; ++c) {
-      const uint32_t bal = starts(c);
-      if (!bal) continue;
-      if (open != ~0u) {
-        if ((uint32_t)(c * 32 + __ffs(bal) - 1) - open == biggest) emit(open);
-        open = ~0u;
-      }
-      const uint32_t nx = next_in_chunk(c, bal);
-      uint32_t hb = __ballot_sync(0xffffffffu, ((bal >> lane) & 1u) && nx && nx - (c * 32 + lane) == biggest);
-      while (hb && got < a.max_hits) {
-        emit(c * 32 + __ffs(hb) - 1);
-        hb &= hb - 1;
-      }
-      open = c * 32 + 31 - __clz(bal);
     }
-    if (open != ~0u && got < a.max_hits && n - open == biggest) emit(open);
     if (lane == 0) a.nbest[sid] = got;
     account(a, lane, L, nq, post, got);
-    __syncwarp();  // keys are rewritten by the next strand
+    __syncwarp();
+    // empty the slots this strand used (owners and offsets are rewritten)
+#pragma unroll
+    for (int r = 0; r < kRounds; ++r) {
+      if (lane + 32 * r < n) {
+        tkey[sl[r]] = kEmpty;
+        tcnt[sl[r]] = 0;
+      }
+    }
+    __syncwarp();
   }
 }
 
@@ -568,14 +505,15 @@ void launch_seed_km(cudaStream_t st, const SeedArgs& a) {
   // the listed strands: grids of a few waves stride over the lists (their
   // lengths are on the device)
   int dev = 0, sms = 0;
-  int64_t cap = 1 << 20;
+  int64_t cap = 1 << 16;
   if (cudaGetDevice(&dev) == cudaSuccess &&
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && sms > 0)
-    cap = (int64_t)sms * 4 * 4;
-  const int64_t hash_blocks = std::min<int64_t>((strands + kHashWarps - 1) / kHashWarps, 2 * cap);
-  seed_hash_kernel<KM><<<(unsigned)hash_blocks, kHashWarps * 32, 0, st>>>(a);
-  const int64_t sort_blocks = std::min<int64_t>((strands + kSeedWarps - 1) / kSeedWarps, cap);
-  seed_sort_kernel<kSortCap, KM><<<(unsigned)sort_blocks, kSeedWarps * 32, 0, st>>>(a);
+    cap = (int64_t)sms * 8;
+  constexpr int kMidWarps = 8, kBigWarps = 3;
+  const int64_t mid_blocks = std::min<int64_t>((strands + kMidWarps - 1) / kMidWarps, 2 * cap);
+  seed_hash_kernel<KM, kMidCap, kMidWarps><<<(unsigned)mid_blocks, kMidWarps * 32, 0, st>>>(a);
+  const int64_t big_blocks = std::min<int64_t>((strands + kBigWarps - 1) / kBigWarps, 2 * cap);
+  seed_hash_kernel<KM, kBigCap, kBigWarps><<<(unsigned)big_blocks, kBigWarps * 32, 0, st>>>(a);
 }
 
 void launch_seed(cudaStream_t st, const SeedArgs& a) {
@@ -593,7 +531,7 @@ void launch_seed(cudaStream_t st, const SeedArgs& a) {
     launch_seed_km<kM>(st, a);
 }
 
-int seed_smem_cap() { return kSortCap; }
+int seed_smem_cap() { return kBigCap; }
 
 void launch_seed_overflow(cudaStream_t st, const SeedArgs& a, int n_overflow,
                           const uint64_t* tab_off, const uint32_t* tab_size) {

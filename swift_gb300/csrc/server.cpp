@@ -1,6 +1,6 @@
 // Serving loop with continuous batching.  The reference and index stay
-// resident on the device.  Requests (one reads FASTA each) are parsed and
-// checked when they are submitted; workers (a context and stream each) take
+// resident on the device.  Requests (one reads FASTA each) are queued as
+// they come; workers (a context and stream each) take
 // every queued request of one query-length class, oldest first, up to a
 // read cap and a device-memory budget, and run them as ONE merged wave:
 // one seeding launch over all their reads, one set of Smith-Waterman
@@ -17,6 +17,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <chrono>
 #include <condition_variable>
 #include <deque>
@@ -43,11 +44,12 @@ enum : int { kQueued = 0, kRunning = 1, kDone = 2, kCancelled = 3 };
 struct Request {
   int64_t ticket = 0;
   std::vector<char> reads;
-  HostReads hr;              // its reads, parsed at submission
+  HostReads hr;              // its reads, parsed by the worker that takes it
   int32_t Q = 0;             // its query length
   int cls = 0;               // packed shape class of Q: one class per wave
   std::vector<int32_t> repeats;
   int64_t est_bytes = 0;
+  int64_t est_reads = 0;     // its '>' count, before it is parsed
   int64_t n_reads = 0;
   Clock::time_point submitted, started, finished;
   int state = kQueued;
@@ -56,6 +58,7 @@ struct Request {
   char* out = nullptr;       // malloc'ed text, handed to the caller
   size_t out_len = 0;
   double device_ms = 0;      // its wave's device time
+  double parse_ms = 0, wave_ms = 0;  // host times of its parse and its wave
   int64_t wave_requests = 0, wave_reads = 0;
 };
 
@@ -159,8 +162,10 @@ void run_requests(swift_server* s, Worker& w, const std::vector<Request*>& take)
   memset(&st, 0, sizeof(st));
   const size_t guess = n_reads * 520 + (1 << 20);
   ensure_pinned(&w.pin_out, &w.pin_out_cap, std::max(guess, w.pin_out_cap));
+  const auto t_wave = Clock::now();
   rc = run_wave(w.ctx, s->idx, &s->params, src, bytes, rd, &wave, w.pin_out,
                 w.pin_out ? w.pin_out_cap : 0, &out_len, &st);
+  const double wave_ms = ms_between(t_wave, Clock::now());
   if (rc != SWIFT_OK) err = swift_last_error(w.ctx);
   const char* text = nullptr;
   std::vector<char> fetched;
@@ -175,15 +180,10 @@ void run_requests(swift_server* s, Worker& w, const std::vector<Request*>& take)
       ensure_pinned(&w.pin_out, &w.pin_out_cap, out_len);
     }
   }
-  const auto now = Clock::now();
-  std::lock_guard<std::mutex> lk(s->mu);
+  // each request's text out of the wave's (before taking the lock)
   for (size_t i = 0; i < take.size(); ++i) {
     Request* r = take[i];
-    r->finished = now;
     r->status = rc;
-    r->device_ms = st.total_ms;
-    r->wave_requests = (int64_t)take.size();
-    r->wave_reads = (int64_t)n_reads;
     if (rc == SWIFT_OK) {
       const size_t len = (size_t)(wave[i].text1 - wave[i].text0);
       r->out = (char*)malloc(len + 1);
@@ -201,10 +201,22 @@ void run_requests(swift_server* s, Worker& w, const std::vector<Request*>& take)
     r->reads.clear();
     r->reads.shrink_to_fit();
     r->hr = HostReads();
+  }
+  const auto now = Clock::now();
+  std::lock_guard<std::mutex> lk(s->mu);
+  for (size_t i = 0; i < take.size(); ++i) {
+    Request* r = take[i];
+    r->finished = now;
+    r->device_ms = st.total_ms;
+    r->wave_ms = wave_ms;
+    r->wave_requests = (int64_t)take.size();
+    r->wave_reads = (int64_t)n_reads;
     r->state = kDone;
     s->in_flight -= r->est_bytes;
   }
 }
+
+int admit(const swift_server* s, Request* r);
 
 void worker(swift_server* s, int wi) {
   Worker& w = s->workers[wi];
@@ -227,11 +239,12 @@ void worker(swift_server* s, int wi) {
       for (auto it = s->queue.begin(); it != s->queue.end();) {
         Request* r = *it;
         const bool first = take.empty();
+        const int64_t nr = r->est_reads;
         if (r->cls == cls &&
-            (first || (reads + (int64_t)r->hr.rd.size() <= kWaveMaxReads &&
+            (first || (reads + nr <= kWaveMaxReads &&
                        s->in_flight + est + r->est_bytes <= s->budget))) {
           take.push_back(r);
-          reads += (int64_t)r->hr.rd.size();
+          reads += nr;
           est += r->est_bytes;
           it = s->queue.erase(it);
         } else {
@@ -245,13 +258,63 @@ void worker(swift_server* s, int wi) {
         r->state = kRunning;
       }
     }
-    run_requests(s, w, take);
+    // parse and check each request (outside the lock); one that fails is
+    // done at once with its own error and leaves the wave
+    std::vector<Request*> ok, failed;
+    std::vector<int> failed_rc;
+    for (Request* r : take) {
+      const auto t0 = Clock::now();
+      const int rc = admit(s, r);
+      r->parse_ms = ms_between(t0, Clock::now());
+      if (rc == SWIFT_OK) {
+        ok.push_back(r);
+      } else {
+        failed.push_back(r);
+        failed_rc.push_back(rc);
+      }
+    }
+    if (!failed.empty()) {
+      std::lock_guard<std::mutex> lk(s->mu);
+      const auto now = Clock::now();
+      for (size_t i = 0; i < failed.size(); ++i) {
+        Request* r = failed[i];
+        r->status = failed_rc[i];
+        r->finished = now;
+        r->reads.clear();
+        r->reads.shrink_to_fit();
+        r->state = kDone;
+        s->in_flight -= r->est_bytes;
+      }
+    }
+    if (!ok.empty()) run_requests(s, w, ok);
     s->cv_done.notify_all();
     s->cv_work.notify_all();
   }
 }
 
-// The checks swift_align makes on a request alone, at submission.
+// At submission, without parsing: the query length the request will have
+// if it is well formed (qry_len, else the first read's line length, one less
+// when that line ends the input without a newline, as getSeqSize counts),
+// its shape class and a memory estimate from its header count.
+void classify(const swift_server* s, Request* r) {
+  const char* b = r->reads.data();
+  const size_t n = r->reads.size();
+  int64_t q = 0;
+  const char* nl = n ? (const char*)memchr(b, '\n', n) : nullptr;
+  if (nl) {
+    const size_t s1 = (size_t)(nl - b) + 1;
+    const char* nl2 = s1 < n ? (const char*)memchr(b + s1, '\n', n - s1) : nullptr;
+    q = nl2 ? (int64_t)(nl2 - (b + s1)) : (int64_t)(n - s1) - 1;
+  }
+  const swift_params& p = s->params;
+  if (p.qry_len > 0) q = p.qry_len;
+  const int c = q >= 1 && q <= kMaxQ ? packed_class((int)q) : 0;
+  r->cls = c < 0 ? 0 : c;
+  r->est_reads = (int64_t)std::count(b, b + n, '>');
+  r->est_bytes = estimate_bytes(r->est_reads, n);
+}
+
+// The checks swift_align makes on a request alone, before its wave runs.
 int admit(const swift_server* s, Request* r) {
   std::string err;
   const int limit = read_limit_of(&s->params);
@@ -279,7 +342,6 @@ int admit(const swift_server* s, Request* r) {
   r->n_reads = r->hr.n;
   r->cls = packed_class(Q);
   if (p.seeder != 1) r->repeats = phase1_stale_repeats(r->hr.n, r->hr.n_gt);
-  r->est_bytes = estimate_bytes(r->hr.n, r->reads.size());
   return SWIFT_OK;
 }
 
@@ -319,6 +381,10 @@ int swift_server_create(int device, const swift_index* idx, const swift_params* 
       return rc;
     }
     s->workers[w].ctx = c;
+    // staging for a wave of up to kWaveMaxReads reads of 300 bases and
+    // their records, pinned once here rather than grown while serving
+    ensure_pinned(&s->workers[w].pin_in, &s->workers[w].pin_in_cap, 64ull << 20);
+    ensure_pinned(&s->workers[w].pin_out, &s->workers[w].pin_out_cap, 160ull << 20);
   }
   for (int w = 0; w < workers; ++w) s->threads.emplace_back(worker, s, w);
   *out = s;
@@ -330,7 +396,7 @@ int swift_server_submit(swift_server* s, const char* reads, size_t len, int64_t*
   Request* r = new Request();
   r->reads.assign(reads, reads + len);
   r->submitted = Clock::now();
-  const int rc = admit(s, r);
+  classify(s, r);  // parsed by the worker that takes it
   {
     std::lock_guard<std::mutex> lk(s->mu);
     if (s->stop) {
@@ -340,18 +406,9 @@ int swift_server_submit(swift_server* s, const char* reads, size_t len, int64_t*
     r->ticket = s->next_ticket++;
     s->all[r->ticket] = r;
     *ticket = r->ticket;
-    if (rc != SWIFT_OK) {  // fails alone, at once
-      r->status = rc;
-      r->state = kDone;
-      r->started = r->finished = r->submitted;
-    } else {
-      s->queue.push_back(r);
-    }
+    s->queue.push_back(r);
   }
-  if (rc != SWIFT_OK)
-    s->cv_done.notify_all();
-  else
-    s->cv_work.notify_all();
+  s->cv_work.notify_all();
   return SWIFT_OK;
 }
 
@@ -411,6 +468,8 @@ int swift_server_wait(swift_server* s, int64_t ticket, char** out, size_t* out_l
     st->device_ms = r->device_ms;
     st->wave_requests = r->wave_requests;
     st->wave_reads = r->wave_reads;
+    st->parse_ms = r->parse_ms;
+    st->wave_ms = r->wave_ms;
   }
   if (err && err_cap) {
     strncpy(err, r->error.c_str(), err_cap - 1);

@@ -108,8 +108,8 @@ BAD_INPUTS = [b">a\nACGT\n\n>b\nACGT\n", b">a\nACGT\nACGT\n", b">a\n", b">a\nAC>
 
 
 def test_server_checks_match_swift_align(sg, setup):
-    # requests are parsed on the host at submission: every malformed input
-    # fails there with swift_align's status and message
+    # requests are parsed on the host by the worker that takes them: every
+    # malformed input fails there, alone, with swift_align's status and message
     ctx, ix, _, _ = setup
     p = params(sg)
     srv = sg.Server(ix, params=p, workers=1)
