@@ -2098,6 +2098,10 @@ static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swi
   pa.qbuf = qbuf;
   pa.wbuf = wbuf;
   pa.Qs = Qs;
+  uint8_t* read_cls;
+  CK(sc.get(&read_cls, (size_t)std::max<int64_t>(rd->n, 1)));
+  pa.read_cls = read_cls;
+  pa.n_reads = rd->n;
   // a wave of several query lengths: each record's own, for the pair
   // builder and every Smith-Waterman pass (rows past it match nothing)
   int32_t* pair_q = nullptr;

@@ -270,6 +270,9 @@ struct PairArgs {
   char* qbuf;                 // n x Qs
   char* wbuf;                 // n x kWinPad
   int Qs;                     // query stride (>= every query length + 1)
+  uint8_t* read_cls;          // optional scratch, n_reads bytes: per read 0 when its
+                              // query bytes are all A, C, G or T (word-wise copy)
+  int64_t n_reads;
 };
 void launch_build_pairs(cudaStream_t st, const PairArgs& a);
 
@@ -447,6 +450,8 @@ struct FastArgs {
                                    // cells they computed (early stop counted)
   int shape_g, shape_rpl;     // optional: the (lanes, rows per lane) shape of the
                               // exact passes and walk; 0: the default for Q
+  uint32_t one, four;         // trace pass: 1 and 4, as values the compiler cannot
+                              // fold (set by launch_sw_trace)
 };
 bool fast_params_ok(int Q, int R, int m, int x, int o, int e, int* bias);
 constexpr int kFastMaxR = 512;  // window columns the packed passes take

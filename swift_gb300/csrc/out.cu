@@ -215,69 +215,98 @@ __global__ void format_sizes_kernel(FormatArgs a) {
 }
 
 constexpr int kFmtWarps = 8;
+constexpr int kFmtPerWarp = 4;  // records a warp looks at (about one in four is printed)
 
+// The literal pieces of a header line, one after another:
+//   "Qry: " | " | Ref: " | " | Score: " | ".0 | AlignStart: " | " | AlignEnd: "
+//   | " | AlignLength: " | "\nR: "
+__device__ const char kHdrLit[] =
+    "Qry:  | Ref:  | Score: .0 | AlignStart:  | AlignEnd:  | AlignLength: \nR: ";
+__device__ __forceinline__ void lit_piece(char* o, int src, int n, int lane) {
+  if (lane < n) o[lane] = kHdrLit[src + lane];
+}
+
+// v's decimal digits (and sign) to o, ndigits(v) bytes
+__device__ __forceinline__ void put_int_at(char* o, int v, int nd) {
+  unsigned u = v < 0 ? (unsigned)(-(int64_t)v) : (unsigned)v;
+  if (v < 0) *o = '-';
+  for (int i = nd - 1; i >= (v < 0 ? 1 : 0); --i) {
+    o[i] = (char)('0' + u % 10);
+    u /= 10;
+  }
+}
+
+// One warp per kFmtPerWarp consecutive records; a printed record's header
+// is written by the lanes in parallel straight into the text: every piece
+// (separator, literals, the two names, the four numbers, one lane each) at
+// an offset all lanes compute from the piece lengths.
 __global__ void __launch_bounds__(kFmtWarps * 32) format_write_kernel(FormatArgs a) {
-  __shared__ char hdr_all[kFmtWarps][320];  // header line: at most 257 bytes
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t j = a.first + (int64_t)blockIdx.x * kFmtWarps + wib;
-  if (j >= a.n || !a.keep[j]) return;
-  const DevPair p = a.pairs[j];
-  const DevAln al = a.aln[j];
-  char* hdr = hdr_all[wib];
-  int hn = 0;
-  if (lane == 0) {
-    char* o;
-    if (!a.pe_sep)
-      o = put_str(hdr, "\n****************************************\n");  // 42 bytes
-    else if (a.pe_sep[j])
-      o = put_str(hdr, "\n*************************************\n");  // 39 bytes
-    else
-      o = put_str(hdr, "\n");
-    o = put_str(o, "Qry: ");
-    const int ql = qname_len(a, p);
-    for (int i = 0; i < ql; ++i) *o++ = qname_at(a, p, i);
-    o = put_str(o, " | Ref: ");
+  const int64_t j0 = a.first + ((int64_t)blockIdx.x * kFmtWarps + wib) * kFmtPerWarp;
+  const int64_t jt = j0 + lane;
+  uint32_t todo = __ballot_sync(0xffffffffu, lane < kFmtPerWarp && jt < a.n && a.keep[jt]);
+  while (todo) {
+    const int64_t j = j0 + __ffs(todo) - 1;
+    todo &= todo - 1;
+    const DevPair p = a.pairs[j];
+    const DevAln al = a.aln[j];
+    const DevRead rd = a.rd[p.read];
     const DevRecord& rec = a.recs[p.ref_idx];
-    for (uint32_t i = 0; i < rec.name_len; ++i) *o++ = rec.name[i];
-    o = put_str(o, " | Score: ");
-    o = put_int(o, al.score);
-    o = put_str(o, ".0 | AlignStart: ");
-    o = put_int(o, al.start + p.ref_dist);
-    o = put_str(o, " | AlignEnd: ");
-    o = put_int(o, al.end + p.ref_dist);
-    o = put_str(o, " | AlignLength: ");
-    o = put_int(o, al.len);
-    o = put_str(o, "\nR: ");
-    hn = (int)(o - hdr);
-  }
-  hn = __shfl_sync(0xffffffffu, hn, 0);
-  __syncwarp();
-  char* out = a.text + a.offs[j];
-  for (int i = lane; i < hn; i += 32) out[i] = hdr[i];
-  out += hn;
-  const int L = al.len > 0 ? al.len : 0;
-  const char* rc = a.rcons + j * a.cons_stride;
-  const char* qc = a.qcons + j * a.cons_stride;
-  // "R: " already written; reversed strings
-  for (int z = lane; z < L; z += 32) {
-    const char r = rc[L - 1 - z], q = qc[L - 1 - z];
-    out[z] = r;
-    const int ur = (unsigned)(r - 'a') < 26u ? r - 32 : r;
-    const int uq = (unsigned)(q - 'a') < 26u ? q - 32 : q;
-    const char m = (ur == uq || r == 'N' || q == 'N') ? '|' : (r == '-' || q == '-') ? '-' : '.';
-    out[L + 4 + z] = m;
-    out[2 * L + 8 + z] = q;
-  }
-  if (lane == 0) {
-    out[L] = '\n';
-    out[L + 1] = ' ';
-    out[L + 2] = ' ';
-    out[L + 3] = ' ';
-    out[2 * L + 4] = '\n';
-    out[2 * L + 5] = 'Q';
-    out[2 * L + 6] = ':';
-    out[2 * L + 7] = ' ';
-    out[3 * L + 8] = '\n';
+    const int sepn = !a.pe_sep ? 42 : a.pe_sep[j] ? 39 : 1;
+    const int ql = rd.name_len + (p.strand ? 1 : 0);
+    const int rl = (int)rec.name_len;
+    const int v0 = al.score, v1 = al.start + p.ref_dist, v2 = al.end + p.ref_dist, v3 = al.len;
+    const int n0 = ndigits(v0), n1 = ndigits(v1), n2 = ndigits(v2), n3 = ndigits(v3);
+    char* o = a.text + a.offs[j];
+    // separator line
+    for (int i = lane; i < sepn; i += 32) o[i] = (i == 0 || i == sepn - 1) ? '\n' : '*';
+    char* q = o + sepn;
+    lit_piece(q, 0, 5, lane);  // "Qry: "
+    q += 5;
+    for (int i = lane; i < ql; i += 32) q[i] = i < rd.name_len ? a.reads[rd.name_off + 1 + i] : '*';
+    q += ql;
+    lit_piece(q, 5, 8, lane);  // " | Ref: "
+    q += 8;
+    for (int i = lane; i < rl; i += 32) q[i] = rec.name[i];
+    q += rl;
+    lit_piece(q, 13, 10, lane);  // " | Score: "
+    char* d0 = q + 10;
+    q = d0 + n0;
+    lit_piece(q, 23, 17, lane);  // ".0 | AlignStart: "
+    char* d1 = q + 17;
+    q = d1 + n1;
+    lit_piece(q, 40, 13, lane);  // " | AlignEnd: "
+    char* d2 = q + 13;
+    q = d2 + n2;
+    lit_piece(q, 53, 16, lane);  // " | AlignLength: "
+    char* d3 = q + 16;
+    q = d3 + n3;
+    lit_piece(q, 69, 4, lane);  // "\nR: "
+    if (lane < 4) {
+      const int v = lane == 0 ? v0 : lane == 1 ? v1 : lane == 2 ? v2 : v3;
+      const int nd = lane == 0 ? n0 : lane == 1 ? n1 : lane == 2 ? n2 : n3;
+      char* d = lane == 0 ? d0 : lane == 1 ? d1 : lane == 2 ? d2 : d3;
+      put_int_at(d, v, nd);
+    }
+    char* out = q + 4;
+    const int L = al.len > 0 ? al.len : 0;
+    const char* rc = a.rcons + j * a.cons_stride;
+    const char* qc = a.qcons + j * a.cons_stride;
+    // "R: " already written; reversed strings
+    for (int z = lane; z < L; z += 32) {
+      const char r = rc[L - 1 - z], qq = qc[L - 1 - z];
+      out[z] = r;
+      const int ur = (unsigned)(r - 'a') < 26u ? r - 32 : r;
+      const int uq = (unsigned)(qq - 'a') < 26u ? qq - 32 : qq;
+      const char m = (ur == uq || r == 'N' || qq == 'N') ? '|' : (r == '-' || qq == '-') ? '-' : '.';
+      out[L + 4 + z] = m;
+      out[2 * L + 8 + z] = qq;
+    }
+    if (lane < 9) {
+      // "\n   " after R, "\nQ: " after the match line, "\n" at the end
+      const int at = lane < 4 ? L + lane : lane < 8 ? 2 * L + lane : 3 * L + 8;
+      out[at] = lane == 0 || lane == 4 || lane == 8 ? '\n' : lane < 4 ? ' ' : lane == 5 ? 'Q' : lane == 6 ? ':' : ' ';
+    }
   }
 }
 
@@ -441,7 +470,8 @@ void launch_format_sizes(cudaStream_t st, const FormatArgs& a) {
 void launch_format_write(cudaStream_t st, const FormatArgs& a) {
   const int64_t n = a.n - a.first;
   if (n <= 0) return;
-  format_write_kernel<<<(unsigned)((n + kFmtWarps - 1) / kFmtWarps), kFmtWarps * 32, 0, st>>>(a);
+  const int64_t warps = (n + kFmtPerWarp - 1) / kFmtPerWarp;
+  format_write_kernel<<<(unsigned)((warps + kFmtWarps - 1) / kFmtWarps), kFmtWarps * 32, 0, st>>>(a);
 }
 
 }  // namespace swift

@@ -28,6 +28,39 @@ __device__ __forceinline__ char comp_char(char c) {
   return c == 'A' ? 'T' : c == 'C' ? 'G' : c == 'G' ? 'C' : 'A';
 }
 
+// four bytes from p (any alignment): two aligned loads and a funnel shift
+// (the second load stays inside the buffer's padding past the last read)
+__device__ __forceinline__ uint32_t load4(const char* p) {
+  const uintptr_t ad = (uintptr_t)p;
+  const uint32_t* wp = reinterpret_cast<const uint32_t*>(ad & ~(uintptr_t)3);
+  return __funnelshift_r(wp[0], wp[1], (uint32_t)(ad & 3) * 8);
+}
+
+// comp_char of four upper-case A, C, G, T bytes at once: A <-> T differ in
+// 0x15, C <-> G in 0x04, and bit 1 is clear exactly for A and T
+__device__ __forceinline__ uint32_t comp4(uint32_t x) {
+  return x ^ ((((~x) >> 1) & 0x01010101u) * 0x11u | 0x04040404u);
+}
+
+// Per read: 0 when its query (the first Q bytes, Q <= its length) is all
+// upper-case A, C, G, T, so that both strands' queries are whole-word
+// copies; else 1 (the per-byte path of build_pairs_kernel).
+__global__ void read_class_kernel(PairArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (r >= a.n_reads) return;
+  const DevRead rd = a.rd[r];
+  const int Q = a.read_q ? a.read_q[r] : a.Q;
+  bool bad = rd.len < Q;
+  const char* s = a.reads + rd.seq_off;
+  for (int i = lane; i < Q && !bad; i += 32) {
+    const char c = s[i];
+    bad = !(c == 'A' || c == 'C' || c == 'G' || c == 'T');
+  }
+  bad = __any_sync(0xffffffffu, bad);
+  if (lane == 0) a.read_cls[r] = bad ? 1 : 0;
+}
+
 // getRefSeq2's walk over the file bytes: up to 300 characters from file
 // offset off, newlines dropped, stopping at a header line or end of file.
 // The first kPre 32-byte rounds are loaded up front so the warp waits for
@@ -177,6 +210,22 @@ __global__ void __launch_bounds__(kPairWarps * 32) build_pairs_kernel(PairArgs a
   if (a.pair_q && lane == 0) a.pair_q[j] = Q;
   const int avail = rd.len < Q ? rd.len : Q;
   char* qout = a.qbuf + j * (int64_t)a.Qs;
+  if (a.read_cls && a.read_cls[read] == 0) {
+    // upper-case A, C, G, T only (avail = Q, not odd): whole words, the
+    // reverse complement byte-reversed and complemented four at a time
+    for (int i0 = 4 * lane; i0 < a.Qs; i0 += 128) {
+      uint32_t word = 0;
+      if (i0 + 4 <= Q) {
+        word = strand == 0 ? load4(s + i0) : comp4(__byte_perm(load4(s + Q - 4 - i0), 0u, 0x0123));
+      } else if (i0 < Q) {
+        for (int b = 0; b < Q - i0; ++b) {
+          const char c = strand == 0 ? s[i0 + b] : comp_char(s[Q - 1 - i0 - b]);
+          word |= (uint32_t)(uint8_t)c << (8 * b);
+        }
+      }
+      *reinterpret_cast<uint32_t*>(qout + i0) = word;
+    }
+  } else
   // four bytes per lane, one 32-bit store each (Qs is a multiple of 16)
   for (int i0 = 4 * lane; i0 < a.Qs; i0 += 128) {
     uint32_t word = 0;
@@ -214,6 +263,8 @@ __global__ void __launch_bounds__(kPairWarps * 32) build_pairs_kernel(PairArgs a
 
 void launch_build_pairs(cudaStream_t st, const PairArgs& a) {
   if (a.n <= 0) return;
+  if (a.read_cls && a.n_reads > 0)
+    read_class_kernel<<<(unsigned)((a.n_reads * 32 + 255) / 256), 256, 0, st>>>(a);
   unsigned grid = (unsigned)((a.n + kPairWarps - 1) / kPairWarps);
   build_pairs_kernel<<<grid, kPairWarps * 32, 0, st>>>(a);
 }

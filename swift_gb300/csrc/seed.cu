@@ -243,32 +243,37 @@ __global__ void __launch_bounds__(kSeedWarps * 32) seed_fast_kernel(SeedArgs a) 
 
 // The strands of one list (a.mid_list: kFastHits < hits <= kMidCap;
 // a.big_list: kMidCap < hits <= kBigCap), without a sort.  The hits are
-// gathered cooperatively, hit h by lane h mod 32 (each hit's query offset
-// from a per-hit owner array), every posting load of the strand issued
-// before any is used, and kept in registers.  Each hit enters a per-warp
-// open-addressing table over its cluster key (refIdx, shift + bias) that
-// counts the cluster; the biggest count is a warp max over the hits' own
-// counts, and the first max_hits clusters of that size in key order, with
-// each one's smallest query offset, come from warp minima over the hits.
+// gathered cooperatively, hit h by lane h mod 32: the lookups that have
+// postings mark their first hit in a bit mask, and hit h belongs to the last
+// mark at or before it (found from the mask words, warp-uniform), every
+// posting load of the strand issued before any is used and kept in
+// registers.  Each hit enters a per-warp open-addressing table over its
+// cluster key (refIdx, shift + bias) that counts the cluster (at most half
+// full); the biggest count is a warp max over the hits' own counts.  Every
+// lane keeps the three smallest keys among its hits of that size (equal
+// keys merged, their offsets minimised), and the first clusters in key
+// order, each with its smallest query offset, are warp minima over those;
+// beyond three clusters a scan over the hits continues from the last key.
 // A strand's work grows with its hits, not with the table: the table is
 // emptied once per warp and each strand empties only the slots it used.
 // Warps stride over the list, whose length is on the device.
 template <int KM, int CAP, int WARPS>
 __global__ void __launch_bounds__(WARPS * 32) seed_hash_kernel(SeedArgs a) {
   constexpr unsigned long long kEmpty = ~0ull;  // above every cluster key
-  constexpr int kSlots = 2 * CAP;               // a strand takes 2^k >= 1.5 hits + 1
+  constexpr int kSlots = 2 * CAP;               // load <= 1/2
   constexpr int kRounds = CAP / 32;             // hits per lane at most
-  constexpr int kOffsets = 32 * KM;             // query offsets a strand can have
+  constexpr int kKeep = 3;                      // smallest keys kept per lane
+  static_assert(32 * KM <= 512 && kSlots <= 1024 && CAP < 1024, "meta bit fields");
   __shared__ unsigned long long tkey_all[WARPS][kSlots];
   __shared__ uint32_t tcnt_all[WARPS][kSlots];
-  __shared__ uint16_t owner_all[WARPS][CAP];    // hit -> its query offset
-  __shared__ uint32_t off_all[WARPS][kOffsets];  // offset -> first posting - first hit
+  __shared__ uint2 start_all[WARPS][CAP];       // first hit -> (posting - hit, offset)
+  __shared__ uint32_t mark_all[WARPS][kRounds];  // first hits as bits
   __shared__ __align__(16) WarpSmem smem[WARPS];
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   unsigned long long* tkey = tkey_all[wib];
   uint32_t* tcnt = tcnt_all[wib];
-  uint16_t* owner = owner_all[wib];
-  uint32_t* off = off_all[wib];
+  uint2* start = start_all[wib];
+  uint32_t* mark = mark_all[wib];
   const bool big = CAP > kMidCap;
   const int64_t n_list = big ? *a.n_big : *a.n_mid;
   const int32_t* list = big ? a.big_list : a.mid_list;
@@ -276,9 +281,10 @@ __global__ void __launch_bounds__(WARPS * 32) seed_hash_kernel(SeedArgs a) {
     tkey[i] = kEmpty;
     tcnt[i] = 0;
   }
-  __syncwarp();
   for (int64_t t = (int64_t)blockIdx.x * WARPS + wib; t < n_list;
        t += (int64_t)gridDim.x * WARPS) {
+    if (lane < kRounds) mark[lane] = 0;
+    __syncwarp();
     const int64_t sid = list[t];
     const DevRead rd = a.rd[sid >> 1];
     const int strand = (int)(sid & 1);
@@ -294,50 +300,57 @@ __global__ void __launch_bounds__(WARPS * 32) seed_hash_kernel(SeedArgs a) {
     }
     const uint32_t n = __shfl_sync(0xffffffffu, incl, 31);  // in the list's range
     const uint32_t post = __reduce_add_sync(0xffffffffu, posting_sectors<KM>(cnt));
-    // hit h (h in [first, first + cnt) of offset i) is posting off[i] + h
     uint32_t pos = incl - my;
 #pragma unroll
     for (int m = 0; m < KM; ++m) {
       if (cnt[m]) {
-        const uint32_t i = (uint32_t)(lane * M + m);
-        off[i] = beg[m] - pos;
-        for (uint32_t j = 0; j < cnt[m]; ++j) owner[pos + j] = (uint16_t)i;
+        start[pos] = make_uint2(beg[m] - pos, (uint32_t)(lane * M + m));
+        atomicOr(&mark[pos >> 5], 1u << (pos & 31));
         pos += cnt[m];
       }
     }
-    uint32_t T = 64;  // table slots of this strand: load <= 2/3
-    while (T < n + n / 2 + 1) T <<= 1;
     __syncwarp();
+    // per hit: its posting, then (refIdx, shift + bias); meta packs the
+    // query offset (bits 0-8), the table slot (9-18) and the cluster's count
     uint2 ph[kRounds];
-    uint32_t ih[kRounds], sl[kRounds];
+    uint32_t meta[kRounds];
+    uint32_t carry = 0;  // the last first hit before the round (hit 0 is one)
 #pragma unroll
     for (int r = 0; r < kRounds; ++r) {
-      const uint32_t h = lane + 32 * r;
-      ih[r] = 0;
-      sl[r] = 0;
+      meta[r] = 0;
       ph[r] = make_uint2(0, 0);
-      if (h < n) {
-        ih[r] = owner[h];
-        ph[r] = __ldg(&a.postings[off[ih[r]] + h]);
+      if (32u * r < n) {
+        const uint32_t w = mark[r];
+        const uint32_t below = w & (0xffffffffu >> (31 - lane));
+        const uint32_t st = below ? 32u * r + 31u - __clz(below) : carry;
+        carry = w ? 32u * r + 31u - __clz(w) : carry;
+        const uint32_t h = lane + 32u * r;
+        if (h < n) {
+          const uint2 inf = start[st];
+          meta[r] = inf.y;
+          ph[r] = __ldg(&a.postings[inf.x + h]);
+        }
       }
     }
+#pragma unroll
+    for (int r = 0; r < kRounds; ++r)
+      ph[r].x = (uint32_t)((int32_t)ph[r].x - (int32_t)meta[r] + kShiftBias);
     auto key_of = [&](int r) -> unsigned long long {
-      return ((unsigned long long)ph[r].y << 32) |
-             (uint32_t)((int32_t)ph[r].x - (int32_t)ih[r] + kShiftBias);
+      return ((unsigned long long)ph[r].y << 32) | ph[r].x;
     };
 #pragma unroll
     for (int r = 0; r < kRounds; ++r) {
-      if (lane + 32 * r < n) {
+      if (lane + 32u * r < n) {
         const unsigned long long ck = key_of(r);
-        uint32_t slot = cluster_mix(ck) & (T - 1);
-        for (uint32_t probe = 0; probe < T; ++probe) {  // T > n: a free slot exists
+        uint32_t slot = cluster_mix(ck) & (kSlots - 1);
+        for (int probe = 0; probe < kSlots; ++probe) {  // kSlots > n: a free slot exists
           const unsigned long long old = atomicCAS(&tkey[slot], kEmpty, ck);
           if (old == kEmpty || old == ck) {
             atomicAdd(&tcnt[slot], 1u);
-            sl[r] = slot;
+            meta[r] |= slot << 9;
             break;
           }
-          slot = (slot + 1) & (T - 1);
+          slot = (slot + 1) & (kSlots - 1);
         }
       }
     }
@@ -345,53 +358,110 @@ __global__ void __launch_bounds__(WARPS * 32) seed_hash_kernel(SeedArgs a) {
     // the biggest cluster over the hits' own counts; its hits as bits
     uint32_t bigc = 0;
 #pragma unroll
-    for (int r = 0; r < kRounds; ++r)
-      if (lane + 32 * r < n) bigc = max(bigc, tcnt[sl[r]]);
+    for (int r = 0; r < kRounds; ++r) {
+      if (lane + 32u * r < n) {
+        const uint32_t c = tcnt[(meta[r] >> 9) & 1023u];
+        meta[r] |= c << 19;
+        bigc = max(bigc, c);
+      }
+    }
     bigc = __reduce_max_sync(0xffffffffu, bigc);
-    uint32_t cand = 0;
+    // the lane's kKeep smallest keys of that size, ascending
+    unsigned long long lk[kKeep];
+    uint32_t lo[kKeep];
 #pragma unroll
-    for (int r = 0; r < kRounds; ++r)
-      if (lane + 32 * r < n && tcnt[sl[r]] == bigc) cand |= 1u << r;
-    // the first max_hits cluster keys of that size, smallest first (every
-    // key is above 0), each with its smallest query offset
-    int got = 0;
-    int3* out = a.best + sid * a.max_hits;
-    unsigned long long last = 0;
-    while (got < a.max_hits) {
-      unsigned long long mk = kEmpty;
+    for (int q = 0; q < kKeep; ++q) {
+      lk[q] = kEmpty;
+      lo[q] = 0xffffffffu;
+    }
 #pragma unroll
-      for (int r = 0; r < kRounds; ++r) {
-        if ((cand >> r) & 1u) {
-          const unsigned long long k = key_of(r);
-          if (k > last && k < mk) mk = k;
+    for (int r = 0; r < kRounds; ++r) {
+      if ((meta[r] >> 19) == bigc) {  // bigc >= 1: only real hits
+        unsigned long long k = key_of(r);
+        uint32_t o = meta[r] & 511u;
+#pragma unroll
+        for (int q = 0; q < kKeep; ++q) {
+          if (k == lk[q]) {
+            lo[q] = min(lo[q], o);
+            k = kEmpty;
+          } else if (k < lk[q]) {
+            const unsigned long long tk = lk[q];
+            const uint32_t to = lo[q];
+            lk[q] = k;
+            lo[q] = o;
+            k = tk;
+            o = to;
+          }
         }
       }
-      const uint32_t hmin = __reduce_min_sync(0xffffffffu, (uint32_t)(mk >> 32));
+    }
+    int got = 0;
+    int3* out = a.best + sid * a.max_hits;
+    unsigned long long last = 0;  // every key is above 0
+    const int first = min(a.max_hits, kKeep);
+    while (got < first) {
+      // the lane's first key not taken yet is lk[0]: taken keys shift out
+      const uint32_t hmin = __reduce_min_sync(0xffffffffu, (uint32_t)(lk[0] >> 32));
       if (hmin == 0xffffffffu) break;  // no cluster left
       const uint32_t lmin = __reduce_min_sync(
-          0xffffffffu, (uint32_t)(mk >> 32) == hmin ? (uint32_t)mk : 0xffffffffu);
+          0xffffffffu, (uint32_t)(lk[0] >> 32) == hmin ? (uint32_t)lk[0] : 0xffffffffu);
       const unsigned long long K = ((unsigned long long)hmin << 32) | lmin;
-      uint32_t mi = 0xffffffffu;
-#pragma unroll
-      for (int r = 0; r < kRounds; ++r)
-        if (((cand >> r) & 1u) && key_of(r) == K) mi = min(mi, ih[r]);
-      mi = __reduce_min_sync(0xffffffffu, mi);
+      const bool mine = lk[0] == K;
+      const uint32_t mi = __reduce_min_sync(0xffffffffu, mine ? lo[0] : 0xffffffffu);
       if (lane == 0) {
         const int32_t shift = (int32_t)lmin - kShiftBias;
         out[got] = make_int3((int32_t)hmin, shift, shift + (int32_t)mi);
       }
+      if (mine) {
+#pragma unroll
+        for (int q = 0; q + 1 < kKeep; ++q) {
+          lk[q] = lk[q + 1];
+          lo[q] = lo[q + 1];
+        }
+        lk[kKeep - 1] = kEmpty;
+      }
       last = K;
       ++got;
+    }
+    // more than kKeep clusters wanted (and kKeep found): scan the hits for
+    // the next keys
+    if (got == kKeep) {
+      while (got < a.max_hits) {
+        unsigned long long mk = kEmpty;
+#pragma unroll
+        for (int r = 0; r < kRounds; ++r) {
+          if ((meta[r] >> 19) == bigc) {
+            const unsigned long long k = key_of(r);
+            if (k > last && k < mk) mk = k;
+          }
+        }
+        const uint32_t hmin = __reduce_min_sync(0xffffffffu, (uint32_t)(mk >> 32));
+        if (hmin == 0xffffffffu) break;  // no cluster left
+        const uint32_t lmin = __reduce_min_sync(
+            0xffffffffu, (uint32_t)(mk >> 32) == hmin ? (uint32_t)mk : 0xffffffffu);
+        const unsigned long long K = ((unsigned long long)hmin << 32) | lmin;
+        uint32_t mi = 0xffffffffu;
+#pragma unroll
+        for (int r = 0; r < kRounds; ++r)
+          if ((meta[r] >> 19) == bigc && key_of(r) == K) mi = min(mi, meta[r] & 511u);
+        mi = __reduce_min_sync(0xffffffffu, mi);
+        if (lane == 0) {
+          const int32_t shift = (int32_t)lmin - kShiftBias;
+          out[got] = make_int3((int32_t)hmin, shift, shift + (int32_t)mi);
+        }
+        last = K;
+        ++got;
+      }
     }
     if (lane == 0) a.nbest[sid] = got;
     account(a, lane, L, nq, post, got);
     __syncwarp();
-    // empty the slots this strand used (owners and offsets are rewritten)
+    // empty the slots this strand used (marks are cleared, starts rewritten)
 #pragma unroll
     for (int r = 0; r < kRounds; ++r) {
-      if (lane + 32 * r < n) {
-        tkey[sl[r]] = kEmpty;
-        tcnt[sl[r]] = 0;
+      if (lane + 32u * r < n) {
+        tkey[(meta[r] >> 9) & 1023u] = kEmpty;
+        tcnt[(meta[r] >> 9) & 1023u] = 0;
       }
     }
     __syncwarp();

@@ -75,6 +75,15 @@ __device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t s) {
   return d;
 }
 
+// a * b + c as an integer multiply-add: with b a runtime value the compiler
+// cannot fold, it stays one (FMA-pipe) instruction instead of becoming a
+// shift-add or an add on the ALU pipe
+__device__ __forceinline__ uint32_t mad_u32(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t d;
+  asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+  return d;
+}
+
 __device__ __forceinline__ uint32_t sel(uint32_t m, uint32_t a, uint32_t b) {
   return (a & m) | (b & ~m);
 }
@@ -85,10 +94,11 @@ __device__ __forceinline__ uint32_t sel(uint32_t m, uint32_t a, uint32_t b) {
 //     region[(ln * steps8 + step) * kDirWords + w],  steps8 = steps rounded up to 8,
 // so a block of 4 steps is one 16 * kDirWords-byte store and a traceback,
 // which moves one step back on most cells, reads neighbouring words of one
-// stream per lane.  A word holds 8 rows x 2 pairs x 2 bits: bits
-// 2 * (k & 7) (first pair) and 16 + 2 * (k & 7) (second pair) of row k are
-// 2 for DIAG, 1 for UP and 0 for LEFT or NONE (NONE is the cell with H = 0,
-// which the traceback knows from the scores).
+// stream per lane.  A word holds up to 8 rows x 2 pairs x 2 bits, its last
+// row lowest: with n rows in the word (8, or what is left of the lane's
+// rows), bits 2 * (n - 1 - (k & 7)) (first pair) and 16 + the same (second
+// pair) of row k are 2 for UP, 1 for LEFT and 0 for DIAG or NONE (NONE is
+// the cell with H = 0, which the traceback knows from the scores).
 // first-maximum tags of the trace pass (see packed_item)
 constexpr uint32_t kTagOld = 0x000F000Fu;
 constexpr int kTagWindow = 12;
@@ -194,20 +204,26 @@ __device__ __forceinline__ void packed_item(const FastArgs& a, const int64_t war
         dg = h16p[k];
         const uint32_t h16 = hx & 0xFFF0FFF0u;
         h16p[k] = h16;
-        up = (hx & 0x00020002u) * KU + h16;
-        xl[k] = (hx & 0x00010001u) * KL + h16;
+        const uint32_t bu = hx & 0x00020002u, bl = hx & 0x00010001u;  // UP, LEFT
+        up = bu * KU + h16;
+        xl[k] = bl * KL + h16;
         if (TRACE) {
           // first maximum of the row: the key's tag makes an earlier step of
           // the window win a tie, and the window's last best keeps tag 15
-          const uint32_t key = VAR && var_r ? (h16 + tag) & cm : h16 + tag;
-          bestv[k] = __vimax_s16x2_relu(bestv[k], key);  // both non-negative
-          // bits 1 (UP) and 2 (DIAG) of each half's code to 2 * (k & 7): a
-          // mask, then a multiply-add (the rows' fields do not overlap), which
-          // issues on the FMA pipe
+          // (one add-max; both operands non-negative)
+          if (VAR && var_r)
+            bestv[k] = __vimax_s16x2_relu(bestv[k], (h16 + tag) & cm);
+          else
+            bestv[k] = __viaddmax_s16x2(h16, tag, bestv[k]);
+          // the UP and LEFT bits of each half's code enter the word by
+          // Horner's rule (word * 4 + bits; 8 rows of 2 bits fill a half
+          // without crossing into the other), with the masks above, as two
+          // FMA-pipe multiply-adds
           if ((k & 7) == 0) {
-            acc[k >> 3] |= (hx >> 1) & 0x00030003u;
+            acc[k >> 3] = mad_u32(bl, a.one, bu);
           } else {
-            acc[k >> 3] += (hx & 0x00060006u) * (1u << (2 * (k & 7) - 1));
+            acc[k >> 3] = mad_u32(acc[k >> 3], a.four, bu);
+            acc[k >> 3] = mad_u32(bl, a.one, acc[k >> 3]);
           }
         } else if (k & 1) {
           bestv[0] = __vimax3_s16x2_relu(bestv[0], hpair, h16);
@@ -566,7 +582,7 @@ __global__ void __launch_bounds__(256) sw_walk_kernel(FastArgs a) {
   auto pick = [](const uint4& v, int w) -> uint32_t {
     return w == 0 ? v.x : w == 1 ? v.y : w == 2 ? v.z : v.w;
   };
-  // 2 DIAG, 1 UP, 0 LEFT or NONE
+  // 2 UP, 1 LEFT, 0 DIAG or NONE
   auto code_at = [&](int i, int jj) -> uint32_t {
     const int ln = (i - 1) / RPL, k = (i - 1) % RPL;
     const int64_t at = ((int64_t)ln * S8 + (jj + ln - 1)) * kNW + (k >> 3);
@@ -579,7 +595,8 @@ __global__ void __launch_bounds__(256) sw_walk_kernel(FastArgs a) {
     }
     const int o = (int)(b - blk), w = (int)(at & 3);
     const uint32_t word = o == 0 ? pick(c0, w) : o == 1 ? pick(c1, w) : pick(c2, w);
-    return (word >> (shift_half + 2 * (k & 7))) & 3u;
+    const int rows_w = min(8, RPL - (k & ~7));  // rows of the word, the last lowest
+    return (word >> (shift_half + 2 * (rows_w - 1 - (k & 7)))) & 3u;
   };
   // query and window bytes in 16-byte blocks too (rows start 16-byte
   // aligned, strides are multiples of 16)
@@ -628,7 +645,7 @@ __global__ void __launch_bounds__(256) sw_walk_kernel(FastArgs a) {
   // with code 0 is NONE exactly when h = 0 (any other cell has h > 0).
   enum : int { kNone = 0, kDiag = 1, kUp = 2, kLeft = 3 };
   auto dir_of = [](uint32_t code, int h) -> int {
-    return code == 2u ? kDiag : code == 1u ? kUp : (h == 0 ? kNone : kLeft);
+    return code == 2u ? kUp : code == 1u ? kLeft : (h == 0 ? kNone : kDiag);
   };
   const int m = a.match, x = a.mismatch, o = a.gap_open, e = a.gap_ext;
   auto upc = [](char c) -> char { return (unsigned)(c - 'a') < 26u ? (char)(c - 32) : c; };
@@ -653,7 +670,7 @@ __global__ void __launch_bounds__(256) sw_walk_kernel(FastArgs a) {
       nh = h - sub;
     } else {
       // the gap costs gap_ext when the predecessor itself moved the same way
-      const bool same = nr != 0 && nc != 0 && (d == kUp ? pc == 1u : pc == 0u);
+      const bool same = nr != 0 && nc != 0 && (d == kUp ? pc == 2u : pc == 1u);
       nh = h - (same ? e : o);
     }
     nd = (nr == 0 || nc == 0) ? kNone : dir_of(pc, nh);
@@ -880,6 +897,8 @@ int launch_sw_trace(cudaStream_t st, const FastArgs& a, int64_t max_pairs, cudaE
   if (a.cons_stride % 4 != 0) return 0;  // the walk stores 32-bit words
   FastArgs b = a;
   b.chunk = max_pairs;
+  b.one = 1;
+  b.four = 4;
   if (before && cudaEventRecord(before, st) != cudaSuccess) return 0;
   int k = a.q_len ? launch_shape<true, true>(st, b, max_pairs) : launch_shape<true, false>(st, b, max_pairs);
   if (after && cudaEventRecord(after, st) != cudaSuccess) return 0;

@@ -248,6 +248,25 @@ def test_seed_overflow_path(ctx, oracle):
     assert st["seed_overflow_strands"] > 0
 
 
+@pytest.mark.parametrize("max_hits", [1, 3, 4, 9])
+def test_seed_every_hit_class(ctx, oracle, max_hits):
+    # half of the reference is diverged copies of 20 repeat units: of the 800
+    # strands of reads of 100-199 bases, about 570 have at most 32 hits, 50
+    # 33-128, 180 129-512 and a few more (the warp-match, both hash-table and
+    # the overflow kernels); more than three clusters per strand take the
+    # hash-table kernels past their kept keys
+    from swift_gb300 import synth
+    names, seqs = synth.make_reference(1_000_000, 2, sigma=0.3, repeat_frac=0.5, n_units=20,
+                                       unit_len=300, divergence=0.05, seed=3)
+    ref = synth.fasta_bytes(names, seqs)
+    rn, rs, _ = synth.make_reads(seqs, 400, 150, 0.01, 0.001, 0.05, seed=4, len_range=(100, 199))
+    reads = synth.reads_fasta(rn, rs)
+    ix = ctx.index(ref)
+    got = ctx.seed(ix, reads, max_hits=max_hits)
+    want = oracle.phase1(ref, reads, oparams(ctx, oracle, max_hits=max_hits))
+    assert got == want
+
+
 # ---------------------------------------------------------------------------
 # whole pipeline
 
