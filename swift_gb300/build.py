@@ -40,7 +40,8 @@ def _stale(target: str, deps) -> bool:
 
 def build(verbose: bool = False, ptxas_info: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
-    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".h")]
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC)
+               if f.endswith(".h") or f.endswith(".cuh")]
     headers.append(os.path.join(os.path.dirname(HERE), "include", "swift_gb300.h"))
     srcs = sorted(f for f in os.listdir(CSRC)
                   if (f.endswith(".cu") or f.endswith(".cpp")) and f != "cli.cpp")

@@ -1643,11 +1643,11 @@ int swift_sw_pairs(swift_ctx* ctx, const char* qry, const int64_t* q_off, const 
         CK(cudaMemcpyAsync(hc.data(), seg_count, nseg * 4, cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
       }
-      // launch groups: packed pairs by shape class (their keys are
+      // launch groups: packed pairs by row class (their keys are
       // consecutive), generic pairs by exact shape
       struct Group {
         bool gen;
-        int Q, R;           // generic: the shape; packed: class's longest query, widest window
+        int Q, R;           // generic: the shape; packed: the class's rows, widest window
         int64_t start, count;
       };
       std::vector<Group> groups;
@@ -1661,13 +1661,12 @@ int swift_sw_pairs(swift_ctx* ctx, const char* qry, const int64_t* q_off, const 
         }
         const bool gen = (hk[s] >> 20) & 1;
         const int q = (hk[s] >> 11) & 511, R = hk[s] & 2047;
-        if (!gen && !groups.empty() && !groups.back().gen &&
-            groups.back().Q == packed_class_max_q(q)) {
+        if (!gen && !groups.empty() && !groups.back().gen && groups.back().Q == 8 * q) {
           groups.back().R = std::max(groups.back().R, R);
           groups.back().count += hc[s];
           continue;
         }
-        groups.push_back({gen, gen ? q : packed_class_max_q(q), R, hs[s], hc[s]});
+        groups.push_back({gen, gen ? q : 8 * q, R, hs[s], hc[s]});
       }
       ps.segments += (int64_t)groups.size();
       // launch sizes go to the device (the kernels read counts there)
@@ -1726,9 +1725,9 @@ int swift_sw_pairs(swift_ctx* ctx, const char* qry, const int64_t* q_off, const 
           sg = cg[ctx->tuning - 2];
           srpl = crpl[ctx->tuning - 2];
         }
-        const int tkey = packed_class(Q) * 64 + (R + 63) / 64;
+        const int tkey = (Q / 8) * 64 + (R + 63) / 64;
         const bool tune = ctx->tuning == 1 && ncand > 1 && !ctx->tuned.count(tkey) &&
-                          cnt >= 4096;
+                          cnt >= 1024;
         int64_t words = 0;
         for (int c = 0; c < (tune ? ncand : 1); ++c)
           words = std::max(words, trace_scratch_words(Q, R, std::min(cnt, sub),

@@ -465,9 +465,17 @@ __host__ __device__ inline int packed_class_max_q(int c) {
   return c == 0 ? 32 : c == 1 ? 64 : c == 2 ? 104 : c == 3 ? 128 : c == 4 ? 208 : c == 5 ? 256
        : 320;
 }
+// Row class of a query of swift_sw_pairs' packed pairs: the rows of the
+// trace-pass shape that takes it exactly (a multiple of 8 up to 128, of 16
+// up to 256, of 32 up to 320, at least 32); -1 beyond 320.
+__host__ __device__ inline int var_rows(int Q) {
+  return Q <= 32 ? 32 : Q <= 128 ? (Q + 7) & ~7 : Q <= 256 ? (Q + 15) & ~15
+       : Q <= 320 ? (Q + 31) & ~31 : -1;
+}
 int64_t trace_scratch_words(int Q, int R, int64_t pairs, int shape_g = 0, int shape_rpl = 0);
-// The compiled shapes the autotuner tries for queries up to Q (the default
-// first); returns how many.
+// The compiled shapes of the per-pair-length trace pass the autotuner tries
+// for the queries of Q's row class (the exact fit, its default, first);
+// returns how many.
 int packed_shape_candidates(int Q, int32_t* g, int32_t* rpl, int cap);
 int launch_sw_score(cudaStream_t st, const FastArgs& a, int64_t max_pairs);
 // before / after (optional) are recorded around the trace pass alone

@@ -3,12 +3,13 @@
 // Smith-Waterman passes covers pairs of one (Q, R).
 //
 // Shape key: bits 0-10 window length R (<= 1024); for pairs of the packed
-// passes bits 11-19 hold the packed shape class of Q, for the others (a
-// byte outside ACGTacgt, or a shape or scoring the packed passes do not
-// take) bit 20 is set and bits 11-19 hold Q itself.  A counting sort over
-// the 2^21 keys orders the pairs by key: packed pairs of one class form one
-// launch (sorted by window length, so a warp's pairs sweep similar widths),
-// generic pairs one launch per exact shape.
+// passes bits 11-19 hold Q's row class / 8 (var_rows: the rows of the
+// trace shape that takes Q exactly), for the others (a byte outside
+// ACGTacgt, or a shape or scoring the packed passes do not take) bit 20 is
+// set and bits 11-19 hold Q itself.  A counting sort over the 2^21 keys
+// orders the pairs by key: packed pairs of one row class form one set of
+// launches (sorted by window length, so a warp's pairs sweep similar
+// widths), generic pairs one launch per exact shape.
 #include "internal.h"
 
 namespace swift {
@@ -73,7 +74,7 @@ __global__ void __launch_bounds__(kVarWarps * 32) pack_var_kernel(VarPairArgs a)
     const bool gen = odd || R > a.fast_max_r || Q < 1 || R < 1 || cls < 0 ||
                      !((a.class_ok >> cls) & 1u);
     const uint32_t key = gen ? (1u << 20) | ((uint32_t)Q << 11) | (uint32_t)R
-                             : ((uint32_t)cls << 11) | (uint32_t)R;
+                             : ((uint32_t)(var_rows(Q) >> 3) << 11) | (uint32_t)R;
     a.key[i] = key;
     atomicAdd(&a.hist[key], 1u);
   }
