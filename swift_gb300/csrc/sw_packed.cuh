@@ -437,9 +437,10 @@ __global__ void __launch_bounds__(256) sw_walk_kernel(FastArgs a) {
   auto pick = [](const uint4& v, int w) -> uint32_t {
     return w == 0 ? v.x : w == 1 ? v.y : w == 2 ? v.z : v.w;
   };
-  // 2 UP, 1 LEFT, 0 DIAG or NONE
-  auto code_at = [&](int i, int jj) -> uint32_t {
-    const int ln = (i - 1) / RPL, k = (i - 1) % RPL;
+  // the 2-bit code (2 UP, 1 LEFT, 0 DIAG or NONE) of the cell in row
+  // ln * RPL + k + 1 (lane ln, its row k) and column jj: word
+  // (ln * S8 + jj + ln - 1) * kNW + k / 8 of the lane streams
+  auto code_at = [&](int ln, int k, int jj) -> uint32_t {
     const int64_t at = ((int64_t)ln * S8 + (jj + ln - 1)) * kNW + (k >> 3);
     const int64_t b = at >> 2;
     if (b < blk || b > blk + 2) {
@@ -483,18 +484,6 @@ __global__ void __launch_bounds__(256) sw_walk_kernel(FastArgs a) {
   uint32_t* qcw = cons ? reinterpret_cast<uint32_t*>(a.qcons + (int64_t)p * a.cons_stride) : nullptr;
   uint32_t* rcw = cons ? reinterpret_cast<uint32_t*>(a.rcons + (int64_t)p * a.cons_stride) : nullptr;
   uint32_t qacc = 0, racc = 0;
-  auto emit = [&](int tick, char r, char q) {
-    const int sh = 8 * (tick & 3);
-    racc |= (uint32_t)(uint8_t)r << sh;
-    qacc |= (uint32_t)(uint8_t)q << sh;
-    if ((tick & 3) == 3) {
-      if (cons) {
-        rcw[tick >> 2] = racc;
-        qcw[tick >> 2] = qacc;
-      }
-      racc = qacc = 0;
-    }
-  };
   // Directions of the reference's kernel (NONE, DIAG, UP, LEFT) from the
   // 2-bit codes and the cell's score h, which the walk carries: a cell
   // with code 0 is NONE exactly when h = 0 (any other cell has h > 0).
@@ -505,49 +494,53 @@ __global__ void __launch_bounds__(256) sw_walk_kernel(FastArgs a) {
   const int m = a.match, x = a.mismatch, o = a.gap_open, e = a.gap_ext;
   auto upc = [](char c) -> char { return (unsigned)(c - 'a') < 26u ? (char)(c - 32) : c; };
   const int2 b = a.best[p];
-  int cr = b.y / W, cc = b.y % W;
-  int h = b.x;                       // score of (cr, cc)
-  int d = (cr == 0 || cc == 0) ? kNone : dir_of(code_at(cr, cc), h);
-  // predecessor (nr, nc) of (cr, cc) and its score nh
-  int nr = cr, nc = cc, nh = h, nd = kNone;
-  auto advance = [&]() {
-    nr = cr - ((d == kDiag || d == kUp) ? 1 : 0);
-    nc = cc - ((d == kDiag || d == kLeft) ? 1 : 0);
-    if (d == kNone) {
-      nh = h;
-      nd = kNone;
-      return;
-    }
-    const uint32_t pc = (nr == 0 || nc == 0) ? 0u : code_at(nr, nc);
-    if (d == kDiag) {
-      const char qc = upc(qbyte(cr - 1)), rc = upc(wbyte(cc - 1));
-      const int sub = (qc == rc || qc == 'N' || rc == 'N') ? m : x;
-      nh = h - sub;
-    } else {
-      // the gap costs gap_ext when the predecessor itself moved the same way
-      const bool same = nr != 0 && nc != 0 && (d == kUp ? pc == 2u : pc == 1u);
-      nh = h - (same ? e : o);
-    }
-    nd = (nr == 0 || nc == 0) ? kNone : dir_of(pc, nh);
-  };
-  advance();
+  int cr = b.y / W, cc = b.y % W;  // current cell
+  int h = b.x;                     // its score
+  // its lane and row in the lane (kept as the walk moves up)
+  int ln = cr > 0 ? (cr - 1) / RPL : 0, k = cr > 0 ? (cr - 1) % RPL : 0;
+  int d = (cr == 0 || cc == 0) ? kNone : dir_of(code_at(ln, k, cc), h);
+  // One move per step: its consensus bytes (a gap where the row or column
+  // stays), then, unless it reached row or column 0, the predecessor's
+  // score (the substitution score for a DIAG move; for a gap, gap_ext when
+  // the predecessor itself moved the same way, else gap_open) and
+  // direction.  The walk ends at a NONE cell or at the border.
   int tick = -1, nref = -1, start = 0;
-  while ((cr != nr || cc != nc) && nc != 0 && nr != 0) {
+  while (d != kNone) {
+    const bool up = d != kLeft, left = d != kUp;  // row / column move
+    const char qc = qbyte(cr - 1), rc = wbyte(cc - 1);
     ++tick;
-    char rch = '-';
-    if (nc != cc) { rch = wbyte(cc - 1); ++nref; }
-    emit(tick, rch, nr == cr ? '-' : qbyte(cr - 1));
+    nref += left ? 1 : 0;
+    {
+      const int sh = 8 * (tick & 3);
+      racc |= (uint32_t)(uint8_t)(left ? rc : '-') << sh;
+      qacc |= (uint32_t)(uint8_t)(up ? qc : '-') << sh;
+      if ((tick & 3) == 3) {
+        if (cons) {
+          rcw[tick >> 2] = racc;
+          qcw[tick >> 2] = qacc;
+        }
+        racc = qacc = 0;
+      }
+    }
     start = cc;
-    cr = nr; cc = nc; h = nh; d = nd;
-    if (d == kNone) break;
-    advance();
-  }
-  if ((cr != nr || cc != nc) && (nc == 0 || nr == 0)) {
-    ++tick;
-    char rch = '-';
-    if (nc != cc) { rch = wbyte(cc - 1); ++nref; }
-    emit(tick, rch, nr == cr ? '-' : qbyte(cr - 1));
-    start = cc;
+    const int nr = cr - (up ? 1 : 0), nc = cc - (left ? 1 : 0);
+    if (nr == 0 || nc == 0) break;
+    if (up && --k < 0) {
+      k = RPL - 1;
+      --ln;
+    }
+    const uint32_t pc = code_at(ln, k, nc);
+    int nh;
+    if (d == kDiag) {
+      const char uq = upc(qc), ur = upc(rc);
+      nh = h - ((uq == ur || uq == 'N' || ur == 'N') ? m : x);
+    } else {
+      nh = h - ((d == kUp ? pc == 2u : pc == 1u) ? e : o);
+    }
+    cr = nr;
+    cc = nc;
+    h = nh;
+    d = dir_of(pc, nh);
   }
   if (cons && tick >= 0 && (tick & 3) != 3) {
     rcw[tick >> 2] = racc;
