@@ -51,11 +51,12 @@ def metric_for(args):
 TRACE_DRAM_BYTES_PER_PAIR = (134.6e6 + 1922.8e6) / 200000
 TRACE_ALGO_BYTES_PER_PAIR = 112 + 304 + 8 + 8 * 2 * 312 * 4 // 2
 # ALU-pipe instructions the trace pass issues per 2 cells (per lane), from
-# the same capture: 909.6 M warp instructions on the ALU pipe (86.05 % of its
-# 2 per SM per cycle over 3.477 M cycles on 152 SMs) for 6.0 G cells.
-TRACE_ALU_PER_2_CELLS = 9.70
-TRACE_NOTE = ("the trace formulation issues about 10 ALU instructions per 2 cells (first "
-              "maximum of every row, direction bits), so about 0.1 is its ceiling")
+# an ncu capture of the same launch: 794.6 M warp instructions on the ALU
+# pipe for 6.0 G cells (16.39 warp instructions in all per 2 cells).
+TRACE_ALU_PER_2_CELLS = 8.48
+TRACE_NOTE = ("the trace formulation issues about 8.5 ALU-pipe instructions per 2 cells (the "
+              "substitution permute, two DPX max ops, three masks, the first-maximum add-max) "
+              "and 16.4 instructions in all, so about 0.12 is its ceiling")
 SCORE_NOTE = ("the exact formulation issues about 6.5 ALU instructions per 2 cells, so about "
               "0.15 is its ceiling")
 
@@ -71,9 +72,13 @@ def parse_args():
     ap.add_argument("--format", default="default", choices=["default", "sam"],
                     help="output records: the default text or SAM (-f 1)")
     ap.add_argument("--reads", type=int, default=None)
+    ap.add_argument("--read-len", type=int, default=100,
+                    help="scale workload: read length (reads past 199 bases set max_read_len 300)")
+    ap.add_argument("--ref-mbp", type=int, default=50,
+                    help="scale workload: reference size in Mbp (24 sequences)")
     ap.add_argument("--cpu-sample", type=int, default=20000)
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--serve-workers", type=int, default=2,
+    ap.add_argument("--serve-workers", type=int, default=4,
                     help="serving: concurrent wave pipelines")
     ap.add_argument("--no-configs", action="store_true",
                     help="skip the short runs of the batched, long-region and serving "
@@ -169,13 +174,14 @@ def make_workload(args, rank):
         rn, rs, orig = synth.make_reads(seqs, n, 100, 0.01, 0.001, 0.0, seed=1 + rank)
         desc = "small: 1 Mbp / 1 seq, %d x 100 bp reads" % n
     else:
-        names, seqs = synth.make_reference(50_000_000, 24, sigma=0.8, repeat_frac=0.10,
-                                           n_units=500, unit_len=300, divergence=0.03, seed=0)
+        names, seqs = synth.make_reference(args.ref_mbp * 1_000_000, 24, sigma=0.8,
+                                           repeat_frac=0.10, n_units=500, unit_len=300,
+                                           divergence=0.03, seed=0)
         n = args.reads or 1_000_000
-        rn, rs, orig = synth.make_reads(seqs, n, 100, 0.01, 0.001, 0.05, seed=1 + rank)
-        desc = ("scale: 50 Mbp / 24 seqs (log-normal sigma 0.8, 10%% repeats of 500 x 300 bp "
-                "units at 3%% divergence), %d x 100 bp reads (1%% subs, 0.1%% indels, 5%% random)"
-                % n)
+        rn, rs, orig = synth.make_reads(seqs, n, args.read_len, 0.01, 0.001, 0.05, seed=1 + rank)
+        desc = ("scale: %d Mbp / 24 seqs (log-normal sigma 0.8, 10%% repeats of 500 x 300 bp "
+                "units at 3%% divergence), %d x %d bp reads (1%% subs, 0.1%% indels, 5%% random)"
+                % (args.ref_mbp, n, args.read_len))
     wl = {"seqs": seqs, "reads": rs, "origins": orig}
     return synth.fasta_bytes(names, seqs), synth.reads_fasta(rn, rs), n, desc, wl
 
@@ -186,13 +192,13 @@ def sample_reads(reads: bytes, n: int) -> bytes:
 
 
 def cpu_reference(ref: bytes, reads: bytes, n_sample: int, steps: int, warmup: int,
-                  seeder: int = 0, device_mem: int = 0):
+                  seeder: int = 0, device_mem: int = 0, max_read_len: int = 0):
     """The reference algorithm on the host cores (oracle port): reads/s,
     threads, seconds, and the last run's output (for the parity check)."""
     from oracle import oracle as O
     threads = os.cpu_count() or 1
     sess = O.Session(ref, O.default_params(threads=threads, seeder=seeder,
-                                           device_mem=device_mem))
+                                           device_mem=device_mem, max_read_len=max_read_len))
     sample = sample_reads(reads, n_sample)
     for _ in range(warmup):
         sess.align(sample)
@@ -600,7 +606,8 @@ def main():
         steps, warm = max(args.steps, 1), max(args.warmup, 0)
         n_sample = min(args.cpu_sample, n)
         rps, threads, dt, _ = cpu_reference(ref, reads, n_sample, steps, min(warm, 1),
-                                            1 if args.seeder == "lt13" else 0)
+                                            1 if args.seeder == "lt13" else 0,
+                                            max_read_len=300 if args.read_len > 199 else 0)
         line = {
             "impl": "reference", "metric": metric_for(args), "value": rps, "unit": "reads/s",
             "n_gpus": args.gpus, "steps": steps, "warmup": warm,
@@ -644,7 +651,9 @@ def main():
     rd = ctx.reads(reads)
     peak_cells = ctx.peak_dpx_cells_per_s()
     seeder = 1 if args.seeder == "lt13" else 0
-    params = sg.default_params(seeder=seeder, out_format=1 if args.format == "sam" else 0)
+    max_read = 300 if args.read_len > 199 else 0
+    params = sg.default_params(seeder=seeder, out_format=1 if args.format == "sam" else 0,
+                               max_read_len=max_read)
     # warm start: the index written to a file and read back (its load time)
     index_load_s = None
     try:
@@ -723,7 +732,8 @@ def main():
     model = cpu_model()
     try:
         rps, threads, dt, cpu_out = cpu_reference(ref, reads, k_cpu, 1, 0, seeder,
-                                                  device_mem=ctx.info()["total_mem"])
+                                                  device_mem=ctx.info()["total_mem"],
+                                                  max_read_len=max_read)
         cpu = {"value": rps, "unit": "reads/s", "cores": threads, "kind": "port",
                "cpu_model": model,
                "sample": f"{k_cpu} reads of the workload, index prebuilt"}
@@ -786,8 +796,8 @@ def main():
                    "peak_source": hbm_src + " HBM copy bandwidth",
                    "model": "per read strand ceil(L/4) + 32 B per k-mer lookup + "
                             "32 * ceil(5 n / 32) B per occupied bucket of n postings + 12 B "
-                            "per hit out; the bucket directory and postings (about 70 MB) "
-                            "stay resident in L2"}
+                            "per hit out; on the 50 Mbp reference the bucket directory and "
+                            "postings (about 70 MB) stay resident in L2"}
     # short seeded runs of BASELINE configs 2 and 3 (config 4, serving, below)
     configs = None
     if not args.no_configs and args.workload == "scale" and args.format == "default":

@@ -175,18 +175,17 @@ struct SeedArgs {
   int32_t* overflow_list;     // strands too big for the on-chip paths
   int32_t* n_overflow;
   int max_len;                // longest read (sizes the per-lane offsets)
-  int32_t* mid_list;          // strands for the hash-table kernel (zeroed count)
+  int32_t* mid_list;          // strands for the small hash-table kernel (zeroed count)
   int32_t* n_mid;
-  int32_t* big_list;          // strands for the sort kernel (zeroed count)
+  int32_t* big_list;          // strands for the large hash-table kernel (zeroed count)
   int32_t* n_big;
   unsigned long long* model_bytes;  // optional: kSeedModelSlots counters of
                                     // the roofline's sector-model bytes
   uint64_t* scratch;          // overflow path: per-strand hash tables
 };
 constexpr int kSeedModelSlots = 64;
-// The sort-free kernel over every strand, then the hash-table and sort
-// kernels over the strands it listed; strands beyond those go to
-// a.overflow_list.
+// The sort-free kernel over every strand, then the two hash-table kernels
+// over the strands it listed; strands beyond those go to a.overflow_list.
 void launch_seed(cudaStream_t st, const SeedArgs& a);
 
 // seed13.cu: lt13 seed-and-extend seeding (search2Queries)

@@ -36,6 +36,10 @@ __device__ __forceinline__ char qname_at(const FormatArgs& a, const DevPair& p, 
 }
 
 __device__ bool names_equal(const FormatArgs& a, const DevPair& s, const DevPair& t) {
+  // records of one read: the same name, or it and it + "*" (either strand),
+  // which the comparison below finds equal whenever the name and its '*'
+  // fit the slot
+  if (s.read == t.read && a.rd[s.read].name_len + 1 < kNameMax) return true;
   // qryNameCmp over the 50-byte name slots
   int i;
   for (i = 0; i < kNameMax; ++i) {

@@ -45,17 +45,24 @@ __device__ __forceinline__ uint32_t comp4(uint32_t x) {
 // Per read: 0 when its query (the first Q bytes, Q <= its length) is all
 // upper-case A, C, G, T, so that both strands' queries are whole-word
 // copies; else 1 (the per-byte path of build_pairs_kernel).
+constexpr int kClsRounds = 10;  // queries up to 320 bytes
+
 __global__ void read_class_kernel(PairArgs a) {
   const int lane = threadIdx.x & 31;
   const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (r >= a.n_reads) return;
   const DevRead rd = a.rd[r];
   const int Q = a.read_q ? a.read_q[r] : a.Q;
-  bool bad = rd.len < Q;
+  bool bad = rd.len < Q || Q > 32 * kClsRounds;
   const char* s = a.reads + rd.seq_off;
-  for (int i = lane; i < Q && !bad; i += 32) {
-    const char c = s[i];
-    bad = !(c == 'A' || c == 'C' || c == 'G' || c == 'T');
+  if (!bad) {
+    // every byte loaded before any is tested
+    char c[kClsRounds];
+#pragma unroll
+    for (int t = 0; t < kClsRounds; ++t) c[t] = lane + 32 * t < Q ? s[lane + 32 * t] : 'A';
+#pragma unroll
+    for (int t = 0; t < kClsRounds; ++t)
+      bad |= !(c[t] == 'A' || c[t] == 'C' || c[t] == 'G' || c[t] == 'T');
   }
   bad = __any_sync(0xffffffffu, bad);
   if (lane == 0) a.read_cls[r] = bad ? 1 : 0;
@@ -106,6 +113,10 @@ __global__ void __launch_bounds__(kPairWarps * 32) build_pairs_kernel(PairArgs a
   if (j >= a.n) return;
   char* tmp = tmp_all[wib];
   const int32_t read = a.m_read[j], strand = a.m_strand[j], ri = a.m_ri[j], rp = a.m_rp[j];
+  // the read's record and class, loaded with the reference record's
+  const DevRead rd = a.rd[read];
+  const int Q = a.read_q ? a.read_q[read] : a.Q;  // the read's request's query length
+  const bool words = a.read_cls && a.read_cls[read] == 0;
   const int32_t dist = rp - kShiftBases > 0 ? rp - kShiftBases : 0;
   const DevRecord& rec = a.recs[ri];
   const uint32_t off = (uint32_t)rec.seq_off + (uint32_t)dist +
@@ -118,9 +129,24 @@ __global__ void __launch_bounds__(kPairWarps * 32) build_pairs_kernel(PairArgs a
   // ACGTacgt bytes (no N to trim): a straight copy of the concatenated bases,
   // 16 bytes per lane.
   bool direct = false;
+  static_assert(kWinPad % 16 == 0 && kWin % 4 == 0 && kWinPad - kWin == 4,
+                "the last lane's fourth word is the padding");
+  uint32_t w[5] = {0, 0, 0, 0, 0};
+  uint32_t sh = 0;
   if (rec.regular && a.odd) {
     const uint64_t avail = rec.cat_len > (uint64_t)dist ? rec.cat_len - (uint64_t)dist : 0;
     if (avail >= (uint64_t)kWin) {
+      // the window's words are loaded while the bitmap of non-ACGT
+      // positions is (both in bounds of the record's concatenated bases)
+      if (lane < kWinPad / 16) {
+        // four output words from five aligned loads (the reads past the
+        // window's end stay inside the cat buffer's padding)
+        const uintptr_t ad = (uintptr_t)(a.cat + rec.cat_start + dist + 16 * lane);
+        const uint32_t* wp = reinterpret_cast<const uint32_t*>(ad & ~(uintptr_t)3);
+        sh = (uint32_t)(ad & 3) * 8;
+#pragma unroll
+        for (int q = 0; q < 5; ++q) w[q] = wp[q];
+      }
       const uint64_t g0 = rec.cat_start + (uint64_t)dist, g1 = g0 + kWin - 1;
       const uint64_t w0 = g0 >> 5;
       uint32_t bits = 0;
@@ -133,17 +159,7 @@ __global__ void __launch_bounds__(kPairWarps * 32) build_pairs_kernel(PairArgs a
     }
   }
   if (direct) {
-    static_assert(kWinPad % 16 == 0 && kWin % 4 == 0 && kWinPad - kWin == 4,
-                  "the last lane's fourth word is the padding");
     if (lane < kWinPad / 16) {
-      // four output words from five aligned loads (the reads past the
-      // window's end stay inside the cat buffer's padding)
-      const uintptr_t ad = (uintptr_t)(a.cat + rec.cat_start + dist + 16 * lane);
-      const uint32_t* wp = reinterpret_cast<const uint32_t*>(ad & ~(uintptr_t)3);
-      const uint32_t sh = (uint32_t)(ad & 3) * 8;
-      uint32_t w[5];
-#pragma unroll
-      for (int q = 0; q < 5; ++q) w[q] = wp[q];
       uint4 o;
       o.x = __funnelshift_r(w[0], w[1], sh);
       o.y = __funnelshift_r(w[1], w[2], sh);
@@ -204,13 +220,11 @@ __global__ void __launch_bounds__(kPairWarps * 32) build_pairs_kernel(PairArgs a
     }
   }  // window not copied directly
   // query
-  const DevRead rd = a.rd[read];
   const char* s = a.reads + rd.seq_off;
-  const int Q = a.read_q ? a.read_q[read] : a.Q;  // the read's request's query length
   if (a.pair_q && lane == 0) a.pair_q[j] = Q;
   const int avail = rd.len < Q ? rd.len : Q;
   char* qout = a.qbuf + j * (int64_t)a.Qs;
-  if (a.read_cls && a.read_cls[read] == 0) {
+  if (words) {
     // upper-case A, C, G, T only (avail = Q, not odd): whole words, the
     // reverse complement byte-reversed and complemented four at a time
     for (int i0 = 4 * lane; i0 < a.Qs; i0 += 128) {
