@@ -393,7 +393,7 @@ def serving_pool(seqs, pool_size: int, seed: int, max_len: int = SERVE_MAX_READ)
 
 
 def serving_run(idx, device, seqs, pool_size=120, per_load=200, loads=(0.8,), seed=3,
-                workers=2):
+                workers=4):
     """Serving on a resident index: the saturation throughput (every request
     of the pool queued at once), then Poisson arrivals at fractions of it,
     with per-request latency from submission to result (p50 / p99)."""
@@ -817,7 +817,8 @@ def main():
                                                    seed=0)
             s_idx = ctx.index(synth.fasta_bytes(s_names, s_seqs))
             with ClockSampler(device) as cclk:
-                configs["serving"] = serving_run(s_idx, device, s_seqs)
+                configs["serving"] = serving_run(s_idx, device, s_seqs,
+                                                 workers=args.serve_workers)
             configs["serving"]["clocks"] = cclk.summary()
             configs["serving"]["workload"] = ("serving: 200 Mbp / 24 seqs resident; request "
                                               "sizes log-uniform [1, 10000] reads")
