@@ -245,42 +245,43 @@ __global__ void __launch_bounds__(kSeedWarps * 32) seed_fast_kernel(SeedArgs a) 
 // a.big_list: kMidCap < hits <= kBigCap), without a sort.  The hits are
 // gathered cooperatively, hit h by lane h mod 32: the lookups that have
 // postings mark their first hit in a bit mask, and hit h belongs to the last
-// mark at or before it (found from the mask words, warp-uniform), every
-// posting load of the strand issued before any is used and kept in
-// registers.  Each hit enters a per-warp open-addressing table over its
-// cluster key (refIdx, shift + bias) that counts the cluster (at most half
-// full); the biggest count is a warp max over the hits' own counts.  Every
-// lane keeps the three smallest keys among its hits of that size (equal
-// keys merged, their offsets minimised), and the first clusters in key
-// order, each with its smallest query offset, are warp minima over those;
-// beyond three clusters a scan over the hits continues from the last key.
-// A strand's work grows with its hits, not with the table: the table is
-// emptied once per warp and each strand empties only the slots it used.
-// Warps stride over the list, whose length is on the device.
-template <int KM, int CAP, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32) seed_hash_kernel(SeedArgs a) {
-  constexpr unsigned long long kEmpty = ~0ull;  // above every cluster key
-  constexpr int kSlots = 2 * CAP;               // load <= 1/2
+// mark at or before it (found from the mask words, warp-uniform).  Each hit
+// enters a per-warp open-addressing table whose slot holds its cluster's key
+// (refIdx, shift + bias) above a 16-bit count: one compare-and-swap claims a
+// free slot with count 1, an add counts the hits of a slot already holding
+// the key; the table is at most two thirds full.  Hits are gathered and
+// entered in passes of half the rounds (every posting load of a pass issued
+// before any is used), and what a hit keeps afterwards is its query offset
+// and slot: its key and its cluster's size are in the table.  The biggest
+// count is a warp max; every lane keeps the three smallest keys of that
+// count among its hits (equal keys merged, their offsets minimised), and the
+// first clusters in key order, each with its smallest query offset, are
+// warp minima over those; beyond three clusters a scan over the hits
+// continues from the last key.  A strand's work grows with its hits, not
+// with the table: the table is emptied once per warp and each strand empties
+// only the slots it used.  Warps stride over the list, whose length is on
+// the device.
+template <int KM, int CAP, int WARPS, int MIN_BLOCKS>
+__global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) seed_hash_kernel(SeedArgs a) {
+  constexpr unsigned long long kEmpty = ~0ull;  // above every slot value
+  constexpr int kSlots = CAP + CAP / 2;         // load <= 2/3
   constexpr int kRounds = CAP / 32;             // hits per lane at most
+  constexpr int kPasses = CAP > 128 ? 2 : 1;    // gather and enter in passes
+  constexpr int kPassRounds = kRounds / kPasses;
   constexpr int kKeep = 3;                      // smallest keys kept per lane
-  static_assert(32 * KM <= 512 && kSlots <= 1024 && CAP < 1024, "meta bit fields");
-  __shared__ unsigned long long tkey_all[WARPS][kSlots];
-  __shared__ uint32_t tcnt_all[WARPS][kSlots];
+  static_assert(32 * KM <= 512 && kSlots <= 2048 && kRounds % kPasses == 0, "meta bit fields");
+  __shared__ unsigned long long tab_all[WARPS][kSlots];  // key << 16 | count
   __shared__ uint2 start_all[WARPS][CAP];       // first hit -> (posting - hit, offset)
   __shared__ uint32_t mark_all[WARPS][kRounds];  // first hits as bits
   __shared__ __align__(16) WarpSmem smem[WARPS];
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  unsigned long long* tkey = tkey_all[wib];
-  uint32_t* tcnt = tcnt_all[wib];
+  unsigned long long* tab = tab_all[wib];
   uint2* start = start_all[wib];
   uint32_t* mark = mark_all[wib];
   const bool big = CAP > kMidCap;
   const int64_t n_list = big ? *a.n_big : *a.n_mid;
   const int32_t* list = big ? a.big_list : a.mid_list;
-  for (int i = lane; i < kSlots; i += 32) {
-    tkey[i] = kEmpty;
-    tcnt[i] = 0;
-  }
+  for (int i = lane; i < kSlots; i += 32) tab[i] = kEmpty;
   for (int64_t t = (int64_t)blockIdx.x * WARPS + wib; t < n_list;
        t += (int64_t)gridDim.x * WARPS) {
     if (lane < kRounds) mark[lane] = 0;
@@ -310,61 +311,58 @@ __global__ void __launch_bounds__(WARPS * 32) seed_hash_kernel(SeedArgs a) {
       }
     }
     __syncwarp();
-    // per hit: its posting, then (refIdx, shift + bias); meta packs the
-    // query offset (bits 0-8), the table slot (9-18) and the cluster's count
-    uint2 ph[kRounds];
+    // per hit: its query offset (bits 0-8) and table slot (bits 9-20)
     uint32_t meta[kRounds];
     uint32_t carry = 0;  // the last first hit before the round (hit 0 is one)
 #pragma unroll
-    for (int r = 0; r < kRounds; ++r) {
-      meta[r] = 0;
-      ph[r] = make_uint2(0, 0);
-      if (32u * r < n) {
-        const uint32_t w = mark[r];
-        const uint32_t below = w & (0xffffffffu >> (31 - lane));
-        const uint32_t st = below ? 32u * r + 31u - __clz(below) : carry;
-        carry = w ? 32u * r + 31u - __clz(w) : carry;
-        const uint32_t h = lane + 32u * r;
-        if (h < n) {
-          const uint2 inf = start[st];
-          meta[r] = inf.y;
-          ph[r] = __ldg(&a.postings[inf.x + h]);
+    for (int ps = 0; ps < kPasses; ++ps) {
+      uint2 ph[kPassRounds];
+#pragma unroll
+      for (int q = 0; q < kPassRounds; ++q) {
+        const int r = ps * kPassRounds + q;
+        meta[r] = 0;
+        ph[q] = make_uint2(0, 0);
+        if (32u * r < n) {
+          const uint32_t w = mark[r];
+          const uint32_t below = w & (0xffffffffu >> (31 - lane));
+          const uint32_t st = below ? 32u * r + 31u - __clz(below) : carry;
+          carry = w ? 32u * r + 31u - __clz(w) : carry;
+          const uint32_t h = lane + 32u * r;
+          if (h < n) {
+            const uint2 inf = start[st];
+            meta[r] = inf.y;
+            ph[q] = __ldg(&a.postings[inf.x + h]);
+          }
         }
       }
-    }
 #pragma unroll
-    for (int r = 0; r < kRounds; ++r)
-      ph[r].x = (uint32_t)((int32_t)ph[r].x - (int32_t)meta[r] + kShiftBias);
-    auto key_of = [&](int r) -> unsigned long long {
-      return ((unsigned long long)ph[r].y << 32) | ph[r].x;
-    };
-#pragma unroll
-    for (int r = 0; r < kRounds; ++r) {
-      if (lane + 32u * r < n) {
-        const unsigned long long ck = key_of(r);
-        uint32_t slot = cluster_mix(ck) & (kSlots - 1);
-        for (int probe = 0; probe < kSlots; ++probe) {  // kSlots > n: a free slot exists
-          const unsigned long long old = atomicCAS(&tkey[slot], kEmpty, ck);
-          if (old == kEmpty || old == ck) {
-            atomicAdd(&tcnt[slot], 1u);
-            meta[r] |= slot << 9;
-            break;
+      for (int q = 0; q < kPassRounds; ++q) {
+        const int r = ps * kPassRounds + q;
+        if (lane + 32u * r < n) {
+          const unsigned long long key =
+              ((unsigned long long)ph[q].y << 32) |
+              (uint32_t)((int32_t)ph[q].x - (int32_t)meta[r] + kShiftBias);
+          uint32_t slot = (uint32_t)(((unsigned long long)cluster_mix(key) * kSlots) >> 32);
+          for (int probe = 0; probe < kSlots; ++probe) {  // kSlots > n: a free slot exists
+            const unsigned long long old = atomicCAS(&tab[slot], kEmpty, (key << 16) | 1ull);
+            if (old == kEmpty) break;
+            if ((old >> 16) == key) {
+              atomicAdd(&tab[slot], 1ull);
+              break;
+            }
+            slot = slot + 1 == (uint32_t)kSlots ? 0u : slot + 1;
           }
-          slot = (slot + 1) & (kSlots - 1);
+          meta[r] |= slot << 9;
         }
       }
     }
     __syncwarp();
-    // the biggest cluster over the hits' own counts; its hits as bits
+    auto slot_of = [&](int r) -> uint32_t { return (meta[r] >> 9) & 4095u; };
+    // the biggest cluster over the hits' own slots
     uint32_t bigc = 0;
 #pragma unroll
-    for (int r = 0; r < kRounds; ++r) {
-      if (lane + 32u * r < n) {
-        const uint32_t c = tcnt[(meta[r] >> 9) & 1023u];
-        meta[r] |= c << 19;
-        bigc = max(bigc, c);
-      }
-    }
+    for (int r = 0; r < kRounds; ++r)
+      if (lane + 32u * r < n) bigc = max(bigc, (uint32_t)(tab[slot_of(r)] & 0xFFFFu));
     bigc = __reduce_max_sync(0xffffffffu, bigc);
     // the lane's kKeep smallest keys of that size, ascending
     unsigned long long lk[kKeep];
@@ -376,21 +374,24 @@ __global__ void __launch_bounds__(WARPS * 32) seed_hash_kernel(SeedArgs a) {
     }
 #pragma unroll
     for (int r = 0; r < kRounds; ++r) {
-      if ((meta[r] >> 19) == bigc) {  // bigc >= 1: only real hits
-        unsigned long long k = key_of(r);
-        uint32_t o = meta[r] & 511u;
+      if (lane + 32u * r < n) {
+        const unsigned long long v = tab[slot_of(r)];
+        if ((uint32_t)(v & 0xFFFFu) == bigc) {
+          unsigned long long k = v >> 16;
+          uint32_t o = meta[r] & 511u;
 #pragma unroll
-        for (int q = 0; q < kKeep; ++q) {
-          if (k == lk[q]) {
-            lo[q] = min(lo[q], o);
-            k = kEmpty;
-          } else if (k < lk[q]) {
-            const unsigned long long tk = lk[q];
-            const uint32_t to = lo[q];
-            lk[q] = k;
-            lo[q] = o;
-            k = tk;
-            o = to;
+          for (int q = 0; q < kKeep; ++q) {
+            if (k == lk[q]) {
+              lo[q] = min(lo[q], o);
+              k = kEmpty;
+            } else if (k < lk[q]) {
+              const unsigned long long tk = lk[q];
+              const uint32_t to = lo[q];
+              lk[q] = k;
+              lo[q] = o;
+              k = tk;
+              o = to;
+            }
           }
         }
       }
@@ -430,9 +431,10 @@ __global__ void __launch_bounds__(WARPS * 32) seed_hash_kernel(SeedArgs a) {
         unsigned long long mk = kEmpty;
 #pragma unroll
         for (int r = 0; r < kRounds; ++r) {
-          if ((meta[r] >> 19) == bigc) {
-            const unsigned long long k = key_of(r);
-            if (k > last && k < mk) mk = k;
+          if (lane + 32u * r < n) {
+            const unsigned long long v = tab[slot_of(r)];
+            const unsigned long long k = v >> 16;
+            if ((uint32_t)(v & 0xFFFFu) == bigc && k > last && k < mk) mk = k;
           }
         }
         const uint32_t hmin = __reduce_min_sync(0xffffffffu, (uint32_t)(mk >> 32));
@@ -443,7 +445,7 @@ __global__ void __launch_bounds__(WARPS * 32) seed_hash_kernel(SeedArgs a) {
         uint32_t mi = 0xffffffffu;
 #pragma unroll
         for (int r = 0; r < kRounds; ++r)
-          if ((meta[r] >> 19) == bigc && key_of(r) == K) mi = min(mi, meta[r] & 511u);
+          if (lane + 32u * r < n && (tab[slot_of(r)] >> 16) == K) mi = min(mi, meta[r] & 511u);
         mi = __reduce_min_sync(0xffffffffu, mi);
         if (lane == 0) {
           const int32_t shift = (int32_t)lmin - kShiftBias;
@@ -458,12 +460,8 @@ __global__ void __launch_bounds__(WARPS * 32) seed_hash_kernel(SeedArgs a) {
     __syncwarp();
     // empty the slots this strand used (marks are cleared, starts rewritten)
 #pragma unroll
-    for (int r = 0; r < kRounds; ++r) {
-      if (lane + 32u * r < n) {
-        tkey[(meta[r] >> 9) & 1023u] = kEmpty;
-        tcnt[(meta[r] >> 9) & 1023u] = 0;
-      }
-    }
+    for (int r = 0; r < kRounds; ++r)
+      if (lane + 32u * r < n) tab[slot_of(r)] = kEmpty;
     __syncwarp();
   }
 }
@@ -579,11 +577,13 @@ void launch_seed_km(cudaStream_t st, const SeedArgs& a) {
   if (cudaGetDevice(&dev) == cudaSuccess &&
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && sms > 0)
     cap = (int64_t)sms * 8;
-  constexpr int kMidWarps = 8, kBigWarps = 3;
+  constexpr int kMidWarps = 8, kBigWarps = 4;
   const int64_t mid_blocks = std::min<int64_t>((strands + kMidWarps - 1) / kMidWarps, 2 * cap);
-  seed_hash_kernel<KM, kMidCap, kMidWarps><<<(unsigned)mid_blocks, kMidWarps * 32, 0, st>>>(a);
-  const int64_t big_blocks = std::min<int64_t>((strands + kBigWarps - 1) / kBigWarps, 2 * cap);
-  seed_hash_kernel<KM, kBigCap, kBigWarps><<<(unsigned)big_blocks, kBigWarps * 32, 0, st>>>(a);
+  seed_hash_kernel<KM, kMidCap, kMidWarps, 5>
+      <<<(unsigned)mid_blocks, kMidWarps * 32, 0, st>>>(a);
+  const int64_t big_blocks = std::min<int64_t>((strands + kBigWarps - 1) / kBigWarps, 4 * cap);
+  seed_hash_kernel<KM, kBigCap, kBigWarps, 5>
+      <<<(unsigned)big_blocks, kBigWarps * 32, 0, st>>>(a);
 }
 
 void launch_seed(cudaStream_t st, const SeedArgs& a) {
