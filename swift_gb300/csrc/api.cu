@@ -18,6 +18,32 @@
 
 using namespace swift;
 
+bool swift::global_bases(const std::vector<RefRecord>& recs, std::vector<uint32_t>* gbase) {
+  gbase->assign(recs.size() + 1, 0);
+  uint64_t at = kGPad;
+  for (size_t r = 0; r < recs.size(); ++r) {
+    (*gbase)[r] = (uint32_t)at;
+    at += recs[r].cat_len + kGPad;
+    if (at >= (1ull << 32) - 64) return false;
+  }
+  (*gbase)[recs.size()] = (uint32_t)at;
+  return true;
+}
+
+// The postings as global positions for the SSAHA seeding kernels (left null
+// when the reference is too long for them).
+int index_global_positions(swift_index* ix, cudaStream_t st) {
+  std::vector<uint32_t> gb;
+  if (ix->total <= 0 || !global_bases(ix->recs, &gb)) return SWIFT_OK;
+  if (cudaMalloc(&ix->d_gbase, gb.size() * sizeof(uint32_t)) != cudaSuccess ||
+      cudaMalloc(&ix->d_gpos, (size_t)ix->total * sizeof(uint32_t)) != cudaSuccess ||
+      cudaMemcpyAsync(ix->d_gbase, gb.data(), gb.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                      st) != cudaSuccess)
+    return SWIFT_E_CUDA;
+  launch_global_positions(st, ix->d_post, ix->total, ix->d_gbase, ix->d_gpos);
+  return cudaGetLastError() == cudaSuccess ? SWIFT_OK : SWIFT_E_CUDA;
+}
+
 namespace {
 
 int fail(swift_ctx* ctx, int code, const std::string& msg) {
@@ -464,6 +490,24 @@ int ensure_lt2(swift_ctx* ctx, const swift_index* cidx) {
   CK(cudaMalloc(&idx->d_post_pe, (size_t)std::max<int64_t>(src->total, 1) * sizeof(uint2)));
   if (src->total)
     CK(cudaMemcpy(idx->d_post_pe, post.data(), src->total * sizeof(uint2), cudaMemcpyHostToDevice));
+  // their global positions, when every position stays within 64 of its
+  // sequence (the keys then keep to their sequence's range)
+  std::vector<uint32_t> gb;
+  if (idx->d_gbase && src->total && global_bases(idx->recs, &gb)) {
+    std::vector<uint32_t> gpos((size_t)src->total);
+    bool ok = true;
+    for (int64_t i = 0; i < src->total && ok; ++i) {
+      const int32_t pos = (int32_t)post[i].x;
+      const uint32_t r = post[i].y;
+      ok = r < idx->recs.size() && pos >= -64 && pos <= (int64_t)idx->recs[r].cat_len + 64;
+      if (ok) gpos[i] = (uint32_t)((int64_t)gb[r] + pos);
+    }
+    if (ok) {
+      CK(cudaMalloc(&idx->d_gpos_pe, (size_t)src->total * sizeof(uint32_t)));
+      CK(cudaMemcpy(idx->d_gpos_pe, gpos.data(), src->total * sizeof(uint32_t),
+                    cudaMemcpyHostToDevice));
+    }
+  }
   idx->pe_ready = true;
   return SWIFT_OK;
 }
@@ -674,6 +718,9 @@ int run_seed(swift_ctx* ctx, const swift_index* idx, const swift_reads* rd, int 
     a.groups = idx->d_groups;
     a.cstart = idx->d_cstart;
     a.postings = idx->d_post;
+    a.gpos = idx->d_gpos;
+    a.gbase = idx->d_gbase;
+    a.n_recs = (int)idx->recs.size();
     a.k = idx->k;
     a.max_hits = max_hits;
     a.best = best;
@@ -1071,6 +1118,7 @@ int swift_index_build(swift_ctx* ctx, const char* ref, size_t len, int32_t k, in
                           ix->d_count, ix->d_offsets, d_cursor, ix->d_post);
     launch_order_buckets(st, ix->d_offsets, ix->nb, ix->d_post);
     CKI(cudaGetLastError());
+    if (index_global_positions(ix, st) != SWIFT_OK) CKI(cudaErrorMemoryAllocation);
     const int64_t ng = (ix->nb + 63) / 64;
     uint32_t *d_bits32, *d_gcnt, *d_grank, *d_nocc;
     CKI(sc.get(&d_bits32, (size_t)(ix->nb + 31) / 32));
@@ -1107,6 +1155,9 @@ int swift_index_destroy(swift_index* ix) {
   cudaFree(ix->d_tbase13);
   cudaFree(ix->d_ntup13);
   cudaFree(ix->d_post_pe);
+  cudaFree(ix->d_gpos);
+  cudaFree(ix->d_gbase);
+  cudaFree(ix->d_gpos_pe);
   if (ix->pe_sub) swift_index_destroy(ix->pe_sub);
   delete ix;
   return SWIFT_OK;
@@ -2690,6 +2741,9 @@ static int align_paired_impl(swift_ctx* ctx, const swift_index* idx, const char*
     a.cstart = src->d_cstart;
     a.offsets = src->d_offsets;
     a.postings = idx->d_post_pe;
+    a.gpos = idx->d_gpos_pe;
+    a.gbase = idx->d_gbase;
+    a.n_recs = (int)idx->recs.size();
     a.k = idx->k;
     a.max_hits = kHits;
     a.fixed_len = Q;

@@ -49,6 +49,11 @@ struct swift_index {
   uint4* d_groups = nullptr;   // compact bucket directory for seeding
   uint32_t* d_cstart = nullptr;
   uint2* d_post = nullptr;
+  // the postings as global positions (gbase[ref_idx] + ref_pos), for the
+  // SSAHA seeding kernels: half the bytes, and 32-bit cluster keys; null
+  // when the reference is too long for 32-bit positions
+  uint32_t* d_gpos = nullptr;
+  uint32_t* d_gbase = nullptr;
   int64_t total = 0;
   int64_t nb = 0;
   // lt13 seeding (seed13.cu), built on first use
@@ -68,6 +73,7 @@ struct swift_index {
   bool pe_ready = false;
   swift_index* pe_sub = nullptr;
   uint2* d_post_pe = nullptr;
+  uint32_t* d_gpos_pe = nullptr;  // its global positions (null: keys as pairs)
 };
 
 struct swift_reads {
@@ -88,3 +94,6 @@ int run_wave(swift_ctx* ctx, const swift_index* idx, const swift_params* p, cons
              size_t len, const std::vector<swift::DevRead>& rd, std::vector<swift::WaveReq>* wave,
              char* host_out, size_t host_cap, size_t* out_len, swift_stats* stats);
 int read_limit_of(const swift_params* p);
+// api.cu: the index's postings as global positions (for the seeding kernels);
+// SWIFT_OK also when the reference is too long for them (left null)
+int index_global_positions(swift_index* ix, cudaStream_t st);

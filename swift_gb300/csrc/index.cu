@@ -284,4 +284,18 @@ void launch_order_buckets(cudaStream_t st, const uint32_t* offsets, int64_t nb, 
   order_buckets_kernel<<<grid_for(nb, 256), 256, 0, st>>>(offsets, nb, post);
 }
 
+namespace {
+__global__ void global_pos_kernel(const uint2* __restrict__ post, int64_t n,
+                                  const uint32_t* __restrict__ gbase, uint32_t* __restrict__ gpos) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    gpos[i] = gbase[post[i].y] + post[i].x;
+}
+}  // namespace
+
+void launch_global_positions(cudaStream_t st, const uint2* post, int64_t n, const uint32_t* gbase,
+                             uint32_t* gpos) {
+  if (n > 0) global_pos_kernel<<<grid_for(n, 256), 256, 0, st>>>(post, n, gbase, gpos);
+}
+
 }  // namespace swift

@@ -148,6 +148,13 @@ void launch_scatter_tuples(cudaStream_t st, const uint32_t* packed, const DevRec
                            uint32_t thres, const uint32_t* count, const uint32_t* offsets,
                            uint32_t* cursor, uint2* post);
 void launch_order_buckets(cudaStream_t st, const uint32_t* offsets, int64_t nb, uint2* post);
+// gpos[i] = gbase[post[i].y] + post[i].x (the seeding kernels' global positions)
+void launch_global_positions(cudaStream_t st, const uint2* post, int64_t n, const uint32_t* gbase,
+                             uint32_t* gpos);
+// Per sequence its first global position: kGPad, then kGPad past the end of
+// the one before; false when the last end passes 2^32 - 64 (seeding then
+// keeps (ref_pos, ref_idx) keys).
+bool global_bases(const std::vector<RefRecord>& recs, std::vector<uint32_t>* gbase);
 
 // scan.cu
 size_t scan_temp_bytes(int64_t n);
@@ -166,6 +173,9 @@ struct SeedArgs {
   const uint4* groups;        // compact bucket directory (index.cu)
   const uint32_t* cstart;
   const uint2* postings;      // (ref_pos, ref_idx)
+  const uint32_t* gpos;       // optional, same order: gbase[ref_idx] + ref_pos
+  const uint32_t* gbase;      // with gpos: per sequence its first global position
+  int n_recs;
   int k;
   int max_hits;
   int fixed_len;              // > 0: every strand has this many bases (the
@@ -184,6 +194,8 @@ struct SeedArgs {
   uint64_t* scratch;          // overflow path: per-strand hash tables
 };
 constexpr int kSeedModelSlots = 64;
+// global positions: sequences kGPad apart, the first at kGPad
+constexpr uint32_t kGPad = 512;
 // The sort-free kernel over every strand, then the two hash-table kernels
 // over the strands it listed; strands beyond those go to a.overflow_list.
 void launch_seed(cudaStream_t st, const SeedArgs& a);

@@ -304,9 +304,10 @@ int swift_index_load(swift_ctx* ctx, const char* path, swift_index** out) {
     dr[i].regular = ix->recs[i].regular ? 1 : 0;
   }
   if (nr) CKL(cudaMemcpy(ix->d_recs, dr.data(), nr * sizeof(DevRecord), cudaMemcpyHostToDevice));
-  // derived from the bases, not stored
+  // derived from the bases and postings, not stored
   launch_odd_bits(nullptr, ix->d_cat, (int64_t)nw, ix->d_odd);
   CKL(cudaGetLastError());
+  if (index_global_positions(ix, nullptr) != SWIFT_OK) CKL(cudaErrorMemoryAllocation);
   CKL(cudaDeviceSynchronize());
 #undef CKL
   ix->lt13_ready = h.has_lt13 != 0;

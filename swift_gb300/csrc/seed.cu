@@ -136,6 +136,22 @@ __device__ __forceinline__ uint32_t cluster_mix(uint64_t x) {
   return (uint32_t)x;
 }
 
+// With global positions (a.gpos), a cluster key is the hit's global
+// position minus its query offset: sequence r's keys lie in
+// [gbase[r] - 319, gbase[r] + length + 64), and sequences sit kGPad = 512
+// positions apart, so the sequence of a key is the last r with
+// gbase[r] - 400 <= key (a binary search, for the few clusters emitted),
+// and keys order as (refIdx, shift) do.
+__device__ __forceinline__ int3 global_cluster(const SeedArgs& a, uint32_t key, int32_t qoff) {
+  int lo = 0, hi = a.n_recs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(&a.gbase[mid]) - 400u <= key) lo = mid; else hi = mid - 1;
+  }
+  const int32_t shift = (int32_t)(key - __ldg(&a.gbase[lo]));
+  return make_int3(lo, shift, shift + qoff);
+}
+
 // lane 0 adds one strand's model bytes (warp-uniform arguments)
 __device__ __forceinline__ void account(const SeedArgs& a, int lane, int L, int nq,
                                         uint32_t post_bytes, int hits_out) {
@@ -148,7 +164,7 @@ __device__ __forceinline__ int strand_nq(const SeedArgs& a, int L) {
   return (a.fixed_len > 0 ? a.fixed_len : L) - a.k + 1;
 }
 
-template <int KM>
+template <int KM, bool G>
 __global__ void __launch_bounds__(kSeedWarps * 32) seed_fast_kernel(SeedArgs a) {
   __shared__ __align__(16) WarpSmem smem[kSeedWarps];
   __shared__ uint2 info_all[kSeedWarps][kFastHits];
@@ -204,21 +220,27 @@ __global__ void __launch_bounds__(kSeedWarps * 32) seed_fast_kernel(SeedArgs a) 
   }
   smask = __reduce_or_sync(0xffffffffu, smask);
   __syncwarp();
-  // cluster key (refIdx, shift + bias); lanes without a hit get distinct
-  // keys above every real one
-  uint64_t ck = ~0ull - (uint64_t)lane;
-  uint32_t ri = 0;
+  // cluster key (refIdx, shift + bias), or the global shift; lanes without
+  // a hit get distinct keys above every real one
+  uint64_t ck = G ? (uint64_t)(0xffffffffu - (uint32_t)lane) : ~0ull - (uint64_t)lane;
+  uint32_t ri = 0, pidx = 0;
   int32_t shift = 0, qi = 0;
   if ((uint32_t)lane < n) {
     const int st = 31 - __clz(smask & (0xffffffffu >> (31 - lane)));
     const uint2 inf = info[st];
-    const uint2 p = __ldg(&a.postings[inf.x + (uint32_t)lane]);
-    ri = p.y;
     qi = (int32_t)inf.y;
-    shift = (int32_t)p.x - qi;
-    ck = ((uint64_t)ri << 32) | (uint32_t)(shift + kShiftBias);
+    pidx = inf.x + (uint32_t)lane;
+    if (G) {
+      ck = (uint64_t)(__ldg(&a.gpos[pidx]) - (uint32_t)qi);
+    } else {
+      const uint2 p = __ldg(&a.postings[inf.x + (uint32_t)lane]);
+      ri = p.y;
+      shift = (int32_t)p.x - qi;
+      ck = ((uint64_t)ri << 32) | (uint32_t)(shift + kShiftBias);
+    }
   }
-  const uint32_t same = __match_any_sync(0xffffffffu, ck);
+  const uint32_t same = G ? __match_any_sync(0xffffffffu, (uint32_t)ck)
+                          : __match_any_sync(0xffffffffu, ck);
   const uint32_t size = (uint32_t)lane < n ? (uint32_t)__popc(same) : 0u;
   const uint32_t biggest = __reduce_max_sync(0xffffffffu, size);
   // a cluster's first hit in key order is its lowest lane (offset order, and
@@ -233,7 +255,14 @@ __global__ void __launch_bounds__(kSeedWarps * 32) seed_fast_kernel(SeedArgs a) 
     const uint32_t hmin = __reduce_min_sync(0xffffffffu, in ? hi : 0xffffffffu);
     const uint32_t lmin = __reduce_min_sync(0xffffffffu, in && hi == hmin ? lo : 0xffffffffu);
     const uint32_t win = __ballot_sync(0xffffffffu, in && hi == hmin && lo == lmin);
-    if (lane == __ffs(win) - 1) out[got] = make_int3((int32_t)ri, shift, shift + qi);
+    if (lane == __ffs(win) - 1) {
+      if (G) {  // the winning hit's own posting
+        const uint2 p = __ldg(&a.postings[pidx]);
+        out[got] = make_int3((int32_t)p.y, (int32_t)p.x - qi, (int32_t)p.x);
+      } else {
+        out[got] = make_int3((int32_t)ri, shift, shift + qi);
+      }
+    }
     cand &= ~win;
     ++got;
   }
@@ -261,7 +290,7 @@ __global__ void __launch_bounds__(kSeedWarps * 32) seed_fast_kernel(SeedArgs a) 
 // with the table: the table is emptied once per warp and each strand empties
 // only the slots it used.  Warps stride over the list, whose length is on
 // the device.
-template <int KM, int CAP, int WARPS, int MIN_BLOCKS>
+template <int KM, int CAP, int WARPS, int MIN_BLOCKS, bool G>
 __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) seed_hash_kernel(SeedArgs a) {
   constexpr unsigned long long kEmpty = ~0ull;  // above every slot value
   constexpr int kSlots = CAP + CAP / 2;         // load <= 2/3
@@ -331,7 +360,10 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) seed_hash_kernel(SeedA
           if (h < n) {
             const uint2 inf = start[st];
             meta[r] = inf.y;
-            ph[q] = __ldg(&a.postings[inf.x + h]);
+            if (G)
+              ph[q].x = __ldg(&a.gpos[inf.x + h]);
+            else
+              ph[q] = __ldg(&a.postings[inf.x + h]);
           }
         }
       }
@@ -340,8 +372,9 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) seed_hash_kernel(SeedA
         const int r = ps * kPassRounds + q;
         if (lane + 32u * r < n) {
           const unsigned long long key =
-              ((unsigned long long)ph[q].y << 32) |
-              (uint32_t)((int32_t)ph[q].x - (int32_t)meta[r] + kShiftBias);
+              G ? (unsigned long long)(ph[q].x - meta[r])
+                : ((unsigned long long)ph[q].y << 32) |
+                      (uint32_t)((int32_t)ph[q].x - (int32_t)meta[r] + kShiftBias);
           uint32_t slot = (uint32_t)(((unsigned long long)cluster_mix(key) * kSlots) >> 32);
           for (int probe = 0; probe < kSlots; ++probe) {  // kSlots > n: a free slot exists
             const unsigned long long old = atomicCAS(&tab[slot], kEmpty, (key << 16) | 1ull);
@@ -411,7 +444,8 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) seed_hash_kernel(SeedA
       const uint32_t mi = __reduce_min_sync(0xffffffffu, mine ? lo[0] : 0xffffffffu);
       if (lane == 0) {
         const int32_t shift = (int32_t)lmin - kShiftBias;
-        out[got] = make_int3((int32_t)hmin, shift, shift + (int32_t)mi);
+        out[got] = G ? global_cluster(a, lmin, (int32_t)mi)
+                     : make_int3((int32_t)hmin, shift, shift + (int32_t)mi);
       }
       if (mine) {
 #pragma unroll
@@ -449,7 +483,8 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) seed_hash_kernel(SeedA
         mi = __reduce_min_sync(0xffffffffu, mi);
         if (lane == 0) {
           const int32_t shift = (int32_t)lmin - kShiftBias;
-          out[got] = make_int3((int32_t)hmin, shift, shift + (int32_t)mi);
+          out[got] = G ? global_cluster(a, lmin, (int32_t)mi)
+                       : make_int3((int32_t)hmin, shift, shift + (int32_t)mi);
         }
         last = K;
         ++got;
@@ -480,6 +515,7 @@ __device__ __forceinline__ uint32_t mix(uint64_t x) {
   return (uint32_t)x;
 }
 
+template <bool G>
 __global__ void __launch_bounds__(kOvThreads) seed_overflow_kernel(SeedArgs a,
                                                                    const uint64_t* tab_off,
                                                                    const uint32_t* tab_size) {
@@ -505,8 +541,13 @@ __global__ void __launch_bounds__(kOvThreads) seed_overflow_kernel(SeedArgs a,
     for (int t = k - 1; t >= 0; --t) h = (h << 2) | codes[i + t];
     uint32_t b = a.offsets[h], e = a.offsets[h + 1];
     for (uint32_t j = b + lane; j < e; j += 32) {
-      uint2 p = a.postings[j];
-      uint64_t ck = make_key(p.y, (int32_t)p.x - i, 0) >> 9;  // nonzero
+      uint64_t ck;  // nonzero
+      if (G) {
+        ck = (uint64_t)(a.gpos[j] - (uint32_t)i);
+      } else {
+        const uint2 p = a.postings[j];
+        ck = make_key(p.y, (int32_t)p.x - i, 0) >> 9;
+      }
       uint32_t slot = mix(ck) & (S - 1);
       for (uint32_t probe = 0; probe < S; ++probe) {
         unsigned long long old = atomicCAS((unsigned long long*)&tk[slot], 0ull,
@@ -553,9 +594,13 @@ __global__ void __launch_bounds__(kOvThreads) seed_overflow_kernel(SeedArgs a,
     if (threadIdx.x == 0) {
       uint32_t slot = mix(mn) & (S - 1);
       while (tk[slot] != mn) slot = (slot + 1) & (S - 1);
-      int32_t ri = (int32_t)(mn >> 32);
-      int32_t shift = (int32_t)(mn & 0xffffffffu) - kShiftBias;
-      out[got] = make_int3(ri, shift, shift + (int32_t)(1023u - ti[slot]));
+      if (G) {
+        out[got] = global_cluster(a, (uint32_t)mn, (int32_t)(1023u - ti[slot]));
+      } else {
+        int32_t ri = (int32_t)(mn >> 32);
+        int32_t shift = (int32_t)(mn & 0xffffffffu) - kShiftBias;
+        out[got] = make_int3(ri, shift, shift + (int32_t)(1023u - ti[slot]));
+      }
     }
     ++got;
     last = mn;
@@ -565,11 +610,11 @@ __global__ void __launch_bounds__(kOvThreads) seed_overflow_kernel(SeedArgs a,
 
 }  // namespace
 
-template <int KM>
-void launch_seed_km(cudaStream_t st, const SeedArgs& a) {
+template <int KM, bool G>
+void launch_seed_kg(cudaStream_t st, const SeedArgs& a) {
   const int64_t strands = 2 * a.n_reads;
   const unsigned grid = (unsigned)((strands + kSeedWarps - 1) / kSeedWarps);
-  seed_fast_kernel<KM><<<grid, kSeedWarps * 32, 0, st>>>(a);
+  seed_fast_kernel<KM, G><<<grid, kSeedWarps * 32, 0, st>>>(a);
   // the listed strands: grids of a few waves stride over the lists (their
   // lengths are on the device)
   int dev = 0, sms = 0;
@@ -579,11 +624,19 @@ void launch_seed_km(cudaStream_t st, const SeedArgs& a) {
     cap = (int64_t)sms * 8;
   constexpr int kMidWarps = 8, kBigWarps = 4;
   const int64_t mid_blocks = std::min<int64_t>((strands + kMidWarps - 1) / kMidWarps, 2 * cap);
-  seed_hash_kernel<KM, kMidCap, kMidWarps, 5>
+  seed_hash_kernel<KM, kMidCap, kMidWarps, 5, G>
       <<<(unsigned)mid_blocks, kMidWarps * 32, 0, st>>>(a);
   const int64_t big_blocks = std::min<int64_t>((strands + kBigWarps - 1) / kBigWarps, 4 * cap);
-  seed_hash_kernel<KM, kBigCap, kBigWarps, 5>
+  seed_hash_kernel<KM, kBigCap, kBigWarps, 5, G>
       <<<(unsigned)big_blocks, kBigWarps * 32, 0, st>>>(a);
+}
+
+template <int KM>
+void launch_seed_km(cudaStream_t st, const SeedArgs& a) {
+  if (a.gpos)
+    launch_seed_kg<KM, true>(st, a);
+  else
+    launch_seed_kg<KM, false>(st, a);
 }
 
 void launch_seed(cudaStream_t st, const SeedArgs& a) {
@@ -606,7 +659,10 @@ int seed_smem_cap() { return kBigCap; }
 void launch_seed_overflow(cudaStream_t st, const SeedArgs& a, int n_overflow,
                           const uint64_t* tab_off, const uint32_t* tab_size) {
   if (n_overflow <= 0) return;
-  seed_overflow_kernel<<<n_overflow, kOvThreads, 0, st>>>(a, tab_off, tab_size);
+  if (a.gpos)
+    seed_overflow_kernel<true><<<n_overflow, kOvThreads, 0, st>>>(a, tab_off, tab_size);
+  else
+    seed_overflow_kernel<false><<<n_overflow, kOvThreads, 0, st>>>(a, tab_off, tab_size);
 }
 
 }  // namespace swift

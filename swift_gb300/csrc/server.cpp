@@ -1,8 +1,9 @@
 // Serving loop with continuous batching.  The reference and index stay
 // resident on the device.  Requests (one reads FASTA each) are queued as
 // they come; workers (a context and stream each) take
-// every queued request of one query-length class, oldest first, up to a
-// read cap and a device-memory budget, and run them as ONE merged wave:
+// the queued requests of neighbouring query-length classes (packed shapes at
+// most twice as tall as each other), oldest first, up to a read cap and a
+// device-memory budget, and run them as ONE merged wave:
 // one seeding launch over all their reads, one set of Smith-Waterman
 // launches over all their pairs, one formatting pass.  Requests that arrive
 // while a wave runs join the next one; with two or more workers the next
@@ -11,9 +12,9 @@
 // Each request keeps what is its own when it runs alone (query length,
 // the stale-read tail of its 16-read loop, its Phase-2 batches), so its
 // records are byte-identical to swift_align on that request alone.
-// Requests of one class share the packed Smith-Waterman shape, so merging
-// them adds no cells: each pair's rows past its own query are the
-// all-mismatch rows the shape computes anyway.
+// A wave runs the packed Smith-Waterman shapes of its tallest class; each
+// pair's rows past its own query are all-mismatch rows, so a request of a
+// shorter class gets its own results from them (at up to twice the rows).
 #include <stdlib.h>
 #include <string.h>
 
@@ -46,7 +47,8 @@ struct Request {
   std::vector<char> reads;
   HostReads hr;              // its reads, parsed by the worker that takes it
   int32_t Q = 0;             // its query length
-  int cls = 0;               // packed shape class of Q: one class per wave
+  int cls = 0;               // packed shape class of Q (a wave spans classes whose
+                             // shapes are at most twice as tall as each other)
   std::vector<int32_t> repeats;
   int64_t est_bytes = 0;
   int64_t est_reads = 0;     // its '>' count, before it is parsed
@@ -234,18 +236,25 @@ void worker(swift_server* s, int wi) {
         return s->in_flight + f->est_bytes <= s->budget || s->in_flight == 0;
       });
       if (s->stop && s->queue.empty()) return;
-      const int cls = s->queue.front()->cls;
+      // requests of query-length classes whose packed shapes are at most
+      // twice as tall as each other's share the wave: the wave runs the
+      // tallest class's shapes, rows past a shorter query are the
+      // all-mismatch rows those shapes compute anyway
+      int lo = s->queue.front()->cls, hi = lo;
       int64_t reads = 0, est = 0;
       for (auto it = s->queue.begin(); it != s->queue.end();) {
         Request* r = *it;
         const bool first = take.empty();
         const int64_t nr = r->est_reads;
-        if (r->cls == cls &&
+        const int nlo = std::min(lo, r->cls), nhi = std::max(hi, r->cls);
+        if (packed_class_max_q(nhi) <= 2 * packed_class_max_q(nlo) &&
             (first || (reads + nr <= kWaveMaxReads &&
                        s->in_flight + est + r->est_bytes <= s->budget))) {
           take.push_back(r);
           reads += nr;
           est += r->est_bytes;
+          lo = nlo;
+          hi = nhi;
           it = s->queue.erase(it);
         } else {
           ++it;
