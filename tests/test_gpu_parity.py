@@ -472,6 +472,30 @@ def test_align_into_overlapped_copies(ctx, sg):
         assert e.value.code == -5
 
 
+def test_align_into_large_calls(ctx, sg):
+    # 140,007 reads through the host-buffer call (text in record ranges,
+    # each copied while the next is written): the same bytes as swift_align,
+    # with a stale 16-read tail, both output formats and both seeders, also
+    # where every read has the same name (one best-per-read group)
+    import torch
+    from swift_gb300 import synth
+    names, seqs = synth.make_reference(2_000_000, 4, sigma=0.5, repeat_frac=0.1, n_units=30,
+                                       unit_len=300, divergence=0.03, seed=14)
+    ref = synth.fasta_bytes(names, seqs)
+    rn, rs, _ = synth.make_reads(seqs, 140_007, 100, 0.01, 0.001, 0.05, seed=15)
+    ix = ctx.index(ref)
+    for reads in (synth.reads_fasta(rn, rs), synth.reads_fasta(["dup"] * len(rs), rs)):
+        src = torch.empty(len(reads), dtype=torch.uint8, pin_memory=True)
+        src.numpy()[:] = memoryview(reads)
+        for kw in (dict(), dict(out_format=1), dict(seeder=1)):
+            p = sg.default_params(**kw)
+            want, st = ctx.align(ix, reads, p, stats=True)
+            out = torch.zeros(len(want) + 16, dtype=torch.uint8, pin_memory=True)
+            n, st2 = ctx.align_into(ix, src.data_ptr(), len(reads), out.data_ptr(), len(out), p)
+            assert n == len(want) and out.numpy()[:n].tobytes() == want, kw
+            assert st2["reads"] == st["reads"] and st2["printed"] == st["printed"], kw
+
+
 def test_cli_matches_oracle(ctx, oracle, sg):
     ref, reads = small_case(n_reads=300, seed=55)
     with tempfile.TemporaryDirectory() as d:
