@@ -220,23 +220,13 @@ __global__ void fill_matches_kernel(const int32_t* __restrict__ nbest, const int
 __global__ void partition_pairs_kernel(const DevPair* __restrict__ pairs, int64_t n, int all_generic,
                                        int32_t* fast, int32_t* n_fast, int32_t* gen,
                                        int32_t* n_gen) {
-  // warp-aggregated appends: one atomic per warp and list
+  // block-aggregated appends: one atomic per block and list
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int lane = threadIdx.x & 31;
   const bool valid = i < n;
   const bool g = valid && (all_generic || (pairs[i].flags & 1));
   const bool f = valid && !g;
-  const uint32_t bg = __ballot_sync(0xffffffffu, g), bf = __ballot_sync(0xffffffffu, f);
-  int32_t base_g = 0, base_f = 0;
-  if (lane == 0) {
-    if (bg) base_g = atomicAdd(n_gen, __popc(bg));
-    if (bf) base_f = atomicAdd(n_fast, __popc(bf));
-  }
-  base_g = __shfl_sync(0xffffffffu, base_g, 0);
-  base_f = __shfl_sync(0xffffffffu, base_f, 0);
-  const uint32_t below = (1u << lane) - 1;
-  if (g) gen[base_g + __popc(bg & below)] = (int32_t)i;
-  if (f) fast[base_f + __popc(bf & below)] = (int32_t)i;
+  block_append(g, (int32_t)i, gen, n_gen);
+  block_append(f, (int32_t)i, fast, n_fast);
 }
 
 // Printed pairs of the packed path that have not been traced yet (with
@@ -247,17 +237,10 @@ __global__ void traceback_list_kernel(const DevPair* __restrict__ pairs,
                                       const int32_t* __restrict__ cand, int64_t n, int all_generic,
                                       int32_t* list, int32_t* cnt, int32_t* printed) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int lane = threadIdx.x & 31;
   const bool k = i < n && keep[i];
   const bool t = k && !all_generic && !(pairs[i].flags & 1) && !(cand && cand[i] == (int32_t)i);
-  const uint32_t b = __ballot_sync(0xffffffffu, t), bk = __ballot_sync(0xffffffffu, k);
-  int32_t base = 0;
-  if (lane == 0) {
-    if (b) base = atomicAdd(cnt, __popc(b));
-    if (bk) atomicAdd(printed, __popc(bk));
-  }
-  base = __shfl_sync(0xffffffffu, base, 0);
-  if (t) list[base + __popc(b & ((1u << lane) - 1))] = (int32_t)i;
+  block_append(t, (int32_t)i, list, cnt);
+  block_count(k, printed);
 }
 
 // Early-stop order of a pair list.  The exact passes stop a warp once the

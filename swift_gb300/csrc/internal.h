@@ -156,6 +156,38 @@ void launch_global_positions(cudaStream_t st, const uint2* post, int64_t n, cons
 // keeps (ref_pos, ref_idx) keys).
 bool global_bases(const std::vector<RefRecord>& recs, std::vector<uint32_t>* gbase);
 
+#ifdef __CUDACC__
+// Appends the ids whose flag is set to list with one atomic per block on
+// cnt (list order within and across blocks is arbitrary).  Every thread of
+// the block calls it, blocks of at most 1024 threads.
+__device__ __forceinline__ void block_append(bool flag, int32_t id, int32_t* list, int32_t* cnt) {
+  __shared__ int32_t wsum[32];
+  __shared__ int32_t base;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  const uint32_t b = __ballot_sync(0xffffffffu, flag);
+  if (lane == 0) wsum[wid] = __popc(b);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int32_t t = 0;
+    for (int w = 0; w < nw; ++w) {
+      const int32_t c = wsum[w];
+      wsum[w] = t;
+      t += c;
+    }
+    base = t ? atomicAdd(cnt, t) : 0;
+  }
+  __syncthreads();
+  if (flag) list[base + wsum[wid] + __popc(b & ((1u << lane) - 1))] = id;
+  __syncthreads();  // wsum and base free for the next call
+}
+
+// Adds the block's count of set flags to cnt with one atomic.
+__device__ __forceinline__ void block_count(bool flag, int32_t* cnt) {
+  const int32_t c = __syncthreads_count(flag);
+  if (threadIdx.x == 0 && c) atomicAdd(cnt, c);
+}
+#endif
+
 // scan.cu
 size_t scan_temp_bytes(int64_t n);
 // Each returns the number of kernels it launched.

@@ -82,16 +82,6 @@ __global__ void select_kernel(FormatArgs a) {
   for (int64_t i = j; i <= e; ++i) a.keep[i] = i == keep ? 1 : 0;
 }
 
-// Appends the flagged ids of a warp to list with one atomic.
-__device__ __forceinline__ void warp_append(bool flag, int32_t id, int32_t* list, int32_t* cnt) {
-  const int lane = threadIdx.x & 31;
-  const uint32_t b = __ballot_sync(0xffffffffu, flag);
-  int32_t base = 0;
-  if (lane == 0 && b) base = atomicAdd(cnt, __popc(b));
-  base = __shfl_sync(0xffffffffu, base, 0);
-  if (flag) list[base + __popc(b & ((1u << lane) - 1))] = id;
-}
-
 // Bounded selection, step 1: per best-per-read group (the groups of
 // select_kernel) the candidate is the first pair with the largest key, the
 // exact score for pairs of the generic kernel and the upper bound for the
@@ -118,7 +108,7 @@ __global__ void candidate_kernel(FormatArgs a, int32_t* list, int32_t* cnt) {
       app = !(a.pairs[best].flags & 1);
     }
   }
-  warp_append(app, cand, list, cnt);
+  block_append(app, cand, list, cnt);
 }
 
 // Bounded selection, step 2 (after the candidates' exact scores): a
@@ -140,7 +130,7 @@ __global__ void prune_kernel(FormatArgs a, DevAln* aln, int32_t* list, int32_t* 
       }
     }
   }
-  warp_append(app, (int32_t)i, list, cnt);
+  block_append(app, (int32_t)i, list, cnt);
 }
 
 // The same rule over a list of pairs (none of them a candidate) after a
@@ -160,7 +150,7 @@ __global__ void prune_list_kernel(FormatArgs a, DevAln* aln, const int32_t* in, 
       aln[i].score = -1;
     }
   }
-  warp_append(app, i, list, cnt);
+  block_append(app, i, list, cnt);
 }
 
 __device__ __forceinline__ int ndigits(int v) {
