@@ -240,8 +240,9 @@ typedef struct {
 } swift_pairs_stats;
 
 /* Packed-shape choice of swift_sw_pairs: 1 (default) times the candidate
- * (lanes, rows per lane) shapes of each query class and window bin on a
- * sample of the call's pairs the first time the context meets them, and
+ * (lanes, rows per lane) shapes of each row class and window bin (with at
+ * least 1,024 pairs) on a sample of the call's pairs the first time the
+ * context meets them, and
  * keeps the fastest for the context; 0 uses the fixed default shapes;
  * k >= 2 runs the (k - 2)-th candidate of every class (the default when it
  * has fewer).  All give identical results. */
@@ -258,9 +259,10 @@ int swift_ctx_set_tuning(swift_ctx *ctx, int32_t mode);
  * pairs beyond 256 x 1024 (or q_len > 128 with r_len > 768) run on the long
  * kernel, one CTA each, which needs negative mismatch and gap penalties.
  * Inputs all host or all device memory; outputs likewise.
- *   mode 0 (batched): pairs sorted by (q_len, r_len) on the device, one set
- *          of launches per shape: packed 16-bit passes for pairs of ACGT
- *          bytes, the int32 kernel for the rest;
+ *   mode 0 (batched): pairs sorted on the device by row class (q_len rounded
+ *          up to 8 rows up to 128, 16 up to 256) and r_len, one set of
+ *          launches per class: packed 16-bit passes for pairs of ACGT bytes,
+ *          the int32 kernel for the rest;
  *   mode 1 (plain): every pair padded to the largest shape, one launch of
  *          the int32 kernel, as the reference runs a batch (pairs up to
  *          256 x 1024 only).  Padding leaves

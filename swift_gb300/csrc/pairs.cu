@@ -119,8 +119,6 @@ __global__ void __launch_bounds__(kPairWarps * 32) build_pairs_kernel(PairArgs a
   const bool words = a.read_cls && a.read_cls[read] == 0;
   const int32_t dist = rp - kShiftBases > 0 ? rp - kShiftBases : 0;
   const DevRecord& rec = a.recs[ri];
-  const uint32_t off = (uint32_t)rec.seq_off + (uint32_t)dist +
-                       (rec.bpl > 0 ? (uint32_t)dist / rec.bpl : 0u);
   int got = 0;
   char* wout = a.wbuf + j * kWinPad;
   bool odd = false;  // a byte the packed score pass does not take
@@ -180,6 +178,10 @@ __global__ void __launch_bounds__(kPairWarps * 32) build_pairs_kernel(PairArgs a
         if (i < got) tmp[i] = src[i];
       }
     } else {
+      // the file offset refMapGetOffsets gives (only irregular records
+      // read the file bytes)
+      const uint32_t off = (uint32_t)rec.seq_off + (uint32_t)dist +
+                           (rec.bpl > 0 ? (uint32_t)dist / rec.bpl : 0u);
       got = fetch_window(a, off, tmp, lane);
     }
     __syncwarp();
