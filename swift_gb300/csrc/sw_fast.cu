@@ -297,10 +297,10 @@ int launch_bound(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {
 int launch_walk(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {
   const Shape s = shape_of(a);
   if (s.G == 0 || max_pairs <= 0) return 0;
-  const unsigned grid = (unsigned)((max_pairs + 255) / 256);
+  const unsigned grid = (unsigned)((max_pairs + kWalkThreads - 1) / kWalkThreads);
 #define SWIFT_WK(G_, R_)                                      \
   if (s.G == G_ && s.RPL == R_) {                              \
-    sw_walk_kernel<G_, R_><<<grid, 256, 0, st>>>(a);           \
+    sw_walk_kernel<G_, R_><<<grid, kWalkThreads, 0, st>>>(a);  \
     return 1;                                                  \
   }
   SWIFT_WK(8, 4)

@@ -406,8 +406,10 @@ __global__ void __launch_bounds__(kPkWarps * 32, (TRACE || RPL > 13) ? 2 : 3) sw
 // Traceback walk (src/smithWaterman.cu:911-1026), one thread per printed
 // pair: dependent loads of the 4-bit directions the trace pass streamed out;
 // many walks in flight hide each other's latency.
+constexpr int kWalkThreads = 128;  // small blocks: walks of uneven length leave SMs sooner
+
 template <int G, int RPL>
-__global__ void __launch_bounds__(256) sw_walk_kernel(FastArgs a) {
+__global__ void __launch_bounds__(kWalkThreads) sw_walk_kernel(FastArgs a) {
   constexpr int kGroups = 32 / G;
   constexpr int kPairs = 2 * kGroups;
   constexpr int kNW = DirLayout<RPL>::kWords;

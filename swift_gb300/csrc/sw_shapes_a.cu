@@ -31,7 +31,7 @@ int launch_trace_var_a(int G, int RPL, unsigned grid, size_t smem, cudaStream_t 
 int launch_walk_a(int G, int RPL, unsigned grid, cudaStream_t st, const FastArgs& a) {
 #define SWIFT_WKX(G_, R_)                                      \
   if (G == G_ && RPL == R_) {                                  \
-    sw_walk_kernel<G_, R_><<<grid, 256, 0, st>>>(a);           \
+    sw_walk_kernel<G_, R_><<<grid, kWalkThreads, 0, st>>>(a);  \
     return 1;                                                  \
   }
   SWIFT_WKX(8, 5)
