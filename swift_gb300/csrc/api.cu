@@ -272,6 +272,30 @@ __global__ void stop_key_count_kernel(const int32_t* __restrict__ list, const in
   if (threadIdx.x <= kSufBlocks && h[threadIdx.x]) atomicAdd(&hist[threadIdx.x], h[threadIdx.x]);
 }
 
+// Trace order of the candidates (no bound pass has run for them; they stop
+// early on the suffix LCS values).  Key: the LCS bound's shortfall from a
+// whole-query match, largest first: reads with no true window (their trace
+// runs to the window's end) come first and share warps, and the pairs that
+// stop once their alignment ends share the rest.
+__global__ void cand_key_count_kernel(const int32_t* __restrict__ list, const int32_t* __restrict__ n,
+                                      const uint8_t* __restrict__ lsuf,
+                                      const int32_t* __restrict__ q_len, int Q,
+                                      int32_t* __restrict__ keys, int32_t* hist) {
+  __shared__ int32_t h[kSufBlocks + 1];
+  if (threadIdx.x <= kSufBlocks) h[threadIdx.x] = 0;
+  __syncthreads();
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < *n) {
+    const int32_t p = list[i];
+    const int shortfall = (q_len ? q_len[p] : Q) - (int)lsuf[(int64_t)p * kSufBlocks];
+    const int k = kSufBlocks - min(kSufBlocks, max(shortfall, 0));
+    keys[i] = k;
+    atomicAdd(&h[k], 1);
+  }
+  __syncthreads();
+  if (threadIdx.x <= kSufBlocks && h[threadIdx.x]) atomicAdd(&hist[threadIdx.x], h[threadIdx.x]);
+}
+
 __global__ void stop_key_scatter_kernel(const int32_t* __restrict__ list, const int32_t* __restrict__ n,
                                         const int32_t* __restrict__ keys,
                                         const int32_t* __restrict__ hist, int32_t* fill,
@@ -2221,16 +2245,21 @@ static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swi
   fa2.q_len = pair_q;
   int32_t *ub = nullptr, *cand = nullptr;
   uint16_t* suf = nullptr;
+  uint8_t* lsuf = nullptr;  // suffix LCS values: the candidates' early stop
   if (bounded) {
     CK(sc.get(&ub, nn));
     CK(sc.get(&cand, nn));
     CK(sc.get(&suf, nn * kSufBlocks));
+    if (Q <= 255) CK(sc.get(&lsuf, nn * kSufBlocks));
   }
   fa2.ub = ub;
   fa2.suf = suf;
+  fa2.lsuf = lsuf;
+  // cells computed: [0] score passes and later traces, [1] the candidates'
+  // trace pass
   unsigned long long* d_cells;
-  CK(sc.get(&d_cells, 1));
-  CK(cudaMemsetAsync(d_cells, 0, sizeof(unsigned long long), st));
+  CK(sc.get(&d_cells, 2));
+  CK(cudaMemsetAsync(d_cells, 0, 2 * sizeof(unsigned long long), st));
   fa2.cells_done = d_cells;
   CK(cudaEventRecord(ctx->ev[7], st));
   if (fast_ok && nproc > 0 && !sam) {
@@ -2320,14 +2349,18 @@ static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swi
   }
   const int m_max = (kWin - 1) / kSufSteps;
   int sort_uses = 0;
+  // (cand_order: the candidates' key from the suffix LCS values instead)
   auto sort_by_stop = [&](const int32_t* list, const int32_t* count, int64_t max_n,
-                          int32_t* out) -> int {
+                          int32_t* out, bool cand_order) -> int {
     if (max_n <= 0) return SWIFT_OK;
     int32_t* hist = cnt + 8 + 2 * (kSufBlocks + 1) * sort_uses;
     int32_t* fill = hist + (kSufBlocks + 1);
     ++sort_uses;
     const unsigned grid = (unsigned)((max_n + 255) / 256);
-    stop_key_count_kernel<<<grid, 256, 0, st>>>(list, count, ub, suf, m_max, keys, hist);
+    if (cand_order)
+      cand_key_count_kernel<<<grid, 256, 0, st>>>(list, count, lsuf, pair_q, Q, keys, hist);
+    else
+      stop_key_count_kernel<<<grid, 256, 0, st>>>(list, count, ub, suf, m_max, keys, hist);
     stop_key_scatter_kernel<<<grid, 256, 0, st>>>(list, count, keys, hist, fill, out);
     CKLAUNCH();
     launches += 2;
@@ -2356,9 +2389,18 @@ static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swi
     CK(cudaEventRecord(ctx->ev[6], st));
     cand_n = h_cnt[2];
     fa2.suf = nullptr;
-    rc = trace_list(tb_list, cnt + 2, cand_n, true);
+    fa2.cells_done = d_cells + 1;
+    int32_t* cand_list = tb_list;
+    if (lsuf) {
+      rc = sort_by_stop(tb_list, cnt + 2, cand_n, sorted, true);
+      if (rc != SWIFT_OK) return rc;
+      cand_list = sorted;
+    }
+    rc = trace_list(cand_list, cnt + 2, cand_n, true);
     if (rc != SWIFT_OK) return rc;
     fa2.suf = suf;
+    fa2.lsuf = nullptr;
+    fa2.cells_done = d_cells;
     // pairs whose LCS bound cannot rule them out against their candidate's
     // score get the relaxed bound, then the same test again
     int32_t* k1_list = fast_list;  // free once the LCS pass has run
@@ -2384,7 +2426,7 @@ static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swi
     CK(cudaMemcpyAsync(h_cnt, cnt, sizeof(h_cnt), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     const int64_t ex_max = h_cnt[6];
-    rc = sort_by_stop(k2_list, cnt + 6, ex_max, sorted);
+    rc = sort_by_stop(k2_list, cnt + 6, ex_max, sorted, false);
     if (rc != SWIFT_OK) return rc;
     fa2.list = sorted;
     fa2.count = cnt + 6;
@@ -2422,8 +2464,9 @@ static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swi
   uint64_t total = 0;
   CK(cudaMemcpyAsync(&total, tot_d, 8, cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(h_cnt, cnt, sizeof(h_cnt), cudaMemcpyDeviceToHost, st));
-  unsigned long long h_cells = 0, h_model[kSeedModelSlots] = {};
-  CK(cudaMemcpyAsync(&h_cells, d_cells, sizeof(h_cells), cudaMemcpyDeviceToHost, st));
+  unsigned long long h_cells2[2] = {0, 0}, h_model[kSeedModelSlots] = {};
+  CK(cudaMemcpyAsync(h_cells2, d_cells, sizeof(h_cells2), cudaMemcpyDeviceToHost, st));
+  const unsigned long long h_cells = h_cells2[0] + h_cells2[1];
   // a wave: each request's text starts at its first record's offset
   std::vector<uint64_t> h_t0;
   if (wave) {
@@ -2474,15 +2517,15 @@ static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swi
     s.pairs_ms = t;
     cudaEventElapsedTime(&t, ctx->ev[2], ctx->ev[3]);
     s.sw_ms = t;
-    // the trace pass over every cell of its pairs: all packed pairs (SAM) or
-    // the candidates (bounded selection; no early stop for them)
+    // the trace pass of all packed pairs (SAM, whole windows) or of the
+    // candidates (bounded selection, up to their early stop)
     double trace_sum = 0;
     for (int c = 0; c < timed_chunks; ++c) {
       cudaEventElapsedTime(&t, ctx->chunk_ev[2 * c], ctx->chunk_ev[2 * c + 1]);
       trace_sum += t;
     }
     s.trace_ms = trace_sum;
-    s.trace_cells = (sam ? (int64_t)h_cnt[0] : cand_n) * Q * kWin;
+    s.trace_cells = sam ? (int64_t)h_cnt[0] * Q * kWin : (int64_t)h_cells2[1];
     if (!sam) {
       cudaEventElapsedTime(&t, ctx->ev[7], ctx->ev[8]);
       s.first_pass_ms = t;

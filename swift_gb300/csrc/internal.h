@@ -495,6 +495,10 @@ struct FastArgs {
                               // exact passes and walk; 0: the default for Q
   uint32_t one, four;         // trace pass: 1 and 4, as values the compiler cannot
                               // fold (set by launch_sw_trace)
+  uint8_t* lsuf;              // LCS bound pass writes, per pair, kSufBlocks suffix
+                              // LCS values: entry m = LCS(query, window columns
+                              // kSufSteps * m + 1 .. R); the trace pass (with no
+                              // suf) reads them to stop early; may be null
 };
 bool fast_params_ok(int Q, int R, int m, int x, int o, int e, int* bias);
 constexpr int kFastMaxR = 512;  // window columns the packed passes take
@@ -525,7 +529,8 @@ int launch_sw_score(cudaStream_t st, const FastArgs& a, int64_t max_pairs);
 int launch_sw_trace(cudaStream_t st, const FastArgs& a, int64_t max_pairs,
                     cudaEvent_t before = nullptr, cudaEvent_t after = nullptr);
 int launch_sw_bound(cudaStream_t st, const FastArgs& a, int64_t max_pairs);
-// sw_lcs.cu: a.ub[p] = match * LCS(query, window) for the listed pairs
+// sw_lcs.cu: a.ub[p] = match * LCS(query, window) for the listed pairs, and
+// with a.lsuf the suffix LCS values (queries up to 255 bases)
 int launch_sw_lcs(cudaStream_t st, const FastArgs& a, int64_t max_pairs);
 int measure_dpx_peak(cudaStream_t st, int device, double* lane_instr_per_s);
 

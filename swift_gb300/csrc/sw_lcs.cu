@@ -17,12 +17,20 @@
 // One thread per pair; V lives in registers as NW 32-bit words (one carry
 // chain per column), PM in shared memory, [class][word][thread], so the
 // four loads of a column are conflict-free.
+//
+// The window is scanned from its last column to its first, against the
+// query reversed (LCS(q, w) = LCS(reverse q, reverse w)): after the columns
+// c..R the zeros of V are LCS(q, w[c..R]), so the same pass also yields the
+// suffix values the trace pass stops early with.  The reversed query sits
+// in the top Q bits of the 32 * NW; the bits below it match nothing, stay
+// one and never carry.
 #include "internal.h"
 
 namespace swift {
 namespace {
 
 constexpr int kLcsThreads = 256;
+static_assert(kSufSteps == 16, "suffix LCS values are taken per 16-byte block of the window");
 
 // base class of four ACGTacgt bytes at once: A 0, C 1, G 2, T 3 (any map
 // works as long as query and window share it)
@@ -118,13 +126,21 @@ __global__ void __launch_bounds__(kLcsThreads) sw_lcs_kernel(FastArgs a) {
     const int lo = 32 * wd;
     qmask[wd] = Q >= lo + 32 ? ~0u : Q <= lo ? 0u : (1u << (Q - lo)) - 1u;
   }
+  // query position i to bit 32 * NW - 1 - i
+  uint32_t r0[NW], r1[NW], rmask[NW];
+#pragma unroll
+  for (int wd = 0; wd < NW; ++wd) {
+    r0[wd] = __brev(b0[NW - 1 - wd]);
+    r1[wd] = __brev(b1[NW - 1 - wd]);
+    rmask[wd] = __brev(qmask[NW - 1 - wd]);
+  }
   uint32_t* pm = pm_all + threadIdx.x;
 #pragma unroll
   for (int c = 0; c < 4; ++c)
 #pragma unroll
     for (int wd = 0; wd < NW; ++wd)
       pm[(c * NW + wd) * kLcsThreads] =
-          ((c & 1) ? b0[wd] : ~b0[wd]) & ((c & 2) ? b1[wd] : ~b1[wd]) & qmask[wd];
+          ((c & 1) ? r0[wd] : ~r0[wd]) & ((c & 2) ? r1[wd] : ~r1[wd]) & rmask[wd];
   uint32_t v[NW];
 #pragma unroll
   for (int wd = 0; wd < NW; ++wd) v[wd] = ~0u;
@@ -140,32 +156,40 @@ __global__ void __launch_bounds__(kLcsThreads) sw_lcs_kernel(FastArgs a) {
 #pragma unroll
     for (int wd = 0; wd < NW; ++wd) v[wd] = s[wd] | (v[wd] & ~m[wd]);
   };
+  auto zeros = [&]() {
+    int z = 0;
+#pragma unroll
+    for (int wd = 0; wd < NW; ++wd) z += __popc(~v[wd] & rmask[wd]);
+    return z;
+  };
+  // suffix values: entry m after the columns 16 m + 1 .. R (one-based), that
+  // is after the 16-byte block m of the window
+  uint8_t* suf = a.lsuf ? a.lsuf + (int64_t)p * kSufBlocks : nullptr;
   // window: 16 bytes per load (rows are 16-byte aligned, w_stride a
-  // multiple of 16, R <= w_stride)
+  // multiple of 16, R <= w_stride), last block first
   const uint4* w16 = reinterpret_cast<const uint4*>(a.w + (int64_t)p * a.w_stride);
   const int full = R >> 4;
-  for (int k = 0; k < full; ++k) {
-    const uint4 x = __ldg(w16 + k);
-    const uint32_t xs[4] = {x.x, x.y, x.z, x.w};
-#pragma unroll
-    for (int h = 0; h < 4; ++h) {
-      const uint32_t cls = class4(xs[h]);
-#pragma unroll
-      for (int b = 0; b < 4; ++b) column((cls >> (8 * b)) & 3u);
-    }
-  }
   if (R & 15) {
     const uint4 x = __ldg(w16 + full);
     const uint32_t xs[4] = {x.x, x.y, x.z, x.w};
-    for (int j = 16 * full; j < R; ++j) {
+    for (int j = R - 1; j >= 16 * full; --j) {
       const int o = j & 15;
       column((class4(xs[o >> 2]) >> (8 * (o & 3))) & 3u);
     }
+    if (suf) suf[full] = (uint8_t)zeros();
   }
-  int zeros = 0;
+  for (int k = full - 1; k >= 0; --k) {
+    const uint4 x = __ldg(w16 + k);
+    const uint32_t xs[4] = {x.x, x.y, x.z, x.w};
 #pragma unroll
-  for (int wd = 0; wd < NW; ++wd) zeros += __popc(~v[wd] & qmask[wd]);
-  a.ub[p] = a.match * zeros;
+    for (int h = 3; h >= 0; --h) {
+      const uint32_t cls = class4(xs[h]);
+#pragma unroll
+      for (int b = 3; b >= 0; --b) column((cls >> (8 * b)) & 3u);
+    }
+    if (suf) suf[k] = (uint8_t)zeros();
+  }
+  a.ub[p] = a.match * zeros();
 }
 
 }  // namespace
@@ -173,6 +197,8 @@ __global__ void __launch_bounds__(kLcsThreads) sw_lcs_kernel(FastArgs a) {
 int launch_sw_lcs(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {
   if (max_pairs <= 0) return 0;
   if (a.w_stride % 16 != 0 || a.q_stride % 4 != 0 || a.R > a.w_stride) return 0;
+  // suffix values: one byte each, one per 16-column block
+  if (a.lsuf && (a.Q > 255 || a.R > kSufSteps * kSufBlocks)) return 0;
   const unsigned grid = (unsigned)((max_pairs + kLcsThreads - 1) / kLcsThreads);
 #define SWIFT_LCS(NW_)                                                        \
   if (a.Q <= 32 * NW_) {                                                      \

@@ -56,7 +56,9 @@
 namespace swift {
 namespace {
 
-constexpr int kPkWarps = 8;
+// warps per block: small blocks, because a block holds its SM slot until
+// its last warp ends and warps that stop early end at different steps
+constexpr int kPkWarps = 2;
 
 __device__ __forceinline__ uint32_t base_class(uint32_t c) {
   uint32_t u = c & 0xDFu;
@@ -267,6 +269,69 @@ __device__ __forceinline__ void packed_item(const FastArgs& a, const int64_t war
       bestv[k] |= kTagOld;
     }
   };
+  // Early stop of a trace pass with no bound pass (each read's candidate),
+  // from the suffix LCS values of the LCS bound pass.  After step
+  // s = kSufSteps * m + G - 1 every cell not computed yet lies right of
+  // column kSufSteps * m.  Unrolling the recurrence from such a cell back
+  // to its origin gives a chain of cells that starts either with H = 0
+  // among the cells not computed (its matches then lie in columns
+  // > kSufSteps * m) or at a computed cell f = (i, j) one of whose
+  // successors is not computed (its matches then lie in rows > i and
+  // columns > j).  Mismatches and gaps only lower a chain, so the cell's H
+  // is at most
+  //     max(match * L_m, H(f) + match * min(Q - i, L_m)),
+  // L_m = LCS(query, window columns kSufSteps * m + 1 .. R).  Those f are
+  // each row's current cell and, for the last row of a lane, the cell one
+  // column back, which the lane below holds as its diagonal input.  Once
+  // the bound is below the pair's maximum so far, no cell left can be (or
+  // tie) its first maximum and the traceback never reaches one.  Every
+  // value stays at most 16 * match * Q + B (H(f) <= match * i).
+  const bool lcs_on = TRACE && a.lsuf != nullptr && a.suf == nullptr && !var_r;
+  uint32_t lnext0 = 0, lnext1 = 0;  // L_m of the next check, loaded ahead
+  if (lcs_on) {
+    lnext0 = a.lsuf[(int64_t)p0 * kSufBlocks + 1];
+    lnext1 = a.lsuf[(int64_t)p1 * kSufBlocks + 1];
+  }
+  auto lcs_stop = [&](const int m) -> bool {
+    const uint32_t L0 = lnext0, L1 = lnext1;
+    if (m + 1 < kSufBlocks) {
+      lnext0 = a.lsuf[(int64_t)p0 * kSufBlocks + m + 1];
+      lnext1 = a.lsuf[(int64_t)p1 * kSufBlocks + m + 1];
+    }
+    // the pair's maximum so far, 16 * score + B per half
+    uint32_t v = bestv[0];
+#pragma unroll
+    for (int k = 1; k < (TRACE ? RPL : 1); ++k) v = __vimax_s16x2_relu(v, bestv[k]);
+#pragma unroll
+    for (int d = G / 2; d > 0; d >>= 1) v = __vimax_s16x2_relu(v, __shfl_xor_sync(0xffffffffu, v, d, G));
+    v &= 0xFFF0FFF0u;
+    const uint32_t M16 = 16u * (uint32_t)a.match;
+    auto below = [&](uint32_t f) {
+      return (!has0 || (f & 0xFFFFu) < (v & 0xFFFFu)) && (!has1 || (f >> 16) < (v >> 16));
+    };
+    uint32_t F = (B + M16 * L0) | ((B + M16 * L1) << 16);
+    // chains that start among the cells not computed first (cheap, and
+    // false until the window's rest holds too few matches)
+    if (!__all_sync(0xffffffffu, below(F))) return false;
+    // 16 * match * (rows below row k of the lane) per half, signed: row k
+    // has a - k below it (a lane wholly past the query starts at -1), so
+    // min(that, 16 * match * L) clamped at 0 is the chain's largest gain
+    const int a0 = max(Q0 - sl * RPL - 1, -1), a1 = max(Q1 - sl * RPL - 1, -1);
+    const uint32_t L16 = (M16 * L0) | ((M16 * L1) << 16);
+    const uint32_t step_dn = (0x10000u - M16) * 0x00010001u;  // -16 * match, both halves
+    constexpr uint32_t kNoFloor = 0x80008000u;                 // max(x, this) = x
+    uint32_t A = ((M16 * (uint32_t)a0) & 0xFFFFu) | ((M16 * (uint32_t)a1) << 16);
+    // the lane above's last row (row 0 for lane 0, H = 0) has a + 1 below it
+    F = __viaddmax_s16x2(diag, __vimin_s16x2_relu(__viaddmax_s16x2(A, M16 * 0x00010001u, kNoFloor), L16), F);
+#pragma unroll
+    for (int k = 0; k < RPL; ++k) {
+      F = __viaddmax_s16x2(h16p[k], __vimin_s16x2_relu(A, L16), F);
+      A = __viaddmax_s16x2(A, step_dn, kNoFloor);
+    }
+#pragma unroll
+    for (int d = G / 2; d > 0; d >>= 1) F = __vimax_s16x2_relu(F, __shfl_xor_sync(0xffffffffu, F, d, G));
+    return __all_sync(0xffffffffu, below(F));
+  };
   // steps in blocks of 4: the trace pass keeps a block's direction words in
   // registers and writes each word index as one 16-byte store
   uint32_t hist[TRACE ? 4 : 1][kNW];
@@ -333,6 +398,11 @@ __device__ __forceinline__ void packed_item(const FastArgs& a, const int64_t war
         break;
       }
     }
+    if (lcs_on && s >= kSufSteps + G - 1 && ((s - (G - 1)) & (kSufSteps - 1)) == 0 &&
+        lcs_stop((s - (G - 1)) / kSufSteps)) {
+      s_end = s + 1;
+      break;
+    }
   }
   if (a.cells_done) {
     // cells of the warp's pairs inside the columns every lane finished
@@ -394,7 +464,8 @@ __device__ __forceinline__ void packed_item(const FastArgs& a, const int64_t war
 
 // One work item of kPairs pairs per warp.
 template <int G, int RPL, bool TRACE, bool VAR>
-__global__ void __launch_bounds__(kPkWarps * 32, (TRACE || RPL > 13) ? 2 : 3) sw_packed_kernel(FastArgs a) {
+__global__ void __launch_bounds__(kPkWarps * 32, (TRACE || RPL > 13) ? 16 / kPkWarps : 24 / kPkWarps)
+    sw_packed_kernel(FastArgs a) {
   constexpr int kPairs = 2 * (32 / G);
   extern __shared__ uint32_t wsel_all[];  // [warps * groups][R + 1]
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
