@@ -2,8 +2,9 @@
 
 One step = one pass of the whole pipeline over one batch of reads already
 resident on the device: SSAHA seeding of both strands, window construction,
-Smith-Waterman (LCS and relaxed score bounds, traceback of each read's
-candidate, exact scores of the pairs the bounds keep), best alignment per read
+Smith-Waterman (LCS bound with suffix values, traceback of each read's
+candidate, exact scores of the pairs the bound keeps, both passes stopped
+early), best alignment per read
 and the default text records (left on the device).  The one-time index build
 is excluded and reported separately; `e2e` repeats the step through
 swift_align_into with the reads and the text in pinned host memory.
@@ -42,21 +43,24 @@ METRIC_LT13 = ("reads/s (lt13 seed-and-extend seeding + Smith-Waterman + best pe
 
 def metric_for(args):
     return METRIC_LT13 if args.seeder == "lt13" else METRIC
-# The trace pass over whole windows, per pair: algorithmic bytes 112 B query
-# + 304 B window read, 8 B first maximum and the direction words written
-# (8 lanes x 2 words x 312 steps x 4 B per two pairs at 100 bp); DRAM bytes,
-# read + written, from one ncu capture of the candidates' launch (200,000
-# pairs of the scale workload with 200 K reads: 134.6 MB read, 1922.8 MB
+# The candidates' trace pass (up to its early stop), per pair: algorithmic
+# bytes 112 B query + 304 B window read and 8 B first maximum, plus the
+# direction words written for the steps it ran (8 lanes x 2 words x 4 B per
+# step for two pairs at 100 bp: 32 B per step and pair, 100 cells a step, so
+# 0.32 B per cell computed).  DRAM bytes per cell computed, read + written,
+# from one ncu capture of the candidates' launch (210,162 pairs of the scale
+# workload with 200 K reads, 4.44 G cells computed: 161.0 MB read, 1416.5 MB
 # written).
-TRACE_DRAM_BYTES_PER_PAIR = (134.6e6 + 1922.8e6) / 200000
-TRACE_ALGO_BYTES_PER_PAIR = 112 + 304 + 8 + 8 * 2 * 312 * 4 // 2
-# ALU-pipe instructions the trace pass issues per 2 cells (per lane), from
-# an ncu capture of the same launch: 794.6 M warp instructions on the ALU
-# pipe for 6.0 G cells (16.39 warp instructions in all per 2 cells).
-TRACE_ALU_PER_2_CELLS = 8.48
-TRACE_NOTE = ("the trace formulation issues about 8.5 ALU-pipe instructions per 2 cells (the "
-              "substitution permute, two DPX max ops, three masks, the first-maximum add-max) "
-              "and 16.4 instructions in all, so about 0.12 is its ceiling")
+TRACE_DRAM_BYTES_PER_CELL = (161.0e6 + 1416.5e6) / 4.437e9
+TRACE_ALGO_BYTES_PER_PAIR = 112 + 304 + 8
+TRACE_DIR_BYTES_PER_CELL = 8 * 2 * 4 / 2 / 100
+# ALU-pipe instructions the trace pass issues per 2 cells computed (per
+# lane), from the same capture: 612.4 M warp instructions on the ALU pipe
+# (1193.2 M in all) for 4.44 G cells, the early-stop tests included.
+TRACE_ALU_PER_2_CELLS = 8.83
+TRACE_NOTE = ("the trace formulation issues about 8.8 ALU-pipe instructions per 2 cells (the "
+              "substitution permute, two DPX max ops, three masks, the first-maximum add-max, "
+              "the early-stop tests) and 17.2 instructions in all, so about 0.11 is its ceiling")
 SCORE_NOTE = ("the exact formulation issues about 6.5 ALU instructions per 2 cells, so about "
               "0.15 is its ceiling")
 
@@ -192,13 +196,15 @@ def sample_reads(reads: bytes, n: int) -> bytes:
 
 
 def cpu_reference(ref: bytes, reads: bytes, n_sample: int, steps: int, warmup: int,
-                  seeder: int = 0, device_mem: int = 0, max_read_len: int = 0):
+                  seeder: int = 0, device_mem: int = 0, max_read_len: int = 0,
+                  out_format: int = 0):
     """The reference algorithm on the host cores (oracle port): reads/s,
     threads, seconds, and the last run's output (for the parity check)."""
     from oracle import oracle as O
     threads = os.cpu_count() or 1
     sess = O.Session(ref, O.default_params(threads=threads, seeder=seeder,
-                                           device_mem=device_mem, max_read_len=max_read_len))
+                                           device_mem=device_mem, max_read_len=max_read_len,
+                                           out_format=out_format))
     sample = sample_reads(reads, n_sample)
     for _ in range(warmup):
         sess.align(sample)
@@ -607,13 +613,14 @@ def main():
         n_sample = min(args.cpu_sample, n)
         rps, threads, dt, _ = cpu_reference(ref, reads, n_sample, steps, min(warm, 1),
                                             1 if args.seeder == "lt13" else 0,
-                                            max_read_len=300 if args.read_len > 199 else 0)
+                                            max_read_len=300 if args.read_len > 199 else 0,
+                                            out_format=1 if args.format == "sam" else 0)
         line = {
             "impl": "reference", "metric": metric_for(args), "value": rps, "unit": "reads/s",
             "n_gpus": args.gpus, "steps": steps, "warmup": warm,
             "ms_per_step": dt * 1e3 / steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-            "config": {"workload": desc, "seeder": args.seeder,
+            "config": {"workload": desc, "seeder": args.seeder, "format": args.format,
                        "sample_reads_per_step": n_sample},
             "cpu_baseline": {"value": rps, "unit": "reads/s", "cores": threads, "kind": "port",
                              "cpu_model": cpu_model(),
@@ -733,7 +740,8 @@ def main():
     try:
         rps, threads, dt, cpu_out = cpu_reference(ref, reads, k_cpu, 1, 0, seeder,
                                                   device_mem=ctx.info()["total_mem"],
-                                                  max_read_len=max_read)
+                                                  max_read_len=max_read,
+                                                  out_format=params.out_format)
         cpu = {"value": rps, "unit": "reads/s", "cores": threads, "kind": "port",
                "cpu_model": model,
                "sample": f"{k_cpu} reads of the workload, index prebuilt"}
@@ -764,24 +772,26 @@ def main():
     except Exception as ex:
         cpu_sw = {"gcups": None, "note": f"failed: {ex}"}
     # the dominant kernel alone, CUDA events on the library's stream: the
-    # trace pass over whole windows (the candidates, or every pair for SAM)
+    # trace pass of the candidates (up to their early stop), or of every pair
+    # over whole windows for SAM
     last = stats[-1]
     tr_ms = statistics.median(s["trace_ms"] for s in stats)
     fp_ms = statistics.median(s["first_pass_ms"] for s in stats)
     peak = peak_cells / 1e9
     fast_pairs = last["records"] - last["sw_generic_pairs"]
-    cells_per_pair = last["cells"] // max(last["records"], 1)  # Q x window
-    traced = last["trace_cells"] // cells_per_pair if cells_per_pair else 0
+    traced = last["traced_pairs"] - last["retraced_pairs"]
     if tr_ms > 0:
         rf_kernel = ("sw_packed_kernel trace pass (%s)"
-                     % ("every packed pair, SAM output" if args.format == "sam"
-                        else "each read's candidate pair, whole windows"))
+                     % ("every packed pair, SAM output, whole windows" if args.format == "sam"
+                        else "each read's candidate pair, up to the early stop; cells counted "
+                             "over the columns every lane of a warp finished"))
         rf_ms, rf_cells = tr_ms, last["trace_cells"]
-        rf_dram, rf_algo, rf_note = TRACE_DRAM_BYTES_PER_PAIR, TRACE_ALGO_BYTES_PER_PAIR, TRACE_NOTE
-        rf_units = traced
+        rf_traffic = TRACE_DRAM_BYTES_PER_CELL * rf_cells
+        rf_algo = TRACE_ALGO_BYTES_PER_PAIR * traced + TRACE_DIR_BYTES_PER_CELL * rf_cells
+        rf_note = TRACE_NOTE
     else:
         rf_kernel, rf_ms, rf_cells = "sw_packed_kernel score pass", fp_ms, last["first_pass_cells"]
-        rf_dram, rf_algo, rf_note, rf_units = None, 112 + 304 + 4, SCORE_NOTE, fast_pairs
+        rf_traffic, rf_algo, rf_note = None, (112 + 304 + 4) * fast_pairs, SCORE_NOTE
     achieved = rf_cells / (rf_ms * 1e-3) / 1e9 if rf_ms > 0 else None
     # seeding against HBM: the survey's sector-model bytes (counted on the
     # device per strand) over the warp kernels' CUDA-event time
@@ -846,8 +856,8 @@ def main():
                           "(Smith-Waterman passes + selection + traceback phase, %.2f ms); the "
                           "bounds rule most cells out without computing them" % p2_ms),
         "sw_gcups_computed": gcups_computed,
-        "sw_gcups_computed_kind": ("DP cells the kernels computed (trace, relaxed bound, exact "
-                                   "score up to its early stop, generic) / the same time"),
+        "sw_gcups_computed_kind": ("DP cells the kernels computed (trace and exact score "
+                                   "passes up to their early stop, generic) / the same time"),
         "parity": parity,
         "cpu_sw": cpu_sw,
         "seed_roofline": seed_rf,
@@ -859,9 +869,10 @@ def main():
                      "achieved": achieved, "peak": peak,
                      "unit": "Gcells/s", "frac": achieved / peak if peak and achieved else None,
                      "kernel_ms": rf_ms,
-                     "traffic": rf_dram * rf_units if rf_dram else None,
-                     "traffic_unit": "bytes per pass (launches of up to 262,144 pairs)",
-                     "algorithmic_bytes": rf_algo * rf_units,
+                     "traffic": rf_traffic,
+                     "traffic_unit": "bytes per pass (launches of up to 262,144 pairs), "
+                                     "ncu DRAM bytes per cell computed x cells computed",
+                     "algorithmic_bytes": rf_algo,
                      "peak_source": "measured on this GPU: 2 cells per __vimax3_s16x2_relu "
                                     "lane instruction (%s)" % rf_note,
                      # the same issue-rate peak per ALU-pipe instruction: how busy the
@@ -872,7 +883,7 @@ def main():
             "kernel": "sw_lcs_kernel (bit-parallel LCS bound of every packed pair)",
             "kernel_ms": fp_ms, "pairs": fast_pairs,
             "Gcells_per_s": last["first_pass_cells"] / (fp_ms * 1e-3) / 1e9 if fp_ms > 0 else None,
-            "pairs_left_for_the_relaxed_bound": last["lcs_kept"]},
+            "pairs_left_for_the_exact_pass": last["lcs_kept"]},
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": int(sum(s["launches"] for s in stats)),

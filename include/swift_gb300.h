@@ -99,11 +99,13 @@ typedef struct {
                             SAM output (every pair traced)                   */
   int64_t first_pass_cells; /* DP cells that kernel covered               */
   int64_t first_pass_kind;  /* 1 exact score, 3 LCS bound                 */
-  double trace_ms;       /* trace-pass launches over whole windows: the
-                            candidates (default) or every packed pair (SAM) */
-  int64_t trace_cells;   /* DP cells of those launches                     */
+  double trace_ms;       /* trace-pass launches: the candidates (default;
+                            they stop early on suffix LCS values) or every
+                            packed pair over whole windows (SAM)            */
+  int64_t trace_cells;   /* DP cells those launches computed (the columns
+                            every lane of a warp finished)                  */
   int64_t lcs_kept;      /* pairs the LCS bound could not rule out (they get
-                            the relaxed bound pass)                          */
+                            the exact score pass)                            */
   double seed_kernel_ms; /* SSAHA seeding's warp kernels alone (CUDA events) */
   int64_t seed_model_bytes; /* their bytes under the seeding roofline's sector
                             model: per read strand ceil(L/4) + 32 per k-mer
@@ -111,8 +113,8 @@ typedef struct {
                             of n postings + 12 per hit written             */
   int64_t sw_cells_computed; /* DP cells the Smith-Waterman kernels computed:
                             trace and exact score passes (up to their early
-                            stop), relaxed bound pass, generic kernel; the
-                            LCS bound's bit-parallel columns not counted    */
+                            stop), generic kernel; the LCS bound's
+                            bit-parallel columns not counted                */
 } swift_stats;
 
 void swift_params_default(swift_params *p);

@@ -243,28 +243,24 @@ __global__ void traceback_list_kernel(const DevPair* __restrict__ pairs,
   block_count(k, printed);
 }
 
-// Early-stop order of a pair list.  The exact passes stop a warp once the
-// bound pass's suffix maxima rule out every remaining column for all of its
-// pairs, so pairs expected to stop at the same block should share warps.
-// Key: the first block m >= 1 whose suffix maximum is below the pair's
-// score bound (m_max + 1 if none).  A counting sort by key.
-__device__ __forceinline__ int stop_key(const int32_t* ub, const uint16_t* suf, int32_t p,
-                                        int m_max) {
-  const int u = ub[p];
-  for (int m = 1; m <= m_max; ++m)
-    if ((int)suf[(int64_t)p * kSufBlocks + m] < u) return m;
-  return m_max + 1;
-}
-
-__global__ void stop_key_count_kernel(const int32_t* __restrict__ list, const int32_t* __restrict__ n,
-                                      const int32_t* __restrict__ ub, const uint16_t* __restrict__ suf,
-                                      int m_max, int32_t* __restrict__ keys, int32_t* hist) {
+// Order of the exact score pass: the further a pair's LCS bound lies above
+// T, the least score that could make it its group's pick (its candidate's
+// score, + 1 after the candidate in group order), the later the pair can
+// stop (pairs of reads with no true window, whose candidates score low, run
+// to the window's end).  Key: that margin in matches, largest first, so
+// pairs stopping alike share warps.  A counting sort by key.
+__global__ void exact_key_count_kernel(const int32_t* __restrict__ list, const int32_t* __restrict__ n,
+                                       const int32_t* __restrict__ ub, const int32_t* __restrict__ cand,
+                                       const DevAln* __restrict__ aln, int match,
+                                       int32_t* __restrict__ keys, int32_t* hist) {
   __shared__ int32_t h[kSufBlocks + 1];
   if (threadIdx.x <= kSufBlocks) h[threadIdx.x] = 0;
   __syncthreads();
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < *n) {
-    const int k = stop_key(ub, suf, list[i], m_max);
+    const int32_t p = list[i], c = cand[p];
+    const int margin = (ub[p] - (aln[c].score + (p > c ? 1 : 0))) / match;
+    const int k = kSufBlocks - min(kSufBlocks, max(margin, 0));
     keys[i] = k;
     atomicAdd(&h[k], 1);
   }
@@ -272,13 +268,13 @@ __global__ void stop_key_count_kernel(const int32_t* __restrict__ list, const in
   if (threadIdx.x <= kSufBlocks && h[threadIdx.x]) atomicAdd(&hist[threadIdx.x], h[threadIdx.x]);
 }
 
-// Trace order of the candidates (no bound pass has run for them; they stop
-// early on the suffix LCS values).  Key: the LCS bound's shortfall from a
-// whole-query match, largest first: reads with no true window (their trace
+// Trace order of the candidates (and of every pair with SAM output): they
+// stop early on the suffix LCS values.  Key: the LCS bound's shortfall from
+// a whole-query match, largest first: reads with no true window (their trace
 // runs to the window's end) come first and share warps, and the pairs that
-// stop once their alignment ends share the rest.
+// stop once their alignment ends share the rest.  A counting sort by key.
 __global__ void cand_key_count_kernel(const int32_t* __restrict__ list, const int32_t* __restrict__ n,
-                                      const uint8_t* __restrict__ lsuf,
+                                      const uint16_t* __restrict__ lsuf,
                                       const int32_t* __restrict__ q_len, int Q,
                                       int32_t* __restrict__ keys, int32_t* hist) {
   __shared__ int32_t h[kSufBlocks + 1];
@@ -2190,14 +2186,13 @@ static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swi
   const bool sam = p->out_format == 1;
   const bool bounded = fast_ok && ctx->sw_path == 0 && !sam;
   // counters: 0 packed-path pairs, 1 generic pairs, 2 trace list,
-  // 3 pairs the LCS bound keeps, 4 second trace list, 5 printed records,
-  // 6 pairs the relaxed bound keeps (exact-score list)
+  // 3 pairs the LCS bound keeps (exact-score list), 4 second trace list,
+  // 5 printed records
   // counters 8.. : histogram and fill of the early-stop sort (two uses)
-  int32_t *fast_list, *gen_list, *tb_list, *k2_list, *cnt;
+  int32_t *fast_list, *gen_list, *tb_list, *cnt;
   CK(sc.get(&fast_list, nn));
   CK(sc.get(&gen_list, nn));
   CK(sc.get(&tb_list, nn));
-  CK(sc.get(&k2_list, bounded ? nn : 1));
   CK(sc.get(&cnt, 8 + 4 * (kSufBlocks + 1)));
   CK(cudaMemsetAsync(cnt, 0, (8 + 4 * (kSufBlocks + 1)) * sizeof(int32_t), st));
   int launches = 0;
@@ -2244,16 +2239,16 @@ static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swi
   fa2.cons_stride = cs;
   fa2.q_len = pair_q;
   int32_t *ub = nullptr, *cand = nullptr;
-  uint16_t* suf = nullptr;
-  uint8_t* lsuf = nullptr;  // suffix LCS values: the candidates' early stop
-  if (bounded) {
+  // suffix LCS values: early stop of the score and trace passes (bounded
+  // selection; every pair traced with SAM output)
+  uint16_t* lsuf = nullptr;
+  const bool lcs_stop = fast_ok && ctx->sw_path == 0;
+  if (bounded) CK(sc.get(&cand, nn));
+  if (lcs_stop) {
     CK(sc.get(&ub, nn));
-    CK(sc.get(&cand, nn));
-    CK(sc.get(&suf, nn * kSufBlocks));
-    if (Q <= 255) CK(sc.get(&lsuf, nn * kSufBlocks));
+    CK(sc.get(&lsuf, nn * kSufBlocks));
   }
   fa2.ub = ub;
-  fa2.suf = suf;
   fa2.lsuf = lsuf;
   // cells computed: [0] score passes and later traces, [1] the candidates'
   // trace pass
@@ -2265,8 +2260,9 @@ static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swi
   if (fast_ok && nproc > 0 && !sam) {
     fa2.list = fast_list;
     fa2.count = cnt;
-    // bounded: the LCS bound of every packed pair (the relaxed bound pass
-    // runs later on the pairs it cannot rule out); else exact scores
+    // bounded: the LCS bound of every packed pair, with its suffix values
+    // (the exact pass runs later on the pairs it cannot rule out); else
+    // exact scores
     const int k = bounded ? launch_sw_lcs(st, fa2, nproc) : launch_sw_score(st, fa2, nproc);
     if (k == 0) return fail(ctx, SWIFT_E_DEVICE, "first Smith-Waterman pass could not launch");
     launches += k;
@@ -2343,13 +2339,12 @@ static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swi
   int64_t pruned = 0;
   // list[0, *count) -> out in early-stop order (grid sized by max_n)
   int32_t *keys = nullptr, *sorted = nullptr;
-  if (bounded) {
+  if (lcs_stop) {
     CK(sc.get(&keys, nn));
     CK(sc.get(&sorted, nn));
   }
-  const int m_max = (kWin - 1) / kSufSteps;
   int sort_uses = 0;
-  // (cand_order: the candidates' key from the suffix LCS values instead)
+  // cand_order: the traces' key (else the exact score pass's)
   auto sort_by_stop = [&](const int32_t* list, const int32_t* count, int64_t max_n,
                           int32_t* out, bool cand_order) -> int {
     if (max_n <= 0) return SWIFT_OK;
@@ -2360,7 +2355,7 @@ static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swi
     if (cand_order)
       cand_key_count_kernel<<<grid, 256, 0, st>>>(list, count, lsuf, pair_q, Q, keys, hist);
     else
-      stop_key_count_kernel<<<grid, 256, 0, st>>>(list, count, ub, suf, m_max, keys, hist);
+      exact_key_count_kernel<<<grid, 256, 0, st>>>(list, count, ub, cand, aln, p->match, keys, hist);
     stop_key_scatter_kernel<<<grid, 256, 0, st>>>(list, count, keys, hist, fill, out);
     CKLAUNCH();
     launches += 2;
@@ -2373,14 +2368,33 @@ static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swi
     if (fast_ok && nproc > 0) {
       CK(cudaMemcpyAsync(h_cnt, cnt, sizeof(h_cnt), cudaMemcpyDeviceToHost, st));
       CK(cudaStreamSynchronize(st));
-      rc = trace_list(fast_list, cnt, h_cnt[0], true);
+      int32_t* sam_list = fast_list;
+      if (lsuf) {
+        // suffix LCS values for the early stop, then the order that groups
+        // pairs stopping alike
+        fa2.list = fast_list;
+        fa2.count = cnt;
+        fa2.list_offset = 0;
+        const int k = launch_sw_lcs(st, fa2, h_cnt[0]);
+        if (k == 0) return fail(ctx, SWIFT_E_DEVICE, "LCS pass could not launch");
+        launches += k;
+        CKLAUNCH();
+        rc = sort_by_stop(fast_list, cnt, h_cnt[0], sorted, true);
+        if (rc != SWIFT_OK) return rc;
+        sam_list = sorted;
+      }
+      fa2.cells_done = d_cells + 1;
+      rc = trace_list(sam_list, cnt, h_cnt[0], true);
       if (rc != SWIFT_OK) return rc;
+      fa2.cells_done = d_cells;
+      fa2.lsuf = nullptr;
     }
   }
   int64_t lcs_kept = 0, cand_n = 0;
   if (bounded && nproc > 0) {
-    // candidates (largest LCS bound of their group) traced first, with no
-    // early stop: no relaxed bound has run for them
+    // candidates (largest LCS bound of their group) traced first; they stop
+    // early on the LCS pass's suffix values, in an order that groups pairs
+    // stopping alike
     launch_candidates(st, fa, tb_list, cnt + 2);
     CKLAUNCH();
     ++launches;
@@ -2388,7 +2402,6 @@ static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swi
     CK(cudaStreamSynchronize(st));
     CK(cudaEventRecord(ctx->ev[6], st));
     cand_n = h_cnt[2];
-    fa2.suf = nullptr;
     fa2.cells_done = d_cells + 1;
     int32_t* cand_list = tb_list;
     if (lsuf) {
@@ -2398,11 +2411,10 @@ static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swi
     }
     rc = trace_list(cand_list, cnt + 2, cand_n, true);
     if (rc != SWIFT_OK) return rc;
-    fa2.suf = suf;
-    fa2.lsuf = nullptr;
     fa2.cells_done = d_cells;
     // pairs whose LCS bound cannot rule them out against their candidate's
-    // score get the relaxed bound, then the same test again
+    // score get the exact score pass, which drops each pair once its score
+    // is settled or provably too low to be its group's pick
     int32_t* k1_list = fast_list;  // free once the LCS pass has run
     launch_prune(st, fa, aln, k1_list, cnt + 3);
     CKLAUNCH();
@@ -2411,28 +2423,20 @@ static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swi
     CK(cudaStreamSynchronize(st));
     lcs_kept = h_cnt[3];
     if (lcs_kept > 0) {
-      fa2.list = k1_list;
+      int32_t* ex_list = k1_list;
+      if (lsuf) {
+        rc = sort_by_stop(k1_list, cnt + 3, lcs_kept, sorted, false);
+        if (rc != SWIFT_OK) return rc;
+        ex_list = sorted;
+      }
+      fa2.list = ex_list;
       fa2.count = cnt + 3;
       fa2.list_offset = 0;
-      const int kb = launch_sw_bound(st, fa2, lcs_kept);
-      if (kb == 0) return fail(ctx, SWIFT_E_DEVICE, "bound pass could not launch");
-      launches += kb;
+      fa2.cand = cand;
+      launches += launch_sw_score(st, fa2, lcs_kept);
       CKLAUNCH();
-      launch_prune_list(st, fa, aln, k1_list, cnt + 3, lcs_kept, k2_list, cnt + 6);
-      CKLAUNCH();
-      ++launches;
+      fa2.cand = nullptr;
     }
-    // the kept count sizes the exact pass's grid
-    CK(cudaMemcpyAsync(h_cnt, cnt, sizeof(h_cnt), cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    const int64_t ex_max = h_cnt[6];
-    rc = sort_by_stop(k2_list, cnt + 6, ex_max, sorted, false);
-    if (rc != SWIFT_OK) return rc;
-    fa2.list = sorted;
-    fa2.count = cnt + 6;
-    fa2.list_offset = 0;
-    launches += launch_sw_score(st, fa2, ex_max);
-    CKLAUNCH();
   }
   if (!sam) {
     launch_select(st, fa);
@@ -2451,7 +2455,7 @@ static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swi
     CK(cudaStreamSynchronize(st));
     rc = trace_list(list2, cnt + 4, h_cnt[4], false);
     if (rc != SWIFT_OK) return rc;
-    if (bounded) pruned = std::max<int64_t>(h_cnt[0] - h_cnt[2] - h_cnt[6], 0);
+    if (bounded) pruned = std::max<int64_t>(h_cnt[0] - h_cnt[2] - lcs_kept, 0);
   }
   CK(cudaEventRecord(ctx->ev[4], st));
   if (sam)
@@ -2517,15 +2521,15 @@ static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swi
     s.pairs_ms = t;
     cudaEventElapsedTime(&t, ctx->ev[2], ctx->ev[3]);
     s.sw_ms = t;
-    // the trace pass of all packed pairs (SAM, whole windows) or of the
-    // candidates (bounded selection, up to their early stop)
+    // the trace pass of all packed pairs (SAM) or of the candidates
+    // (bounded selection), up to their early stop
     double trace_sum = 0;
     for (int c = 0; c < timed_chunks; ++c) {
       cudaEventElapsedTime(&t, ctx->chunk_ev[2 * c], ctx->chunk_ev[2 * c + 1]);
       trace_sum += t;
     }
     s.trace_ms = trace_sum;
-    s.trace_cells = sam ? (int64_t)h_cnt[0] * Q * kWin : (int64_t)h_cells2[1];
+    s.trace_cells = (int64_t)h_cells2[1];
     if (!sam) {
       cudaEventElapsedTime(&t, ctx->ev[7], ctx->ev[8]);
       s.first_pass_ms = t;
@@ -2535,9 +2539,9 @@ static int align_resident_impl(swift_ctx* ctx, const swift_index* idx, const swi
     s.lcs_kept = lcs_kept;
     s.seed_kernel_ms = so.kernel_ms;
     for (int i = 0; i < kSeedModelSlots; ++i) s.seed_model_bytes += (int64_t)h_model[i];
-    // the relaxed bound pass and the generic kernel compute every cell of
-    // their pairs; the packed score and trace passes counted theirs
-    s.sw_cells_computed = (int64_t)h_cells + (lcs_kept + (int64_t)h_cnt[1]) * Q * kWin;
+    // the generic kernel computes every cell of its pairs; the packed score
+    // and trace passes counted theirs
+    s.sw_cells_computed = (int64_t)h_cells + (int64_t)h_cnt[1] * Q * kWin;
     cudaEventElapsedTime(&t, ctx->ev[3], ctx->ev[6]);
     s.select_ms = t;
     cudaEventElapsedTime(&t, ctx->ev[6], ctx->ev[4]);

@@ -463,7 +463,8 @@ bool long_prof_ok(int m, int x, int gap_open, int max_q);
 int launch_sw_long(cudaStream_t st, const LongArgs& a, int rpl, bool prof);
 
 // sw_fast.cu: packed 16-bit passes (score of every pair; trace of printed pairs)
-// Bound-pass suffix maxima: blocks of wavefront steps, blocks per pair.
+// Suffix LCS values: window columns per block (the wavefront steps between
+// two early-stop tests), blocks per pair.
 constexpr int kSufSteps = 16;
 constexpr int kSufBlocks = 32;
 struct FastArgs {
@@ -479,10 +480,7 @@ struct FastArgs {
   DevAln* aln;                // score pass: .score; trace pass: all fields
   const int32_t* q_len;       // trace pass: per-pair query and window lengths
   const int32_t* r_len;       // (pairs of one launch may differ), or null
-  int32_t* ub;                // bound pass: upper bound of the score per pair
-  uint16_t* suf;              // bound pass: per pair, kSufBlocks suffix maxima of
-                              // kSufSteps-step blocks (read by the exact passes
-                              // to stop early); may be null
+  int32_t* ub;                // LCS bound pass: upper bound of the score per pair
   int2* best;                 // trace pass: (score, first maximum cell) per pair
   uint32_t* dirs;             // trace pass: direction scratch
   int64_t chunk;              // trace pass: pairs of this launch
@@ -495,10 +493,15 @@ struct FastArgs {
                               // exact passes and walk; 0: the default for Q
   uint32_t one, four;         // trace pass: 1 and 4, as values the compiler cannot
                               // fold (set by launch_sw_trace)
-  uint8_t* lsuf;              // LCS bound pass writes, per pair, kSufBlocks suffix
+  uint16_t* lsuf;             // LCS bound pass writes, per pair, kSufBlocks suffix
                               // LCS values: entry m = LCS(query, window columns
-                              // kSufSteps * m + 1 .. R); the trace pass (with no
-                              // suf) reads them to stop early; may be null
+                              // kSufSteps * m + 1 .. R); the score and trace
+                              // passes read them to stop early; may be null
+  const int32_t* cand;        // score pass with lsuf, optional: per pair its
+                              // best-per-read group's candidate, whose score
+                              // (aln) is known; a pair stops once it provably
+                              // cannot reach that score (or tie it from before
+                              // the candidate) and then reports a score below
 };
 bool fast_params_ok(int Q, int R, int m, int x, int o, int e, int* bias);
 constexpr int kFastMaxR = 512;  // window columns the packed passes take
@@ -528,9 +531,8 @@ int launch_sw_score(cudaStream_t st, const FastArgs& a, int64_t max_pairs);
 // before / after (optional) are recorded around the trace pass alone
 int launch_sw_trace(cudaStream_t st, const FastArgs& a, int64_t max_pairs,
                     cudaEvent_t before = nullptr, cudaEvent_t after = nullptr);
-int launch_sw_bound(cudaStream_t st, const FastArgs& a, int64_t max_pairs);
 // sw_lcs.cu: a.ub[p] = match * LCS(query, window) for the listed pairs, and
-// with a.lsuf the suffix LCS values (queries up to 255 bases)
+// with a.lsuf the suffix LCS values
 int launch_sw_lcs(cudaStream_t st, const FastArgs& a, int64_t max_pairs);
 int measure_dpx_peak(cudaStream_t st, int device, double* lane_instr_per_s);
 
@@ -562,8 +564,6 @@ struct FormatArgs {
 void launch_select(cudaStream_t st, const FormatArgs& a);
 void launch_candidates(cudaStream_t st, const FormatArgs& a, int32_t* list, int32_t* cnt);
 void launch_prune(cudaStream_t st, const FormatArgs& a, DevAln* aln, int32_t* list, int32_t* cnt);
-void launch_prune_list(cudaStream_t st, const FormatArgs& a, DevAln* aln, const int32_t* in,
-                       const int32_t* in_cnt, int64_t max_n, int32_t* list, int32_t* cnt);
 void launch_format_sizes(cudaStream_t st, const FormatArgs& a);
 void launch_format_write(cudaStream_t st, const FormatArgs& a);
 // SAM output: every record, sizes then text (keep is not read)

@@ -133,26 +133,6 @@ __global__ void prune_kernel(FormatArgs a, DevAln* aln, int32_t* list, int32_t* 
   block_append(app, (int32_t)i, list, cnt);
 }
 
-// The same rule over a list of pairs (none of them a candidate) after a
-// tighter bound has replaced a.ub for them.
-__global__ void prune_list_kernel(FormatArgs a, DevAln* aln, const int32_t* in, const int32_t* in_cnt,
-                                  int32_t* list, int32_t* cnt) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  bool app = false;
-  int32_t i = 0;
-  if (t < *in_cnt) {
-    i = in[t];
-    const int32_t c = a.cand[i];
-    const int S = aln[c].score, u = a.ub[i];
-    if (u > S || (u == S && i < c)) {
-      app = true;
-    } else {
-      aln[i].score = -1;
-    }
-  }
-  block_append(app, i, list, cnt);
-}
-
 __device__ __forceinline__ int ndigits(int v) {
   unsigned u = v < 0 ? (unsigned)(-(int64_t)v) : (unsigned)v;
   int n = 1;
@@ -448,12 +428,6 @@ void launch_candidates(cudaStream_t st, const FormatArgs& a, int32_t* list, int3
 void launch_prune(cudaStream_t st, const FormatArgs& a, DevAln* aln, int32_t* list, int32_t* cnt) {
   if (a.n <= 0) return;
   prune_kernel<<<(unsigned)((a.n + 255) / 256), 256, 0, st>>>(a, aln, list, cnt);
-}
-
-void launch_prune_list(cudaStream_t st, const FormatArgs& a, DevAln* aln, const int32_t* in,
-                       const int32_t* in_cnt, int64_t max_n, int32_t* list, int32_t* cnt) {
-  if (max_n <= 0) return;
-  prune_list_kernel<<<(unsigned)((max_n + 255) / 256), 256, 0, st>>>(a, aln, in, in_cnt, list, cnt);
 }
 
 void launch_format_sizes(cudaStream_t st, const FormatArgs& a) {

@@ -5,9 +5,10 @@
 // M <= LCS(q, w); every other column of it (mismatch, gap) scores below
 // zero on the packed path (mismatch, gap_open, gap_ext < 0), so its score is
 // at most match * M <= match * LCS(q, w).  That bound is far cheaper than
-// the relaxed recurrence of the bound pass and already rules out most pairs
-// that cannot be their read's best; the bound pass then runs only on the
-// pairs it leaves.
+// any recurrence over the cells and already rules out most pairs that
+// cannot be their read's best; the exact score pass then runs only on the
+// pairs it leaves, and the suffix values let it and the trace pass stop
+// early.
 //
 // LCS by the bit-vector recurrence of Allison and Dix as simplified by
 // Hyyro (one pass over the window, the query as a bit vector V of Q bits,
@@ -164,7 +165,7 @@ __global__ void __launch_bounds__(kLcsThreads) sw_lcs_kernel(FastArgs a) {
   };
   // suffix values: entry m after the columns 16 m + 1 .. R (one-based), that
   // is after the 16-byte block m of the window
-  uint8_t* suf = a.lsuf ? a.lsuf + (int64_t)p * kSufBlocks : nullptr;
+  uint16_t* suf = a.lsuf ? a.lsuf + (int64_t)p * kSufBlocks : nullptr;
   // window: 16 bytes per load (rows are 16-byte aligned, w_stride a
   // multiple of 16, R <= w_stride), last block first
   const uint4* w16 = reinterpret_cast<const uint4*>(a.w + (int64_t)p * a.w_stride);
@@ -176,7 +177,7 @@ __global__ void __launch_bounds__(kLcsThreads) sw_lcs_kernel(FastArgs a) {
       const int o = j & 15;
       column((class4(xs[o >> 2]) >> (8 * (o & 3))) & 3u);
     }
-    if (suf) suf[full] = (uint8_t)zeros();
+    if (suf) suf[full] = (uint16_t)zeros();
   }
   for (int k = full - 1; k >= 0; --k) {
     const uint4 x = __ldg(w16 + k);
@@ -187,7 +188,7 @@ __global__ void __launch_bounds__(kLcsThreads) sw_lcs_kernel(FastArgs a) {
 #pragma unroll
       for (int b = 3; b >= 0; --b) column((cls >> (8 * b)) & 3u);
     }
-    if (suf) suf[k] = (uint8_t)zeros();
+    if (suf) suf[k] = (uint16_t)zeros();
   }
   a.ub[p] = a.match * zeros();
 }
@@ -197,8 +198,8 @@ __global__ void __launch_bounds__(kLcsThreads) sw_lcs_kernel(FastArgs a) {
 int launch_sw_lcs(cudaStream_t st, const FastArgs& a, int64_t max_pairs) {
   if (max_pairs <= 0) return 0;
   if (a.w_stride % 16 != 0 || a.q_stride % 4 != 0 || a.R > a.w_stride) return 0;
-  // suffix values: one byte each, one per 16-column block
-  if (a.lsuf && (a.Q > 255 || a.R > kSufSteps * kSufBlocks)) return 0;
+  // suffix values: one per 16-column block
+  if (a.lsuf && a.R > kSufSteps * kSufBlocks) return 0;
   const unsigned grid = (unsigned)((max_pairs + kLcsThreads - 1) / kLcsThreads);
 #define SWIFT_LCS(NW_)                                                        \
   if (a.Q <= 32 * NW_) {                                                      \

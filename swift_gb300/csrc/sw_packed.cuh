@@ -1,13 +1,12 @@
 // Phase 2 in packed 16-bit lanes with the DPX add-max instructions.
 //
 // Same recurrence and tie rules as sw.cu (the reference kernel's,
-// src/smithWaterman.cu:510-645 and 911-1026).  Three kernels share the
+// src/smithWaterman.cu:510-645 and 911-1026).  Two passes share the
 // layout:
-//   bound pass   (sw_bound_kernel): an upper bound of every pair's score
-//                from a relaxed recurrence, so most pairs that cannot be
-//                their read's best need no exact pass;
 //   score pass   (TRACE = false): the exact maximum score of a pair, for
-//                best-per-read selection;
+//                best-per-read selection (with the LCS pass's suffix values,
+//                stopped once the score is settled or provably too low to
+//                be picked);
 //   trace pass   (TRACE = true):  for the printed pairs, the first
 //                row-major maximum and 4-bit directions streamed to global
 //                scratch; sw_walk_kernel then walks the reference's
@@ -269,7 +268,7 @@ __device__ __forceinline__ void packed_item(const FastArgs& a, const int64_t war
       bestv[k] |= kTagOld;
     }
   };
-  // Early stop of a trace pass with no bound pass (each read's candidate),
+  // Early stop (the trace of each read's candidate, the exact score pass),
   // from the suffix LCS values of the LCS bound pass.  After step
   // s = kSufSteps * m + G - 1 every cell not computed yet lies right of
   // column kSufSteps * m.  Unrolling the recurrence from such a cell back
@@ -284,13 +283,25 @@ __device__ __forceinline__ void packed_item(const FastArgs& a, const int64_t war
   // each row's current cell and, for the last row of a lane, the cell one
   // column back, which the lane below holds as its diagonal input.  Once
   // the bound is below the pair's maximum so far, no cell left can be (or
-  // tie) its first maximum and the traceback never reaches one.  Every
+  // tie) its first maximum and the traceback never reaches one.  The score
+  // pass needs only the maximum, so a bound equal to it is enough, and with
+  // a.cand a pair also stops once the bound and its maximum so far are both
+  // below T, the least score that could still make it its group's pick
+  // (its candidate's score, + 1 after the candidate in group order): its
+  // maximum so far, reported, stays below T as its true score does.  Every
   // value stays at most 16 * match * Q + B (H(f) <= match * i).
-  const bool lcs_on = TRACE && a.lsuf != nullptr && a.suf == nullptr && !var_r;
+  const bool lcs_on = a.lsuf != nullptr && !var_r;
   uint32_t lnext0 = 0, lnext1 = 0;  // L_m of the next check, loaded ahead
+  uint32_t thr = 0;                 // score pass: 16 * T + B per half, 0: none
   if (lcs_on) {
     lnext0 = a.lsuf[(int64_t)p0 * kSufBlocks + 1];
     lnext1 = a.lsuf[(int64_t)p1 * kSufBlocks + 1];
+    if (!TRACE && a.cand) {
+      const int32_t c0 = a.cand[p0], c1 = a.cand[p1];
+      const uint32_t t0 = (uint32_t)(a.aln[c0].score + (p0 > c0 ? 1 : 0));
+      const uint32_t t1 = (uint32_t)(a.aln[c1].score + (p1 > c1 ? 1 : 0));
+      thr = (B + 16u * t0) | ((B + 16u * t1) << 16);
+    }
   }
   auto lcs_stop = [&](const int m) -> bool {
     const uint32_t L0 = lnext0, L1 = lnext1;
@@ -306,8 +317,14 @@ __device__ __forceinline__ void packed_item(const FastArgs& a, const int64_t war
     for (int d = G / 2; d > 0; d >>= 1) v = __vimax_s16x2_relu(v, __shfl_xor_sync(0xffffffffu, v, d, G));
     v &= 0xFFF0FFF0u;
     const uint32_t M16 = 16u * (uint32_t)a.match;
+    // per half: nothing left can raise the maximum (trace pass: or tie it),
+    // or nothing, computed or left, reaches the threshold
+    auto settled = [&](uint32_t f, uint32_t b, uint32_t t) {
+      return TRACE ? f < b : (f <= b || (f < t && b < t));
+    };
     auto below = [&](uint32_t f) {
-      return (!has0 || (f & 0xFFFFu) < (v & 0xFFFFu)) && (!has1 || (f >> 16) < (v >> 16));
+      return (!has0 || settled(f & 0xFFFFu, v & 0xFFFFu, thr & 0xFFFFu)) &&
+             (!has1 || settled(f >> 16, v >> 16, thr >> 16));
     };
     uint32_t F = (B + M16 * L0) | ((B + M16 * L1) << 16);
     // chains that start among the cells not computed first (cheap, and
@@ -373,31 +390,9 @@ __device__ __forceinline__ void packed_item(const FastArgs& a, const int64_t war
         sw = s0 + 4;
       }
     }
-    // Early stop: after step s = kSufSteps * m + G - 1 every cell left lies
-    // right of column kSufSteps * m, and the bound pass's suffix maximum
-    // suf[m] bounds them all.  Once it is below the score reached so far
-    // for every pair of the warp, no cell left can be (or tie) the first
-    // maximum, and the traceback never reaches them.  ((G - 1) % 4 == 3,
-    // so such an s ends a block.)
+    // early-stop test after steps s = kSufSteps * m + G - 1 ((G - 1) % 4 ==
+    // 3, so such an s ends a block)
     const int s = s0 + 3;
-    if (a.suf && s >= kSufSteps + G - 1 && ((s - (G - 1)) & (kSufSteps - 1)) == 0) {
-      const int m = (s - (G - 1)) / kSufSteps;
-      uint32_t v = bestv[0];
-      if (TRACE) {
-#pragma unroll
-        for (int k = 1; k < RPL; ++k) v = __vimax_s16x2_relu(v, bestv[k]);
-      }
-#pragma unroll
-      for (int d = G / 2; d > 0; d >>= 1) v = __vimax_s16x2_relu(v, __shfl_xor_sync(0xffffffffu, v, d, G));
-      const uint32_t v0 = v & 0xFFFFu, v1 = v >> 16;
-      const int s0v = v0 > B ? (int)((v0 - B) >> 4) : 0, s1v = v1 > B ? (int)((v1 - B) >> 4) : 0;
-      const bool done0 = !has0 || (int)a.suf[(int64_t)p0 * kSufBlocks + m] < s0v;
-      const bool done1 = !has1 || (int)a.suf[(int64_t)p1 * kSufBlocks + m] < s1v;
-      if (__all_sync(0xffffffffu, done0 && done1)) {
-        s_end = s + 1;
-        break;
-      }
-    }
     if (lcs_on && s >= kSufSteps + G - 1 && ((s - (G - 1)) & (kSufSteps - 1)) == 0 &&
         lcs_stop((s - (G - 1)) / kSufSteps)) {
       s_end = s + 1;

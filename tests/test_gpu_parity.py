@@ -551,7 +551,7 @@ def test_bounded_selection_with_repeats(ctx, oracle):
     got, st = ctx.align(ix, reads, stats=True)
     assert st["retraced_pairs"] > 0
     assert st["bound_pruned"] < st["records"] - st["sw_generic_pairs"]
-    # the LCS bound rules out some pairs and leaves others to the relaxed bound
+    # the LCS bound rules out some pairs and leaves others to the exact pass
     fast = st["records"] - st["sw_generic_pairs"]
     assert 0 < st["lcs_kept"] < fast
     ctx.set_sw_path(2)
