@@ -23,7 +23,11 @@ test point that
   * when the trace pass would stop, the first maximum is already computed and
     every cell its traceback visits too,
   * when the score pass would stop on the threshold T, the pair's score is
-    below T.
+    below T;
+
+and that the LCS pass's scan (the query reversed into the top bits of its
+bit vector, the window from its last column down) yields exactly those suffix
+values.
 """
 import random
 
@@ -195,3 +199,39 @@ def test_threshold_stop_of_the_score_pass():
                 assert best < T  # reported below T, as the true score is
                 break
     assert stops > 0
+
+
+def suffix_lcs_by_reverse_scan(q: bytes, w: bytes, nw: int):
+    """The LCS pass's scan (sw_lcs.cu): Hyyro's bit-vector LCS over 32 * nw
+    bits, the query reversed into the top len(q) bits (the bits below match
+    nothing), the window from its last column down; after each 16-column
+    block m (columns 16 m + 1 .. R, one-based) the zeros among the query's
+    bits are LCS(q, w[16 m:])."""
+    T = 32 * nw
+    full = (1 << T) - 1
+    qmask = ((1 << len(q)) - 1) << (T - len(q))
+    pm = {}
+    for i, c in enumerate(q):  # query position i to bit T - 1 - i
+        pm[c] = pm.get(c, 0) | (1 << (T - 1 - i))
+    v = full
+    out = {}
+    for j in range(len(w) - 1, -1, -1):
+        m_c = pm.get(w[j], 0)
+        u = v & m_c
+        v = ((v + u) | (v & ~m_c)) & full
+        if j % 16 == 0:
+            out[j // 16] = bin(~v & qmask).count("1")
+    return out
+
+
+def test_reverse_scan_gives_the_suffix_values():
+    rng = random.Random(31)
+    for q, w in cases(41, 24, 30, 100) + cases(43, 8, 100, 300):
+        nw = (len(q) + 31) // 32
+        got = suffix_lcs_by_reverse_scan(q, w, nw)
+        assert sorted(got) == list(range((len(w) - 1) // 16 + 1))
+        for m, z in got.items():
+            assert z == lcs(q, w[16 * m:])
+    # a query shorter than its words leaves inert bits below it
+    q, w = planted(rng, 40, 120, 2, 1)
+    assert suffix_lcs_by_reverse_scan(q, w, 4)[0] == lcs(q, w)
